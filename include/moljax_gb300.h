@@ -1,0 +1,176 @@
+/*
+ * moljax_gb300 -- C ABI of the GB300 (sm_103a) method-of-lines step path.
+ *
+ * Every entry point takes plain device pointers, sizes, host-side parameter
+ * structs and a CUDA stream handle (passed as void*; NULL = legacy default
+ * stream).  The caller owns all device memory: plans (twiddle and symbol
+ * tables) and workspaces are caller-provided buffers whose sizes come from
+ * the *_bytes() queries, so no step call allocates device memory.
+ * Numerical failure is reported through status codes (never a device trap).
+ *
+ * Layout: fields are interior-only (no ghost cells), row-major [ny][nx] with
+ * y on axis 0 (the reference's convention), several fields stored back to
+ * back ([nfields][ny][nx]).  dtype MJX_F32 or MJX_F64 for every buffer.
+ *
+ * Each function names the reference (gogipav14/moljax) interface it replaces.
+ */
+#ifndef MOLJAX_GB300_H
+#define MOLJAX_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum mjx_status {
+  MJX_OK = 0,
+  MJX_BAD_SHAPE = 1,     /* unsupported or inconsistent sizes */
+  MJX_BAD_DTYPE = 2,
+  MJX_NOT_FINITE = 3,    /* moljax StatusCode.NON_FINITE_VALUES */
+  MJX_MAX_ITERS = 4,     /* moljax StatusCode.MAX_STEPS_REACHED */
+  MJX_DT_TOO_SMALL = 5,  /* moljax StatusCode.DT_TOO_SMALL */
+  MJX_NK_FAILED = 6,     /* moljax StatusCode.NK_FAILED */
+  MJX_OOM = 7,
+  MJX_CUDA_ERROR = 8,
+  MJX_BAD_ARG = 9,
+  MJX_WORKSPACE = 10     /* workspace smaller than the *_bytes() query */
+} mjx_status;
+
+typedef enum mjx_dtype { MJX_F32 = 0, MJX_F64 = 1 } mjx_dtype;
+
+/* Periodic Laplacian eigenvalues: FD 5-point symbol (moljax/core/fft_solvers.py:124-154)
+ * or pseudo-spectral -(kx^2+ky^2) (benchmarks/benchmark_vs_scipy.py:77-80). */
+typedef enum mjx_symbol { MJX_SYMBOL_FD = 0, MJX_SYMBOL_SPECTRAL = 1 } mjx_symbol;
+
+/* Spectral multipliers applied between forward and inverse transform. */
+typedef enum mjx_mult {
+  MJX_MULT_SCALE = 0,      /* identity (round trip) */
+  MJX_MULT_HELMHOLTZ = 1,  /* 1/(1 - h D lam), |denominator| clamped at 1e-14 */
+  MJX_MULT_CN = 2,         /* (1 + h D lam/2)/(1 - h D lam/2) */
+  MJX_MULT_EXP = 3         /* exp(h D lam) */
+} mjx_mult;
+
+typedef enum mjx_reaction {
+  MJX_REACT_NONE = 0,
+  MJX_REACT_GRAY_SCOTT = 1, /* u: -uv^2 + F(1-u); v: uv^2 - (F+k)v  (operators.py:644-677) */
+  MJX_REACT_FISHER = 2      /* r u (1-u) on every field          (operators.py:680-705) */
+} mjx_reaction;
+
+/* Ghost-cell BC kinds (moljax/core/bc.py:26-30 BCType). */
+typedef enum mjx_bc_kind { MJX_BC_PERIODIC = 0, MJX_BC_DIRICHLET = 1, MJX_BC_NEUMANN = 2 } mjx_bc_kind;
+
+typedef struct mjx_grid2d {
+  int ny, nx;          /* interior points, powers of two in [2, 4096] */
+  double dy, dx;
+} mjx_grid2d;
+
+/* moljax/core/dt_policy.py:49-78 (PIDParams) */
+typedef struct mjx_pid_params {
+  double safety, kI, kP, dt_min, dt_max, max_factor, min_factor, atol, rtol;
+} mjx_pid_params;
+
+typedef struct mjx_imex_problem {
+  int reaction;        /* mjx_reaction */
+  int nfields;         /* 1..4 (Gray-Scott: 2, fields u then v) */
+  double D[4];         /* per-field diffusivity; D <= 1e-14 passes the field through */
+  double F, k, r;      /* reaction parameters */
+  double dt_cfl;       /* imex_cfl_dt (moljax/core/dt_policy.py:430-502), host-computed */
+  int use_strang;      /* 1: IMEX-Strang (order 2).  0 is rejected (MJX_BAD_ARG). */
+  int max_attempts;    /* hard cap on step attempts (accepted + rejected); <= 0 -> default */
+} mjx_imex_problem;
+
+/* moljax/core/stepping.py:710-720 (AdaptiveResult scalars) */
+typedef struct mjx_adaptive_result {
+  double t_final, dt_next, prev_err, last_err;
+  int n_accepted, n_rejected, n_attempts, n_saved, status, finite;
+} mjx_adaptive_result;
+
+const char* mjx_version(void);
+const char* mjx_status_string(int status);
+
+/* ---- periodic 2D spectral plans ------------------------------------------------ */
+/* Device bytes of a plan: twiddle tables for nx and ny plus the 1D symbols.
+ * Replaces FFTCache2D / create_fft_cache_2d (moljax/core/fft_solvers.py:38-42, 181-198). */
+size_t mjx_spec2d_plan_bytes(int ny, int nx, int dtype);
+mjx_status mjx_spec2d_plan_init(void* plan, const mjx_grid2d* grid, int symbol, int dtype,
+                                void* stream);
+/* Spectrum workspace for nfields fields: nfields * ny * (nx/2+1 padded) complex. */
+size_t mjx_spec2d_ws_bytes(int ny, int nx, int nfields, int dtype);
+
+/* out_f = IFFT2( m(h, D_f, lam) * FFT2(in_f) ) for each of nfields fields.
+ * Generic spectral pass: Helmholtz (solve_helmholtz_2d, fft_solvers.py:261-294,
+ * apply_diffusion_inverse_fft 406-445), CN factor, exponential.  in may equal out.
+ * Fields with D <= 1e-14 are copied unchanged (fft_solvers.py:435-443). */
+mjx_status mjx_spectral_apply2d(const void* plan, const mjx_grid2d* grid, int dtype, int nfields,
+                                const double* D, double h, int mult, const void* in, void* out,
+                                void* ws, size_t ws_bytes, void* stream);
+
+/* n_steps Crank-Nicolson steps u <- real(IFFT2(G * FFT2(u))) executed one by one;
+ * G = (1 + dt D lam/2)/(1 - dt D lam/2).  Replaces the benchmark FFT-CN step
+ * (benchmarks/benchmark_vs_scipy.py:74-91) behind fft_solvers.fft_cn_step. */
+mjx_status mjx_fft_cn2d(const void* plan, const mjx_grid2d* grid, int dtype, double D, double dt,
+                        int n_steps, const void* u_in, void* u_out, void* ws, size_t ws_bytes,
+                        void* stream);
+
+/* ---- ghost cells and finite-difference stencils on padded fields ---------------- */
+/* Padded layout: [nfields][ny+2g][nx+2g].  kinds[f] is an mjx_bc_kind; values holds
+ * 4 constants per field (left, right, bottom, top): Dirichlet boundary values or
+ * Neumann fluxes (NULL = homogeneous).  Ghost fill follows moljax/core/bc.py:202-307
+ * (x ghosts first, then y ghosts, so corners are BC_y(BC_x(u))). */
+
+/* interior [nf][ny][nx] -> padded with ghosts filled (create_state_from_interior +
+ * apply_bc; state.py:268-295, bc.py:358-404). */
+mjx_status mjx_bc_pad2d(const void* interior, void* padded, int nfields, int ny, int nx, int n_ghost,
+                        const int* kinds, const double* values, double dy, double dx, int dtype,
+                        void* stream);
+/* padded -> padded with ghosts refilled (apply_bc, bc.py:358-404); in != out. */
+mjx_status mjx_bc_fill2d(const void* padded_in, void* padded_out, int nfields, int ny, int nx,
+                         int n_ghost, const int* kinds, const double* values, double dy, double dx,
+                         int dtype, void* stream);
+/* padded -> interior copy (get_interior_state, state.py:298-309). */
+mjx_status mjx_unpad2d(const void* padded, void* interior, int nfields, int ny, int nx, int n_ghost,
+                       int dtype, void* stream);
+/* out = coef_f * Laplacian(in_f) on the interior, ghosts of out zero
+ * (laplacian_2d, operators.py:311-322).  fill_bc != 0 evaluates the BC ghosts
+ * on the fly instead of reading the input's ghost cells. */
+mjx_status mjx_laplacian2d(const void* padded_in, void* padded_out, int nfields, int ny, int nx,
+                           int n_ghost, const double* coef, int fill_bc, const int* kinds,
+                           const double* values, double dy, double dx, int dtype, void* stream);
+/* Model right-hand side with BCs applied on the fly: D_f Lap(u_f) + reaction
+ * (MOLModel.rhs, model.py:100-118; Gray-Scott operators.py:644-667; for
+ * MJX_REACT_FISHER the parameter F carries r, operators.py:680-705). */
+mjx_status mjx_rhs2d(const void* padded_in, void* padded_out, int nfields, int ny, int nx,
+                     int n_ghost, int reaction, const double* D, double F, double k,
+                     const int* kinds, const double* values, double dy, double dx, int dtype,
+                     void* stream);
+
+/* ---- IMEX-Strang (diffusion implicit by FFT, reaction explicit Heun) ------------- */
+size_t mjx_imex2d_ws_bytes(int ny, int nx, int nfields, int dtype);
+
+/* One fixed IMEX-Strang step of length dt (moljax/core/stepping.py:370-435).
+ * y_in may equal y_out. */
+mjx_status mjx_imex_strang_step2d(const void* plan, const mjx_grid2d* grid, int dtype,
+                                  const mjx_imex_problem* prob, double dt, const void* y_in,
+                                  void* y_out, void* ws, size_t ws_bytes, void* stream);
+
+/* Adaptive IMEX-Strang with step doubling and the PI controller, run as one
+ * device-side loop (a CUDA graph with a conditional while node); no host
+ * synchronisation per step.  Replaces adaptive_integrate_imex
+ * (moljax/core/stepping.py:1146-1371) with estimate_error_imex_doubling (566-608),
+ * scaled_error_norm (state.py:312-343) and propose_dt_imex (dt_policy.py:544-610).
+ * hist_t/hist_dt (double[max_saves]) and hist_y ([max_saves][nfields][ny][nx])
+ * may be NULL.  max_saves = max_steps // save_every + 1 as in the reference.
+ * Blocks until the run finishes and fills *result. */
+mjx_status mjx_imex_adaptive2d(const void* plan, const mjx_grid2d* grid, int dtype,
+                               const mjx_imex_problem* prob, const mjx_pid_params* pid,
+                               double t0, double t_end, double dt0, int max_steps, int save_every,
+                               const void* y0, void* y_final, double* hist_t, double* hist_dt,
+                               void* hist_y, void* ws, size_t ws_bytes,
+                               mjx_adaptive_result* result, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MOLJAX_GB300_H */

@@ -1,0 +1,137 @@
+"""ctypes binding of ``libmoljax_gb300.so`` (C ABI in ``include/moljax_gb300.h``).
+
+The library is loaded from ``moljax_gb300/_lib`` (built in-tree by
+``moljax_gb300.build_native``).  There is no fallback: when the library is
+missing or CUDA is unavailable every entry point raises.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+
+import torch
+
+from moljax_gb300.build_native import LIB
+
+_lock = threading.Lock()
+_lib = None
+
+MJX_OK = 0
+STATUS_NAMES = {
+    0: "MJX_OK", 1: "MJX_BAD_SHAPE", 2: "MJX_BAD_DTYPE", 3: "MJX_NOT_FINITE",
+    4: "MJX_MAX_ITERS", 5: "MJX_DT_TOO_SMALL", 6: "MJX_NK_FAILED", 7: "MJX_OOM",
+    8: "MJX_CUDA_ERROR", 9: "MJX_BAD_ARG", 10: "MJX_WORKSPACE",
+}
+F32, F64 = 0, 1
+SYMBOL_FD, SYMBOL_SPECTRAL = 0, 1
+MULT_SCALE, MULT_HELMHOLTZ, MULT_CN, MULT_EXP = 0, 1, 2, 3
+REACT_NONE, REACT_GRAY_SCOTT, REACT_FISHER = 0, 1, 2
+
+
+class Grid2DC(C.Structure):
+    _fields_ = [("ny", C.c_int), ("nx", C.c_int), ("dy", C.c_double), ("dx", C.c_double)]
+
+
+class PIDParamsC(C.Structure):
+    _fields_ = [(n, C.c_double) for n in
+                ("safety", "kI", "kP", "dt_min", "dt_max", "max_factor", "min_factor", "atol", "rtol")]
+
+
+class ImexProblemC(C.Structure):
+    _fields_ = [("reaction", C.c_int), ("nfields", C.c_int), ("D", C.c_double * 4),
+                ("F", C.c_double), ("k", C.c_double), ("r", C.c_double), ("dt_cfl", C.c_double),
+                ("use_strang", C.c_int), ("max_attempts", C.c_int)]
+
+
+class AdaptiveResultC(C.Structure):
+    _fields_ = [("t_final", C.c_double), ("dt_next", C.c_double), ("prev_err", C.c_double),
+                ("last_err", C.c_double), ("n_accepted", C.c_int), ("n_rejected", C.c_int),
+                ("n_attempts", C.c_int), ("n_saved", C.c_int), ("status", C.c_int),
+                ("finite", C.c_int)]
+
+
+_vp, _sz, _i, _d = C.c_void_p, C.c_size_t, C.c_int, C.c_double
+# name -> (restype, argtypes); the list is the exported C ABI
+SIGNATURES = {
+    "mjx_version": (C.c_char_p, []),
+    "mjx_status_string": (C.c_char_p, [_i]),
+    "mjx_spec2d_plan_bytes": (_sz, [_i, _i, _i]),
+    "mjx_spec2d_plan_init": (_i, [_vp, C.POINTER(Grid2DC), _i, _i, _vp]),
+    "mjx_spec2d_ws_bytes": (_sz, [_i, _i, _i, _i]),
+    "mjx_spectral_apply2d": (_i, [_vp, C.POINTER(Grid2DC), _i, _i, C.POINTER(C.c_double), _d, _i,
+                                  _vp, _vp, _vp, _sz, _vp]),
+    "mjx_fft_cn2d": (_i, [_vp, C.POINTER(Grid2DC), _i, _d, _d, _i, _vp, _vp, _vp, _sz, _vp]),
+    "mjx_bc_pad2d": (_i, [_vp, _vp, _i, _i, _i, _i, _vp, _vp, _d, _d, _i, _vp]),
+    "mjx_bc_fill2d": (_i, [_vp, _vp, _i, _i, _i, _i, _vp, _vp, _d, _d, _i, _vp]),
+    "mjx_unpad2d": (_i, [_vp, _vp, _i, _i, _i, _i, _i, _vp]),
+    "mjx_laplacian2d": (_i, [_vp, _vp, _i, _i, _i, _i, _vp, _i, _vp, _vp, _d, _d, _i, _vp]),
+    "mjx_rhs2d": (_i, [_vp, _vp, _i, _i, _i, _i, _i, _vp, _d, _d, _vp, _vp, _d, _d, _i, _vp]),
+    "mjx_imex2d_ws_bytes": (_sz, [_i, _i, _i, _i]),
+    "mjx_imex_strang_step2d": (_i, [_vp, C.POINTER(Grid2DC), _i, C.POINTER(ImexProblemC), _d,
+                                    _vp, _vp, _vp, _sz, _vp]),
+    "mjx_imex_adaptive2d": (_i, [_vp, C.POINTER(Grid2DC), _i, C.POINTER(ImexProblemC),
+                                 C.POINTER(PIDParamsC), _d, _d, _d, _i, _i, _vp, _vp,
+                                 C.POINTER(C.c_double), C.POINTER(C.c_double), _vp, _vp, _sz,
+                                 C.POINTER(AdaptiveResultC), _vp]),
+}
+
+
+class NativeError(RuntimeError):
+    def __init__(self, fn, status):
+        super().__init__(f"{fn} failed: {STATUS_NAMES.get(status, status)}")
+        self.status = status
+
+
+def load(path: str | None = None):
+    """Loads (once) and returns the native library; raises if it is missing."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        p = path or LIB
+        if not os.path.exists(p):
+            raise RuntimeError(
+                f"native library {p} is missing: run moljax_gb300.build_native.build() "
+                "(or __graft_entry__.build()) first")
+        lib = C.CDLL(p)
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+        return lib
+
+
+def lib():
+    return _lib if _lib is not None else load()
+
+
+def check(name, status):
+    if status != MJX_OK:
+        raise NativeError(name, status)
+
+
+def require_cuda(*tensors):
+    if not torch.cuda.is_available():
+        raise RuntimeError("moljax_gb300 needs a CUDA GPU: no CPU fallback exists")
+    for t in tensors:
+        if t is not None and (not t.is_cuda or not t.is_contiguous()):
+            raise ValueError("device buffers must be contiguous CUDA tensors")
+
+
+def dtype_code(dt: torch.dtype) -> int:
+    if dt == torch.float32:
+        return F32
+    if dt == torch.float64:
+        return F64
+    raise TypeError(f"unsupported dtype {dt}; use float32 or float64")
+
+
+def stream_ptr(device=None):
+    return C.c_void_p(torch.cuda.current_stream(device).cuda_stream)
+
+
+def ptr(t):
+    return C.c_void_p(t.data_ptr()) if t is not None else C.c_void_p(0)

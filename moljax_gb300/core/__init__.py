@@ -1,0 +1,16 @@
+"""moljax_gb300.core -- GPU-native counterpart of ``moljax.core``."""
+
+from moljax_gb300.core.grid import Grid1D, Grid2D
+from moljax_gb300.core.bc import BCType, FieldBCSpec, apply_bc
+from moljax_gb300.core import fft_solvers, operators, stepping, dt_policy, model
+from moljax_gb300.core.operators import LinearOp, NonlinearOp, laplacian_2d
+from moljax_gb300.core.model import (MOLModel, create_gray_scott_model,
+                                     create_gray_scott_periodic_fft, gray_scott_factory)
+from moljax_gb300.core.stepping import (IntegratorType, AdaptiveResult, adaptive_integrate,
+                                        adaptive_integrate_imex, imex_strang_step,
+                                        integrate_imex_fixed_dt)
+from moljax_gb300.core.dt_policy import CFLParams, PIDParams
+from moljax_gb300.core.fft_solvers import (create_fft_cache, solve_helmholtz_2d,
+                                           apply_diffusion_inverse_fft, fft_cn_step,
+                                           laplacian_symbol_2d)
+from moljax_gb300.core.utils import StatusCode

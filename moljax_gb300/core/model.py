@@ -1,0 +1,155 @@
+"""PDE model assembly (moljax/core/model.py drop-in).
+
+``MOLModel`` keeps the reference fields (grid, bc_spec, params, linear_ops,
+nonlinear_ops, metadata; model.py:34-118).  ``rhs`` runs the fused native
+kernel (BCs + D Lap + reaction) when the model was built by a factory below.
+"""
+
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+from typing import Any, Dict, List, Optional, Tuple
+
+import torch
+
+from moljax_gb300 import _native as N
+from moljax_gb300.core.bc import BCType, FieldBCSpec
+from moljax_gb300.core.grid import Grid2D
+from moljax_gb300.core.operators import LinearOp, NonlinearOp, gray_scott_reaction_op, \
+    fisher_kpp_reaction_op
+
+
+@dataclass(frozen=True)
+class MOLModel:
+    grid: Any
+    bc_spec: Dict[str, FieldBCSpec]
+    params: Dict[str, Any]
+    linear_ops: Tuple[LinearOp, ...] = field(default_factory=tuple)
+    nonlinear_ops: Tuple[NonlinearOp, ...] = field(default_factory=tuple)
+    metadata: Dict[str, Any] = field(default_factory=dict)
+
+    @property
+    def dtype(self) -> torch.dtype:
+        return self.params.get("dtype", torch.float64)
+
+    @property
+    def field_names(self) -> List[str]:
+        return list(self.bc_spec.keys())
+
+    # native description of the model: (reaction id, per-field diffusivities)
+    @property
+    def reaction_kind(self) -> int:
+        kinds = [op.kind for op in self.nonlinear_ops]
+        if not kinds:
+            return N.REACT_NONE
+        if len(kinds) != 1 or kinds[0] is None:
+            raise NotImplementedError(
+                "fused GPU drivers support one built-in reaction (Gray-Scott or Fisher-KPP); "
+                f"got {[op.name for op in self.nonlinear_ops]}")
+        return kinds[0]
+
+    def diffusivities(self) -> Dict[str, float]:
+        if "diffusivities" in self.metadata:
+            return dict(self.metadata["diffusivities"])
+        out = {}
+        for n in self.field_names:
+            out[n] = float(self.params.get(f"D{n}", self.params.get("D", 0.0)))
+        return out
+
+    def apply_bcs(self, state, t: float = 0.0):
+        from moljax_gb300.core import stencil
+        return stencil.apply_bc(state, self.grid, self.bc_spec, t, self.params)
+
+    def rhs(self, state, t: float = 0.0):
+        """apply_bcs -> D Lap + reaction, fused in one kernel (model.py:100-118)."""
+        from moljax_gb300.core import stencil
+        D = self.diffusivities()
+        names = self.field_names
+        rx = self.reaction_kind
+        F = self.params.get("r", 1.0) if rx == N.REACT_FISHER else self.params.get("F", 0.0)
+        return stencil.model_rhs(state, self.grid, self.bc_spec, names, rx,
+                                 [D[n] for n in names], F, self.params.get("k", 0.0), t,
+                                 self.params)
+
+    def create_initial_state(self, init_fns=None, fill_values=None, device="cuda"):
+        init_fns = init_fns or {}
+        fill_values = fill_values or {}
+        g = self.grid
+        shape = (g.ny_total, g.nx_total)
+        out = {}
+        for n in self.field_names:
+            if n in init_fns:
+                X, Y = g.meshgrid(include_ghost=True)
+                out[n] = torch.as_tensor(init_fns[n](X, Y)).to(device=device, dtype=self.dtype)
+            else:
+                out[n] = torch.full(shape, float(fill_values.get(n, 0.0)), dtype=self.dtype,
+                                    device=device)
+        return out
+
+
+def create_gray_scott_model(grid: Grid2D, Du: float = 0.16, Dv: float = 0.08, F: float = 0.04,
+                            k: float = 0.06, bc_type: BCType = BCType.PERIODIC,
+                            dtype: torch.dtype = torch.float64) -> MOLModel:
+    """moljax/core/model.py:213-292."""
+    from moljax_gb300.core import stencil
+    bc_spec = {"u": FieldBCSpec(kind=bc_type), "v": FieldBCSpec(kind=bc_type)}
+    params = {"Du": Du, "Dv": Dv, "F": F, "k": k, "dtype": dtype}
+
+    def diffusion_apply(state, grid, t, params):
+        return {"u": stencil.laplacian_2d(state["u"], grid, params["Du"]),
+                "v": stencil.laplacian_2d(state["v"], grid, params["Dv"])}
+
+    def diffusion_dt_bound(grid, params):
+        return 0.25 * grid.min_dx2 / (max(params["Du"], params["Dv"]) + 1e-14)
+
+    diffusion = LinearOp("gray_scott_diffusion", diffusion_apply, diffusion_dt_bound, "diffusion")
+    return MOLModel(grid, bc_spec, params, (diffusion,), (gray_scott_reaction_op(),),
+                    {"field_names": ["u", "v"], "pde_type": "reaction_diffusion", "stiff": True,
+                     "diffusivities": {"u": Du, "v": Dv}})
+
+
+def create_gray_scott_periodic_fft(grid: Grid2D, Du: float = 0.16, Dv: float = 0.08,
+                                   F: float = 0.04, k: float = 0.06,
+                                   dtype: torch.dtype = torch.float64, device=None):
+    """moljax/core/model.py:529-584 -> (model, fft_cache, diffusivities)."""
+    from moljax_gb300.core.fft_solvers import create_fft_cache
+    model = create_gray_scott_model(grid, Du, Dv, F, k, BCType.PERIODIC, dtype)
+    cache = create_fft_cache(grid, dtype, device)
+    diff = {"u": Du, "v": Dv}
+    md = dict(model.metadata)
+    md.update(fft_cache=cache, diffusivities=diff, supports_fft=True)
+    return MOLModel(model.grid, model.bc_spec, model.params, model.linear_ops,
+                    model.nonlinear_ops, md), cache, diff
+
+
+def gray_scott_factory(nx: int = 256, ny: Optional[int] = None, Du: float = 2e-5,
+                       Dv: float = 1e-5, F: float = 0.035, k: float = 0.065, L: float = 2.5,
+                       dtype: torch.dtype = torch.float32, device=None) -> MOLModel:
+    """README.md:65-73 factory: periodic Gray-Scott on [0, L]^2 with its FFT cache."""
+    grid = Grid2D(nx, ny or nx, 0.0, L, 0.0, L)
+    model, _, _ = create_gray_scott_periodic_fft(grid, Du, Dv, F, k, dtype, device)
+    return model
+
+
+def create_fisher_kpp_model(grid: Grid2D, D: float = 0.01, r: float = 1.0,
+                            bc_type: BCType = BCType.PERIODIC,
+                            dtype: torch.dtype = torch.float64) -> MOLModel:
+    """moljax/core/model.py:470-524 (D Lap u + r u (1-u))."""
+    from moljax_gb300.core import stencil
+    params = {"D": D, "r": r, "dtype": dtype}
+
+    def diffusion_apply(state, grid, t, params):
+        return {"u": stencil.laplacian_2d(state["u"], grid, params["D"])}
+
+    diffusion = LinearOp("fisher_diffusion", diffusion_apply, None, "diffusion")
+    return MOLModel(grid, {"u": FieldBCSpec(kind=bc_type)}, params, (diffusion,),
+                    (fisher_kpp_reaction_op("u", "r"),),
+                    {"field_names": ["u"], "diffusivities": {"u": D}})
+
+
+def get_fft_cache(model: MOLModel):
+    return model.metadata.get("fft_cache")
+
+
+def get_diffusivities(model: MOLModel) -> Dict[str, float]:
+    return model.diffusivities()

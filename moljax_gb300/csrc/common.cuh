@@ -1,0 +1,57 @@
+// Shared helpers for the moljax_gb300 CUDA kernels (sm_103a).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/moljax_gb300.h"
+
+namespace mjx {
+
+template <typename T> struct cplx_of;
+template <> struct cplx_of<float> { typedef float2 type; };
+template <> struct cplx_of<double> { typedef double2 type; };
+template <typename T> using cx = typename cplx_of<T>::type;
+
+template <typename C> __device__ __forceinline__ C mk(decltype(C::x) re, decltype(C::x) im) {
+  C r; r.x = re; r.y = im; return r;
+}
+template <typename C> __device__ __forceinline__ C cadd(C a, C b) { return mk<C>(a.x + b.x, a.y + b.y); }
+template <typename C> __device__ __forceinline__ C csub(C a, C b) { return mk<C>(a.x - b.x, a.y - b.y); }
+template <typename C> __device__ __forceinline__ C cmul(C a, C b) {
+  return mk<C>(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+// a * conj(b)
+template <typename C> __device__ __forceinline__ C cmulc(C a, C b) {
+  return mk<C>(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y);
+}
+template <typename C> __device__ __forceinline__ C cconj(C a) { return mk<C>(a.x, -a.y); }
+template <typename C, typename S> __device__ __forceinline__ C cscale(C a, S s) {
+  return mk<C>(a.x * s, a.y * s);
+}
+
+// Records a CUDA launch/runtime error as an mjx status.
+static inline mjx_status cuda_status(cudaError_t e) {
+  return e == cudaSuccess ? MJX_OK : MJX_CUDA_ERROR;
+}
+
+static inline int ilog2_exact(long long n) {
+  if (n <= 0 || (n & (n - 1))) return -1;
+  int l = 0;
+  while ((1LL << l) < n) ++l;
+  return l;
+}
+
+}  // namespace mjx
+
+#define MJX_TRY(expr)                                   \
+  do {                                                  \
+    mjx_status _s = (expr);                             \
+    if (_s != MJX_OK) return _s;                        \
+  } while (0)
+
+#define MJX_CUDA_TRY(expr)                              \
+  do {                                                  \
+    cudaError_t _e = (expr);                            \
+    if (_e != cudaSuccess) return MJX_CUDA_ERROR;       \
+  } while (0)

@@ -1,0 +1,510 @@
+// Periodic 2D spectral passes: fused row r2c/c2r (+ pointwise work) and
+// column forward-multiply-inverse kernels, plans, and the C ABI for the
+// Helmholtz / CN / exponential multipliers and the FFT-CN stepper.
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <vector>
+
+#include "spectral.cuh"
+
+namespace mjx {
+
+static inline size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
+
+int spec_ldc(int nx) { return ((nx / 2 + 1) + 3) & ~3; }
+
+size_t plan_bytes(int ny, int nx, int elem) {
+  const size_t c = 2 * (size_t)elem;
+  return align256(nx * c) + align256(ny * c) + align256(spec_ldc(nx) * (size_t)elem) +
+         align256(ny * (size_t)elem);
+}
+
+PlanView plan_view(const void* plan, int ny, int nx, int elem) {
+  const size_t c = 2 * (size_t)elem;
+  const char* p = (const char*)plan;
+  PlanView v;
+  v.twx = p; p += align256(nx * c);
+  v.twy = p; p += align256(ny * c);
+  v.lamx = p; p += align256(spec_ldc(nx) * (size_t)elem);
+  v.lamy = p;
+  return v;
+}
+
+int row_nseq(int n, int nrows) {
+  const int tps = n >= 16 ? n / 16 : 1;
+  int ns = 256 / tps;
+  if (ns < 1) ns = 1;
+  if (ns > nrows) ns = nrows;
+  return ns;
+}
+
+int row_ctas(int n, int nrows, int npairs) { return npairs * nrows / row_nseq(n, nrows); }
+
+// ------------------------------------------------------------------ reactions
+template <typename T, int RX>
+__device__ __forceinline__ void react_heun(T& a, T& b, T h, T F, T k, T r) {
+  if (RX == RX_GRAY_SCOTT) {
+    // moljax/core/stepping.py:402-415 with operators.py:655-667
+    const T uvv = a * b * b;
+    const T fu = -uvv + F * ((T)1 - a);
+    const T fv = uvv - (F + k) * b;
+    const T ua = a + h * fu, va = b + h * fv;
+    const T uvv2 = ua * va * va;
+    const T gu = -uvv2 + F * ((T)1 - ua);
+    const T gv = uvv2 - (F + k) * va;
+    const T hh = (T)0.5 * h;
+    a = a + hh * (fu + gu);
+    b = b + hh * (fv + gv);
+  } else if (RX == RX_FISHER) {
+    const T fa = r * a * ((T)1 - a), fb = r * b * ((T)1 - b);
+    const T ta = a + h * fa, tb = b + h * fb;
+    const T hh = (T)0.5 * h;
+    a = a + hh * (fa + r * ta * ((T)1 - ta));
+    b = b + hh * (fb + r * tb * ((T)1 - tb));
+  }
+}
+
+template <typename T> __device__ __forceinline__ bool finite_(T v) { return isfinite(v); }
+
+// ------------------------------------------------------------------ row pass
+template <typename T, int RX>
+__global__ void __launch_bounds__(256, 2) row_kernel(const __grid_constant__ RowArgs<T> a) {
+  typedef cx<T> C;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* buf = reinterpret_cast<C*>(smem_raw);
+  const DevState* st = a.st;
+  if (st != nullptr && st->done) return;
+
+  const int n = a.n, half = n >> 1;
+  const int tps = n >= 16 ? n / 16 : 1;
+  const int tid = threadIdx.x;
+  const int s_loc = tid / tps, lt = tid % tps;
+  const int seq0 = blockIdx.x * a.nseq;
+  const int q = seq0 / a.nrows;  // uniform within the CTA (nrows % nseq == 0)
+  const RowPair pr = a.pr[q];
+  const int flags = pr.flags;
+  const long long y = (seq0 % a.nrows) + s_loc;
+  const int cur = st != nullptr ? st->cur : 0;
+  const T* rin = a.rin_sel < 0 ? a.rin[0] : a.rin[a.rin_sel == 0 ? cur : 1 - cur];
+  T* rout = a.rout_sel < 0 ? a.rout[0] : a.rout[a.rout_sel == 0 ? cur : 1 - cur];
+  C* z = buf + s_loc * n;
+
+  // 1. load: spectrum rows (c2r) or real rows
+  if (flags & ROW_LOAD_SPEC) {
+    const C* A = a.spec + pr.sa + y * a.ldc;
+    const C* B = a.spec + pr.sb + y * a.ldc;
+    for (int kk = lt; kk <= half; kk += tps) {
+      const C Ak = A[kk], Bk = B[kk];
+      z[kk] = mk<C>(Ak.x - Bk.y, Ak.y + Bk.x);                    // A_k + i B_k
+      if (kk > 0 && kk < half) z[n - kk] = mk<C>(Ak.x + Bk.y, Bk.x - Ak.y);  // conj(A_k) + i conj(B_k)
+    }
+    __syncthreads();
+    fft_smem<T, true, false>(buf, n, a.log2n, a.nseq, n, 1, a.tw, tid);
+  } else {
+    const T* ra = rin + pr.ra + y * a.rstride;
+    const T* rb = rin + pr.rb + y * a.rstride;
+    for (int x = lt; x < n; x += tps) z[x] = mk<C>(ra[x], rb[x]);
+    __syncthreads();
+  }
+
+  // 2. pointwise work on the real rows (each thread owns x = lt + m*tps)
+  const T sc = (flags & ROW_LOAD_SPEC) ? a.inv_scale : (T)1;
+  T h = (T)0;
+  if (flags & ROW_REACT) h = (T)((st != nullptr ? st->dtc : a.hfixed) * pr.hfac);
+  T esum = (T)0;
+  int bad = 0;
+  T* oa = rout + pr.ra + y * a.rstride;
+  T* ob = rout + pr.rb + y * a.rstride;
+  const T* ea = a.eref + pr.ra + y * a.rstride;
+  const T* eb = a.eref + pr.rb + y * a.rstride;
+  for (int x = lt; x < n; x += tps) {
+    const C v = z[x];
+    T va = v.x * sc, vb = v.y * sc;
+    if (flags & ROW_REACT) react_heun<T, RX>(va, vb, h, (T)a.F, (T)a.k, (T)a.r);
+    if (flags & ROW_STORE_REAL) { oa[x] = va; ob[x] = vb; }
+    if (flags & ROW_ERRNORM) {
+      // moljax/core/state.py:335-339: (err / (atol + rtol |y_new|))^2
+      const T da = (va - ea[x]) / ((T)a.atol + (T)a.rtol * fabs(va));
+      const T db = (vb - eb[x]) / ((T)a.atol + (T)a.rtol * fabs(vb));
+      esum += da * da + db * db;
+      bad |= !(finite_(va) && finite_(vb));
+    }
+    z[x] = mk<C>(va, vb);
+  }
+
+  // 3. r2c and split into the two half spectra
+  if (flags & ROW_STORE_SPEC) {
+    __syncthreads();
+    fft_smem<T, false, false>(buf, n, a.log2n, a.nseq, n, 1, a.tw, tid);
+    C* A = a.spec + pr.sa + y * a.ldc;
+    C* B = a.spec + pr.sb + y * a.ldc;
+    for (int kk = lt; kk <= half; kk += tps) {
+      const C Zk = z[kk], Zm = z[(n - kk) & (n - 1)];
+      A[kk] = mk<C>((T)0.5 * (Zk.x + Zm.x), (T)0.5 * (Zk.y - Zm.y));
+      B[kk] = mk<C>((T)0.5 * (Zk.y + Zm.y), (T)0.5 * (Zm.x - Zk.x));
+    }
+  }
+
+  // 4. block reduction of the error partials (FP64 across threads)
+  if (flags & ROW_ERRNORM) {
+    __shared__ double red[32];
+    __shared__ int redbad[32];
+    double v = (double)esum;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      v += __shfl_xor_sync(0xffffffffu, v, o);
+      bad |= __shfl_xor_sync(0xffffffffu, bad, o);
+    }
+    const int w = tid >> 5, nw = (blockDim.x + 31) >> 5;
+    if ((tid & 31) == 0) { red[w] = v; redbad[w] = bad; }
+    __syncthreads();
+    if (tid == 0) {
+      double s = 0.0, c = 0.0;  // Kahan
+      int b2 = 0;
+      for (int i = 0; i < nw; ++i) {
+        const double yv = red[i] - c;
+        const double tv = s + yv;
+        c = (tv - s) - yv;
+        s = tv;
+        b2 |= redbad[i];
+      }
+      a.partial[blockIdx.x] = s;
+      a.nonfinite[blockIdx.x] = b2;
+    }
+  }
+}
+
+// ------------------------------------------------------------------ column pass
+template <typename T>
+__device__ __forceinline__ T multiplier(int mul, T hD, T lam, int pw) {
+  T m;
+  if (mul == MUL_HELMHOLTZ) {
+    T den = (T)1 - hD * lam;  // moljax/core/fft_solvers.py:281-285
+    if (fabs(den) < (T)1e-14) den = (T)1e-14;
+    m = (T)1 / den;
+  } else if (mul == MUL_CN) {
+    const T x = (T)0.5 * hD * lam;
+    m = ((T)1 + x) / ((T)1 - x);
+  } else if (mul == MUL_EXP) {
+    m = exp(hD * lam);
+  } else {
+    m = (T)1;
+  }
+  return pw == 2 ? m * m : m;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(512) col_kernel(const __grid_constant__ ColArgs<T> a) {
+  typedef cx<T> C;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* buf = reinterpret_cast<C*>(smem_raw);
+  if (a.st != nullptr && a.st->done) return;
+  const ColJob jb = a.job[blockIdx.y];
+  const int Cn = a.C, nout = jb.nout, W = Cn * nout;
+  const int kx0 = blockIdx.x * Cn;
+  const int ny = a.ny, tid = threadIdx.x, nth = blockDim.x;
+  const long long ldc = a.ldc;
+
+  for (int e = tid; e < ny * Cn; e += nth) {
+    const int ky = e / Cn, c = e - ky * Cn, kx = kx0 + c;
+    buf[ky * W + c] = kx < a.ncols ? a.spec[jb.sin + ky * ldc + kx] : mk<C>((T)0, (T)0);
+  }
+  __syncthreads();
+  fft_smem<T, false, true>(buf, ny, a.log2ny, Cn, 1, W, a.tw, tid);
+
+  const double h = a.st != nullptr ? a.st->dtc : a.hfixed;
+  const T hD0 = (T)(h * jb.hfac[0] * jb.D), hD1 = (T)(h * jb.hfac[1] * jb.D);
+  for (int e = tid; e < ny * Cn; e += nth) {
+    const int ky = e / Cn, c = e - ky * Cn, kx = kx0 + c;
+    const T lam = (kx < a.ncols ? a.lamx[kx] : (T)0) + a.lamy[ky];
+    const C v = buf[ky * W + c];
+    buf[ky * W + c] = cscale(v, a.scale * multiplier<T>(jb.mul, hD0, lam, jb.pow[0]));
+    if (nout > 1) buf[ky * W + Cn + c] = cscale(v, a.scale * multiplier<T>(jb.mul, hD1, lam, jb.pow[1]));
+  }
+  __syncthreads();
+  fft_smem<T, true, true>(buf, ny, a.log2ny, W, 1, W, a.tw, tid);
+
+  for (int e = tid; e < ny * W; e += nth) {
+    const int ky = e / W, col = e - ky * W;
+    const int o = col / Cn, c = col - o * Cn, kx = kx0 + c;
+    if (kx < a.ncols) a.spec[jb.sout[o] + ky * ldc + kx] = buf[ky * W + col];
+  }
+}
+
+// ------------------------------------------------------------------ launchers
+static size_t row_smem(int n, int nseq, int elem) { return (size_t)nseq * n * 2 * elem; }
+
+template <typename T, int RX>
+cudaError_t launch_row(const RowArgs<T>& a, cudaStream_t s) {
+  const int tps = a.n >= 16 ? a.n / 16 : 1;
+  const int grid = a.npairs * a.nrows / a.nseq;
+  const size_t smem = row_smem(a.n, a.nseq, sizeof(T));
+  row_kernel<T, RX><<<grid, a.nseq * tps, smem, s>>>(a);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_col(const ColArgs<T>& a, cudaStream_t s) {
+  int maxout = 1;
+  for (int j = 0; j < a.njobs; ++j) maxout = a.job[j].nout > maxout ? a.job[j].nout : maxout;
+  const int tps = a.ny >= 16 ? a.ny / 16 : 1;
+  dim3 grid((a.ncols + a.C - 1) / a.C, a.njobs);
+  const size_t smem = (size_t)a.ny * a.C * maxout * sizeof(cx<T>);
+  col_kernel<T><<<grid, a.C * maxout * tps, smem, s>>>(a);
+  return cudaGetLastError();
+}
+
+#define MJX_INST_ROW(T, RX) template cudaError_t launch_row<T, RX>(const RowArgs<T>&, cudaStream_t);
+MJX_INST_ROW(float, RX_NONE)
+MJX_INST_ROW(float, RX_GRAY_SCOTT)
+MJX_INST_ROW(float, RX_FISHER)
+MJX_INST_ROW(double, RX_NONE)
+MJX_INST_ROW(double, RX_GRAY_SCOTT)
+MJX_INST_ROW(double, RX_FISHER)
+template cudaError_t launch_col<float>(const ColArgs<float>&, cudaStream_t);
+template cudaError_t launch_col<double>(const ColArgs<double>&, cudaStream_t);
+
+// Column tile width: ~256 threads per output, capped by 512 threads and ~200 KB smem.
+int col_tile(int ny, int ncols, int nout, int elem) {
+  const int tps = ny >= 16 ? ny / 16 : 1;
+  int C = 256 / tps;
+  if (C < 1) C = 1;
+  if (C > 16) C = 16;
+  while (C > 1 && (C * nout * tps > 512 || (size_t)ny * C * nout * 2 * elem > 200 * 1024)) C >>= 1;
+  (void)ncols;
+  return C;
+}
+
+// Raise the dynamic shared-memory limit of every kernel once per process.
+mjx_status ensure_kernel_attrs() {
+  static int done = 0;
+  if (done) return MJX_OK;
+  const int big = 227 * 1024;
+  MJX_CUDA_TRY(cudaFuncSetAttribute(row_kernel<float, RX_NONE>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+  MJX_CUDA_TRY(cudaFuncSetAttribute(row_kernel<float, RX_GRAY_SCOTT>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+  MJX_CUDA_TRY(cudaFuncSetAttribute(row_kernel<float, RX_FISHER>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+  MJX_CUDA_TRY(cudaFuncSetAttribute(row_kernel<double, RX_NONE>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+  MJX_CUDA_TRY(cudaFuncSetAttribute(row_kernel<double, RX_GRAY_SCOTT>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+  MJX_CUDA_TRY(cudaFuncSetAttribute(row_kernel<double, RX_FISHER>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+  MJX_CUDA_TRY(cudaFuncSetAttribute(col_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+  MJX_CUDA_TRY(cudaFuncSetAttribute(col_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
+  done = 1;
+  return MJX_OK;
+}
+
+mjx_status check_grid(const mjx_grid2d* g) {
+  if (g == nullptr) return MJX_BAD_ARG;
+  if (ilog2_exact(g->nx) < 1 || ilog2_exact(g->ny) < 1) return MJX_BAD_SHAPE;
+  if (g->nx > 4096 || g->ny > 4096) return MJX_BAD_SHAPE;
+  if (!(g->dx > 0) || !(g->dy > 0)) return MJX_BAD_ARG;
+  return MJX_OK;
+}
+
+int elem_size(int dtype) { return dtype == MJX_F32 ? 4 : (dtype == MJX_F64 ? 8 : 0); }
+
+// Row pass over nfields single fields, pairing rows y and y + ny/2 of each field.
+template <typename T>
+RowArgs<T> field_rows(const mjx_grid2d* g, int nfields, const PlanView& pv, cx<T>* spec) {
+  RowArgs<T> r;
+  memset(&r, 0, sizeof(r));
+  r.n = g->nx; r.log2n = ilog2_exact(g->nx); r.ldc = spec_ldc(g->nx);
+  r.nrows = g->ny / 2; r.npairs = nfields; r.nseq = row_nseq(g->nx, r.nrows);
+  r.rstride = g->nx; r.rin_sel = -1; r.rout_sel = -1;
+  r.spec = spec; r.tw = (const cx<T>*)pv.twx; r.inv_scale = (T)1;
+  for (int f = 0; f < nfields; ++f) {
+    r.pr[f].ra = (long long)f * g->ny * g->nx;
+    r.pr[f].rb = r.pr[f].ra + (long long)(g->ny / 2) * g->nx;
+    r.pr[f].sa = (long long)f * g->ny * r.ldc;
+    r.pr[f].sb = r.pr[f].sa + (long long)(g->ny / 2) * r.ldc;
+    r.pr[f].hfac = 1.0;
+  }
+  return r;
+}
+
+template <typename T>
+ColArgs<T> field_cols(const mjx_grid2d* g, const PlanView& pv, cx<T>* spec, int nout) {
+  ColArgs<T> c;
+  memset(&c, 0, sizeof(c));
+  c.ny = g->ny; c.log2ny = ilog2_exact(g->ny); c.ncols = g->nx / 2 + 1; c.ldc = spec_ldc(g->nx);
+  c.C = col_tile(g->ny, c.ncols, nout, sizeof(T));
+  c.spec = spec; c.lamx = (const T*)pv.lamx; c.lamy = (const T*)pv.lamy;
+  c.tw = (const cx<T>*)pv.twy; c.scale = (T)(1.0 / ((double)g->nx * (double)g->ny));
+  return c;
+}
+
+template <typename T>
+mjx_status spectral_apply(const void* plan, const mjx_grid2d* g, int nfields, const double* D,
+                          double h, int mult, const T* in, T* out, void* ws, cudaStream_t s) {
+  const PlanView pv = plan_view(plan, g->ny, g->nx, sizeof(T));
+  cx<T>* spec = (cx<T>*)ws;
+  const size_t fsz = (size_t)g->ny * g->nx;
+  // gather the fields that diffuse; pass the others through
+  int idx[4], nd = 0;
+  for (int f = 0; f < nfields; ++f) {
+    if (D[f] > 1e-14) idx[nd++] = f;
+    else if (in != out)
+      MJX_CUDA_TRY(cudaMemcpyAsync(out + f * fsz, in + f * fsz, fsz * sizeof(T), cudaMemcpyDeviceToDevice, s));
+  }
+  if (nd == 0) return MJX_OK;
+  RowArgs<T> r = field_rows<T>(g, nd, pv, spec);
+  for (int i = 0; i < nd; ++i) {
+    const long long off = (long long)idx[i] * fsz;
+    r.pr[i].ra += off - (long long)i * fsz;
+    r.pr[i].rb += off - (long long)i * fsz;
+  }
+  r.rin[0] = in; r.rout[0] = out;
+  for (int i = 0; i < nd; ++i) r.pr[i].flags = ROW_STORE_SPEC;
+  MJX_CUDA_TRY((launch_row<T, RX_NONE>(r, s)));
+  ColArgs<T> c = field_cols<T>(g, pv, spec, 1);
+  c.hfixed = h; c.njobs = nd;
+  for (int i = 0; i < nd; ++i) {
+    ColJob& j = c.job[i];
+    j.sin = j.sout[0] = j.sout[1] = (long long)i * g->ny * spec_ldc(g->nx);
+    j.D = D[idx[i]]; j.hfac[0] = j.hfac[1] = 1.0; j.pow[0] = j.pow[1] = 1; j.nout = 1; j.mul = mult;
+  }
+  MJX_CUDA_TRY(launch_col<T>(c, s));
+  for (int i = 0; i < nd; ++i) r.pr[i].flags = ROW_LOAD_SPEC | ROW_STORE_REAL;
+  MJX_CUDA_TRY((launch_row<T, RX_NONE>(r, s)));
+  return MJX_OK;
+}
+
+template <typename T>
+mjx_status fft_cn(const void* plan, const mjx_grid2d* g, double D, double dt, int n_steps,
+                  const T* u_in, T* u_out, void* ws, cudaStream_t s) {
+  const PlanView pv = plan_view(plan, g->ny, g->nx, sizeof(T));
+  cx<T>* spec = (cx<T>*)ws;
+  RowArgs<T> fwd = field_rows<T>(g, 1, pv, spec);
+  RowArgs<T> inv = fwd;
+  fwd.pr[0].flags = ROW_STORE_SPEC;
+  inv.pr[0].flags = ROW_LOAD_SPEC | ROW_STORE_REAL;
+  inv.rout[0] = u_out;
+  ColArgs<T> c = field_cols<T>(g, pv, spec, 1);
+  c.hfixed = dt; c.njobs = 1;
+  c.job[0].D = D; c.job[0].hfac[0] = c.job[0].hfac[1] = 1.0; c.job[0].pow[0] = c.job[0].pow[1] = 1;
+  c.job[0].nout = 1; c.job[0].mul = MUL_CN;
+  if (n_steps <= 0) {
+    if (u_in != u_out)
+      MJX_CUDA_TRY(cudaMemcpyAsync(u_out, u_in, sizeof(T) * g->ny * g->nx, cudaMemcpyDeviceToDevice, s));
+    return MJX_OK;
+  }
+  for (int i = 0; i < n_steps; ++i) {
+    fwd.rin[0] = i == 0 ? u_in : u_out;
+    MJX_CUDA_TRY((launch_row<T, RX_NONE>(fwd, s)));
+    MJX_CUDA_TRY(launch_col<T>(c, s));
+    MJX_CUDA_TRY((launch_row<T, RX_NONE>(inv, s)));
+  }
+  return MJX_OK;
+}
+
+}  // namespace mjx
+
+using namespace mjx;
+
+extern "C" {
+
+const char* mjx_version(void) { return "moljax_gb300 0.1.0 (sm_103a)"; }
+
+const char* mjx_status_string(int st) {
+  switch (st) {
+    case MJX_OK: return "ok";
+    case MJX_BAD_SHAPE: return "unsupported or inconsistent shape";
+    case MJX_BAD_DTYPE: return "unsupported dtype";
+    case MJX_NOT_FINITE: return "non-finite values";
+    case MJX_MAX_ITERS: return "maximum steps/iterations reached";
+    case MJX_DT_TOO_SMALL: return "time step below dt_min";
+    case MJX_NK_FAILED: return "Newton-Krylov failed";
+    case MJX_OOM: return "out of memory";
+    case MJX_CUDA_ERROR: return "CUDA error";
+    case MJX_BAD_ARG: return "bad argument";
+    case MJX_WORKSPACE: return "workspace too small";
+    default: return "unknown status";
+  }
+}
+
+size_t mjx_spec2d_plan_bytes(int ny, int nx, int dtype) {
+  const int e = elem_size(dtype);
+  if (!e || ilog2_exact(nx) < 1 || ilog2_exact(ny) < 1) return 0;
+  return plan_bytes(ny, nx, e);
+}
+
+size_t mjx_spec2d_ws_bytes(int ny, int nx, int nfields, int dtype) {
+  const int e = elem_size(dtype);
+  if (!e || ilog2_exact(nx) < 1 || ilog2_exact(ny) < 1 || nfields < 1) return 0;
+  return (size_t)nfields * ny * spec_ldc(nx) * 2 * e;
+}
+
+mjx_status mjx_spec2d_plan_init(void* plan, const mjx_grid2d* g, int symbol, int dtype,
+                                void* stream) {
+  MJX_TRY(check_grid(g));
+  const int e = elem_size(dtype);
+  if (!e) return MJX_BAD_DTYPE;
+  if (plan == nullptr) return MJX_BAD_ARG;
+  if (symbol != MJX_SYMBOL_FD && symbol != MJX_SYMBOL_SPECTRAL) return MJX_BAD_ARG;
+  const int nx = g->nx, ny = g->ny, ldc = spec_ldc(nx);
+  const size_t bytes = plan_bytes(ny, nx, e);
+  std::vector<unsigned char> host(bytes, 0);
+  PlanView pv = plan_view(host.data(), ny, nx, e);
+  const double twopi = 6.283185307179586476925286766559;
+  auto put_tw = [&](const void* dst, int n) {
+    for (int j = 0; j < n; ++j) {
+      const double ang = twopi * (double)j / (double)n;
+      const double c = cos(ang), s = -sin(ang);
+      if (e == 4) { float* p = (float*)dst; p[2 * j] = (float)c; p[2 * j + 1] = (float)s; }
+      else { double* p = (double*)dst; p[2 * j] = c; p[2 * j + 1] = s; }
+    }
+  };
+  // eigenvalue of the 1D periodic Laplacian for integer frequency m on n points of spacing d
+  auto lam1 = [&](int m, int n, double d) {
+    if (symbol == MJX_SYMBOL_FD) return (2.0 * cos(twopi * (double)m / (double)n) - 2.0) / (d * d);
+    const double k = twopi * (double)m / ((double)n * d);
+    return -k * k;
+  };
+  put_tw(pv.twx, nx);
+  put_tw(pv.twy, ny);
+  for (int kx = 0; kx < ldc; ++kx) {
+    const double v = kx <= nx / 2 ? lam1(kx, nx, g->dx) : 0.0;
+    if (e == 4) ((float*)pv.lamx)[kx] = (float)v; else ((double*)pv.lamx)[kx] = v;
+  }
+  for (int ky = 0; ky < ny; ++ky) {
+    const int m = ky < ny / 2 ? ky : ky - ny;  // fftfreq order
+    const double v = lam1(m, ny, g->dy);
+    if (e == 4) ((float*)pv.lamy)[ky] = (float)v; else ((double*)pv.lamy)[ky] = v;
+  }
+  MJX_CUDA_TRY(cudaMemcpyAsync(plan, host.data(), bytes, cudaMemcpyHostToDevice, (cudaStream_t)stream));
+  MJX_CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream));
+  return MJX_OK;
+}
+
+mjx_status mjx_spectral_apply2d(const void* plan, const mjx_grid2d* g, int dtype, int nfields,
+                                const double* D, double h, int mult, const void* in, void* out,
+                                void* ws, size_t ws_bytes, void* stream) {
+  MJX_TRY(check_grid(g));
+  if (nfields < 1 || nfields > 4 || D == nullptr || plan == nullptr || in == nullptr || out == nullptr)
+    return MJX_BAD_ARG;
+  if (mult < MJX_MULT_SCALE || mult > MJX_MULT_EXP) return MJX_BAD_ARG;
+  const int e = elem_size(dtype);
+  if (!e) return MJX_BAD_DTYPE;
+  if (ws == nullptr || ws_bytes < mjx_spec2d_ws_bytes(g->ny, g->nx, nfields, dtype)) return MJX_WORKSPACE;
+  MJX_TRY(ensure_kernel_attrs());
+  cudaStream_t s = (cudaStream_t)stream;
+  if (e == 4) return spectral_apply<float>(plan, g, nfields, D, h, mult, (const float*)in, (float*)out, ws, s);
+  return spectral_apply<double>(plan, g, nfields, D, h, mult, (const double*)in, (double*)out, ws, s);
+}
+
+mjx_status mjx_fft_cn2d(const void* plan, const mjx_grid2d* g, int dtype, double D, double dt,
+                        int n_steps, const void* u_in, void* u_out, void* ws, size_t ws_bytes,
+                        void* stream) {
+  MJX_TRY(check_grid(g));
+  if (plan == nullptr || u_in == nullptr || u_out == nullptr || n_steps < 0) return MJX_BAD_ARG;
+  const int e = elem_size(dtype);
+  if (!e) return MJX_BAD_DTYPE;
+  if (ws == nullptr || ws_bytes < mjx_spec2d_ws_bytes(g->ny, g->nx, 1, dtype)) return MJX_WORKSPACE;
+  MJX_TRY(ensure_kernel_attrs());
+  cudaStream_t s = (cudaStream_t)stream;
+  if (e == 4) return fft_cn<float>(plan, g, D, dt, n_steps, (const float*)u_in, (float*)u_out, ws, s);
+  return fft_cn<double>(plan, g, D, dt, n_steps, (const double*)u_in, (double*)u_out, ws, s);
+}
+
+}  // extern "C"

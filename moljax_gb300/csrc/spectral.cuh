@@ -1,0 +1,115 @@
+// Row and column spectral passes over 2D periodic fields (internal interface).
+//
+// Data layout in HBM (all interior-only, no ghost cells):
+//   real field   f[y][x], row stride `rstride` elements, fields `fstride` apart
+//   half spectrum S[ky][kx], kx in [0, nx/2], row stride ldc (complex elements)
+// Two real rows (a, b) are packed as one complex row z = a + i b for every
+// row transform ("pair"), which gives two real FFTs for the price of one.
+#pragma once
+
+#include "common.cuh"
+#include "fft.cuh"
+
+namespace mjx {
+
+// Device-resident state of an adaptive run (lives in the caller's workspace).
+struct DevState {
+  double t, dt, dtc, t_end, prev_err, err_last, dt_cfl, dt_last_accepted;
+  int cur, status, n_acc, n_rej, write_idx, attempts, done, finite;
+  int max_saves, save_every, max_attempts, order;
+  int save_slot, pad0, pad1, pad2;
+};
+
+enum { MJX_MAXPAIR = 8, MJX_MAXJOB = 8 };
+
+// moljax StatusCode values (moljax/core/utils.py:265-272), kept in DevState.status
+enum {
+  MJX_STATUS_SUCCESS_CODE = 0,
+  MJX_STATUS_RUNNING_CODE = 1,
+  MJX_STATUS_MAX_STEPS_CODE = 2,
+  MJX_STATUS_DT_TOO_SMALL_CODE = 3,
+  MJX_STATUS_NON_FINITE_CODE = 4,
+  MJX_STATUS_NK_FAILED_CODE = 5
+};
+
+// per-pair runtime flags of a row pass
+enum {
+  ROW_LOAD_SPEC = 1,   // input is a half spectrum (c2r first); else real rows
+  ROW_STORE_REAL = 2,  // store the real rows (after the pointwise op)
+  ROW_REACT = 4,       // Heun reaction step of length hfac*dt on (a, b)
+  ROW_STORE_SPEC = 8,  // r2c at the end and store the half spectrum
+  ROW_ERRNORM = 16,    // accumulate the scaled error of (a, b) against eref
+};
+
+// pointwise reaction kinds (compile-time)
+enum { RX_NONE = 0, RX_GRAY_SCOTT = 1, RX_FISHER = 2, RX_LINEAR = 3 };
+
+struct RowPair {
+  long long ra, rb;    // real row offsets (elements) of rows a and b at y = 0
+  long long sa, sb;    // spectrum offsets (complex elements) at ky = 0
+  double hfac;         // reaction step = hfac * (dt from state, or hfixed)
+  int flags;
+  int pad;
+};
+
+template <typename T> struct RowArgs {
+  int n, log2n, ldc, nrows, npairs, nseq;
+  long long rstride;
+  const T* rin[2];     // real input bases; rin_sel: -1 -> rin[0], 0 -> rin[cur], 1 -> rin[1-cur]
+  T* rout[2];
+  int rin_sel, rout_sel;
+  const T* eref;       // error reference base (same offsets as the real output)
+  cx<T>* spec;         // spectrum base (read and/or written in place)
+  const cx<T>* tw;     // twiddles for n
+  T inv_scale;         // scale applied after the inverse transform
+  double hfixed;       // reaction step when st == nullptr
+  double F, k, r;      // reaction parameters
+  double atol, rtol;
+  double* partial;     // per-CTA error partial sums (ROW_ERRNORM)
+  int* nonfinite;      // per-CTA non-finite flags (ROW_ERRNORM)
+  const DevState* st;
+  RowPair pr[MJX_MAXPAIR];
+};
+
+enum { MUL_SCALE = 0, MUL_HELMHOLTZ = 1, MUL_CN = 2, MUL_EXP = 3 };
+
+struct ColJob {
+  long long sin;         // spectrum offset of the input column block (ky=0, kx=0)
+  long long sout[2];     // outputs (may equal sin)
+  double D;              // diffusivity of this field
+  double hfac[2];        // step = hfac * dt
+  int pow[2];            // multiplier power (1 or 2)
+  int nout;
+  int mul;               // MUL_*
+};
+
+template <typename T> struct ColArgs {
+  int ny, log2ny, ncols, ldc, C, njobs;
+  cx<T>* spec;
+  const T* lamx;         // symbol along x, length ldc (kx = 0..nx/2)
+  const T* lamy;         // symbol along y, length ny (fftfreq order)
+  const cx<T>* tw;       // twiddles for ny
+  T scale;               // normalisation 1/(nx*ny)
+  double hfixed;
+  const DevState* st;
+  ColJob job[MJX_MAXJOB];
+};
+
+// Plan layout (device bytes): twx[nx] twy[ny] lamx[ldc] lamy[ny], 256-byte aligned parts.
+struct PlanView {
+  const void* twx; const void* twy; const void* lamx; const void* lamy;
+};
+size_t plan_bytes(int ny, int nx, int elem);
+PlanView plan_view(const void* plan, int ny, int nx, int elem);
+int spec_ldc(int nx);
+
+template <typename T, int RX>
+cudaError_t launch_row(const RowArgs<T>& a, cudaStream_t s);
+template <typename T>
+cudaError_t launch_col(const ColArgs<T>& a, cudaStream_t s);
+
+// Row-pass CTA geometry helpers (sequences per CTA and CTA count).
+int row_nseq(int n, int nrows);
+int row_ctas(int n, int nrows, int npairs);
+
+}  // namespace mjx

@@ -1,0 +1,66 @@
+"""Oracle: FFT Crank-Nicolson on a periodic box.
+
+TEST INFRASTRUCTURE ONLY (see ``oracle/__init__.py``).  Restates the FFT-CN
+step the reference benchmarks use (it is not a function of the moljax
+package itself):
+
+* ``benchmarks/benchmark_vs_scipy.py:74-114`` -- 2D, pseudo-spectral symbol
+  -(kx^2+ky^2), ``cn_factor = (1 + dt D lam/2) / (1 - dt D lam/2)``, each step
+  ``real(ifft2(fft2(u) * cn_factor))``;
+* ``benchmarks/sisc/bench_precision_fp32_fp64.py:41-100`` -- the same at
+  128^2, D=0.1, T=0.1 for a range of dt (the published error table);
+* ``benchmarks/benchmark_solver_comparison.py:152-163`` -- the 1D form.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+
+from oracle.mol import fd_symbol_1d, spectral_symbol_1d
+
+
+def node_grid_ic(n, L=1.0):
+    """u0 = sin(2 pi x) sin(2 pi y) on x = j L/n, meshgrid 'ij' (benchmark_vs_scipy.py:62-65)."""
+    x = np.linspace(0.0, L, n, endpoint=False)
+    X, Y = np.meshgrid(x, x, indexing="ij")
+    return np.sin(2 * np.pi * X) * np.sin(2 * np.pi * Y)
+
+
+def symbol_2d(n0, n1, d0, d1, kind="spectral"):
+    """Laplacian eigenvalues on an (n0, n1) periodic grid, fftfreq order."""
+    f = spectral_symbol_1d if kind == "spectral" else fd_symbol_1d
+    return f(n0, d0)[:, None] + f(n1, d1)[None, :]
+
+
+def cn_factor(lam, D, dt):
+    """benchmarks/benchmark_vs_scipy.py:74-81."""
+    return (1.0 + 0.5 * dt * D * lam) / (1.0 - 0.5 * dt * D * lam)
+
+
+def fft_cn_2d(u0, D, dx, dt, n_steps, kind="spectral", dy=None):
+    """benchmarks/benchmark_vs_scipy.py:83-91 / 99-114: n_steps one-by-one CN steps."""
+    dy = dx if dy is None else dy
+    lam = symbol_2d(u0.shape[0], u0.shape[1], dy, dx, kind)
+    G = cn_factor(lam, D, dt)
+    u = np.array(u0, dtype=np.float64, copy=True)
+    for _ in range(n_steps):
+        u = np.real(np.fft.ifft2(np.fft.fft2(u) * G))
+    return u
+
+
+def fft_cn_1d(u0, D, dx, dt, n_steps, kind="spectral", v=0.0):
+    """benchmarks/benchmark_solver_comparison.py:145-163 (v != 0 adds -i k v)."""
+    n = u0.shape[0]
+    k = 2 * np.pi * np.fft.fftfreq(n, dx)
+    lam = -(k * k) if kind == "spectral" else fd_symbol_1d(n, dx)
+    L = D * lam + v * (-1j * k)
+    G = (1 + 0.5 * dt * L) / (1 - 0.5 * dt * L)
+    u = np.array(u0, dtype=np.float64, copy=True)
+    for _ in range(n_steps):
+        u = np.real(np.fft.ifft(np.fft.fft(u) * G))
+    return u
+
+
+def analytic_decay(u0, D, T):
+    """exp(-8 pi^2 D T) u0 (benchmark_vs_scipy.py:67-68)."""
+    return np.exp(-8 * np.pi ** 2 * D * T) * u0

@@ -1,0 +1,49 @@
+"""Writes tests/golden/*.json from the reference's own published result files.
+
+Run in a checkout that has the reference (gogipav14/moljax) at REF (default
+/root/reference).  The fixtures hold only the numbers the tests pin:
+the FFT-CN error tables of benchmarks/results/precision_fp32_fp64.json and
+benchmarks/results/scipy_comparison.json, and the CN reactor conversions of
+benchmarks/results/method_comparison_results.json.
+"""
+
+import json
+import os
+import sys
+
+REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def main():
+    res = os.path.join(REF, "benchmarks", "results")
+    prec = json.load(open(os.path.join(res, "precision_fp32_fp64.json")))
+    sc = json.load(open(os.path.join(res, "scipy_comparison.json")))
+    out = {
+        "source": "benchmarks/results/precision_fp32_fp64.json, scipy_comparison.json",
+        "grid": 128, "L": 1.0,
+        "precision_table": {
+            "D": prec["config"]["D"], "t_final": prec["config"]["t_final"],
+            "fp64": [{"dt": r["dt"], "n_steps": r["n_steps"], "error": r["error"]} for r in prec["fp64"]],
+            "fp32": [{"dt": r["dt"], "n_steps": r["n_steps"], "error": r["error"]} for r in prec["fp32"]],
+        },
+        "scipy_comparison": {
+            "D": sc["config"]["D"], "t_final": sc["config"]["t_final"],
+            "n_steps": sc["config"]["fft_cn_steps"], "dt": sc["config"]["fft_cn_dt"],
+            "numpy_error": sc["results"]["numpy_fft_cn"]["error"],
+            "jax_error": sc["results"]["jax_fft_cn"]["error"],
+        },
+    }
+    with open(os.path.join(HERE, "fftcn_published.json"), "w") as f:
+        json.dump(out, f, indent=1)
+    mc = json.load(open(os.path.join(res, "method_comparison_results.json")))
+    reactor = {k: {"CN": {kk: v["CN"][kk] for kk in ("conversion", "steps", "dt", "t_final")},
+                   "analytical": v.get("analytical")}
+               for k, v in mc["reactor_methods"].items()}
+    with open(os.path.join(HERE, "reactor_published.json"), "w") as f:
+        json.dump({"source": "benchmarks/results/method_comparison_results.json",
+                   "reactor_methods": reactor}, f, indent=1)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,99 @@
+"""IMEX-Strang step and the adaptive device loop vs the NumPy FP64 oracle."""
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import imex as OI
+from oracle import mol
+
+pytestmark = pytest.mark.gpu
+
+
+def _setup(n, dtype, cuda, seed=11):
+    import moljax_gb300 as M
+    grid = M.Grid2D(n, n, 0.0, 2.5, 0.0, 2.5)
+    model, cache, diff = M.create_gray_scott_periodic_fft(grid, 2e-5, 1e-5, 0.035, 0.065, dtype, cuda)
+    og = mol.Grid2D(n, n, 0, 2.5, 0, 2.5)
+    y0 = mol.gray_scott_ic(og, seed)
+    ym = {k: torch.tensor(v, dtype=dtype, device=cuda) for k, v in y0.items()}
+    omodel, lam, odiff = OI.gray_scott_periodic(og, 2e-5, 1e-5, 0.035, 0.065)
+    return M, grid, model, cache, diff, ym, og, y0, omodel, lam, odiff
+
+
+def _rel(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+@pytest.mark.parametrize("n", [16, 64, 256])
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+def test_strang_step_vs_oracle(cuda, n, dtype):
+    M, grid, model, cache, diff, ym, og, y0, om, lam, od = _setup(n, dtype, cuda)
+    out = M.imex_strang_step(model, ym, 0.0, 0.8, cache, diff)
+    ref = OI.imex_strang_step(om, y0, 0.8, lam, od)
+    tol = 1e-13 if dtype == torch.float64 else 2e-6
+    for k in ("u", "v"):
+        assert _rel(out[k].cpu().numpy(), ref[k]) < tol  # ghosts included (periodic fill)
+
+
+def test_adaptive_fp64_matches_oracle_counts(cuda):
+    M, grid, model, cache, diff, ym, og, y0, om, lam, od = _setup(32, torch.float64, cuda)
+    pid = M.PIDParams(atol=1e-7, rtol=1e-5)
+    r = M.adaptive_integrate_imex(model, ym, 0.0, 40.0, 1.0, cache, diff, pid_params=pid,
+                                  save_every=1, max_steps=2000)
+    ro = OI.adaptive_integrate_imex(om, y0, 0.0, 40.0, 1.0, lam, od,
+                                    pid=OI.PIDParams(atol=1e-7, rtol=1e-5), save_every=1,
+                                    max_steps=2000)
+    assert r.status == ro.status == 0
+    assert (r.n_accepted, r.n_rejected) == (ro.n_accepted, ro.n_rejected)
+    assert r.t_final == pytest.approx(ro.t_final, abs=1e-12)
+    for k in ("u", "v"):
+        assert _rel(r.y_final[k].cpu().numpy(), ro.y_final[k]) < 1e-11
+    nh = ro.n_steps
+    assert r.n_steps == nh
+    np.testing.assert_allclose(r.t_history.cpu().numpy()[:nh], ro.t_history[:nh], rtol=1e-13)
+    np.testing.assert_allclose(r.dt_history.cpu().numpy()[:nh], ro.dt_history[:nh], rtol=1e-10)
+    for k in ("u", "v"):
+        assert _rel(r.y_history[k][:nh].cpu().numpy(), ro.y_history[k][:nh]) < 1e-11
+
+
+def test_adaptive_fp32_close_to_fp64_oracle(cuda):
+    M, grid, model, cache, diff, ym, og, y0, om, lam, od = _setup(64, torch.float32, cuda)
+    pid = M.PIDParams(atol=1e-7, rtol=1e-5)
+    r = M.adaptive_integrate_imex(model, ym, 0.0, 20.0, 1.0, cache, diff, pid_params=pid,
+                                  save_every=1000, save_y_history=False)
+    ro = OI.adaptive_integrate_imex(om, y0, 0.0, 20.0, 1.0, lam, od,
+                                    pid=OI.PIDParams(atol=1e-7, rtol=1e-5), save_every=1000,
+                                    keep_history=False)
+    assert r.status == ro.status == 0
+    assert abs(r.n_accepted - ro.n_accepted) <= 2
+    for k in ("u", "v"):
+        assert _rel(r.y_final[k].cpu().numpy(), ro.y_final[k]) < 1e-5
+
+
+def test_adaptive_nonfinite_status(cuda):
+    # a NaN in the initial data: the first attempt is rejected and the run stops
+    M, grid, model, cache, diff, ym, og, y0, om, lam, od = _setup(16, torch.float64, cuda)
+    ym["u"][5, 5] = float("nan")
+    r = M.adaptive_integrate_imex(model, ym, 0.0, 10.0, 1.0, cache, diff)
+    assert r.status == M.StatusCode.NON_FINITE_VALUES
+    assert r.n_accepted == 0 and r.n_rejected == 1
+
+
+def test_adaptive_dt_too_small(cuda):
+    # impossible tolerance with dt_min close to dt: DT_TOO_SMALL as the reference
+    M, grid, model, cache, diff, ym, og, y0, om, lam, od = _setup(16, torch.float64, cuda)
+    pid = M.PIDParams(atol=1e-30, rtol=1e-30, dt_min=0.3)
+    r = M.adaptive_integrate_imex(model, ym, 0.0, 10.0, 1.0, cache, diff, pid_params=pid)
+    ro = OI.adaptive_integrate_imex(om, y0, 0.0, 10.0, 1.0, lam, od,
+                                    pid=OI.PIDParams(atol=1e-30, rtol=1e-30, dt_min=0.3))
+    assert r.status == ro.status == M.StatusCode.DT_TOO_SMALL
+    assert (r.n_accepted, r.n_rejected) == (ro.n_accepted, ro.n_rejected)
+
+
+def test_adaptive_max_steps(cuda):
+    M, grid, model, cache, diff, ym, og, y0, om, lam, od = _setup(16, torch.float64, cuda)
+    r = M.adaptive_integrate_imex(model, ym, 0.0, 100.0, 1.0, cache, diff, max_steps=5)
+    ro = OI.adaptive_integrate_imex(om, y0, 0.0, 100.0, 1.0, lam, od, max_steps=5)
+    assert r.status == ro.status == M.StatusCode.MAX_STEPS_REACHED
+    assert r.n_accepted == ro.n_accepted == 5

@@ -1,0 +1,146 @@
+"""The oracle against the reference's published numbers and known answers (CPU)."""
+
+import json
+import os
+
+import numpy as np
+import pytest
+
+from oracle import fftcn, imex, mol
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def _load(name):
+    with open(os.path.join(GOLD, name)) as f:
+        return json.load(f)
+
+
+@pytest.mark.parametrize("row", _load("fftcn_published.json")["precision_table"]["fp64"])
+def test_fftcn_error_table_fp64(row):
+    # benchmarks/results/precision_fp32_fp64.json: 128^2, D=0.1, T=0.1, max error vs analytic
+    g = _load("fftcn_published.json")
+    D, T = g["precision_table"]["D"], g["precision_table"]["t_final"]
+    u0 = fftcn.node_grid_ic(128)
+    n = int(T / row["dt"])
+    assert n == row["n_steps"]
+    u = fftcn.fft_cn_2d(u0, D, 1.0 / 128, row["dt"], n)
+    err = np.max(np.abs(u - fftcn.analytic_decay(u0, D, n * row["dt"])))
+    # the published value carries FP64 rounding of the reference run (~1e-16 * steps)
+    assert err == pytest.approx(row["error"], rel=1e-9, abs=2e-14 * n)
+
+
+def test_fftcn_scipy_comparison_bitwise():
+    # benchmarks/results/scipy_comparison.json: the NumPy FFT-CN error, reproduced exactly
+    s = _load("fftcn_published.json")["scipy_comparison"]
+    u0 = fftcn.node_grid_ic(128)
+    u = fftcn.fft_cn_2d(u0, s["D"], 1.0 / 128, s["dt"], s["n_steps"])
+    err = np.max(np.abs(u - fftcn.analytic_decay(u0, s["D"], s["t_final"])))
+    assert err == pytest.approx(s["numpy_error"], rel=1e-12)
+    assert err == pytest.approx(s["jax_error"], rel=1e-5)
+
+
+def test_fd_symbol_zero_mode_and_sign():
+    # tests/test_fft_solver.py:43-57
+    lam = mol.fd_symbol_2d(16, 16, 0.1, 0.1)
+    assert lam[0, 0] == pytest.approx(0.0, abs=1e-12)
+    assert np.all(lam.ravel()[1:] < 0)
+
+
+def test_helmholtz_residual():
+    # tests/test_fft_solver.py:140-205: (I - dt D lam) u = rhs in Fourier space
+    rng = np.random.default_rng(0)
+    rhs = rng.standard_normal((32, 32))
+    lam = mol.fd_symbol_2d(32, 32, 1 / 32, 1 / 32)
+    u = mol.solve_helmholtz_2d(rhs, lam, 0.01, 0.1)
+    back = np.fft.ifft2(np.fft.fft2(u) * (1 - 0.01 * 0.1 * lam)).real
+    assert np.max(np.abs(back - rhs)) < 1e-12
+
+
+def test_helmholtz_fd_residual():
+    # tests/test_fft_solver.py:207-247: u - dt D Lap_FD(u) == rhs with periodic ghosts
+    g = mol.Grid2D(32, 32, 0, 1, 0, 1)
+    rng = np.random.default_rng(1)
+    rhs = rng.standard_normal((32, 32))
+    lam = mol.fd_symbol_2d(32, 32, g.dy, g.dx)
+    u = mol.solve_helmholtz_2d(rhs, lam, 0.01, 0.1)
+    up = mol.bc_2d(mol.pad(u, g), g, mol.PERIODIC)
+    lap = mol.interior(mol.laplacian_2d(up, g), g)
+    assert np.max(np.abs(u - 0.01 * 0.1 * lap - rhs)) < 1e-10
+
+
+def _gs(n=32):
+    g = mol.Grid2D(n, n, 0, 2.5, 0, 2.5)
+    model, lam, diff = imex.gray_scott_periodic(g, 2e-5, 1e-5, 0.035, 0.065)
+    return g, model, lam, diff
+
+
+def test_imex_pure_diffusion_decay():
+    # tests/test_imex.py:99-136: sin mode decays like exp(-2 D t) (rtol 0.01)
+    n = 32
+    g = mol.Grid2D(n, n, 0, 2 * np.pi, 0, 2 * np.pi)
+    model = imex.Model(g, {"u": mol.PERIODIC}, {}, None)
+    lam = mol.fd_symbol_2d(n, n, g.dy, g.dx)
+    X, Y = g.meshgrid(include_ghost=True)
+    y = {"u": np.sin(X) * np.sin(Y)}
+    D, dt = 0.1, 0.01
+    for _ in range(100):
+        y = imex.imex_strang_step(model, y, dt, lam, {"u": D})
+    ratio = np.max(np.abs(mol.interior(y["u"], g))) / np.max(np.abs(np.sin(X) * np.sin(Y))[g.interior_slice])
+    assert ratio == pytest.approx(np.exp(-2 * D * 1.0), rel=0.01)
+
+
+def test_fixed_dt_equals_manual_steps():
+    # tests/test_imex.py:233-259
+    g, model, lam, diff = _gs(16)
+    y0 = mol.gray_scott_ic(g, seed=3)
+    ts, ys, yf = imex.integrate_imex_fixed_dt(model, y0, 0.0, 2.0, 0.5, lam, diff)
+    y = y0
+    for _ in range(len(ts)):
+        y = imex.imex_strang_step(model, y, 0.5, lam, diff)
+    for k in y:
+        assert np.max(np.abs(y[k] - yf[k])) < 1e-10
+
+
+def test_adaptive_imex_success_and_accept_rate():
+    # tests/test_imex.py:185-231: SUCCESS, accept rate > 0.5, bounded GS fields
+    g, model, lam, diff = _gs(16)
+    y0 = mol.gray_scott_ic(g, seed=4)
+    pid = imex.PIDParams(atol=1e-7, rtol=1e-5)
+    r = imex.adaptive_integrate_imex(model, y0, 0.0, 20.0, 1.0, lam, diff, pid=pid,
+                                     save_every=100, keep_history=False)
+    assert r.status == imex.SUCCESS
+    assert r.t_final == pytest.approx(20.0)
+    assert r.n_accepted / (r.n_accepted + r.n_rejected) > 0.5
+    for k in r.y_final:
+        assert np.all(np.isfinite(r.y_final[k]))
+        assert np.all(r.y_final[k] > -0.5) and np.all(r.y_final[k] < 1.5)
+
+
+def test_controller_formulas():
+    # dt_policy.py:178-268 by hand
+    pid = imex.PIDParams()
+    dt, pe = imex.pid_controller_dt(0.1, 0.5, 1.0, pid, 2)
+    fac = min(max((2.0 ** 0.35) * ((1.0 / 0.5) ** 0.2) * 0.9, 0.2), 5.0)
+    assert dt == pytest.approx(0.1 * fac) and pe == 0.5
+    assert imex.handle_rejected_step(0.1, 4.0, pid, 2) == pytest.approx(0.1 * 0.9 * 0.25 ** 0.35)
+    assert imex.handle_rejected_step(0.1, 1e6, pid, 2) == pytest.approx(0.02)
+
+
+def test_imex_cfl_gray_scott():
+    # dt_policy.py:430-502: reaction limit 0.5/(F+k) -> 5, capped by dt_max 1, x safety 0.9
+    g = mol.Grid2D(8, 8, 0, 1, 0, 1)
+    assert imex.imex_cfl_dt(g, {"F": 0.035, "k": 0.065}, imex.CFLParams()) == pytest.approx(0.9)
+
+
+def test_bc_formulas_2d():
+    # tests/test_bc.py: periodic wrap, Dirichlet 2b-u, Neumann u -/+ 2 dx q
+    g = mol.Grid2D(4, 3, 0, 1, 0, 1)
+    rng = np.random.default_rng(2)
+    f = rng.standard_normal((5, 6))
+    p = mol.bc_2d(f, g, mol.PERIODIC)
+    assert np.allclose(p[1:-1, 0], f[1:-1, 4]) and np.allclose(p[0, 1:-1], p[3, 1:-1])
+    d = mol.bc_2d(f, g, mol.DIRICHLET, {"left": 1.0})
+    assert np.allclose(d[1:-1, 0], 2.0 - f[1:-1, 1])
+    n = mol.bc_2d(f, g, mol.NEUMANN, {"top": 0.5})
+    assert np.allclose(n[4, :], n[3, :] + 2 * g.dy * 0.5)
