@@ -70,8 +70,10 @@ __device__ __forceinline__ void react_heun(T& a, T& b, T h, T F, T k, T r) {
 template <typename T> __device__ __forceinline__ bool finite_(T v) { return isfinite(v); }
 
 // ------------------------------------------------------------------ row pass
+template <typename T> struct Occ { static constexpr int row = sizeof(T) == 4 ? 4 : 2, col = sizeof(T) == 4 ? 2 : 1; };
+
 template <typename T, int RX>
-__global__ void __launch_bounds__(256, 2) row_kernel(const __grid_constant__ RowArgs<T> a) {
+__global__ void __launch_bounds__(256, Occ<T>::row) row_kernel(const __grid_constant__ RowArgs<T> a) {
   typedef cx<T> C;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* buf = reinterpret_cast<C*>(smem_raw);
@@ -97,17 +99,37 @@ __global__ void __launch_bounds__(256, 2) row_kernel(const __grid_constant__ Row
   if (flags & ROW_LOAD_SPEC) {
     const C* A = a.spec + pr.sa + y * a.ldc;
     const C* B = a.spec + pr.sb + y * a.ldc;
-    for (int kk = lt; kk <= half; kk += tps) {
-      const C Ak = A[kk], Bk = B[kk];
-      Z(kk) = mk<C>(Ak.x - Bk.y, Ak.y + Bk.x);                    // A_k + i B_k
-      if (kk > 0 && kk < half) Z(n - kk) = mk<C>(Ak.x + Bk.y, Bk.x - Ak.y);  // conj(A_k) + i conj(B_k)
+    // every thread owns kk = lt + m*tps, m < 9 (n/2+1 <= 9*tps): issue all loads first
+    C Ak[9], Bk[9];
+#pragma unroll
+    for (int m = 0; m < 9; ++m) {
+      const int kk = lt + m * tps;
+      if (kk <= half) { Ak[m] = A[kk]; Bk[m] = B[kk]; }
+    }
+#pragma unroll
+    for (int m = 0; m < 9; ++m) {
+      const int kk = lt + m * tps;
+      if (kk <= half) {
+        Z(kk) = mk<C>(Ak[m].x - Bk[m].y, Ak[m].y + Bk[m].x);                    // A_k + i B_k
+        if (kk > 0 && kk < half) Z(n - kk) = mk<C>(Ak[m].x + Bk[m].y, Bk[m].x - Ak[m].y);  // conj(A_k) + i conj(B_k)
+      }
     }
     __syncthreads();
     fft_smem<T, true, false>(buf, n, a.log2n, a.nseq, n, 1, a.tw, tid);
   } else {
     const T* ra = rin + pr.ra + y * a.rstride;
     const T* rb = rin + pr.rb + y * a.rstride;
-    for (int x = lt; x < n; x += tps) Z(x) = mk<C>(ra[x], rb[x]);
+    T va[16], vb[16];
+#pragma unroll
+    for (int m = 0; m < 16; ++m) {
+      const int x = lt + m * tps;
+      if (x < n) { va[m] = ra[x]; vb[m] = rb[x]; }
+    }
+#pragma unroll
+    for (int m = 0; m < 16; ++m) {
+      const int x = lt + m * tps;
+      if (x < n) Z(x) = mk<C>(va[m], vb[m]);
+    }
     __syncthreads();
   }
 
@@ -121,15 +143,26 @@ __global__ void __launch_bounds__(256, 2) row_kernel(const __grid_constant__ Row
   T* ob = rout + pr.rb + y * a.rstride;
   const T* ea = a.eref + pr.ra + y * a.rstride;
   const T* eb = a.eref + pr.rb + y * a.rstride;
-  for (int x = lt; x < n; x += tps) {
+  T ra_[16], rb_[16];
+  if (flags & ROW_ERRNORM) {
+#pragma unroll
+    for (int m = 0; m < 16; ++m) {
+      const int x = lt + m * tps;
+      if (x < n) { ra_[m] = ea[x]; rb_[m] = eb[x]; }
+    }
+  }
+#pragma unroll
+  for (int m = 0; m < 16; ++m) {
+    const int x = lt + m * tps;
+    if (x >= n) continue;
     const C v = Z(x);
     T va = v.x * sc, vb = v.y * sc;
     if (flags & ROW_REACT) react_heun<T, RX>(va, vb, h, (T)a.F, (T)a.k, (T)a.r);
     if (flags & ROW_STORE_REAL) { oa[x] = va; ob[x] = vb; }
     if (flags & ROW_ERRNORM) {
       // moljax/core/state.py:335-339: (err / (atol + rtol |y_new|))^2
-      const T da = (va - ea[x]) / ((T)a.atol + (T)a.rtol * fabs(va));
-      const T db = (vb - eb[x]) / ((T)a.atol + (T)a.rtol * fabs(vb));
+      const T da = (va - ra_[m]) / ((T)a.atol + (T)a.rtol * fabs(va));
+      const T db = (vb - rb_[m]) / ((T)a.atol + (T)a.rtol * fabs(vb));
       esum += da * da + db * db;
       bad |= !(finite_(va) && finite_(vb));
     }
@@ -142,7 +175,10 @@ __global__ void __launch_bounds__(256, 2) row_kernel(const __grid_constant__ Row
     fft_smem<T, false, false>(buf, n, a.log2n, a.nseq, n, 1, a.tw, tid);
     C* A = a.spec + pr.sa + y * a.ldc;
     C* B = a.spec + pr.sb + y * a.ldc;
-    for (int kk = lt; kk <= half; kk += tps) {
+#pragma unroll
+    for (int m = 0; m < 9; ++m) {
+      const int kk = lt + m * tps;
+      if (kk > half) continue;
       const C Zk = Z(kk), Zm = Z((n - kk) & (n - 1));
       A[kk] = mk<C>((T)0.5 * (Zk.x + Zm.x), (T)0.5 * (Zk.y - Zm.y));
       B[kk] = mk<C>((T)0.5 * (Zk.y + Zm.y), (T)0.5 * (Zm.x - Zk.x));
@@ -199,7 +235,7 @@ __device__ __forceinline__ T multiplier(int mul, T hD, T lam, int pw) {
 }
 
 template <typename T>
-__global__ void __launch_bounds__(512) col_kernel(const __grid_constant__ ColArgs<T> a) {
+__global__ void __launch_bounds__(512, Occ<T>::col) col_kernel(const __grid_constant__ ColArgs<T> a) {
   typedef cx<T> C;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* buf = reinterpret_cast<C*>(smem_raw);
@@ -210,9 +246,20 @@ __global__ void __launch_bounds__(512) col_kernel(const __grid_constant__ ColArg
   const int ny = a.ny, tid = threadIdx.x, nth = blockDim.x;
   const long long ldc = a.ldc;
 
-  for (int e = tid; e < ny * Cn; e += nth) {
-    const int ky = e / Cn, c = e - ky * Cn, kx = kx0 + c;
-    buf[sp(ky * W + c)] = kx < a.ncols ? a.spec[jb.sin + ky * ldc + kx] : mk<C>((T)0, (T)0);
+  {
+    C v[16];
+#pragma unroll
+    for (int m = 0; m < 16; ++m) {
+      const int e = tid + m * nth;
+      const int ky = e / Cn, c = e - ky * Cn, kx = kx0 + c;
+      if (e < ny * Cn) v[m] = kx < a.ncols ? a.spec[jb.sin + ky * ldc + kx] : mk<C>((T)0, (T)0);
+    }
+#pragma unroll
+    for (int m = 0; m < 16; ++m) {
+      const int e = tid + m * nth;
+      const int ky = e / Cn, c = e - ky * Cn;
+      if (e < ny * Cn) buf[sp(ky * W + c)] = v[m];
+    }
   }
   __syncthreads();
   fft_smem<T, false, true>(buf, ny, a.log2ny, Cn, 1, W, a.tw, tid);
