@@ -171,6 +171,23 @@ mjx_status mjx_imex_adaptive2d(const void* plan, const mjx_grid2d* grid, int dty
                                void* hist_y, void* ws, size_t ws_bytes,
                                mjx_adaptive_result* result, void* stream);
 
+/* Workspace bytes of mjx_imex_adaptive2d_mixed. */
+size_t mjx_imex2d_mixed_ws_bytes(int ny, int nx, int nfields);
+
+/* Adaptive IMEX-Strang in the mixed FP32/FP64 form: the state is kept as its
+ * FP64 half spectrum, diffusion multipliers are applied in FP64, and only the
+ * reaction increments and the error estimate pass through FP32 transforms, so
+ * FP32 rounding scales with the increments instead of the state.  Same loop,
+ * controller and result semantics as mjx_imex_adaptive2d (adaptive_integrate_imex,
+ * moljax/core/stepping.py:1146-1371).  plan32/plan64: FD-symbol plans of the grid
+ * in FP32 and FP64.  io_dtype: dtype of y0 and y_final.  No y history. */
+mjx_status mjx_imex_adaptive2d_mixed(const void* plan32, const void* plan64, const mjx_grid2d* grid,
+                                     int io_dtype, const mjx_imex_problem* prob,
+                                     const mjx_pid_params* pid, double t0, double t_end, double dt0,
+                                     int max_steps, int save_every, const void* y0, void* y_final,
+                                     double* hist_t, double* hist_dt, void* ws, size_t ws_bytes,
+                                     mjx_adaptive_result* result, void* stream);
+
 /* Launches a single kernel of one fused adaptive attempt, for timing and
  * profiling: which = 0 seeds the workspace (both state buffers = y, step dt),
  * 1..7 launch the row/column passes K1..K7 (see csrc/imex.cu).  No reference

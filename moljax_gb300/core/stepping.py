@@ -121,13 +121,19 @@ def adaptive_integrate_imex(model, y0, t0, t_end, dt0, fft_cache=None, diffusivi
                             use_strang: bool = True, max_steps: int = 10000,
                             cfl_params: Optional[CFLParams] = None,
                             pid_params: Optional[PIDParams] = None, save_every: int = 1,
-                            save_y_history: bool = True, max_attempts: int = 0) -> AdaptiveResult:
+                            save_y_history: bool = True, max_attempts: int = 0,
+                            precision: Optional[str] = None) -> AdaptiveResult:
     """Adaptive IMEX with step doubling and PI control (stepping.py:1146-1371).
 
     Runs entirely on the GPU as one graph launch.  ``save_y_history=False``
     skips the (max_steps//save_every+1) x state history buffer; t/dt histories
     are always kept.  ``max_attempts`` caps accepted+rejected attempts
     (default 20*max_steps+1000) so the device loop always terminates.
+
+    ``precision``: ``"fp64"`` (FP64 everywhere; default for float64 models),
+    ``"fp32"`` (FP32 state and transforms) or ``"mixed"`` (FP64 spectral state,
+    FP32 transforms of the reaction increments; FP32 in/out; no y history).
+    float32 models default to ``"fp32"``.
     """
     if not use_strang:
         raise NotImplementedError("adaptive IMEX-Euler is not built; use_strang=True")
@@ -143,6 +149,15 @@ def adaptive_integrate_imex(model, y0, t0, t_end, dt0, fft_cache=None, diffusivi
     interior = stencil.unpad(stencil.stack(y0, names), grid)
     plan = _plan_of(fft_cache, grid.ny, grid.nx, interior.dtype)
     prob = _problem(model, diffusivities, cfl_params, max_attempts)
+    if precision is None:
+        precision = "fp64" if interior.dtype == torch.float64 else "fp32"
+    if precision == "mixed":
+        return _adaptive_mixed(model, interior, plan, prob, pid_params, t0, t_end, dt0, max_steps,
+                               save_every)
+    if precision not in ("fp32", "fp64"):
+        raise ValueError(f"precision must be 'fp32', 'fp64' or 'mixed', not {precision!r}")
+    if (precision == "fp64") != (interior.dtype == torch.float64):
+        raise TypeError(f"precision {precision!r} needs a {'float64' if precision == 'fp64' else 'float32'} state")
     pid = N.PIDParamsC(pid_params.safety, pid_params.kI, pid_params.kP, pid_params.dt_min,
                        pid_params.dt_max, pid_params.max_factor, pid_params.min_factor,
                        pid_params.atol, pid_params.rtol)
@@ -167,6 +182,37 @@ def adaptive_integrate_imex(model, y0, t0, t_end, dt0, fft_cache=None, diffusivi
     y_history = ({n: y_hist[:, i] for i, n in enumerate(names)} if y_hist is not None else None)
     return AdaptiveResult(res.t_final, y_fin, t_hist, y_history, dt_hist, res.n_saved,
                           res.n_accepted, res.n_rejected, res.status)
+
+
+def _adaptive_mixed(model, interior, plan, prob, pid_params, t0, t_end, dt0, max_steps,
+                    save_every) -> AdaptiveResult:
+    from moljax_gb300.core.fft_solvers import get_plan
+    grid = model.grid
+    names = model.field_names
+    p32 = get_plan(plan.ny, plan.nx, plan.dy, plan.dx, plan.symbol, torch.float32, plan.device)
+    p64 = get_plan(plan.ny, plan.nx, plan.dy, plan.dx, plan.symbol, torch.float64, plan.device)
+    pid = N.PIDParamsC(pid_params.safety, pid_params.kI, pid_params.kP, pid_params.dt_min,
+                       pid_params.dt_max, pid_params.max_factor, pid_params.min_factor,
+                       pid_params.atol, pid_params.rtol)
+    lib = N.lib()
+    dev = plan.device
+    max_saves = max_steps // save_every + 1
+    ws = workspace(lib.mjx_imex2d_mixed_ws_bytes(grid.ny, grid.nx, len(names)), dev, "imex_mixed")
+    y_final = torch.empty_like(interior)
+    t_hist = torch.empty(max_saves, dtype=torch.float64, device=dev)
+    dt_hist = torch.empty(max_saves, dtype=torch.float64, device=dev)
+    res = N.AdaptiveResultC()
+    N.check("mjx_imex_adaptive2d_mixed", lib.mjx_imex_adaptive2d_mixed(
+        N.ptr(p32.buf), N.ptr(p64.buf), C.byref(p32.cgrid), N.dtype_code(interior.dtype),
+        C.byref(prob), C.byref(pid), float(t0), float(t_end), float(dt0), int(max_steps),
+        int(save_every), N.ptr(interior), N.ptr(y_final),
+        C.cast(C.c_void_p(t_hist.data_ptr()), C.POINTER(C.c_double)),
+        C.cast(C.c_void_p(dt_hist.data_ptr()), C.POINTER(C.c_double)),
+        N.ptr(ws), ws.numel(), C.byref(res), N.stream_ptr(dev)))
+    padded = stencil.pad_interior(y_final, grid, model.bc_spec, names, res.t_final, model.params)
+    y_fin = {n: padded[i] for i, n in enumerate(names)}
+    return AdaptiveResult(res.t_final, y_fin, t_hist, None, dt_hist, res.n_saved, res.n_accepted,
+                          res.n_rejected, res.status)
 
 
 def adaptive_integrate(model, y0=None, t0: float = 0.0, t_end: Optional[float] = None,

@@ -27,7 +27,6 @@ namespace mjx {
 mjx_status ensure_kernel_attrs();
 mjx_status check_grid(const mjx_grid2d* g);
 int elem_size(int dtype);
-int col_tile(int ny, int ncols, int nout, int elem);
 
 struct ImexLayout {
   size_t y0, y1, yf, sa, sb, part, bad, st, total;
@@ -67,18 +66,7 @@ static ImexLayout imex_layout(int ny, int nx, int nf, int elem, int nrows, int n
 }
 
 // ------------------------------------------------------------------ controller
-struct CtlArgs {
-  DevState* st;
-  const double* partial;
-  const int* nonfinite;
-  int nparts;
-  double n_dof;
-  mjx_pid_params pid;
-  double* hist_t;
-  double* hist_dt;
-  cudaGraphConditionalHandle handle;
-  int use_handle;
-};
+
 
 // NaN-propagating min/max (jnp.minimum/maximum semantics).
 __device__ __forceinline__ double jmax(double a, double b) { return (a != a || b != b) ? (a + b) : (a > b ? a : b); }
@@ -171,6 +159,11 @@ __global__ void __launch_bounds__(256) controller_kernel(CtlArgs a) {
     else if (st->status == MJX_STATUS_RUNNING_CODE) st->status = MJX_STATUS_MAX_STEPS_CODE;
   }
   if (a.use_handle) cudaGraphSetConditional(a.handle, running ? 1u : 0u);
+}
+
+cudaError_t launch_controller(const CtlArgs& a, cudaStream_t s) {
+  controller_kernel<<<1, 256, 0, s>>>(a);
+  return cudaGetLastError();
 }
 
 // Copies the current state into the history slot chosen by the controller.

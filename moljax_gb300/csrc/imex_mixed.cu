@@ -1,0 +1,503 @@
+// Adaptive IMEX-Strang with an FP64 spectral state and FP32 transforms.
+//
+// The state is kept as its FP64 half spectrum Y^.  Diffusion half steps are
+// pointwise in spectral space and applied in FP64 as Y^ += Y^ * mu with
+// mu = m - 1 = x/(1 - x), x = h D lam (computed in FP32: mu is small wherever
+// Y^ carries energy, so its FP32 rounding stays far below the state's).  Only
+// the reaction increments Delta = R_heun(y*) - y* go through FP32 transforms:
+//   y*  = IFFT32(M(h/2) Y^)          (c2r in FP32)
+//   Y^' = M(h/2) (M(h/2) Y^ + FFT32(Delta(y*)))
+// so the FP32 rounding enters in proportion to |Delta|, not |y|.  The error
+// estimate y_half - y_full = IFFT32(Y^_half - Y^_full) is a transform of a small
+// FP64 difference.  Same step doubling / PI controller / accept-reject loop as
+// the FP32 path (csrc/imex.cu), six kernels per attempt:
+//
+//   C1 col  Y^[cur] -> PA = M(dt/2)Y^, PB = M(dt/4)Y^;  ZA = IFFT_y(PA), ZB = IFFT_y(PB)
+//   R1 row  ZA: c2r, Delta(dt), r2c;  ZB: c2r, Delta(dt/2), r2c
+//   C2 col  PA = M(dt/2)(PA + FFT_y ZA);  PB = M(dt/4)M(dt/4)(PB + FFT_y ZB);  ZB = IFFT_y(PB)
+//   R2 row  ZB: c2r, Delta(dt/2), r2c
+//   C3 col  Y^[1-cur] = M(dt/4)(PB + FFT_y ZB);  ZA = IFFT_y(Y^[1-cur] - PA), ZB = IFFT_y(Y^[1-cur])
+//   R3 row  c2r of (ZA, ZB) pairs -> scaled error partials
+#include <math.h>
+#include <string.h>
+
+#include "spectral.cuh"
+
+namespace mjx {
+
+mjx_status ensure_kernel_attrs();
+mjx_status check_grid(const mjx_grid2d* g);
+int elem_size(int dtype);
+void set_last_error(cudaError_t e, const char* file, int line);
+
+enum { MC_SPLIT = 0, MC_FULL_END = 1, MC_HALF_MID = 2, MC_HALF_END = 3 };
+
+struct MJob {
+  int type;
+  int pad;
+  long long off;  // field offset (complex elements) shared by every buffer
+  double D;
+};
+
+struct MColArgs {
+  int ny, log2ny, ncols, ldc, C, njobs;
+  double2* ys[2];
+  double2* pa;
+  double2* pb;
+  float2* za;
+  float2* zb;
+  const float* lamx;
+  const float* lamy;
+  const float2* tw;
+  float inv_norm;
+  double hfixed;
+  const DevState* st;
+  MJob job[8];
+};
+
+__device__ __forceinline__ double2 dmk(double x, double y) { double2 r; r.x = x; r.y = y; return r; }
+__device__ __forceinline__ float2 fmk(float x, float y) { float2 r; r.x = x; r.y = y; return r; }
+
+// X + X * mu, mu = x/(1-x), x = hD * lam (FP32, |1-x| clamped at 1e-14 like the reference)
+__device__ __forceinline__ double2 mstep(double2 X, float hD, float lam) {
+  const float x = hD * lam;
+  float den = 1.0f - x;
+  if (fabsf(den) < 1e-14f) den = 1e-14f;
+  const double mu = (double)(x / den);
+  return dmk(fma(X.x, mu, X.x), fma(X.y, mu, X.y));
+}
+
+__global__ void __launch_bounds__(512, 1) mcol_kernel(const __grid_constant__ MColArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2* buf = reinterpret_cast<float2*>(smem_raw);
+  const DevState* st = a.st;
+  if (st != nullptr && st->done) return;
+  const MJob jb = a.job[blockIdx.y];
+  const int Cn = a.C, W = 2 * Cn;
+  const int kx0 = blockIdx.x * Cn;
+  const int ny = a.ny, tid = threadIdx.x, nth = blockDim.x;
+  const long long ldc = a.ldc;
+  const int cur = st != nullptr ? st->cur : 0;
+  const double h = st != nullptr ? st->dtc : a.hfixed;
+  const float hA = (float)(0.5 * h * jb.D), hB = (float)(0.25 * h * jb.D);
+  const float nrm = a.inv_norm;
+
+  if (jb.type != MC_SPLIT) {
+    // load the FP32 increment tile and transform it forward along y
+    const float2* zin = jb.type == MC_FULL_END ? a.za : a.zb;
+    float2 v[16];
+#pragma unroll
+    for (int m = 0; m < 16; ++m) {
+      const int e = tid + m * nth;
+      const int ky = e / Cn, c = e - ky * Cn, kx = kx0 + c;
+      if (e < ny * Cn) v[m] = kx < a.ncols ? zin[jb.off + ky * ldc + kx] : fmk(0.f, 0.f);
+    }
+#pragma unroll
+    for (int m = 0; m < 16; ++m) {
+      const int e = tid + m * nth;
+      const int ky = e / Cn, c = e - ky * Cn;
+      if (e < ny * Cn) buf[sp(ky * W + c)] = v[m];
+    }
+    __syncthreads();
+    fft_smem<float, false, true>(buf, ny, a.log2ny, Cn, 1, W, a.tw, tid);
+  }
+
+  // FP64 combine, element by element
+  for (int e = tid; e < ny * Cn; e += nth) {
+    const int ky = e / Cn, c = e - ky * Cn, kx = kx0 + c;
+    if (kx >= a.ncols) {
+      buf[sp(ky * W + c)] = fmk(0.f, 0.f);
+      buf[sp(ky * W + Cn + c)] = fmk(0.f, 0.f);
+      continue;
+    }
+    const long long g = jb.off + ky * ldc + kx;
+    const float lam = a.lamx[kx] + a.lamy[ky];
+    if (jb.type == MC_SPLIT) {
+      const double2 Y = a.ys[cur][g];
+      const double2 PA = mstep(Y, hA, lam), PB = mstep(Y, hB, lam);
+      a.pa[g] = PA;
+      a.pb[g] = PB;
+      buf[sp(ky * W + c)] = fmk((float)(PA.x * nrm), (float)(PA.y * nrm));
+      buf[sp(ky * W + Cn + c)] = fmk((float)(PB.x * nrm), (float)(PB.y * nrm));
+    } else {
+      const float2 d = buf[sp(ky * W + c)];
+      if (jb.type == MC_FULL_END) {
+        const double2 P = a.pa[g];
+        a.pa[g] = mstep(dmk(P.x + (double)d.x, P.y + (double)d.y), hA, lam);
+      } else if (jb.type == MC_HALF_MID) {
+        const double2 P = a.pb[g];
+        const double2 X = mstep(mstep(dmk(P.x + (double)d.x, P.y + (double)d.y), hB, lam), hB, lam);
+        a.pb[g] = X;
+        buf[sp(ky * W + c)] = fmk((float)(X.x * nrm), (float)(X.y * nrm));
+      } else {  // MC_HALF_END
+        const double2 P = a.pb[g];
+        const double2 X = mstep(dmk(P.x + (double)d.x, P.y + (double)d.y), hB, lam);
+        a.ys[1 - cur][g] = X;
+        const double2 Fa = a.pa[g];
+        buf[sp(ky * W + c)] = fmk((float)((X.x - Fa.x) * nrm), (float)((X.y - Fa.y) * nrm));
+        buf[sp(ky * W + Cn + c)] = fmk((float)(X.x * nrm), (float)(X.y * nrm));
+      }
+    }
+  }
+  if (jb.type == MC_FULL_END) return;
+  __syncthreads();
+  const int nseq = (jb.type == MC_HALF_MID) ? Cn : W;
+  fft_smem<float, true, true>(buf, ny, a.log2ny, nseq, 1, W, a.tw, tid);
+  for (int e = tid; e < ny * nseq; e += nth) {
+    const int ky = e / nseq, col = e - ky * nseq;
+    const int half = col / Cn, c = col - half * Cn, kx = kx0 + c;
+    if (kx >= a.ncols) continue;
+    const long long g = jb.off + ky * ldc + kx;
+    const float2 v = buf[sp(ky * W + col)];
+    if (jb.type == MC_HALF_MID) a.zb[g] = v;
+    else if (half == 0) a.za[g] = v;
+    else a.zb[g] = v;
+  }
+}
+
+__global__ void f32_to_f64(const float* in, double* out, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    out[i] = (double)in[i];
+}
+__global__ void f64_to_f32(const double* in, float* out, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    out[i] = (float)in[i];
+}
+__global__ void select_state_kernel(const DevState* st, const double2* y0, const double2* y1, double2* out, long long n) {
+  const double2* src = st->cur == 0 ? y0 : y1;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    out[i] = src[i];
+}
+
+
+
+struct MixLayout {
+  size_t ys0, ys1, pa, pb, za, zb, part, bad, st, total;
+  int nparts;
+  long long fs;  // complex elements per field spectrum
+};
+
+static inline size_t al256m(size_t b) { return (b + 255) & ~size_t(255); }
+
+static MixLayout mix_layout(int ny, int nx, int nf, int nparts) {
+  MixLayout L;
+  L.fs = (long long)ny * spec_ldc(nx);
+  const size_t s64 = (size_t)nf * L.fs * 16, s32 = (size_t)nf * L.fs * 8;
+  size_t o = 0;
+  L.ys0 = o; o += al256m(s64);
+  L.ys1 = o; o += al256m(s64);
+  L.pa = o; o += al256m(s64);
+  L.pb = o; o += al256m(s64);
+  L.za = o; o += al256m(s32);
+  L.zb = o; o += al256m(s32);
+  L.nparts = nparts;
+  L.part = o; o += al256m(sizeof(double) * (size_t)nparts);
+  L.bad = o; o += al256m(sizeof(int) * (size_t)nparts);
+  L.st = o; o += al256m(sizeof(DevState));
+  L.total = o;
+  return L;
+}
+
+static int mix_nparts(int ny, int nx, int nf) { return row_ctas(nx, ny, nf); }
+
+struct MixAttempt {
+  MColArgs c1, c2, c3;
+  RowArgs<float> r1, r2, r3;
+  int rx;
+  size_t csmem;
+};
+
+static MixAttempt build_mix(const void* plan32, const mjx_grid2d* g, const mjx_imex_problem* pb,
+                            const mjx_pid_params* pid, char* ws, const MixLayout& L, DevState* st) {
+  MixAttempt A;
+  const int nf = pb->nfields, ldc = spec_ldc(g->nx);
+  const PlanView pv = plan_view(plan32, g->ny, g->nx, 4);
+  A.rx = pb->reaction == MJX_REACT_GRAY_SCOTT ? RX_GRAY_SCOTT : (pb->reaction == MJX_REACT_FISHER ? RX_FISHER : RX_NONE);
+  MColArgs c;
+  memset(&c, 0, sizeof(c));
+  c.ny = g->ny; c.log2ny = ilog2_exact(g->ny); c.ncols = g->nx / 2 + 1; c.ldc = ldc;
+  const int tps = g->ny >= 16 ? g->ny / 16 : 1;
+  int C = 256 / tps;
+  if (C < 1) C = 1;
+  if (C > 8) C = 8;
+  while (C > 1 && (2 * C * tps > 512 || (size_t)sp_size(g->ny * 2 * C) * 8 > 200 * 1024)) C >>= 1;
+  c.C = C;
+  c.ys[0] = (double2*)(ws + L.ys0); c.ys[1] = (double2*)(ws + L.ys1);
+  c.pa = (double2*)(ws + L.pa); c.pb = (double2*)(ws + L.pb);
+  c.za = (float2*)(ws + L.za); c.zb = (float2*)(ws + L.zb);
+  c.lamx = (const float*)pv.lamx; c.lamy = (const float*)pv.lamy; c.tw = (const float2*)pv.twy;
+  c.inv_norm = (float)(1.0 / ((double)g->nx * (double)g->ny));
+  c.st = st;
+  A.csmem = (size_t)sp_size(g->ny * 2 * C) * sizeof(float2);
+  A.c1 = c; A.c2 = c; A.c3 = c;
+  for (int f = 0; f < nf; ++f) {
+    const double D = pb->D[f] > 1e-14 ? pb->D[f] : 0.0;
+    MJob j;
+    memset(&j, 0, sizeof(j));
+    j.off = (long long)f * L.fs; j.D = D;
+    j.type = MC_SPLIT; A.c1.job[A.c1.njobs++] = j;
+    j.type = MC_FULL_END; A.c2.job[A.c2.njobs++] = j;
+    j.type = MC_HALF_MID; A.c2.job[A.c2.njobs++] = j;
+    j.type = MC_HALF_END; A.c3.job[A.c3.njobs++] = j;
+  }
+  // row passes over the FP32 row spectra ZA/ZB (contiguous: ZB = ZA + zoff)
+  const long long zoff = (long long)((L.zb - L.za) / sizeof(float2));
+  RowArgs<float> r;
+  memset(&r, 0, sizeof(r));
+  r.n = g->nx; r.log2n = ilog2_exact(g->nx); r.ldc = ldc; r.rstride = g->nx;
+  r.rin_sel = -1; r.rout_sel = -1;
+  r.spec = (cx<float>*)(ws + L.za); r.tw = (const cx<float>*)pv.twx; r.inv_scale = 1.0f;
+  r.F = pb->F; r.k = pb->k; r.r = pb->r; r.atol = pid->atol; r.rtol = pid->rtol;
+  r.partial = (double*)(ws + L.part); r.nonfinite = (int*)(ws + L.bad); r.st = st;
+  const long long fs = L.fs;
+  auto reaction_pairs = [&](RowArgs<float>& rr, int b0, int nb, const double* hf) {
+    const int fl = ROW_LOAD_SPEC | ROW_REACT | ROW_DELTA | ROW_STORE_SPEC;
+    int q = 0;
+    for (int b = b0; b < b0 + nb; ++b) {
+      const long long base = b == 0 ? 0 : zoff;
+      if (A.rx == RX_GRAY_SCOTT) {  // (u_y, v_y)
+        RowPair& p = rr.pr[q++];
+        p.sa = base; p.sb = base + fs; p.hfac = hf[b - b0]; p.flags = fl;
+      } else {                      // (f_y, f_{y+ny/2})
+        for (int f = 0; f < nf; ++f) {
+          RowPair& p = rr.pr[q++];
+          p.sa = base + f * fs; p.sb = p.sa + (long long)(g->ny / 2) * ldc; p.hfac = hf[b - b0]; p.flags = fl;
+        }
+      }
+    }
+    rr.npairs = q;
+    rr.nrows = A.rx == RX_GRAY_SCOTT ? g->ny : g->ny / 2;
+    rr.nseq = row_nseq(g->nx, rr.nrows);
+  };
+  const double h2[2] = {1.0, 0.5};
+  A.r1 = r; reaction_pairs(A.r1, 0, 2, h2);
+  const double hh[1] = {0.5};
+  A.r2 = r; reaction_pairs(A.r2, 1, 1, hh);
+  A.r3 = r;  // pairs (error row, solution row) of each field
+  for (int f = 0; f < nf; ++f) {
+    RowPair& p = A.r3.pr[f];
+    p.sa = f * fs; p.sb = zoff + f * fs; p.hfac = 0.0; p.flags = ROW_LOAD_SPEC | ROW_ERRPAIR;
+  }
+  A.r3.npairs = nf; A.r3.nrows = g->ny; A.r3.nseq = row_nseq(g->nx, g->ny);
+  return A;
+}
+
+static cudaError_t mcol(const MColArgs& c, size_t smem, cudaStream_t s) {
+  const int tps = c.ny >= 16 ? c.ny / 16 : 1;
+  dim3 grid((c.ncols + c.C - 1) / c.C, c.njobs);
+  mcol_kernel<<<grid, 2 * c.C * tps, smem, s>>>(c);
+  return cudaGetLastError();
+}
+
+static cudaError_t mrow(const RowArgs<float>& r, int rx, cudaStream_t s) {
+  return rx == RX_GRAY_SCOTT ? launch_row<float, RX_GRAY_SCOTT>(r, s)
+         : (rx == RX_FISHER ? launch_row<float, RX_FISHER>(r, s) : launch_row<float, RX_NONE>(r, s));
+}
+
+static cudaError_t launch_mix_attempt(const MixAttempt& A, cudaStream_t s) {
+  cudaError_t e;
+  if ((e = mcol(A.c1, A.csmem, s)) != cudaSuccess) return e;
+  if ((e = mrow(A.r1, A.rx, s)) != cudaSuccess) return e;
+  if ((e = mcol(A.c2, A.csmem, s)) != cudaSuccess) return e;
+  if ((e = mrow(A.r2, A.rx, s)) != cudaSuccess) return e;
+  if ((e = mcol(A.c3, A.csmem, s)) != cudaSuccess) return e;
+  return mrow(A.r3, RX_NONE, s);
+}
+
+// FP64 transform helpers for the initial and final conversions (split pairing, FP64 plan)
+static mjx_status to_spectrum64(const void* plan64, const mjx_grid2d* g, int nf, const double* real,
+                                double2* spec, cudaStream_t s) {
+  const PlanView pv = plan_view(plan64, g->ny, g->nx, 8);
+  const int ldc = spec_ldc(g->nx);
+  RowArgs<double> r;
+  memset(&r, 0, sizeof(r));
+  r.n = g->nx; r.log2n = ilog2_exact(g->nx); r.ldc = ldc; r.nrows = g->ny / 2; r.npairs = nf;
+  r.nseq = row_nseq(g->nx, r.nrows); r.rstride = g->nx; r.rin_sel = -1; r.rout_sel = -1;
+  r.rin[0] = real; r.spec = (cx<double>*)spec; r.tw = (const cx<double>*)pv.twx; r.inv_scale = 1.0;
+  for (int f = 0; f < nf; ++f) {
+    r.pr[f].ra = (long long)f * g->ny * g->nx; r.pr[f].rb = r.pr[f].ra + (long long)(g->ny / 2) * g->nx;
+    r.pr[f].sa = (long long)f * g->ny * ldc; r.pr[f].sb = r.pr[f].sa + (long long)(g->ny / 2) * ldc;
+    r.pr[f].flags = ROW_STORE_SPEC;
+  }
+  MJX_CUDA_TRY((launch_row<double, RX_NONE>(r, s)));
+  ColArgs<double> c;
+  memset(&c, 0, sizeof(c));
+  c.ny = g->ny; c.log2ny = ilog2_exact(g->ny); c.ncols = g->nx / 2 + 1; c.ldc = ldc;
+  c.C = col_tile(g->ny, c.ncols, 1, 8); c.spec = (cx<double>*)spec; c.lamx = (const double*)pv.lamx;
+  c.lamy = (const double*)pv.lamy; c.tw = (const cx<double>*)pv.twy; c.scale = 1.0; c.njobs = nf;
+  for (int f = 0; f < nf; ++f) {
+    ColJob& j = c.job[f];
+    j.sin = j.sout[0] = j.sout[1] = (long long)f * g->ny * ldc;
+    j.nout = 1; j.mul = MUL_SCALE; j.dirs = 1; j.scale = 1.0; j.pow[0] = j.pow[1] = 1;
+  }
+  MJX_CUDA_TRY(launch_col<double>(c, s));
+  return MJX_OK;
+}
+
+static mjx_status from_spectrum64(const void* plan64, const mjx_grid2d* g, int nf, double2* spec,
+                                  double* real, cudaStream_t s) {
+  const PlanView pv = plan_view(plan64, g->ny, g->nx, 8);
+  const int ldc = spec_ldc(g->nx);
+  ColArgs<double> c;
+  memset(&c, 0, sizeof(c));
+  c.ny = g->ny; c.log2ny = ilog2_exact(g->ny); c.ncols = g->nx / 2 + 1; c.ldc = ldc;
+  c.C = col_tile(g->ny, c.ncols, 1, 8); c.spec = (cx<double>*)spec; c.lamx = (const double*)pv.lamx;
+  c.lamy = (const double*)pv.lamy; c.tw = (const cx<double>*)pv.twy; c.njobs = nf;
+  for (int f = 0; f < nf; ++f) {
+    ColJob& j = c.job[f];
+    j.sin = j.sout[0] = j.sout[1] = (long long)f * g->ny * ldc;
+    j.nout = 1; j.mul = MUL_SCALE; j.dirs = 2; j.scale = 1.0 / ((double)g->nx * (double)g->ny);
+    j.pow[0] = j.pow[1] = 1;
+  }
+  MJX_CUDA_TRY(launch_col<double>(c, s));
+  RowArgs<double> r;
+  memset(&r, 0, sizeof(r));
+  r.n = g->nx; r.log2n = ilog2_exact(g->nx); r.ldc = ldc; r.nrows = g->ny / 2; r.npairs = nf;
+  r.nseq = row_nseq(g->nx, r.nrows); r.rstride = g->nx; r.rin_sel = -1; r.rout_sel = -1;
+  r.rout[0] = real; r.spec = (cx<double>*)spec; r.tw = (const cx<double>*)pv.twx; r.inv_scale = 1.0;
+  for (int f = 0; f < nf; ++f) {
+    r.pr[f].ra = (long long)f * g->ny * g->nx; r.pr[f].rb = r.pr[f].ra + (long long)(g->ny / 2) * g->nx;
+    r.pr[f].sa = (long long)f * g->ny * ldc; r.pr[f].sb = r.pr[f].sa + (long long)(g->ny / 2) * ldc;
+    r.pr[f].flags = ROW_LOAD_SPEC | ROW_STORE_REAL;
+  }
+  MJX_CUDA_TRY((launch_row<double, RX_NONE>(r, s)));
+  return MJX_OK;
+}
+
+mjx_status ensure_mix_attrs() {
+  static int done = 0;
+  if (done) return MJX_OK;
+  int dev = 0, optin = 0;
+  MJX_CUDA_TRY(cudaGetDevice(&dev));
+  MJX_CUDA_TRY(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  MJX_CUDA_TRY(cudaFuncSetAttribute(mcol_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
+  done = 1;
+  return MJX_OK;
+}
+
+}  // namespace mjx
+
+using namespace mjx;
+
+extern "C" {
+
+size_t mjx_imex2d_mixed_ws_bytes(int ny, int nx, int nfields) {
+  if (ilog2_exact(nx) < 1 || ilog2_exact(ny) < 1 || nfields < 1 || nfields > 4) return 0;
+  return mix_layout(ny, nx, nfields, mix_nparts(ny, nx, nfields)).total;
+}
+
+mjx_status mjx_imex_adaptive2d_mixed(const void* plan32, const void* plan64, const mjx_grid2d* g,
+                                     int io_dtype, const mjx_imex_problem* pb,
+                                     const mjx_pid_params* pid, double t0, double t_end, double dt0,
+                                     int max_steps, int save_every, const void* y0, void* y_final,
+                                     double* hist_t, double* hist_dt, void* ws, size_t ws_bytes,
+                                     mjx_adaptive_result* res, void* stream) {
+  MJX_TRY(check_grid(g));
+  if (pb == nullptr || pid == nullptr || plan32 == nullptr || plan64 == nullptr || !y0 || !y_final)
+    return MJX_BAD_ARG;
+  if (pb->nfields < 1 || pb->nfields > 4 || !pb->use_strang) return MJX_BAD_ARG;
+  if (pb->reaction == MJX_REACT_GRAY_SCOTT && pb->nfields != 2) return MJX_BAD_ARG;
+  if (max_steps < 0 || save_every < 1) return MJX_BAD_ARG;
+  const int e = elem_size(io_dtype);
+  if (!e) return MJX_BAD_DTYPE;
+  const int nf = pb->nfields;
+  const MixLayout L = mix_layout(g->ny, g->nx, nf, mix_nparts(g->ny, g->nx, nf));
+  if (ws == nullptr || ws_bytes < L.total) return MJX_WORKSPACE;
+  MJX_TRY(ensure_kernel_attrs());
+  MJX_TRY(ensure_mix_attrs());
+  cudaStream_t s = (cudaStream_t)stream;
+  char* w = (char*)ws;
+  DevState* st = (DevState*)(w + L.st);
+  const long long nelem = (long long)nf * g->ny * g->nx;
+  const int max_saves = max_steps / save_every + 1;
+
+  // initial spectral state in FP64 (real input staged in PA)
+  double* real64 = (double*)(w + L.pa);
+  if (e == 4) {
+    f32_to_f64<<<304, 256, 0, s>>>((const float*)y0, real64, nelem);
+    MJX_CUDA_TRY(cudaGetLastError());
+  } else {
+    MJX_CUDA_TRY(cudaMemcpyAsync(real64, y0, nelem * 8, cudaMemcpyDeviceToDevice, s));
+  }
+  MJX_TRY(to_spectrum64(plan64, g, nf, real64, (double2*)(w + L.ys0), s));
+
+  DevState h;
+  memset(&h, 0, sizeof(h));
+  const double dt_init = (dt0 < pb->dt_cfl || dt0 != dt0) ? dt0 : pb->dt_cfl;
+  h.t = t0; h.dt = dt_init; h.t_end = t_end; h.prev_err = 1.0; h.dt_cfl = pb->dt_cfl;
+  h.status = MJX_STATUS_RUNNING_CODE; h.write_idx = 1; h.finite = 1;
+  h.max_saves = max_saves; h.save_every = save_every; h.order = 2; h.save_slot = -1;
+  h.max_attempts = pb->max_attempts > 0 ? pb->max_attempts : 20 * max_steps + 1000;
+  const bool running = (t0 < t_end) && (1 < max_saves);
+  if (running) h.dtc = dt_init < t_end - t0 ? dt_init : t_end - t0;
+  else { h.done = 1; h.status = (t0 >= t_end) ? MJX_STATUS_SUCCESS_CODE : MJX_STATUS_MAX_STEPS_CODE; }
+  MJX_CUDA_TRY(cudaMemcpyAsync(st, &h, sizeof(h), cudaMemcpyHostToDevice, s));
+  if (hist_t) {
+    MJX_CUDA_TRY(cudaMemsetAsync(hist_t, 0, sizeof(double) * max_saves, s));
+    MJX_CUDA_TRY(cudaMemcpyAsync(hist_t, &t0, sizeof(double), cudaMemcpyHostToDevice, s));
+  }
+  if (hist_dt) MJX_CUDA_TRY(cudaMemsetAsync(hist_dt, 0, sizeof(double) * max_saves, s));
+  MJX_CUDA_TRY(cudaStreamSynchronize(s));
+
+  const MixAttempt A = build_mix(plan32, g, pb, pid, w, L, st);
+  CtlArgs ca;
+  memset(&ca, 0, sizeof(ca));
+  ca.st = st; ca.partial = (const double*)(w + L.part); ca.nonfinite = (const int*)(w + L.bad);
+  ca.nparts = L.nparts; ca.n_dof = (double)nelem; ca.pid = *pid; ca.hist_t = hist_t; ca.hist_dt = hist_dt;
+  if (running) {
+    cudaStream_t cs = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaError_t ce = cudaSuccess;
+    do {
+      if ((ce = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking)) != cudaSuccess) break;
+      if ((ce = cudaGraphCreate(&graph, 0)) != cudaSuccess) break;
+      cudaGraphConditionalHandle hdl;
+      if ((ce = cudaGraphConditionalHandleCreate(&hdl, graph, 1, cudaGraphCondAssignDefault)) != cudaSuccess) break;
+      cudaGraphNodeParams np = {cudaGraphNodeTypeConditional};
+      np.conditional.handle = hdl;
+      np.conditional.type = cudaGraphCondTypeWhile;
+      np.conditional.size = 1;
+      cudaGraphNode_t node;
+      if ((ce = cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, &np)) != cudaSuccess) break;
+      cudaGraph_t body = np.conditional.phGraph_out[0];
+      if ((ce = cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) break;
+      ca.handle = hdl; ca.use_handle = 1;
+      cudaError_t le = launch_mix_attempt(A, cs);
+      if (le == cudaSuccess) le = launch_controller(ca, cs);
+      cudaGraph_t captured = nullptr;
+      ce = cudaStreamEndCapture(cs, &captured);
+      if (le != cudaSuccess) { ce = le; break; }
+      if (ce != cudaSuccess) break;
+      if ((ce = cudaGraphInstantiate(&exec, graph, 0)) != cudaSuccess) break;
+      ce = cudaGraphLaunch(exec, s);
+    } while (0);
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    if (cs) cudaStreamDestroy(cs);
+    if (ce != cudaSuccess) { set_last_error(ce, __FILE__, __LINE__); return MJX_CUDA_ERROR; }
+  }
+  // final real state: select Y^[cur] into PB, inverse FP64 transform, write real into PA
+  double2* spec = (double2*)(w + L.pb);
+  select_state_kernel<<<304, 256, 0, s>>>(st, (const double2*)(w + L.ys0), (const double2*)(w + L.ys1), spec,
+                                          (long long)nf * L.fs);
+  MJX_CUDA_TRY(cudaGetLastError());
+  MJX_TRY(from_spectrum64(plan64, g, nf, spec, real64, s));
+  if (e == 4) {
+    f64_to_f32<<<304, 256, 0, s>>>(real64, (float*)y_final, nelem);
+    MJX_CUDA_TRY(cudaGetLastError());
+  } else {
+    MJX_CUDA_TRY(cudaMemcpyAsync(y_final, real64, nelem * 8, cudaMemcpyDeviceToDevice, s));
+  }
+  DevState out;
+  MJX_CUDA_TRY(cudaMemcpyAsync(&out, st, sizeof(out), cudaMemcpyDeviceToHost, s));
+  MJX_CUDA_TRY(cudaStreamSynchronize(s));
+  if (res) {
+    res->t_final = out.t; res->dt_next = out.dt; res->prev_err = out.prev_err; res->last_err = out.err_last;
+    res->n_accepted = out.n_acc; res->n_rejected = out.n_rej; res->n_attempts = out.attempts;
+    res->n_saved = out.write_idx; res->status = out.status; res->finite = out.finite;
+  }
+  return MJX_OK;
+}
+
+}  // extern "C"

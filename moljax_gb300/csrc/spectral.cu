@@ -69,6 +69,31 @@ __device__ __forceinline__ void react_heun(T& a, T& b, T h, T F, T k, T r) {
 
 template <typename T> __device__ __forceinline__ bool finite_(T v) { return isfinite(v); }
 
+// The Heun increment y** - y* computed without forming y** (no cancellation).
+template <typename T, int RX>
+__device__ __forceinline__ void react_delta(T& a, T& b, T h, T F, T k, T r) {
+  const T hh = (T)0.5 * h;
+  if (RX == RX_GRAY_SCOTT) {
+    const T uvv = a * b * b;
+    const T fu = -uvv + F * ((T)1 - a);
+    const T fv = uvv - (F + k) * b;
+    const T ua = a + h * fu, va = b + h * fv;
+    const T uvv2 = ua * va * va;
+    const T gu = -uvv2 + F * ((T)1 - ua);
+    const T gv = uvv2 - (F + k) * va;
+    a = hh * (fu + gu);
+    b = hh * (fv + gv);
+  } else if (RX == RX_FISHER) {
+    const T fa = r * a * ((T)1 - a), fb = r * b * ((T)1 - b);
+    const T ta = a + h * fa, tb = b + h * fb;
+    a = hh * (fa + r * ta * ((T)1 - ta));
+    b = hh * (fb + r * tb * ((T)1 - tb));
+  } else {
+    a = (T)0;
+    b = (T)0;
+  }
+}
+
 // ------------------------------------------------------------------ row pass
 template <typename T> struct Occ { static constexpr int row = sizeof(T) == 4 ? 4 : 2, col = sizeof(T) == 4 ? 2 : 1; };
 
@@ -157,13 +182,21 @@ __global__ void __launch_bounds__(256, Occ<T>::row) row_kernel(const __grid_cons
     if (x >= n) continue;
     const C v = Z(x);
     T va = v.x * sc, vb = v.y * sc;
-    if (flags & ROW_REACT) react_heun<T, RX>(va, vb, h, (T)a.F, (T)a.k, (T)a.r);
+    if (flags & ROW_REACT) {
+      if (flags & ROW_DELTA) react_delta<T, RX>(va, vb, h, (T)a.F, (T)a.k, (T)a.r);
+      else react_heun<T, RX>(va, vb, h, (T)a.F, (T)a.k, (T)a.r);
+    }
     if (flags & ROW_STORE_REAL) { oa[x] = va; ob[x] = vb; }
     if (flags & ROW_ERRNORM) {
       // moljax/core/state.py:335-339: (err / (atol + rtol |y_new|))^2
       const T da = (va - ra_[m]) / ((T)a.atol + (T)a.rtol * fabs(va));
       const T db = (vb - rb_[m]) / ((T)a.atol + (T)a.rtol * fabs(vb));
       esum += da * da + db * db;
+      bad |= !(finite_(va) && finite_(vb));
+    }
+    if (flags & ROW_ERRPAIR) {
+      const T da = va / ((T)a.atol + (T)a.rtol * fabs(vb));
+      esum += da * da;
       bad |= !(finite_(va) && finite_(vb));
     }
     Z(x) = mk<C>(va, vb);
@@ -186,7 +219,7 @@ __global__ void __launch_bounds__(256, Occ<T>::row) row_kernel(const __grid_cons
   }
 
   // 4. block reduction of the error partials (FP64 across threads)
-  if (flags & ROW_ERRNORM) {
+  if (flags & (ROW_ERRNORM | ROW_ERRPAIR)) {
     __shared__ double red[32];
     __shared__ int redbad[32];
     double v = (double)esum;
@@ -262,7 +295,9 @@ __global__ void __launch_bounds__(512, Occ<T>::col) col_kernel(const __grid_cons
     }
   }
   __syncthreads();
-  fft_smem<T, false, true>(buf, ny, a.log2ny, Cn, 1, W, a.tw, tid);
+  const int dirs = jb.dirs ? jb.dirs : 3;
+  if (dirs & 1) fft_smem<T, false, true>(buf, ny, a.log2ny, Cn, 1, W, a.tw, tid);
+  const T jscale = jb.scale != 0.0 ? (T)jb.scale : a.scale;
 
   const double h = a.st != nullptr ? a.st->dtc : a.hfixed;
   const T hD0 = (T)(h * jb.hfac[0] * jb.D), hD1 = (T)(h * jb.hfac[1] * jb.D);
@@ -270,11 +305,11 @@ __global__ void __launch_bounds__(512, Occ<T>::col) col_kernel(const __grid_cons
     const int ky = e / Cn, c = e - ky * Cn, kx = kx0 + c;
     const T lam = (kx < a.ncols ? a.lamx[kx] : (T)0) + a.lamy[ky];
     const C v = buf[sp(ky * W + c)];
-    buf[sp(ky * W + c)] = cscale(v, a.scale * multiplier<T>(jb.mul, hD0, lam, jb.pow[0]));
-    if (nout > 1) buf[sp(ky * W + Cn + c)] = cscale(v, a.scale * multiplier<T>(jb.mul, hD1, lam, jb.pow[1]));
+    buf[sp(ky * W + c)] = cscale(v, jscale * multiplier<T>(jb.mul, hD0, lam, jb.pow[0]));
+    if (nout > 1) buf[sp(ky * W + Cn + c)] = cscale(v, jscale * multiplier<T>(jb.mul, hD1, lam, jb.pow[1]));
   }
   __syncthreads();
-  fft_smem<T, true, true>(buf, ny, a.log2ny, W, 1, W, a.tw, tid);
+  if (dirs & 2) fft_smem<T, true, true>(buf, ny, a.log2ny, W, 1, W, a.tw, tid);
 
   for (int e = tid; e < ny * W; e += nth) {
     const int ky = e / W, col = e - ky * W;

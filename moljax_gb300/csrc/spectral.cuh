@@ -39,6 +39,8 @@ enum {
   ROW_REACT = 4,       // Heun reaction step of length hfac*dt on (a, b)
   ROW_STORE_SPEC = 8,  // r2c at the end and store the half spectrum
   ROW_ERRNORM = 16,    // accumulate the scaled error of (a, b) against eref
+  ROW_DELTA = 32,      // with ROW_REACT: keep only the reaction increment (new - old)
+  ROW_ERRPAIR = 64,    // accumulate (a / (atol + rtol |b|))^2: a = error row, b = solution row
 };
 
 // pointwise reaction kinds (compile-time)
@@ -81,6 +83,8 @@ struct ColJob {
   int pow[2];            // multiplier power (1 or 2)
   int nout;
   int mul;               // MUL_*
+  int dirs;              // bit 0: forward transform first, bit 1: inverse after (0 means both)
+  double scale;          // multiplier scale (0: use ColArgs::scale)
 };
 
 template <typename T> struct ColArgs {
@@ -107,6 +111,22 @@ template <typename T, int RX>
 cudaError_t launch_row(const RowArgs<T>& a, cudaStream_t s);
 template <typename T>
 cudaError_t launch_col(const ColArgs<T>& a, cudaStream_t s);
+
+// Arguments of the adaptive controller kernel (csrc/imex.cu).
+struct CtlArgs {
+  DevState* st;
+  const double* partial;
+  const int* nonfinite;
+  int nparts;
+  double n_dof;
+  mjx_pid_params pid;
+  double* hist_t;
+  double* hist_dt;
+  cudaGraphConditionalHandle handle;
+  int use_handle;
+};
+cudaError_t launch_controller(const CtlArgs& a, cudaStream_t s);
+int col_tile(int ny, int ncols, int nout, int elem);
 
 // Row-pass CTA geometry helpers (sequences per CTA and CTA count).
 int row_nseq(int n, int nrows);

@@ -98,3 +98,24 @@ def test_adaptive_max_steps(cuda):
     ro = OI.adaptive_integrate_imex(om, y0, 0.0, 100.0, 1.0, lam, od, max_steps=5)
     assert r.status == ro.status == M.StatusCode.MAX_STEPS_REACHED
     assert r.n_accepted == ro.n_accepted == 5
+
+
+@pytest.mark.parametrize("n", [32, 128])
+def test_adaptive_mixed_precision_vs_oracle(cuda, n):
+    # FP64 spectral state + FP32 increment transforms: FP64-level accuracy, same step counts
+    M, grid, model, cache, diff, ym, og, y0, om, lam, od = _setup(n, torch.float32, cuda)
+    pid = M.PIDParams(atol=1e-7, rtol=1e-5)
+    r = M.adaptive_integrate_imex(model, ym, 0.0, 30.0, 1.0, cache, diff, pid_params=pid,
+                                  save_every=100, precision="mixed")
+    ro = OI.adaptive_integrate_imex(om, y0, 0.0, 30.0, 1.0, lam, od,
+                                    pid=OI.PIDParams(atol=1e-7, rtol=1e-5), save_every=100,
+                                    keep_history=False)
+    assert r.status == ro.status == 0
+    assert (r.n_accepted, r.n_rejected) == (ro.n_accepted, ro.n_rejected)
+    for k in ("u", "v"):
+        assert _rel(r.y_final[k].cpu().numpy(), ro.y_final[k]) < 1e-6
+    rf = M.adaptive_integrate_imex(model, ym, 0.0, 30.0, 1.0, cache, diff, pid_params=pid,
+                                   save_every=100, save_y_history=False, precision="fp32")
+    e_mixed = max(_rel(r.y_final[k].cpu().numpy(), ro.y_final[k]) for k in ("u", "v"))
+    e_fp32 = max(_rel(rf.y_final[k].cpu().numpy(), ro.y_final[k]) for k in ("u", "v"))
+    assert e_mixed < e_fp32
