@@ -145,8 +145,56 @@ def kernel_bytes(n, elem):
     }
 
 
+def kernel_bytes_mixed(n):
+    """Algorithmic bytes of the six passes of one mixed-precision attempt (2 fields).
+
+    Per field and half-spectrum element: FP64 state/scratch 16 B, FP32 row spectra 8 B.
+    """
+    nc = n * (n // 2 + 1)
+    f = 2
+    return {"C1 col split": f * nc * 64, "R1 row delta x2": f * nc * 32,
+            "C2 col combine": f * nc * 88, "R2 row delta": f * nc * 16,
+            "C3 col end+err": f * nc * 72, "R3 row err": f * nc * 16}
+
+
+def time_kernels_mixed(M, model, cache, diff, y0, dev, reps=30):
+    """CUDA-event time of each mixed-precision attempt kernel on the launching stream."""
+    import torch
+    from moljax_gb300 import _native as N
+    from moljax_gb300.core import stencil
+    from moljax_gb300.core.fft_solvers import workspace, get_plan
+    from moljax_gb300.core.stepping import _problem
+    grid = model.grid
+    interior = stencil.unpad(stencil.stack(y0, model.field_names), grid)
+    p32 = get_plan(grid.ny, grid.nx, grid.dy, grid.dx, "fd", torch.float32, dev)
+    p64 = get_plan(grid.ny, grid.nx, grid.dy, grid.dx, "fd", torch.float64, dev)
+    prob = _problem(model, diff, M.CFLParams())
+    pid = N.PIDParamsC(0.9, 0.7, 0.4, 1e-12, 1.0, 5.0, 0.2, ATOL, RTOL)
+    lib = N.lib()
+    ws = workspace(lib.mjx_imex2d_mixed_ws_bytes(grid.ny, grid.nx, 2), dev, "imex_mixed")
+    stream = N.stream_ptr(dev)
+    call = lambda w: N.check("mjx_imex_mixed_attempt_kernel2d", lib.mjx_imex_mixed_attempt_kernel2d(  # noqa
+        N.ptr(p32.buf), N.ptr(p64.buf), C.byref(p32.cgrid), C.byref(prob), C.byref(pid), w, 0.9,
+        N.ptr(interior), N.ptr(ws), ws.numel(), stream))
+    call(0)
+    names = list(kernel_bytes_mixed(grid.nx).keys())
+    out = {}
+    s = torch.cuda.current_stream(dev)
+    for w in range(1, 7):
+        for _ in range(3):
+            call(w)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        for _ in range(reps):
+            call(w)
+        e1.record(s)
+        e1.synchronize()
+        out[names[w - 1]] = e0.elapsed_time(e1) / reps * 1e-3
+    return out
+
+
 def time_kernels(M, model, cache, diff, y0, dev, reps=30):
-    """CUDA-event time of each attempt kernel on the launching stream."""
+    """CUDA-event time of each FP32 attempt kernel on the launching stream."""
     import torch
     from moljax_gb300 import _native as N
     from moljax_gb300.core import stencil
@@ -287,8 +335,12 @@ def run_ours(args, rank, world, local):
                      "ms_per_solve": tq * 1e3, "rel_l2_vs_fp64": (nq / den) ** 0.5,
                      "n_accepted": rq.n_accepted, "n_rejected": rq.n_rejected}
         # live per-kernel timing for the roofline of the dominant kernel
-        ktimes = time_kernels(M, model, cache, diff, y0, dev)
-        kb = kernel_bytes(grid.nx, 4)
+        if P == "mixed":
+            ktimes = time_kernels_mixed(M, model, cache, diff, y0, dev)
+            kb = kernel_bytes_mixed(grid.nx)
+        else:
+            ktimes = time_kernels(M, model, cache, diff, y0, dev)
+            kb = kernel_bytes(grid.nx, 4)
         dom = max(ktimes, key=lambda k: ktimes[k])
         peak, peak_kind = peaks()
         achieved = kb[dom] / ktimes[dom] / 1e9
@@ -319,7 +371,7 @@ def run_ours(args, rank, world, local):
                          "peak_kind": f"of {peak_kind}", "unit": "GB/s", "frac": achieved / peak,
                          "traffic": traffic, "alg_bytes": kb[dom],
                          "kernel_us": {k: v * 1e6 for k, v in ktimes.items()}},
-            "gpu_launches": args.steps * 0 + attempts * 8 + args.steps * 3,
+            "gpu_launches": attempts * (7 if P == "mixed" else 8) + args.steps * (9 if P == "mixed" else 3),
             "clocks": clk,
             "wall_s": wall,
         }

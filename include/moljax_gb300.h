@@ -188,6 +188,14 @@ mjx_status mjx_imex_adaptive2d_mixed(const void* plan32, const void* plan64, con
                                      double* hist_t, double* hist_dt, void* ws, size_t ws_bytes,
                                      mjx_adaptive_result* result, void* stream);
 
+/* Launches a single kernel of one mixed-precision attempt (timing/profiling):
+ * which = 0 seeds the workspace from the FP32 state y with step dt; 1..6 launch
+ * C1, R1, C2, R2, C3, R3 (see csrc/imex_mixed.cu).  No reference counterpart. */
+mjx_status mjx_imex_mixed_attempt_kernel2d(const void* plan32, const void* plan64,
+                                           const mjx_grid2d* grid, const mjx_imex_problem* prob,
+                                           const mjx_pid_params* pid, int which, double dt,
+                                           const void* y, void* ws, size_t ws_bytes, void* stream);
+
 /* Launches a single kernel of one fused adaptive attempt, for timing and
  * profiling: which = 0 seeds the workspace (both state buffers = y, step dt),
  * 1..7 launch the row/column passes K1..K7 (see csrc/imex.cu).  No reference

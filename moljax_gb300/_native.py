@@ -81,6 +81,8 @@ SIGNATURES = {
                                        C.POINTER(PIDParamsC), _d, _d, _d, _i, _i, _vp, _vp,
                                        C.POINTER(C.c_double), C.POINTER(C.c_double), _vp, _sz,
                                        C.POINTER(AdaptiveResultC), _vp]),
+    "mjx_imex_mixed_attempt_kernel2d": (_i, [_vp, _vp, C.POINTER(Grid2DC), C.POINTER(ImexProblemC),
+                                             C.POINTER(PIDParamsC), _i, _d, _vp, _vp, _sz, _vp]),
     "mjx_imex_attempt_kernel2d": (_i, [_vp, C.POINTER(Grid2DC), _i, C.POINTER(ImexProblemC),
                                        C.POINTER(PIDParamsC), _i, _d, _vp, _vp, _sz, _vp]),
 }

@@ -381,6 +381,51 @@ using namespace mjx;
 
 extern "C" {
 
+mjx_status mjx_imex_mixed_attempt_kernel2d(const void* plan32, const void* plan64,
+                                           const mjx_grid2d* g, const mjx_imex_problem* pb,
+                                           const mjx_pid_params* pid, int which, double dt,
+                                           const void* y, void* ws, size_t ws_bytes, void* stream) {
+  MJX_TRY(check_grid(g));
+  if (pb == nullptr || pid == nullptr || plan32 == nullptr || plan64 == nullptr) return MJX_BAD_ARG;
+  if (pb->nfields < 1 || pb->nfields > 4) return MJX_BAD_ARG;
+  const int nf = pb->nfields;
+  const MixLayout L = mix_layout(g->ny, g->nx, nf, mix_nparts(g->ny, g->nx, nf));
+  if (ws == nullptr || ws_bytes < L.total) return MJX_WORKSPACE;
+  MJX_TRY(ensure_kernel_attrs());
+  MJX_TRY(ensure_mix_attrs());
+  cudaStream_t s = (cudaStream_t)stream;
+  char* w = (char*)ws;
+  DevState* st = (DevState*)(w + L.st);
+  if (which == 0) {  // seed: FP32 y -> FP64 spectral state, step dt
+    if (y == nullptr) return MJX_BAD_ARG;
+    const long long nelem = (long long)nf * g->ny * g->nx;
+    double* real64 = (double*)(w + L.pa);
+    f32_to_f64<<<304, 256, 0, s>>>((const float*)y, real64, nelem);
+    MJX_CUDA_TRY(cudaGetLastError());
+    MJX_TRY(to_spectrum64(plan64, g, nf, real64, (double2*)(w + L.ys0), s));
+    MJX_CUDA_TRY(cudaMemcpyAsync(w + L.ys1, w + L.ys0, (size_t)nf * L.fs * 16, cudaMemcpyDeviceToDevice, s));
+    DevState h;
+    memset(&h, 0, sizeof(h));
+    h.dt = dt; h.dtc = dt; h.t_end = 1e300; h.prev_err = 1.0; h.status = MJX_STATUS_RUNNING_CODE;
+    h.order = 2; h.save_slot = -1; h.max_saves = 1 << 30; h.save_every = 1 << 30; h.max_attempts = 1 << 30;
+    MJX_CUDA_TRY(cudaMemcpyAsync(st, &h, sizeof(h), cudaMemcpyHostToDevice, s));
+    MJX_CUDA_TRY(cudaStreamSynchronize(s));
+    return MJX_OK;
+  }
+  const MixAttempt A = build_mix(plan32, g, pb, pid, w, L, st);
+  cudaError_t e;
+  switch (which) {
+    case 1: e = mcol(A.c1, A.csmem, s); break;
+    case 2: e = mrow(A.r1, A.rx, s); break;
+    case 3: e = mcol(A.c2, A.csmem, s); break;
+    case 4: e = mrow(A.r2, A.rx, s); break;
+    case 5: e = mcol(A.c3, A.csmem, s); break;
+    case 6: e = mrow(A.r3, RX_NONE, s); break;
+    default: return MJX_BAD_ARG;
+  }
+  return cuda_status(e);
+}
+
 size_t mjx_imex2d_mixed_ws_bytes(int ny, int nx, int nfields) {
   if (ilog2_exact(nx) < 1 || ilog2_exact(ny) < 1 || nfields < 1 || nfields > 4) return 0;
   return mix_layout(ny, nx, nfields, mix_nparts(ny, nx, nfields)).total;
