@@ -171,6 +171,29 @@ mjx_status mjx_imex_adaptive2d(const void* plan, const mjx_grid2d* grid, int dty
                                void* hist_y, void* ws, size_t ws_bytes,
                                mjx_adaptive_result* result, void* stream);
 
+/* ---- ETDRK4 (Cox-Matthews) for coupled Gray-Scott ------------------------------ */
+/* Workspace: row spectra ZU/ZN/ZX, 2D spectra U^/N^u/a^/S and the coefficient tables. */
+size_t mjx_etdrk4_ws_bytes(int ny, int nx, int dtype);
+
+/* n_steps fixed ETDRK4 steps of the coupled Gray-Scott system (fields u then v,
+ * interior [2][ny][nx]); restates benchmarks/benchmark_gray_scott.py:336-417.
+ * The coefficient tables E, E2, Q, f1, f2, f3 are evaluated on the GPU in FP64
+ * by the 32-point contour mean (336-356) when recompute_coeffs != 0 and kept in
+ * the workspace (pass 0 to reuse them for the same grid, D, dt and symbol).
+ * symbol: mjx_symbol (FD as DiffusionOperator, or pseudo-spectral as the benchmark).
+ * f2_factor: 2 = Cox-Matthews ETDRK4 (as fft_integrators.py:110, b2 = 2 phi2 - 4 phi3);
+ * 1 = the benchmark script's update, which omits that factor (benchmark_gray_scott.py:415).
+ * Also backs fft_integrators.etdrk4_step (moljax/core/fft_integrators.py:252-341). */
+mjx_status mjx_etdrk4_gray_scott2d(const void* plan, const mjx_grid2d* grid, int dtype, int symbol,
+                                   const double* D, double F, double k, double dt, double f2_factor,
+                                   int n_steps,
+                                   const void* y_in, void* y_out, void* ws, size_t ws_bytes,
+                                   int recompute_coeffs, void* stream);
+/* Launches one kernel of an ETDRK4 step for timing/profiling (which = 1..8:
+ * C1, R1, C2, R2, C3, R3, C4, R4).  No reference counterpart. */
+mjx_status mjx_etdrk4_kernel2d(const void* plan, const mjx_grid2d* grid, int dtype, double F,
+                               double k, int which, void* ws, size_t ws_bytes, void* stream);
+
 /* Workspace bytes of mjx_imex_adaptive2d_mixed. */
 size_t mjx_imex2d_mixed_ws_bytes(int ny, int nx, int nfields);
 

@@ -76,6 +76,10 @@ SIGNATURES = {
                                  C.POINTER(PIDParamsC), _d, _d, _d, _i, _i, _vp, _vp,
                                  C.POINTER(C.c_double), C.POINTER(C.c_double), _vp, _vp, _sz,
                                  C.POINTER(AdaptiveResultC), _vp]),
+    "mjx_etdrk4_ws_bytes": (_sz, [_i, _i, _i]),
+    "mjx_etdrk4_gray_scott2d": (_i, [_vp, C.POINTER(Grid2DC), _i, _i, C.POINTER(C.c_double), _d, _d,
+                                     _d, _d, _i, _vp, _vp, _vp, _sz, _i, _vp]),
+    "mjx_etdrk4_kernel2d": (_i, [_vp, C.POINTER(Grid2DC), _i, _d, _d, _i, _vp, _sz, _vp]),
     "mjx_imex2d_mixed_ws_bytes": (_sz, [_i, _i, _i]),
     "mjx_imex_adaptive2d_mixed": (_i, [_vp, _vp, C.POINTER(Grid2DC), _i, C.POINTER(ImexProblemC),
                                        C.POINTER(PIDParamsC), _d, _d, _d, _i, _i, _vp, _vp,

@@ -14,3 +14,6 @@ from moljax_gb300.core.fft_solvers import (create_fft_cache, solve_helmholtz_2d,
                                            apply_diffusion_inverse_fft, fft_cn_step,
                                            laplacian_symbol_2d)
 from moljax_gb300.core.utils import StatusCode
+from moljax_gb300.core import fft_integrators, fft_operators
+from moljax_gb300.core.fft_integrators import etdrk4_gray_scott, etdrk4_step, etd_integrate
+from moljax_gb300.core.fft_operators import DiffusionOperator

@@ -244,6 +244,13 @@ def adaptive_integrate(model, y0=None, t0: float = 0.0, t_end: Optional[float] =
         if y0 is None:
             raise TypeError("adaptive_integrate needs an initial state y0")
     method = IntegratorType(int(method))
+    if method == IntegratorType.ETDRK4:
+        # the reference has no adaptive ETDRK4: fixed steps of dt0 over the span
+        from moljax_gb300.core.fft_integrators import etd_integrate
+        y, tf = etd_integrate(model, y0, t0, t_end, dt0, kw.pop("symbol", "fd"))
+        n = int(round((tf - t0) / dt0))
+        return AdaptiveResult(tf, y, torch.tensor([t0, tf], dtype=torch.float64), None,
+                              torch.tensor([dt0], dtype=torch.float64), 2, n, 0, 0)
     if method == IntegratorType.IMEX_STRANG:
         return adaptive_integrate_imex(model, y0, t0, t_end, dt0, None, None, True, max_steps,
                                        cfl_params, pid_params, save_every, **kw)

@@ -1,0 +1,376 @@
+// ETDRK4 (Cox-Matthews) for coupled Gray-Scott on a periodic box.
+//
+// Restates benchmarks/benchmark_gray_scott.py:336-417.  Coefficients E, E2,
+// Q, f1, f2, f3 per Fourier mode come from the M = 32 point contour mean
+// (compute_etdrk4_coeffs, 336-356), evaluated once on the GPU in FP64 (the
+// contour sums cancel catastrophically in FP32) and stored in the state
+// precision.  One step (etdrk4_step, 369-417) is 4 column passes that fuse
+// forward FFT_y -> stage combination -> inverse FFT_y, and 4 row passes that
+// fuse c2r -> N(u, v) -> r2c:
+//
+//   C1  U^ = F(ZU), N^u = F(ZN); a^ = E2 U^ + Q N^u; store U^, N^u, a^; ZX = F^-1 a^
+//   R1  ZX <- r2c N(c2r ZX)                                   (N^a in row space)
+//   C2  N^a = F(ZX); b^ = E2 U^ + Q N^a; S = N^a; ZX = F^-1 b^
+//   R2  ZX <- r2c N(c2r ZX)
+//   C3  N^b = F(ZX); c^ = E2 a^ + Q (2 N^b - N^u); S += N^b; ZX = F^-1 c^
+//   R3  ZX <- r2c N(c2r ZX)
+//   C4  N^c = F(ZX); U^' = E U^ + f1 N^u + f2 S + f3 N^c; ZU = F^-1 U^'
+//   R4  ZN <- r2c N(c2r ZU)                                   (next step's N^u)
+//
+// ZU/ZN/ZX are row spectra (FFT along x only); U^, N^u, a^, S full 2D spectra.
+// f2 is stored pre-multiplied by f2_factor: 2 gives Cox-Matthews / Kassam-
+// Trefethen ETDRK4 (the library's b2 = 2 phi2 - 4 phi3, fft_integrators.py:110);
+// 1 reproduces the benchmark script, whose update uses f2 (N^a + N^b) without
+// the factor 2 (benchmark_gray_scott.py:415).
+#include <math.h>
+#include <string.h>
+
+#include "spectral.cuh"
+
+namespace mjx {
+
+mjx_status ensure_kernel_attrs();
+mjx_status check_grid(const mjx_grid2d* g);
+int elem_size(int dtype);
+void set_last_error(cudaError_t e, const char* file, int line);
+
+// ------------------------------------------------------------------ FP64 contour coefficients
+struct zc { double x, y; };
+__device__ __forceinline__ zc zadd(zc a, zc b) { return {a.x + b.x, a.y + b.y}; }
+__device__ __forceinline__ zc zsub(zc a, zc b) { return {a.x - b.x, a.y - b.y}; }
+__device__ __forceinline__ zc zmul(zc a, zc b) { return {a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x}; }
+__device__ __forceinline__ zc zsc(zc a, double s) { return {a.x * s, a.y * s}; }
+__device__ __forceinline__ zc zdiv(zc a, zc b) {
+  const double d = b.x * b.x + b.y * b.y;
+  return {(a.x * b.x + a.y * b.y) / d, (a.y * b.x - a.x * b.y) / d};
+}
+__device__ __forceinline__ zc zexp(zc a) {
+  double s, c;
+  sincos(a.y, &s, &c);
+  const double e = exp(a.x);
+  return {e * c, e * s};
+}
+
+// tab layout: [field][coef 0..5][ky][ldc] with coef = E, E2, Q, f1, f2, f3
+template <typename T>
+__global__ void etd_coeff_kernel(T* tab, int ny, int nx, int ldc, int symbol, double dy, double dx,
+                                 double D0, double D1, double dt, int M, double f2_factor) {
+  const long long per = (long long)ny * ldc;
+  const int nf = 2;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < per * nf;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int f = (int)(i / per);
+    const long long r = i - f * per;
+    const int ky = (int)(r / ldc), kx = (int)(r - (long long)ky * ldc);
+    const int my = ky < ny / 2 ? ky : ky - ny;
+    double lam;
+    if (kx > nx / 2) {
+      lam = 0.0;
+    } else if (symbol == MJX_SYMBOL_FD) {
+      lam = (2.0 * cospi(2.0 * kx / nx) - 2.0) / (dx * dx) + (2.0 * cospi(2.0 * my / ny) - 2.0) / (dy * dy);
+    } else {
+      const double kxx = 6.283185307179586476925 * kx / (nx * dx), kyy = 6.283185307179586476925 * my / (ny * dy);
+      lam = -(kxx * kxx + kyy * kyy);
+    }
+    const double z = dt * (f == 0 ? D0 : D1) * lam;
+    zc Q = {0, 0}, f1 = {0, 0}, f2 = {0, 0}, f3 = {0, 0};
+    for (int j = 1; j <= M; ++j) {
+      double s, c;
+      sincospi((j - 0.5) / M, &s, &c);
+      const zc LR = {z + c, s};
+      const zc eLR = zexp(LR), eLR2 = zexp(zsc(LR, 0.5));
+      const zc LR2 = zmul(LR, LR), LR3 = zmul(LR2, LR);
+      Q = zadd(Q, zdiv(zsub(eLR2, {1, 0}), LR));
+      // (-4 - LR + e^LR (4 - 3 LR + LR^2)) / LR^3
+      f1 = zadd(f1, zdiv(zadd(zsub({-4, 0}, LR), zmul(eLR, zadd(zsub({4, 0}, zsc(LR, 3)), LR2))), LR3));
+      // (2 + LR + e^LR (-2 + LR)) / LR^3
+      f2 = zadd(f2, zdiv(zadd(zadd({2, 0}, LR), zmul(eLR, zadd({-2, 0}, LR))), LR3));
+      // (-4 - 3 LR - LR^2 + e^LR (4 - LR)) / LR^3
+      f3 = zadd(f3, zdiv(zadd(zsub(zsub({-4, 0}, zsc(LR, 3)), LR2), zmul(eLR, zsub({4, 0}, LR))), LR3));
+    }
+    const double w = dt / M;
+    T* t = tab + (long long)f * 6 * per + r;
+    t[0 * per] = (T)exp(z);
+    t[1 * per] = (T)exp(0.5 * z);
+    t[2 * per] = (T)(w * Q.x);
+    t[3 * per] = (T)(w * f1.x);
+    t[4 * per] = (T)(f2_factor * w * f2.x);
+    t[5 * per] = (T)(w * f3.x);
+  }
+}
+
+// ------------------------------------------------------------------ stage column pass
+enum { E1 = 1, E2S = 2, E3 = 3, E4 = 4 };
+
+template <typename T> struct EArgs {
+  int ny, log2ny, ncols, ldc, C, njobs;
+  cx<T>* zu; cx<T>* zn; cx<T>* zx;
+  cx<T>* uh; cx<T>* nu; cx<T>* ah; cx<T>* ss;
+  const T* tab;
+  long long fs;  // elements per field in every buffer (ny * ldc)
+  const cx<T>* tw;
+  T scale;
+  int type;
+  int pad;
+};
+
+template <typename T> struct EOcc { static constexpr int v = sizeof(T) == 4 ? 2 : 1; };
+
+template <typename T>
+__global__ void __launch_bounds__(512, EOcc<T>::v) etd_col_kernel(const __grid_constant__ EArgs<T> a) {
+  typedef cx<T> Cx;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  Cx* buf = reinterpret_cast<Cx*>(smem_raw);
+  const int f = blockIdx.y;
+  const int Cn = a.C, W = 2 * Cn;
+  const int kx0 = blockIdx.x * Cn;
+  const int ny = a.ny, tid = threadIdx.x, nth = blockDim.x;
+  const long long ldc = a.ldc, fo = (long long)f * a.fs, per = a.fs;
+  const T* tab = a.tab + (long long)f * 6 * per;
+  const int type = a.type;
+
+  // load one (or, for E1, two) row-spectrum tiles
+  const Cx* in0 = type == E1 ? a.zu : a.zx;
+  const int nin = type == E1 ? 2 : 1;
+  for (int e = tid; e < ny * Cn * nin; e += nth) {
+    const int which = e / (ny * Cn), r = e - which * ny * Cn;
+    const int ky = r / Cn, c = r - ky * Cn, kx = kx0 + c;
+    const Cx* src = which == 0 ? in0 : a.zn;
+    buf[sp(ky * W + which * Cn + c)] = kx < a.ncols ? src[fo + ky * ldc + kx] : mk<Cx>((T)0, (T)0);
+  }
+  __syncthreads();
+  fft_smem<T, false, true>(buf, ny, a.log2ny, Cn * nin, 1, W, a.tw, tid);
+
+  for (int e = tid; e < ny * Cn; e += nth) {
+    const int ky = e / Cn, c = e - ky * Cn, kx = kx0 + c;
+    if (kx >= a.ncols) { buf[sp(ky * W + c)] = mk<Cx>((T)0, (T)0); continue; }
+    const long long g = fo + ky * ldc + kx, tg = ky * ldc + kx;
+    const Cx x = buf[sp(ky * W + c)];
+    Cx out;
+    if (type == E1) {
+      const Cx n = buf[sp(ky * W + Cn + c)];
+      const T e2 = tab[1 * per + tg], q = tab[2 * per + tg];
+      a.uh[g] = x;
+      a.nu[g] = n;
+      out = mk<Cx>(e2 * x.x + q * n.x, e2 * x.y + q * n.y);
+      a.ah[g] = out;
+    } else if (type == E2S) {
+      const T e2 = tab[1 * per + tg], q = tab[2 * per + tg];
+      const Cx u = a.uh[g];
+      a.ss[g] = x;
+      out = mk<Cx>(e2 * u.x + q * x.x, e2 * u.y + q * x.y);
+    } else if (type == E3) {
+      const T e2 = tab[1 * per + tg], q = tab[2 * per + tg];
+      const Cx ah = a.ah[g], nu = a.nu[g], s = a.ss[g];
+      a.ss[g] = cadd(s, x);
+      out = mk<Cx>(e2 * ah.x + q * ((T)2 * x.x - nu.x), e2 * ah.y + q * ((T)2 * x.y - nu.y));
+    } else {
+      const T E = tab[0 * per + tg], f1 = tab[3 * per + tg], f2 = tab[4 * per + tg], f3 = tab[5 * per + tg];
+      const Cx u = a.uh[g], nu = a.nu[g], s = a.ss[g];
+      out = mk<Cx>(E * u.x + f1 * nu.x + f2 * s.x + f3 * x.x, E * u.y + f1 * nu.y + f2 * s.y + f3 * x.y);
+    }
+    buf[sp(ky * W + c)] = cscale(out, a.scale);
+  }
+  __syncthreads();
+  fft_smem<T, true, true>(buf, ny, a.log2ny, Cn, 1, W, a.tw, tid);
+  Cx* dst = type == E4 ? a.zu : a.zx;
+  for (int e = tid; e < ny * Cn; e += nth) {
+    const int ky = e / Cn, c = e - ky * Cn, kx = kx0 + c;
+    if (kx < a.ncols) dst[fo + ky * ldc + kx] = buf[sp(ky * W + c)];
+  }
+}
+
+// ------------------------------------------------------------------ driver
+struct EtdLayout {
+  size_t zu, zn, zx, uh, nu, ah, ss, tab, total;
+  long long fs;
+};
+
+static inline size_t al(size_t b) { return (b + 255) & ~size_t(255); }
+
+static EtdLayout etd_layout(int ny, int nx, int elem) {
+  EtdLayout L;
+  L.fs = (long long)ny * spec_ldc(nx);
+  const size_t sc = (size_t)2 * L.fs * 2 * elem;  // 2 fields of complex
+  size_t o = 0;
+  L.zu = o; o += sc;  // ZU, ZN, ZX contiguous (row-kernel offsets are relative to ZU)
+  L.zn = o; o += sc;
+  L.zx = o; o += al(sc);
+  L.uh = o; o += al(sc);
+  L.nu = o; o += al(sc);
+  L.ah = o; o += al(sc);
+  L.ss = o; o += al(sc);
+  L.tab = o; o += al((size_t)2 * 6 * L.fs * elem);
+  L.total = o;
+  return L;
+}
+
+template <typename T>
+struct EtdPlan {
+  EArgs<T> c[5];
+  RowArgs<T> rN, r4, rin, rout;
+  size_t csmem;
+};
+
+template <typename T>
+static EtdPlan<T> build_etd(const void* plan, const mjx_grid2d* g, double F, double k, char* ws,
+                            const EtdLayout& L, const T* y_in, T* y_out) {
+  EtdPlan<T> P;
+  const PlanView pv = plan_view(plan, g->ny, g->nx, sizeof(T));
+  const int ldc = spec_ldc(g->nx);
+  EArgs<T> e;
+  memset(&e, 0, sizeof(e));
+  e.ny = g->ny; e.log2ny = ilog2_exact(g->ny); e.ncols = g->nx / 2 + 1; e.ldc = ldc;
+  const int tps = g->ny >= 16 ? g->ny / 16 : 1;
+  int C = 256 / tps;
+  if (C < 1) C = 1;
+  if (C > 8) C = 8;
+  const int maxth = sizeof(T) == 4 ? 512 : 512;
+  while (C > 1 && (2 * C * tps > maxth || (size_t)sp_size(g->ny * 2 * C) * 2 * sizeof(T) > 200 * 1024)) C >>= 1;
+  e.C = C; e.njobs = 2;
+  e.zu = (cx<T>*)(ws + L.zu); e.zn = (cx<T>*)(ws + L.zn); e.zx = (cx<T>*)(ws + L.zx);
+  e.uh = (cx<T>*)(ws + L.uh); e.nu = (cx<T>*)(ws + L.nu); e.ah = (cx<T>*)(ws + L.ah); e.ss = (cx<T>*)(ws + L.ss);
+  e.tab = (const T*)(ws + L.tab); e.fs = L.fs; e.tw = (const cx<T>*)pv.twy;
+  e.scale = (T)(1.0 / ((double)g->nx * (double)g->ny));
+  for (int t = 1; t <= 4; ++t) { P.c[t] = e; P.c[t].type = t; }
+  P.csmem = (size_t)sp_size(g->ny * 2 * C) * 2 * sizeof(T);
+
+  RowArgs<T> r;
+  memset(&r, 0, sizeof(r));
+  r.n = g->nx; r.log2n = ilog2_exact(g->nx); r.ldc = ldc; r.nrows = g->ny; r.npairs = 1;
+  r.nseq = row_nseq(g->nx, g->ny); r.rstride = g->nx; r.rin_sel = -1; r.rout_sel = -1;
+  r.spec = (cx<T>*)(ws + L.zu); r.tw = (const cx<T>*)pv.twx; r.inv_scale = (T)1; r.F = F; r.k = k;
+  r.rin[0] = y_in; r.rout[0] = y_out;
+  const long long zx = (long long)((L.zx - L.zu) / sizeof(cx<T>)), zn = (long long)((L.zn - L.zu) / sizeof(cx<T>));
+  const long long fr = (long long)g->ny * g->nx;
+  RowPair p;
+  memset(&p, 0, sizeof(p));
+  p.ra = 0; p.rb = fr;
+  P.rN = r; p.sa = zx; p.sb = zx + L.fs; p.flags = ROW_LOAD_SPEC | ROW_NONLIN | ROW_STORE_SPEC; P.rN.pr[0] = p;
+  P.r4 = r; p.sa = 0; p.sb = L.fs; p.oa = zn; p.ob = zn + L.fs;
+  p.flags = ROW_LOAD_SPEC | ROW_NONLIN | ROW_STORE_SPEC | ROW_SPEC_ALT; P.r4.pr[0] = p;
+  P.rin = r; p.sa = 0; p.sb = L.fs; p.flags = ROW_STORE_SPEC; P.rin.pr[0] = p;
+  P.rout = r; p.flags = ROW_LOAD_SPEC | ROW_STORE_REAL; P.rout.pr[0] = p;
+  return P;
+}
+
+template <typename T>
+static cudaError_t etd_col(const EArgs<T>& e, size_t smem, cudaStream_t s) {
+  const int tps = e.ny >= 16 ? e.ny / 16 : 1;
+  dim3 grid((e.ncols + e.C - 1) / e.C, e.njobs);
+  etd_col_kernel<T><<<grid, 2 * e.C * tps, smem, s>>>(e);
+  return cudaGetLastError();
+}
+
+template <typename T>
+static cudaError_t etd_step(const EtdPlan<T>& P, cudaStream_t s) {
+  cudaError_t e;
+  for (int t = 1; t <= 4; ++t) {
+    if ((e = etd_col<T>(P.c[t], P.csmem, s)) != cudaSuccess) return e;
+    const RowArgs<T>& r = t < 4 ? P.rN : P.r4;
+    if ((e = launch_row<T, RX_GRAY_SCOTT>(r, s)) != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+template <typename T>
+static mjx_status etd_run(const void* plan, const mjx_grid2d* g, int symbol, const double* D, double F,
+                          double k, double dt, double f2_factor, int n_steps, const T* y_in, T* y_out,
+                          char* ws, const EtdLayout& L, int recompute, cudaStream_t s) {
+  static int attr = 0;
+  if (!attr) {
+    int dev = 0, optin = 0;
+    MJX_CUDA_TRY(cudaGetDevice(&dev));
+    MJX_CUDA_TRY(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    MJX_CUDA_TRY(cudaFuncSetAttribute(etd_col_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
+    MJX_CUDA_TRY(cudaFuncSetAttribute(etd_col_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
+    attr = 1;
+  }
+  if (recompute) {
+    etd_coeff_kernel<T><<<152 * 8, 256, 0, s>>>((T*)(ws + L.tab), g->ny, g->nx, spec_ldc(g->nx), symbol,
+                                                 g->dy, g->dx, D[0], D[1], dt, 32, f2_factor);
+    MJX_CUDA_TRY(cudaGetLastError());
+  }
+  const EtdPlan<T> P = build_etd<T>(plan, g, F, k, ws, L, y_in, y_out);
+  MJX_CUDA_TRY((launch_row<T, RX_GRAY_SCOTT>(P.rin, s)));
+  MJX_CUDA_TRY((launch_row<T, RX_GRAY_SCOTT>(P.r4, s)));
+  if (n_steps > 0) {
+    // one step captured once, replayed n_steps times
+    cudaStream_t cs = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaError_t ce = cudaSuccess;
+    do {
+      if ((ce = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking)) != cudaSuccess) break;
+      if ((ce = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) break;
+      const cudaError_t le = etd_step<T>(P, cs);
+      ce = cudaStreamEndCapture(cs, &graph);
+      if (le != cudaSuccess) { ce = le; break; }
+      if (ce != cudaSuccess) break;
+      if ((ce = cudaGraphInstantiate(&exec, graph, 0)) != cudaSuccess) break;
+      for (int i = 0; i < n_steps && ce == cudaSuccess; ++i) ce = cudaGraphLaunch(exec, s);
+    } while (0);
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    if (cs) cudaStreamDestroy(cs);
+    if (ce != cudaSuccess) { set_last_error(ce, __FILE__, __LINE__); return MJX_CUDA_ERROR; }
+  }
+  MJX_CUDA_TRY((launch_row<T, RX_GRAY_SCOTT>(P.rout, s)));
+  return MJX_OK;
+}
+
+}  // namespace mjx
+
+using namespace mjx;
+
+extern "C" {
+
+size_t mjx_etdrk4_ws_bytes(int ny, int nx, int dtype) {
+  const int e = elem_size(dtype);
+  if (!e || ilog2_exact(nx) < 1 || ilog2_exact(ny) < 1) return 0;
+  return etd_layout(ny, nx, e).total;
+}
+
+mjx_status mjx_etdrk4_gray_scott2d(const void* plan, const mjx_grid2d* g, int dtype, int symbol,
+                                   const double* D, double F, double k, double dt, double f2_factor,
+                                   int n_steps,
+                                   const void* y_in, void* y_out, void* ws, size_t ws_bytes,
+                                   int recompute_coeffs, void* stream) {
+  MJX_TRY(check_grid(g));
+  const int e = elem_size(dtype);
+  if (!e) return MJX_BAD_DTYPE;
+  if (!plan || !D || !y_in || !y_out || n_steps < 0) return MJX_BAD_ARG;
+  if (symbol != MJX_SYMBOL_FD && symbol != MJX_SYMBOL_SPECTRAL) return MJX_BAD_ARG;
+  const EtdLayout L = etd_layout(g->ny, g->nx, e);
+  if (!ws || ws_bytes < L.total) return MJX_WORKSPACE;
+  MJX_TRY(ensure_kernel_attrs());
+  cudaStream_t s = (cudaStream_t)stream;
+  if (e == 4)
+    return etd_run<float>(plan, g, symbol, D, F, k, dt, f2_factor, n_steps, (const float*)y_in, (float*)y_out,
+                          (char*)ws, L, recompute_coeffs, s);
+  return etd_run<double>(plan, g, symbol, D, F, k, dt, f2_factor, n_steps, (const double*)y_in, (double*)y_out,
+                         (char*)ws, L, recompute_coeffs, s);
+}
+
+mjx_status mjx_etdrk4_kernel2d(const void* plan, const mjx_grid2d* g, int dtype, double F, double k,
+                               int which, void* ws, size_t ws_bytes, void* stream) {
+  MJX_TRY(check_grid(g));
+  const int e = elem_size(dtype);
+  if (!e) return MJX_BAD_DTYPE;
+  const EtdLayout L = etd_layout(g->ny, g->nx, e);
+  if (!ws || ws_bytes < L.total || which < 1 || which > 8) return MJX_BAD_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  cudaError_t ce;
+  if (e == 4) {
+    const EtdPlan<float> P = build_etd<float>(plan, g, F, k, (char*)ws, L, nullptr, nullptr);
+    ce = (which & 1) ? etd_col<float>(P.c[(which + 1) / 2], P.csmem, s)
+                     : launch_row<float, RX_GRAY_SCOTT>(which == 8 ? P.r4 : P.rN, s);
+  } else {
+    const EtdPlan<double> P = build_etd<double>(plan, g, F, k, (char*)ws, L, nullptr, nullptr);
+    ce = (which & 1) ? etd_col<double>(P.c[(which + 1) / 2], P.csmem, s)
+                     : launch_row<double, RX_GRAY_SCOTT>(which == 8 ? P.r4 : P.rN, s);
+  }
+  return cuda_status(ce);
+}
+
+}  // extern "C"

@@ -182,6 +182,18 @@ __global__ void __launch_bounds__(256, Occ<T>::row) row_kernel(const __grid_cons
     if (x >= n) continue;
     const C v = Z(x);
     T va = v.x * sc, vb = v.y * sc;
+    if (flags & ROW_NONLIN) {
+      // Gray-Scott reaction terms (operators.py:655-667); Fisher-KPP r u (1-u)
+      if (RX == RX_GRAY_SCOTT) {
+        const T uvv = va * vb * vb;
+        const T nu = -uvv + (T)a.F * ((T)1 - va), nv = uvv - (T)(a.F + a.k) * vb;
+        va = nu; vb = nv;
+      } else if (RX == RX_FISHER) {
+        va = (T)a.r * va * ((T)1 - va); vb = (T)a.r * vb * ((T)1 - vb);
+      } else {
+        va = (T)0; vb = (T)0;
+      }
+    }
     if (flags & ROW_REACT) {
       if (flags & ROW_DELTA) react_delta<T, RX>(va, vb, h, (T)a.F, (T)a.k, (T)a.r);
       else react_heun<T, RX>(va, vb, h, (T)a.F, (T)a.k, (T)a.r);
@@ -206,8 +218,8 @@ __global__ void __launch_bounds__(256, Occ<T>::row) row_kernel(const __grid_cons
   if (flags & ROW_STORE_SPEC) {
     __syncthreads();
     fft_smem<T, false, false>(buf, n, a.log2n, a.nseq, n, 1, a.tw, tid);
-    C* A = a.spec + pr.sa + y * a.ldc;
-    C* B = a.spec + pr.sb + y * a.ldc;
+    C* A = a.spec + ((flags & ROW_SPEC_ALT) ? pr.oa : pr.sa) + y * a.ldc;
+    C* B = a.spec + ((flags & ROW_SPEC_ALT) ? pr.ob : pr.sb) + y * a.ldc;
 #pragma unroll
     for (int m = 0; m < 9; ++m) {
       const int kk = lt + m * tps;

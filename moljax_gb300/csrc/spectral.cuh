@@ -41,6 +41,8 @@ enum {
   ROW_ERRNORM = 16,    // accumulate the scaled error of (a, b) against eref
   ROW_DELTA = 32,      // with ROW_REACT: keep only the reaction increment (new - old)
   ROW_ERRPAIR = 64,    // accumulate (a / (atol + rtol |b|))^2: a = error row, b = solution row
+  ROW_NONLIN = 128,    // replace (a, b) by the reaction terms N(a, b) (exponential integrators)
+  ROW_SPEC_ALT = 256,  // store the spectrum at (oa, ob) instead of (sa, sb)
 };
 
 // pointwise reaction kinds (compile-time)
@@ -49,6 +51,7 @@ enum { RX_NONE = 0, RX_GRAY_SCOTT = 1, RX_FISHER = 2, RX_LINEAR = 3 };
 struct RowPair {
   long long ra, rb;    // real row offsets (elements) of rows a and b at y = 0
   long long sa, sb;    // spectrum offsets (complex elements) at ky = 0
+  long long oa, ob;    // output spectrum offsets with ROW_SPEC_ALT
   double hfac;         // reaction step = hfac * (dt from state, or hfixed)
   int flags;
   int pad;

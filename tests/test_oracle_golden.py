@@ -144,3 +144,23 @@ def test_bc_formulas_2d():
     assert np.allclose(d[1:-1, 0], 2.0 - f[1:-1, 1])
     n = mol.bc_2d(f, g, mol.NEUMANN, {"top": 0.5})
     assert np.allclose(n[4, :], n[3, :] + 2 * g.dy * 0.5)
+
+
+def test_etdrk4_oracle_orders():
+    # Cox-Matthews form is 4th order (tests/test_fft_operators.py:561-617: order > 3);
+    # the benchmark-script form (f2 without the factor 2) is not
+    from oracle import etdrk4 as OE
+    n, L = 16, 2.5
+    g = mol.Grid2D(n, n, 0, L, 0, L)
+    y0 = mol.gray_scott_ic(g, 3)
+    u0, v0 = mol.interior(y0["u"], g), mol.interior(y0["v"], g)
+    lam = mol.fd_symbol_2d(n, n, g.dy, g.dx)
+    args = (u0, v0, lam, 2e-3, 1e-3, 0.035, 0.065)
+    for fac, lo in ((2.0, 12.0), (1.0, None)):
+        ref = OE.etdrk4_gray_scott(*args, 0.0625, 128, fac)[0]
+        e1 = np.linalg.norm(OE.etdrk4_gray_scott(*args, 2.0, 4, fac)[0] - ref)
+        e2 = np.linalg.norm(OE.etdrk4_gray_scott(*args, 1.0, 8, fac)[0] - ref)
+        if lo is not None:
+            assert e1 / e2 > lo
+        else:
+            assert e1 / e2 < 4.0
