@@ -231,7 +231,10 @@ static EtdPlan<T> build_etd(const void* plan, const mjx_grid2d* g, double F, dou
   e.zu = (cx<T>*)(ws + L.zu); e.zn = (cx<T>*)(ws + L.zn); e.zx = (cx<T>*)(ws + L.zx);
   e.uh = (cx<T>*)(ws + L.uh); e.nu = (cx<T>*)(ws + L.nu); e.ah = (cx<T>*)(ws + L.ah); e.ss = (cx<T>*)(ws + L.ss);
   e.tab = (const T*)(ws + L.tab); e.fs = L.fs; e.tw = (const cx<T>*)pv.twy;
-  e.scale = (T)(1.0 / ((double)g->nx * (double)g->ny));
+  // column inverses normalise by 1/ny and every c2r row pass by 1/nx, so the
+  // row-space state ZU is an unnormalised row DFT both after the initial r2c and
+  // after each step
+  e.scale = (T)(1.0 / (double)g->ny);
   for (int t = 1; t <= 4; ++t) { P.c[t] = e; P.c[t].type = t; }
   P.csmem = (size_t)sp_size(g->ny * 2 * C) * 2 * sizeof(T);
 
@@ -239,7 +242,8 @@ static EtdPlan<T> build_etd(const void* plan, const mjx_grid2d* g, double F, dou
   memset(&r, 0, sizeof(r));
   r.n = g->nx; r.log2n = ilog2_exact(g->nx); r.ldc = ldc; r.nrows = g->ny; r.npairs = 1;
   r.nseq = row_nseq(g->nx, g->ny); r.rstride = g->nx; r.rin_sel = -1; r.rout_sel = -1;
-  r.spec = (cx<T>*)(ws + L.zu); r.tw = (const cx<T>*)pv.twx; r.inv_scale = (T)1; r.F = F; r.k = k;
+  r.spec = (cx<T>*)(ws + L.zu); r.tw = (const cx<T>*)pv.twx; r.inv_scale = (T)(1.0 / (double)g->nx);
+  r.F = F; r.k = k;
   r.rin[0] = y_in; r.rout[0] = y_out;
   const long long zx = (long long)((L.zx - L.zu) / sizeof(cx<T>)), zn = (long long)((L.zn - L.zu) / sizeof(cx<T>));
   const long long fr = (long long)g->ny * g->nx;
