@@ -43,7 +43,7 @@ def test_etdrk4_coefficients_vs_phi(cuda):
     h1, _, _ = OE.phi_functions(lam / 2)
     np.testing.assert_allclose(Q, 0.5 * h1, rtol=1e-10)
     np.testing.assert_allclose(f1, p1 - 3 * p2 + 4 * p3, rtol=1e-9)
-    np.testing.assert_allclose(f2, 2 * p2 - 4 * p3, rtol=1e-9)
+    np.testing.assert_allclose(f2, p2 - 2 * p3, rtol=1e-9)  # 2 f2 = b2 = 2 phi2 - 4 phi3
     np.testing.assert_allclose(f3, -p2 + 4 * p3, rtol=1e-9)
 
 
