@@ -171,6 +171,36 @@ mjx_status mjx_imex_adaptive2d(const void* plan, const mjx_grid2d* grid, int dty
                                void* hist_y, void* ws, size_t ws_bytes,
                                mjx_adaptive_result* result, void* stream);
 
+/* ---- Newton-Krylov implicit steps ------------------------------------------------ */
+typedef enum mjx_method { MJX_METHOD_BE = 3, MJX_METHOD_CN = 4, MJX_METHOD_BDF2 = 5 } mjx_method;
+
+/* moljax/core/newton_krylov.py:29-38 (NKParams) plus the GMRES restart length. */
+typedef struct mjx_nk_params {
+  int max_newton_iters, max_krylov_iters, restart, max_backtrack;
+  double newton_tol, krylov_tol, damping, backtrack_factor, min_residual_decrease;
+} mjx_nk_params;
+
+size_t mjx_nk_vardiff_ws_bytes(int n, int restart);
+
+/* n_steps fixed implicit steps (BE, CN, or BDF2 with a BE first step) of
+ * u_t = div((a + b u^2) grad u) - c u^3 on an n x n cell-centred grid with
+ * homogeneous Dirichlet ghosts (model_abc = {a, b, c}); y0/y_out are FP64
+ * interiors.  Each step solves its residual (create_implicit_residual /
+ * create_bdf2_residual, moljax/core/newton_krylov.py:362-448) with
+ * newton_krylov_solve semantics (171-359): FP64 residual, FP32 hand-written
+ * JVP and Krylov vectors, left-preconditioned restarted GMRES with the
+ * Hessenberg/Givens least squares in FP64 on the GPU, preconditioner
+ * (alpha0 I - beta Dbar Lap_D)^-1 (DST diagonal via the odd extension,
+ * plan2 = FP32 FD plan of the (2n)^2 periodic grid with the same spacing).
+ * BE initial guess: explicit Euler (stepping.py:195-196) or, with
+ * be_guess_previous != 0, y_n.  stats (optional, 3 ints per step): Newton
+ * iterations, GMRES iterations, converged. */
+mjx_status mjx_nk_vardiff_integrate2d(const void* plan2, int n, double dy, double dx,
+                                      const double* model_abc, int method, double dt, int n_steps,
+                                      int be_guess_previous, const mjx_nk_params* nkp,
+                                      const double* y0, double* y_out, int* stats, void* ws,
+                                      size_t ws_bytes, void* stream);
+
 /* ---- ETDRK4 (Cox-Matthews) for coupled Gray-Scott ------------------------------ */
 /* Workspace: row spectra ZU/ZN/ZX, 2D spectra U^/N^u/a^/S and the coefficient tables. */
 size_t mjx_etdrk4_ws_bytes(int ny, int nx, int dtype);

@@ -45,6 +45,13 @@ class ImexProblemC(C.Structure):
                 ("use_strang", C.c_int), ("max_attempts", C.c_int)]
 
 
+class NKParamsC(C.Structure):
+    _fields_ = [("max_newton_iters", C.c_int), ("max_krylov_iters", C.c_int), ("restart", C.c_int),
+                ("max_backtrack", C.c_int), ("newton_tol", C.c_double), ("krylov_tol", C.c_double),
+                ("damping", C.c_double), ("backtrack_factor", C.c_double),
+                ("min_residual_decrease", C.c_double)]
+
+
 class AdaptiveResultC(C.Structure):
     _fields_ = [("t_final", C.c_double), ("dt_next", C.c_double), ("prev_err", C.c_double),
                 ("last_err", C.c_double), ("n_accepted", C.c_int), ("n_rejected", C.c_int),
@@ -76,6 +83,10 @@ SIGNATURES = {
                                  C.POINTER(PIDParamsC), _d, _d, _d, _i, _i, _vp, _vp,
                                  C.POINTER(C.c_double), C.POINTER(C.c_double), _vp, _vp, _sz,
                                  C.POINTER(AdaptiveResultC), _vp]),
+    "mjx_nk_vardiff_ws_bytes": (_sz, [_i, _i]),
+    "mjx_nk_vardiff_integrate2d": (_i, [_vp, _i, _d, _d, C.POINTER(C.c_double), _i, _d, _i, _i,
+                                        C.POINTER(NKParamsC), _vp, _vp, C.POINTER(C.c_int), _vp, _sz,
+                                        _vp]),
     "mjx_etdrk4_ws_bytes": (_sz, [_i, _i, _i]),
     "mjx_etdrk4_gray_scott2d": (_i, [_vp, C.POINTER(Grid2DC), _i, _i, C.POINTER(C.c_double), _d, _d,
                                      _d, _d, _i, _vp, _vp, _vp, _sz, _i, _vp]),

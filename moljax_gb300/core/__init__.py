@@ -17,3 +17,8 @@ from moljax_gb300.core.utils import StatusCode
 from moljax_gb300.core import fft_integrators, fft_operators
 from moljax_gb300.core.fft_integrators import etdrk4_gray_scott, etdrk4_step, etd_integrate
 from moljax_gb300.core.fft_operators import DiffusionOperator
+from moljax_gb300.core import newton_krylov, preconditioners
+from moljax_gb300.core.newton_krylov import (NKParams, NKStats, newton_krylov_solve,
+                                             integrate_implicit_vardiff)
+from moljax_gb300.core.preconditioners import (DiffusionPreconditioner, IdentityPreconditioner,
+                                               BlockJacobiPreconditioner)

@@ -1,0 +1,215 @@
+"""Newton-Krylov (moljax/core/newton_krylov.py drop-in).
+
+Two levels:
+
+* ``integrate_implicit_vardiff`` -- the fused native path (hot path of the
+  NK benchmark configuration): fixed-dt BE/CN/BDF2 steps of
+  u_t = div((a + b u^2) grad u) - c u^3 with homogeneous Dirichlet ghosts,
+  each step solved by ``mjx_nk_vardiff_integrate2d``: FP64 residual, FP32
+  hand-written JVP and Krylov vectors, left-preconditioned restarted GMRES with
+  the Hessenberg/Givens least squares in FP64 on the GPU, DST preconditioner;
+* ``newton_krylov_solve(residual_fn, x0, ...)`` -- the reference signature
+  for arbitrary Python residuals (newton_krylov.py:171-359): same Newton /
+  backtracking semantics, exact JVP by torch forward-mode AD (the counterpart
+  of jax.jvp) and a restarted GMRES on torch tensors.  This generic form runs
+  user callables and is not the fused path.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import math
+from typing import Any, Callable, Dict, NamedTuple, Optional
+
+import torch
+
+from moljax_gb300 import _native as N
+
+
+class NKParams(NamedTuple):
+    """newton_krylov.py:29-38 (+ gmres_restart; JAX's gmres default restart is 20)."""
+    max_newton_iters: int = 10
+    max_krylov_iters: int = 50
+    newton_tol: float = 1e-8
+    krylov_tol: float = 1e-6
+    damping: float = 1.0
+    backtrack_factor: float = 0.5
+    max_backtrack: int = 3
+    min_residual_decrease: float = 1e-4
+    gmres_restart: int = 20
+
+
+class NKStats(NamedTuple):
+    converged: bool
+    newton_iters: int
+    lin_iters: int
+    final_res_norm: float
+
+
+class NKResult(NamedTuple):
+    solution: Any
+    stats: NKStats
+
+
+def _cparams(p: NKParams) -> N.NKParamsC:
+    return N.NKParamsC(p.max_newton_iters, p.max_krylov_iters, p.gmres_restart, p.max_backtrack,
+                       p.newton_tol, p.krylov_tol, p.damping, p.backtrack_factor,
+                       p.min_residual_decrease)
+
+
+def integrate_implicit_vardiff(u0: torch.Tensor, dx: float, dt: float, n_steps: int,
+                               method: str = "bdf2", a: float = 1.0, b: float = 1.0,
+                               c: float = 1.0, nk_params: Optional[NKParams] = None,
+                               be_guess: str = "euler", dy: Optional[float] = None):
+    """Fixed-dt implicit steps on the GPU; u0 is an (n, n) interior (FP64 state).
+
+    method: "be", "cn" or "bdf2" (BE first step, stepping.py:1077-1139).
+    be_guess: "euler" (be_step's explicit Euler guess, stepping.py:195-196) or
+    "previous" (start Newton from y_n).  Returns (u, stats) where stats is an
+    (n_steps, 3) int tensor of (Newton iterations, GMRES iterations, converged).
+    """
+    from moljax_gb300.core.fft_solvers import get_plan, workspace
+    nk_params = nk_params or NKParams()
+    u = u0.to(torch.float64).contiguous()
+    N.require_cuda(u)
+    n = u.shape[-1]
+    dy = dx if dy is None else dy
+    plan2 = get_plan(2 * n, 2 * n, dy, dx, "fd", torch.float32, u.device)
+    lib = N.lib()
+    ws = workspace(lib.mjx_nk_vardiff_ws_bytes(n, nk_params.gmres_restart), plan2.device, "nk")
+    out = torch.empty_like(u)
+    stats = (C.c_int * (3 * max(n_steps, 1)))()
+    abc = (C.c_double * 3)(a, b, c)
+    meth = {"be": 3, "cn": 4, "bdf2": 5}[method]
+    cp = _cparams(nk_params)
+    N.check("mjx_nk_vardiff_integrate2d", lib.mjx_nk_vardiff_integrate2d(
+        N.ptr(plan2.buf), n, float(dy), float(dx), abc, meth, float(dt), int(n_steps),
+        int(be_guess == "previous"), C.byref(cp), N.ptr(u), N.ptr(out), stats, N.ptr(ws),
+        ws.numel(), N.stream_ptr(plan2.device)))
+    st = torch.tensor(list(stats)[: 3 * n_steps], dtype=torch.int32).reshape(n_steps, 3)
+    return out, st
+
+
+# ----------------------------------------------------------------- generic form
+def _flat(state):
+    keys = list(state.keys())
+    return torch.cat([state[k].reshape(-1) for k in keys]), keys, [state[k].shape for k in keys]
+
+
+def _unflat(vec, keys, shapes):
+    out, o = {}, 0
+    for k, s in zip(keys, shapes):
+        m = int(math.prod(s))
+        out[k] = vec[o:o + m].reshape(s)
+        o += m
+    return out
+
+
+def _gmres(matvec, b, tol, restart, maxiter, M=None):
+    """Left-preconditioned restarted GMRES (MGS, Givens) on flat torch vectors."""
+    Mf = M or (lambda v: v)
+    bp = Mf(b)
+    bnorm = float(torch.linalg.norm(bp))
+    x = torch.zeros_like(b)
+    its = 0
+    if bnorm == 0.0:
+        return x, 0
+    for _ in range(maxiter):
+        r = Mf(b - matvec(x)) if its else bp
+        beta = float(torch.linalg.norm(r))
+        if beta <= tol * bnorm:
+            break
+        V = [r / beta]
+        H = torch.zeros(restart + 1, restart, dtype=torch.float64)
+        cs, sn = torch.zeros(restart, dtype=torch.float64), torch.zeros(restart, dtype=torch.float64)
+        g = torch.zeros(restart + 1, dtype=torch.float64)
+        g[0] = beta
+        k = 0
+        for j in range(restart):
+            w = Mf(matvec(V[j]))
+            for i in range(j + 1):
+                H[i, j] = float(torch.dot(V[i], w))
+                w = w - H[i, j].item() * V[i]
+            hn = float(torch.linalg.norm(w))
+            H[j + 1, j] = hn
+            for i in range(j):
+                t = cs[i] * H[i, j] + sn[i] * H[i + 1, j]
+                H[i + 1, j] = -sn[i] * H[i, j] + cs[i] * H[i + 1, j]
+                H[i, j] = t
+            den = math.hypot(float(H[j, j]), float(H[j + 1, j]))
+            cs[j], sn[j] = H[j, j] / den, H[j + 1, j] / den
+            H[j, j], H[j + 1, j] = den, 0.0
+            g[j + 1] = -sn[j] * g[j]
+            g[j] = cs[j] * g[j]
+            its += 1
+            k = j + 1
+            if abs(float(g[j + 1])) <= tol * bnorm or hn == 0.0:
+                break
+            V.append(w / hn)
+        y = torch.linalg.solve_triangular(H[:k, :k], g[:k, None], upper=True)[:, 0]
+        for i in range(k):
+            x = x + float(y[i]) * V[i]
+        if abs(float(g[k])) <= tol * bnorm:
+            break
+    return x, its
+
+
+def newton_krylov_solve(residual_fn: Callable, x0, grid=None, params: Optional[Dict] = None,
+                        preconditioner=None, nk_params: Optional[NKParams] = None, dt: float = 1.0,
+                        *, gmres_restart: Optional[int] = None, rtol: Optional[float] = None):
+    """Reference signature (newton_krylov.py:171-359) and README kwargs.
+
+    ``rtol`` (README) sets newton_tol; ``gmres_restart`` sets the restart length.
+    """
+    from moljax_gb300.core.preconditioners import PrecondContext, IdentityPreconditioner
+    p = nk_params or NKParams()
+    if rtol is not None:
+        p = p._replace(newton_tol=rtol)
+    if gmres_restart is not None:
+        p = p._replace(gmres_restart=gmres_restart)
+    single = not isinstance(x0, dict)
+    x0d = {"x": x0} if single else x0
+    res_fn = (lambda d: {"x": residual_fn(d["x"])}) if single else residual_fn
+    xf, keys, shapes = _flat(x0d)
+    ctx = PrecondContext(grid, dt, params or {})
+    prec = preconditioner if preconditioner is not None else IdentityPreconditioner()
+
+    def R(v):
+        return _flat(res_fn(_unflat(v, keys, shapes)))[0]
+
+    def M(v):
+        return _flat(prec.apply(_unflat(v, keys, shapes), ctx))[0]
+
+    use_m = not isinstance(prec, IdentityPreconditioner)
+    x = xf.clone()
+    rn = float(torch.linalg.norm(R(x)))
+    converged = rn < p.newton_tol
+    it = lits = 0
+    res = rn
+    while it < p.max_newton_iters and not converged:
+        r = R(x)
+        rn = float(torch.linalg.norm(r))
+        converged = rn < p.newton_tol
+        xc = x
+
+        def jv(v):
+            return torch.func.jvp(R, (xc,), (v,))[1]
+
+        dx, li = _gmres(jv, -r, p.krylov_tol, p.gmres_restart, p.max_krylov_iters,
+                        M if use_m else None)
+        lits += li
+        alpha, xb, rb, acc = p.damping, x, rn, False
+        for _ in range(p.max_backtrack):
+            if acc:
+                break
+            xn = xb + alpha * dx
+            rnn = float(torch.linalg.norm(R(xn)))
+            if rnn < (1.0 - p.min_residual_decrease * alpha) * rb:
+                xb, rb, acc = xn, rnn, True
+            else:
+                alpha *= p.backtrack_factor
+        x = xb if acc else x + p.damping * dx
+        res = rb
+        it += 1
+    sol = _unflat(x, keys, shapes)
+    return NKResult(sol["x"] if single else sol, NKStats(bool(converged), it, lits, res))

@@ -1,0 +1,125 @@
+"""Preconditioners (moljax/core/preconditioners.py drop-in).
+
+``DiffusionPreconditioner`` accepts both spellings:
+
+* reference form ``DiffusionPreconditioner(field_diffusivities={...},
+  n_iterations=5, omega=0.6667)`` -- weighted Jacobi on (I - dt D Lap)
+  (preconditioners.py:121-198), applied with torch on padded fields;
+* README form ``DiffusionPreconditioner(D, dx, dt)`` (README.md:148) -- the
+  exact diagonal inverse (alpha0 I - kappa Lap_D)^-1 for homogeneous Dirichlet
+  ghosts by the sine transform (DST-II through the odd extension to a periodic
+  box, native spectral pass).  This is the preconditioner of the native
+  Newton-Krylov path.
+"""
+
+from __future__ import annotations
+
+from dataclasses import dataclass
+from typing import Any, Dict, Optional
+
+import torch
+
+
+class PrecondContext:
+    """preconditioners.py:29-43."""
+
+    def __init__(self, grid, dt, params, **kw):
+        self.grid, self.dt, self.params = grid, dt, params
+        for k, v in kw.items():
+            setattr(self, k, v)
+
+
+@dataclass(frozen=True)
+class IdentityPreconditioner:
+    name: str = "identity"
+
+    def apply(self, r, context):
+        return r
+
+
+@dataclass(frozen=True)
+class BlockJacobiPreconditioner:
+    """preconditioners.py:69-118: r / (1 + dt D 4/dx^2 + dt |v|/dx) per field."""
+    name: str = "block_jacobi"
+    diffusion_keys: Optional[Dict[str, str]] = None
+    advection_keys: Optional[Dict[str, str]] = None
+
+    def apply(self, r, context):
+        g, dt, params = context.grid, context.dt, context.params
+        out = {}
+        for name, f in r.items():
+            scale = 1.0
+            if self.diffusion_keys and name in self.diffusion_keys:
+                scale += dt * params.get(self.diffusion_keys[name], 0.0) * 4.0 / g.min_dx2
+            if self.advection_keys and name in self.advection_keys:
+                v = params.get(self.advection_keys[name], 0.0)
+                scale += dt * float(torch.as_tensor(v).abs().max()) / g.min_dx
+            out[name] = f / scale
+        return out
+
+
+class DiffusionPreconditioner:
+    """Both spellings; see the module docstring."""
+
+    def __init__(self, D=None, dx=None, dt=None, *, name: str = "diffusion",
+                 field_diffusivities: Optional[Dict[str, str]] = None, n_iterations: int = 5,
+                 omega: float = 0.6667, alpha0: float = 1.0):
+        self.name = name
+        self.field_diffusivities = field_diffusivities
+        self.n_iterations = n_iterations
+        self.omega = omega
+        self.spectral = D is not None and not isinstance(D, dict)
+        if isinstance(D, dict):
+            self.field_diffusivities = D
+        self.D, self.dx, self.dt, self.alpha0 = D, dx, dt, alpha0
+
+    # -- reference Jacobi form (preconditioners.py:146-198)
+    def _jacobi(self, rhs, grid, dt, D):
+        from moljax_gb300.core.stencil import laplacian_2d
+        diag = 1.0 + dt * D * (2.0 / grid.dx ** 2 + 2.0 / grid.dy ** 2)
+        x = rhs
+        for _ in range(self.n_iterations):
+            x = self.omega * (rhs + dt * D * laplacian_2d(x, grid)) / diag + (1.0 - self.omega) * x
+        return x
+
+    def apply(self, r, context):
+        if self.spectral:
+            return {k: self.solve(v, context.grid) for k, v in r.items()}
+        out = {}
+        for name, f in r.items():
+            key = (self.field_diffusivities or {}).get(name)
+            D = context.params.get(key, 0.0) if key is not None else 0.0
+            out[name] = self._jacobi(f, context.grid, context.dt, D) if D > 1e-14 else f
+        return out
+
+    def solve(self, r_interior: torch.Tensor, grid=None):
+        """(alpha0 I - dt D Lap_D)^-1 r on an interior (n, n) field (Dirichlet ghosts)."""
+        n = r_interior.shape[-1]
+        dx = float(self.dx if self.dx is not None else grid.dx)
+        return dirichlet_helmholtz(r_interior, dx, dx, self.alpha0, float(self.dt) * float(self.D))
+
+
+def dirichlet_helmholtz(r: torch.Tensor, dy: float, dx: float, alpha: float, kappa: float):
+    """(alpha I - kappa Lap_D)^-1 r for homogeneous Dirichlet ghosts (cell-centred).
+
+    The odd extension of r to a (2ny, 2nx) periodic box turns Lap_D into the
+    periodic 5-point Laplacian; the native Helmholtz pass inverts it exactly.
+    """
+    from moljax_gb300.core.fft_solvers import get_plan
+    from moljax_gb300 import _native as N
+    ny, nx = r.shape[-2:]
+    e = torch.empty((2 * ny, 2 * nx), dtype=r.dtype, device=r.device)
+    e[:ny, :nx] = r
+    e[:ny, nx:] = -r.flip(-1)
+    e[ny:, :] = -e[:ny, :].flip(0)
+    plan = get_plan(2 * ny, 2 * nx, dy, dx, "fd", r.dtype, r.device)
+    out = plan.apply(e, kappa / alpha, 1.0, N.MULT_HELMHOLTZ)
+    return out[:ny, :nx] / alpha
+
+
+def create_gray_scott_preconditioner(Du_key="Du", Dv_key="Dv") -> DiffusionPreconditioner:
+    """preconditioners.py:423-446."""
+    return DiffusionPreconditioner(field_diffusivities={"u": Du_key, "v": Dv_key})
+
+
+Preconditioner = Any

@@ -1,0 +1,768 @@
+// Matrix-free Newton-Krylov for implicit steps of the nonlinear diffusion-
+// reaction model F(u) = div((a + b u^2) grad u) - c u^3 on a cell-centred grid
+// with homogeneous Dirichlet ghosts (ghost = -neighbour).
+//
+// Restates moljax/core/newton_krylov.py:171-448: Newton with the convergence
+// flag evaluated before the update, left-preconditioned restarted GMRES on
+// M^-1 J dx = -M^-1 R, 3-try backtracking (accept if |R(x + alpha dx)| <
+// (1 - 1e-4 alpha) |R|, alpha halves; full damped step when no try is
+// accepted), and the BE/CN/BDF2 residual builders (362-448; BDF2 alphas and
+// beta as the reference, beta = dt (1 + w)/(1 + 2w)).
+//
+// Precision: state, residual (the Newton refinement) and the Hessenberg /
+// Givens least squares in FP64; Krylov vectors, the hand-written JVP and the
+// preconditioner in FP32.
+//
+// Preconditioner M^-1 = (alpha0 I - beta Dbar Lap_D)^-1, Dbar = a + b mean(u_n^2),
+// exact through the odd extension to a (2N)^2 periodic box (cell-centred
+// Dirichlet = DST-II diagonalisation), applied with the periodic spectral pass.
+//
+// The Arnoldi steps of a GMRES cycle run as one CUDA graph with a conditional
+// while node; the Givens kernel updates the residual estimate on the device and
+// clears the loop flag, so a cycle costs one host synchronisation.
+#include <math.h>
+#include <string.h>
+
+#include "spectral.cuh"
+
+namespace mjx {
+
+mjx_status ensure_kernel_attrs();
+int elem_size(int dtype);
+void set_last_error(cudaError_t e, const char* file, int line);
+
+enum { NK_MAXM = 64 };
+
+struct NKConsts {
+  double a0, beta;      // residual R = a0 y + cst - beta F(y)
+  double inv_a0;        // preconditioner output scale
+  double pa, pb, pc;    // model a, b, c
+  double alpha;         // line-search step for the trial point
+  double dbar;          // preconditioner diffusivity
+};
+
+struct GmresState {
+  int j, m, converged, k_used;
+  double tol_abs, beta0, hnext_inv, res_est;
+  double H[(NK_MAXM + 1) * NK_MAXM];
+  double cs[NK_MAXM], sn[NK_MAXM], g[NK_MAXM + 1], y[NK_MAXM];
+};
+
+// --------------------------------------------------------------- stencils
+// u at (i, j) with homogeneous Dirichlet ghosts (x ghosts first, then y: corners
+// are not used by the 5-point stencil)
+template <typename T>
+__device__ __forceinline__ T dval(const T* u, int i, int j, int n) {
+  const int ii = i < 0 ? 0 : (i >= n ? n - 1 : i);
+  const int jj = j < 0 ? 0 : (j >= n ? n - 1 : j);
+  const T v = u[(long long)ii * n + jj];
+  return ((i < 0) != (i >= n)) || ((j < 0) != (j >= n)) ? -v : v;
+}
+
+// R = a0 y + cst - beta F(y); part[block] = sum R^2; b32 = -R (optional)
+__global__ void vd_residual_kernel(const double* __restrict__ y, const double* __restrict__ cst,
+                                   double* __restrict__ R, float* __restrict__ b32,
+                                   double* __restrict__ part, const NKConsts* __restrict__ K,
+                                   int n, double idx2, double idy2) {
+  const double a = K->pa, b = K->pb, c = K->pc, a0 = K->a0, beta = K->beta;
+  double acc = 0.0;
+  const long long N2 = (long long)n * n;
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < N2;
+       p += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(p / n), j = (int)(p - (long long)i * n);
+    const double uc = y[p];
+    const double ue = dval(y, i, j + 1, n), uw = dval(y, i, j - 1, n);
+    const double un = dval(y, i + 1, j, n), us = dval(y, i - 1, j, n);
+    const double Dc = a + b * uc * uc;
+    const double De = a + b * ue * ue, Dw = a + b * uw * uw, Dn = a + b * un * un, Ds = a + b * us * us;
+    const double fx = 0.5 * (Dc + De) * (ue - uc) - 0.5 * (Dw + Dc) * (uc - uw);
+    const double fy = 0.5 * (Dc + Dn) * (un - uc) - 0.5 * (Ds + Dc) * (uc - us);
+    const double F = fx * idx2 + fy * idy2 - c * uc * uc * uc;
+    const double r = a0 * uc + cst[p] - beta * F;
+    R[p] = r;
+    if (b32) b32[p] = (float)(-r);
+    acc += r * r;
+  }
+  __shared__ double red[32];
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += red[w];
+    part[blockIdx.x] = s;
+  }
+}
+
+// odd extension N x N -> 2N x 2N (Dirichlet cell-centred <-> periodic)
+__global__ void oddext_kernel(const float* __restrict__ r, float* __restrict__ e, int n,
+                              const GmresState* gs) {
+  if (gs && gs->converged) return;
+  const int m = 2 * n;
+  const long long M2 = (long long)m * m;
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < M2;
+       p += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(p / m), j = (int)(p - (long long)i * m);
+    const int ii = i < n ? i : 2 * n - 1 - i, jj = j < n ? j : 2 * n - 1 - j;
+    const float sgn = ((i < n) == (j < n)) ? 1.f : -1.f;
+    e[p] = sgn * r[(long long)ii * n + jj];
+  }
+}
+
+__global__ void restrict_kernel(const float* __restrict__ e, float* __restrict__ w, int n,
+                                const NKConsts* K, const GmresState* gs) {
+  if (gs && gs->converged) return;
+  const float s = (float)K->inv_a0;
+  const long long N2 = (long long)n * n;
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < N2;
+       p += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(p / n), j = (int)(p - (long long)i * n);
+    w[p] = s * e[(long long)i * 2 * n + j];
+  }
+}
+
+// partial dots <V_i, w>, i = 0..j, FP64 accumulation; part[i * nblk + block]
+__global__ void gmres_dots_kernel(const float* __restrict__ V, const float* __restrict__ w,
+                                  const GmresState* gs, double* part, long long N2) {
+  if (gs->converged) return;
+  const int j = gs->j;
+  __shared__ double red[32];
+  for (int i = 0; i <= j; ++i) {
+    const float* vi = V + (long long)i * N2;
+    double acc = 0.0;
+    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < N2;
+         p += (long long)gridDim.x * blockDim.x)
+      acc += (double)vi[p] * (double)w[p];
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double s = 0.0;
+      for (int q = 0; q < (int)(blockDim.x >> 5); ++q) s += red[q];
+      part[(long long)i * gridDim.x + blockIdx.x] = s;
+    }
+    __syncthreads();
+  }
+}
+
+// H[i][j] = sum of the partial dots
+__global__ void gmres_hcol_kernel(const double* part, int nblk, GmresState* gs) {
+  if (gs->converged) return;
+  const int j = gs->j;
+  __shared__ double red[32];
+  for (int i = 0; i <= j; ++i) {
+    double acc = 0.0;
+    for (int b = threadIdx.x; b < nblk; b += blockDim.x) acc += part[(long long)i * nblk + b];
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double s = 0.0;
+      for (int q = 0; q < (int)(blockDim.x >> 5); ++q) s += red[q];
+      gs->H[i * NK_MAXM + j] = s;
+    }
+    __syncthreads();
+  }
+}
+
+// V_{j+1} = w - sum_i H[i][j] V_i (classical Gram-Schmidt), partial norms of V_{j+1}
+__global__ void gmres_orth_kernel(float* __restrict__ V, const float* __restrict__ w,
+                                  const GmresState* gs, double* part, long long N2) {
+  if (gs->converged) return;
+  const int j = gs->j;
+  float h[NK_MAXM];
+  for (int i = 0; i <= j; ++i) h[i] = (float)gs->H[i * NK_MAXM + j];
+  float* vn = V + (long long)(j + 1) * N2;
+  double acc = 0.0;
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < N2;
+       p += (long long)gridDim.x * blockDim.x) {
+    float x = w[p];
+    for (int i = 0; i <= j; ++i) x -= h[i] * V[(long long)i * N2 + p];
+    vn[p] = x;
+    acc += (double)x * (double)x;
+  }
+  __shared__ double red[32];
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) s += red[q];
+    part[blockIdx.x] = s;
+  }
+}
+
+// one Givens step in FP64 (single thread) and the loop flag
+__global__ void gmres_givens_kernel(const double* part, int nblk, GmresState* gs,
+                                    cudaGraphConditionalHandle h, int use_handle) {
+  __shared__ double red[32];
+  double acc = 0.0;
+  for (int b = threadIdx.x; b < nblk; b += blockDim.x) acc += part[b];
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x != 0) return;
+  if (gs->converged) {
+    if (use_handle) cudaGraphSetConditional(h, 0u);
+    return;
+  }
+  double s = 0.0;
+  for (int q = 0; q < (int)(blockDim.x >> 5); ++q) s += red[q];
+  const int j = gs->j;
+  const double hn = sqrt(s);
+  double* H = gs->H;
+  H[(j + 1) * NK_MAXM + j] = hn;
+  for (int i = 0; i < j; ++i) {
+    const double a = H[i * NK_MAXM + j], b = H[(i + 1) * NK_MAXM + j];
+    H[i * NK_MAXM + j] = gs->cs[i] * a + gs->sn[i] * b;
+    H[(i + 1) * NK_MAXM + j] = -gs->sn[i] * a + gs->cs[i] * b;
+  }
+  const double a = H[j * NK_MAXM + j], b = H[(j + 1) * NK_MAXM + j];
+  const double den = hypot(a, b);
+  const double c = den > 0 ? a / den : 1.0, sn = den > 0 ? b / den : 0.0;
+  gs->cs[j] = c;
+  gs->sn[j] = sn;
+  H[j * NK_MAXM + j] = den;
+  H[(j + 1) * NK_MAXM + j] = 0.0;
+  gs->g[j + 1] = -sn * gs->g[j];
+  gs->g[j] = c * gs->g[j];
+  gs->k_used = j + 1;
+  gs->res_est = fabs(gs->g[j + 1]);
+  const bool conv = gs->res_est <= gs->tol_abs || hn == 0.0;
+  gs->j = j + 1;
+  gs->hnext_inv = hn > 0 ? 1.0 / hn : 0.0;
+  const bool more = !conv && gs->j < gs->m;
+  if (conv) gs->converged = 1;
+  if (use_handle) cudaGraphSetConditional(h, more ? 1u : 0u);
+}
+
+// cycle start: beta0 = |V_0|, g = (beta0, 0, ...), tolerance on the first cycle
+__global__ void gmres_init_kernel(const double* part, int nblk, GmresState* gs, int first, double tol,
+                                  int m) {
+  __shared__ double red[32];
+  double acc = 0.0;
+  for (int b = threadIdx.x; b < nblk; b += blockDim.x) acc += part[b];
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x != 0) return;
+  double s = 0.0;
+  for (int q = 0; q < (int)(blockDim.x >> 5); ++q) s += red[q];
+  const double b0 = sqrt(s);
+  if (first) gs->tol_abs = tol * b0;
+  gs->beta0 = b0;
+  gs->j = 0;
+  gs->m = m;
+  gs->k_used = 0;
+  for (int i = 0; i <= m; ++i) gs->g[i] = 0.0;
+  gs->g[0] = b0;
+  gs->res_est = b0;
+  gs->hnext_inv = b0 > 0 ? 1.0 / b0 : 0.0;
+  gs->converged = (b0 <= gs->tol_abs || b0 == 0.0) ? 1 : 0;
+}
+
+// back substitution R y = g (FP64)
+__global__ void gmres_solve_kernel(GmresState* gs) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const int k = gs->k_used;
+  for (int i = k - 1; i >= 0; --i) {
+    double s = gs->g[i];
+    for (int q = i + 1; q < k; ++q) s -= gs->H[i * NK_MAXM + q] * gs->y[q];
+    const double d = gs->H[i * NK_MAXM + i];
+    gs->y[i] = d != 0.0 ? s / d : 0.0;
+  }
+}
+
+// dx += sum_i y_i V_i (V_0..V_{k-1} normalised)
+__global__ void gmres_update_kernel(float* dx, const float* V, const GmresState* gs, long long N2) {
+  const int k = gs->k_used;
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < N2;
+       p += (long long)gridDim.x * blockDim.x) {
+    double x = dx[p];
+    for (int i = 0; i < k; ++i) x += gs->y[i] * (double)V[(long long)i * N2 + p];
+    dx[p] = (float)x;
+  }
+}
+
+__global__ void sub_kernel(const float* b, const float* t, float* r, long long N2) {
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < N2;
+       p += (long long)gridDim.x * blockDim.x)
+    r[p] = b[p] - t[p];
+}
+
+// out = x + alpha dx (FP64 + FP32), alpha from K
+__global__ void trial_kernel(const double* x, const float* dx, double* out, const NKConsts* K,
+                             float* y32, long long N2) {
+  const double al = K->alpha;
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < N2;
+       p += (long long)gridDim.x * blockDim.x) {
+    const double v = x[p] + al * (double)dx[p];
+    out[p] = v;
+    if (y32) y32[p] = (float)v;
+  }
+}
+
+__global__ void lincomb_kernel(const double* a, double ca, const double* b, double cb, double* out,
+                               float* o32, long long N2) {
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < N2;
+       p += (long long)gridDim.x * blockDim.x) {
+    const double v = ca * a[p] + (b ? cb * b[p] : 0.0);
+    out[p] = v;
+    if (o32) o32[p] = (float)v;
+  }
+}
+
+// partial sums of y^2 (preconditioner Dbar) and the 2N Helmholtz step for the spectral pass
+__global__ void sumsq_kernel(const double* y, double* part, long long N2) {
+  double acc = 0.0;
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < N2;
+       p += (long long)gridDim.x * blockDim.x)
+    acc += y[p] * y[p];
+  __shared__ double red[32];
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) s += red[q];
+    part[blockIdx.x] = s;
+  }
+}
+
+__global__ void sumsq32_kernel(const float* v, double* part, long long N2) {
+  double acc = 0.0;
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < N2;
+       p += (long long)gridDim.x * blockDim.x)
+    acc += (double)v[p] * (double)v[p];
+  __shared__ double red[32];
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) s += red[q];
+    part[blockIdx.x] = s;
+  }
+}
+
+__global__ void nk_consts_kernel(const double* part, int nblk, NKConsts* K, DevState* pst, double n2) {
+  __shared__ double red[32];
+  double acc = 0.0;
+  for (int b = threadIdx.x; b < nblk; b += blockDim.x) acc += part[b];
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x != 0) return;
+  double s = 0.0;
+  for (int q = 0; q < (int)(blockDim.x >> 5); ++q) s += red[q];
+  K->dbar = K->pa + K->pb * s / n2;
+  K->inv_a0 = 1.0 / K->a0;
+  // M^-1 = (1/a0) (I - (beta dbar / a0) Lap)^-1 : Helmholtz step h with D = 1
+  pst->dtc = K->beta * K->dbar / K->a0;
+  pst->done = 0;
+}
+
+// JVP of the current Arnoldi vector V_j (j read on the device)
+// (gs == nullptr: t = J vin for the plain vector vin = V)
+__global__ void vd_jvp_j_kernel(const float* y32, float* V, const GmresState* gs, float* t,
+                                const NKConsts* K, int n, float idx2, float idy2, long long N2) {
+  if (gs && gs->converged) return;
+  const int j = gs ? gs->j : 0;
+  const float* vin = V + (long long)j * N2;
+  const float a = (float)K->pa, b = (float)K->pb, c = (float)K->pc;
+  const float a0 = (float)K->a0, beta = (float)K->beta;
+  const float s = gs ? (float)gs->hnext_inv : 1.0f;
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < N2;
+       p += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(p / n), jj = (int)(p - (long long)i * n);
+    const float uc = y32[p], ue = dval(y32, i, jj + 1, n), uw = dval(y32, i, jj - 1, n);
+    const float un = dval(y32, i + 1, jj, n), us = dval(y32, i - 1, jj, n);
+    const float vc = s * vin[p], ve = s * dval(vin, i, jj + 1, n), vw = s * dval(vin, i, jj - 1, n);
+    const float vn = s * dval(vin, i + 1, jj, n), vs = s * dval(vin, i - 1, jj, n);
+    const float Dc = a + b * uc * uc, De = a + b * ue * ue, Dw = a + b * uw * uw;
+    const float Dn = a + b * un * un, Ds = a + b * us * us;
+    const float dc = 2.f * b * uc * vc, de = 2.f * b * ue * ve, dw = 2.f * b * uw * vw;
+    const float dn = 2.f * b * un * vn, ds = 2.f * b * us * vs;
+    const float gx = 0.5f * (Dc + De) * (ve - vc) + 0.5f * (dc + de) * (ue - uc)
+                   - 0.5f * (Dw + Dc) * (vc - vw) - 0.5f * (dw + dc) * (uc - uw);
+    const float gy = 0.5f * (Dc + Dn) * (vn - vc) + 0.5f * (dc + dn) * (un - uc)
+                   - 0.5f * (Ds + Dc) * (vc - vs) - 0.5f * (ds + dc) * (uc - us);
+    t[p] = a0 * vc - beta * (gx * idx2 + gy * idy2 - 3.f * c * uc * uc * vc);
+  }
+}
+
+__global__ void nk_scale_j_kernel(float* V, const GmresState* gs, long long N2) {
+  if (gs->converged) return;
+  float* v = V + (long long)gs->j * N2;
+  const float s = (float)gs->hnext_inv;
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < N2;
+       p += (long long)gridDim.x * blockDim.x)
+    v[p] *= s;
+}
+
+
+// --------------------------------------------------------------- host driver
+struct NKLayout {
+  size_t y0, y1, y2, cst, R, xt, y32, b32, dx, t, e, V, spec, part, gs, K, pst, total;
+  int nblk, m;
+};
+static inline size_t al(size_t b) { return (b + 255) & ~size_t(255); }
+
+static NKLayout nk_layout(int n, int m) {
+  NKLayout L;
+  const size_t N2 = (size_t)n * n;
+  L.nblk = 152 * 4;
+  L.m = m;
+  size_t o = 0;
+  L.y0 = o; o += al(N2 * 8);
+  L.y1 = o; o += al(N2 * 8);
+  L.y2 = o; o += al(N2 * 8);
+  L.cst = o; o += al(N2 * 8);
+  L.R = o; o += al(N2 * 8);
+  L.xt = o; o += al(N2 * 8);
+  L.y32 = o; o += al(N2 * 4);
+  L.b32 = o; o += al(N2 * 4);
+  L.dx = o; o += al(N2 * 4);
+  L.t = o; o += al(N2 * 4);
+  L.e = o; o += al(4 * N2 * 4);
+  L.V = o; o += al((size_t)(m + 1) * N2 * 4);
+  L.spec = o; o += al((size_t)(2 * n) * spec_ldc(2 * n) * 8);
+  L.part = o; o += al((size_t)(m + 2) * L.nblk * 8);
+  L.gs = o; o += al(sizeof(GmresState));
+  L.K = o; o += al(sizeof(NKConsts));
+  L.pst = o; o += al(sizeof(DevState));
+  L.total = o;
+  return L;
+}
+
+struct NKRun {
+  const void* plan2;  // FP32 plan of the (2n)^2 periodic grid (FD symbol, same spacing)
+  int n;
+  double dy, dx;
+  char* ws;
+  NKLayout L;
+  cudaStream_t s;
+  int grid;  // elementwise grid
+  cudaGraphExec_t arnoldi;
+};
+
+static double* P64(NKRun& r, size_t off) { return (double*)(r.ws + off); }
+static float* P32(NKRun& r, size_t off) { return (float*)(r.ws + off); }
+
+// w = M^-1 src (FP32): odd extension, periodic Helmholtz on (2n)^2, restriction
+static cudaError_t precond(NKRun& r, const float* src, float* w, const GmresState* gs) {
+  const int n = r.n;
+  oddext_kernel<<<r.grid * 4, 256, 0, r.s>>>(src, P32(r, r.L.e), n, gs);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  const PlanView pv = plan_view(r.plan2, 2 * n, 2 * n, 4);
+  cx<float>* spec = (cx<float>*)(r.ws + r.L.spec);
+  RowArgs<float> ro;
+  memset(&ro, 0, sizeof(ro));
+  ro.n = 2 * n; ro.log2n = ilog2_exact(2 * n); ro.ldc = spec_ldc(2 * n); ro.nrows = n; ro.npairs = 1;
+  ro.nseq = row_nseq(2 * n, n); ro.rstride = 2 * n; ro.rin_sel = -1; ro.rout_sel = -1;
+  ro.rin[0] = P32(r, r.L.e); ro.rout[0] = P32(r, r.L.e); ro.spec = spec; ro.tw = (const cx<float>*)pv.twx;
+  ro.inv_scale = 1.0f;
+  ro.pr[0].ra = 0; ro.pr[0].rb = (long long)n * 2 * n; ro.pr[0].sa = 0; ro.pr[0].sb = (long long)n * ro.ldc;
+  ro.pr[0].flags = ROW_STORE_SPEC;
+  // converged Arnoldi steps skip the pass through the state flag of the spectral kernels
+  ro.st = (const DevState*)(r.ws + r.L.pst);
+  if ((e = launch_row<float, RX_NONE>(ro, r.s)) != cudaSuccess) return e;
+  ColArgs<float> c;
+  memset(&c, 0, sizeof(c));
+  c.ny = 2 * n; c.log2ny = ilog2_exact(2 * n); c.ncols = n + 1; c.ldc = ro.ldc;
+  c.C = col_tile(2 * n, c.ncols, 1, 4); c.spec = spec; c.lamx = (const float*)pv.lamx;
+  c.lamy = (const float*)pv.lamy; c.tw = (const cx<float>*)pv.twy;
+  c.scale = (float)(1.0 / (4.0 * n * n)); c.st = ro.st; c.njobs = 1;
+  c.job[0].nout = 1; c.job[0].mul = MUL_HELMHOLTZ; c.job[0].D = 1.0; c.job[0].hfac[0] = c.job[0].hfac[1] = 1.0;
+  c.job[0].pow[0] = c.job[0].pow[1] = 1;
+  if ((e = launch_col<float>(c, r.s)) != cudaSuccess) return e;
+  ro.pr[0].flags = ROW_LOAD_SPEC | ROW_STORE_REAL;
+  if ((e = launch_row<float, RX_NONE>(ro, r.s)) != cudaSuccess) return e;
+  restrict_kernel<<<r.grid, 256, 0, r.s>>>(P32(r, r.L.e), w, n, (const NKConsts*)(r.ws + r.L.K), gs);
+  return cudaGetLastError();
+}
+
+static cudaError_t arnoldi_step(NKRun& r, cudaGraphConditionalHandle h, int use_handle) {
+  const long long N2 = (long long)r.n * r.n;
+  GmresState* gs = (GmresState*)(r.ws + r.L.gs);
+  NKConsts* K = (NKConsts*)(r.ws + r.L.K);
+  double* part = P64(r, r.L.part);
+  // V_j arrives unnormalised: the JVP applies 1/|V_j| on the fly, then V_j is normalised in place
+  // (the index j lives on the device, so the kernels get V and read j themselves)
+  float* V = P32(r, r.L.V);
+  float* t = P32(r, r.L.t);
+  cudaError_t e;
+  vd_jvp_j_kernel<<<r.grid, 256, 0, r.s>>>(P32(r, r.L.y32), V, gs, t, K, r.n,
+                                           (float)(1.0 / (r.dx * r.dx)), (float)(1.0 / (r.dy * r.dy)), N2);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  nk_scale_j_kernel<<<r.grid, 256, 0, r.s>>>(V, gs, N2);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  if ((e = precond(r, t, t, gs)) != cudaSuccess) return e;
+  gmres_dots_kernel<<<r.L.nblk, 256, 0, r.s>>>(V, t, gs, part, N2);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  gmres_hcol_kernel<<<1, 256, 0, r.s>>>(part, r.L.nblk, gs);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  gmres_orth_kernel<<<r.L.nblk, 256, 0, r.s>>>(V, t, gs, part, N2);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  gmres_givens_kernel<<<1, 256, 0, r.s>>>(part, r.L.nblk, gs, h, use_handle);
+  return cudaGetLastError();
+}
+
+static cudaError_t build_arnoldi_graph(NKRun& r) {
+  cudaStream_t cs = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaError_t ce = cudaSuccess;
+  r.arnoldi = nullptr;
+  do {
+    if ((ce = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking)) != cudaSuccess) break;
+    if ((ce = cudaGraphCreate(&graph, 0)) != cudaSuccess) break;
+    cudaGraphConditionalHandle hdl;
+    if ((ce = cudaGraphConditionalHandleCreate(&hdl, graph, 1, cudaGraphCondAssignDefault)) != cudaSuccess) break;
+    cudaGraphNodeParams np = {cudaGraphNodeTypeConditional};
+    np.conditional.handle = hdl;
+    np.conditional.type = cudaGraphCondTypeWhile;
+    np.conditional.size = 1;
+    cudaGraphNode_t node;
+    if ((ce = cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, &np)) != cudaSuccess) break;
+    cudaGraph_t body = np.conditional.phGraph_out[0];
+    NKRun rc = r;
+    rc.s = cs;
+    if ((ce = cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) break;
+    const cudaError_t le = arnoldi_step(rc, hdl, 1);
+    cudaGraph_t captured = nullptr;
+    ce = cudaStreamEndCapture(cs, &captured);
+    if (le != cudaSuccess) { ce = le; break; }
+    if (ce != cudaSuccess) break;
+    ce = cudaGraphInstantiate(&r.arnoldi, graph, 0);
+  } while (0);
+  if (graph) cudaGraphDestroy(graph);
+  if (cs) cudaStreamDestroy(cs);
+  return ce;
+}
+
+static cudaError_t norm_of(NKRun& r, double* part_dev, double* host_out) {
+  // the residual kernel already left per-block partial sums in part_dev
+  double h[152 * 4];
+  cudaError_t e = cudaMemcpyAsync(h, part_dev, sizeof(double) * r.L.nblk, cudaMemcpyDeviceToHost, r.s);
+  if (e != cudaSuccess) return e;
+  if ((e = cudaStreamSynchronize(r.s)) != cudaSuccess) return e;
+  double s = 0.0;
+  for (int i = 0; i < r.L.nblk; ++i) s += h[i];
+  *host_out = sqrt(s);
+  return cudaSuccess;
+}
+
+// R(x) into R (FP64), optionally -R into b32; returns |R|
+static cudaError_t residual(NKRun& r, const double* x, double* rnorm, bool rhs) {
+  NKConsts* K = (NKConsts*)(r.ws + r.L.K);
+  vd_residual_kernel<<<r.L.nblk, 256, 0, r.s>>>(x, P64(r, r.L.cst), P64(r, r.L.R),
+                                                rhs ? P32(r, r.L.b32) : nullptr, P64(r, r.L.part), K,
+                                                r.n, 1.0 / (r.dx * r.dx), 1.0 / (r.dy * r.dy));
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  return norm_of(r, P64(r, r.L.part), rnorm);
+}
+
+struct NKParamsC {
+  int max_newton, max_krylov, restart, max_backtrack;
+  double newton_tol, krylov_tol, damping, backtrack, min_decrease;
+};
+
+// Newton on R(x) = 0 from the guess in x (FP64, updated in place)
+static cudaError_t newton(NKRun& r, double* x, const NKParamsC& P, int* n_newton, int* n_lin,
+                          int* conv_out, double* res_out) {
+  const long long N2 = (long long)r.n * r.n;
+  NKConsts* K = (NKConsts*)(r.ws + r.L.K);
+  GmresState* gs = (GmresState*)(r.ws + r.L.gs);
+  float* y32 = P32(r, r.L.y32);
+  float* dx = P32(r, r.L.dx);
+  float* V = P32(r, r.L.V);
+  float* t = P32(r, r.L.t);
+  double* part = P64(r, r.L.part);
+  double* xt = P64(r, r.L.xt);
+  const float idx2 = (float)(1.0 / (r.dx * r.dx)), idy2 = (float)(1.0 / (r.dy * r.dy));
+  cudaError_t e;
+  double rn;
+  lincomb_kernel<<<r.grid, 256, 0, r.s>>>(x, 1.0, nullptr, 0.0, x, y32, N2);
+  if ((e = residual(r, x, &rn, true)) != cudaSuccess) return e;
+  int converged = rn < P.newton_tol;  // initial state (newton_krylov.py:338-346)
+  int it = 0, lits = 0;
+  double res = rn;
+  bool have_r = true;  // R and b32 hold R(x), y32 holds x
+  while (it < P.max_newton && !converged) {
+    if (!have_r) {
+      lincomb_kernel<<<r.grid, 256, 0, r.s>>>(x, 1.0, nullptr, 0.0, x, y32, N2);
+      if ((e = residual(r, x, &rn, true)) != cudaSuccess) return e;
+    }
+    converged = rn < P.newton_tol;  // evaluated before the update (newton_krylov.py:249-254)
+    // restarted GMRES on M^-1 J dx = -M^-1 R
+    if ((e = cudaMemsetAsync(dx, 0, sizeof(float) * N2, r.s)) != cudaSuccess) return e;
+    for (int cyc = 0; cyc < P.max_krylov; ++cyc) {
+      const float* src = P32(r, r.L.b32);
+      if (cyc > 0) {  // r = b - J dx
+        vd_jvp_j_kernel<<<r.grid, 256, 0, r.s>>>(y32, dx, nullptr, t, K, r.n, idx2, idy2, N2);
+        sub_kernel<<<r.grid, 256, 0, r.s>>>(P32(r, r.L.b32), t, t, N2);
+        src = t;
+      }
+      if ((e = precond(r, src, V, nullptr)) != cudaSuccess) return e;
+      sumsq32_kernel<<<r.L.nblk, 256, 0, r.s>>>(V, part, N2);
+      gmres_init_kernel<<<1, 256, 0, r.s>>>(part, r.L.nblk, gs, cyc == 0, P.krylov_tol, P.restart);
+      if ((e = cudaGetLastError()) != cudaSuccess) return e;
+      if ((e = cudaGraphLaunch(r.arnoldi, r.s)) != cudaSuccess) return e;
+      gmres_solve_kernel<<<1, 1, 0, r.s>>>(gs);
+      gmres_update_kernel<<<r.grid, 256, 0, r.s>>>(dx, V, gs, N2);
+      if ((e = cudaGetLastError()) != cudaSuccess) return e;
+      int hdr[4];
+      if ((e = cudaMemcpyAsync(hdr, gs, sizeof(hdr), cudaMemcpyDeviceToHost, r.s)) != cudaSuccess) return e;
+      if ((e = cudaStreamSynchronize(r.s)) != cudaSuccess) return e;
+      lits += hdr[3];  // k_used
+      if (hdr[2]) break;  // converged
+    }
+    // backtracking line search (newton_krylov.py:270-316)
+    double alpha = P.damping, rb = rn;
+    bool acc = false;
+    for (int bt = 0; bt < P.max_backtrack && !acc; ++bt) {
+      if ((e = cudaMemcpyAsync(&K->alpha, &alpha, sizeof(double), cudaMemcpyHostToDevice, r.s)) != cudaSuccess) return e;
+      trial_kernel<<<r.grid, 256, 0, r.s>>>(x, dx, xt, K, nullptr, N2);
+      double rnn;
+      if ((e = residual(r, xt, &rnn, true)) != cudaSuccess) return e;
+      if (rnn < (1.0 - P.min_decrease * alpha) * rb) {
+        acc = true;
+        rb = rnn;
+        if ((e = cudaMemcpyAsync(x, xt, sizeof(double) * N2, cudaMemcpyDeviceToDevice, r.s)) != cudaSuccess) return e;
+      } else {
+        alpha *= P.backtrack;
+      }
+    }
+    if (acc) {
+      have_r = true;  // R/b32 hold R(x_new); refresh the FP32 copy
+      lincomb_kernel<<<r.grid, 256, 0, r.s>>>(x, 1.0, nullptr, 0.0, x, y32, N2);
+      rn = rb;
+    } else {
+      // no try accepted: full damped step (newton_krylov.py:318-322)
+      if ((e = cudaMemcpyAsync(&K->alpha, &P.damping, sizeof(double), cudaMemcpyHostToDevice, r.s)) != cudaSuccess) return e;
+      trial_kernel<<<r.grid, 256, 0, r.s>>>(x, dx, x, K, y32, N2);
+      have_r = false;
+    }
+    res = rb;
+    ++it;
+  }
+  if ((e = cudaStreamSynchronize(r.s)) != cudaSuccess) return e;
+  *n_newton = it; *n_lin = lits; *conv_out = converged; *res_out = res;
+  return cudaSuccess;
+}
+
+}  // namespace mjx
+
+using namespace mjx;
+
+extern "C" {
+
+size_t mjx_nk_vardiff_ws_bytes(int n, int restart) {
+  if (ilog2_exact(n) < 1 || n > 2048 || restart < 1 || restart > NK_MAXM) return 0;
+  return nk_layout(n, restart).total;
+}
+
+mjx_status mjx_nk_vardiff_integrate2d(const void* plan2, int n, double dy, double dx,
+                                      const double* model_abc, int method, double dt, int n_steps,
+                                      int be_guess_previous, const mjx_nk_params* nkp,
+                                      const double* y0, double* y_out, int* stats, void* ws,
+                                      size_t ws_bytes, void* stream) {
+  if (plan2 == nullptr || model_abc == nullptr || nkp == nullptr || y0 == nullptr || y_out == nullptr)
+    return MJX_BAD_ARG;
+  if (ilog2_exact(n) < 1 || n > 2048 || !(dx > 0) || !(dy > 0) || n_steps < 0) return MJX_BAD_SHAPE;
+  if (method != MJX_METHOD_BE && method != MJX_METHOD_CN && method != MJX_METHOD_BDF2) return MJX_BAD_ARG;
+  if (nkp->restart < 1 || nkp->restart > NK_MAXM) return MJX_BAD_ARG;
+  NKRun r;
+  r.plan2 = plan2; r.n = n; r.dy = dy; r.dx = dx; r.ws = (char*)ws; r.L = nk_layout(n, nkp->restart);
+  r.s = (cudaStream_t)stream;
+  r.grid = 152 * 4;
+  if (ws == nullptr || ws_bytes < r.L.total) return MJX_WORKSPACE;
+  MJX_TRY(ensure_kernel_attrs());
+  const long long N2 = (long long)n * n;
+  NKConsts* K = (NKConsts*)(r.ws + r.L.K);
+  DevState* pst = (DevState*)(r.ws + r.L.pst);
+  MJX_CUDA_TRY(cudaMemsetAsync(pst, 0, sizeof(DevState), r.s));
+  NKParamsC P;
+  P.max_newton = nkp->max_newton_iters; P.max_krylov = nkp->max_krylov_iters; P.restart = nkp->restart;
+  P.max_backtrack = nkp->max_backtrack; P.newton_tol = nkp->newton_tol; P.krylov_tol = nkp->krylov_tol;
+  P.damping = nkp->damping; P.backtrack = nkp->backtrack_factor; P.min_decrease = nkp->min_residual_decrease;
+  MJX_CUDA_TRY(build_arnoldi_graph(r));
+  double* yp = P64(r, r.L.y0);   // y_{n-1}
+  double* yc = P64(r, r.L.y1);   // y_n
+  double* yn = P64(r, r.L.y2);   // Newton iterate
+  double* cst = P64(r, r.L.cst);
+  MJX_CUDA_TRY(cudaMemcpyAsync(yc, y0, sizeof(double) * N2, cudaMemcpyDeviceToDevice, r.s));
+  MJX_CUDA_TRY(cudaMemcpyAsync(yp, y0, sizeof(double) * N2, cudaMemcpyDeviceToDevice, r.s));
+  mjx_status rc = MJX_OK;
+  for (int step = 0; step < n_steps && rc == MJX_OK; ++step) {
+    // residual coefficients (newton_krylov.py:362-448)
+    NKConsts h;
+    memset(&h, 0, sizeof(h));
+    h.pa = model_abc[0]; h.pb = model_abc[1]; h.pc = model_abc[2];
+    const bool be = method == MJX_METHOD_BE || (method == MJX_METHOD_BDF2 && step == 0);
+    double a1 = -1.0, a2 = 0.0;
+    if (be) { h.a0 = 1.0; h.beta = dt; }
+    else if (method == MJX_METHOD_BDF2) {  // omega = dt/dt_prev = 1
+      const double om = 1.0;
+      h.a0 = (1 + 2 * om) / (1 + om); a1 = -(1 + om); a2 = om * om / (1 + om); h.beta = dt * (1 + om) / (1 + 2 * om);
+    } else {  // CN: R = y - y_n - dt/2 (F_n + F(y)); F_n folded into cst below
+      h.a0 = 1.0; h.beta = 0.5 * dt;
+    }
+    h.alpha = 1.0;
+    cudaError_t e = cudaMemcpyAsync(K, &h, sizeof(h), cudaMemcpyHostToDevice, r.s);
+    if (e == cudaSuccess) {
+      // cst = a1 y_n + a2 y_{n-1} (CN: -y_n - dt/2 F(y_n), through the residual kernel at y_n)
+      if (method == MJX_METHOD_CN) {
+        // R(y_n) with cst = 0: a0 y_n - beta F(y_n); cst = -y_n - beta F(y_n) = R(y_n) - 2 y_n
+        lincomb_kernel<<<r.grid, 256, 0, r.s>>>(yc, 0.0, nullptr, 0.0, cst, nullptr, N2);
+        vd_residual_kernel<<<r.L.nblk, 256, 0, r.s>>>(yc, cst, P64(r, r.L.R), nullptr, P64(r, r.L.part), K,
+                                                      n, 1.0 / (dx * dx), 1.0 / (dy * dy));
+        lincomb_kernel<<<r.grid, 256, 0, r.s>>>(P64(r, r.L.R), 1.0, yc, -2.0, cst, nullptr, N2);
+      } else {
+        lincomb_kernel<<<r.grid, 256, 0, r.s>>>(yc, a1, yp, a2, cst, nullptr, N2);
+      }
+      // initial guess: BE -> explicit Euler (stepping.py:195-196) or y_n; BDF2 -> 2 y_n - y_{n-1};
+      // CN -> explicit Euler
+      if (method == MJX_METHOD_BDF2 && !be) {
+        lincomb_kernel<<<r.grid, 256, 0, r.s>>>(yc, 2.0, yp, -1.0, yn, nullptr, N2);
+      } else if (be && be_guess_previous) {
+        lincomb_kernel<<<r.grid, 256, 0, r.s>>>(yc, 1.0, nullptr, 0.0, yn, nullptr, N2);
+      } else {
+        // y_n + dt F(y_n): residual with a0 = 0, beta = -dt, cst = y_n gives y_n + dt F(y_n)
+        NKConsts ge = h;
+        ge.a0 = 0.0; ge.beta = -dt;
+        e = cudaMemcpyAsync(K, &ge, sizeof(ge), cudaMemcpyHostToDevice, r.s);
+        if (e == cudaSuccess) {
+          vd_residual_kernel<<<r.L.nblk, 256, 0, r.s>>>(yc, yc, yn, nullptr, P64(r, r.L.part), K,
+                                                        n, 1.0 / (dx * dx), 1.0 / (dy * dy));
+          e = cudaMemcpyAsync(K, &h, sizeof(h), cudaMemcpyHostToDevice, r.s);
+        }
+      }
+    }
+    if (e == cudaSuccess) {
+      // preconditioner constants from y_n
+      sumsq_kernel<<<r.L.nblk, 256, 0, r.s>>>(yc, P64(r, r.L.part), N2);
+      nk_consts_kernel<<<1, 256, 0, r.s>>>(P64(r, r.L.part), r.L.nblk, K, pst, (double)N2);
+      e = cudaGetLastError();
+    }
+    int nn = 0, nl = 0, cv = 0;
+    double res = 0.0;
+    if (e == cudaSuccess) e = newton(r, yn, P, &nn, &nl, &cv, &res);
+    if (e != cudaSuccess) { set_last_error(e, __FILE__, __LINE__); rc = MJX_CUDA_ERROR; break; }
+    if (stats) { stats[3 * step] = nn; stats[3 * step + 1] = nl; stats[3 * step + 2] = cv; }
+    // rotate y_{n-1} <- y_n <- y_{n+1}
+    double* tmp = yp; yp = yc; yc = yn; yn = tmp;
+  }
+  if (rc == MJX_OK) {
+    cudaError_t e = cudaMemcpyAsync(y_out, yc, sizeof(double) * N2, cudaMemcpyDeviceToDevice, r.s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(r.s);
+    if (e != cudaSuccess) { set_last_error(e, __FILE__, __LINE__); rc = MJX_CUDA_ERROR; }
+  }
+  if (r.arnoldi) cudaGraphExecDestroy(r.arnoldi);
+  return rc;
+}
+
+}  // extern "C"
+
