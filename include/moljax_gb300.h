@@ -192,7 +192,7 @@ size_t mjx_nk_vardiff_ws_bytes(int n, int restart);
  * Hessenberg/Givens least squares in FP64 on the GPU, preconditioner
  * (alpha0 I - beta Dbar Lap_D)^-1 (DST diagonal via the odd extension,
  * plan2 = FP32 FD plan of the (2n)^2 periodic grid with the same spacing).
- * BE initial guess: explicit Euler (stepping.py:195-196) or, with
+ * BE/CN initial guess: explicit Euler (stepping.py:195-196, 242-243) or, with
  * be_guess_previous != 0, y_n.  stats (optional, 3 ints per step): Newton
  * iterations, GMRES iterations, converged. */
 mjx_status mjx_nk_vardiff_integrate2d(const void* plan2, int n, double dy, double dx,

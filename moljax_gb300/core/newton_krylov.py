@@ -64,8 +64,9 @@ def integrate_implicit_vardiff(u0: torch.Tensor, dx: float, dt: float, n_steps: 
     """Fixed-dt implicit steps on the GPU; u0 is an (n, n) interior (FP64 state).
 
     method: "be", "cn" or "bdf2" (BE first step, stepping.py:1077-1139).
-    be_guess: "euler" (be_step's explicit Euler guess, stepping.py:195-196) or
-    "previous" (start Newton from y_n).  Returns (u, stats) where stats is an
+    be_guess: "euler" (the explicit Euler guess of be_step/cn_step,
+    stepping.py:195-196, 242-243) or "previous" (start Newton from y_n); BDF2
+    steps always start from 2 y_n - y_{n-1} (stepping.py:299-300).  Returns (u, stats) where stats is an
     (n_steps, 3) int tensor of (Newton iterations, GMRES iterations, converged).
     """
     from moljax_gb300.core.fft_solvers import get_plan, workspace

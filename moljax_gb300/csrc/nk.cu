@@ -727,7 +727,7 @@ mjx_status mjx_nk_vardiff_integrate2d(const void* plan2, int n, double dy, doubl
       // CN -> explicit Euler
       if (method == MJX_METHOD_BDF2 && !be) {
         lincomb_kernel<<<r.grid, 256, 0, r.s>>>(yc, 2.0, yp, -1.0, yn, nullptr, N2);
-      } else if (be && be_guess_previous) {
+      } else if ((be || method == MJX_METHOD_CN) && be_guess_previous) {
         lincomb_kernel<<<r.grid, 256, 0, r.s>>>(yc, 1.0, nullptr, 0.0, yn, nullptr, N2);
       } else {
         // y_n + dt F(y_n): residual with a0 = 0, beta = -dt, cst = y_n gives y_n + dt F(y_n)

@@ -41,7 +41,7 @@ def _oracle(u0, dx, dt, n, method):
         if method == "be":
             a0, beta, cst, guess = 1.0, dt, -u, u.copy()
         else:
-            a0, beta, cst, guess = 1.0, 0.5 * dt, -u - 0.5 * dt * F(u), u + dt * F(u)
+            a0, beta, cst, guess = 1.0, 0.5 * dt, -u - 0.5 * dt * F(u), u.copy()
         Db = 1.0 + float(np.mean(u * u))
         res = lambda y: a0 * y + cst - beta * F(y)  # noqa: E731
         jvp = lambda y, v: a0 * v - beta * J(y, v)  # noqa: E731
