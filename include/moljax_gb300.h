@@ -147,6 +147,12 @@ mjx_status mjx_rhs2d(const void* padded_in, void* padded_out, int nfields, int n
                      const int* kinds, const double* values, double dy, double dx, int dtype,
                      void* stream);
 
+/* 1D stencils on padded fields [nfields][nx+2g], output ghosts 0: op 0 Laplacian
+ * (laplacian_1d, operators.py:141-152), 1 first-order upwind d/dx for velocity v
+ * (d1_upwind_1d, 64-110: backward if v >= 0), 2 central d/dx (d1_central_1d, 35-61). */
+mjx_status mjx_stencil1d(const void* padded_in, void* padded_out, int nfields, int nx, int n_ghost,
+                        int op, double v, double dx, int dtype, void* stream);
+
 /* ---- IMEX-Strang (diffusion implicit by FFT, reaction explicit Heun) ------------- */
 size_t mjx_imex2d_ws_bytes(int ny, int nx, int nfields, int dtype);
 
@@ -200,6 +206,33 @@ mjx_status mjx_nk_vardiff_integrate2d(const void* plan2, int n, double dy, doubl
                                       int be_guess_previous, const mjx_nk_params* nkp,
                                       const double* y0, double* y_out, int* stats, void* ws,
                                       size_t ws_bytes, void* stream);
+
+/* ---- 1D tubular reactor, Crank-Nicolson, batched --------------------------------- */
+typedef enum mjx_reactor_variant {
+  MJX_REACTOR_DANCKWERTS = 0, /* benchmarks/benchmark_reactor_vs_diffrax.py:40-138 */
+  MJX_REACTOR_DIRICHLET = 1   /* benchmarks/benchmark_method_comparison.py:56-160 */
+} mjx_reactor_variant;
+
+/* One reactor solve of c_t = c_zz/Pe - c_z - Da c: n points, n_steps fixed CN
+ * steps of dt from the uniform state c_init (the Dirichlet variant also sets
+ * c[0] = c_inlet, as benchmark_method_comparison.py:188-190). */
+typedef struct mjx_reactor_instance {
+  int n, variant, n_steps, pad;
+  long long offset;    /* element offset of this instance's final state in out */
+  double Pe, Da, dt, c_init, c_inlet;
+} mjx_reactor_instance;
+
+/* Dynamic shared memory of one instance of size n. */
+size_t mjx_reactor_smem_bytes(int n, int dtype);
+/* n_inst independent reactor solves of different sizes and parameters in one
+ * launch (one CTA per instance, every step of an instance in shared memory).
+ * inst_dev: device array of instances; max_n: largest n in the batch (<= 4096
+ * FP64, <= 8192 FP32).  Replaces solve_reactor_cn_jit
+ * (benchmark_reactor_vs_diffrax.py:116-138) and run_reactor_cn
+ * (benchmark_method_comparison.py:134-160), whose dense O(n^2) solves become
+ * a tridiagonal factorisation plus two parallel substitution scans per step. */
+mjx_status mjx_reactor_cn_batch(const mjx_reactor_instance* inst_dev, int n_inst, int max_n,
+                                int dtype, void* out, void* stream);
 
 /* ---- ETDRK4 (Cox-Matthews) for coupled Gray-Scott ------------------------------ */
 /* Workspace: row spectra ZU/ZN/ZX, 2D spectra U^/N^u/a^/S and the coefficient tables. */

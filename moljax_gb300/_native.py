@@ -52,6 +52,12 @@ class NKParamsC(C.Structure):
                 ("min_residual_decrease", C.c_double)]
 
 
+class ReactorInstanceC(C.Structure):
+    _fields_ = [("n", C.c_int), ("variant", C.c_int), ("n_steps", C.c_int), ("pad", C.c_int),
+                ("offset", C.c_longlong), ("Pe", C.c_double), ("Da", C.c_double),
+                ("dt", C.c_double), ("c_init", C.c_double), ("c_inlet", C.c_double)]
+
+
 class AdaptiveResultC(C.Structure):
     _fields_ = [("t_final", C.c_double), ("dt_next", C.c_double), ("prev_err", C.c_double),
                 ("last_err", C.c_double), ("n_accepted", C.c_int), ("n_rejected", C.c_int),
@@ -75,6 +81,7 @@ SIGNATURES = {
     "mjx_bc_fill2d": (_i, [_vp, _vp, _i, _i, _i, _i, _vp, _vp, _d, _d, _i, _vp]),
     "mjx_unpad2d": (_i, [_vp, _vp, _i, _i, _i, _i, _i, _vp]),
     "mjx_laplacian2d": (_i, [_vp, _vp, _i, _i, _i, _i, _vp, _i, _vp, _vp, _d, _d, _i, _vp]),
+    "mjx_stencil1d": (_i, [_vp, _vp, _i, _i, _i, _i, _d, _d, _i, _vp]),
     "mjx_rhs2d": (_i, [_vp, _vp, _i, _i, _i, _i, _i, _vp, _d, _d, _vp, _vp, _d, _d, _i, _vp]),
     "mjx_imex2d_ws_bytes": (_sz, [_i, _i, _i, _i]),
     "mjx_imex_strang_step2d": (_i, [_vp, C.POINTER(Grid2DC), _i, C.POINTER(ImexProblemC), _d,
@@ -83,6 +90,8 @@ SIGNATURES = {
                                  C.POINTER(PIDParamsC), _d, _d, _d, _i, _i, _vp, _vp,
                                  C.POINTER(C.c_double), C.POINTER(C.c_double), _vp, _vp, _sz,
                                  C.POINTER(AdaptiveResultC), _vp]),
+    "mjx_reactor_smem_bytes": (_sz, [_i, _i]),
+    "mjx_reactor_cn_batch": (_i, [_vp, _i, _i, _i, _vp, _vp]),
     "mjx_nk_vardiff_ws_bytes": (_sz, [_i, _i]),
     "mjx_nk_vardiff_integrate2d": (_i, [_vp, _i, _d, _d, C.POINTER(C.c_double), _i, _d, _i, _i,
                                         C.POINTER(NKParamsC), _vp, _vp, C.POINTER(C.c_int), _vp, _sz,

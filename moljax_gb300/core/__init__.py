@@ -22,3 +22,5 @@ from moljax_gb300.core.newton_krylov import (NKParams, NKStats, newton_krylov_so
                                              integrate_implicit_vardiff)
 from moljax_gb300.core.preconditioners import (DiffusionPreconditioner, IdentityPreconditioner,
                                                BlockJacobiPreconditioner)
+from moljax_gb300.core import reactor, stencil1d
+from moljax_gb300.core.operators import laplacian_1d, gradient_1d, d1_upwind_1d

@@ -1,0 +1,212 @@
+// Batched 1D tubular-reactor Crank-Nicolson: one CTA per instance, the whole
+// time loop of an instance in shared memory.
+//
+// Model c_t = (1/Pe) c_zz - c_z - Da c in two reference discretisations:
+//  MJX_REACTOR_DANCKWERTS  benchmarks/benchmark_reactor_vs_diffrax.py:40-138:
+//    N cells, dz = 1/N, diffusion implicit (CN), upwind advection and
+//    reaction explicit, Danckwerts inlet flux -(c0 - 1)/dz, outlet Neumann row.
+//  MJX_REACTOR_DIRICHLET   benchmarks/benchmark_method_comparison.py:56-160:
+//    N nodes, dz = 1/(N-1), fully implicit CN of L = D2/Pe - D1 - Da with a
+//    Dirichlet inlet row and the one-sided outlet row.
+// The reference solves with a dense inverse / LU (O(N^2) per step); the system
+// matrix is tridiagonal and constant in time, so each CTA factorises it once
+// (Thomas) and runs every step's two substitution sweeps as parallel affine
+// scans over the CTA (x_i = alpha_i x_{i-1} + beta_i composes associatively).
+#include <math.h>
+#include <string.h>
+
+#include "common.cuh"
+
+namespace mjx {
+
+int elem_size(int dtype);
+void set_last_error(cudaError_t e, const char* file, int line);
+
+struct ReactorArgs {
+  const mjx_reactor_instance* inst;
+  void* out;          // concatenated states, instance i at inst[i].offset
+  int n_inst;
+};
+
+// affine map y -> a y + b, composition "first p then q"
+template <typename T> struct Aff { T a, b; };
+template <typename T> __device__ __forceinline__ Aff<T> comp(Aff<T> p, Aff<T> q) {
+  Aff<T> r; r.a = q.a * p.a; r.b = q.a * p.b + q.b; return r;
+}
+
+// Inclusive scan of x_i = al[i] x_{i-1} + be[i] (x_{-1} = 0) over n elements in
+// smem, processed in order ord(i) (forward, or reverse when REV).  Result in be[].
+template <typename T, bool REV>
+__device__ void affine_scan(T* al, T* be, int n, Aff<T>* wsum) {
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int per = (n + nt - 1) / nt;
+  const int lo = tid * per, hi = min(n, lo + per);
+  auto idx = [&](int i) { return REV ? n - 1 - i : i; };
+  Aff<T> acc; acc.a = (T)1; acc.b = (T)0;
+  for (int i = lo; i < hi; ++i) {
+    Aff<T> e; e.a = al[idx(i)]; e.b = be[idx(i)];
+    acc = comp(acc, e);
+  }
+  // warp inclusive scan of the thread aggregates
+  const int lane = tid & 31, w = tid >> 5;
+  Aff<T> inc = acc;
+  for (int o = 1; o < 32; o <<= 1) {
+    Aff<T> up;
+    up.a = __shfl_up_sync(0xffffffffu, inc.a, o);
+    up.b = __shfl_up_sync(0xffffffffu, inc.b, o);
+    if (lane >= o) inc = comp(up, inc);
+  }
+  if (lane == 31) wsum[w] = inc;
+  __syncthreads();
+  if (tid == 0) {  // scan of the warp totals (<= 32 warps)
+    Aff<T> run; run.a = (T)1; run.b = (T)0;
+    for (int q = 0; q < (nt >> 5); ++q) { run = comp(run, wsum[q]); wsum[q] = run; }
+  }
+  __syncthreads();
+  // exclusive prefix for this thread
+  Aff<T> ex;
+  Aff<T> up;
+  up.a = __shfl_up_sync(0xffffffffu, inc.a, 1);
+  up.b = __shfl_up_sync(0xffffffffu, inc.b, 1);
+  if (lane == 0) { ex.a = (T)1; ex.b = (T)0; } else { ex = up; }
+  if (w > 0) ex = comp(wsum[w - 1], ex);
+  T y = ex.b;  // value x_{lo-1} (the composite applied to x_{-1} = 0)
+  __syncthreads();
+  for (int i = lo; i < hi; ++i) {
+    y = al[idx(i)] * y + be[idx(i)];
+    be[idx(i)] = y;
+  }
+  __syncthreads();
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) reactor_kernel(ReactorArgs A) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const mjx_reactor_instance I = A.inst[blockIdx.x];
+  const int n = I.n;
+  T* c = reinterpret_cast<T*>(smem_raw);   // state
+  T* d = c + n;                            // rhs / scan values
+  T* al = d + n;                           // forward scan coefficients -a_i m_i
+  T* m = al + n;                           // pivots 1/(b_i - a_i c'_{i-1})
+  T* cp = m + n;                           // c'_i  (backward coefficients are -c'_i)
+  Aff<T>* wsum = reinterpret_cast<Aff<T>*>(cp + n);
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const double Pe = I.Pe, Da = I.Da, dt = I.dt;
+  const bool dk = I.variant == MJX_REACTOR_DANCKWERTS;
+  const double dz = dk ? 1.0 / n : 1.0 / (n - 1);
+  // tridiagonal entries of the implicit matrix and of the explicit operator
+  double kap = 0, Ls = 0, Ld = 0, Lp = 0, Lsl = 0, Ldl = 0;
+  if (dk) {
+    kap = 0.5 * dt / (Pe * dz * dz);
+  } else {
+    const double q = (1.0 / Pe) / (dz * dz);
+    Ls = q + 1.0 / dz; Ld = -2.0 * q - 1.0 / dz - Da; Lp = q;   // rows 1..N-2
+    Lsl = q; Ldl = -q - 1.0 / dz - Da;                           // row N-1
+  }
+  auto sub = [&](int i) -> double {  // A[i][i-1]
+    if (dk) return i == n - 1 ? -2.0 * kap : -kap;
+    if (i == 0) return 0.0;
+    return i == n - 1 ? -0.5 * dt * Lsl : -0.5 * dt * Ls;
+  };
+  auto dia = [&](int i) -> double {
+    if (dk) return 1.0 + 2.0 * kap;
+    if (i == 0) return 1.0;
+    return i == n - 1 ? 1.0 - 0.5 * dt * Ldl : 1.0 - 0.5 * dt * Ld;
+  };
+  auto sup = [&](int i) -> double {  // A[i][i+1]
+    if (dk) return i == n - 1 ? 0.0 : -kap;
+    if (i == 0 || i == n - 1) return 0.0;
+    return -0.5 * dt * Lp;
+  };
+  // Thomas factorisation once (sequential, FP64)
+  if (tid == 0) {
+    double cprev = 0.0;
+    for (int i = 0; i < n; ++i) {
+      const double mi = 1.0 / (dia(i) - sub(i) * cprev);
+      m[i] = (T)mi;
+      al[i] = (T)(-sub(i) * mi);
+      cprev = sup(i) * mi;
+      cp[i] = (T)cprev;
+    }
+  }
+  for (int i = tid; i < n; i += nt) c[i] = (T)I.c_init;
+  if (!dk && tid == 0) c[0] = (T)I.c_inlet;
+  __syncthreads();
+  const T idz = (T)(1.0 / dz), Dat = (T)Da, dtt = (T)dt, kp = (T)kap;
+  const T half_dt = (T)(0.5 * dt);
+  for (int step = 0; step < I.n_steps; ++step) {
+    // right-hand side
+    for (int i = tid; i < n; i += nt) {
+      const T ci = c[i];
+      T r;
+      if (dk) {
+        const T cl = i > 0 ? c[i - 1] : (T)0, cr = i < n - 1 ? c[i + 1] : (T)0;
+        T lap;  // (L c)_i dz^2
+        if (i == n - 1) lap = (T)2 * cl - (T)2 * ci;
+        else lap = cl - (T)2 * ci + cr;
+        const T adv = i == 0 ? -(ci - (T)1) * idz : -(ci - cl) * idz;
+        r = ci + kp * lap + dtt * (adv - Dat * ci);
+      } else {
+        if (i == 0) {
+          r = (T)I.c_inlet;
+        } else {
+          const T cl = c[i - 1];
+          T Lc;
+          if (i == n - 1) Lc = (T)Lsl * cl + (T)Ldl * ci;
+          else Lc = (T)Ls * cl + (T)Ld * ci + (T)Lp * c[i + 1];
+          r = ci + half_dt * Lc;
+        }
+      }
+      d[i] = r * m[i];  // beta_i of the forward sweep
+    }
+    __syncthreads();
+    affine_scan<T, false>(al, d, n, wsum);      // d'_i
+    // backward: x_i = d'_i - c'_i x_{i+1}; reuse c[] for the -c' coefficients
+    for (int i = tid; i < n; i += nt) c[i] = -cp[i];
+    __syncthreads();
+    affine_scan<T, true>(c, d, n, wsum);         // x in d[]
+    for (int i = tid; i < n; i += nt) c[i] = d[i];
+    __syncthreads();
+  }
+  T* out = reinterpret_cast<T*>(A.out) + I.offset;
+  for (int i = tid; i < n; i += nt) out[i] = c[i];
+}
+
+}  // namespace mjx
+
+using namespace mjx;
+
+extern "C" {
+
+size_t mjx_reactor_smem_bytes(int n, int dtype) {
+  const int e = elem_size(dtype);
+  if (!e || n < 2) return 0;
+  return (size_t)5 * n * e + 32 * 2 * e;
+}
+
+mjx_status mjx_reactor_cn_batch(const mjx_reactor_instance* inst_dev, int n_inst, int max_n,
+                                int dtype, void* out, void* stream) {
+  const int e = elem_size(dtype);
+  if (!e) return MJX_BAD_DTYPE;
+  if (!inst_dev || !out || n_inst < 0 || max_n < 2) return MJX_BAD_ARG;
+  if (n_inst == 0) return MJX_OK;
+  const size_t smem = mjx_reactor_smem_bytes(max_n, dtype);
+  static int attr_done = 0;
+  if (!attr_done) {
+    int dev = 0, optin = 0;
+    MJX_CUDA_TRY(cudaGetDevice(&dev));
+    MJX_CUDA_TRY(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    MJX_CUDA_TRY(cudaFuncSetAttribute(reactor_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
+    MJX_CUDA_TRY(cudaFuncSetAttribute(reactor_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
+    attr_done = 1;
+  }
+  if (smem > 227 * 1024) return MJX_BAD_SHAPE;
+  ReactorArgs A;
+  A.inst = inst_dev; A.out = out; A.n_inst = n_inst;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (e == 4) reactor_kernel<float><<<n_inst, 256, smem, s>>>(A);
+  else reactor_kernel<double><<<n_inst, 256, smem, s>>>(A);
+  return cuda_status(cudaGetLastError());
+}
+
+}  // extern "C"

@@ -174,6 +174,27 @@ static mjx_status check_pad(int nf, int ny, int nx, int g, const int* kinds) {
   return MJX_OK;
 }
 
+// 1D stencils on padded fields [nf][nx+2g] (ghosts read as stored; output ghosts 0):
+// op 0: Laplacian (operators.py:113-152), 1: upwind d/dx with velocity v (64-110),
+// 2: central d/dx (35-61)
+template <typename T>
+__global__ void stencil1d_kernel(const T* __restrict__ in, T* __restrict__ out, int nf, int nx, int g,
+                                 int op, double v, double dx) {
+  const int ld = nx + 2 * g;
+  const long long total = (long long)nf * ld;
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < total;
+       p += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(p % ld);
+    if (i < g || i >= nx + g) { out[p] = (T)0; continue; }
+    const T c = in[p], l = in[p - 1], r = in[p + 1];
+    T res;
+    if (op == 0) res = (r - (T)2 * c + l) / (T)(dx * dx);
+    else if (op == 1) res = v >= 0 ? (c - l) / (T)dx : (r - c) / (T)dx;
+    else res = (r - l) / (T)(2.0 * dx);
+    out[p] = res;
+  }
+}
+
 }  // namespace mjx
 
 using namespace mjx;
@@ -239,6 +260,19 @@ mjx_status mjx_laplacian2d(const void* padded_in, void* padded_out, int nfields,
   if (e == 4) { if (fill_bc) MJX_LAP(float, true); else MJX_LAP(float, false); }
   else { if (fill_bc) MJX_LAP(double, true); else MJX_LAP(double, false); }
 #undef MJX_LAP
+  return cuda_status(cudaGetLastError());
+}
+
+mjx_status mjx_stencil1d(const void* padded_in, void* padded_out, int nfields, int nx, int n_ghost,
+                        int op, double v, double dx, int dtype, void* stream) {
+  const int e = elem_size(dtype);
+  if (!e) return MJX_BAD_DTYPE;
+  if (!padded_in || !padded_out || padded_in == padded_out) return MJX_BAD_ARG;
+  if (nfields < 1 || nx < 1 || n_ghost < 1 || op < 0 || op > 2 || !(dx > 0)) return MJX_BAD_ARG;
+  const long long total = (long long)nfields * (nx + 2 * n_ghost);
+  cudaStream_t s = (cudaStream_t)stream;
+  if (e == 4) stencil1d_kernel<float><<<grid_for(total), 256, 0, s>>>((const float*)padded_in, (float*)padded_out, nfields, nx, n_ghost, op, v, dx);
+  else stencil1d_kernel<double><<<grid_for(total), 256, 0, s>>>((const double*)padded_in, (double*)padded_out, nfields, nx, n_ghost, op, v, dx);
   return cuda_status(cudaGetLastError());
 }
 
