@@ -16,6 +16,7 @@ from __future__ import annotations
 
 import ctypes as C
 import math
+import threading
 from typing import Dict, NamedTuple, Optional
 
 import torch
@@ -37,8 +38,9 @@ def _device(device=None):
 
 
 def workspace(nbytes: int, device, tag: str = "ws") -> torch.Tensor:
-    """Reusable device scratch of at least nbytes (one per device and tag)."""
-    key = (str(device), tag)
+    """Reusable device scratch of at least nbytes (one per device, tag and host thread,
+    so that concurrent solves on per-thread streams never share scratch)."""
+    key = (str(device), tag, threading.get_ident())
     buf = _ws.get(key)
     if buf is None or buf.numel() < nbytes:
         buf = torch.empty(max(int(nbytes), 256), dtype=torch.uint8, device=device)
