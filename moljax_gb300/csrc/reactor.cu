@@ -28,6 +28,11 @@ struct ReactorArgs {
   int n_inst;
 };
 
+// shared-memory index with one pad word per 16: the scans give each thread a
+// contiguous chunk (stride = chunk length), which would otherwise hit one bank
+__device__ __forceinline__ int pz(int i) { return i + (i >> 4); }
+__host__ __device__ __forceinline__ int pz_size(int n) { return n + (n >> 4) + 1; }
+
 // affine map y -> a y + b, composition "first p then q"
 template <typename T> struct Aff { T a, b; };
 template <typename T> __device__ __forceinline__ Aff<T> comp(Aff<T> p, Aff<T> q) {
@@ -41,7 +46,7 @@ __device__ void affine_scan(T* al, T* be, int n, Aff<T>* wsum) {
   const int tid = threadIdx.x, nt = blockDim.x;
   const int per = (n + nt - 1) / nt;
   const int lo = tid * per, hi = min(n, lo + per);
-  auto idx = [&](int i) { return REV ? n - 1 - i : i; };
+  auto idx = [&](int i) { return pz(REV ? n - 1 - i : i); };
   Aff<T> acc; acc.a = (T)1; acc.b = (T)0;
   for (int i = lo; i < hi; ++i) {
     Aff<T> e; e.a = al[idx(i)]; e.b = be[idx(i)];
@@ -84,12 +89,13 @@ __global__ void __launch_bounds__(256) reactor_kernel(ReactorArgs A) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const mjx_reactor_instance I = A.inst[blockIdx.x];
   const int n = I.n;
+  const int np = pz_size(n);               // padded length (index through pz)
   T* c = reinterpret_cast<T*>(smem_raw);   // state
-  T* d = c + n;                            // rhs / scan values
-  T* al = d + n;                           // forward scan coefficients -a_i m_i
-  T* m = al + n;                           // pivots 1/(b_i - a_i c'_{i-1})
-  T* cp = m + n;                           // c'_i  (backward coefficients are -c'_i)
-  Aff<T>* wsum = reinterpret_cast<Aff<T>*>(cp + n);
+  T* d = c + np;                           // rhs / scan values
+  T* al = d + np;                          // forward scan coefficients -a_i m_i
+  T* m = al + np;                          // pivots 1/(b_i - a_i c'_{i-1})
+  T* cp = m + np;                          // c'_i  (backward coefficients are -c'_i)
+  Aff<T>* wsum = reinterpret_cast<Aff<T>*>(cp + np);
   const int tid = threadIdx.x, nt = blockDim.x;
   const double Pe = I.Pe, Da = I.Da, dt = I.dt;
   const bool dk = I.variant == MJX_REACTOR_DANCKWERTS;
@@ -123,24 +129,24 @@ __global__ void __launch_bounds__(256) reactor_kernel(ReactorArgs A) {
     double cprev = 0.0;
     for (int i = 0; i < n; ++i) {
       const double mi = 1.0 / (dia(i) - sub(i) * cprev);
-      m[i] = (T)mi;
-      al[i] = (T)(-sub(i) * mi);
+      m[pz(i)] = (T)mi;
+      al[pz(i)] = (T)(-sub(i) * mi);
       cprev = sup(i) * mi;
-      cp[i] = (T)cprev;
+      cp[pz(i)] = (T)cprev;
     }
   }
-  for (int i = tid; i < n; i += nt) c[i] = (T)I.c_init;
-  if (!dk && tid == 0) c[0] = (T)I.c_inlet;
+  for (int i = tid; i < n; i += nt) c[pz(i)] = (T)I.c_init;
+  if (!dk && tid == 0) c[pz(0)] = (T)I.c_inlet;
   __syncthreads();
   const T idz = (T)(1.0 / dz), Dat = (T)Da, dtt = (T)dt, kp = (T)kap;
   const T half_dt = (T)(0.5 * dt);
   for (int step = 0; step < I.n_steps; ++step) {
     // right-hand side
     for (int i = tid; i < n; i += nt) {
-      const T ci = c[i];
+      const T ci = c[pz(i)];
       T r;
       if (dk) {
-        const T cl = i > 0 ? c[i - 1] : (T)0, cr = i < n - 1 ? c[i + 1] : (T)0;
+        const T cl = i > 0 ? c[pz(i - 1)] : (T)0, cr = i < n - 1 ? c[pz(i + 1)] : (T)0;
         T lap;  // (L c)_i dz^2
         if (i == n - 1) lap = (T)2 * cl - (T)2 * ci;
         else lap = cl - (T)2 * ci + cr;
@@ -150,26 +156,26 @@ __global__ void __launch_bounds__(256) reactor_kernel(ReactorArgs A) {
         if (i == 0) {
           r = (T)I.c_inlet;
         } else {
-          const T cl = c[i - 1];
+          const T cl = c[pz(i - 1)];
           T Lc;
           if (i == n - 1) Lc = (T)Lsl * cl + (T)Ldl * ci;
-          else Lc = (T)Ls * cl + (T)Ld * ci + (T)Lp * c[i + 1];
+          else Lc = (T)Ls * cl + (T)Ld * ci + (T)Lp * c[pz(i + 1)];
           r = ci + half_dt * Lc;
         }
       }
-      d[i] = r * m[i];  // beta_i of the forward sweep
+      d[pz(i)] = r * m[pz(i)];  // beta_i of the forward sweep
     }
     __syncthreads();
     affine_scan<T, false>(al, d, n, wsum);      // d'_i
     // backward: x_i = d'_i - c'_i x_{i+1}; reuse c[] for the -c' coefficients
-    for (int i = tid; i < n; i += nt) c[i] = -cp[i];
+    for (int i = tid; i < n; i += nt) c[pz(i)] = -cp[pz(i)];
     __syncthreads();
     affine_scan<T, true>(c, d, n, wsum);         // x in d[]
-    for (int i = tid; i < n; i += nt) c[i] = d[i];
+    for (int i = tid; i < n; i += nt) c[pz(i)] = d[pz(i)];
     __syncthreads();
   }
   T* out = reinterpret_cast<T*>(A.out) + I.offset;
-  for (int i = tid; i < n; i += nt) out[i] = c[i];
+  for (int i = tid; i < n; i += nt) out[i] = c[pz(i)];
 }
 
 }  // namespace mjx
@@ -181,7 +187,7 @@ extern "C" {
 size_t mjx_reactor_smem_bytes(int n, int dtype) {
   const int e = elem_size(dtype);
   if (!e || n < 2) return 0;
-  return (size_t)5 * n * e + 32 * 2 * e;
+  return (size_t)5 * pz_size(n) * e + 32 * 2 * e;
 }
 
 mjx_status mjx_reactor_cn_batch(const mjx_reactor_instance* inst_dev, int n_inst, int max_n,
