@@ -115,6 +115,27 @@ mjx_status mjx_fft_cn2d(const void* plan, const mjx_grid2d* grid, int dtype, dou
                         int n_steps, const void* u_in, void* u_out, void* ws, size_t ws_bytes,
                         void* stream);
 
+/* Size of the fixed device scratch used by mjx_fft_cn2d_noalloc (8 MiB). */
+#define MJX_NOALLOC_SCRATCH_BYTES (8u << 20)
+
+/* mjx_fft_cn2d for callers that cannot call cudaMalloc: an allocator-free
+ * host (an embedded driver loop, a signal-safe or real-time context, a host
+ * whose device memory is owned by another framework's allocator) can still
+ * run FFT-CN steps with only its input and output buffers.  The spectrum
+ * scratch is a fixed 8 MiB array inside the library (held by every GPU that
+ * loads the library until process exit), so the grid must satisfy
+ * mjx_spec2d_ws_bytes(ny, nx, 1, dtype) <= MJX_NOALLOC_SCRATCH_BYTES (e.g.
+ * 1024^2 FP32, 512^2 FP64); larger grids return MJX_WORKSPACE.  The first call
+ * on a device looks up the scratch address once (make that call before any
+ * stream capture).  No device memory is allocated or freed.  All calls share
+ * the one scratch array, so calls that overlap on the GPU (different streams,
+ * or different host threads without ordering) race; nothing in the scratch
+ * needs to start at zero, because each step writes every spectrum entry it
+ * later reads.  No counterpart in the reference. */
+mjx_status mjx_fft_cn2d_noalloc(const void* plan, const mjx_grid2d* grid, int dtype, double D,
+                                double dt, int n_steps, const void* u_in, void* u_out,
+                                void* stream);
+
 /* ---- ghost cells and finite-difference stencils on padded fields ---------------- */
 /* Padded layout: [nfields][ny+2g][nx+2g].  kinds[f] is an mjx_bc_kind; values holds
  * 4 constants per field (left, right, bottom, top): Dirichlet boundary values or

@@ -77,6 +77,7 @@ SIGNATURES = {
     "mjx_spectral_apply2d": (_i, [_vp, C.POINTER(Grid2DC), _i, _i, C.POINTER(C.c_double), _d, _i,
                                   _vp, _vp, _vp, _sz, _vp]),
     "mjx_fft_cn2d": (_i, [_vp, C.POINTER(Grid2DC), _i, _d, _d, _i, _vp, _vp, _vp, _sz, _vp]),
+    "mjx_fft_cn2d_noalloc": (_i, [_vp, C.POINTER(Grid2DC), _i, _d, _d, _i, _vp, _vp, _vp]),
     "mjx_bc_pad2d": (_i, [_vp, _vp, _i, _i, _i, _i, _vp, _vp, _d, _d, _i, _vp]),
     "mjx_bc_fill2d": (_i, [_vp, _vp, _i, _i, _i, _i, _vp, _vp, _d, _d, _i, _vp]),
     "mjx_unpad2d": (_i, [_vp, _vp, _i, _i, _i, _i, _i, _vp]),

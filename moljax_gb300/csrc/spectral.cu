@@ -6,6 +6,7 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <mutex>
 #include <vector>
 
 #include "spectral.cuh"
@@ -517,6 +518,30 @@ mjx_status fft_cn(const void* plan, const mjx_grid2d* g, double D, double dt, in
   return MJX_OK;
 }
 
+// Fixed device scratch for mjx_fft_cn2d_noalloc.  It lives in the library's
+// own device memory: every GPU that loads the library holds these bytes until
+// the process exits.  Host code must not pass the symbol itself to a kernel
+// (in host code it is only a stand-in); the device address comes from
+// cudaGetSymbolAddress, once per device.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[MJX_NOALLOC_SCRATCH_BYTES];
+
+static std::mutex g_noalloc_mu;
+static void* g_noalloc_ptr[64];
+
+static mjx_status noalloc_scratch(void** out) {
+  int dev = 0;
+  MJX_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return MJX_BAD_ARG;
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (g_noalloc_ptr[dev] == nullptr) {
+    void* p = nullptr;
+    MJX_CUDA_TRY(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+    g_noalloc_ptr[dev] = p;
+  }
+  *out = g_noalloc_ptr[dev];
+  return MJX_OK;
+}
+
 }  // namespace mjx
 
 using namespace mjx;
@@ -622,6 +647,24 @@ mjx_status mjx_fft_cn2d(const void* plan, const mjx_grid2d* g, int dtype, double
   const int e = elem_size(dtype);
   if (!e) return MJX_BAD_DTYPE;
   if (ws == nullptr || ws_bytes < mjx_spec2d_ws_bytes(g->ny, g->nx, 1, dtype)) return MJX_WORKSPACE;
+  MJX_TRY(ensure_kernel_attrs());
+  cudaStream_t s = (cudaStream_t)stream;
+  if (e == 4) return fft_cn<float>(plan, g, D, dt, n_steps, (const float*)u_in, (float*)u_out, ws, s);
+  return fft_cn<double>(plan, g, D, dt, n_steps, (const double*)u_in, (double*)u_out, ws, s);
+}
+
+// FFT-CN stepping for callers that cannot allocate device memory: the
+// spectrum scratch is the fixed library buffer above instead of a workspace.
+mjx_status mjx_fft_cn2d_noalloc(const void* plan, const mjx_grid2d* g, int dtype, double D, double dt,
+                                int n_steps, const void* u_in, void* u_out, void* stream) {
+  MJX_TRY(check_grid(g));
+  if (plan == nullptr || u_in == nullptr || u_out == nullptr || n_steps < 0) return MJX_BAD_ARG;
+  const int e = elem_size(dtype);
+  if (!e) return MJX_BAD_DTYPE;
+  // the spectrum of one field must fit the fixed scratch
+  if (mjx_spec2d_ws_bytes(g->ny, g->nx, 1, dtype) > (size_t)MJX_NOALLOC_SCRATCH_BYTES) return MJX_WORKSPACE;
+  void* ws = nullptr;
+  MJX_TRY(noalloc_scratch(&ws));  // first call on a device: symbol lookup (no allocation)
   MJX_TRY(ensure_kernel_attrs());
   cudaStream_t s = (cudaStream_t)stream;
   if (e == 4) return fft_cn<float>(plan, g, D, dt, n_steps, (const float*)u_in, (float*)u_out, ws, s);
