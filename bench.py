@@ -1,17 +1,23 @@
-"""Benchmark: adaptive IMEX-Strang Gray-Scott, 1024^2, FP32, t in (0, 2000).
+"""Benchmark: adaptive IMEX-Strang Gray-Scott, 1024^2, t in (0, 2000).
 
 One "step" is one full adaptive solve over t_span = (0, 2000) (step doubling,
 PI control, accept/reject all on the device).  The metric is
-grid-point-steps/s = interior points x accepted steps / time.
+grid-point-steps/s = interior points x accepted steps / time.  The default
+precision is "mixed": FP64 spectral state, FP32 transforms of the reaction
+increments (rel-L2 vs the FP64 path is reported in the line).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+  python bench.py --kernels-only [--reps R]   # per-kernel CUDA-event times only
 
 Our arm prints one JSON line with the device-timed value, the end-to-end
 number through the public API with host buffers, the live roofline of the
-dominant kernel, the FP32-vs-FP64 error, the CPU baseline and SM clocks.
-``--impl reference`` times the CPU restatement of the reference algorithm
-(NumPy/SciPy FP64, all host threads) on a bounded sample of the same workload.
-The path does not shard: N > 1 runs N independent replicas (one per rank).
+dominant kernel, the error against the FP64 path, the CPU baseline and SM
+clocks.  ``--impl reference`` times the CPU restatement of the reference
+algorithm (NumPy/SciPy FP64, all host threads) on a bounded sample of the same
+workload.  The path does not shard: N > 1 runs N independent replicas (one per
+rank).  ``--kernels-only`` launches each attempt kernel R times through the
+per-kernel entry point and prints their CUDA-event times (the small case the
+kernel profiles are captured on).
 """
 
 from __future__ import annotations
@@ -50,6 +56,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp32"])
+    ap.add_argument("--kernels-only", action="store_true")
+    ap.add_argument("--reps", type=int, default=30)
     return ap.parse_args()
 
 
@@ -181,7 +189,7 @@ def time_kernels_mixed(M, model, cache, diff, y0, dev, reps=30):
     out = {}
     s = torch.cuda.current_stream(dev)
     for w in range(1, 7):
-        for _ in range(3):
+        for _ in range(min(3, reps)):
             call(w)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(s)
@@ -216,7 +224,7 @@ def time_kernels(M, model, cache, diff, y0, dev, reps=30):
     out = {}
     s = torch.cuda.current_stream(dev)
     for w in range(1, 8):
-        for _ in range(3):
+        for _ in range(min(3, reps)):
             call(w)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(s)
@@ -380,6 +388,19 @@ def run_ours(args, rank, world, local):
     return out
 
 
+def run_kernels_only(args, local):
+    import torch
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    M, grid, model, cache, diff, y0 = make_problem(torch.float32, dev, args.n)
+    if args.precision == "mixed":
+        kt = time_kernels_mixed(M, model, cache, diff, y0, dev, reps=args.reps)
+    else:
+        kt = time_kernels(M, model, cache, diff, y0, dev, reps=args.reps)
+    return {"kernels_us": {k: v * 1e6 for k, v in kt.items()}, "precision": args.precision,
+            "n": args.n, "reps": args.reps}
+
+
 # ------------------------------------------------------------------ CPU (oracle) arms
 def cpu_sample(n, attempts, workers):
     """Adaptive IMEX-Strang on the CPU oracle for a bounded number of attempts."""
@@ -412,9 +433,8 @@ def run_reference(args, rank, world):
     if rank != 0:
         return None
     workers = os.cpu_count() or 1
-    cpu_sample(args.n, 1, workers)  # warm the FFT plans
-    for _ in range(max(0, args.warmup - 1)):
-        pass
+    for _ in range(max(1, args.warmup)):  # untimed: warms the FFT plans and caches
+        cpu_sample(args.n, 1, workers)
     vals, tot_units, tot_t = [], 0, 0.0
     att = 8
     for _ in range(args.steps):
@@ -442,6 +462,8 @@ def main():
     rank, world, local = dist_env()
     if args.impl == "reference":
         out = run_reference(args, rank, world)
+    elif args.kernels_only:
+        out = run_kernels_only(args, local)
     else:
         out = run_ours(args, rank, world, local)
     if rank == 0 and out:

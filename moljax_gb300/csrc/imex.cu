@@ -18,6 +18,7 @@
 //   K7 row  SB: c2r -> Y[1-cur] (two half steps) + scaled error vs YF
 //   K8      controller: error norm, accept/reject, PI dt, counters, loop flag
 #include <math.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include "spectral.cuh"
@@ -159,6 +160,14 @@ __global__ void __launch_bounds__(256) controller_kernel(CtlArgs a) {
     else if (st->status == MJX_STATUS_RUNNING_CODE) st->status = MJX_STATUS_MAX_STEPS_CODE;
   }
   if (a.use_handle) cudaGraphSetConditional(a.handle, running ? 1u : 0u);
+}
+
+bool host_loop_mode() {
+  static const int mode = [] {
+    const char* v = getenv("MJX_HOST_LOOP");
+    return (v != nullptr && v[0] == '1') ? 1 : 0;
+  }();
+  return mode == 1;
 }
 
 cudaError_t launch_controller(const CtlArgs& a, cudaStream_t s) {
@@ -368,7 +377,18 @@ static mjx_status adaptive_run(const void* plan, const mjx_grid2d* g, const mjx_
   ca.st = st; ca.partial = (const double*)(ws + L.part); ca.nonfinite = (const int*)(ws + L.bad);
   ca.nparts = L.nparts; ca.n_dof = (double)nelem; ca.pid = *pid; ca.hist_t = hist_t; ca.hist_dt = hist_dt;
 
-  if (running) {
+  if (running && host_loop_mode()) {
+    const cudaError_t e = run_host_loop([&](cudaStream_t ls) -> cudaError_t {
+      cudaError_t le = launch_attempt<T>(A, ls);
+      if (le == cudaSuccess) le = launch_controller(ca, ls);
+      if (le == cudaSuccess && hist_y) {
+        hist_copy_kernel<T><<<304, 256, 0, ls>>>(st, (const T*)(ws + L.y0), (const T*)(ws + L.y1), hist_y, nelem);
+        le = cudaGetLastError();
+      }
+      return le;
+    }, st, h.max_attempts, s);
+    MJX_CUDA_TRY(e);
+  } else if (running) {
     // Graph: while (cond) { attempt; controller sets cond }.
     cudaStream_t cs = nullptr;
     cudaGraph_t graph = nullptr;

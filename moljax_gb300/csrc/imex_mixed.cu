@@ -489,7 +489,13 @@ mjx_status mjx_imex_adaptive2d_mixed(const void* plan32, const void* plan64, con
   memset(&ca, 0, sizeof(ca));
   ca.st = st; ca.partial = (const double*)(w + L.part); ca.nonfinite = (const int*)(w + L.bad);
   ca.nparts = L.nparts; ca.n_dof = (double)nelem; ca.pid = *pid; ca.hist_t = hist_t; ca.hist_dt = hist_dt;
-  if (running) {
+  if (running && host_loop_mode()) {
+    const cudaError_t he = run_host_loop([&](cudaStream_t ls) -> cudaError_t {
+      const cudaError_t le = launch_mix_attempt(A, ls);
+      return le == cudaSuccess ? launch_controller(ca, ls) : le;
+    }, st, h.max_attempts, s);
+    MJX_CUDA_TRY(he);
+  } else if (running) {
     cudaStream_t cs = nullptr;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;

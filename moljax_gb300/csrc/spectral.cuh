@@ -131,6 +131,35 @@ struct CtlArgs {
 cudaError_t launch_controller(const CtlArgs& a, cudaStream_t s);
 int col_tile(int ny, int ncols, int nout, int elem);
 
+// Adaptive-loop driver selection.  The default keeps the whole loop on the
+// device (a CUDA graph whose conditional while node repeats attempt +
+// controller).  With MJX_HOST_LOOP=1 in the environment the host launches the
+// attempts itself, in batches, and reads the done flag between batches:
+// profilers that cannot see kernels inside conditional graphs (Nsight Compute)
+// then see every launch.  Results are identical: every attempt kernel returns
+// at once when the state is done, so the attempts after the end of a batch do
+// nothing.
+bool host_loop_mode();
+
+// Host-driven loop: launch_attempt(stream) enqueues one attempt and its
+// controller (no conditional handle).  At most max_attempts + batch attempts
+// are launched; the controller ends the run at max_attempts.
+template <typename F>
+cudaError_t run_host_loop(F&& launch_attempt, const DevState* st, int max_attempts, cudaStream_t s) {
+  const int batch = 32;
+  int done = 0;
+  for (long long launched = 0; !done && launched <= (long long)max_attempts + batch; launched += batch) {
+    for (int k = 0; k < batch; ++k) {
+      const cudaError_t e = launch_attempt(s);
+      if (e != cudaSuccess) return e;
+    }
+    cudaError_t e = cudaMemcpyAsync(&done, &st->done, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
 // Row-pass CTA geometry helpers (sequences per CTA and CTA count).
 int row_nseq(int n, int nrows);
 int row_ctas(int n, int nrows, int npairs);

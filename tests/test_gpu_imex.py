@@ -119,3 +119,52 @@ def test_adaptive_mixed_precision_vs_oracle(cuda, n):
     e_mixed = max(_rel(r.y_final[k].cpu().numpy(), ro.y_final[k]) for k in ("u", "v"))
     e_fp32 = max(_rel(rf.y_final[k].cpu().numpy(), ro.y_final[k]) for k in ("u", "v"))
     assert e_mixed < e_fp32
+
+
+_HOST_LOOP_CHILD = r"""
+import sys, numpy as np, torch
+sys.path.insert(0, sys.argv[1])
+import moljax_gb300 as M
+from oracle import mol
+dev = torch.device("cuda", 0)
+out = {}
+for prec, dtype in (("fp64", torch.float64), ("fp32", torch.float32), ("mixed", torch.float32)):
+    grid = M.Grid2D(64, 64, 0.0, 2.5, 0.0, 2.5)
+    model, cache, diff = M.create_gray_scott_periodic_fft(grid, 2e-5, 1e-5, 0.035, 0.065, dtype, dev)
+    y0 = mol.gray_scott_ic(mol.Grid2D(64, 64, 0, 2.5, 0, 2.5), 11)
+    ym = {k: torch.tensor(v, dtype=dtype, device=dev) for k, v in y0.items()}
+    r = M.adaptive_integrate_imex(model, ym, 0.0, 25.0, 1.0, cache, diff,
+                                  pid_params=M.PIDParams(atol=1e-7, rtol=1e-5), save_every=3,
+                                  max_steps=2000, precision=prec)
+    out[prec + "_u"] = r.y_final["u"].cpu().numpy()
+    out[prec + "_counts"] = np.array([r.n_accepted, r.n_rejected, r.status])
+    out[prec + "_t"] = r.t_history.cpu().numpy()
+np.savez(sys.argv[2], **out)
+"""
+
+
+def test_host_driven_loop_matches_device_loop(cuda, tmp_path):
+    # MJX_HOST_LOOP=1 (read once per process) launches the attempts from the host in
+    # batches instead of the conditional graph: identical kernels, identical results
+    import os
+    import subprocess
+    import sys
+    from oracle import mol as omol
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    path = str(tmp_path / "host_loop.npz")
+    env = dict(os.environ, MJX_HOST_LOOP="1")
+    subprocess.run([sys.executable, "-c", _HOST_LOOP_CHILD, root, path], env=env, check=True,
+                   timeout=600)
+    child = np.load(path)
+    import moljax_gb300 as M
+    for prec, dtype in (("fp64", torch.float64), ("fp32", torch.float32), ("mixed", torch.float32)):
+        grid = M.Grid2D(64, 64, 0.0, 2.5, 0.0, 2.5)
+        model, cache, diff = M.create_gray_scott_periodic_fft(grid, 2e-5, 1e-5, 0.035, 0.065, dtype, cuda)
+        y0 = omol.gray_scott_ic(omol.Grid2D(64, 64, 0, 2.5, 0, 2.5), 11)
+        ym = {k: torch.tensor(v, dtype=dtype, device=cuda) for k, v in y0.items()}
+        r = M.adaptive_integrate_imex(model, ym, 0.0, 25.0, 1.0, cache, diff,
+                                      pid_params=M.PIDParams(atol=1e-7, rtol=1e-5), save_every=3,
+                                      max_steps=2000, precision=prec)
+        assert list(child[prec + "_counts"]) == [r.n_accepted, r.n_rejected, r.status]
+        np.testing.assert_array_equal(child[prec + "_u"], r.y_final["u"].cpu().numpy())
+        np.testing.assert_array_equal(child[prec + "_t"], r.t_history.cpu().numpy())
