@@ -3,8 +3,8 @@
 One "step" is one full adaptive solve over t_span = (0, 2000) (step doubling,
 PI control, accept/reject all on the device).  The metric is
 grid-point-steps/s = interior points x accepted steps / time.  The default
-precision is "mixed": FP64 spectral state, FP32 transforms of the reaction
-increments (rel-L2 vs the FP64 path is reported in the line).
+precision is "mixed": float-float (FP32 pair) spectral state, FP32 transforms
+of the reaction increments (rel-L2 vs the FP64 path is reported in the line).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
   python bench.py --kernels-only [--reps R]   # per-kernel CUDA-event times only
@@ -156,7 +156,7 @@ def kernel_bytes(n, elem):
 def kernel_bytes_mixed(n):
     """Algorithmic bytes of the six passes of one mixed-precision attempt (2 fields).
 
-    Per field and half-spectrum element: FP64 state/scratch 16 B, FP32 row spectra 8 B.
+    Per field and half-spectrum element: float-float state/scratch 16 B, FP32 row spectra 8 B.
     """
     nc = n * (n // 2 + 1)
     f = 2
@@ -361,7 +361,7 @@ def run_ours(args, rank, world, local):
             "metric": METRIC, "value": units / t_dev, "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": t_dev / args.steps * 1e3, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32" if P == "fp32" else "f32 transforms + f64 spectral state", "data": "synthetic",
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32" if P == "fp32" else "f32 transforms + float-float (f32 pair) spectral state", "data": "synthetic",
             "config": {"workload": f"gray-scott IMEX-Strang adaptive {grid.ny}x{grid.nx} FP32, "
                                    f"t_span=(0,{args.t_end:g}), rtol={RTOL}, atol={ATOL}, "
                                    "Du=2e-5 Dv=1e-5 F=0.035 k=0.065 L=2.5",

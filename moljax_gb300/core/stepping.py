@@ -131,7 +131,7 @@ def adaptive_integrate_imex(model, y0, t0, t_end, dt0, fft_cache=None, diffusivi
     (default 20*max_steps+1000) so the device loop always terminates.
 
     ``precision``: ``"fp64"`` (FP64 everywhere; default for float64 models),
-    ``"fp32"`` (FP32 state and transforms) or ``"mixed"`` (FP64 spectral state,
+    ``"fp32"`` (FP32 state and transforms) or ``"mixed"`` (float-float spectral state,
     FP32 transforms of the reaction increments; FP32 in/out; no y history).
     float32 models default to ``"fp32"``.
     """

@@ -1,16 +1,20 @@
-// Adaptive IMEX-Strang with an FP64 spectral state and FP32 transforms.
+// Adaptive IMEX-Strang with an extended-precision spectral state and FP32
+// transforms.
 //
-// The state is kept as its FP64 half spectrum Y^.  Diffusion half steps are
-// pointwise in spectral space and applied in FP64 as Y^ += Y^ * mu with
-// mu = m - 1 = x/(1 - x), x = h D lam (computed in FP32: mu is small wherever
-// Y^ carries energy, so its FP32 rounding stays far below the state's).  Only
-// the reaction increments Delta = R_heun(y*) - y* go through FP32 transforms:
+// The state is kept as its half spectrum Y^ in float-float form: every real
+// component is the unevaluated sum hi + lo of two FP32 numbers (about 48
+// significant bits; GB300 runs FP32 at 64x its FP64 rate, so all state
+// arithmetic stays on the FP32 pipe).  Diffusion half steps are pointwise in
+// spectral space, Y^ += Y^ * mu with mu = m - 1 = x/(1 - x), x = h D lam
+// (computed in FP32: mu is small wherever Y^ carries energy, so its FP32
+// rounding stays far below the state's).  Only the reaction increments
+// Delta = R_heun(y*) - y* go through FP32 transforms:
 //   y*  = IFFT32(M(h/2) Y^)          (c2r in FP32)
 //   Y^' = M(h/2) (M(h/2) Y^ + FFT32(Delta(y*)))
 // so the FP32 rounding enters in proportion to |Delta|, not |y|.  The error
 // estimate y_half - y_full = IFFT32(Y^_half - Y^_full) is a transform of a small
-// FP64 difference.  Same step doubling / PI controller / accept-reject loop as
-// the FP32 path (csrc/imex.cu), six kernels per attempt:
+// difference taken in float-float.  Same step doubling / PI controller /
+// accept-reject loop as the FP32 path (csrc/imex.cu), six kernels per attempt:
 //
 //   C1 col  Y^[cur] -> PA = M(dt/2)Y^, PB = M(dt/4)Y^;  ZA = IFFT_y(PA), ZB = IFFT_y(PB)
 //   R1 row  ZA: c2r, Delta(dt), r2c;  ZB: c2r, Delta(dt/2), r2c
@@ -39,11 +43,12 @@ struct MJob {
   double D;
 };
 
+// Float-float complex element in HBM: {re_hi, im_hi, re_lo, im_lo}.
 struct MColArgs {
   int ny, log2ny, ncols, ldc, C, njobs;
-  double2* ys[2];
-  double2* pa;
-  double2* pb;
+  float4* ys[2];
+  float4* pa;
+  float4* pb;
   float2* za;
   float2* zb;
   const float* lamx;
@@ -55,18 +60,61 @@ struct MColArgs {
   MJob job[8];
 };
 
-__device__ __forceinline__ double2 dmk(double x, double y) { double2 r; r.x = x; r.y = y; return r; }
 __device__ __forceinline__ float2 fmk(float x, float y) { float2 r; r.x = x; r.y = y; return r; }
 
-// X + X * mu, mu = x/(1-x), x = hD * lam (FP32, |1-x| clamped at 1e-14 like the reference)
-__device__ __forceinline__ double2 mstep(double2 X, float hD, float lam) {
+// ---- float-float arithmetic (error-free transformations: Knuth's two-sum,
+// Dekker's fast two-sum, the FMA two-product).  The _rn intrinsics are never
+// contracted into FMAs or reassociated, which the transformations rely on.
+struct FF { float h, l; };
+
+__device__ __forceinline__ FF ff_fast2sum(float a, float b) {  // |a| >= |b| or a == 0
+  const float s = __fadd_rn(a, b);
+  FF r; r.h = s; r.l = __fsub_rn(b, __fsub_rn(s, a));
+  return r;
+}
+__device__ __forceinline__ float ff_2sum_err(float a, float b, float s) {  // s = fl(a + b)
+  const float bb = __fsub_rn(s, a);
+  return __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+// x + d, d an FP32 number
+__device__ __forceinline__ FF ff_add_f(FF x, float d) {
+  const float s = __fadd_rn(x.h, d);
+  return ff_fast2sum(s, __fadd_rn(ff_2sum_err(x.h, d, s), x.l));
+}
+// x + x * mu
+__device__ __forceinline__ FF ff_mstep(FF x, float mu) {
+  const float p = __fmul_rn(x.h, mu);
+  const float pe = __fmaf_rn(x.l, mu, __fmaf_rn(x.h, mu, -p));  // x*mu - p
+  const float s = __fadd_rn(x.h, p);
+  return ff_fast2sum(s, __fadd_rn(ff_2sum_err(x.h, p, s), __fadd_rn(x.l, pe)));
+}
+// s * (x - y) rounded to FP32 (the hi difference is exact when x, y are close)
+__device__ __forceinline__ float ff_diff_scaled(FF x, FF y, float s) {
+  return __fmul_rn(__fadd_rn(__fsub_rn(x.h, y.h), __fsub_rn(x.l, y.l)), s);
+}
+// s * x rounded to FP32
+__device__ __forceinline__ float ff_scaled(FF x, float s) { return __fmaf_rn(x.l, s, __fmul_rn(x.h, s)); }
+
+__device__ __forceinline__ FF ff_re(float4 v) { FF r; r.h = v.x; r.l = v.z; return r; }
+__device__ __forceinline__ FF ff_im(float4 v) { FF r; r.h = v.y; r.l = v.w; return r; }
+__device__ __forceinline__ float4 ff_pack(FF re, FF im) { return make_float4(re.h, im.h, re.l, im.l); }
+
+// mu = x/(1-x), x = hD * lam (FP32, |1-x| clamped at 1e-14 like the reference)
+__device__ __forceinline__ float mu_of(float hD, float lam) {
   const float x = hD * lam;
   float den = 1.0f - x;
   if (fabsf(den) < 1e-14f) den = 1e-14f;
-  const double mu = (double)(x / den);
-  return dmk(fma(X.x, mu, X.x), fma(X.y, mu, X.y));
+  return x / den;
+}
+__device__ __forceinline__ float4 ff_mstep_c(float4 X, float mu) {
+  return ff_pack(ff_mstep(ff_re(X), mu), ff_mstep(ff_im(X), mu));
+}
+__device__ __forceinline__ float4 ff_add_c(float4 X, float2 d) {
+  return ff_pack(ff_add_f(ff_re(X), d.x), ff_add_f(ff_im(X), d.y));
 }
 
+// One CTA: C adjacent kx columns of one job over all ny rows.  Threads per CTA
+// = 2 C ny/16, so every thread combines exactly min(8, ny/2) elements.
 __global__ void __launch_bounds__(512, 1) mcol_kernel(const __grid_constant__ MColArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float2* buf = reinterpret_cast<float2*>(smem_raw);
@@ -76,34 +124,55 @@ __global__ void __launch_bounds__(512, 1) mcol_kernel(const __grid_constant__ MC
   const int Cn = a.C, W = 2 * Cn;
   const int kx0 = blockIdx.x * Cn;
   const int ny = a.ny, tid = threadIdx.x, nth = blockDim.x;
+  const int total = ny * Cn;
   const long long ldc = a.ldc;
   const int cur = st != nullptr ? st->cur : 0;
   const double h = st != nullptr ? st->dtc : a.hfixed;
   const float hA = (float)(0.5 * h * jb.D), hB = (float)(0.25 * h * jb.D);
   const float nrm = a.inv_norm;
+  const int type = jb.type;
 
-  if (jb.type != MC_SPLIT) {
-    // load the FP32 increment tile and transform it forward along y
-    const float2* zin = jb.type == MC_FULL_END ? a.za : a.zb;
-    float2 v[16];
+  // State operands of this thread's elements, loaded first so that their
+  // latency overlaps the forward transform below.
+  float4 P[8], Q[8];
 #pragma unroll
-    for (int m = 0; m < 16; ++m) {
+  for (int m = 0; m < 8; ++m) {
+    const int e = tid + m * nth;
+    const int ky = e / Cn, c = e - ky * Cn, kx = kx0 + c;
+    if (e < total && kx < a.ncols) {
+      const long long g = jb.off + ky * ldc + kx;
+      if (type == MC_SPLIT) P[m] = a.ys[cur][g];
+      else if (type == MC_FULL_END) P[m] = a.pa[g];
+      else P[m] = a.pb[g];
+      if (type == MC_HALF_END) Q[m] = a.pa[g];
+    }
+  }
+
+  if (type != MC_SPLIT) {
+    // load the FP32 increment tile and transform it forward along y
+    const float2* zin = type == MC_FULL_END ? a.za : a.zb;
+    float2 v[8];
+#pragma unroll
+    for (int m = 0; m < 8; ++m) {
       const int e = tid + m * nth;
       const int ky = e / Cn, c = e - ky * Cn, kx = kx0 + c;
-      if (e < ny * Cn) v[m] = kx < a.ncols ? zin[jb.off + ky * ldc + kx] : fmk(0.f, 0.f);
+      if (e < total) v[m] = kx < a.ncols ? zin[jb.off + ky * ldc + kx] : fmk(0.f, 0.f);
     }
 #pragma unroll
-    for (int m = 0; m < 16; ++m) {
+    for (int m = 0; m < 8; ++m) {
       const int e = tid + m * nth;
       const int ky = e / Cn, c = e - ky * Cn;
-      if (e < ny * Cn) buf[sp(ky * W + c)] = v[m];
+      if (e < total) buf[sp(ky * W + c)] = v[m];
     }
     __syncthreads();
     fft_smem<float, false, true>(buf, ny, a.log2ny, Cn, 1, W, a.tw, tid);
   }
 
-  // FP64 combine, element by element
-  for (int e = tid; e < ny * Cn; e += nth) {
+  // float-float combine, element by element
+#pragma unroll
+  for (int m = 0; m < 8; ++m) {
+    const int e = tid + m * nth;
+    if (e >= total) continue;
     const int ky = e / Cn, c = e - ky * Cn, kx = kx0 + c;
     if (kx >= a.ncols) {
       buf[sp(ky * W + c)] = fmk(0.f, 0.f);
@@ -112,36 +181,34 @@ __global__ void __launch_bounds__(512, 1) mcol_kernel(const __grid_constant__ MC
     }
     const long long g = jb.off + ky * ldc + kx;
     const float lam = a.lamx[kx] + a.lamy[ky];
-    if (jb.type == MC_SPLIT) {
-      const double2 Y = a.ys[cur][g];
-      const double2 PA = mstep(Y, hA, lam), PB = mstep(Y, hB, lam);
+    if (type == MC_SPLIT) {
+      const float4 PA = ff_mstep_c(P[m], mu_of(hA, lam)), PB = ff_mstep_c(P[m], mu_of(hB, lam));
       a.pa[g] = PA;
       a.pb[g] = PB;
-      buf[sp(ky * W + c)] = fmk((float)(PA.x * nrm), (float)(PA.y * nrm));
-      buf[sp(ky * W + Cn + c)] = fmk((float)(PB.x * nrm), (float)(PB.y * nrm));
+      buf[sp(ky * W + c)] = fmk(ff_scaled(ff_re(PA), nrm), ff_scaled(ff_im(PA), nrm));
+      buf[sp(ky * W + Cn + c)] = fmk(ff_scaled(ff_re(PB), nrm), ff_scaled(ff_im(PB), nrm));
     } else {
       const float2 d = buf[sp(ky * W + c)];
-      if (jb.type == MC_FULL_END) {
-        const double2 P = a.pa[g];
-        a.pa[g] = mstep(dmk(P.x + (double)d.x, P.y + (double)d.y), hA, lam);
-      } else if (jb.type == MC_HALF_MID) {
-        const double2 P = a.pb[g];
-        const double2 X = mstep(mstep(dmk(P.x + (double)d.x, P.y + (double)d.y), hB, lam), hB, lam);
+      if (type == MC_FULL_END) {
+        a.pa[g] = ff_mstep_c(ff_add_c(P[m], d), mu_of(hA, lam));
+      } else if (type == MC_HALF_MID) {
+        const float mu = mu_of(hB, lam);
+        const float4 X = ff_mstep_c(ff_mstep_c(ff_add_c(P[m], d), mu), mu);
         a.pb[g] = X;
-        buf[sp(ky * W + c)] = fmk((float)(X.x * nrm), (float)(X.y * nrm));
+        buf[sp(ky * W + c)] = fmk(ff_scaled(ff_re(X), nrm), ff_scaled(ff_im(X), nrm));
       } else {  // MC_HALF_END
-        const double2 P = a.pb[g];
-        const double2 X = mstep(dmk(P.x + (double)d.x, P.y + (double)d.y), hB, lam);
+        const float4 X = ff_mstep_c(ff_add_c(P[m], d), mu_of(hB, lam));
         a.ys[1 - cur][g] = X;
-        const double2 Fa = a.pa[g];
-        buf[sp(ky * W + c)] = fmk((float)((X.x - Fa.x) * nrm), (float)((X.y - Fa.y) * nrm));
-        buf[sp(ky * W + Cn + c)] = fmk((float)(X.x * nrm), (float)(X.y * nrm));
+        const float4 Fa = Q[m];
+        buf[sp(ky * W + c)] = fmk(ff_diff_scaled(ff_re(X), ff_re(Fa), nrm),
+                                  ff_diff_scaled(ff_im(X), ff_im(Fa), nrm));
+        buf[sp(ky * W + Cn + c)] = fmk(ff_scaled(ff_re(X), nrm), ff_scaled(ff_im(X), nrm));
       }
     }
   }
-  if (jb.type == MC_FULL_END) return;
+  if (type == MC_FULL_END) return;
   __syncthreads();
-  const int nseq = (jb.type == MC_HALF_MID) ? Cn : W;
+  const int nseq = (type == MC_HALF_MID) ? Cn : W;
   fft_smem<float, true, true>(buf, ny, a.log2ny, nseq, 1, W, a.tw, tid);
   for (int e = tid; e < ny * nseq; e += nth) {
     const int ky = e / nseq, col = e - ky * nseq;
@@ -149,7 +216,7 @@ __global__ void __launch_bounds__(512, 1) mcol_kernel(const __grid_constant__ MC
     if (kx >= a.ncols) continue;
     const long long g = jb.off + ky * ldc + kx;
     const float2 v = buf[sp(ky * W + col)];
-    if (jb.type == MC_HALF_MID) a.zb[g] = v;
+    if (type == MC_HALF_MID) a.zb[g] = v;
     else if (half == 0) a.za[g] = v;
     else a.zb[g] = v;
   }
@@ -163,12 +230,24 @@ __global__ void f64_to_f32(const double* in, float* out, long long n) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
     out[i] = (float)in[i];
 }
-__global__ void select_state_kernel(const DevState* st, const double2* y0, const double2* y1, double2* out, long long n) {
-  const double2* src = st->cur == 0 ? y0 : y1;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-    out[i] = src[i];
+// FP64 complex -> float-float complex, in place (each element is 16 bytes either way)
+__global__ void c64_to_ff(double2* data, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const double2 z = data[i];
+    const float rh = __double2float_rn(z.x), ih = __double2float_rn(z.y);
+    const float rl = __double2float_rn(z.x - (double)rh), il = __double2float_rn(z.y - (double)ih);
+    reinterpret_cast<float4*>(data)[i] = make_float4(rh, ih, rl, il);
+  }
 }
-
+// current float-float state -> FP64 complex
+__global__ void select_state_kernel(const DevState* st, const float4* y0, const float4* y1, double2* out, long long n) {
+  const float4* src = st->cur == 0 ? y0 : y1;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    const float4 v = src[i];
+    double2 z; z.x = (double)v.x + (double)v.z; z.y = (double)v.y + (double)v.w;
+    out[i] = z;
+  }
+}
 
 
 struct MixLayout {
@@ -222,8 +301,8 @@ static MixAttempt build_mix(const void* plan32, const mjx_grid2d* g, const mjx_i
   if (C > 8) C = 8;
   while (C > 1 && (2 * C * tps > 512 || (size_t)sp_size(g->ny * 2 * C) * 8 > 200 * 1024)) C >>= 1;
   c.C = C;
-  c.ys[0] = (double2*)(ws + L.ys0); c.ys[1] = (double2*)(ws + L.ys1);
-  c.pa = (double2*)(ws + L.pa); c.pb = (double2*)(ws + L.pb);
+  c.ys[0] = (float4*)(ws + L.ys0); c.ys[1] = (float4*)(ws + L.ys1);
+  c.pa = (float4*)(ws + L.pa); c.pb = (float4*)(ws + L.pb);
   c.za = (float2*)(ws + L.za); c.zb = (float2*)(ws + L.zb);
   c.lamx = (const float*)pv.lamx; c.lamy = (const float*)pv.lamy; c.tw = (const float2*)pv.twy;
   c.inv_norm = (float)(1.0 / ((double)g->nx * (double)g->ny));
@@ -403,6 +482,8 @@ mjx_status mjx_imex_mixed_attempt_kernel2d(const void* plan32, const void* plan6
     f32_to_f64<<<304, 256, 0, s>>>((const float*)y, real64, nelem);
     MJX_CUDA_TRY(cudaGetLastError());
     MJX_TRY(to_spectrum64(plan64, g, nf, real64, (double2*)(w + L.ys0), s));
+    c64_to_ff<<<304, 256, 0, s>>>((double2*)(w + L.ys0), (long long)nf * L.fs);
+    MJX_CUDA_TRY(cudaGetLastError());
     MJX_CUDA_TRY(cudaMemcpyAsync(w + L.ys1, w + L.ys0, (size_t)nf * L.fs * 16, cudaMemcpyDeviceToDevice, s));
     DevState h;
     memset(&h, 0, sizeof(h));
@@ -465,6 +546,8 @@ mjx_status mjx_imex_adaptive2d_mixed(const void* plan32, const void* plan64, con
     MJX_CUDA_TRY(cudaMemcpyAsync(real64, y0, nelem * 8, cudaMemcpyDeviceToDevice, s));
   }
   MJX_TRY(to_spectrum64(plan64, g, nf, real64, (double2*)(w + L.ys0), s));
+  c64_to_ff<<<304, 256, 0, s>>>((double2*)(w + L.ys0), (long long)nf * L.fs);
+  MJX_CUDA_TRY(cudaGetLastError());
 
   DevState h;
   memset(&h, 0, sizeof(h));
@@ -530,7 +613,7 @@ mjx_status mjx_imex_adaptive2d_mixed(const void* plan32, const void* plan64, con
   }
   // final real state: select Y^[cur] into PB, inverse FP64 transform, write real into PA
   double2* spec = (double2*)(w + L.pb);
-  select_state_kernel<<<304, 256, 0, s>>>(st, (const double2*)(w + L.ys0), (const double2*)(w + L.ys1), spec,
+  select_state_kernel<<<304, 256, 0, s>>>(st, (const float4*)(w + L.ys0), (const float4*)(w + L.ys1), spec,
                                           (long long)nf * L.fs);
   MJX_CUDA_TRY(cudaGetLastError());
   MJX_TRY(from_spectrum64(plan64, g, nf, spec, real64, s));
