@@ -76,7 +76,7 @@ typedef struct mjx_imex_problem {
   double D[4];         /* per-field diffusivity; D <= 1e-14 passes the field through */
   double F, k, r;      /* reaction parameters */
   double dt_cfl;       /* imex_cfl_dt (moljax/core/dt_policy.py:430-502), host-computed */
-  int use_strang;      /* 1: IMEX-Strang (order 2).  0 is rejected (MJX_BAD_ARG). */
+  int use_strang;      /* 1: IMEX-Strang (order 2); 0: IMEX-Euler (order 1, not in the mixed form) */
   int max_attempts;    /* hard cap on step attempts (accepted + rejected); <= 0 -> default */
 } mjx_imex_problem;
 
@@ -177,19 +177,22 @@ mjx_status mjx_stencil1d(const void* padded_in, void* padded_out, int nfields, i
 /* ---- IMEX-Strang (diffusion implicit by FFT, reaction explicit Heun) ------------- */
 size_t mjx_imex2d_ws_bytes(int ny, int nx, int nfields, int dtype);
 
-/* One fixed IMEX-Strang step of length dt (moljax/core/stepping.py:370-435).
- * y_in may equal y_out. */
+/* One fixed IMEX step of length dt: IMEX-Strang (moljax/core/stepping.py:370-435)
+ * or, with prob->use_strang == 0, IMEX-Euler (317-367).  y_in may equal y_out. */
 mjx_status mjx_imex_strang_step2d(const void* plan, const mjx_grid2d* grid, int dtype,
                                   const mjx_imex_problem* prob, double dt, const void* y_in,
                                   void* y_out, void* ws, size_t ws_bytes, void* stream);
 
-/* Adaptive IMEX-Strang with step doubling and the PI controller, run as one
+/* Adaptive IMEX-Strang (or IMEX-Euler, prob->use_strang == 0, error order 1)
+ * with step doubling and the PI controller, run as one
  * device-side loop (a CUDA graph with a conditional while node); no host
  * synchronisation per step.  Replaces adaptive_integrate_imex
  * (moljax/core/stepping.py:1146-1371) with estimate_error_imex_doubling (566-608),
  * scaled_error_norm (state.py:312-343) and propose_dt_imex (dt_policy.py:544-610).
  * hist_t/hist_dt (double[max_saves]) and hist_y ([max_saves][nfields][ny][nx])
- * may be NULL.  max_saves = max_steps // save_every + 1 as in the reference.
+ * may be NULL.  hist_y may be device memory or pinned host memory (cudaHostAlloc /
+ * cudaHostRegister): the saved states then stream straight to the host as the loop
+ * runs, so the device holds no history.  max_saves = max_steps // save_every + 1 as in the reference.
  * Blocks until the run finishes and fills *result. */
 mjx_status mjx_imex_adaptive2d(const void* plan, const mjx_grid2d* grid, int dtype,
                                const mjx_imex_problem* prob, const mjx_pid_params* pid,
@@ -227,6 +230,62 @@ mjx_status mjx_nk_vardiff_integrate2d(const void* plan2, int n, double dy, doubl
                                       int be_guess_previous, const mjx_nk_params* nkp,
                                       const double* y0, double* y_out, int* stats, void* ws,
                                       size_t ws_bytes, void* stream);
+
+/* out = F(y) = div((a + b y^2) grad y) - c y^3 on the n x n interior with homogeneous
+ * Dirichlet ghosts (MOLModel.rhs of this model, moljax/core/model.py:100-118 with
+ * apply_variable_diffusion_2d, moljax/core/variable_coeff.py:232-287).  FP64. */
+mjx_status mjx_vardiff_rhs2d(int n, double dy, double dx, const double* model_abc, const double* y,
+                             double* out, void* stream);
+
+/* One implicit step of this model: be_step (moljax/core/stepping.py:170-214), cn_step
+ * (217-260) or bdf2_step (263-310, omega = dt/dt_prev, y_prev = y_{n-1}), solved as in
+ * mjx_nk_vardiff_integrate2d.  stats (optional): Newton iterations, GMRES iterations,
+ * converged; res_norm (optional): final residual norm (NKStats, newton_krylov.py:41-46). */
+mjx_status mjx_nk_vardiff_step2d(const void* plan2, int n, double dy, double dx,
+                                 const double* model_abc, int method, double dt, double dt_prev,
+                                 int be_guess_previous, const mjx_nk_params* nkp, const double* y_n,
+                                 const double* y_prev, double* y_out, int* stats, double* res_norm,
+                                 void* ws, size_t ws_bytes, void* stream);
+
+/* Adaptive implicit integration of this model: the implicit branch of adaptive_integrate
+ * (moljax/core/stepping.py:723-1021).  BE error = dt F(y_BE); CN and BDF2 error =
+ * y_method - y_BE (a second, BE solve per attempt; BDF2 takes BE steps while no step has
+ * been accepted).  Acceptance also needs Newton convergence; the next dt follows
+ * propose_dt (moljax/core/dt_policy.py:324-408) with implicit_robustness_dt (279-321).
+ * The accept/reject loop runs on the host (one synchronisation per attempt, after the
+ * Newton solves).  hist_t/hist_dt: HOST arrays of max_saves doubles (may be NULL);
+ * hist_y: device array of max_saves n x n FP64 states (may be NULL).  nk_totals
+ * (optional, 3 ints): Newton iterations, GMRES iterations and non-converged solves
+ * summed over all attempts.  attempt_log (optional HOST array of 6 * log_cap doubles):
+ * per attempt t, dt tried, error ratio, Newton converged, Newton iterations, accepted.
+ * Workspace: mjx_nk_vardiff_ws_bytes. */
+mjx_status mjx_nk_vardiff_adaptive2d(const void* plan2, int n, double dy, double dx,
+                                     const double* model_abc, int method,
+                                     const mjx_pid_params* pid, double t0, double t_end, double dt0,
+                                     int max_steps, int save_every, int be_guess_previous,
+                                     const mjx_nk_params* nkp, const double* y0, double* y_final,
+                                     double* hist_t, double* hist_dt, double* hist_y,
+                                     int* nk_totals, double* attempt_log, int log_cap,
+                                     mjx_adaptive_result* res, void* ws, size_t ws_bytes,
+                                     void* stream);
+
+/* ---- DST-I and the Dirichlet spectral solvers -------------------------------------- */
+/* Plan of the length-n DST-I (twiddles; for 2(n+1) not a power of two, the Bluestein
+ * chirp and filter).  Lengths: 1 <= n <= 1023, or n = 2^k - 1 <= 2047.  0 = unsupported. */
+size_t mjx_dst1_plan_bytes(int n, int dtype);
+mjx_status mjx_dst1_plan_init(void* plan, int n, int dtype, void* stream);
+
+/* Row-batched transforms and solvers along rows of n values (nrows rows, contiguous):
+ *  mode 0: out = scale * DST-I(x)   (dst_I_fast, moljax/core/fft_nonperiodic.py:97-122;
+ *          scale 2/(n+1) gives idst_I_fast, 125-133)
+ *  mode 1: out = IDST(DST(x) / (1 - h D lam))  (solve_helmholtz_dirichlet, 308-330)
+ *  mode 2: out = IDST(DST(x) / lam)            (solve_poisson_dirichlet, 244-271)
+ *  mode 3: out = IDST(exp(h lam) DST(u) + h phi1(h lam) DST(N))  (etd1_dirichlet, 360-398),
+ *          x holds the nrows rows of u followed by the nrows rows of N(u).
+ * lam: device array of n values in the data type (the symbol, or the eigenvalues for mode 3);
+ * NULL for mode 0.  One kernel launch; out must not overlap x. */
+mjx_status mjx_dst1(const void* plan, int n, long long nrows, int dtype, int mode, const void* x,
+                    void* out, const void* lam, double h, double D, double scale, void* stream);
 
 /* ---- 1D tubular reactor, Crank-Nicolson, batched --------------------------------- */
 typedef enum mjx_reactor_variant {
@@ -281,10 +340,13 @@ mjx_status mjx_etdrk4_kernel2d(const void* plan, const mjx_grid2d* grid, int dty
 /* Workspace bytes of mjx_imex_adaptive2d_mixed. */
 size_t mjx_imex2d_mixed_ws_bytes(int ny, int nx, int nfields);
 
-/* Adaptive IMEX-Strang in the mixed FP32/FP64 form: the state is kept as its
- * FP64 half spectrum, diffusion multipliers are applied in FP64, and only the
- * reaction increments and the error estimate pass through FP32 transforms, so
- * FP32 rounding scales with the increments instead of the state.  Same loop,
+/* Adaptive IMEX-Strang in mixed precision: the state is kept as its half
+ * spectrum in float-float form (each real value an unevaluated sum of two FP32
+ * numbers, about 48 significant bits, all arithmetic on the FP32 pipe), the
+ * diffusion multipliers are applied to it in that form, and only the reaction
+ * increments and the error estimate pass through FP32 transforms, so FP32
+ * rounding scales with the increments instead of the state.  The initial and
+ * final conversions between the real state and the spectrum run in FP64.  Same loop,
  * controller and result semantics as mjx_imex_adaptive2d (adaptive_integrate_imex,
  * moljax/core/stepping.py:1146-1371).  plan32/plan64: FD-symbol plans of the grid
  * in FP32 and FP64.  io_dtype: dtype of y0 and y_final.  No y history. */
@@ -305,7 +367,8 @@ mjx_status mjx_imex_mixed_attempt_kernel2d(const void* plan32, const void* plan6
 
 /* Launches a single kernel of one fused adaptive attempt, for timing and
  * profiling: which = 0 seeds the workspace (both state buffers = y, step dt),
- * 1..7 launch the row/column passes K1..K7 (see csrc/imex.cu).  No reference
+ * 1..7 launch the row/column passes K1..K7 of IMEX-Strang, or 1..5 the passes
+ * E1..E5 of IMEX-Euler (see csrc/imex.cu).  No reference
  * counterpart: the reference has no per-kernel entry points. */
 mjx_status mjx_imex_attempt_kernel2d(const void* plan, const mjx_grid2d* grid, int dtype,
                                      const mjx_imex_problem* prob, const mjx_pid_params* pid,

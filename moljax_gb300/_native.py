@@ -97,6 +97,19 @@ SIGNATURES = {
     "mjx_nk_vardiff_integrate2d": (_i, [_vp, _i, _d, _d, C.POINTER(C.c_double), _i, _d, _i, _i,
                                         C.POINTER(NKParamsC), _vp, _vp, C.POINTER(C.c_int), _vp, _sz,
                                         _vp]),
+    "mjx_vardiff_rhs2d": (_i, [_i, _d, _d, C.POINTER(C.c_double), _vp, _vp, _vp]),
+    "mjx_nk_vardiff_step2d": (_i, [_vp, _i, _d, _d, C.POINTER(C.c_double), _i, _d, _d, _i,
+                                   C.POINTER(NKParamsC), _vp, _vp, _vp, C.POINTER(C.c_int),
+                                   C.POINTER(C.c_double), _vp, _sz, _vp]),
+    "mjx_nk_vardiff_adaptive2d": (_i, [_vp, _i, _d, _d, C.POINTER(C.c_double), _i,
+                                       C.POINTER(PIDParamsC), _d, _d, _d, _i, _i, _i,
+                                       C.POINTER(NKParamsC), _vp, _vp, C.POINTER(C.c_double),
+                                       C.POINTER(C.c_double), _vp, C.POINTER(C.c_int),
+                                       C.POINTER(C.c_double), _i, C.POINTER(AdaptiveResultC), _vp,
+                                       _sz, _vp]),
+    "mjx_dst1_plan_bytes": (_sz, [_i, _i]),
+    "mjx_dst1_plan_init": (_i, [_vp, _i, _i, _vp]),
+    "mjx_dst1": (_i, [_vp, _i, C.c_longlong, _i, _i, _vp, _vp, _vp, _d, _d, _d, _vp]),
     "mjx_etdrk4_ws_bytes": (_sz, [_i, _i, _i]),
     "mjx_etdrk4_gray_scott2d": (_i, [_vp, C.POINTER(Grid2DC), _i, _i, C.POINTER(C.c_double), _d, _d,
                                      _d, _d, _i, _vp, _vp, _vp, _sz, _i, _vp]),

@@ -5,10 +5,12 @@ from moljax_gb300.core.bc import BCType, FieldBCSpec, apply_bc
 from moljax_gb300.core import fft_solvers, operators, stepping, dt_policy, model
 from moljax_gb300.core.operators import LinearOp, NonlinearOp, laplacian_2d
 from moljax_gb300.core.model import (MOLModel, create_gray_scott_model,
-                                     create_gray_scott_periodic_fft, gray_scott_factory)
+                                     create_gray_scott_periodic_fft, gray_scott_factory,
+                                     create_variable_diffusion_model)
 from moljax_gb300.core.stepping import (IntegratorType, AdaptiveResult, adaptive_integrate,
-                                        adaptive_integrate_imex, imex_strang_step,
-                                        integrate_imex_fixed_dt)
+                                        adaptive_integrate_imex, imex_strang_step, imex_euler_step,
+                                        integrate_imex_fixed_dt, be_step, cn_step, bdf2_step,
+                                        integrate_fixed_dt)
 from moljax_gb300.core.dt_policy import CFLParams, PIDParams
 from moljax_gb300.core.fft_solvers import (create_fft_cache, solve_helmholtz_2d,
                                            apply_diffusion_inverse_fft, fft_cn_step,
@@ -24,3 +26,8 @@ from moljax_gb300.core.preconditioners import (DiffusionPreconditioner, Identity
                                                BlockJacobiPreconditioner)
 from moljax_gb300.core import reactor, stencil1d
 from moljax_gb300.core.operators import laplacian_1d, gradient_1d, d1_upwind_1d
+from moljax_gb300.core import fft_nonperiodic
+from moljax_gb300.core.fft_nonperiodic import (dst_I_fast, idst_I_fast, laplacian_symbol_dirichlet,
+                                               create_nonperiodic_fft_cache,
+                                               solve_poisson_dirichlet, solve_helmholtz_dirichlet,
+                                               etd1_dirichlet)

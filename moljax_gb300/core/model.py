@@ -63,6 +63,8 @@ class MOLModel:
     def rhs(self, state, t: float = 0.0):
         """apply_bcs -> D Lap + reaction, fused in one kernel (model.py:100-118)."""
         from moljax_gb300.core import stencil
+        if self.metadata.get("kind") == "vardiff":
+            return _vardiff_rhs(self, state)
         D = self.diffusivities()
         names = self.field_names
         rx = self.reaction_kind
@@ -145,6 +147,49 @@ def create_fisher_kpp_model(grid: Grid2D, D: float = 0.01, r: float = 1.0,
     return MOLModel(grid, {"u": FieldBCSpec(kind=bc_type)}, params, (diffusion,),
                     (fisher_kpp_reaction_op("u", "r"),),
                     {"field_names": ["u"], "diffusivities": {"u": D}})
+
+
+def create_variable_diffusion_model(grid: Grid2D, a: float = 1.0, b: float = 1.0, c: float = 1.0,
+                                    dtype: torch.dtype = torch.float64) -> MOLModel:
+    """u_t = div((a + b u^2) grad u) - c u^3 with homogeneous Dirichlet ghosts.
+
+    The nonlinear-diffusion model of the Newton-Krylov workload: the flux is the
+    face-averaged conservative form of apply_variable_diffusion_2d
+    (moljax/core/variable_coeff.py:232-287) with D = a + b u^2 evaluated on the
+    ghost-filled state, minus the reaction c u^3.  Square grids (n x n, n a power
+    of two <= 2048) on any spacing.  The implicit steppers (be_step, cn_step,
+    bdf2_step, integrate_fixed_dt, adaptive_integrate with BE/CN/BDF2) run this
+    model on the native Newton-Krylov solver.
+    """
+    if grid.nx != grid.ny:
+        raise NotImplementedError("the native variable-diffusion model needs nx == ny")
+    bc_spec = {"u": FieldBCSpec(kind=BCType.DIRICHLET)}
+    params = {"a": a, "b": b, "c": c, "dtype": dtype}
+    op = NonlinearOp("variable_diffusion_reaction", lambda st, g, tt, pp: _vardiff_rhs_raw(
+        st, g, pp), None)
+    return MOLModel(grid, bc_spec, params, (), (op,),
+                    {"field_names": ["u"], "kind": "vardiff", "abc": (a, b, c), "stiff": True})
+
+
+def _vardiff_rhs_raw(state, grid, params):
+    import ctypes as C
+    from moljax_gb300.core import stencil
+    u = state["u"]
+    N.require_cuda(u)
+    interior = stencil.unpad(u[None], grid)[0].to(torch.float64).contiguous()
+    out = torch.empty_like(interior)
+    abc = (C.c_double * 3)(params["a"], params["b"], params["c"])
+    N.check("mjx_vardiff_rhs2d", N.lib().mjx_vardiff_rhs2d(
+        grid.nx, float(grid.dy), float(grid.dx), abc, N.ptr(interior), N.ptr(out),
+        N.stream_ptr(u.device)))
+    padded = torch.zeros_like(u, dtype=torch.float64)
+    padded[grid.interior_slice] = out
+    return {"u": padded.to(u.dtype)}
+
+
+def _vardiff_rhs(model: MOLModel, state):
+    """MOLModel.rhs of the variable-diffusion model (ghosts zeroed, as the reference ops)."""
+    return _vardiff_rhs_raw(state, model.grid, model.params)
 
 
 def get_fft_cache(model: MOLModel):

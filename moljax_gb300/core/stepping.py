@@ -1,6 +1,6 @@
 """Time integration drivers (moljax/core/stepping.py drop-in, GPU-native).
 
-IMEX paths run in the native library: one IMEX-Strang step
+IMEX paths run in the native library: one IMEX-Strang or IMEX-Euler step
 (``mjx_imex_strang_step2d``) and the whole adaptive loop
 (``mjx_imex_adaptive2d``), where step doubling, the scaled error norm, the PI
 controller and the accept/reject bookkeeping stay on the device inside a CUDA
@@ -10,7 +10,9 @@ step.
 
 ``adaptive_integrate`` accepts the reference signature
 (model, y0, t0, t_end, dt0, method, ...) and the README form
-(model, t_span=, integrator=, rtol=, atol=).
+(model, t_span=, integrator=, rtol=, atol=).  BE/CN/BDF2 (``be_step``,
+``cn_step``, ``bdf2_step``, ``integrate_fixed_dt``, ``adaptive_integrate``) run
+on the native Newton-Krylov solver for the variable-diffusion model.
 """
 
 from __future__ import annotations
@@ -53,7 +55,7 @@ class AdaptiveResult(NamedTuple):
     status: int
 
 
-def _problem(model, diffusivities, cfl_params, max_attempts=0):
+def _problem(model, diffusivities, cfl_params, max_attempts=0, use_strang=True):
     names = model.field_names
     if len(names) > 4:
         raise NotImplementedError("at most 4 fields per native IMEX call")
@@ -67,7 +69,7 @@ def _problem(model, diffusivities, cfl_params, max_attempts=0):
     p.k = float(model.params.get("k", 0.0))
     p.r = float(model.params.get("r", 0.0))
     p.dt_cfl = imex_cfl_dt(model.grid, model.params, cfl_params)
-    p.use_strang = 1
+    p.use_strang = 1 if use_strang else 0
     p.max_attempts = int(max_attempts)
     return p
 
@@ -81,12 +83,21 @@ def _periodic_only(model):
 
 def imex_strang_step(model, y, t, dt, fft_cache, diffusivities):
     """One IMEX-Strang step H(dt/2) R(dt) H(dt/2) (moljax/core/stepping.py:370-435)."""
+    return _imex_step(model, y, t, dt, fft_cache, diffusivities, True)
+
+
+def imex_euler_step(model, y, t, dt, fft_cache, diffusivities):
+    """One IMEX-Euler step H(dt) (y + dt N(y)) (moljax/core/stepping.py:317-367)."""
+    return _imex_step(model, y, t, dt, fft_cache, diffusivities, False)
+
+
+def _imex_step(model, y, t, dt, fft_cache, diffusivities, use_strang):
     _periodic_only(model)
     grid = model.grid
     names = model.field_names
     interior = stencil.unpad(stencil.stack(y, names), grid)
     plan = _plan_of(fft_cache, grid.ny, grid.nx, interior.dtype)
-    prob = _problem(model, diffusivities, CFLParams())
+    prob = _problem(model, diffusivities, CFLParams(), use_strang=use_strang)
     lib = N.lib()
     ws = workspace(lib.mjx_imex2d_ws_bytes(grid.ny, grid.nx, len(names), plan.code), plan.device,
                    "imex")
@@ -101,19 +112,17 @@ def imex_strang_step(model, y, t, dt, fft_cache, diffusivities):
 def integrate_imex_fixed_dt(model, y0, t0, t_end, dt, fft_cache, diffusivities,
                             use_strang: bool = True, save_every: int = 1):
     """moljax/core/stepping.py:1374-1436: int((t_end-t0)/dt)+1 fixed steps."""
-    if not use_strang:
-        raise NotImplementedError("IMEX-Euler fixed-dt path is not built")
     n = int((t_end - t0) / dt) + 1
     y = y0
     t = t0
     ts, ys = [], []
     for _ in range(n):
-        y = imex_strang_step(model, y, t, dt, fft_cache, diffusivities)
+        y = _imex_step(model, y, t, dt, fft_cache, diffusivities, use_strang)
         t = t + dt
         ts.append(t)
-        ys.append({k: stencil.unpad(v[None], model.grid)[0] for k, v in y.items()})
+        ys.append(y)
     t_out = torch.tensor(ts, dtype=torch.float64)
-    y_out = {k: torch.stack([s[k] for s in ys]) for k in y0}
+    y_out = {k: torch.stack([s[k] for s in ys]) for k in y0}  # padded, as the scan outputs
     return t_out, y_out, y
 
 
@@ -134,9 +143,13 @@ def adaptive_integrate_imex(model, y0, t0, t_end, dt0, fft_cache=None, diffusivi
     ``"fp32"`` (FP32 state and transforms) or ``"mixed"`` (float-float spectral state,
     FP32 transforms of the reaction increments; FP32 in/out; no y history).
     float32 models default to ``"fp32"``.
+    ``save_y_history="host"`` streams the saved states into pinned host memory as
+    the loop runs (the history never occupies HBM; O(max_saves * n) histories at
+    1024^2 stay on the host side of NVLink-C2C).
+
+    ``use_strang=False`` runs IMEX-Euler under the same step doubling with
+    error order 1 (stepping.py:1193); it has the "fp32" and "fp64" forms.
     """
-    if not use_strang:
-        raise NotImplementedError("adaptive IMEX-Euler is not built; use_strang=True")
     _periodic_only(model)
     cfl_params = cfl_params or CFLParams()
     pid_params = pid_params or PIDParams()
@@ -148,10 +161,12 @@ def adaptive_integrate_imex(model, y0, t0, t_end, dt0, fft_cache=None, diffusivi
         fft_cache = model.metadata.get("fft_cache") or create_fft_cache(grid, model.dtype)
     interior = stencil.unpad(stencil.stack(y0, names), grid)
     plan = _plan_of(fft_cache, grid.ny, grid.nx, interior.dtype)
-    prob = _problem(model, diffusivities, cfl_params, max_attempts)
+    prob = _problem(model, diffusivities, cfl_params, max_attempts, use_strang)
     if precision is None:
         precision = "fp64" if interior.dtype == torch.float64 else "fp32"
     if precision == "mixed":
+        if not use_strang:
+            raise NotImplementedError("the mixed-precision form is built for IMEX-Strang only")
         return _adaptive_mixed(model, interior, plan, prob, pid_params, t0, t_end, dt0, max_steps,
                                save_every)
     if precision not in ("fp32", "fp64"):
@@ -168,8 +183,13 @@ def adaptive_integrate_imex(model, y0, t0, t_end, dt0, fft_cache=None, diffusivi
     y_final = torch.empty_like(interior)
     t_hist = torch.empty(max_saves, dtype=torch.float64, device=dev)
     dt_hist = torch.empty(max_saves, dtype=torch.float64, device=dev)
-    y_hist = (torch.empty((max_saves,) + tuple(interior.shape), dtype=interior.dtype, device=dev)
-              if save_y_history else None)
+    if save_y_history == "host":  # streamed to pinned host memory by the history kernel
+        y_hist = torch.empty((max_saves,) + tuple(interior.shape), dtype=interior.dtype,
+                             pin_memory=True)
+    elif save_y_history:
+        y_hist = torch.empty((max_saves,) + tuple(interior.shape), dtype=interior.dtype, device=dev)
+    else:
+        y_hist = None
     res = N.AdaptiveResultC()
     N.check("mjx_imex_adaptive2d", lib.mjx_imex_adaptive2d(
         N.ptr(plan.buf), C.byref(plan.cgrid), plan.code, C.byref(prob), C.byref(pid),
@@ -215,6 +235,149 @@ def _adaptive_mixed(model, interior, plan, prob, pid_params, t0, t_end, dt0, max
                           res.n_rejected, res.status)
 
 
+# ------------------------------------------------------------------ implicit steppers
+_IMPLICIT = {IntegratorType.BE: 3, IntegratorType.CN: 4, IntegratorType.BDF2: 5}
+
+
+def _require_vardiff(model):
+    if model.metadata.get("kind") != "vardiff":
+        raise NotImplementedError(
+            "the native implicit steppers are built for the variable-diffusion model "
+            "(create_variable_diffusion_model); for other residuals call newton_krylov_solve")
+
+
+def _nk_setup(model, nk_params):
+    import ctypes as Cc
+    from moljax_gb300.core.fft_solvers import get_plan
+    from moljax_gb300.core.newton_krylov import NKParams, _cparams
+    _require_vardiff(model)
+    p = nk_params or NKParams()
+    g = model.grid
+    a, b, c = model.metadata["abc"]
+    return p, _cparams(p), (Cc.c_double * 3)(a, b, c), g
+
+
+def _interior64(model, y):
+    u = y["u"]
+    N.require_cuda(u)
+    return stencil.unpad(u[None], model.grid)[0].to(torch.float64).contiguous()
+
+
+def _padded(model, interior, like):
+    out = torch.zeros(like.shape, dtype=torch.float64, device=interior.device)
+    out[model.grid.interior_slice] = interior
+    out = stencil.apply_bc({"u": out}, model.grid, model.bc_spec, 0.0, model.params)["u"]
+    return out.to(like.dtype)
+
+
+def _implicit_step(model, y, y_prev, dt, dt_prev, method, nk_params, be_guess):
+    from moljax_gb300.core.fft_solvers import get_plan, workspace
+    from moljax_gb300.core.newton_krylov import NKStats
+    p, cp, abc, g = _nk_setup(model, nk_params)
+    yn = _interior64(model, y)
+    yp = _interior64(model, y_prev) if y_prev is not None else yn
+    n = g.nx
+    plan2 = get_plan(2 * n, 2 * n, g.dy, g.dx, "fd", torch.float32, yn.device)
+    lib = N.lib()
+    ws = workspace(lib.mjx_nk_vardiff_ws_bytes(n, p.gmres_restart), plan2.device, "nk")
+    out = torch.empty_like(yn)
+    st = (C.c_int * 3)()
+    rn = C.c_double(0.0)
+    N.check("mjx_nk_vardiff_step2d", lib.mjx_nk_vardiff_step2d(
+        N.ptr(plan2.buf), n, float(g.dy), float(g.dx), abc, int(method), float(dt), float(dt_prev),
+        int(be_guess == "previous"), C.byref(cp), N.ptr(yn), N.ptr(yp), N.ptr(out), st,
+        C.byref(rn), N.ptr(ws), ws.numel(), N.stream_ptr(plan2.device)))
+    return ({"u": _padded(model, out, y["u"])},
+            NKStats(bool(st[2]), int(st[0]), int(st[1]), float(rn.value)))
+
+
+def be_step(model, y, t, dt, preconditioner=None, nk_params=None, *, be_guess: str = "euler"):
+    """Backward Euler y_{n+1} = y_n + dt F(y_{n+1}) (moljax/core/stepping.py:170-214).
+
+    Newton-Krylov on the native solver; the explicit-Euler initial guess of the
+    reference, or y_n with ``be_guess="previous"``.  The solver always applies its
+    own (alpha0 I - beta Dbar Lap_D)^-1 preconditioner (``preconditioner`` is
+    accepted for the reference signature; it changes GMRES counts, not the root).
+    Returns (y_new, NKStats).
+    """
+    return _implicit_step(model, y, None, dt, dt, 3, nk_params, be_guess)
+
+
+def cn_step(model, y, t, dt, preconditioner=None, nk_params=None, *, be_guess: str = "euler"):
+    """Crank-Nicolson y_{n+1} = y_n + dt/2 (F(y_n) + F(y_{n+1})) (stepping.py:217-260)."""
+    return _implicit_step(model, y, None, dt, dt, 4, nk_params, be_guess)
+
+
+def bdf2_step(model, y, y_prev, t, dt, dt_prev, preconditioner=None, nk_params=None):
+    """Variable-step BDF2 with the reference coefficients (stepping.py:263-310,
+    newton_krylov.py:406-448); guess 2 y_n - y_{n-1}."""
+    return _implicit_step(model, y, y_prev, dt, dt_prev, 5, nk_params, "euler")
+
+
+def integrate_fixed_dt(model, y0, t0, t_end, dt, method=IntegratorType.RK4, save_every: int = 1,
+                       preconditioner=None, nk_params=None, *, be_guess: str = "euler"):
+    """moljax/core/stepping.py:1028-1139 for the implicit methods: int((t_end-t0)/dt)+1
+    fixed steps (BDF2 takes a BE first step); returns (t_history, y_history, y_final)
+    with every step's padded state, as the reference's scan outputs."""
+    method = IntegratorType(int(method))
+    if method not in _IMPLICIT:
+        raise NotImplementedError(f"{method.name}: explicit fixed-dt drivers are not built on the GPU path")
+    n_steps = int((t_end - t0) / dt) + 1
+    y, y_prev, t = y0, y0, t0
+    ts, ys = [], []
+    for step in range(n_steps):
+        if method == IntegratorType.BE or (method == IntegratorType.BDF2 and step < 1):
+            y_new, _ = be_step(model, y, t, dt, preconditioner, nk_params, be_guess=be_guess)
+        elif method == IntegratorType.CN:
+            y_new, _ = cn_step(model, y, t, dt, preconditioner, nk_params, be_guess=be_guess)
+        else:
+            y_new, _ = bdf2_step(model, y, y_prev, t, dt, dt, preconditioner, nk_params)
+        y_prev, y, t = y, y_new, t + dt
+        ts.append(t)
+        ys.append(y)
+    return (torch.tensor(ts, dtype=torch.float64),
+            {k: torch.stack([s[k] for s in ys]) for k in y0}, y)
+
+
+def _adaptive_implicit(model, y0, t0, t_end, dt0, method, max_steps, pid_params, nk_params,
+                       save_every, be_guess, save_y_history=True, attempt_log=None):
+    from moljax_gb300.core.fft_solvers import get_plan, workspace
+    pid_params = pid_params or PIDParams()
+    p, cp, abc, g = _nk_setup(model, nk_params)
+    u0 = _interior64(model, y0)
+    n = g.nx
+    dev = u0.device
+    plan2 = get_plan(2 * n, 2 * n, g.dy, g.dx, "fd", torch.float32, dev)
+    lib = N.lib()
+    ws = workspace(lib.mjx_nk_vardiff_ws_bytes(n, p.gmres_restart), plan2.device, "nk")
+    max_saves = max_steps // save_every + 1
+    t_hist = (C.c_double * max_saves)()
+    dt_hist = (C.c_double * max_saves)()
+    y_hist = (torch.empty((max_saves, n, n), dtype=torch.float64, device=dev)
+              if save_y_history else None)
+    y_final = torch.empty_like(u0)
+    tot = (C.c_int * 3)()
+    log_cap = 20 * max_steps + 1000 if attempt_log is not None else 0
+    log = (C.c_double * (6 * max(log_cap, 1)))() if attempt_log is not None else None
+    res = N.AdaptiveResultC()
+    pid = N.PIDParamsC(pid_params.safety, pid_params.kI, pid_params.kP, pid_params.dt_min,
+                       pid_params.dt_max, pid_params.max_factor, pid_params.min_factor,
+                       pid_params.atol, pid_params.rtol)
+    N.check("mjx_nk_vardiff_adaptive2d", lib.mjx_nk_vardiff_adaptive2d(
+        N.ptr(plan2.buf), n, float(g.dy), float(g.dx), abc, _IMPLICIT[method], C.byref(pid),
+        float(t0), float(t_end), float(dt0), int(max_steps), int(save_every),
+        int(be_guess == "previous"), C.byref(cp), N.ptr(u0), N.ptr(y_final), t_hist, dt_hist,
+        N.ptr(y_hist), tot, log, int(log_cap), C.byref(res), N.ptr(ws), ws.numel(),
+        N.stream_ptr(dev)))
+    if attempt_log is not None:  # (t, dt, err, converged, newton_iters, accepted) per attempt
+        attempt_log.extend(tuple(log[6 * i:6 * i + 6]) for i in range(res.n_attempts))
+    y_fin = {"u": _padded(model, y_final, y0["u"])}
+    th = torch.tensor(list(t_hist), dtype=torch.float64)
+    dth = torch.tensor(list(dt_hist), dtype=torch.float64)
+    return AdaptiveResult(res.t_final, y_fin, th, {"u": y_hist} if y_hist is not None else None,
+                          dth, res.n_saved, res.n_accepted, res.n_rejected, res.status)
+
+
 def adaptive_integrate(model, y0=None, t0: float = 0.0, t_end: Optional[float] = None,
                        dt0: float = 1.0, method: int = IntegratorType.RK4, max_steps: int = 10000,
                        cfl_params: Optional[CFLParams] = None,
@@ -223,9 +386,11 @@ def adaptive_integrate(model, y0=None, t0: float = 0.0, t_end: Optional[float] =
                        rtol: Optional[float] = None, atol: Optional[float] = None, **kw):
     """Reference form (stepping.py:723-1021) or README form (README.md:75-80).
 
-    IMEX_STRANG routes to ``adaptive_integrate_imex`` (the reference's real
-    IMEX driver).  Other methods are dispatched to their native drivers as they
-    are built; unbuilt ones raise NotImplementedError.
+    IMEX_STRANG and IMEX_EULER route to ``adaptive_integrate_imex`` (the
+    reference's real IMEX driver; the reference's own adaptive_integrate lets
+    both fall through to its BDF2 branch, stepping.py:864-877).  Other methods
+    are dispatched to their native drivers as they are built; unbuilt ones
+    raise NotImplementedError.
     """
     if t_span is not None:
         t0, t_end = float(t_span[0]), float(t_span[1])
@@ -251,7 +416,12 @@ def adaptive_integrate(model, y0=None, t0: float = 0.0, t_end: Optional[float] =
         n = int(round((tf - t0) / dt0))
         return AdaptiveResult(tf, y, torch.tensor([t0, tf], dtype=torch.float64), None,
                               torch.tensor([dt0], dtype=torch.float64), 2, n, 0, 0)
-    if method == IntegratorType.IMEX_STRANG:
-        return adaptive_integrate_imex(model, y0, t0, t_end, dt0, None, None, True, max_steps,
+    if method in _IMPLICIT:
+        return _adaptive_implicit(model, y0, t0, t_end, dt0, method, max_steps, pid_params,
+                                  nk_params, save_every, kw.pop("be_guess", "euler"),
+                                  kw.pop("save_y_history", True), kw.pop("attempt_log", None))
+    if method in (IntegratorType.IMEX_STRANG, IntegratorType.IMEX_EULER):
+        return adaptive_integrate_imex(model, y0, t0, t_end, dt0, None, None,
+                                       method == IntegratorType.IMEX_STRANG, max_steps,
                                        cfl_params, pid_params, save_every, **kw)
     raise NotImplementedError(f"{method.name} adaptive driver is not built on the GPU path")

@@ -201,6 +201,7 @@ struct Attempt {
   RowArgs<T> k1, k3, k5, k7;
   ColArgs<T> k2, k4, k6;
   int rx;
+  int euler;  // IMEX-Euler attempt: k1..k5 only
 };
 
 template <typename T>
@@ -304,7 +305,72 @@ static Attempt<T> build_attempt(const void* plan, const mjx_grid2d* g, const mjx
     A.k4.job[A.k4.njobs++] = job(b, b, b, 1, D, 0.25, 0.25, 2, 2);
     A.k6.job[A.k6.njobs++] = job(b, b, b, 1, D, 0.25, 0.25, 1, 1);
   }
+  A.euler = 0;
   return A;
+}
+
+// IMEX-Euler step E(h) = H(h) (y + h N(y)) (imex_euler_step, stepping.py:317-367)
+// under step doubling: the full step E(dt) on branch A, E(dt/2) E(dt/2) on branch B.
+//
+//   E1 row  Y[cur]: Euler(dt) -> r2c SA;  Euler(dt/2) -> r2c SB
+//   E2 col  SA *= m(dt);  SB *= m(dt/2)
+//   E3 row  SA: c2r -> YF (full step);  SB: c2r, Euler(dt/2), r2c
+//   E4 col  SB *= m(dt/2)
+//   E5 row  SB: c2r -> Y[1-cur] (two half steps) + scaled error vs YF
+template <typename T>
+static Attempt<T> build_attempt_euler(const void* plan, const mjx_grid2d* g, const mjx_imex_problem* pb,
+                                      const mjx_pid_params* pid, char* ws, const ImexLayout& L,
+                                      DevState* st) {
+  Attempt<T> A = build_attempt<T>(plan, g, pb, pid, ws, L, st);
+  const Pairing pg = pairing_for(pb, g);
+  const int nf = pb->nfields, ldc = spec_ldc(g->nx);
+  long long s_off[2] = {0, (long long)((L.sb - L.sa) / sizeof(cx<T>))};
+  const RowArgs<T> base = A.k1;  // shared geometry; pairs are rebuilt below
+  const double h1[2] = {1.0, 0.5};
+  const int RE = ROW_REACT | ROW_EULER;
+  {  // E1: both branches from the real state
+    A.k1 = base;
+    const int fl[2] = {RE | ROW_STORE_SPEC, RE | ROW_STORE_SPEC};
+    make_pairs(A.k1, pg, g, nf, 0, 2, h1, fl, s_off);
+  }
+  {  // E3: SA -> YF; SB: c2r -> Euler(dt/2) -> r2c
+    A.k3 = base;
+    A.k3.rout[0] = (T*)(ws + L.yf); A.k3.rout_sel = -1;
+    const int fl[2] = {ROW_LOAD_SPEC | ROW_STORE_REAL, ROW_LOAD_SPEC | RE | ROW_STORE_SPEC};
+    make_pairs(A.k3, pg, g, nf, 0, 2, h1, fl, s_off);
+  }
+  {  // E5: SB -> Y[1-cur] + error
+    A.k5 = base;
+    const double hf[1] = {1.0};
+    const int fl[1] = {ROW_LOAD_SPEC | ROW_STORE_REAL | ROW_ERRNORM};
+    make_pairs(A.k5, pg, g, nf, 1, 1, hf, fl, s_off);
+  }
+  const long long fs = (long long)g->ny * ldc;
+  ColArgs<T> cb = A.k4;
+  cb.njobs = 0;
+  cb.C = col_tile(g->ny, cb.ncols, 1, sizeof(T));
+  A.k2 = cb; A.k4 = cb;
+  for (int f = 0; f < nf; ++f) {
+    const double D = pb->D[f] > 1e-14 ? pb->D[f] : 0.0;
+    const long long a = s_off[0] + f * fs, b = s_off[1] + f * fs;
+    ColJob j;
+    memset(&j, 0, sizeof(j));
+    j.nout = 1; j.D = D; j.mul = MUL_HELMHOLTZ; j.pow[0] = j.pow[1] = 1;
+    j.sin = j.sout[0] = j.sout[1] = a; j.hfac[0] = j.hfac[1] = 1.0;
+    A.k2.job[A.k2.njobs++] = j;
+    j.sin = j.sout[0] = j.sout[1] = b; j.hfac[0] = j.hfac[1] = 0.5;
+    A.k2.job[A.k2.njobs++] = j;
+    A.k4.job[A.k4.njobs++] = j;
+  }
+  A.euler = 1;
+  return A;
+}
+
+template <typename T>
+static Attempt<T> make_attempt(const void* plan, const mjx_grid2d* g, const mjx_imex_problem* pb,
+                               const mjx_pid_params* pid, char* ws, const ImexLayout& L, DevState* st) {
+  return pb->use_strang ? build_attempt<T>(plan, g, pb, pid, ws, L, st)
+                        : build_attempt_euler<T>(plan, g, pb, pid, ws, L, st);
 }
 
 template <typename T>
@@ -319,6 +385,7 @@ static cudaError_t launch_attempt(const Attempt<T>& A, cudaStream_t s) {
   MJX_ROW(A.k3);
   if ((e = launch_col<T>(A.k4, s)) != cudaSuccess) return e;
   MJX_ROW(A.k5);
+  if (A.euler) return cudaSuccess;
   if ((e = launch_col<T>(A.k6, s)) != cudaSuccess) return e;
   MJX_ROW(A.k7);
 #undef MJX_ROW
@@ -330,7 +397,6 @@ static mjx_status check_problem(const mjx_imex_problem* pb, const mjx_grid2d* g)
   if (pb->nfields < 1 || pb->nfields > 4) return MJX_BAD_ARG;
   if (pb->reaction == MJX_REACT_GRAY_SCOTT && pb->nfields != 2) return MJX_BAD_ARG;
   if (pb->reaction < MJX_REACT_NONE || pb->reaction > MJX_REACT_FISHER) return MJX_BAD_ARG;
-  if (!pb->use_strang) return MJX_BAD_ARG;
   (void)g;
   return MJX_OK;
 }
@@ -351,7 +417,8 @@ static mjx_status adaptive_run(const void* plan, const mjx_grid2d* g, const mjx_
   const double dt_init = (dt0 < pb->dt_cfl || dt0 != dt0) ? dt0 : pb->dt_cfl;  // jnp.minimum
   h.t = t0; h.dt = dt_init; h.t_end = t_end; h.prev_err = 1.0; h.dt_cfl = pb->dt_cfl;
   h.cur = 0; h.status = MJX_STATUS_RUNNING_CODE; h.write_idx = 1; h.finite = 1;
-  h.max_saves = max_saves; h.save_every = save_every; h.order = 2; h.save_slot = -1;
+  h.max_saves = max_saves; h.save_every = save_every; h.order = pb->use_strang ? 2 : 1;  // stepping.py:1193
+  h.save_slot = -1;
   h.max_attempts = pb->max_attempts > 0 ? pb->max_attempts : 20 * max_steps + 1000;
   const bool running = (t0 < t_end) && (1 < max_saves);
   if (running) {
@@ -367,11 +434,11 @@ static mjx_status adaptive_run(const void* plan, const mjx_grid2d* g, const mjx_
     MJX_CUDA_TRY(cudaMemcpyAsync(hist_t, &t0, sizeof(double), cudaMemcpyHostToDevice, s));
   }
   if (hist_dt) MJX_CUDA_TRY(cudaMemsetAsync(hist_dt, 0, sizeof(double) * max_saves, s));
-  if (hist_y) MJX_CUDA_TRY(cudaMemcpyAsync(hist_y, y0, nelem * sizeof(T), cudaMemcpyDeviceToDevice, s));
+  if (hist_y) MJX_CUDA_TRY(cudaMemcpyAsync(hist_y, y0, nelem * sizeof(T), cudaMemcpyDefault, s));
   // the host copies above read host memory: make sure they are done before it goes away
   MJX_CUDA_TRY(cudaStreamSynchronize(s));
 
-  const Attempt<T> A = build_attempt<T>(plan, g, pb, pid, ws, L, st);
+  const Attempt<T> A = make_attempt<T>(plan, g, pb, pid, ws, L, st);
   CtlArgs ca;
   memset(&ca, 0, sizeof(ca));
   ca.st = st; ca.partial = (const double*)(ws + L.part); ca.nonfinite = (const int*)(ws + L.bad);
@@ -453,6 +520,29 @@ static mjx_status strang_step(const void* plan, const mjx_grid2d* g, const mjx_i
   mjx_pid_params pid;
   memset(&pid, 0, sizeof(pid));
   pid.atol = 1.0; pid.rtol = 0.0;
+  if (!pb->use_strang) {
+    // E(dt) = H(dt) (y + dt N(y)): E1 and E2 on branch A, then c2r of SA into y_out
+    Attempt<T> E = build_attempt_euler<T>(plan, g, pb, &pid, ws, L, nullptr);
+    const Pairing pg = pairing_for(pb, g);
+    E.k1.rin[0] = y_in; E.k1.rin_sel = -1; E.k1.hfixed = dt; E.k1.npairs = pg.npairs_per_branch;
+    E.k2.hfixed = dt;
+    int nj = 0;
+    for (int j = 0; j < E.k2.njobs; j += 2) E.k2.job[nj++] = E.k2.job[j];
+    E.k2.njobs = nj;
+    RowArgs<T> fin = E.k3;
+    fin.npairs = pg.npairs_per_branch;
+    fin.rout[0] = y_out; fin.rout_sel = -1;
+    cudaError_t e;
+#define MJX_ROW(args)                                                                           \
+  e = E.rx == RX_GRAY_SCOTT ? launch_row<T, RX_GRAY_SCOTT>(args, s)                              \
+      : (E.rx == RX_FISHER ? launch_row<T, RX_FISHER>(args, s) : launch_row<T, RX_NONE>(args, s)); \
+  if (e != cudaSuccess) return cuda_status(e);
+    MJX_ROW(E.k1);
+    MJX_CUDA_TRY(launch_col<T>(E.k2, s));
+    MJX_ROW(fin);
+#undef MJX_ROW
+    return MJX_OK;
+  }
   Attempt<T> A = build_attempt<T>(plan, g, pb, &pid, ws, L, nullptr);
   const long long nelem = (long long)pb->nfields * g->ny * g->nx;
   A.k1.rin[0] = y_in; A.k1.rin_sel = -1;
@@ -496,7 +586,7 @@ static mjx_status attempt_kernel(const void* plan, const mjx_grid2d* g, const mj
     memset(&h, 0, sizeof(h));
     h.t = 0.0; h.dt = dt; h.dtc = dt; h.t_end = 1e300; h.prev_err = 1.0; h.dt_cfl = pb->dt_cfl;
     h.status = MJX_STATUS_RUNNING_CODE; h.write_idx = 1; h.finite = 1; h.max_saves = 1 << 30;
-    h.save_every = 1 << 30; h.max_attempts = 1 << 30; h.order = 2; h.save_slot = -1;
+    h.save_every = 1 << 30; h.max_attempts = 1 << 30; h.order = pb->use_strang ? 2 : 1; h.save_slot = -1;
     const long long nelem = (long long)pb->nfields * g->ny * g->nx;
     MJX_CUDA_TRY(cudaMemcpyAsync(ws + L.y0, y, nelem * sizeof(T), cudaMemcpyDeviceToDevice, s));
     MJX_CUDA_TRY(cudaMemcpyAsync(ws + L.y1, y, nelem * sizeof(T), cudaMemcpyDeviceToDevice, s));
@@ -504,7 +594,8 @@ static mjx_status attempt_kernel(const void* plan, const mjx_grid2d* g, const mj
     MJX_CUDA_TRY(cudaStreamSynchronize(s));
     return MJX_OK;
   }
-  const Attempt<T> A = build_attempt<T>(plan, g, pb, pid, ws, L, st);
+  const Attempt<T> A = make_attempt<T>(plan, g, pb, pid, ws, L, st);
+  if (A.euler && which > 5) return MJX_BAD_ARG;
   cudaError_t e = cudaSuccess;
   auto row = [&](const RowArgs<T>& r) {
     return A.rx == RX_GRAY_SCOTT ? launch_row<T, RX_GRAY_SCOTT>(r, s)
@@ -587,6 +678,19 @@ mjx_status mjx_imex_adaptive2d(const void* plan, const mjx_grid2d* g, int dtype,
   if (max_steps < 0 || save_every < 1) return MJX_BAD_ARG;
   if (ws == nullptr || ws_bytes < mjx_imex2d_ws_bytes(g->ny, g->nx, pb->nfields, dtype)) return MJX_WORKSPACE;
   MJX_TRY(ensure_kernel_attrs());
+  // hist_y in pinned host memory: the history kernel writes it directly (NVLink-C2C on
+  // Grace-Blackwell), through the device view of the allocation
+  if (hist_y) {
+    cudaPointerAttributes pa;
+    MJX_CUDA_TRY(cudaPointerGetAttributes(&pa, hist_y));
+    if (pa.type == cudaMemoryTypeHost) {
+      void* d = nullptr;
+      MJX_CUDA_TRY(cudaHostGetDevicePointer(&d, hist_y, 0));
+      hist_y = d;
+    } else if (pa.type != cudaMemoryTypeDevice && pa.type != cudaMemoryTypeManaged) {
+      return MJX_BAD_ARG;  // pageable host memory cannot be written by the GPU
+    }
+  }
   const Pairing pg = pairing_for(pb, g);
   const ImexLayout L = imex_layout(g->ny, g->nx, pb->nfields, e, pg.nrows, pg.npairs_per_branch);
   cudaStream_t s = (cudaStream_t)stream;

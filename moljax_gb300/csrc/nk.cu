@@ -94,6 +94,24 @@ __global__ void vd_residual_kernel(const double* __restrict__ y, const double* _
   }
 }
 
+// out = s F(y) (the model right-hand side, scaled), constants by value
+__global__ void vd_rhs_kernel(const double* __restrict__ y, double* __restrict__ out, double a,
+                              double b, double c, double s, int n, double idx2, double idy2) {
+  const long long N2 = (long long)n * n;
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < N2;
+       p += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(p / n), j = (int)(p - (long long)i * n);
+    const double uc = y[p];
+    const double ue = dval(y, i, j + 1, n), uw = dval(y, i, j - 1, n);
+    const double un = dval(y, i + 1, j, n), us = dval(y, i - 1, j, n);
+    const double Dc = a + b * uc * uc;
+    const double De = a + b * ue * ue, Dw = a + b * uw * uw, Dn = a + b * un * un, Ds = a + b * us * us;
+    const double fx = 0.5 * (Dc + De) * (ue - uc) - 0.5 * (Dw + Dc) * (uc - uw);
+    const double fy = 0.5 * (Dc + Dn) * (un - uc) - 0.5 * (Ds + Dc) * (uc - us);
+    out[p] = s * (fx * idx2 + fy * idy2 - c * uc * uc * uc);
+  }
+}
+
 // odd extension N x N -> 2N x 2N (Dirichlet cell-centred <-> periodic)
 __global__ void oddext_kernel(const float* __restrict__ r, float* __restrict__ e, int n,
                               const GmresState* gs) {
@@ -345,6 +363,36 @@ __global__ void sumsq32_kernel(const float* v, double* part, long long N2) {
   }
 }
 
+// scaled error partials: sum (E / (atol + rtol |y|))^2 and a non-finite flag on y
+// (scaled_error_norm, moljax/core/state.py:312-343; is_finite, utils.py:186-197)
+__global__ void errnorm_kernel(const double* E, const double* y, double atol, double rtol,
+                               double* part, int* bad, long long N2) {
+  double acc = 0.0;
+  int nf = 0;
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < N2;
+       p += (long long)gridDim.x * blockDim.x) {
+    const double v = y[p];
+    const double q = E[p] / (atol + rtol * fabs(v));
+    acc += q * q;
+    nf |= !isfinite(v);
+  }
+  __shared__ double red[32];
+  __shared__ int redb[32];
+  for (int o = 16; o > 0; o >>= 1) {
+    acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    nf |= __shfl_xor_sync(0xffffffffu, nf, o);
+  }
+  if ((threadIdx.x & 31) == 0) { red[threadIdx.x >> 5] = acc; redb[threadIdx.x >> 5] = nf; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    int b = 0;
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) { s += red[q]; b |= redb[q]; }
+    part[blockIdx.x] = s;
+    bad[blockIdx.x] = b;
+  }
+}
+
 __global__ void nk_consts_kernel(const double* part, int nblk, NKConsts* K, DevState* pst, double n2) {
   __shared__ double red[32];
   double acc = 0.0;
@@ -403,7 +451,7 @@ __global__ void nk_scale_j_kernel(float* V, const GmresState* gs, long long N2) 
 
 // --------------------------------------------------------------- host driver
 struct NKLayout {
-  size_t y0, y1, y2, cst, R, xt, y32, b32, dx, t, e, V, spec, part, gs, K, pst, total;
+  size_t y0, y1, y2, y3, y4, cst, R, xt, y32, b32, dx, t, e, V, spec, part, gs, K, pst, total;
   int nblk, m;
 };
 static inline size_t al(size_t b) { return (b + 255) & ~size_t(255); }
@@ -417,6 +465,8 @@ static NKLayout nk_layout(int n, int m) {
   L.y0 = o; o += al(N2 * 8);
   L.y1 = o; o += al(N2 * 8);
   L.y2 = o; o += al(N2 * 8);
+  L.y3 = o; o += al(N2 * 8);
+  L.y4 = o; o += al(N2 * 8);
   L.cst = o; o += al(N2 * 8);
   L.R = o; o += al(N2 * 8);
   L.xt = o; o += al(N2 * 8);
@@ -653,6 +703,97 @@ static cudaError_t newton(NKRun& r, double* x, const NKParamsC& P, int* n_newton
   return cudaSuccess;
 }
 
+// One implicit step of the reference step functions: be_step (stepping.py:170-214),
+// cn_step (217-260) or bdf2_step (263-310, omega = dt/dt_prev), residuals from
+// create_implicit_residual / create_bdf2_residual (newton_krylov.py:362-448).
+// yc = y_n, yp = y_{n-1} (BDF2 only); the solution is written to yout.
+struct StepOut { int newton, lin, converged; double res; };
+
+static cudaError_t implicit_step(NKRun& r, const NKParamsC& P, const double* abc, int method,
+                                 double dt, double dt_prev, int guess_previous, const double* yc,
+                                 const double* yp, double* yout, StepOut* so) {
+  const long long N2 = (long long)r.n * r.n;
+  NKConsts* K = (NKConsts*)(r.ws + r.L.K);
+  DevState* pst = (DevState*)(r.ws + r.L.pst);
+  double* cst = P64(r, r.L.cst);
+  const double idx2 = 1.0 / (r.dx * r.dx), idy2 = 1.0 / (r.dy * r.dy);
+  NKConsts h;
+  memset(&h, 0, sizeof(h));
+  h.pa = abc[0]; h.pb = abc[1]; h.pc = abc[2];
+  double a1 = -1.0, a2 = 0.0;
+  if (method == MJX_METHOD_BE) {
+    h.a0 = 1.0; h.beta = dt;
+  } else if (method == MJX_METHOD_BDF2) {
+    const double om = dt / dt_prev;
+    h.a0 = (1 + 2 * om) / (1 + om); a1 = -(1 + om); a2 = om * om / (1 + om);
+    h.beta = dt * (1 + om) / (1 + 2 * om);
+  } else {  // CN: R = y - y_n - dt/2 (F_n + F(y)); F_n folded into cst below
+    h.a0 = 1.0; h.beta = 0.5 * dt;
+  }
+  h.alpha = 1.0;
+  cudaError_t e = cudaMemcpyAsync(K, &h, sizeof(h), cudaMemcpyHostToDevice, r.s);
+  if (e != cudaSuccess) return e;
+  if (method == MJX_METHOD_CN) {
+    // R(y_n) with cst = 0 is y_n - dt/2 F(y_n); cst = -y_n - dt/2 F(y_n) = R(y_n) - 2 y_n
+    lincomb_kernel<<<r.grid, 256, 0, r.s>>>(yc, 0.0, nullptr, 0.0, cst, nullptr, N2);
+    vd_residual_kernel<<<r.L.nblk, 256, 0, r.s>>>(yc, cst, P64(r, r.L.R), nullptr, P64(r, r.L.part), K,
+                                                  r.n, idx2, idy2);
+    lincomb_kernel<<<r.grid, 256, 0, r.s>>>(P64(r, r.L.R), 1.0, yc, -2.0, cst, nullptr, N2);
+  } else {
+    lincomb_kernel<<<r.grid, 256, 0, r.s>>>(yc, a1, yp, a2, cst, nullptr, N2);
+  }
+  // initial guess: BDF2 -> 2 y_n - y_{n-1}; BE/CN -> explicit Euler y_n + dt F(y_n)
+  // (stepping.py:195-196, 242-243) or, with guess_previous, y_n
+  if (method == MJX_METHOD_BDF2) {
+    lincomb_kernel<<<r.grid, 256, 0, r.s>>>(yc, 2.0, yp, -1.0, yout, nullptr, N2);
+  } else if (guess_previous) {
+    lincomb_kernel<<<r.grid, 256, 0, r.s>>>(yc, 1.0, nullptr, 0.0, yout, nullptr, N2);
+  } else {
+    // the residual kernel with a0 = 0, beta = -dt, cst = y_n gives y_n + dt F(y_n)
+    NKConsts ge = h;
+    ge.a0 = 0.0; ge.beta = -dt;
+    if ((e = cudaMemcpyAsync(K, &ge, sizeof(ge), cudaMemcpyHostToDevice, r.s)) != cudaSuccess) return e;
+    vd_residual_kernel<<<r.L.nblk, 256, 0, r.s>>>(yc, yc, yout, nullptr, P64(r, r.L.part), K, r.n, idx2, idy2);
+    if ((e = cudaMemcpyAsync(K, &h, sizeof(h), cudaMemcpyHostToDevice, r.s)) != cudaSuccess) return e;
+  }
+  // preconditioner constants from y_n
+  sumsq_kernel<<<r.L.nblk, 256, 0, r.s>>>(yc, P64(r, r.L.part), N2);
+  nk_consts_kernel<<<1, 256, 0, r.s>>>(P64(r, r.L.part), r.L.nblk, K, pst, (double)N2);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  return newton(r, yout, P, &so->newton, &so->lin, &so->converged, &so->res);
+}
+
+// dt * F(y) into out (the BE error estimate of adaptive_integrate, stepping.py:823-826)
+static cudaError_t scaled_rhs(NKRun& r, const double* abc, double dt, const double* y, double* out) {
+  vd_rhs_kernel<<<r.grid, 256, 0, r.s>>>(y, out, abc[0], abc[1], abc[2], dt, r.n, 1.0 / (r.dx * r.dx),
+                                         1.0 / (r.dy * r.dy));
+  return cudaGetLastError();
+}
+
+// NaN-propagating min/max (jnp.minimum / jnp.maximum)
+static inline double hmax(double a, double b) { return (a != a || b != b) ? a + b : (a > b ? a : b); }
+static inline double hmin(double a, double b) { return (a != a || b != b) ? a + b : (a < b ? a : b); }
+static inline double hclip(double x, double lo, double hi) { return hmin(hmax(x, lo), hi); }
+
+static mjx_status nk_setup(NKRun& r, const void* plan2, int n, double dy, double dx,
+                           const mjx_nk_params* nkp, void* ws, size_t ws_bytes, void* stream,
+                           NKParamsC* P) {
+  if (ilog2_exact(n) < 1 || n > 2048 || !(dx > 0) || !(dy > 0)) return MJX_BAD_SHAPE;
+  if (nkp->restart < 1 || nkp->restart > NK_MAXM) return MJX_BAD_ARG;
+  r.plan2 = plan2; r.n = n; r.dy = dy; r.dx = dx; r.ws = (char*)ws; r.L = nk_layout(n, nkp->restart);
+  r.s = (cudaStream_t)stream;
+  r.grid = 152 * 4;
+  r.arnoldi = nullptr;
+  if (ws == nullptr || ws_bytes < r.L.total) return MJX_WORKSPACE;
+  MJX_TRY(ensure_kernel_attrs());
+  MJX_CUDA_TRY(cudaMemsetAsync(r.ws + r.L.pst, 0, sizeof(DevState), r.s));
+  P->max_newton = nkp->max_newton_iters; P->max_krylov = nkp->max_krylov_iters; P->restart = nkp->restart;
+  P->max_backtrack = nkp->max_backtrack; P->newton_tol = nkp->newton_tol; P->krylov_tol = nkp->krylov_tol;
+  P->damping = nkp->damping; P->backtrack = nkp->backtrack_factor; P->min_decrease = nkp->min_residual_decrease;
+  MJX_CUDA_TRY(build_arnoldi_graph(r));
+  return MJX_OK;
+}
+
 }  // namespace mjx
 
 using namespace mjx;
@@ -671,92 +812,31 @@ mjx_status mjx_nk_vardiff_integrate2d(const void* plan2, int n, double dy, doubl
                                       size_t ws_bytes, void* stream) {
   if (plan2 == nullptr || model_abc == nullptr || nkp == nullptr || y0 == nullptr || y_out == nullptr)
     return MJX_BAD_ARG;
-  if (ilog2_exact(n) < 1 || n > 2048 || !(dx > 0) || !(dy > 0) || n_steps < 0) return MJX_BAD_SHAPE;
+  if (n_steps < 0) return MJX_BAD_SHAPE;
   if (method != MJX_METHOD_BE && method != MJX_METHOD_CN && method != MJX_METHOD_BDF2) return MJX_BAD_ARG;
-  if (nkp->restart < 1 || nkp->restart > NK_MAXM) return MJX_BAD_ARG;
   NKRun r;
-  r.plan2 = plan2; r.n = n; r.dy = dy; r.dx = dx; r.ws = (char*)ws; r.L = nk_layout(n, nkp->restart);
-  r.s = (cudaStream_t)stream;
-  r.grid = 152 * 4;
-  if (ws == nullptr || ws_bytes < r.L.total) return MJX_WORKSPACE;
-  MJX_TRY(ensure_kernel_attrs());
-  const long long N2 = (long long)n * n;
-  NKConsts* K = (NKConsts*)(r.ws + r.L.K);
-  DevState* pst = (DevState*)(r.ws + r.L.pst);
-  MJX_CUDA_TRY(cudaMemsetAsync(pst, 0, sizeof(DevState), r.s));
   NKParamsC P;
-  P.max_newton = nkp->max_newton_iters; P.max_krylov = nkp->max_krylov_iters; P.restart = nkp->restart;
-  P.max_backtrack = nkp->max_backtrack; P.newton_tol = nkp->newton_tol; P.krylov_tol = nkp->krylov_tol;
-  P.damping = nkp->damping; P.backtrack = nkp->backtrack_factor; P.min_decrease = nkp->min_residual_decrease;
-  MJX_CUDA_TRY(build_arnoldi_graph(r));
+  MJX_TRY(nk_setup(r, plan2, n, dy, dx, nkp, ws, ws_bytes, stream, &P));
+  const long long N2 = (long long)n * n;
   double* yp = P64(r, r.L.y0);   // y_{n-1}
   double* yc = P64(r, r.L.y1);   // y_n
   double* yn = P64(r, r.L.y2);   // Newton iterate
-  double* cst = P64(r, r.L.cst);
-  MJX_CUDA_TRY(cudaMemcpyAsync(yc, y0, sizeof(double) * N2, cudaMemcpyDeviceToDevice, r.s));
-  MJX_CUDA_TRY(cudaMemcpyAsync(yp, y0, sizeof(double) * N2, cudaMemcpyDeviceToDevice, r.s));
   mjx_status rc = MJX_OK;
+  cudaError_t e = cudaMemcpyAsync(yc, y0, sizeof(double) * N2, cudaMemcpyDeviceToDevice, r.s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(yp, y0, sizeof(double) * N2, cudaMemcpyDeviceToDevice, r.s);
+  if (e != cudaSuccess) { set_last_error(e, __FILE__, __LINE__); rc = MJX_CUDA_ERROR; }
+  // integrate_fixed_dt (stepping.py:1028-1139): BDF2 takes a BE first step
   for (int step = 0; step < n_steps && rc == MJX_OK; ++step) {
-    // residual coefficients (newton_krylov.py:362-448)
-    NKConsts h;
-    memset(&h, 0, sizeof(h));
-    h.pa = model_abc[0]; h.pb = model_abc[1]; h.pc = model_abc[2];
-    const bool be = method == MJX_METHOD_BE || (method == MJX_METHOD_BDF2 && step == 0);
-    double a1 = -1.0, a2 = 0.0;
-    if (be) { h.a0 = 1.0; h.beta = dt; }
-    else if (method == MJX_METHOD_BDF2) {  // omega = dt/dt_prev = 1
-      const double om = 1.0;
-      h.a0 = (1 + 2 * om) / (1 + om); a1 = -(1 + om); a2 = om * om / (1 + om); h.beta = dt * (1 + om) / (1 + 2 * om);
-    } else {  // CN: R = y - y_n - dt/2 (F_n + F(y)); F_n folded into cst below
-      h.a0 = 1.0; h.beta = 0.5 * dt;
-    }
-    h.alpha = 1.0;
-    cudaError_t e = cudaMemcpyAsync(K, &h, sizeof(h), cudaMemcpyHostToDevice, r.s);
-    if (e == cudaSuccess) {
-      // cst = a1 y_n + a2 y_{n-1} (CN: -y_n - dt/2 F(y_n), through the residual kernel at y_n)
-      if (method == MJX_METHOD_CN) {
-        // R(y_n) with cst = 0: a0 y_n - beta F(y_n); cst = -y_n - beta F(y_n) = R(y_n) - 2 y_n
-        lincomb_kernel<<<r.grid, 256, 0, r.s>>>(yc, 0.0, nullptr, 0.0, cst, nullptr, N2);
-        vd_residual_kernel<<<r.L.nblk, 256, 0, r.s>>>(yc, cst, P64(r, r.L.R), nullptr, P64(r, r.L.part), K,
-                                                      n, 1.0 / (dx * dx), 1.0 / (dy * dy));
-        lincomb_kernel<<<r.grid, 256, 0, r.s>>>(P64(r, r.L.R), 1.0, yc, -2.0, cst, nullptr, N2);
-      } else {
-        lincomb_kernel<<<r.grid, 256, 0, r.s>>>(yc, a1, yp, a2, cst, nullptr, N2);
-      }
-      // initial guess: BE -> explicit Euler (stepping.py:195-196) or y_n; BDF2 -> 2 y_n - y_{n-1};
-      // CN -> explicit Euler
-      if (method == MJX_METHOD_BDF2 && !be) {
-        lincomb_kernel<<<r.grid, 256, 0, r.s>>>(yc, 2.0, yp, -1.0, yn, nullptr, N2);
-      } else if ((be || method == MJX_METHOD_CN) && be_guess_previous) {
-        lincomb_kernel<<<r.grid, 256, 0, r.s>>>(yc, 1.0, nullptr, 0.0, yn, nullptr, N2);
-      } else {
-        // y_n + dt F(y_n): residual with a0 = 0, beta = -dt, cst = y_n gives y_n + dt F(y_n)
-        NKConsts ge = h;
-        ge.a0 = 0.0; ge.beta = -dt;
-        e = cudaMemcpyAsync(K, &ge, sizeof(ge), cudaMemcpyHostToDevice, r.s);
-        if (e == cudaSuccess) {
-          vd_residual_kernel<<<r.L.nblk, 256, 0, r.s>>>(yc, yc, yn, nullptr, P64(r, r.L.part), K,
-                                                        n, 1.0 / (dx * dx), 1.0 / (dy * dy));
-          e = cudaMemcpyAsync(K, &h, sizeof(h), cudaMemcpyHostToDevice, r.s);
-        }
-      }
-    }
-    if (e == cudaSuccess) {
-      // preconditioner constants from y_n
-      sumsq_kernel<<<r.L.nblk, 256, 0, r.s>>>(yc, P64(r, r.L.part), N2);
-      nk_consts_kernel<<<1, 256, 0, r.s>>>(P64(r, r.L.part), r.L.nblk, K, pst, (double)N2);
-      e = cudaGetLastError();
-    }
-    int nn = 0, nl = 0, cv = 0;
-    double res = 0.0;
-    if (e == cudaSuccess) e = newton(r, yn, P, &nn, &nl, &cv, &res);
+    const int m = (method == MJX_METHOD_BDF2 && step == 0) ? MJX_METHOD_BE : method;
+    StepOut so;
+    e = implicit_step(r, P, model_abc, m, dt, dt, be_guess_previous, yc, yp, yn, &so);
     if (e != cudaSuccess) { set_last_error(e, __FILE__, __LINE__); rc = MJX_CUDA_ERROR; break; }
-    if (stats) { stats[3 * step] = nn; stats[3 * step + 1] = nl; stats[3 * step + 2] = cv; }
+    if (stats) { stats[3 * step] = so.newton; stats[3 * step + 1] = so.lin; stats[3 * step + 2] = so.converged; }
     // rotate y_{n-1} <- y_n <- y_{n+1}
     double* tmp = yp; yp = yc; yc = yn; yn = tmp;
   }
   if (rc == MJX_OK) {
-    cudaError_t e = cudaMemcpyAsync(y_out, yc, sizeof(double) * N2, cudaMemcpyDeviceToDevice, r.s);
+    e = cudaMemcpyAsync(y_out, yc, sizeof(double) * N2, cudaMemcpyDeviceToDevice, r.s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(r.s);
     if (e != cudaSuccess) { set_last_error(e, __FILE__, __LINE__); rc = MJX_CUDA_ERROR; }
   }
@@ -764,5 +844,193 @@ mjx_status mjx_nk_vardiff_integrate2d(const void* plan2, int n, double dy, doubl
   return rc;
 }
 
-}  // extern "C"
+mjx_status mjx_vardiff_rhs2d(int n, double dy, double dx, const double* model_abc, const double* y,
+                             double* out, void* stream) {
+  if (model_abc == nullptr || y == nullptr || out == nullptr) return MJX_BAD_ARG;
+  if (n < 1 || !(dx > 0) || !(dy > 0)) return MJX_BAD_SHAPE;
+  vd_rhs_kernel<<<152 * 4, 256, 0, (cudaStream_t)stream>>>(y, out, model_abc[0], model_abc[1], model_abc[2],
+                                                           1.0, n, 1.0 / (dx * dx), 1.0 / (dy * dy));
+  return cuda_status(cudaGetLastError());
+}
 
+mjx_status mjx_nk_vardiff_step2d(const void* plan2, int n, double dy, double dx,
+                                 const double* model_abc, int method, double dt, double dt_prev,
+                                 int be_guess_previous, const mjx_nk_params* nkp, const double* y_n,
+                                 const double* y_prev, double* y_out, int* stats, double* res_norm,
+                                 void* ws, size_t ws_bytes, void* stream) {
+  if (plan2 == nullptr || model_abc == nullptr || nkp == nullptr || y_n == nullptr || y_out == nullptr)
+    return MJX_BAD_ARG;
+  if (method != MJX_METHOD_BE && method != MJX_METHOD_CN && method != MJX_METHOD_BDF2) return MJX_BAD_ARG;
+  if (method == MJX_METHOD_BDF2 && (y_prev == nullptr || !(dt_prev > 0))) return MJX_BAD_ARG;
+  NKRun r;
+  NKParamsC P;
+  MJX_TRY(nk_setup(r, plan2, n, dy, dx, nkp, ws, ws_bytes, stream, &P));
+  const long long N2 = (long long)n * n;
+  double* yc = P64(r, r.L.y1);
+  double* yp = P64(r, r.L.y0);
+  double* yn = P64(r, r.L.y2);
+  mjx_status rc = MJX_OK;
+  cudaError_t e = cudaMemcpyAsync(yc, y_n, sizeof(double) * N2, cudaMemcpyDeviceToDevice, r.s);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(yp, y_prev ? y_prev : y_n, sizeof(double) * N2, cudaMemcpyDeviceToDevice, r.s);
+  StepOut so;
+  memset(&so, 0, sizeof(so));
+  if (e == cudaSuccess) e = implicit_step(r, P, model_abc, method, dt, dt_prev, be_guess_previous, yc, yp, yn, &so);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(y_out, yn, sizeof(double) * N2, cudaMemcpyDeviceToDevice, r.s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(r.s);
+  if (e != cudaSuccess) { set_last_error(e, __FILE__, __LINE__); rc = MJX_CUDA_ERROR; }
+  if (stats) { stats[0] = so.newton; stats[1] = so.lin; stats[2] = so.converged; }
+  if (res_norm) *res_norm = so.res;
+  if (r.arnoldi) cudaGraphExecDestroy(r.arnoldi);
+  return rc;
+}
+
+mjx_status mjx_nk_vardiff_adaptive2d(const void* plan2, int n, double dy, double dx,
+                                     const double* model_abc, int method,
+                                     const mjx_pid_params* pid, double t0, double t_end, double dt0,
+                                     int max_steps, int save_every, int be_guess_previous,
+                                     const mjx_nk_params* nkp, const double* y0, double* y_final,
+                                     double* hist_t, double* hist_dt, double* hist_y,
+                                     int* nk_totals, double* attempt_log, int log_cap,
+                                     mjx_adaptive_result* res, void* ws, size_t ws_bytes,
+                                     void* stream) {
+  if (plan2 == nullptr || model_abc == nullptr || nkp == nullptr || pid == nullptr || y0 == nullptr ||
+      y_final == nullptr)
+    return MJX_BAD_ARG;
+  if (method != MJX_METHOD_BE && method != MJX_METHOD_CN && method != MJX_METHOD_BDF2) return MJX_BAD_ARG;
+  if (max_steps < 0 || save_every < 1) return MJX_BAD_ARG;
+  NKRun r;
+  NKParamsC P;
+  MJX_TRY(nk_setup(r, plan2, n, dy, dx, nkp, ws, ws_bytes, stream, &P));
+  const long long N2 = (long long)n * n;
+  // buffers: y_{n-1}, y_n, candidate, BE comparison solve, error
+  double* yp = P64(r, r.L.y0);
+  double* yc = P64(r, r.L.y1);
+  double* yn = P64(r, r.L.y2);
+  double* ybe = P64(r, r.L.y3);
+  double* E = P64(r, r.L.y4);
+  double* part = P64(r, r.L.part);
+  int* bad = (int*)(part + r.L.nblk);  // the part buffer holds (m + 2) * nblk doubles
+  const int max_saves = max_steps / save_every + 1;
+  const int order = method == MJX_METHOD_BE ? 1 : 2;  // compute_error_order (dt_policy.py:411-423)
+  // AdaptiveState initial values (stepping.py:778-813); implicit methods take dt0 as is
+  double t = t0, dt = dt0, dt_prev = dt0, prev_err = 1.0;
+  int step_count = 0, write_idx = 1, n_acc = 0, n_rej = 0, attempts = 0;
+  int status = MJX_STATUS_RUNNING_CODE, all_finite = 1;
+  int tot_newton = 0, tot_lin = 0, not_conv = 0;
+  const int max_attempts = 20 * max_steps + 1000;  // bound on the host loop
+  mjx_status rc = MJX_OK;
+  cudaError_t e = cudaMemcpyAsync(yc, y0, sizeof(double) * N2, cudaMemcpyDeviceToDevice, r.s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(yp, y0, sizeof(double) * N2, cudaMemcpyDeviceToDevice, r.s);
+  if (e == cudaSuccess && hist_y) e = cudaMemcpyAsync(hist_y, y0, sizeof(double) * N2, cudaMemcpyDeviceToDevice, r.s);
+  if (hist_t) { for (int i = 0; i < max_saves; ++i) hist_t[i] = 0.0; hist_t[0] = t0; }
+  if (hist_dt) for (int i = 0; i < max_saves; ++i) hist_dt[i] = 0.0;
+  if (e != cudaSuccess) { set_last_error(e, __FILE__, __LINE__); rc = MJX_CUDA_ERROR; }
+  while (rc == MJX_OK && status == MJX_STATUS_RUNNING_CODE && t < t_end && write_idx < max_saves &&
+         attempts < max_attempts) {
+    ++attempts;
+    const double dtc = hmin(dt, t_end - t);
+    StepOut so, sb;
+    // adaptive_integrate implicit branch (stepping.py:818-858)
+    const bool be_only = method == MJX_METHOD_BE || (method == MJX_METHOD_BDF2 && step_count < 1);
+    if (be_only) {
+      e = implicit_step(r, P, model_abc, MJX_METHOD_BE, dtc, dt_prev, be_guess_previous, yc, yp, yn, &so);
+      if (e == cudaSuccess) e = scaled_rhs(r, model_abc, dtc, yn, E);
+    } else {
+      e = implicit_step(r, P, model_abc, method, dtc, dt_prev, be_guess_previous, yc, yp, yn, &so);
+      if (e == cudaSuccess)
+        e = implicit_step(r, P, model_abc, MJX_METHOD_BE, dtc, dt_prev, be_guess_previous, yc, yp, ybe, &sb);
+      if (e == cudaSuccess) {
+        lincomb_kernel<<<r.grid, 256, 0, r.s>>>(yn, 1.0, ybe, -1.0, E, nullptr, N2);
+        e = cudaGetLastError();
+      }
+    }
+    double hp[152 * 4];
+    int hb[152 * 4];
+    if (e == cudaSuccess) {
+      errnorm_kernel<<<r.L.nblk, 256, 0, r.s>>>(E, yn, pid->atol, pid->rtol, part, bad, N2);
+      e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hp, part, sizeof(double) * r.L.nblk, cudaMemcpyDeviceToHost, r.s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(hb, bad, sizeof(int) * r.L.nblk, cudaMemcpyDeviceToHost, r.s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(r.s);
+    if (e != cudaSuccess) { set_last_error(e, __FILE__, __LINE__); rc = MJX_CUDA_ERROR; break; }
+    double ssum = 0.0, c = 0.0;
+    int nonfinite = 0;
+    for (int i = 0; i < r.L.nblk; ++i) {  // Kahan
+      const double yv = hp[i] - c, tv = ssum + yv;
+      c = (tv - ssum) - yv;
+      ssum = tv;
+      nonfinite |= hb[i];
+    }
+    tot_newton += so.newton; tot_lin += so.lin; not_conv += !so.converged;
+    const double err = hmax(sqrt(ssum / (double)N2), 1e-10);
+    const bool finite = !nonfinite;
+    const bool accept = (err <= 1.0) && finite && so.converged;
+    // propose_dt (dt_policy.py:324-408) for an implicit method
+    double dt_a, pe_new = prev_err;
+    if (err <= 1.0) {  // pid_controller_dt (178-227)
+      const double kI = pid->kI / order, kP = pid->kP / order;
+      const double es = hmax(err, 1e-10), pes = hmax(prev_err, 1e-10);
+      const double fac = hclip(pow(1.0 / es, kI) * pow(pes / es, kP) * pid->safety, pid->min_factor, pid->max_factor);
+      dt_a = hclip(dtc * fac, pid->dt_min, pid->dt_max);
+      pe_new = err;
+    } else {  // handle_rejected_step (230-268)
+      const double kI = pid->kI / order;
+      const double fac = hclip(pid->safety * pow(1.0 / hmax(err, 1.0), kI), pid->min_factor, 1.0);
+      dt_a = hclip(dtc * fac, pid->dt_min, pid->dt_max);
+    }
+    // implicit_robustness_dt (279-321) with its defaults, then the final clamp
+    double dt_r = so.converged ? dt_a : dt_a * 0.5;
+    if (so.converged && so.newton <= 3) dt_r = hmin(dt_r * 1.2, 1.0);
+    dt_r = hclip(dt_r, 1e-12, 1.0);
+    const double dt_new = hclip(dt_r, pid->dt_min, pid->dt_max);
+    if (attempt_log && attempts <= log_cap) {
+      double* L = attempt_log + 6 * (attempts - 1);
+      L[0] = t; L[1] = dtc; L[2] = err; L[3] = so.converged; L[4] = so.newton; L[5] = accept;
+    }
+    if (accept) {  // stepping.py:931-964
+      if (n_acc % save_every == 0) {
+        if (hist_t) hist_t[write_idx] = t + dtc;
+        if (hist_dt) hist_dt[write_idx - 1] = dtc;
+        if (hist_y) {
+          e = cudaMemcpyAsync(hist_y + (long long)write_idx * N2, yn, sizeof(double) * N2,
+                              cudaMemcpyDeviceToDevice, r.s);
+          if (e != cudaSuccess) { set_last_error(e, __FILE__, __LINE__); rc = MJX_CUDA_ERROR; break; }
+        }
+        ++write_idx;
+      }
+      t = t + dtc;
+      double* tmp = yp; yp = yc; yc = yn; yn = tmp;  // y_prev <- y, y <- y_new
+      dt = dt_new;
+      dt_prev = dtc;
+      ++step_count;
+      prev_err = pe_new;
+      ++n_acc;
+    } else {  // stepping.py:966-992
+      dt = hmax(dt_new * 0.5, pid->dt_min);
+      if (dt <= pid->dt_min * 1.1) status = MJX_STATUS_DT_TOO_SMALL_CODE;
+      ++n_rej;
+    }
+    if (!finite) { status = MJX_STATUS_NON_FINITE_CODE; all_finite = 0; }
+  }
+  if (rc == MJX_OK) {
+    // final status (stepping.py:1003-1010)
+    if (t >= t_end) status = MJX_STATUS_SUCCESS_CODE;
+    else if (write_idx >= max_saves) status = MJX_STATUS_MAX_STEPS_CODE;
+    else if (status == MJX_STATUS_RUNNING_CODE) status = MJX_STATUS_MAX_STEPS_CODE;
+    e = cudaMemcpyAsync(y_final, yc, sizeof(double) * N2, cudaMemcpyDeviceToDevice, r.s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(r.s);
+    if (e != cudaSuccess) { set_last_error(e, __FILE__, __LINE__); rc = MJX_CUDA_ERROR; }
+  }
+  if (res) {
+    res->t_final = t; res->dt_next = dt; res->prev_err = prev_err; res->last_err = 0.0;
+    res->n_accepted = n_acc; res->n_rejected = n_rej; res->n_attempts = attempts;
+    res->n_saved = write_idx; res->status = status; res->finite = all_finite;
+  }
+  if (nk_totals) { nk_totals[0] = tot_newton; nk_totals[1] = tot_lin; nk_totals[2] = not_conv; }
+  if (r.arnoldi) cudaGraphExecDestroy(r.arnoldi);
+  return rc;
+}
+
+}  // extern "C"

@@ -68,6 +68,22 @@ __device__ __forceinline__ void react_heun(T& a, T& b, T h, T F, T k, T r) {
   }
 }
 
+// Explicit Euler reaction step y + h N(y) (imex_euler_step, stepping.py:349-359).
+template <typename T, int RX>
+__device__ __forceinline__ void react_euler(T& a, T& b, T h, T F, T k, T r) {
+  if (RX == RX_GRAY_SCOTT) {
+    const T uvv = a * b * b;
+    const T fu = -uvv + F * ((T)1 - a);
+    const T fv = uvv - (F + k) * b;
+    a = a + h * fu;
+    b = b + h * fv;
+  } else if (RX == RX_FISHER) {
+    const T fa = r * a * ((T)1 - a), fb = r * b * ((T)1 - b);
+    a = a + h * fa;
+    b = b + h * fb;
+  }
+}
+
 template <typename T> __device__ __forceinline__ bool finite_(T v) { return isfinite(v); }
 
 // The Heun increment y** - y* computed without forming y** (no cancellation).
@@ -197,6 +213,7 @@ __global__ void __launch_bounds__(256, Occ<T>::row) row_kernel(const __grid_cons
     }
     if (flags & ROW_REACT) {
       if (flags & ROW_DELTA) react_delta<T, RX>(va, vb, h, (T)a.F, (T)a.k, (T)a.r);
+      else if (flags & ROW_EULER) react_euler<T, RX>(va, vb, h, (T)a.F, (T)a.k, (T)a.r);
       else react_heun<T, RX>(va, vb, h, (T)a.F, (T)a.k, (T)a.r);
     }
     if (flags & ROW_STORE_REAL) { oa[x] = va; ob[x] = vb; }

@@ -43,6 +43,7 @@ enum {
   ROW_ERRPAIR = 64,    // accumulate (a / (atol + rtol |b|))^2: a = error row, b = solution row
   ROW_NONLIN = 128,    // replace (a, b) by the reaction terms N(a, b) (exponential integrators)
   ROW_SPEC_ALT = 256,  // store the spectrum at (oa, ob) instead of (sa, sb)
+  ROW_EULER = 512,     // with ROW_REACT: explicit Euler reaction step instead of Heun
 };
 
 // pointwise reaction kinds (compile-time)

@@ -205,6 +205,146 @@ def bdf2_integrate(u0, dy, dx, dt, n_steps, a=1.0, b=1.0, c=1.0, restart=30, new
     return u, stats
 
 
+def implicit_step(u, u_prev, method, dt, dt_prev, dy, dx, a=1.0, b=1.0, c=1.0, restart=30,
+                  newton_tol=1e-8, krylov_tol=1e-6, max_krylov=50, max_newton=10,
+                  be_guess="euler"):
+    """be_step / cn_step / bdf2_step (moljax/core/stepping.py:170-310) for the model above.
+
+    method: "be", "cn" or "bdf2"; returns (u_new, converged, newton_iters, gmres_iters).
+    """
+    F = lambda y: vardiff_F(y, dy, dx, a, b, c)  # noqa: E731
+    J = lambda y, v: vardiff_JF(y, v, dy, dx, a, b, c)  # noqa: E731
+    if method == "be":
+        a0, beta, cst = 1.0, dt, -u
+    elif method == "cn":
+        a0, beta, cst = 1.0, 0.5 * dt, -u - 0.5 * dt * F(u)
+    else:
+        a0, a1, a2, beta = bdf2_coeffs(dt, dt_prev)
+        cst = a1 * u + a2 * u_prev
+    if method == "bdf2":
+        guess = 2 * u - u_prev
+    else:
+        guess = u + dt * F(u) if be_guess == "euler" else u.copy()
+    Dbar = a + b * float(np.mean(u * u))
+    res = lambda y: a0 * y + cst - beta * F(y)  # noqa: E731
+    jvp = lambda y, v: a0 * v - beta * J(y, v)  # noqa: E731
+    Mi = lambda r: dirichlet_helmholtz(r, dy, dx, a0, beta * Dbar)  # noqa: E731
+    un, conv, it, li, rr = newton_krylov(res, jvp, guess, Mi, newton_tol, krylov_tol,
+                                         max_newton=max_newton, restart=restart,
+                                         max_krylov=max_krylov)
+    return un, conv, it, li
+
+
+def adaptive_integrate_implicit(u0, dy, dx, method, t0, t_end, dt0, atol=1e-6, rtol=1e-3,
+                                safety=0.9, kI=0.7, kP=0.4, dt_min=1e-12, dt_max=1.0,
+                                max_factor=5.0, min_factor=0.2, max_steps=10000,
+                                save_every=1, a=1.0, b=1.0, c=1.0, be_guess="euler", **nk):
+    """Implicit branch of adaptive_integrate (moljax/core/stepping.py:723-1021).
+
+    Error: BE -> dt F(y_be); CN/BDF2 -> y_method - y_BE (BDF2 starts with BE while
+    step_count < 1).  propose_dt (dt_policy.py:324-408): PI on accept, the reject
+    formula otherwise, then implicit_robustness_dt (279-321, defaults: x0.5 when
+    Newton did not converge, x1.2 capped at 1.0 when it converged in <= 3
+    iterations, clip to [1e-12, 1]) and the final clamp to [dt_min, dt_max].
+    Returns dict(t, u, t_hist, dt_hist, n_acc, n_rej, status, write_idx).
+    """
+    order = 1 if method == "be" else 2
+    max_saves = max_steps // save_every + 1
+    t_hist, dt_hist = np.zeros(max_saves), np.zeros(max_saves)
+    t_hist[0] = t0
+    nan_max = lambda x, y: x + y if (x != x or y != y) else max(x, y)  # noqa: E731
+    nan_min = lambda x, y: x + y if (x != x or y != y) else min(x, y)  # noqa: E731
+    clip = lambda x, lo, hi: nan_min(nan_max(x, lo), hi)  # noqa: E731
+    t, u, u_prev, dt, dt_prev = float(t0), u0.copy(), u0.copy(), float(dt0), float(dt0)
+    prev_err, step_count, write_idx, n_acc, n_rej, status = 1.0, 0, 1, 0, 0, 1
+    log = []
+    while status == 1 and t < t_end and write_idx < max_saves:
+        dtc = nan_min(dt, t_end - t)
+        if method == "be" or (method == "bdf2" and step_count < 1):
+            un, conv, it, _ = implicit_step(u, u_prev, "be", dtc, dt_prev, dy, dx, a, b, c,
+                                            be_guess=be_guess, **nk)
+            err = dtc * vardiff_F(un, dy, dx, a, b, c)
+        else:
+            un, conv, it, _ = implicit_step(u, u_prev, method, dtc, dt_prev, dy, dx, a, b, c,
+                                            be_guess=be_guess, **nk)
+            ube, _, _, _ = implicit_step(u, u_prev, "be", dtc, dt_prev, dy, dx, a, b, c,
+                                         be_guess=be_guess, **nk)
+            err = un - ube
+        q = err / (atol + rtol * np.abs(un))
+        e = nan_max(float(np.sqrt(np.sum(q * q) / q.size)), 1e-10)
+        finite = bool(np.all(np.isfinite(un)))
+        accept = e <= 1.0 and finite and conv
+        if e <= 1.0:
+            fac = clip((1.0 / max(e, 1e-10)) ** (kI / order) * (max(prev_err, 1e-10) / max(e, 1e-10))
+                       ** (kP / order) * safety, min_factor, max_factor)
+            dt_a, pe_new = clip(dtc * fac, dt_min, dt_max), e
+        else:
+            fac = clip(safety * (1.0 / nan_max(e, 1.0)) ** (kI / order), min_factor, 1.0)
+            dt_a, pe_new = clip(dtc * fac, dt_min, dt_max), prev_err
+        dt_r = dt_a if conv else dt_a * 0.5
+        if conv and it <= 3:
+            dt_r = nan_min(dt_r * 1.2, 1.0)
+        dt_new = clip(clip(dt_r, 1e-12, 1.0), dt_min, dt_max)
+        log.append((t, dtc, e, conv, it, accept))
+        if accept:
+            if n_acc % save_every == 0:
+                t_hist[write_idx] = t + dtc
+                dt_hist[write_idx - 1] = dtc
+                write_idx += 1
+            t = t + dtc
+            u_prev, u = u, un
+            dt, dt_prev = dt_new, dtc
+            step_count += 1
+            prev_err = pe_new
+            n_acc += 1
+        else:
+            dt = nan_max(dt_new * 0.5, dt_min)
+            if dt <= dt_min * 1.1:
+                status = 3
+            n_rej += 1
+        if not finite:
+            status = 4
+    if t >= t_end:
+        status = 0
+    elif write_idx >= max_saves:
+        status = 2
+    return dict(t=t, u=u, t_hist=t_hist, dt_hist=dt_hist, n_acc=n_acc, n_rej=n_rej,
+                status=status, write_idx=write_idx, log=log)
+
+
+def replay_implicit_controller(log, method, t0, t_end, dt0, safety=0.9, kI=0.7, kP=0.4,
+                               dt_min=1e-12, dt_max=1.0, max_factor=5.0, min_factor=0.2):
+    """Re-runs the accept/reject and dt logic of adaptive_integrate's implicit branch on a
+    recorded attempt sequence (t, dt, err, converged, newton_iters, accepted) and returns the
+    (t, dt, accepted) each attempt should have had (stepping.py:723-1021, dt_policy.py:178-408)."""
+    order = 1 if method == "be" else 2
+    nan_max = lambda x, y: x + y if (x != x or y != y) else max(x, y)  # noqa: E731
+    nan_min = lambda x, y: x + y if (x != x or y != y) else min(x, y)  # noqa: E731
+    clip = lambda x, lo, hi: nan_min(nan_max(x, lo), hi)  # noqa: E731
+    t, dt, prev_err = float(t0), float(dt0), 1.0
+    out = []
+    for (_, _, e, conv, it, _) in log:
+        dtc = nan_min(dt, t_end - t)
+        accept = e <= 1.0 and bool(conv)
+        out.append((t, dtc, accept))
+        if e <= 1.0:
+            fac = clip((1.0 / max(e, 1e-10)) ** (kI / order) * (max(prev_err, 1e-10) / max(e, 1e-10))
+                       ** (kP / order) * safety, min_factor, max_factor)
+            dt_a, pe_new = clip(dtc * fac, dt_min, dt_max), e
+        else:
+            fac = clip(safety * (1.0 / nan_max(e, 1.0)) ** (kI / order), min_factor, 1.0)
+            dt_a, pe_new = clip(dtc * fac, dt_min, dt_max), prev_err
+        dt_r = dt_a if conv else dt_a * 0.5
+        if conv and it <= 3:
+            dt_r = nan_min(dt_r * 1.2, 1.0)
+        dt_new = clip(clip(dt_r, 1e-12, 1.0), dt_min, dt_max)
+        if accept:
+            t, dt, prev_err = t + dtc, dt_new, pe_new
+        else:
+            dt = nan_max(dt_new * 0.5, dt_min)
+    return out
+
+
 def gaussians_ic(n, seed=4, count=8):
     """Seeded sum of 8 Gaussians on [0,1]^2 cell centres: A~U[0,1], w~U[0.02,0.1], c~U[0,1]^2."""
     rng = np.random.default_rng(seed)

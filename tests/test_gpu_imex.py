@@ -168,3 +168,69 @@ def test_host_driven_loop_matches_device_loop(cuda, tmp_path):
         assert list(child[prec + "_counts"]) == [r.n_accepted, r.n_rejected, r.status]
         np.testing.assert_array_equal(child[prec + "_u"], r.y_final["u"].cpu().numpy())
         np.testing.assert_array_equal(child[prec + "_t"], r.t_history.cpu().numpy())
+
+
+@pytest.mark.parametrize("n", [16, 128])
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+def test_imex_euler_step_vs_oracle(cuda, n, dtype):
+    M, grid, model, cache, diff, ym, og, y0, om, lam, od = _setup(n, dtype, cuda)
+    out = M.imex_euler_step(model, ym, 0.0, 0.8, cache, diff)
+    ref = OI.imex_euler_step(om, y0, 0.8, lam, od)
+    tol = 1e-13 if dtype == torch.float64 else 2e-6
+    for k in ("u", "v"):
+        assert _rel(out[k].cpu().numpy(), ref[k]) < tol
+
+
+def test_imex_euler_fixed_dt_vs_oracle(cuda):
+    M, grid, model, cache, diff, ym, og, y0, om, lam, od = _setup(32, torch.float64, cuda)
+    t, ys, yf = M.integrate_imex_fixed_dt(model, ym, 0.0, 4.0, 0.5, cache, diff, use_strang=False)
+    to, yo, yfo = OI.integrate_imex_fixed_dt(om, y0, 0.0, 4.0, 0.5, lam, od, use_strang=False)
+    np.testing.assert_allclose(t.numpy(), np.asarray(to), rtol=1e-14)
+    for k in ("u", "v"):
+        assert _rel(yf[k].cpu().numpy(), yfo[k]) < 1e-12
+
+
+def test_adaptive_imex_euler_matches_oracle_counts(cuda):
+    # order-1 step doubling: same accept/reject sequence and result as the oracle
+    M, grid, model, cache, diff, ym, og, y0, om, lam, od = _setup(32, torch.float64, cuda)
+    pid = M.PIDParams(atol=1e-6, rtol=1e-4)
+    r = M.adaptive_integrate(model, ym, 0.0, 15.0, 1.0, M.IntegratorType.IMEX_EULER,
+                             max_steps=5000, pid_params=pid, save_every=1)
+    ro = OI.adaptive_integrate_imex(om, y0, 0.0, 15.0, 1.0, lam, od, use_strang=False,
+                                    pid=OI.PIDParams(atol=1e-6, rtol=1e-4), save_every=1,
+                                    max_steps=5000)
+    assert r.status == ro.status == 0
+    assert (r.n_accepted, r.n_rejected) == (ro.n_accepted, ro.n_rejected)
+    assert r.n_rejected > 0 or r.n_accepted > 5
+    nh = ro.n_steps
+    np.testing.assert_allclose(r.t_history.cpu().numpy()[:nh], ro.t_history[:nh], rtol=1e-9)
+    for k in ("u", "v"):
+        assert _rel(r.y_final[k].cpu().numpy(), ro.y_final[k]) < 1e-10
+
+
+def test_adaptive_imex_euler_fp32(cuda):
+    M, grid, model, cache, diff, ym, og, y0, om, lam, od = _setup(64, torch.float32, cuda)
+    pid = M.PIDParams(atol=1e-6, rtol=1e-4)
+    r = M.adaptive_integrate_imex(model, ym, 0.0, 10.0, 1.0, cache, diff, use_strang=False,
+                                  pid_params=pid, save_every=1000, save_y_history=False)
+    ro = OI.adaptive_integrate_imex(om, y0, 0.0, 10.0, 1.0, lam, od, use_strang=False,
+                                    pid=OI.PIDParams(atol=1e-6, rtol=1e-4), save_every=1000,
+                                    keep_history=False)
+    assert r.status == ro.status == 0
+    assert abs(r.n_accepted - ro.n_accepted) <= 2
+    for k in ("u", "v"):
+        assert _rel(r.y_final[k].cpu().numpy(), ro.y_final[k]) < 1e-5
+
+
+def test_history_streamed_to_host_equals_device_history(cuda):
+    # save_y_history="host": the history kernel writes pinned host memory directly
+    M, grid, model, cache, diff, ym, og, y0, om, lam, od = _setup(64, torch.float32, cuda)
+    pid = M.PIDParams(atol=1e-7, rtol=1e-5)
+    kw = dict(pid_params=pid, save_every=2, max_steps=400, precision="fp32")
+    rd = M.adaptive_integrate_imex(model, ym, 0.0, 12.0, 1.0, cache, diff, save_y_history=True, **kw)
+    rh = M.adaptive_integrate_imex(model, ym, 0.0, 12.0, 1.0, cache, diff, save_y_history="host", **kw)
+    assert rh.y_history["u"].device.type == "cpu" and rh.y_history["u"].is_pinned()
+    assert (rd.n_accepted, rd.n_steps) == (rh.n_accepted, rh.n_steps)
+    k = rd.n_steps
+    for f in ("u", "v"):
+        np.testing.assert_array_equal(rh.y_history[f][:k].numpy(), rd.y_history[f][:k].cpu().numpy())

@@ -58,3 +58,18 @@ def test_readme_kwargs_and_jacobi_preconditioner():
     r = newton_krylov_solve(lambda x: x * x - 4.0, torch.tensor([1.0], dtype=torch.float64),
                             gmres_restart=30, rtol=1e-10)
     assert abs(float(r.solution[0]) - 2.0) < 1e-8
+
+
+def test_oracle_controller_replay_matches_oracle_run():
+    # the replayed controller (used to check the native adaptive implicit driver) makes the
+    # same decisions as the oracle's own adaptive run
+    from oracle import nk as ONK
+    n = 16
+    dx = 1.0 / n
+    u0 = ONK.gaussians_ic(n)
+    ro = ONK.adaptive_integrate_implicit(u0, dx, dx, "cn", 0.0, 0.01, 100 * dx * dx, atol=1e-4,
+                                         rtol=1e-2, restart=20, be_guess="previous")
+    rep = ONK.replay_implicit_controller(ro["log"], "cn", 0.0, 0.01, 100 * dx * dx)
+    assert ro["status"] == 0 and len(rep) == len(ro["log"]) > 3
+    for (t, dt, _, _, _, acc), (t2, dt2, acc2) in zip(ro["log"], rep):
+        assert (t, dt, bool(acc)) == (t2, dt2, acc2)

@@ -164,3 +164,35 @@ def test_etdrk4_oracle_orders():
             assert e1 / e2 > lo
         else:
             assert e1 / e2 < 4.0
+
+
+# ---------------------------------------------------------------- DST-I (fft_nonperiodic.py)
+def test_dst_oracle_pins():
+    import scipy.fft
+    from oracle import dst as OD
+    # tests/test_fft_nonperiodic.py:24-33: DST then IDST recovers the input (rtol 1e-10)
+    N = 32
+    x = np.sin(np.pi * np.arange(1, N + 1) / (N + 1))
+    np.testing.assert_allclose(OD.idst_I_fast(OD.dst_I_fast(x)), x, rtol=1e-10)
+    # 35-46: DST of sin(pi x) concentrates in mode 1
+    N = 64
+    f = np.sin(np.pi * np.arange(1, N + 1) / (N + 1))
+    F = OD.dst_I_fast(f)
+    assert abs(F[0]) > 0.9 * np.linalg.norm(F)
+    # eigenvalues negative and increasing in magnitude (52-70)
+    lam = OD.laplacian_symbol_dirichlet(32, 0.1)
+    assert np.all(lam < 0) and np.all(np.diff(np.abs(lam)) >= 0)
+    # scipy's type-1 DST is twice this transform, for any N
+    rng = np.random.default_rng(0)
+    for N in (1, 2, 7, 33, 100):
+        x = rng.standard_normal((3, N))
+        np.testing.assert_allclose(OD.dst_I_fast(x), 0.5 * scipy.fft.dst(x, type=1, axis=-1),
+                                   rtol=1e-12, atol=1e-12)
+    # the Helmholtz solve inverts (I - dt D Lap_D) with the 3-point Dirichlet Laplacian
+    N, dx, dt, D = 50, 0.02, 0.3, 0.7
+    u = rng.standard_normal(N)
+    lam = OD.laplacian_symbol_dirichlet(N, dx)
+    A = (np.diag(-2.0 * np.ones(N)) + np.diag(np.ones(N - 1), 1) + np.diag(np.ones(N - 1), -1)) / dx ** 2
+    rhs = u - dt * D * A @ u
+    np.testing.assert_allclose(OD.solve_helmholtz_dirichlet(rhs, lam, dt, D), u, rtol=1e-10, atol=1e-12)
+    np.testing.assert_allclose(OD.solve_poisson_dirichlet(A @ u, lam), u, rtol=1e-9, atol=1e-11)
