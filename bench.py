@@ -8,6 +8,7 @@ of the reaction increments (rel-L2 vs the FP64 path is reported in the line).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
   python bench.py --kernels-only [--reps R]   # per-kernel CUDA-event times only
+  python bench.py --workload etdrk4 --n 4096 [--etd-steps S] [--kernels-only]
 
 Our arm prints one JSON line with the device-timed value, the end-to-end
 number through the public API with host buffers, the live roofline of the
@@ -57,6 +58,8 @@ def parse():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp32"])
     ap.add_argument("--kernels-only", action="store_true")
+    ap.add_argument("--workload", default="imex", choices=["imex", "etdrk4"])
+    ap.add_argument("--etd-steps", type=int, default=100)
     ap.add_argument("--reps", type=int, default=30)
     return ap.parse_args()
 
@@ -388,6 +391,79 @@ def run_ours(args, rank, world, local):
     return out
 
 
+def etd_kernel_bytes(n):
+    """Algorithmic bytes of the 8 ETDRK4 passes of one step (2 fields, FP32): per field and
+    half-spectrum element, complex 8 B / coefficient 4 B accesses (C1 6+2, R1 2, C2 4+2, R2 2,
+    C3 6+2, R3 2, C4 5+4, R4 2)."""
+    nc = n * (n // 2 + 1)
+    per = {"C1": 6 * 8 + 2 * 4, "R1": 16, "C2": 4 * 8 + 2 * 4, "R2": 16, "C3": 6 * 8 + 2 * 4,
+           "R3": 16, "C4": 5 * 8 + 4 * 4, "R4": 16}
+    return {k: 2 * nc * v for k, v in per.items()}
+
+
+def run_etdrk4(args, local):
+    """Fixed-step coupled ETDRK4 Gray-Scott (FP32 state, FP64 contour coefficients) at n^2:
+    grid-pt-steps/s over --etd-steps steps, and the live per-pass roofline."""
+    import torch
+    import moljax_gb300 as M
+    from moljax_gb300 import _native as N
+    from moljax_gb300.core.fft_solvers import get_plan, workspace
+    from moljax_gb300.workloads import gray_scott_initial_condition
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    n = args.n
+    grid = M.Grid2D(n, n, 0.0, L_BOX, 0.0, L_BOX)
+    model = M.create_gray_scott_model(grid, DU, DV, F, K, dtype=torch.float32)
+    y0 = gray_scott_initial_condition(grid, SEED, torch.float32, dev)
+    out = {"workload": f"gray-scott ETDRK4 {n}x{n} FP32, dt=1", "n": n, "steps": args.etd_steps}
+    if not args.kernels_only:
+        M.etdrk4_gray_scott(model, y0, 1.0, 3)
+        torch.cuda.synchronize(dev)
+        s = torch.cuda.current_stream(dev)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        M.etdrk4_gray_scott(model, y0, 1.0, args.etd_steps)
+        e1.record(s)
+        e1.synchronize()
+        t = e0.elapsed_time(e1) * 1e-3
+        out["value"] = n * n * args.etd_steps / t
+        out["unit"] = UNIT
+        out["ms_per_step"] = t / args.etd_steps * 1e3
+    # per-pass timing through the single-kernel entry (workspace left by the run above)
+    plan = get_plan(n, n, grid.dy, grid.dx, "fd", torch.float32, dev)
+    lib = N.lib()
+    ws = workspace(lib.mjx_etdrk4_ws_bytes(n, n, plan.code), plan.device, "etd")
+    if args.kernels_only:
+        M.etdrk4_gray_scott(model, y0, 1.0, 1)
+    names = list(etd_kernel_bytes(n).keys())
+    order = [1, 2, 3, 4, 5, 6, 7, 8]
+    reps = args.reps
+    kt = {}
+    s = torch.cuda.current_stream(dev)
+    for w in order:
+        call = lambda: N.check("mjx_etdrk4_kernel2d", lib.mjx_etdrk4_kernel2d(  # noqa: E731
+            N.ptr(plan.buf), C.byref(plan.cgrid), plan.code, F, K, w, N.ptr(ws), ws.numel(),
+            N.stream_ptr(dev)))
+        for _ in range(min(3, reps)):
+            call()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        for _ in range(reps):
+            call()
+        e1.record(s)
+        e1.synchronize()
+        kt[names[w - 1]] = e0.elapsed_time(e1) / reps * 1e-3
+    kb = etd_kernel_bytes(n)
+    peak, peak_kind = peaks()
+    out["kernel_us"] = {k: v * 1e6 for k, v in kt.items()}
+    out["kernel_gbs"] = {k: kb[k] / kt[k] / 1e9 for k in kt}
+    out["step_alg_bytes"] = sum(kb.values())
+    if "value" in out:
+        out["achieved_gbs"] = sum(kb.values()) / (out["ms_per_step"] * 1e-3) / 1e9
+        out["frac_of_" + peak_kind.replace(" ", "_")] = out["achieved_gbs"] / peak
+    return out
+
+
 def run_kernels_only(args, local):
     import torch
     dev = torch.device("cuda", local)
@@ -462,6 +538,8 @@ def main():
     rank, world, local = dist_env()
     if args.impl == "reference":
         out = run_reference(args, rank, world)
+    elif args.workload == "etdrk4":
+        out = run_etdrk4(args, local)
     elif args.kernels_only:
         out = run_kernels_only(args, local)
     else:

@@ -108,6 +108,14 @@ mjx_status mjx_spectral_apply2d(const void* plan, const mjx_grid2d* grid, int dt
                                 const double* D, double h, int mult, const void* in, void* out,
                                 void* ws, size_t ws_bytes, void* stream);
 
+/* out_f = real(IFFT2( FFT2(in_f) / (1 - h (D_f lam - i (vx_f kx + vy_f ky))) )): the exact
+ * periodic advection-diffusion inverse of FFTAdvectionDiffusionPreconditioner
+ * (moljax/core/preconditioners.py:297-420; kx, ky = 2 pi fftfreq, |denominator| clamped at
+ * 1e-14).  Fields with D <= 1e-14 and |v| <= 1e-14 are copied unchanged. */
+mjx_status mjx_advdiff_apply2d(const void* plan, const mjx_grid2d* grid, int dtype, int nfields,
+                               const double* D, const double* vx, const double* vy, double h,
+                               const void* in, void* out, void* ws, size_t ws_bytes, void* stream);
+
 /* n_steps Crank-Nicolson steps u <- real(IFFT2(G * FFT2(u))) executed one by one;
  * G = (1 + dt D lam/2)/(1 - dt D lam/2).  Replaces the benchmark FFT-CN step
  * (benchmarks/benchmark_vs_scipy.py:74-91) behind fft_solvers.fft_cn_step. */
@@ -160,6 +168,17 @@ mjx_status mjx_unpad2d(const void* padded, void* interior, int nfields, int ny, 
 mjx_status mjx_laplacian2d(const void* padded_in, void* padded_out, int nfields, int ny, int nx,
                            int n_ghost, const double* coef, int fill_bc, const int* kinds,
                            const double* values, double dy, double dx, int dtype, void* stream);
+/* 2D first derivative on padded fields, ghosts read as stored, output ghosts zero:
+ * op 1 upwind along axis with scalar velocity v (d1_upwind_2d, operators.py:200-268),
+ * op 2 central (d1_central_2d, 155-197); axis 0 = y, 1 = x; d = spacing along axis. */
+mjx_status mjx_stencil2d(const void* padded_in, void* padded_out, int nfields, int ny, int nx,
+                        int n_ghost, int op, int axis, double v, double d, int dtype, void* stream);
+/* result[0] = sqrt(sum((err/(atol + rtol |y|))^2) / n) (scaled_error_norm, state.py:312-343),
+ * result[1] = 1 if every y is finite else 0 (is_finite, utils.py:186-197); n values each.
+ * Host result, synchronises the stream; ws: mjx_error_norm_ws_bytes() device bytes. */
+size_t mjx_error_norm_ws_bytes(void);
+mjx_status mjx_scaled_error_norm(const void* err, const void* y, long long n, int dtype, double atol,
+                                 double rtol, double* result, void* ws, size_t ws_bytes, void* stream);
 /* Model right-hand side with BCs applied on the fly: D_f Lap(u_f) + reaction
  * (MOLModel.rhs, model.py:100-118; Gray-Scott operators.py:644-667; for
  * MJX_REACT_FISHER the parameter F carries r, operators.py:680-705). */
@@ -268,6 +287,47 @@ mjx_status mjx_nk_vardiff_adaptive2d(const void* plan2, int n, double dy, double
                                      int* nk_totals, double* attempt_log, int log_cap,
                                      mjx_adaptive_result* res, void* ws, size_t ws_bytes,
                                      void* stream);
+
+/* ---- explicit Runge-Kutta (Euler, SSPRK3, RK4) on the 5-point stencil ------------------ */
+/* Reaction-advection-diffusion model for the explicit steppers: per field D_f Lap(u_f)
+ * - vx du_f/dx - vy du_f/dy (advection 0: none, 1: upwind d1_upwind_2d, operators.py:200-268,
+ * 2: central) plus the reaction, with ghost values from the field's BC (bc.py:202-307) computed
+ * on the fly.  method: 0 Euler, 1 SSPRK3, 2 RK4 (IntegratorType, stepping.py:48-57). */
+typedef struct mjx_explicit_problem {
+  int reaction;          /* mjx_reaction */
+  int nfields;           /* 1..4 */
+  double D[4];
+  double F, k, r;
+  double vx, vy;
+  int advection;
+  int method;
+  int bc_kind[4];        /* mjx_bc_kind per field */
+  double bc_values[16];  /* per field: left, right, bottom, top (Dirichlet value / Neumann flux) */
+  double dt_cfl;         /* heisenberg_cfl_dt (moljax/core/dt_policy.py:104-175), host-computed */
+  int max_attempts;      /* <= 0 -> 20 * max_steps + 1000 */
+  int pad;
+} mjx_explicit_problem;
+
+/* Workspace of the explicit steppers: 7 state-sized buffers plus partials and the state. */
+size_t mjx_explicit_ws_bytes(int ny, int nx, int nfields, int dtype);
+/* n_steps fixed steps of euler_step / ssprk3_step / rk4_step (moljax/core/stepping.py:64-163,
+ * integrate_fixed_dt 1028-1139) on interiors [nfields][ny][nx]; one fused kernel per stage. */
+mjx_status mjx_explicit_integrate2d(const mjx_grid2d* grid, int dtype, const mjx_explicit_problem* prob,
+                                    double dt, int n_steps, const void* y0, void* y_out, void* ws,
+                                    size_t ws_bytes, void* stream);
+/* out = F(y): MOLModel.rhs of this model on interiors (moljax/core/model.py:100-118). */
+mjx_status mjx_explicit_rhs2d(const mjx_grid2d* grid, int dtype, const mjx_explicit_problem* prob,
+                              const void* y, void* out, void* stream);
+/* The explicit branch of adaptive_integrate (moljax/core/stepping.py:723-1021): step doubling
+ * (step_explicit_with_error, 648-682), error order 1/3/4, PI controller with the CFL limit
+ * (propose_dt, dt_policy.py:324-408), accept/reject on the device in a conditional-graph loop.
+ * Same history, result and status semantics as mjx_imex_adaptive2d (hist_y may be pinned
+ * host memory).  Any grid size; any BC per field. */
+mjx_status mjx_explicit_adaptive2d(const mjx_grid2d* grid, int dtype, const mjx_explicit_problem* prob,
+                                   const mjx_pid_params* pid, double t0, double t_end, double dt0,
+                                   int max_steps, int save_every, const void* y0, void* y_final,
+                                   double* hist_t, double* hist_dt, void* hist_y, void* ws,
+                                   size_t ws_bytes, mjx_adaptive_result* result, void* stream);
 
 /* ---- DST-I and the Dirichlet spectral solvers -------------------------------------- */
 /* Plan of the length-n DST-I (twiddles; for 2(n+1) not a power of two, the Bluestein

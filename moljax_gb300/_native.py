@@ -58,6 +58,14 @@ class ReactorInstanceC(C.Structure):
                 ("dt", C.c_double), ("c_init", C.c_double), ("c_inlet", C.c_double)]
 
 
+class ExplicitProblemC(C.Structure):
+    _fields_ = [("reaction", C.c_int), ("nfields", C.c_int), ("D", C.c_double * 4),
+                ("F", C.c_double), ("k", C.c_double), ("r", C.c_double), ("vx", C.c_double),
+                ("vy", C.c_double), ("advection", C.c_int), ("method", C.c_int),
+                ("bc_kind", C.c_int * 4), ("bc_values", C.c_double * 16), ("dt_cfl", C.c_double),
+                ("max_attempts", C.c_int), ("pad", C.c_int)]
+
+
 class AdaptiveResultC(C.Structure):
     _fields_ = [("t_final", C.c_double), ("dt_next", C.c_double), ("prev_err", C.c_double),
                 ("last_err", C.c_double), ("n_accepted", C.c_int), ("n_rejected", C.c_int),
@@ -76,6 +84,9 @@ SIGNATURES = {
     "mjx_spec2d_ws_bytes": (_sz, [_i, _i, _i, _i]),
     "mjx_spectral_apply2d": (_i, [_vp, C.POINTER(Grid2DC), _i, _i, C.POINTER(C.c_double), _d, _i,
                                   _vp, _vp, _vp, _sz, _vp]),
+    "mjx_advdiff_apply2d": (_i, [_vp, C.POINTER(Grid2DC), _i, _i, C.POINTER(C.c_double),
+                                 C.POINTER(C.c_double), C.POINTER(C.c_double), _d, _vp, _vp, _vp,
+                                 _sz, _vp]),
     "mjx_fft_cn2d": (_i, [_vp, C.POINTER(Grid2DC), _i, _d, _d, _i, _vp, _vp, _vp, _sz, _vp]),
     "mjx_fft_cn2d_noalloc": (_i, [_vp, C.POINTER(Grid2DC), _i, _d, _d, _i, _vp, _vp, _vp]),
     "mjx_bc_pad2d": (_i, [_vp, _vp, _i, _i, _i, _i, _vp, _vp, _d, _d, _i, _vp]),
@@ -83,6 +94,10 @@ SIGNATURES = {
     "mjx_unpad2d": (_i, [_vp, _vp, _i, _i, _i, _i, _i, _vp]),
     "mjx_laplacian2d": (_i, [_vp, _vp, _i, _i, _i, _i, _vp, _i, _vp, _vp, _d, _d, _i, _vp]),
     "mjx_stencil1d": (_i, [_vp, _vp, _i, _i, _i, _i, _d, _d, _i, _vp]),
+    "mjx_stencil2d": (_i, [_vp, _vp, _i, _i, _i, _i, _i, _i, _d, _d, _i, _vp]),
+    "mjx_error_norm_ws_bytes": (_sz, []),
+    "mjx_scaled_error_norm": (_i, [_vp, _vp, C.c_longlong, _i, _d, _d, C.POINTER(C.c_double), _vp,
+                                   _sz, _vp]),
     "mjx_rhs2d": (_i, [_vp, _vp, _i, _i, _i, _i, _i, _vp, _d, _d, _vp, _vp, _d, _d, _i, _vp]),
     "mjx_imex2d_ws_bytes": (_sz, [_i, _i, _i, _i]),
     "mjx_imex_strang_step2d": (_i, [_vp, C.POINTER(Grid2DC), _i, C.POINTER(ImexProblemC), _d,
@@ -107,6 +122,14 @@ SIGNATURES = {
                                        C.POINTER(C.c_double), _vp, C.POINTER(C.c_int),
                                        C.POINTER(C.c_double), _i, C.POINTER(AdaptiveResultC), _vp,
                                        _sz, _vp]),
+    "mjx_explicit_ws_bytes": (_sz, [_i, _i, _i, _i]),
+    "mjx_explicit_integrate2d": (_i, [C.POINTER(Grid2DC), _i, C.POINTER(ExplicitProblemC), _d, _i,
+                                      _vp, _vp, _vp, _sz, _vp]),
+    "mjx_explicit_rhs2d": (_i, [C.POINTER(Grid2DC), _i, C.POINTER(ExplicitProblemC), _vp, _vp, _vp]),
+    "mjx_explicit_adaptive2d": (_i, [C.POINTER(Grid2DC), _i, C.POINTER(ExplicitProblemC),
+                                     C.POINTER(PIDParamsC), _d, _d, _d, _i, _i, _vp, _vp,
+                                     C.POINTER(C.c_double), C.POINTER(C.c_double), _vp, _vp, _sz,
+                                     C.POINTER(AdaptiveResultC), _vp]),
     "mjx_dst1_plan_bytes": (_sz, [_i, _i]),
     "mjx_dst1_plan_init": (_i, [_vp, _i, _i, _vp]),
     "mjx_dst1": (_i, [_vp, _i, C.c_longlong, _i, _i, _vp, _vp, _vp, _d, _d, _d, _vp]),

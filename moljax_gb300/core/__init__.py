@@ -6,11 +6,13 @@ from moljax_gb300.core import fft_solvers, operators, stepping, dt_policy, model
 from moljax_gb300.core.operators import LinearOp, NonlinearOp, laplacian_2d
 from moljax_gb300.core.model import (MOLModel, create_gray_scott_model,
                                      create_gray_scott_periodic_fft, gray_scott_factory,
-                                     create_variable_diffusion_model)
+                                     create_variable_diffusion_model,
+                                     create_advection_diffusion_model, create_advdiff_periodic_fft,
+                                     create_fisher_kpp_model)
 from moljax_gb300.core.stepping import (IntegratorType, AdaptiveResult, adaptive_integrate,
                                         adaptive_integrate_imex, imex_strang_step, imex_euler_step,
                                         integrate_imex_fixed_dt, be_step, cn_step, bdf2_step,
-                                        integrate_fixed_dt)
+                                        integrate_fixed_dt, euler_step, ssprk3_step, rk4_step)
 from moljax_gb300.core.dt_policy import CFLParams, PIDParams
 from moljax_gb300.core.fft_solvers import (create_fft_cache, solve_helmholtz_2d,
                                            apply_diffusion_inverse_fft, fft_cn_step,
@@ -23,9 +25,13 @@ from moljax_gb300.core import newton_krylov, preconditioners
 from moljax_gb300.core.newton_krylov import (NKParams, NKStats, newton_krylov_solve,
                                              integrate_implicit_vardiff)
 from moljax_gb300.core.preconditioners import (DiffusionPreconditioner, IdentityPreconditioner,
-                                               BlockJacobiPreconditioner)
+                                               BlockJacobiPreconditioner, FFTDiffusionPreconditioner,
+                                               FFTAdvectionDiffusionPreconditioner, PrecondContext)
 from moljax_gb300.core import reactor, stencil1d
-from moljax_gb300.core.operators import laplacian_1d, gradient_1d, d1_upwind_1d
+from moljax_gb300.core.operators import (laplacian_1d, gradient_1d, d1_upwind_1d, d1_upwind_2d,
+                                        d1_central_2d)
+from moljax_gb300.core.utils import scaled_error_norm, is_finite
+from moljax_gb300.core.dt_policy import propose_dt, implicit_robustness_dt, compute_error_order
 from moljax_gb300.core import fft_nonperiodic
 from moljax_gb300.core.fft_nonperiodic import (dst_I_fast, idst_I_fast, laplacian_symbol_dirichlet,
                                                create_nonperiodic_fft_cache,

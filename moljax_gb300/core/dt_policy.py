@@ -160,3 +160,35 @@ def propose_dt_imex(grid, params, state, t, dt_old, err_ratio, controller_state,
         dt_a, st = handle_rejected_step(dt_old, err_ratio, controller_state, pid_params, order)
     dt_f = min(dt_a, imex_cfl_dt(grid, params, cfl_params))
     return _clip(dt_f, pid_params.dt_min, pid_params.dt_max), st
+
+
+def implicit_robustness_dt(dt_old, nk_stats, dt_min: float = 1e-12, dt_max: float = 1.0,
+                           growth_factor: float = 1.2, shrink_factor: float = 0.5,
+                           fast_iters_threshold: int = 3) -> float:
+    """moljax/core/dt_policy.py:279-321: halve on Newton failure, grow 1.2x when Newton
+    converged within fast_iters_threshold iterations, clip to [dt_min, dt_max]."""
+    dt = dt_old if nk_stats.converged else dt_old * shrink_factor
+    if nk_stats.converged and nk_stats.newton_iters <= fast_iters_threshold:
+        dt = min(dt * growth_factor, dt_max)
+    return _clip(dt, dt_min, dt_max)
+
+
+def propose_dt(method: int, grid, params, state, t, dt_old, err_ratio,
+               controller_state: ControllerState, nk_stats=None,
+               cfl_params: Optional[CFLParams] = None, pid_params: Optional[PIDParams] = None,
+               order: int = 4):
+    """moljax/core/dt_policy.py:324-408: PI (accepted) or reject formula, the CFL limit for
+    explicit methods, implicit_robustness_dt for implicit ones, final clamp.
+    Returns (dt, new ControllerState).  The native drivers run the same rule on the device
+    (explicit) or in their C++ loop (implicit)."""
+    cfl_params = cfl_params or CFLParams()
+    pid_params = pid_params or PIDParams()
+    if err_ratio <= 1.0:
+        dt_a, st = pid_controller_dt(dt_old, err_ratio, controller_state, pid_params, order)
+    else:
+        dt_a, st = handle_rejected_step(dt_old, err_ratio, controller_state, pid_params, order)
+    if method < 3:
+        dt_a = min(dt_a, heisenberg_cfl_dt(grid, params, cfl_params))
+    if nk_stats is not None and method >= 3:
+        dt_a = implicit_robustness_dt(dt_a, nk_stats)
+    return _clip(dt_a, pid_params.dt_min, pid_params.dt_max), st

@@ -65,6 +65,8 @@ class MOLModel:
         from moljax_gb300.core import stencil
         if self.metadata.get("kind") == "vardiff":
             return _vardiff_rhs(self, state)
+        if self.metadata.get("advection"):
+            return _explicit_rhs(self, state, t)
         D = self.diffusivities()
         names = self.field_names
         rx = self.reaction_kind
@@ -147,6 +149,76 @@ def create_fisher_kpp_model(grid: Grid2D, D: float = 0.01, r: float = 1.0,
     return MOLModel(grid, {"u": FieldBCSpec(kind=bc_type)}, params, (diffusion,),
                     (fisher_kpp_reaction_op("u", "r"),),
                     {"field_names": ["u"], "diffusivities": {"u": D}})
+
+
+def create_advection_diffusion_model(grid: Grid2D, field_names=("c1", "c2"), D: float = 0.01,
+                                     vx: float = 1.0, vy: float = 0.0,
+                                     bc_type: BCType = BCType.PERIODIC, use_upwind: bool = True,
+                                     dtype: torch.dtype = torch.float64) -> MOLModel:
+    """dc_i/dt = D Lap(c_i) - vx dc_i/dx - vy dc_i/dy (moljax/core/model.py:295-370).
+
+    The operator is one linear op, as in the reference (upwind d1_upwind_2d or
+    central differences); the explicit steppers evaluate it in fused native kernels.
+    """
+    names = list(field_names)
+    bc_spec = {n: FieldBCSpec(kind=bc_type) for n in names}
+    params = {"D": D, "vx": vx, "vy": vy, "dtype": dtype}
+
+    def advdiff_apply(state, g, t, p):
+        return _explicit_rhs_raw(state, g, bc_spec, names, p, 1 if use_upwind else 2, t)
+
+    def advdiff_dt_bound(g, p):  # model.py:358-369
+        vmax = abs(p["vx"]) + abs(p["vy"])
+        return min(g.min_dx / (vmax + 1e-14), 0.25 * g.min_dx2 / (p["D"] + 1e-14))
+
+    op = LinearOp("advection_diffusion", advdiff_apply, advdiff_dt_bound, "advection_diffusion")
+    return MOLModel(grid, bc_spec, params, (op,), (),
+                    {"field_names": names, "pde_type": "advection_diffusion",
+                     "advection": 1 if use_upwind else 2,
+                     "diffusivities": {n: D for n in names}})
+
+
+def create_advdiff_periodic_fft(grid: Grid2D, field_names=("c1", "c2"), D: float = 0.01,
+                                vx: float = 1.0, vy: float = 0.0, use_upwind: bool = True,
+                                dtype: torch.dtype = torch.float64, device=None):
+    """moljax/core/model.py:587-642 -> (model, fft_cache, diffusivities)."""
+    from moljax_gb300.core.fft_solvers import create_fft_cache
+    model = create_advection_diffusion_model(grid, field_names, D, vx, vy, BCType.PERIODIC,
+                                             use_upwind, dtype)
+    cache = create_fft_cache(grid, dtype, device)
+    diff = {n: D for n in model.field_names}
+    md = dict(model.metadata)
+    md.update(fft_cache=cache, diffusivities=diff, supports_fft=True)
+    return MOLModel(model.grid, model.bc_spec, model.params, model.linear_ops,
+                    model.nonlinear_ops, md), cache, diff
+
+
+def _explicit_rhs_raw(state, grid, bc_spec, names, params, advection, t=0.0):
+    proto = MOLModel(grid, bc_spec, params, (), (), {"advection": advection,
+                                                    "diffusivities": {n: params["D"] for n in names}})
+    return _explicit_rhs(proto, state, t)
+
+
+def _explicit_rhs(model: MOLModel, state, t):
+    """MOLModel.rhs through the explicit stage kernel (BCs on the fly, ghosts of the result zero)."""
+    import ctypes as C
+    from moljax_gb300.core import stencil
+    from moljax_gb300.core.stepping import explicit_problem
+    names = model.field_names
+    prob = explicit_problem(model, 2, t=t)
+    interior = stencil.unpad(stencil.stack(state, names), model.grid)
+    N.require_cuda(interior)
+    out = torch.empty_like(interior)
+    g = model.grid
+    N.check("mjx_explicit_rhs2d", N.lib().mjx_explicit_rhs2d(
+        C.byref(N.Grid2DC(g.ny, g.nx, g.dy, g.dx)), N.dtype_code(interior.dtype), C.byref(prob),
+        N.ptr(interior), N.ptr(out), N.stream_ptr(interior.device)))
+    res = {}
+    for i, n in enumerate(names):
+        padded = torch.zeros_like(state[n])
+        padded[g.interior_slice] = out[i]
+        res[n] = padded
+    return res
 
 
 def create_variable_diffusion_model(grid: Grid2D, a: float = 1.0, b: float = 1.0, c: float = 1.0,

@@ -13,6 +13,8 @@ from __future__ import annotations
 from dataclasses import dataclass
 from typing import Any, Callable, Dict, Optional
 
+import torch
+
 from moljax_gb300 import _native as N
 from moljax_gb300.core.grid import Grid1D, Grid2D
 
@@ -37,6 +39,31 @@ def laplacian_2d(f, grid: Grid2D):
     """5-point Laplacian on the interior, ghosts zero (operators.py:311-322)."""
     from moljax_gb300.core import stencil
     return stencil.laplacian_2d(f, grid)
+
+
+def _d1_2d(f, grid: Grid2D, op: int, axis: int, v: float = 0.0):
+    from moljax_gb300 import _native as N
+    N.require_cuda(f)
+    f3 = f.reshape(-1, grid.ny_total, grid.nx_total).contiguous()
+    out = torch.empty_like(f3)
+    d = grid.dy if axis == 0 else grid.dx
+    N.check("mjx_stencil2d", N.lib().mjx_stencil2d(
+        N.ptr(f3), N.ptr(out), f3.shape[0], grid.ny, grid.nx, grid.n_ghost, op, axis, float(v),
+        float(d), N.dtype_code(f.dtype), N.stream_ptr(f.device)))
+    return out.reshape(f.shape)
+
+
+def d1_upwind_2d(f, v, grid: Grid2D, axis: int):
+    """Upwind first derivative along axis (0: y, 1: x) with scalar velocity v, ghosts read as
+    stored, result ghosts zero (operators.py:200-268)."""
+    if not isinstance(v, (int, float)):
+        raise NotImplementedError("d1_upwind_2d: the native stencil takes a scalar velocity")
+    return _d1_2d(f, grid, 1, axis, v)
+
+
+def d1_central_2d(f, grid: Grid2D, axis: int):
+    """Central first derivative along axis (operators.py:155-197)."""
+    return _d1_2d(f, grid, 2, axis)
 
 
 def laplacian_1d(f_or_grid, grid=None, order: int = 2):

@@ -10,7 +10,9 @@ step.
 
 ``adaptive_integrate`` accepts the reference signature
 (model, y0, t0, t_end, dt0, method, ...) and the README form
-(model, t_span=, integrator=, rtol=, atol=).  BE/CN/BDF2 (``be_step``,
+(model, t_span=, integrator=, rtol=, atol=).  EULER/SSPRK3/RK4 (``euler_step``,
+``ssprk3_step``, ``rk4_step``, fixed and adaptive) run fused stencil-stage kernels
+for the built-in reaction-advection-diffusion models with any ghost BCs.  BE/CN/BDF2 (``be_step``,
 ``cn_step``, ``bdf2_step``, ``integrate_fixed_dt``, ``adaptive_integrate``) run
 on the native Newton-Krylov solver for the variable-diffusion model.
 """
@@ -235,6 +237,116 @@ def _adaptive_mixed(model, interior, plan, prob, pid_params, t0, t_end, dt0, max
                           res.n_rejected, res.status)
 
 
+# ------------------------------------------------------------------ explicit steppers
+_EXPLICIT = {IntegratorType.EULER: 0, IntegratorType.SSPRK3: 1, IntegratorType.RK4: 2}
+
+
+def explicit_problem(model, method: int = 2, cfl_params: Optional[CFLParams] = None,
+                     t: float = 0.0, max_attempts: int = 0) -> "N.ExplicitProblemC":
+    """Native description of a built-in model for the explicit steppers: reaction,
+    per-field D, advection (metadata 'advection': 1 upwind, 2 central; params vx, vy),
+    per-field BC kinds and side values at time t, heisenberg_cfl_dt."""
+    from moljax_gb300.core.bc import side_values
+    from moljax_gb300.core.dt_policy import heisenberg_cfl_dt
+    names = model.field_names
+    if len(names) > 4:
+        raise NotImplementedError("at most 4 fields per native explicit call")
+    p = N.ExplicitProblemC()
+    p.reaction = model.reaction_kind
+    p.nfields = len(names)
+    D = model.diffusivities()
+    for i, n in enumerate(names):
+        p.D[i] = float(D.get(n, 0.0))
+        spec = model.bc_spec[n]
+        p.bc_kind[i] = int(spec.kind)
+        for j, v in enumerate(side_values(spec, model.grid, t, model.params)):
+            p.bc_values[4 * i + j] = float(v)
+    p.F = float(model.params.get("F", 0.0))
+    p.k = float(model.params.get("k", 0.0))
+    p.r = float(model.params.get("r", 0.0))
+    p.advection = int(model.metadata.get("advection", 0))
+    p.vx = float(model.params.get("vx", 0.0)) if p.advection else 0.0
+    p.vy = float(model.params.get("vy", 0.0)) if p.advection else 0.0
+    p.method = int(method)
+    p.dt_cfl = heisenberg_cfl_dt(model.grid, model.params, cfl_params or CFLParams())
+    p.max_attempts = int(max_attempts)
+    return p
+
+
+def _explicit_steps(model, y, t, dt, method, n_steps=1):
+    grid = model.grid
+    names = model.field_names
+    interior = stencil.unpad(stencil.stack(y, names), grid)
+    N.require_cuda(interior)
+    prob = explicit_problem(model, method, t=t)
+    lib = N.lib()
+    code = N.dtype_code(interior.dtype)
+    ws = workspace(lib.mjx_explicit_ws_bytes(grid.ny, grid.nx, len(names), code), interior.device,
+                   "explicit")
+    out = torch.empty_like(interior)
+    N.check("mjx_explicit_integrate2d", lib.mjx_explicit_integrate2d(
+        C.byref(N.Grid2DC(grid.ny, grid.nx, grid.dy, grid.dx)), code, C.byref(prob), float(dt),
+        int(n_steps), N.ptr(interior), N.ptr(out), N.ptr(ws), ws.numel(),
+        N.stream_ptr(interior.device)))
+    padded = stencil.pad_interior(out, grid, model.bc_spec, names, t + n_steps * dt, model.params)
+    return {n: padded[i] for i, n in enumerate(names)}
+
+
+def euler_step(model, y, t, dt):
+    """y + dt F(y) (moljax/core/stepping.py:64-84); ghosts refilled from the BCs."""
+    return _explicit_steps(model, y, t, dt, 0)
+
+
+def ssprk3_step(model, y, t, dt):
+    """Shu-Osher SSPRK3 (moljax/core/stepping.py:87-123)."""
+    return _explicit_steps(model, y, t, dt, 1)
+
+
+def rk4_step(model, y, t, dt):
+    """Classical RK4 (moljax/core/stepping.py:126-163)."""
+    return _explicit_steps(model, y, t, dt, 2)
+
+
+def _adaptive_explicit(model, y0, t0, t_end, dt0, method, max_steps, cfl_params, pid_params,
+                       save_every, save_y_history=True, max_attempts=0):
+    grid = model.grid
+    names = model.field_names
+    pid_params = pid_params or PIDParams()
+    interior = stencil.unpad(stencil.stack(y0, names), grid)
+    N.require_cuda(interior)
+    prob = explicit_problem(model, _EXPLICIT[method], cfl_params, t0, max_attempts)
+    lib = N.lib()
+    dev = interior.device
+    code = N.dtype_code(interior.dtype)
+    ws = workspace(lib.mjx_explicit_ws_bytes(grid.ny, grid.nx, len(names), code), dev, "explicit")
+    max_saves = max_steps // save_every + 1
+    y_final = torch.empty_like(interior)
+    t_hist = torch.empty(max_saves, dtype=torch.float64, device=dev)
+    dt_hist = torch.empty(max_saves, dtype=torch.float64, device=dev)
+    if save_y_history == "host":
+        y_hist = torch.empty((max_saves,) + tuple(interior.shape), dtype=interior.dtype,
+                             pin_memory=True)
+    elif save_y_history:
+        y_hist = torch.empty((max_saves,) + tuple(interior.shape), dtype=interior.dtype, device=dev)
+    else:
+        y_hist = None
+    pid = N.PIDParamsC(pid_params.safety, pid_params.kI, pid_params.kP, pid_params.dt_min,
+                       pid_params.dt_max, pid_params.max_factor, pid_params.min_factor,
+                       pid_params.atol, pid_params.rtol)
+    res = N.AdaptiveResultC()
+    N.check("mjx_explicit_adaptive2d", lib.mjx_explicit_adaptive2d(
+        C.byref(N.Grid2DC(grid.ny, grid.nx, grid.dy, grid.dx)), code, C.byref(prob), C.byref(pid),
+        float(t0), float(t_end), float(dt0), int(max_steps), int(save_every), N.ptr(interior),
+        N.ptr(y_final), C.cast(C.c_void_p(t_hist.data_ptr()), C.POINTER(C.c_double)),
+        C.cast(C.c_void_p(dt_hist.data_ptr()), C.POINTER(C.c_double)), N.ptr(y_hist),
+        N.ptr(ws), ws.numel(), C.byref(res), N.stream_ptr(dev)))
+    padded = stencil.pad_interior(y_final, grid, model.bc_spec, names, res.t_final, model.params)
+    y_fin = {n: padded[i] for i, n in enumerate(names)}
+    y_history = ({n: y_hist[:, i] for i, n in enumerate(names)} if y_hist is not None else None)
+    return AdaptiveResult(res.t_final, y_fin, t_hist, y_history, dt_hist, res.n_saved,
+                          res.n_accepted, res.n_rejected, res.status)
+
+
 # ------------------------------------------------------------------ implicit steppers
 _IMPLICIT = {IntegratorType.BE: 3, IntegratorType.CN: 4, IntegratorType.BDF2: 5}
 
@@ -320,9 +432,19 @@ def integrate_fixed_dt(model, y0, t0, t_end, dt, method=IntegratorType.RK4, save
     fixed steps (BDF2 takes a BE first step); returns (t_history, y_history, y_final)
     with every step's padded state, as the reference's scan outputs."""
     method = IntegratorType(int(method))
-    if method not in _IMPLICIT:
-        raise NotImplementedError(f"{method.name}: explicit fixed-dt drivers are not built on the GPU path")
     n_steps = int((t_end - t0) / dt) + 1
+    if method in _EXPLICIT:
+        y, t = y0, t0
+        ts, ys = [], []
+        for _ in range(n_steps):
+            y = _explicit_steps(model, y, t, dt, _EXPLICIT[method])
+            t = t + dt
+            ts.append(t)
+            ys.append(y)
+        return (torch.tensor(ts, dtype=torch.float64),
+                {k: torch.stack([s_[k] for s_ in ys]) for k in y0}, y)
+    if method not in _IMPLICIT:
+        raise NotImplementedError(f"{method.name}: use integrate_imex_fixed_dt for IMEX methods")
     y, y_prev, t = y0, y0, t0
     ts, ys = [], []
     for step in range(n_steps):
@@ -416,6 +538,10 @@ def adaptive_integrate(model, y0=None, t0: float = 0.0, t_end: Optional[float] =
         n = int(round((tf - t0) / dt0))
         return AdaptiveResult(tf, y, torch.tensor([t0, tf], dtype=torch.float64), None,
                               torch.tensor([dt0], dtype=torch.float64), 2, n, 0, 0)
+    if method in _EXPLICIT:
+        return _adaptive_explicit(model, y0, t0, t_end, dt0, method, max_steps, cfl_params,
+                                  pid_params, save_every, kw.pop("save_y_history", True),
+                                  kw.pop("max_attempts", 0))
     if method in _IMPLICIT:
         return _adaptive_implicit(model, y0, t0, t_end, dt0, method, max_steps, pid_params,
                                   nk_params, save_every, kw.pop("be_guess", "euler"),

@@ -299,7 +299,7 @@ static MixAttempt build_mix(const void* plan32, const mjx_grid2d* g, const mjx_i
   int C = 256 / tps;
   if (C < 1) C = 1;
   if (C > 8) C = 8;
-  while (C > 1 && (2 * C * tps > 512 || (size_t)sp_size(g->ny * 2 * C) * 8 > 200 * 1024)) C >>= 1;
+  while (C > 1 && (2 * C * tps > 256 || (size_t)sp_size(g->ny * 2 * C) * 8 > 200 * 1024)) C >>= 1;
   c.C = C;
   c.ys[0] = (float4*)(ws + L.ys0); c.ys[1] = (float4*)(ws + L.ys1);
   c.pa = (float4*)(ws + L.pa); c.pb = (float4*)(ws + L.pb);

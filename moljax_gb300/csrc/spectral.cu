@@ -335,6 +335,31 @@ __global__ void __launch_bounds__(512, Occ<T>::col) col_kernel(const __grid_cons
     const int ky = e / Cn, c = e - ky * Cn, kx = kx0 + c;
     const T lam = (kx < a.ncols ? a.lamx[kx] : (T)0) + a.lamy[ky];
     const C v = buf[sp(ky * W + c)];
+    if (jb.mul == MUL_ADVDIFF) {
+      // m(k) = 1/(1 - h (D lam - i (vx kx + vy ky))), |denominator| < 1e-14 -> 1e-14
+      // (FFTAdvectionDiffusionPreconditioner, moljax/core/preconditioners.py:297-420),
+      // kx, ky = 2 pi fftfreq (the Nyquist index negative).  The reference keeps
+      // real(ifft2(.)); on the half spectrum that is the multiplier (m(k) + conj(m(-k)))/2,
+      // which equals m(k) except on the Nyquist lines, where fftfreq breaks the oddness
+      // of the advection term.
+      const int nxl = 2 * (a.ncols - 1);
+      const int mx = kx < nxl / 2 ? kx : kx - nxl, my = ky < ny / 2 ? ky : ky - ny;
+      const int nmx = mx == -nxl / 2 ? mx : -mx, nmy = my == -ny / 2 ? my : -my;
+      const double hh = h * jb.hfac[0];
+      const double dr0 = 1.0 - (double)hD0 * (double)lam;
+      double mre = 0.0, mim = 0.0;
+      for (int side = 0; side < 2; ++side) {
+        const int qx = side ? nmx : mx, qy = side ? nmy : my;
+        double dr = dr0, di = hh * (jb.vx * a.kxs * qx + jb.vy * a.kys * qy);
+        if (sqrt(dr * dr + di * di) < 1e-14) { dr = 1e-14; di = 0.0; }
+        const double den = dr * dr + di * di;
+        mre += 0.5 * dr / den;
+        mim += side ? 0.5 * di / den : -0.5 * di / den;  // conj(m(-k)) on the second side
+      }
+      const T mr = (T)mre, mi = (T)mim;
+      buf[sp(ky * W + c)] = cscale(mk<C>(v.x * mr - v.y * mi, v.x * mi + v.y * mr), jscale);
+      continue;
+    }
     buf[sp(ky * W + c)] = cscale(v, jscale * multiplier<T>(jb.mul, hD0, lam, jb.pow[0]));
     if (nout > 1) buf[sp(ky * W + Cn + c)] = cscale(v, jscale * multiplier<T>(jb.mul, hD1, lam, jb.pow[1]));
   }
@@ -473,14 +498,16 @@ ColArgs<T> field_cols(const mjx_grid2d* g, const PlanView& pv, cx<T>* spec, int 
 
 template <typename T>
 mjx_status spectral_apply(const void* plan, const mjx_grid2d* g, int nfields, const double* D,
-                          double h, int mult, const T* in, T* out, void* ws, cudaStream_t s) {
+                          double h, int mult, const T* in, T* out, void* ws, cudaStream_t s,
+                          const double* vx = nullptr, const double* vy = nullptr) {
   const PlanView pv = plan_view(plan, g->ny, g->nx, sizeof(T));
   cx<T>* spec = (cx<T>*)ws;
   const size_t fsz = (size_t)g->ny * g->nx;
-  // gather the fields that diffuse; pass the others through
+  // gather the fields that diffuse (or, for MUL_ADVDIFF, move); pass the others through
+  auto moves = [&](int f) { return vx && vy && (fabs(vx[f]) > 1e-14 || fabs(vy[f]) > 1e-14); };
   int idx[4], nd = 0;
   for (int f = 0; f < nfields; ++f) {
-    if (D[f] > 1e-14) idx[nd++] = f;
+    if (D[f] > 1e-14 || moves(f)) idx[nd++] = f;
     else if (in != out)
       MJX_CUDA_TRY(cudaMemcpyAsync(out + f * fsz, in + f * fsz, fsz * sizeof(T), cudaMemcpyDeviceToDevice, s));
   }
@@ -496,10 +523,13 @@ mjx_status spectral_apply(const void* plan, const mjx_grid2d* g, int nfields, co
   MJX_CUDA_TRY((launch_row<T, RX_NONE>(r, s)));
   ColArgs<T> c = field_cols<T>(g, pv, spec, 1);
   c.hfixed = h; c.njobs = nd;
+  c.kxs = 6.283185307179586476925286766559 / ((double)g->nx * g->dx);
+  c.kys = 6.283185307179586476925286766559 / ((double)g->ny * g->dy);
   for (int i = 0; i < nd; ++i) {
     ColJob& j = c.job[i];
     j.sin = j.sout[0] = j.sout[1] = (long long)i * g->ny * spec_ldc(g->nx);
     j.D = D[idx[i]]; j.hfac[0] = j.hfac[1] = 1.0; j.pow[0] = j.pow[1] = 1; j.nout = 1; j.mul = mult;
+    if (vx && vy) { j.vx = vx[idx[i]]; j.vy = vy[idx[i]]; }
   }
   MJX_CUDA_TRY(launch_col<T>(c, s));
   for (int i = 0; i < nd; ++i) r.pr[i].flags = ROW_LOAD_SPEC | ROW_STORE_REAL;
@@ -654,6 +684,23 @@ mjx_status mjx_spectral_apply2d(const void* plan, const mjx_grid2d* g, int dtype
   cudaStream_t s = (cudaStream_t)stream;
   if (e == 4) return spectral_apply<float>(plan, g, nfields, D, h, mult, (const float*)in, (float*)out, ws, s);
   return spectral_apply<double>(plan, g, nfields, D, h, mult, (const double*)in, (double*)out, ws, s);
+}
+
+mjx_status mjx_advdiff_apply2d(const void* plan, const mjx_grid2d* g, int dtype, int nfields,
+                               const double* D, const double* vx, const double* vy, double h,
+                               const void* in, void* out, void* ws, size_t ws_bytes, void* stream) {
+  MJX_TRY(check_grid(g));
+  if (nfields < 1 || nfields > 4 || D == nullptr || vx == nullptr || vy == nullptr || plan == nullptr ||
+      in == nullptr || out == nullptr)
+    return MJX_BAD_ARG;
+  const int e = elem_size(dtype);
+  if (!e) return MJX_BAD_DTYPE;
+  if (ws == nullptr || ws_bytes < mjx_spec2d_ws_bytes(g->ny, g->nx, nfields, dtype)) return MJX_WORKSPACE;
+  MJX_TRY(ensure_kernel_attrs());
+  cudaStream_t s = (cudaStream_t)stream;
+  if (e == 4)
+    return spectral_apply<float>(plan, g, nfields, D, h, MUL_ADVDIFF, (const float*)in, (float*)out, ws, s, vx, vy);
+  return spectral_apply<double>(plan, g, nfields, D, h, MUL_ADVDIFF, (const double*)in, (double*)out, ws, s, vx, vy);
 }
 
 mjx_status mjx_fft_cn2d(const void* plan, const mjx_grid2d* g, int dtype, double D, double dt,

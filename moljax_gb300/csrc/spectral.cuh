@@ -77,7 +77,7 @@ template <typename T> struct RowArgs {
   RowPair pr[MJX_MAXPAIR];
 };
 
-enum { MUL_SCALE = 0, MUL_HELMHOLTZ = 1, MUL_CN = 2, MUL_EXP = 3 };
+enum { MUL_SCALE = 0, MUL_HELMHOLTZ = 1, MUL_CN = 2, MUL_EXP = 3, MUL_ADVDIFF = 4 };
 
 struct ColJob {
   long long sin;         // spectrum offset of the input column block (ky=0, kx=0)
@@ -89,6 +89,7 @@ struct ColJob {
   int mul;               // MUL_*
   int dirs;              // bit 0: forward transform first, bit 1: inverse after (0 means both)
   double scale;          // multiplier scale (0: use ColArgs::scale)
+  double vx, vy;         // MUL_ADVDIFF: advection velocity of this field
 };
 
 template <typename T> struct ColArgs {
@@ -98,6 +99,7 @@ template <typename T> struct ColArgs {
   const T* lamy;         // symbol along y, length ny (fftfreq order)
   const cx<T>* tw;       // twiddles for ny
   T scale;               // normalisation 1/(nx*ny)
+  double kxs, kys;       // MUL_ADVDIFF: wavenumber units 2 pi/(nx dx), 2 pi/(ny dy)
   double hfixed;
   const DevState* st;
   ColJob job[MJX_MAXJOB];

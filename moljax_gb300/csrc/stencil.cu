@@ -12,6 +12,8 @@
 
 namespace mjx {
 
+enum { MJX_ERRNORM_BLOCKS = 152 * 2 };
+
 mjx_status check_grid(const mjx_grid2d* g);
 int elem_size(int dtype);
 
@@ -195,11 +197,107 @@ __global__ void stencil1d_kernel(const T* __restrict__ in, T* __restrict__ out, 
   }
 }
 
+// 2D first derivatives on padded fields, ghosts read as stored, output ghosts 0:
+// op 1: upwind along axis with scalar velocity v (d1_upwind_2d, operators.py:200-268),
+// op 2: central (d1_central_2d, 155-197).  axis 0: y, 1: x.
+template <typename T>
+__global__ void stencil2d_kernel(const T* __restrict__ in, T* __restrict__ out, int nf, int ny, int nx,
+                                 int g, int op, int axis, double v, double d) {
+  const int ldx = nx + 2 * g, ldy = ny + 2 * g;
+  const long long per = (long long)ldx * ldy, total = per * nf;
+  const long long step = axis == 0 ? ldx : 1;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+       i += (long long)gridDim.x * blockDim.x) {
+    const long long r = i % per;
+    const int y = (int)(r / ldx), x = (int)(r - (long long)y * ldx);
+    if (y < g || y >= ny + g || x < g || x >= nx + g) { out[i] = (T)0; continue; }
+    const T c = in[i], lo = in[i - step], hi = in[i + step];
+    if (op == 1) out[i] = v >= 0 ? (c - lo) / (T)d : (hi - c) / (T)d;
+    else out[i] = (hi - lo) / (T)(2.0 * d);
+  }
+}
+
+// scaled error partials over n values: sum (e / (atol + rtol |y|))^2 and non-finite flags of y
+template <typename T>
+__global__ void errnorm_partials(const T* __restrict__ e, const T* __restrict__ y, long long n,
+                                 double atol, double rtol, double* part, int* bad) {
+  double acc = 0.0;
+  int nf = 0;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x) {
+    const double yv = (double)y[i];
+    const double q = (double)e[i] / (atol + rtol * fabs(yv));
+    acc += q * q;
+    nf |= !isfinite(yv);
+  }
+  __shared__ double red[8];
+  __shared__ int rb[8];
+  for (int o = 16; o > 0; o >>= 1) {
+    acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    nf |= __shfl_xor_sync(0xffffffffu, nf, o);
+  }
+  if ((threadIdx.x & 31) == 0) { red[threadIdx.x >> 5] = acc; rb[threadIdx.x >> 5] = nf; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    int b = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) { s += red[w]; b |= rb[w]; }
+    part[blockIdx.x] = s;
+    bad[blockIdx.x] = b;
+  }
+}
+
 }  // namespace mjx
 
 using namespace mjx;
 
 extern "C" {
+
+mjx_status mjx_stencil2d(const void* padded_in, void* padded_out, int nfields, int ny, int nx,
+                        int n_ghost, int op, int axis, double v, double d, int dtype, void* stream) {
+  MJX_TRY(check_pad(nfields, ny, nx, n_ghost, nullptr));
+  const int e = elem_size(dtype);
+  if (!e) return MJX_BAD_DTYPE;
+  if (!padded_in || !padded_out || padded_in == padded_out) return MJX_BAD_ARG;
+  if (op < 1 || op > 2 || axis < 0 || axis > 1 || !(d > 0)) return MJX_BAD_ARG;
+  const long long total = (long long)nfields * (ny + 2 * n_ghost) * (nx + 2 * n_ghost);
+  cudaStream_t s = (cudaStream_t)stream;
+  if (e == 4) stencil2d_kernel<float><<<grid_for(total), 256, 0, s>>>((const float*)padded_in, (float*)padded_out, nfields, ny, nx, n_ghost, op, axis, v, d);
+  else stencil2d_kernel<double><<<grid_for(total), 256, 0, s>>>((const double*)padded_in, (double*)padded_out, nfields, ny, nx, n_ghost, op, axis, v, d);
+  return cuda_status(cudaGetLastError());
+}
+
+size_t mjx_error_norm_ws_bytes(void) { return (size_t)MJX_ERRNORM_BLOCKS * (sizeof(double) + sizeof(int)); }
+
+mjx_status mjx_scaled_error_norm(const void* err, const void* y, long long n, int dtype, double atol,
+                                 double rtol, double* result, void* ws, size_t ws_bytes, void* stream) {
+  const int e = elem_size(dtype);
+  if (!e) return MJX_BAD_DTYPE;
+  if (!err || !y || !result || n < 1) return MJX_BAD_ARG;
+  if (!ws || ws_bytes < mjx_error_norm_ws_bytes()) return MJX_WORKSPACE;
+  double* part = (double*)ws;
+  int* bad = (int*)(part + MJX_ERRNORM_BLOCKS);
+  cudaStream_t s = (cudaStream_t)stream;
+  if (e == 4) errnorm_partials<float><<<MJX_ERRNORM_BLOCKS, 256, 0, s>>>((const float*)err, (const float*)y, n, atol, rtol, part, bad);
+  else errnorm_partials<double><<<MJX_ERRNORM_BLOCKS, 256, 0, s>>>((const double*)err, (const double*)y, n, atol, rtol, part, bad);
+  MJX_CUDA_TRY(cudaGetLastError());
+  double hp[MJX_ERRNORM_BLOCKS];
+  int hb[MJX_ERRNORM_BLOCKS];
+  MJX_CUDA_TRY(cudaMemcpyAsync(hp, part, sizeof(hp), cudaMemcpyDeviceToHost, s));
+  MJX_CUDA_TRY(cudaMemcpyAsync(hb, bad, sizeof(hb), cudaMemcpyDeviceToHost, s));
+  MJX_CUDA_TRY(cudaStreamSynchronize(s));
+  double sum = 0.0, c = 0.0;
+  int nonfinite = 0;
+  for (int i = 0; i < MJX_ERRNORM_BLOCKS; ++i) {  // Kahan
+    const double yv = hp[i] - c, tv = sum + yv;
+    c = (tv - sum) - yv;
+    sum = tv;
+    nonfinite |= hb[i];
+  }
+  result[0] = sqrt(sum / (double)n);
+  result[1] = nonfinite ? 0.0 : 1.0;
+  return MJX_OK;
+}
 
 mjx_status mjx_bc_pad2d(const void* interior, void* padded, int nfields, int ny, int nx, int n_ghost,
                         const int* kinds, const double* values, double dy, double dx, int dtype,

@@ -1,0 +1,192 @@
+"""Explicit Runge-Kutta steppers (fused stencil stages) vs the NumPy FP64 oracle."""
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import explicit as OX
+from oracle import imex as OI
+from oracle import mol
+
+pytestmark = pytest.mark.gpu
+
+SIDES = {"left": 0.2, "right": -0.1, "bottom": 0.05, "top": 0.3}
+
+
+def _rel(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+def _gs(n, kind, cuda, dtype=torch.float64):
+    import moljax_gb300 as M
+    from moljax_gb300.core.bc import FieldBCSpec, BCType
+    grid = M.Grid2D(n, n, 0.0, 2.5, 0.0, 2.5)
+    model = M.create_gray_scott_model(grid, 2e-5, 1e-5, 0.035, 0.065, BCType(kind), dtype)
+    vals = None
+    if kind != mol.PERIODIC:
+        fn = (lambda X, Y, t, p: dict(SIDES))
+        spec = FieldBCSpec(kind=BCType(kind), value=fn) if kind == mol.DIRICHLET else \
+            FieldBCSpec(kind=BCType(kind), flux=fn)
+        model = M.MOLModel(model.grid, {"u": spec, "v": spec}, model.params, model.linear_ops,
+                           model.nonlinear_ops, model.metadata)
+        vals = {"u": dict(SIDES), "v": dict(SIDES)}
+    og = mol.Grid2D(n, n, 0, 2.5, 0, 2.5)
+    y0 = mol.gray_scott_ic(og, 5)
+    om = OX.ExplicitModel(og, {"u": kind, "v": kind}, {"u": 2e-5, "v": 1e-5}, vals or {},
+                          lambda y: mol.gray_scott_reaction(y, 0.035, 0.065),
+                          params={"Du": 2e-5, "Dv": 1e-5, "F": 0.035, "k": 0.065})
+    ym = {k: torch.tensor(v, dtype=dtype, device=cuda) for k, v in y0.items()}
+    return M, model, ym, om, y0
+
+
+def _advdiff(n, kind, upwind, cuda, vx=1.0, vy=-0.5):
+    import moljax_gb300 as M
+    from moljax_gb300.core.bc import BCType
+    grid = M.Grid2D(n, n, 0.0, 1.0, 0.0, 1.0)
+    model = M.create_advection_diffusion_model(grid, ["c1", "c2"], 0.01, vx, vy, BCType(kind), upwind)
+    og = mol.Grid2D(n, n, 0, 1, 0, 1)
+    rng = np.random.default_rng(3)
+    y0 = {k: mol.pad(rng.uniform(0, 1, (n, n)), og) for k in ("c1", "c2")}
+    om = OX.ExplicitModel(og, {"c1": kind, "c2": kind}, {"c1": 0.01, "c2": 0.01},
+                          advection="upwind" if upwind else "central", vx=vx, vy=vy,
+                          params={"D": 0.01, "vx": vx, "vy": vy})
+    ym = {k: torch.tensor(v, device=cuda) for k, v in y0.items()}
+    return M, model, ym, om, y0
+
+
+def _interior(a, n):
+    return a[1:n + 1, 1:n + 1]
+
+
+@pytest.mark.parametrize("kind", [mol.PERIODIC, mol.DIRICHLET, mol.NEUMANN])
+def test_rhs_vs_oracle(cuda, kind):
+    n = 32
+    M, model, ym, om, y0 = _gs(n, kind, cuda)
+    F = model.rhs(ym)
+    R = om.rhs(y0)
+    for k in ("u", "v"):
+        assert _rel(_interior(F[k].cpu().numpy(), n), _interior(R[k], n)) < 1e-12
+    for upwind in (True, False):
+        M, model, ym, om, y0 = _advdiff(n, kind, upwind, cuda)
+        F = model.rhs(ym)
+        R = om.rhs(y0)
+        for k in ("c1", "c2"):
+            assert _rel(_interior(F[k].cpu().numpy(), n), _interior(R[k], n)) < 1e-12
+
+
+@pytest.mark.parametrize("method", [0, 1, 2])
+@pytest.mark.parametrize("kind", [mol.PERIODIC, mol.DIRICHLET, mol.NEUMANN])
+def test_single_steps_vs_oracle(cuda, method, kind):
+    n = 32
+    step = {0: "euler_step", 1: "ssprk3_step", 2: "rk4_step"}[method]
+    M, model, ym, om, y0 = _gs(n, kind, cuda)
+    out = getattr(M, step)(model, ym, 0.0, 0.7)
+    ref = OX.STEPS[method](om, y0, 0.7)
+    for k in ("u", "v"):
+        assert _rel(_interior(out[k].cpu().numpy(), n), _interior(ref[k], n)) < 1e-13
+    M, model, ym, om, y0 = _advdiff(n, kind, True, cuda)
+    out = getattr(M, step)(model, ym, 0.0, 2e-3)
+    ref = OX.STEPS[method](om, y0, 2e-3)
+    for k in ("c1", "c2"):
+        assert _rel(_interior(out[k].cpu().numpy(), n), _interior(ref[k], n)) < 1e-13
+
+
+def test_integrate_fixed_dt_rk4(cuda):
+    n = 32
+    M, model, ym, om, y0 = _advdiff(n, mol.PERIODIC, True, cuda)
+    t, ys, yf = M.integrate_fixed_dt(model, ym, 0.0, 0.02, 4e-3, M.IntegratorType.RK4)
+    assert t.numel() == 6 and ys["c1"].shape[0] == 6
+    y = y0
+    for _ in range(6):
+        y = OX.rk4_step(om, y, 4e-3)
+    for k in ("c1", "c2"):
+        assert _rel(_interior(yf[k].cpu().numpy(), n), _interior(y[k], n)) < 1e-12
+
+
+@pytest.mark.parametrize("method", [0, 1, 2])
+def test_adaptive_explicit_vs_oracle(cuda, method):
+    # step doubling + PI + CFL limit: same accept/reject sequence as the oracle
+    n = 32
+    M, model, ym, om, y0 = _gs(n, mol.NEUMANN, cuda)
+    itype = [M.IntegratorType.EULER, M.IntegratorType.SSPRK3, M.IntegratorType.RK4][method]
+    pid = M.PIDParams(atol=1e-6, rtol=1e-4)
+    r = M.adaptive_integrate(model, ym, 0.0, 30.0, 1.0, itype, max_steps=4000, pid_params=pid,
+                             save_every=1)
+    ro = OX.adaptive_integrate_explicit(om, y0, 0.0, 30.0, 1.0, method, max_steps=4000,
+                                        pid=OI.PIDParams(atol=1e-6, rtol=1e-4), save_every=1)
+    assert r.status == ro.status == 0
+    assert (r.n_accepted, r.n_rejected) == (ro.n_accepted, ro.n_rejected)
+    k = ro.n_steps
+    np.testing.assert_allclose(r.t_history.cpu().numpy()[:k], ro.t_history[:k], rtol=1e-9)
+    for f in ("u", "v"):
+        assert _rel(_interior(r.y_final[f].cpu().numpy(), n), _interior(ro.y_final[f], n)) < 1e-10
+    assert r.y_history["u"].shape[0] == 4001
+
+
+def test_adaptive_advection_cfl_limited(cuda):
+    # advection-diffusion: dt is capped by heisenberg_cfl_dt (0.9 * 0.5 dx / |v|)
+    n = 32
+    M, model, ym, om, y0 = _advdiff(n, mol.PERIODIC, True, cuda)
+    pid = M.PIDParams(atol=1e-3, rtol=1e-2)
+    r = M.adaptive_integrate(model, ym, 0.0, 0.2, 1.0, M.IntegratorType.SSPRK3, max_steps=4000,
+                             pid_params=pid, save_every=1, save_y_history=False)
+    ro = OX.adaptive_integrate_explicit(om, y0, 0.0, 0.2, 1.0, 1, max_steps=4000,
+                                        pid=OI.PIDParams(atol=1e-3, rtol=1e-2), save_every=1)
+    assert r.status == ro.status == 0
+    assert (r.n_accepted, r.n_rejected) == (ro.n_accepted, ro.n_rejected)
+    dt_cfl = 0.9 * 0.5 * (1 / n) / 1.5
+    assert float(r.dt_history[: r.n_steps - 1].max()) <= dt_cfl * (1 + 1e-12)
+    for f in ("c1", "c2"):
+        assert _rel(_interior(r.y_final[f].cpu().numpy(), n), _interior(ro.y_final[f], n)) < 1e-10
+
+
+def test_fft_preconditioners_vs_oracle(cuda):
+    import moljax_gb300 as M
+    n = 64
+    grid = M.Grid2D(n, n, 0.0, 1.0, 0.0, 1.5)
+    cache = M.create_fft_cache(grid, torch.float64, cuda)
+    og = mol.Grid2D(n, n, 0, 1, 0, 1.5)
+    rng = np.random.default_rng(9)
+    r = rng.standard_normal((n, n))
+    params = {"D": 0.02, "v": (1.3, -0.7), "vs": 0.4}
+    ctx = M.PrecondContext(grid, 0.05, params)
+    P = M.FFTAdvectionDiffusionPreconditioner(field_diffusivity_keys={"a": "D", "b": "D"},
+                                              field_velocity_keys={"a": "v", "b": "vs"},
+                                              fft_cache=cache)
+    padded = torch.zeros((n + 2, n + 2), dtype=torch.float64, device=cuda)
+    padded[1:-1, 1:-1] = torch.tensor(r, device=cuda)
+    padded[0, :] = 7.0
+    out = P.apply({"a": torch.tensor(r, device=cuda), "b": padded}, ctx)
+    ref_a = OX.fft_advdiff_inverse(r, og, 0.05, 0.02, 1.3, -0.7)
+    ref_b = OX.fft_advdiff_inverse(r, og, 0.05, 0.02, 0.4, 0.0)
+    assert _rel(out["a"].cpu().numpy(), ref_a) < 1e-12
+    assert _rel(out["b"][1:-1, 1:-1].cpu().numpy(), ref_b) < 1e-12
+    assert float(out["b"][0, 3]) == 7.0  # ghosts kept
+    Q = M.FFTDiffusionPreconditioner(field_diffusivity_keys={"a": "D"}, fft_cache=cache)
+    q = Q.apply({"a": torch.tensor(r, device=cuda)}, ctx)["a"].cpu().numpy()
+    assert _rel(q, OX.fft_advdiff_inverse(r, og, 0.05, 0.02, 0.0, 0.0)) < 1e-12
+
+
+def test_2d_derivatives_error_norm_is_finite(cuda):
+    import moljax_gb300 as M
+    n = 24
+    grid = M.Grid2D(n, n + 8, 0.0, 1.0, 0.0, 2.0)
+    og = mol.Grid2D(n, n + 8, 0, 1, 0, 2)
+    rng = np.random.default_rng(4)
+    f = rng.standard_normal((n + 10, n + 2))  # ghosts included, read as stored
+    ft = torch.tensor(f, device=cuda)
+    for axis in (0, 1):
+        for v in (0.7, -0.3):
+            got = M.d1_upwind_2d(ft, v, grid, axis).cpu().numpy()
+            np.testing.assert_allclose(got, mol.d1_upwind_2d(f, v, og, axis), rtol=1e-13, atol=1e-13)
+    got = M.d1_central_2d(ft, grid, 1).cpu().numpy()
+    np.testing.assert_allclose(got, OX._central(f, og, 1), rtol=1e-13, atol=1e-13)
+    e = {"u": torch.tensor(rng.standard_normal(f.shape), device=cuda), "v": ft * 1e-3}
+    y = {"u": ft, "v": ft + 2.0}
+    ref = mol.scaled_error_norm({k: t.cpu().numpy() for k, t in e.items()},
+                                {k: t.cpu().numpy() for k, t in y.items()}, og, 1e-6, 1e-4)
+    assert M.scaled_error_norm(e, y, grid, 1e-6, 1e-4) == pytest.approx(ref, rel=1e-12)
+    assert M.is_finite(y)
+    y["v"] = y["v"].clone()
+    y["v"][3, 4] = float("nan")
+    assert not M.is_finite(y)
