@@ -239,6 +239,19 @@ def time_kernels(M, model, cache, diff, y0, dev, reps=30):
     return out
 
 
+def reduce_over_ranks(t_dev, units, device):
+    """Replica aggregation: the slowest rank's time and every rank's units (the path does
+    not shard, so there is no data-path collective; this is the only one)."""
+    import torch
+    import torch.distributed as dist
+    tt = torch.tensor([t_dev, float(units)], dtype=torch.float64, device=device)
+    tmax = tt[:1].clone()
+    tsum = tt[1:].clone()
+    dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
+    dist.all_reduce(tsum, op=dist.ReduceOp.SUM)
+    return float(tmax.item()), int(tsum.item())
+
+
 def flush_l2(buf):
     buf.add_(1.0)
 
@@ -285,12 +298,7 @@ def run_ours(args, rank, world, local):
     clk = clocks.stop()
     t_dev = sum(times)
     if world > 1:
-        import torch.distributed as dist
-        tt = torch.tensor([t_dev, float(units)], dtype=torch.float64, device=dev)
-        tmax = tt[:1].clone()
-        dist.all_reduce(tmax, op=dist.ReduceOp.MAX)
-        dist.all_reduce(tt[1:], op=dist.ReduceOp.SUM)
-        t_dev, units = float(tmax.item()), int(tt[1].item())
+        t_dev, units = reduce_over_ranks(t_dev, units, dev)
     status = r.status
     n_acc, n_rej = r.n_accepted, r.n_rejected
     y32 = {k: v.detach().clone() for k, v in r.y_final.items()}
@@ -393,11 +401,11 @@ def run_ours(args, rank, world, local):
 
 def etd_kernel_bytes(n):
     """Algorithmic bytes of the 8 ETDRK4 passes of one step (2 fields, FP32): per field and
-    half-spectrum element, complex 8 B / coefficient 4 B accesses (C1 6+2, R1 2, C2 4+2, R2 2,
-    C3 6+2, R3 2, C4 5+4, R4 2)."""
+    half-spectrum element, complex 8 B / coefficient 4 B accesses (C1 5+2, R1 2, C2 4+2, R2 2,
+    C3 6+2, R3 2, C4 6+4, R4 2)."""
     nc = n * (n // 2 + 1)
-    per = {"C1": 6 * 8 + 2 * 4, "R1": 16, "C2": 4 * 8 + 2 * 4, "R2": 16, "C3": 6 * 8 + 2 * 4,
-           "R3": 16, "C4": 5 * 8 + 4 * 4, "R4": 16}
+    per = {"C1": 5 * 8 + 2 * 4, "R1": 16, "C2": 4 * 8 + 2 * 4, "R2": 16, "C3": 6 * 8 + 2 * 4,
+           "R3": 16, "C4": 6 * 8 + 4 * 4, "R4": 16}
     return {k: 2 * nc * v for k, v in per.items()}
 
 

@@ -8,13 +8,13 @@
 // forward FFT_y -> stage combination -> inverse FFT_y, and 4 row passes that
 // fuse c2r -> N(u, v) -> r2c:
 //
-//   C1  U^ = F(ZU), N^u = F(ZN); a^ = E2 U^ + Q N^u; store U^, N^u, a^; ZX = F^-1 a^
+//   C1  N^u = F(ZN); a^ = E2 U^ + Q N^u; store N^u, a^; ZX = F^-1 a^
 //   R1  ZX <- r2c N(c2r ZX)                                   (N^a in row space)
 //   C2  N^a = F(ZX); b^ = E2 U^ + Q N^a; S = N^a; ZX = F^-1 b^
 //   R2  ZX <- r2c N(c2r ZX)
 //   C3  N^b = F(ZX); c^ = E2 a^ + Q (2 N^b - N^u); S += N^b; ZX = F^-1 c^
 //   R3  ZX <- r2c N(c2r ZX)
-//   C4  N^c = F(ZX); U^' = E U^ + f1 N^u + f2 S + f3 N^c; ZU = F^-1 U^'
+//   C4  N^c = F(ZX); U^' = E U^ + f1 N^u + f2 S + f3 N^c; store U^'; ZU = F^-1 U^'
 //   R4  ZN <- r2c N(c2r ZU)                                   (next step's N^u)
 //
 // ZU/ZN/ZX are row spectra (FFT along x only); U^, N^u, a^, S full 2D spectra.
@@ -100,7 +100,7 @@ __global__ void etd_coeff_kernel(T* tab, int ny, int nx, int ldc, int symbol, do
 }
 
 // ------------------------------------------------------------------ stage column pass
-enum { E1 = 1, E2S = 2, E3 = 3, E4 = 4 };
+enum { E0 = 0, E1 = 1, E2S = 2, E3 = 3, E4 = 4 };
 
 template <typename T> struct EArgs {
   int ny, log2ny, ncols, ldc, C, njobs;
@@ -114,32 +114,33 @@ template <typename T> struct EArgs {
   int pad;
 };
 
-template <typename T> struct EOcc { static constexpr int v = sizeof(T) == 4 ? 2 : 1; };
+// One CTA: C adjacent kx columns of one field (E1 transforms two inputs per column).
+// FP32 CTAs take up to 1024 threads, so that at ny = 4096 a CTA still covers 2-4
+// columns and each warp access reads whole 32-byte sectors of the row-major spectra;
+// FP64 keeps 512 threads (its butterflies need the registers).
+template <typename T> struct EThreads { static constexpr int v = sizeof(T) == 4 ? 1024 : 512; };
 
 template <typename T>
-__global__ void __launch_bounds__(512, EOcc<T>::v) etd_col_kernel(const __grid_constant__ EArgs<T> a) {
+__global__ void __launch_bounds__(EThreads<T>::v, 1) etd_col_kernel(const __grid_constant__ EArgs<T> a) {
   typedef cx<T> Cx;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   Cx* buf = reinterpret_cast<Cx*>(smem_raw);
   const int f = blockIdx.y;
-  const int Cn = a.C, W = 2 * Cn;
+  const int type = a.type;
+  const int Cn = a.C, W = Cn;
   const int kx0 = blockIdx.x * Cn;
   const int ny = a.ny, tid = threadIdx.x, nth = blockDim.x;
   const long long ldc = a.ldc, fo = (long long)f * a.fs, per = a.fs;
   const T* tab = a.tab + (long long)f * 6 * per;
-  const int type = a.type;
 
-  // load one (or, for E1, two) row-spectrum tiles
-  const Cx* in0 = type == E1 ? a.zu : a.zx;
-  const int nin = type == E1 ? 2 : 1;
-  for (int e = tid; e < ny * Cn * nin; e += nth) {
-    const int which = e / (ny * Cn), r = e - which * ny * Cn;
-    const int ky = r / Cn, c = r - ky * Cn, kx = kx0 + c;
-    const Cx* src = which == 0 ? in0 : a.zn;
-    buf[sp(ky * W + which * Cn + c)] = kx < a.ncols ? src[fo + ky * ldc + kx] : mk<Cx>((T)0, (T)0);
+  // load the row-spectrum tile: E0 ZU, E1 ZN, E2-E4 ZX
+  const Cx* in0 = type == E0 ? a.zu : (type == E1 ? a.zn : a.zx);
+  for (int e = tid; e < ny * Cn; e += nth) {
+    const int ky = e / Cn, c = e - ky * Cn, kx = kx0 + c;
+    buf[sp(ky * W + c)] = kx < a.ncols ? in0[fo + ky * ldc + kx] : mk<Cx>((T)0, (T)0);
   }
   __syncthreads();
-  fft_smem<T, false, true>(buf, ny, a.log2ny, Cn * nin, 1, W, a.tw, tid);
+  fft_smem<T, false, true>(buf, ny, a.log2ny, Cn, 1, W, a.tw, tid);
 
   for (int e = tid; e < ny * Cn; e += nth) {
     const int ky = e / Cn, c = e - ky * Cn, kx = kx0 + c;
@@ -147,12 +148,14 @@ __global__ void __launch_bounds__(512, EOcc<T>::v) etd_col_kernel(const __grid_c
     const long long g = fo + ky * ldc + kx, tg = ky * ldc + kx;
     const Cx x = buf[sp(ky * W + c)];
     Cx out;
-    if (type == E1) {
-      const Cx n = buf[sp(ky * W + Cn + c)];
-      const T e2 = tab[1 * per + tg], q = tab[2 * per + tg];
+    if (type == E0) {  // the initial U^ (later steps get it from E4)
       a.uh[g] = x;
-      a.nu[g] = n;
-      out = mk<Cx>(e2 * x.x + q * n.x, e2 * x.y + q * n.y);
+      continue;
+    } else if (type == E1) {
+      const T e2 = tab[1 * per + tg], q = tab[2 * per + tg];
+      const Cx u = a.uh[g];
+      a.nu[g] = x;
+      out = mk<Cx>(e2 * u.x + q * x.x, e2 * u.y + q * x.y);
       a.ah[g] = out;
     } else if (type == E2S) {
       const T e2 = tab[1 * per + tg], q = tab[2 * per + tg];
@@ -168,9 +171,11 @@ __global__ void __launch_bounds__(512, EOcc<T>::v) etd_col_kernel(const __grid_c
       const T E = tab[0 * per + tg], f1 = tab[3 * per + tg], f2 = tab[4 * per + tg], f3 = tab[5 * per + tg];
       const Cx u = a.uh[g], nu = a.nu[g], s = a.ss[g];
       out = mk<Cx>(E * u.x + f1 * nu.x + f2 * s.x + f3 * x.x, E * u.y + f1 * nu.y + f2 * s.y + f3 * x.y);
+      a.uh[g] = out;  // next step's U^ (unnormalised, as the forward transform leaves it)
     }
     buf[sp(ky * W + c)] = cscale(out, a.scale);
   }
+  if (type == E0) return;
   __syncthreads();
   fft_smem<T, true, true>(buf, ny, a.log2ny, Cn, 1, W, a.tw, tid);
   Cx* dst = type == E4 ? a.zu : a.zx;
@@ -209,7 +214,6 @@ template <typename T>
 struct EtdPlan {
   EArgs<T> c[5];
   RowArgs<T> rN, r4, rin, rout;
-  size_t csmem;
 };
 
 template <typename T>
@@ -222,12 +226,14 @@ static EtdPlan<T> build_etd(const void* plan, const mjx_grid2d* g, double F, dou
   memset(&e, 0, sizeof(e));
   e.ny = g->ny; e.log2ny = ilog2_exact(g->ny); e.ncols = g->nx / 2 + 1; e.ldc = ldc;
   const int tps = g->ny >= 16 ? g->ny / 16 : 1;
-  int C = 256 / tps;
-  if (C < 1) C = 1;
-  if (C > 8) C = 8;
-  const int maxth = sizeof(T) == 4 ? 512 : 512;
-  while (C > 1 && (2 * C * tps > maxth || (size_t)sp_size(g->ny * 2 * C) * 2 * sizeof(T) > 200 * 1024)) C >>= 1;
-  e.C = C; e.njobs = 2;
+  // widest tile within the thread cap and ~200 KB of shared memory
+  auto tile = [&](int nin) {
+    int C = 16;
+    while (C > 1 && (C * nin * tps > EThreads<T>::v ||
+                     (size_t)sp_size(g->ny * nin * C) * 2 * sizeof(T) > 200 * 1024)) C >>= 1;
+    return C;
+  };
+  e.njobs = 2;
   e.zu = (cx<T>*)(ws + L.zu); e.zn = (cx<T>*)(ws + L.zn); e.zx = (cx<T>*)(ws + L.zx);
   e.uh = (cx<T>*)(ws + L.uh); e.nu = (cx<T>*)(ws + L.nu); e.ah = (cx<T>*)(ws + L.ah); e.ss = (cx<T>*)(ws + L.ss);
   e.tab = (const T*)(ws + L.tab); e.fs = L.fs; e.tw = (const cx<T>*)pv.twy;
@@ -235,8 +241,11 @@ static EtdPlan<T> build_etd(const void* plan, const mjx_grid2d* g, double F, dou
   // row-space state ZU is an unnormalised row DFT both after the initial r2c and
   // after each step
   e.scale = (T)(1.0 / (double)g->ny);
-  for (int t = 1; t <= 4; ++t) { P.c[t] = e; P.c[t].type = t; }
-  P.csmem = (size_t)sp_size(g->ny * 2 * C) * 2 * sizeof(T);
+  for (int t = E0; t <= E4; ++t) {
+    P.c[t] = e;
+    P.c[t].type = t;
+    P.c[t].C = tile(1);
+  }
 
   RowArgs<T> r;
   memset(&r, 0, sizeof(r));
@@ -259,10 +268,11 @@ static EtdPlan<T> build_etd(const void* plan, const mjx_grid2d* g, double F, dou
 }
 
 template <typename T>
-static cudaError_t etd_col(const EArgs<T>& e, size_t smem, cudaStream_t s) {
+static cudaError_t etd_col(const EArgs<T>& e, cudaStream_t s) {
   const int tps = e.ny >= 16 ? e.ny / 16 : 1;
   dim3 grid((e.ncols + e.C - 1) / e.C, e.njobs);
-  etd_col_kernel<T><<<grid, 2 * e.C * tps, smem, s>>>(e);
+  const size_t smem = (size_t)sp_size(e.ny * e.C) * 2 * sizeof(T);
+  etd_col_kernel<T><<<grid, e.C * tps, smem, s>>>(e);
   return cudaGetLastError();
 }
 
@@ -270,7 +280,7 @@ template <typename T>
 static cudaError_t etd_step(const EtdPlan<T>& P, cudaStream_t s) {
   cudaError_t e;
   for (int t = 1; t <= 4; ++t) {
-    if ((e = etd_col<T>(P.c[t], P.csmem, s)) != cudaSuccess) return e;
+    if ((e = etd_col<T>(P.c[t], s)) != cudaSuccess) return e;
     const RowArgs<T>& r = t < 4 ? P.rN : P.r4;
     if ((e = launch_row<T, RX_GRAY_SCOTT>(r, s)) != cudaSuccess) return e;
   }
@@ -297,6 +307,7 @@ static mjx_status etd_run(const void* plan, const mjx_grid2d* g, int symbol, con
   }
   const EtdPlan<T> P = build_etd<T>(plan, g, F, k, ws, L, y_in, y_out);
   MJX_CUDA_TRY((launch_row<T, RX_GRAY_SCOTT>(P.rin, s)));
+  MJX_CUDA_TRY(etd_col<T>(P.c[E0], s));  // U^ of the initial state
   MJX_CUDA_TRY((launch_row<T, RX_GRAY_SCOTT>(P.r4, s)));
   if (n_steps > 0) {
     // one step captured once, replayed n_steps times
@@ -367,11 +378,11 @@ mjx_status mjx_etdrk4_kernel2d(const void* plan, const mjx_grid2d* g, int dtype,
   cudaError_t ce;
   if (e == 4) {
     const EtdPlan<float> P = build_etd<float>(plan, g, F, k, (char*)ws, L, nullptr, nullptr);
-    ce = (which & 1) ? etd_col<float>(P.c[(which + 1) / 2], P.csmem, s)
+    ce = (which & 1) ? etd_col<float>(P.c[(which + 1) / 2], s)
                      : launch_row<float, RX_GRAY_SCOTT>(which == 8 ? P.r4 : P.rN, s);
   } else {
     const EtdPlan<double> P = build_etd<double>(plan, g, F, k, (char*)ws, L, nullptr, nullptr);
-    ce = (which & 1) ? etd_col<double>(P.c[(which + 1) / 2], P.csmem, s)
+    ce = (which & 1) ? etd_col<double>(P.c[(which + 1) / 2], s)
                      : launch_row<double, RX_GRAY_SCOTT>(which == 8 ? P.r4 : P.rN, s);
   }
   return cuda_status(ce);
