@@ -185,6 +185,9 @@ __global__ void __launch_bounds__(256, Occ<T>::row) row_kernel(const __grid_cons
   T* ob = rout + pr.rb + y * a.rstride;
   const T* ea = a.eref + pr.ra + y * a.rstride;
   const T* eb = a.eref + pr.rb + y * a.rstride;
+  // parameters converted once (the per-element double arithmetic would occupy the FP64 pipe)
+  const T pF = (T)a.F, pK = (T)a.k, pR = (T)a.r, pFK = (T)(a.F + a.k);
+  const T pAtol = (T)a.atol, pRtol = (T)a.rtol;
   T ra_[16], rb_[16];
   if (flags & ROW_ERRNORM) {
 #pragma unroll
@@ -203,29 +206,29 @@ __global__ void __launch_bounds__(256, Occ<T>::row) row_kernel(const __grid_cons
       // Gray-Scott reaction terms (operators.py:655-667); Fisher-KPP r u (1-u)
       if (RX == RX_GRAY_SCOTT) {
         const T uvv = va * vb * vb;
-        const T nu = -uvv + (T)a.F * ((T)1 - va), nv = uvv - (T)(a.F + a.k) * vb;
+        const T nu = -uvv + pF * ((T)1 - va), nv = uvv - pFK * vb;
         va = nu; vb = nv;
       } else if (RX == RX_FISHER) {
-        va = (T)a.r * va * ((T)1 - va); vb = (T)a.r * vb * ((T)1 - vb);
+        va = pR * va * ((T)1 - va); vb = pR * vb * ((T)1 - vb);
       } else {
         va = (T)0; vb = (T)0;
       }
     }
     if (flags & ROW_REACT) {
-      if (flags & ROW_DELTA) react_delta<T, RX>(va, vb, h, (T)a.F, (T)a.k, (T)a.r);
-      else if (flags & ROW_EULER) react_euler<T, RX>(va, vb, h, (T)a.F, (T)a.k, (T)a.r);
-      else react_heun<T, RX>(va, vb, h, (T)a.F, (T)a.k, (T)a.r);
+      if (flags & ROW_DELTA) react_delta<T, RX>(va, vb, h, pF, pK, pR);
+      else if (flags & ROW_EULER) react_euler<T, RX>(va, vb, h, pF, pK, pR);
+      else react_heun<T, RX>(va, vb, h, pF, pK, pR);
     }
     if (flags & ROW_STORE_REAL) { oa[x] = va; ob[x] = vb; }
     if (flags & ROW_ERRNORM) {
       // moljax/core/state.py:335-339: (err / (atol + rtol |y_new|))^2
-      const T da = (va - ra_[m]) / ((T)a.atol + (T)a.rtol * fabs(va));
-      const T db = (vb - rb_[m]) / ((T)a.atol + (T)a.rtol * fabs(vb));
+      const T da = (va - ra_[m]) / (pAtol + pRtol * fabs(va));
+      const T db = (vb - rb_[m]) / (pAtol + pRtol * fabs(vb));
       esum += da * da + db * db;
       bad |= !(finite_(va) && finite_(vb));
     }
     if (flags & ROW_ERRPAIR) {
-      const T da = va / ((T)a.atol + (T)a.rtol * fabs(vb));
+      const T da = va / (pAtol + pRtol * fabs(vb));
       esum += da * da;
       bad |= !(finite_(va) && finite_(vb));
     }
@@ -297,8 +300,10 @@ __device__ __forceinline__ T multiplier(int mul, T hD, T lam, int pw) {
   return pw == 2 ? m * m : m;
 }
 
+template <typename T> struct ColThreads { static constexpr int v = sizeof(T) == 4 ? 1024 : 512; };
+
 template <typename T>
-__global__ void __launch_bounds__(512, Occ<T>::col) col_kernel(const __grid_constant__ ColArgs<T> a) {
+__global__ void __launch_bounds__(ColThreads<T>::v, 1) col_kernel(const __grid_constant__ ColArgs<T> a) {
   typedef cx<T> C;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* buf = reinterpret_cast<C*>(smem_raw);
@@ -411,8 +416,12 @@ int col_tile(int ny, int ncols, int nout, int elem) {
   const int tps = ny >= 16 ? ny / 16 : 1;
   int C = 256 / tps;
   if (C < 1) C = 1;
+  // at least one 32-byte sector of every row per CTA (4 FP32 / 2 FP64 complex columns)
+  const int cmin = 32 / (2 * elem);
+  if (C < cmin) C = cmin;
   if (C > 16) C = 16;
-  while (C > 1 && (C * nout * tps > 512 || (size_t)sp_size(ny * C * nout) * 2 * elem > 200 * 1024)) C >>= 1;
+  const int cap = elem == 4 ? 1024 : 512;  // col_kernel thread limit per precision
+  while (C > 1 && (C * nout * tps > cap || (size_t)sp_size(ny * C * nout) * 2 * elem > 200 * 1024)) C >>= 1;
   (void)ncols;
   return C;
 }
