@@ -9,6 +9,7 @@ of the reaction increments (rel-L2 vs the FP64 path is reported in the line).
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
   python bench.py --kernels-only [--reps R]   # per-kernel CUDA-event times only
   python bench.py --workload etdrk4 --n 4096 [--etd-steps S] [--kernels-only]
+  python bench.py --workload serve [--requests R]
 
 Our arm prints one JSON line with the device-timed value, the end-to-end
 number through the public API with host buffers, the live roofline of the
@@ -58,7 +59,8 @@ def parse():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp32"])
     ap.add_argument("--kernels-only", action="store_true")
-    ap.add_argument("--workload", default="imex", choices=["imex", "etdrk4"])
+    ap.add_argument("--workload", default="imex", choices=["imex", "etdrk4", "serve"])
+    ap.add_argument("--requests", type=int, default=512)
     ap.add_argument("--etd-steps", type=int, default=100)
     ap.add_argument("--reps", type=int, default=30)
     return ap.parse_args()
@@ -472,6 +474,26 @@ def run_etdrk4(args, local):
     return out
 
 
+def run_serve(args, local):
+    """The served mix (Poisson arrivals, 60 % tubular-reactor CN, 40 % Gray-Scott IMEX-Strang
+    64^2..512^2): continuous-batching server vs one FP64 solve at a time (the first
+    min(128, requests) requests for the plain comparator)."""
+    import torch
+    from moljax_gb300.serve import make_mix, Server, run_plain, summarize
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    Server(dev, slots=8).run(make_mix(16, seed=99), realtime=False)  # warm plans and kernels
+    mix = make_mix(args.requests)
+    srv = Server(dev, slots=8)
+    done = srv.run(mix)
+    out = {"workload": f"served mix, {args.requests} requests, Poisson 2000/s", "served": summarize(done, srv.makespan)}
+    out["served"]["batches"] = srv.batches
+    k = min(args.requests, 128)
+    plain = run_plain(mix[:k], torch.float64, dev, realtime=False)
+    out[f"plain_fp64_first{k}"] = summarize(plain, max(c.end for c in plain))
+    return out
+
+
 def run_kernels_only(args, local):
     import torch
     dev = torch.device("cuda", local)
@@ -548,6 +570,8 @@ def main():
         out = run_reference(args, rank, world)
     elif args.workload == "etdrk4":
         out = run_etdrk4(args, local)
+    elif args.workload == "serve":
+        out = run_serve(args, local)
     elif args.kernels_only:
         out = run_kernels_only(args, local)
     else:

@@ -34,9 +34,11 @@ PlanView plan_view(const void* plan, int ny, int nx, int elem) {
   return v;
 }
 
+// Sequences (row pairs) per CTA: ~128 threads per CTA, so that the 1024-row passes
+// launch enough CTAs to fill every SM (n = 1024: 2 sequences, n = 4096: one of 256 threads).
 int row_nseq(int n, int nrows) {
   const int tps = n >= 16 ? n / 16 : 1;
-  int ns = 256 / tps;
+  int ns = 128 / tps;
   if (ns < 1) ns = 1;
   if (ns > nrows) ns = nrows;
   return ns;
