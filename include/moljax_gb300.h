@@ -347,6 +347,19 @@ mjx_status mjx_dst1_plan_init(void* plan, int n, int dtype, void* stream);
 mjx_status mjx_dst1(const void* plan, int n, long long nrows, int dtype, int mode, const void* x,
                     void* out, const void* lam, double h, double D, double scale, void* stream);
 
+/* Orthonormal DCT-II (jax.scipy.fft.dct(type=2, norm='ortho')) and the Neumann spectral
+ * solvers along rows of n values: plan of the length-n transform (1 <= n <= 1024, or n a
+ * power of two <= 2048; 0 = unsupported).
+ *  mode 0: out = scale * DCT(x);  mode 1: out = scale * IDCT(x) (DCT-III, the inverse)
+ *  mode 2: out = IDCT(DCT(x) / (1 - h D lam))        (solve_helmholtz_neumann, 333-355)
+ *  mode 3: out = IDCT(DCT(x) / lam), null modes -> 0 (solve_poisson_neumann, 274-305)
+ *  mode 4: out = IDCT(exp(h lam) DCT(u) + h phi1(h lam) DCT(N)) (etd1_neumann, 401-437),
+ *          x holds the nrows rows of u followed by the nrows rows of N(u). */
+size_t mjx_dct2_plan_bytes(int n, int dtype);
+mjx_status mjx_dct2_plan_init(void* plan, int n, int dtype, void* stream);
+mjx_status mjx_dct2(const void* plan, int n, long long nrows, int dtype, int mode, const void* x,
+                    void* out, const void* lam, double h, double D, double scale, void* stream);
+
 /* ---- 1D tubular reactor, Crank-Nicolson, batched --------------------------------- */
 typedef enum mjx_reactor_variant {
   MJX_REACTOR_DANCKWERTS = 0, /* benchmarks/benchmark_reactor_vs_diffrax.py:40-138 */

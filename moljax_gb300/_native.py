@@ -133,6 +133,9 @@ SIGNATURES = {
     "mjx_dst1_plan_bytes": (_sz, [_i, _i]),
     "mjx_dst1_plan_init": (_i, [_vp, _i, _i, _vp]),
     "mjx_dst1": (_i, [_vp, _i, C.c_longlong, _i, _i, _vp, _vp, _vp, _d, _d, _d, _vp]),
+    "mjx_dct2_plan_bytes": (_sz, [_i, _i]),
+    "mjx_dct2_plan_init": (_i, [_vp, _i, _i, _vp]),
+    "mjx_dct2": (_i, [_vp, _i, C.c_longlong, _i, _i, _vp, _vp, _vp, _d, _d, _d, _vp]),
     "mjx_etdrk4_ws_bytes": (_sz, [_i, _i, _i]),
     "mjx_etdrk4_gray_scott2d": (_i, [_vp, C.POINTER(Grid2DC), _i, _i, C.POINTER(C.c_double), _d, _d,
                                      _d, _d, _i, _vp, _vp, _vp, _sz, _i, _vp]),

@@ -36,4 +36,7 @@ from moljax_gb300.core import fft_nonperiodic
 from moljax_gb300.core.fft_nonperiodic import (dst_I_fast, idst_I_fast, laplacian_symbol_dirichlet,
                                                create_nonperiodic_fft_cache,
                                                solve_poisson_dirichlet, solve_helmholtz_dirichlet,
-                                               etd1_dirichlet)
+                                               etd1_dirichlet, laplacian_symbol_neumann,
+                                               solve_poisson_neumann, solve_helmholtz_neumann,
+                                               etd1_neumann, check_compatibility_neumann,
+                                               project_to_compatible)

@@ -66,3 +66,44 @@ def test_unsupported_length_raises(cuda):
     import moljax_gb300 as M
     with pytest.raises(ValueError):
         M.dst_I_fast(torch.zeros(1500, dtype=torch.float64, device=cuda))
+
+
+DCT_SIZES = [1, 2, 3, 5, 32, 64, 100, 1000, 1024, 2048]
+
+
+@pytest.mark.parametrize("n", DCT_SIZES)
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+def test_dct_matches_oracle(cuda, n, dtype):
+    from moljax_gb300.core import fft_nonperiodic as F
+    rng = np.random.default_rng(n + 7)
+    for shape in [(n,), (3, n), (2, 5, n)]:
+        x = rng.standard_normal(shape)
+        X = F.dct(torch.tensor(x, dtype=dtype, device=cuda)).cpu().numpy()
+        ref = OD.dct2_ortho(x)
+        tol = 1e-12 if dtype == torch.float64 else 2e-5
+        assert _rel(X, ref) < tol, (shape, _rel(X, ref))
+        back = F.idct(torch.tensor(ref, dtype=dtype, device=cuda)).cpu().numpy()
+        assert _rel(back, x) < tol
+
+
+@pytest.mark.parametrize("n", [32, 50, 256])
+def test_neumann_solvers_vs_oracle(cuda, n):
+    from moljax_gb300.core import fft_nonperiodic as F
+    import moljax_gb300 as M
+    rng = np.random.default_rng(11)
+    dx, dt, D = 1.0 / n, 0.01, 0.5
+    rhs = rng.standard_normal((4, n))
+    rhs_c = rhs - rhs.mean(axis=-1, keepdims=True)
+    cache = M.create_nonperiodic_fft_cache(n, dx, "neumann", device=cuda)
+    lam = OD.laplacian_symbol_neumann(n, dx)
+    np.testing.assert_allclose(cache.laplacian_symbol.cpu().numpy(), lam, rtol=1e-14, atol=1e-300)
+    r = torch.tensor(rhs, device=cuda)
+    h = F.solve_helmholtz_neumann(r, cache.laplacian_symbol, dt, D).cpu().numpy()
+    assert _rel(h, OD.solve_helmholtz_neumann(rhs, lam, dt, D)) < 1e-12
+    p = F.solve_poisson_neumann(torch.tensor(rhs_c, device=cuda), cache.laplacian_symbol).cpu().numpy()
+    assert _rel(p, OD.solve_poisson_neumann(rhs_c, lam)) < 1e-12
+    Nu = rng.standard_normal((4, n))
+    e = F.etd1_neumann(r, torch.tensor(Nu, device=cuda), D * cache.laplacian_symbol, dt).cpu().numpy()
+    assert _rel(e, OD.etd1_neumann(rhs, Nu, D * lam, dt)) < 1e-12
+    assert not F.check_compatibility_neumann(torch.ones(32, device=cuda))
+    assert F.check_compatibility_neumann(F.project_to_compatible(torch.ones(32, dtype=torch.float64, device=cuda)))

@@ -196,3 +196,33 @@ def test_dst_oracle_pins():
     rhs = u - dt * D * A @ u
     np.testing.assert_allclose(OD.solve_helmholtz_dirichlet(rhs, lam, dt, D), u, rtol=1e-10, atol=1e-12)
     np.testing.assert_allclose(OD.solve_poisson_dirichlet(A @ u, lam), u, rtol=1e-9, atol=1e-11)
+
+
+def test_dct_oracle_pins():
+    import scipy.fft
+    from oracle import dst as OD
+    rng = np.random.default_rng(1)
+    for N in (1, 2, 5, 32, 100):
+        x = rng.standard_normal((3, N))
+        np.testing.assert_allclose(OD.dct2_ortho(x), scipy.fft.dct(x, type=2, norm="ortho", axis=-1),
+                                   rtol=1e-12, atol=1e-12)
+        np.testing.assert_allclose(OD.idct2_ortho(OD.dct2_ortho(x)), x, rtol=1e-12, atol=1e-12)
+    # tests/test_fft_nonperiodic.py: Neumann symbol null mode, identity limit, constant kept
+    lam = OD.laplacian_symbol_neumann(32, 0.1)
+    assert abs(lam[0]) < 1e-14 and np.all(lam[1:] < 0)
+    rhs = np.cos(np.pi * np.arange(32) / 32)
+    # jnp.allclose defaults: rtol 1e-8 given, atol 1e-8
+    np.testing.assert_allclose(OD.solve_helmholtz_neumann(rhs, lam, 1e-10, 1.0), rhs, rtol=1e-8, atol=1e-8)
+    u = np.full(32, 5.0)
+    for _ in range(10):
+        u = OD.etd1_neumann(u, np.zeros(32), 0.1 * lam, 0.1)
+    np.testing.assert_allclose(u, 5.0, rtol=1e-10, atol=1e-8)
+    # the Helmholtz solve inverts (I - dt D Lap_N), the 3-point Laplacian with mirrored ends
+    N, dx, dt, D = 40, 0.05, 0.2, 0.3
+    A = (np.diag(-2.0 * np.ones(N)) + np.diag(np.ones(N - 1), 1) + np.diag(np.ones(N - 1), -1))
+    A[0, 0] = A[-1, -1] = -1.0
+    A /= dx ** 2
+    v = rng.standard_normal(N)
+    lamN = OD.laplacian_symbol_neumann(N, dx)
+    np.testing.assert_allclose(OD.solve_helmholtz_neumann(v - dt * D * A @ v, lamN, dt, D), v,
+                               rtol=1e-10, atol=1e-12)
