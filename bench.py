@@ -8,7 +8,7 @@ of the reaction increments (rel-L2 vs the FP64 path is reported in the line).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
   python bench.py --kernels-only [--reps R]   # per-kernel CUDA-event times only
-  python bench.py --workload etdrk4 --n 4096 [--etd-steps S] [--kernels-only]
+  python bench.py --workload etdrk4 --n 4096 [--etd-steps S] [--kernels-only] [--etd-method etd1|etd2]
   python bench.py --workload serve [--requests R]
 
 Our arm prints one JSON line with the device-timed value, the end-to-end
@@ -62,6 +62,7 @@ def parse():
     ap.add_argument("--workload", default="imex", choices=["imex", "etdrk4", "serve"])
     ap.add_argument("--requests", type=int, default=512)
     ap.add_argument("--etd-steps", type=int, default=100)
+    ap.add_argument("--etd-method", default="etdrk4", choices=["etdrk4", "etd1", "etd2"])
     ap.add_argument("--reps", type=int, default=30)
     return ap.parse_args()
 
@@ -411,9 +412,51 @@ def etd_kernel_bytes(n):
     return {k: 2 * nc * v for k, v in per.items()}
 
 
+def etd12_step_bytes(n, method):
+    """Algorithmic bytes of one ETD1 / ETD2 step (2 fields, FP32): per field and half-spectrum
+    element, column pass ETD1 4 complex + 2 coefficient accesses, ETD2 6 + 3; row pass 2."""
+    nc = n * (n // 2 + 1)
+    col = 4 * 8 + 2 * 4 if method == "etd1" else 6 * 8 + 3 * 4
+    return 2 * nc * (col + 16)
+
+
+def run_etd12(args, local):
+    """Fixed-step coupled ETD1 / ETD2 Gray-Scott (FP32 state, FP64 phi coefficients) at n^2
+    through etd_integrate: grid-pt-steps/s and the step-level achieved bandwidth."""
+    import torch
+    import moljax_gb300 as M
+    from moljax_gb300.workloads import gray_scott_initial_condition
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    n, S = args.n, args.etd_steps
+    grid = M.Grid2D(n, n, 0.0, L_BOX, 0.0, L_BOX)
+    y0 = gray_scott_initial_condition(grid, SEED, torch.float32, dev)
+    g = grid.n_ghost
+    st = {k: y0[k][g:g + n, g:g + n].contiguous() for k in ("u", "v")}
+    ops = {"u": M.DiffusionOperator(grid, DU, torch.float32), "v": M.DiffusionOperator(grid, DV, torch.float32)}
+    nl = M.NativeNonlinear.gray_scott(F, K)
+    M.etd_integrate(st, (0.0, 3.0), 1.0, ops, nl, method=args.etd_method, save_every=3)
+    torch.cuda.synchronize(dev)
+    s = torch.cuda.current_stream(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    M.etd_integrate(st, (0.0, float(S)), 1.0, ops, nl, method=args.etd_method, save_every=S)
+    e1.record(s)
+    e1.synchronize()
+    t = e0.elapsed_time(e1) * 1e-3
+    b = etd12_step_bytes(n, args.etd_method)
+    peak, peak_kind = peaks()
+    gbs = b * S / t / 1e9
+    return {"workload": f"gray-scott {args.etd_method.upper()} {n}x{n} FP32, dt=1", "n": n, "steps": S,
+            "value": n * n * S / t, "unit": UNIT, "ms_per_step": t / S * 1e3, "step_alg_bytes": b,
+            "achieved_gbs": gbs, "frac_of_" + peak_kind.replace(" ", "_"): gbs / peak}
+
+
 def run_etdrk4(args, local):
     """Fixed-step coupled ETDRK4 Gray-Scott (FP32 state, FP64 contour coefficients) at n^2:
     grid-pt-steps/s over --etd-steps steps, and the live per-pass roofline."""
+    if args.etd_method != "etdrk4":
+        return run_etd12(args, local)
     import torch
     import moljax_gb300 as M
     from moljax_gb300 import _native as N

@@ -42,13 +42,17 @@ typedef enum mjx_dtype { MJX_F32 = 0, MJX_F64 = 1 } mjx_dtype;
 /* Periodic Laplacian eigenvalues: FD 5-point symbol (moljax/core/fft_solvers.py:124-154)
  * or pseudo-spectral -(kx^2+ky^2) (benchmarks/benchmark_vs_scipy.py:77-80). */
 typedef enum mjx_symbol { MJX_SYMBOL_FD = 0, MJX_SYMBOL_SPECTRAL = 1 } mjx_symbol;
+/* OR-ed into an ETD symbol: the symbol has no y part, so each grid row is an
+ * independent periodic 1D problem (moljax's 1D DiffusionOperator, fft_operators.py:80-176). */
+#define MJX_SYMBOL_X_ONLY 0x10
 
 /* Spectral multipliers applied between forward and inverse transform. */
 typedef enum mjx_mult {
   MJX_MULT_SCALE = 0,      /* identity (round trip) */
   MJX_MULT_HELMHOLTZ = 1,  /* 1/(1 - h D lam), |denominator| clamped at 1e-14 */
   MJX_MULT_CN = 2,         /* (1 + h D lam/2)/(1 - h D lam/2) */
-  MJX_MULT_EXP = 3         /* exp(h D lam) */
+  MJX_MULT_EXP = 3,        /* exp(h D lam) */
+  MJX_MULT_LAP = 5         /* h D lam (the operator itself, DiffusionOperator.matvec) */
 } mjx_mult;
 
 typedef enum mjx_reaction {
@@ -405,6 +409,44 @@ mjx_status mjx_etdrk4_gray_scott2d(const void* plan, const mjx_grid2d* grid, int
                                    int n_steps,
                                    const void* y_in, void* y_out, void* ws, size_t ws_bytes,
                                    int recompute_coeffs, void* stream);
+/* ---- ETD1 / ETD2 / ETDRK4 (moljax/core/fft_integrators.py) ---------------------- */
+typedef enum mjx_etd_method { MJX_ETD_1 = 1, MJX_ETD_2 = 2, MJX_ETD_RK4 = 4 } mjx_etd_method;
+typedef enum mjx_etd_coeffs {
+  MJX_ETD_COEFF_CONTOUR = 0, /* 32-point contour mean (benchmark_gray_scott.py:336-356); ETDRK4 only */
+  MJX_ETD_COEFF_PHI = 1      /* phi functions, Taylor below |z| = 1e-4 (fft_integrators.py:39-116) */
+} mjx_etd_coeffs;
+
+typedef struct mjx_etd_problem {
+  int method;       /* mjx_etd_method */
+  int coeffs;       /* mjx_etd_coeffs (ETD1 and ETD2 always use the phi functions) */
+  int symbol;       /* mjx_symbol, optionally | MJX_SYMBOL_X_ONLY */
+  int reaction;     /* MJX_REACT_NONE (N = 0), MJX_REACT_GRAY_SCOTT (nfields 2), MJX_REACT_FISHER (r u (1-u)) */
+  int nfields;      /* 1 or 2; interior fields [nfields][ny][nx] */
+  int pad;
+  double D[2];      /* diffusivity per field: L = D Lap */
+  double F, k, r;   /* reaction parameters */
+  double dt;
+  double f2_factor; /* contour ETDRK4 only: 2 Cox-Matthews, 1 the benchmark script's update */
+} mjx_etd_problem;
+
+/* n_steps fixed steps of u_t = D Lap u + N(u) on a periodic grid, as etd_integrate
+ * (fft_integrators.py:344-393) runs etd1_step (119-175), etd2_step (178-249) or
+ * etdrk4_step (252-341); the nonlinear term of the Gray-Scott pair is evaluated
+ * coupled.  ETD2 without nprev_in starts with an ETD1 step (207-209); with
+ * nprev_in (real N(u_{n-1}), [nfields][ny][nx]) every step is ETD2.  n_out
+ * (optional, n_steps >= 1) receives N at the start of the last step, the N_curr
+ * that etd2_step returns.  The coefficient tables live in the workspace
+ * (size mjx_etdrk4_ws_bytes); recompute_coeffs = 0 reuses them for the same grid,
+ * problem and dt. */
+mjx_status mjx_etd_integrate2d(const void* plan, const mjx_grid2d* grid, int dtype, const mjx_etd_problem* p,
+                               int n_steps, const void* y_in, const void* nprev_in, void* y_out, void* n_out,
+                               void* ws, size_t ws_bytes, int recompute_coeffs, void* stream);
+
+/* N(y) of the ETD problem's reaction on interior fields [nfields][ny][nx] (one row
+ * pass); the nonlinear_rhs of fft_integrators for a native reaction. */
+mjx_status mjx_etd_nonlinear2d(const void* plan, const mjx_grid2d* grid, int dtype, int reaction, int nfields,
+                               double F, double k, double r, const void* y, void* out, void* stream);
+
 /* Launches one kernel of an ETDRK4 step for timing/profiling (which = 1..8:
  * C1, R1, C2, R2, C3, R3, C4, R4).  No reference counterpart. */
 mjx_status mjx_etdrk4_kernel2d(const void* plan, const mjx_grid2d* grid, int dtype, double F,

@@ -26,12 +26,21 @@ STATUS_NAMES = {
 }
 F32, F64 = 0, 1
 SYMBOL_FD, SYMBOL_SPECTRAL = 0, 1
-MULT_SCALE, MULT_HELMHOLTZ, MULT_CN, MULT_EXP = 0, 1, 2, 3
+MULT_SCALE, MULT_HELMHOLTZ, MULT_CN, MULT_EXP, MULT_LAP = 0, 1, 2, 3, 5
 REACT_NONE, REACT_GRAY_SCOTT, REACT_FISHER = 0, 1, 2
+SYMBOL_X_ONLY = 0x10
+ETD_1, ETD_2, ETD_RK4 = 1, 2, 4
+ETD_COEFF_CONTOUR, ETD_COEFF_PHI = 0, 1
 
 
 class Grid2DC(C.Structure):
     _fields_ = [("ny", C.c_int), ("nx", C.c_int), ("dy", C.c_double), ("dx", C.c_double)]
+
+
+class ETDProblemC(C.Structure):
+    _fields_ = [("method", C.c_int), ("coeffs", C.c_int), ("symbol", C.c_int), ("reaction", C.c_int),
+                ("nfields", C.c_int), ("pad", C.c_int), ("D", C.c_double * 2), ("F", C.c_double),
+                ("k", C.c_double), ("r", C.c_double), ("dt", C.c_double), ("f2_factor", C.c_double)]
 
 
 class PIDParamsC(C.Structure):
@@ -139,6 +148,9 @@ SIGNATURES = {
     "mjx_etdrk4_ws_bytes": (_sz, [_i, _i, _i]),
     "mjx_etdrk4_gray_scott2d": (_i, [_vp, C.POINTER(Grid2DC), _i, _i, C.POINTER(C.c_double), _d, _d,
                                      _d, _d, _i, _vp, _vp, _vp, _sz, _i, _vp]),
+    "mjx_etd_integrate2d": (_i, [_vp, C.POINTER(Grid2DC), _i, C.POINTER(ETDProblemC), _i, _vp, _vp, _vp, _vp,
+                                 _vp, _sz, _i, _vp]),
+    "mjx_etd_nonlinear2d": (_i, [_vp, C.POINTER(Grid2DC), _i, _i, _i, _d, _d, _d, _vp, _vp, _vp]),
     "mjx_etdrk4_kernel2d": (_i, [_vp, C.POINTER(Grid2DC), _i, _d, _d, _i, _vp, _sz, _vp]),
     "mjx_imex2d_mixed_ws_bytes": (_sz, [_i, _i, _i]),
     "mjx_imex_adaptive2d_mixed": (_i, [_vp, _vp, C.POINTER(Grid2DC), _i, C.POINTER(ImexProblemC),

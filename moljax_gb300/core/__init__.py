@@ -19,7 +19,9 @@ from moljax_gb300.core.fft_solvers import (create_fft_cache, solve_helmholtz_2d,
                                            laplacian_symbol_2d)
 from moljax_gb300.core.utils import StatusCode
 from moljax_gb300.core import fft_integrators, fft_operators
-from moljax_gb300.core.fft_integrators import etdrk4_gray_scott, etdrk4_step, etd_integrate
+from moljax_gb300.core.fft_integrators import (etdrk4_gray_scott, etdrk4_step, etd_integrate, etd1_step,
+                                               etd2_step, diffusion_only_etd1, NativeNonlinear,
+                                               etd_integrate_model)
 from moljax_gb300.core.fft_operators import DiffusionOperator
 from moljax_gb300.core import newton_krylov, preconditioners
 from moljax_gb300.core.newton_krylov import (NKParams, NKStats, newton_krylov_solve,

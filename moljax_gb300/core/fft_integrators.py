@@ -1,18 +1,35 @@
 """Exponential time differencing on periodic grids (moljax/core/fft_integrators.py).
 
-``etdrk4_gray_scott`` runs the coupled Gray-Scott ETDRK4 of the reference
-benchmark (benchmarks/benchmark_gray_scott.py:336-417) natively: contour-
-integral coefficients in FP64 on the GPU, FP32 or FP64 state, 8 fused kernels
-per step replayed from a CUDA graph.  ``etdrk4_step`` keeps the library
-signature (fft_integrators.py:252-341) for models whose nonlinear part is a
-native reaction; the reference library applies the later stages per field and
-cannot couple u and v (fft_integrators.py:311-327), this implementation couples
-them as the benchmark does.
+Every integrator here runs natively (``mjx_etd_integrate2d``): one column pass
+per stage fuses the forward FFT along y, the stage combination with FP64-built
+coefficient tables and the inverse FFT; one row pass per stage fuses c2r, the
+nonlinear term and r2c.  Steps of one kind are captured once in a CUDA graph
+and replayed.
+
+* ``etd1_step`` / ``etd2_step`` / ``etdrk4_step`` / ``etd_integrate`` keep the
+  library signatures (fft_integrators.py:119-393) on interior fields, 1D
+  ``(n,)`` or 2D ``(ny, nx)``.  ``nonlinear_rhs`` must be a native term: a
+  ``NativeNonlinear`` (Gray-Scott, logistic, zero) or a MOLModel with a
+  Gray-Scott or Fisher-KPP reaction.  The library ETDRK4 evaluates the later
+  stages one field at a time (311-327) and so cannot couple u and v; here the
+  stages are evaluated on all fields together, which is the same for the
+  uncoupled logistic term.  Fields without a linear operator get L = 0, for
+  which the ETD1, ETD2 and ETDRK4 updates reduce to the library's Euler, AB2 and
+  RK4 fallbacks.
+* ``etdrk4_gray_scott`` runs the coupled Gray-Scott ETDRK4 of the benchmark
+  (benchmarks/benchmark_gray_scott.py:336-417) on a padded MOLModel state, with
+  the 32-point contour coefficients.
+
+1D fields are carried as two identical rows of a (2, n) grid whose symbol has
+no y part, so each row is exactly the 1D problem.
 """
 
 from __future__ import annotations
 
 import ctypes as C
+import math
+from typing import Dict, Optional
+
 import torch
 
 from moljax_gb300 import _native as N
@@ -21,9 +38,221 @@ from moljax_gb300.core.fft_solvers import get_plan, workspace
 
 _coeff_key = {}
 
+METHODS = {"etd1": N.ETD_1, "etd2": N.ETD_2, "etdrk4": N.ETD_RK4}
+
 
 def _symbol_code(symbol):
     return {"fd": N.SYMBOL_FD, "spectral": N.SYMBOL_SPECTRAL}[symbol]
+
+
+class NativeNonlinear:
+    """A nonlinear term N(u) that the native row pass evaluates.
+
+    ``NativeNonlinear.gray_scott(F, k)``: (-u v^2 + F (1 - u), u v^2 - (F + k) v)
+    on fields u, v (operators.py:655-667); ``NativeNonlinear.logistic(r)``:
+    r u (1 - u) on each field (operators.py:680-705); ``NativeNonlinear.zero()``.
+    Calling it as ``nonlinear_rhs(state, t)`` evaluates N on the GPU.
+    """
+
+    def __init__(self, kind: int, F: float = 0.0, k: float = 0.0, r: float = 0.0):
+        self.kind, self.F, self.k, self.r = int(kind), float(F), float(k), float(r)
+
+    @classmethod
+    def gray_scott(cls, F: float, k: float) -> "NativeNonlinear":
+        return cls(N.REACT_GRAY_SCOTT, F=F, k=k)
+
+    @classmethod
+    def logistic(cls, r: float) -> "NativeNonlinear":
+        return cls(N.REACT_FISHER, r=r)
+
+    @classmethod
+    def zero(cls) -> "NativeNonlinear":
+        return cls(N.REACT_NONE)
+
+    @classmethod
+    def of(cls, obj) -> "NativeNonlinear":
+        if isinstance(obj, NativeNonlinear):
+            return obj
+        if hasattr(obj, "reaction_kind"):  # a MOLModel
+            kind = obj.reaction_kind
+            p = obj.params
+            return cls(kind, F=p.get("F", 0.0), k=p.get("k", 0.0), r=p.get("r", 1.0))
+        raise NotImplementedError(
+            "the native ETD path needs a native nonlinear term (NativeNonlinear or a MOLModel with "
+            "a Gray-Scott or Fisher-KPP reaction); arbitrary Python callables are not run")
+
+    def __call__(self, state: Dict[str, torch.Tensor], t: float = 0.0) -> Dict[str, torch.Tensor]:
+        names = _field_order(state, self)
+        y, is2d = _pack(state, names)
+        N.require_cuda(y)
+        (ny, nx, dy, dx), _ = _grid_of(state, names, {})
+        plan = get_plan(ny, nx, dy, dx, "fd", y.dtype, y.device)
+        out = torch.empty_like(y)
+        cg = N.Grid2DC(ny, nx, dy, dx)
+        for g in _groups(names):
+            sl = slice(g[0], g[-1] + 1)
+            N.check("mjx_etd_nonlinear2d", N.lib().mjx_etd_nonlinear2d(
+                N.ptr(plan.buf), C.byref(cg), plan.code, self.kind, len(g), self.F, self.k, self.r,
+                N.ptr(y[sl]), N.ptr(out[sl]), N.stream_ptr(plan.device)))
+        return _unpack(out, names, is2d)
+
+
+def _field_order(state, nl: NativeNonlinear):
+    names = list(state.keys())
+    if nl.kind == N.REACT_GRAY_SCOTT:
+        if set(names) != {"u", "v"}:
+            raise ValueError("the Gray-Scott term acts on fields 'u' and 'v'")
+        return ["u", "v"]
+    return names
+
+
+def _pack(state, names):
+    """Stack interior fields to (nf, ny, nx); 1D fields become two identical rows."""
+    f0 = state[names[0]]
+    if f0.ndim == 1:
+        return torch.stack([torch.stack([state[n], state[n]]) for n in names]).contiguous(), False
+    if f0.ndim != 2:
+        raise ValueError("fields must be 1D (n,) or 2D (ny, nx) interior arrays")
+    return torch.stack([state[n] for n in names]).contiguous(), True
+
+
+def _unpack(y, names, is2d):
+    if is2d:
+        return {n: y[i] for i, n in enumerate(names)}
+    return {n: y[i, 0].clone() for i, n in enumerate(names)}
+
+
+def _grid_of(state, names, linear_ops):
+    """(ny, nx, dy, dx, symbol flags) of the packed fields."""
+    f0 = state[names[0]]
+    op = next((linear_ops[n] for n in names if linear_ops and n in linear_ops), None)
+    if f0.ndim == 1:
+        n = f0.shape[0]
+        dx = op.grid.dx if op is not None else 1.0 / n
+        return (2, n, dx, dx), N.SYMBOL_FD | N.SYMBOL_X_ONLY
+    ny, nx = f0.shape
+    if op is not None:
+        return (ny, nx, op.grid.dy, op.grid.dx), N.SYMBOL_FD
+    return (ny, nx, 1.0 / ny, 1.0 / nx), N.SYMBOL_FD
+
+
+def _run(y: torch.Tensor, grid, symbol: int, D, nl: NativeNonlinear, method: int, coeffs: int,
+         dt: float, n_steps: int, nprev: Optional[torch.Tensor] = None, want_n: bool = False,
+         f2_factor: float = 2.0):
+    """n_steps native ETD steps of packed fields y (nf, ny, nx); returns (y_out, n_out)."""
+    nf = y.shape[0]
+    if nf > 2:
+        raise NotImplementedError("the native ETD path takes one or two fields per call")
+    ny, nx, dy, dx = grid
+    plan = get_plan(ny, nx, dy, dx, "fd", y.dtype, y.device)
+    lib = N.lib()
+    ws = workspace(lib.mjx_etdrk4_ws_bytes(ny, nx, plan.code), plan.device, "etd")
+    pb = N.ETDProblemC()
+    pb.method, pb.coeffs, pb.symbol, pb.reaction, pb.nfields = method, coeffs, symbol, nl.kind, nf
+    pb.D[0] = float(D[0])
+    pb.D[1] = float(D[1] if nf > 1 else 0.0)
+    pb.F, pb.k, pb.r, pb.dt, pb.f2_factor = nl.F, nl.k, nl.r, float(dt), float(f2_factor)
+    key = (ny, nx, dy, dx, symbol, y.dtype, tuple(pb.D), float(dt), method, coeffs, float(f2_factor), nf,
+           ws.data_ptr())
+    recompute = int(_coeff_key.get(str(plan.device)) != key)
+    _coeff_key[str(plan.device)] = key
+    out = torch.empty_like(y)
+    n_out = torch.empty_like(y) if want_n else None
+    cg = N.Grid2DC(ny, nx, dy, dx)
+    if nprev is not None:
+        nprev = nprev.to(y.dtype).contiguous()
+    N.check("mjx_etd_integrate2d", lib.mjx_etd_integrate2d(
+        N.ptr(plan.buf), C.byref(cg), plan.code, C.byref(pb), int(n_steps), N.ptr(y),
+        N.ptr(nprev) if nprev is not None else None, N.ptr(out), N.ptr(n_out) if want_n else None,
+        N.ptr(ws), ws.numel(), recompute, N.stream_ptr(plan.device)))
+    return out, n_out
+
+
+def _setup(state, linear_ops, nonlinear_rhs, model=None):
+    nl = NativeNonlinear.of(model if model is not None else nonlinear_rhs)
+    names = _field_order(state, nl)
+    y, is2d = _pack(state, names)
+    N.require_cuda(y)
+    grid, symbol = _grid_of(state, names, linear_ops or {})
+    D = [float(linear_ops[n].D) if linear_ops and n in linear_ops else 0.0 for n in names]
+    return nl, names, y, is2d, grid, symbol, D
+
+
+def _groups(names):
+    """Fields go through the native call two at a time: the Gray-Scott pair
+    together; the other terms act on each field alone."""
+    return [list(range(i, min(len(names), i + 2))) for i in range(0, len(names), 2)]
+
+
+def _advance(state, dt, linear_ops, nonlinear_rhs, method, n_steps, coeffs=N.ETD_COEFF_PHI,
+             N_prev=None, want_n=False, model=None):
+    nl, names, y, is2d, grid, symbol, D = _setup(state, linear_ops, nonlinear_rhs, model)
+    out = torch.empty_like(y)
+    nout = torch.empty_like(y) if want_n else None
+    nprev = None
+    if N_prev is not None:
+        nprev, _ = _pack(N_prev, names)
+    for g in _groups(names):
+        sl = slice(g[0], g[-1] + 1)
+        o, no = _run(y[sl].contiguous(), grid, symbol, [D[i] for i in g], nl, method, coeffs, dt, n_steps,
+                     nprev[sl] if nprev is not None else None, want_n)
+        out[sl] = o
+        if want_n:
+            nout[sl] = no
+    return _unpack(out, names, is2d), (_unpack(nout, names, is2d) if want_n else None)
+
+
+def etd1_step(state, t: float, dt: float, linear_ops, nonlinear_rhs, model=None):
+    """u_{n+1} = exp(dt L) u_n + dt phi1(dt L) N(u_n) (fft_integrators.py:119-175)."""
+    return _advance(state, dt, linear_ops, nonlinear_rhs, N.ETD_1, 1, model=model)[0]
+
+
+def etd2_step(state, t: float, dt: float, linear_ops, nonlinear_rhs, N_prev=None, model=None):
+    """ETD2 (fft_integrators.py:178-249): returns (new_state, N(state)); ETD1 without N_prev."""
+    return _advance(state, dt, linear_ops, nonlinear_rhs, N.ETD_2, 1, N_prev=N_prev, want_n=True,
+                    model=model)
+
+
+def etdrk4_step(state, t: float, dt: float, linear_ops, nonlinear_rhs, model=None):
+    """Cox-Matthews ETDRK4 with the phi-function coefficients (fft_integrators.py:252-341)."""
+    return _advance(state, dt, linear_ops, nonlinear_rhs, N.ETD_RK4, 1, model=model)[0]
+
+
+def etd_integrate(u0, t_span, dt: float, linear_ops, nonlinear_rhs, method: str = "etd1",
+                  save_every: int = 1, model=None):
+    """fft_integrators.py:344-393: int((t_end - t_start) / dt) steps, the state saved
+    every save_every steps; returns (t_history, state_history).  Steps after the last
+    save change nothing that is returned and are not run."""
+    if method not in METHODS:
+        raise ValueError(f"Unknown method: {method}. Use 'etd1', 'etd2', or 'etdrk4'")
+    t0, t1 = t_span
+    n_steps = int((t1 - t0) / dt)
+    nsave = n_steps // save_every
+    t_hist = [t0]
+    hist = [u0]
+    state, N_prev, t = u0, None, t0
+    m = METHODS[method]
+    for s in range(nsave):
+        more = s + 1 < nsave
+        state, n_last = _advance(state, dt, linear_ops, nonlinear_rhs, m, save_every,
+                                 N_prev=N_prev if m == N.ETD_2 else None,
+                                 want_n=(m == N.ETD_2 and more), model=model)
+        N_prev = n_last
+        for _ in range(save_every):
+            t += dt
+        t_hist.append(t)
+        hist.append(state)
+    return torch.tensor(t_hist, dtype=torch.float64), hist
+
+
+def diffusion_only_etd1(u0: torch.Tensor, t_end: float, dt: float, op) -> torch.Tensor:
+    """fft_integrators.py:513-542: max(1, int(t_end/dt)) steps of exp(h L), h = t_end/n."""
+    n = max(1, int(t_end / dt))
+    h = t_end / n
+    u = u0
+    for _ in range(n):
+        u = op.exp_matvec(u, h)
+    return u
 
 
 def etdrk4_gray_scott(model, y0, dt: float, n_steps: int, symbol: str = "fd",
@@ -37,47 +266,21 @@ def etdrk4_gray_scott(model, y0, dt: float, n_steps: int, symbol: str = "fd",
     """
     f2_factor = {"cox-matthews": 2.0, "benchmark": 1.0}[variant]
     if model.reaction_kind != N.REACT_GRAY_SCOTT:
-        raise NotImplementedError("native ETDRK4 is built for the coupled Gray-Scott reaction")
+        raise NotImplementedError("etdrk4_gray_scott is the coupled Gray-Scott integrator")
     grid = model.grid
     names = model.field_names
     interior = stencil.unpad(stencil.stack(y0, names), grid)
     D = model.diffusivities()
-    ny, nx = grid.ny, grid.nx
-    plan = get_plan(ny, nx, grid.dy, grid.dx, symbol, interior.dtype, interior.device)
-    lib = N.lib()
-    ws = workspace(lib.mjx_etdrk4_ws_bytes(ny, nx, plan.code), plan.device, "etd")
-    key = (ny, nx, grid.dy, grid.dx, symbol, interior.dtype, D["u"], D["v"], float(dt), f2_factor,
-           ws.data_ptr())
-    recompute = int(_coeff_key.get(str(plan.device)) != key)
-    _coeff_key[str(plan.device)] = key
-    out = torch.empty_like(interior)
-    Dc = (C.c_double * 2)(D["u"], D["v"])
-    N.check("mjx_etdrk4_gray_scott2d", lib.mjx_etdrk4_gray_scott2d(
-        N.ptr(plan.buf), C.byref(plan.cgrid), plan.code, _symbol_code(symbol), Dc,
-        float(model.params["F"]), float(model.params["k"]), float(dt), f2_factor, int(n_steps),
-        N.ptr(interior), N.ptr(out), N.ptr(ws), ws.numel(), recompute,
-        N.stream_ptr(plan.device)))
+    nl = NativeNonlinear.of(model)
+    out, _ = _run(interior, (grid.ny, grid.nx, grid.dy, grid.dx), _symbol_code(symbol), [D["u"], D["v"]], nl,
+                  N.ETD_RK4, N.ETD_COEFF_CONTOUR, dt, n_steps, f2_factor=f2_factor)
     padded = stencil.pad_interior(out, grid, model.bc_spec, names)
     return {n: padded[i] for i, n in enumerate(names)}
 
 
-def etdrk4_step(state, t: float, dt: float, linear_ops, nonlinear_rhs, model=None):
-    """One ETDRK4 step (fft_integrators.py:252-341).
-
-    ``linear_ops`` maps field names to ``DiffusionOperator``; ``nonlinear_rhs``
-    must be the model's native Gray-Scott reaction (a MOLModel, or a
-    NonlinearOp carrying kind MJX_REACT_GRAY_SCOTT together with ``model=``).
-    """
-    m = model if model is not None else nonlinear_rhs
-    if not hasattr(m, "reaction_kind"):
-        raise NotImplementedError("etdrk4_step runs natively for a Gray-Scott MOLModel")
-    return etdrk4_gray_scott(m, state, dt, 1)
-
-
-def etd_integrate(model, y0, t0: float, t_end: float, dt: float, symbol: str = "fd",
-                  variant: str = "cox-matthews"):
-    """Fixed-step ETDRK4 from t0 to t_end, n = ceil((t_end-t0)/dt) steps
-    (fft_integrators.py:344-393; step count as benchmark_gray_scott.py)."""
-    import math
+def etd_integrate_model(model, y0, t0: float, t_end: float, dt: float, symbol: str = "fd",
+                        variant: str = "cox-matthews"):
+    """Fixed-step coupled ETDRK4 of a Gray-Scott MOLModel from t0 to t_end:
+    n = ceil((t_end - t0)/dt) steps (the benchmark's step count); returns (state, t)."""
     n = int(math.ceil((t_end - t0) / dt - 1e-12))
     return etdrk4_gray_scott(model, y0, dt, n, symbol, variant), t0 + n * dt

@@ -533,8 +533,8 @@ def adaptive_integrate(model, y0=None, t0: float = 0.0, t_end: Optional[float] =
     method = IntegratorType(int(method))
     if method == IntegratorType.ETDRK4:
         # the reference has no adaptive ETDRK4: fixed steps of dt0 over the span
-        from moljax_gb300.core.fft_integrators import etd_integrate
-        y, tf = etd_integrate(model, y0, t0, t_end, dt0, kw.pop("symbol", "fd"))
+        from moljax_gb300.core.fft_integrators import etd_integrate_model
+        y, tf = etd_integrate_model(model, y0, t0, t_end, dt0, kw.pop("symbol", "fd"))
         n = int(round((tf - t0) / dt0))
         return AdaptiveResult(tf, y, torch.tensor([t0, tf], dtype=torch.float64), None,
                               torch.tensor([dt0], dtype=torch.float64), 2, n, 0, 0)

@@ -1,4 +1,5 @@
-// ETDRK4 (Cox-Matthews) for coupled Gray-Scott on a periodic box.
+// Exponential time differencing on a periodic box: ETDRK4 (Cox-Matthews),
+// ETD1 (exponential Euler) and ETD2 (exponential Adams-Bashforth 2).
 //
 // Restates benchmarks/benchmark_gray_scott.py:336-417.  Coefficients E, E2,
 // Q, f1, f2, f3 per Fourier mode come from the M = 32 point contour mean
@@ -22,6 +23,19 @@
 // Trefethen ETDRK4 (the library's b2 = 2 phi2 - 4 phi3, fft_integrators.py:110);
 // 1 reproduces the benchmark script, whose update uses f2 (N^a + N^b) without
 // the factor 2 (benchmark_gray_scott.py:415).
+//
+// The library form (moljax/core/fft_integrators.py) takes its coefficients from
+// the phi functions instead (39-116: Taylor series below |z| = 1e-4, closed form
+// above), and adds ETD1 (119-175) and ETD2 (178-249):
+//
+//   ETD1  N^ = F(ZN); U^' = E U^ + dt phi1 N^; store U^'; ZU = F^-1 U^'     + R4
+//   ETD2  N^ = F(ZN); U^' = E U^ + dt phi1 N^ + dt phi2 (N^ - N^prev);
+//         N^prev <- N^; store U^'; ZU = F^-1 U^'                            + R4
+//
+// (the first ETD2 step without a previous N is an ETD1 step that keeps N^, as
+// etd2_step falls back to etd1_step, 207-209).  The nonlinear term is the
+// coupled Gray-Scott reaction on (u, v), the logistic term r u (1 - u) on each
+// field, or zero; one field pairs rows y and y + ny/2 in the row passes.
 #include <math.h>
 #include <string.h>
 
@@ -51,18 +65,37 @@ __device__ __forceinline__ zc zexp(zc a) {
   return {e * c, e * s};
 }
 
-// tab layout: [field][coef 0..5][ky][ldc] with coef = E, E2, Q, f1, f2, f3
+// phi functions exactly as moljax/core/fft_integrators.py:39-78 evaluates them:
+// a cubic Taylor polynomial for |z| < 1e-4, the closed form otherwise.
+__device__ __forceinline__ double phi1_ref(double z) {
+  if (fabs(z) < 1e-4) return 1.0 + z / 2.0 + z * z / 6.0 + z * z * z / 24.0;
+  return (exp(z) - 1.0) / z;
+}
+__device__ __forceinline__ double phi2_ref(double z) {
+  if (fabs(z) < 1e-4) return 0.5 + z / 6.0 + z * z / 24.0 + z * z * z / 120.0;
+  return (exp(z) - 1.0 - z) / (z * z);
+}
+__device__ __forceinline__ double phi3_ref(double z) {
+  if (fabs(z) < 1e-4) return 1.0 / 6.0 + z / 24.0 + z * z / 120.0 + z * z * z / 720.0;
+  return (exp(z) - 1.0 - z - z * z / 2.0) / (z * z * z);
+}
+
+enum { FORM_CONTOUR_RK4 = 0, FORM_PHI_RK4 = 1, FORM_PHI_ETD12 = 2 };
+
+// tab layout: [field][coef 0..5][ky][ldc]
+//   RK4 forms: E, E2, Q, f1, f2, f3;   ETD1/ETD2: E, dt phi1, dt phi2
+// xonly: the symbol has no y part (each row an independent 1D problem).
 template <typename T>
-__global__ void etd_coeff_kernel(T* tab, int ny, int nx, int ldc, int symbol, double dy, double dx,
-                                 double D0, double D1, double dt, int M, double f2_factor) {
+__global__ void etd_coeff_kernel(T* tab, int ny, int nx, int ldc, int symbol, int xonly, double dy,
+                                 double dx, double D0, double D1, int nf, double dt, int M,
+                                 double f2_factor, int form) {
   const long long per = (long long)ny * ldc;
-  const int nf = 2;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < per * nf;
        i += (long long)gridDim.x * blockDim.x) {
     const int f = (int)(i / per);
     const long long r = i - f * per;
     const int ky = (int)(r / ldc), kx = (int)(r - (long long)ky * ldc);
-    const int my = ky < ny / 2 ? ky : ky - ny;
+    const int my = xonly ? 0 : (ky < ny / 2 ? ky : ky - ny);
     double lam;
     if (kx > nx / 2) {
       lam = 0.0;
@@ -73,6 +106,25 @@ __global__ void etd_coeff_kernel(T* tab, int ny, int nx, int ldc, int symbol, do
       lam = -(kxx * kxx + kyy * kyy);
     }
     const double z = dt * (f == 0 ? D0 : D1) * lam;
+    T* t = tab + (long long)f * 6 * per + r;
+    if (form == FORM_PHI_ETD12) {
+      t[0 * per] = (T)exp(z);
+      t[1 * per] = (T)(dt * phi1_ref(z));
+      t[2 * per] = (T)(dt * phi2_ref(z));
+      continue;
+    }
+    if (form == FORM_PHI_RK4) {
+      // _etdrk4_coefficients (fft_integrators.py:81-116): a = E2 u + (dt/2) phi1(z/2) N,
+      // u' = E u + dt (b1 N + b2 (Na + Nb) + b4 Nc)
+      const double p1 = phi1_ref(z), p2 = phi2_ref(z), p3 = phi3_ref(z);
+      t[0 * per] = (T)exp(z);
+      t[1 * per] = (T)exp(z / 2.0);
+      t[2 * per] = (T)(dt / 2.0 * phi1_ref(z / 2.0));
+      t[3 * per] = (T)(dt * (p1 - 3.0 * p2 + 4.0 * p3));
+      t[4 * per] = (T)(dt * (2.0 * p2 - 4.0 * p3));
+      t[5 * per] = (T)(dt * (-p2 + 4.0 * p3));
+      continue;
+    }
     zc Q = {0, 0}, f1 = {0, 0}, f2 = {0, 0}, f3 = {0, 0};
     for (int j = 1; j <= M; ++j) {
       double s, c;
@@ -89,7 +141,6 @@ __global__ void etd_coeff_kernel(T* tab, int ny, int nx, int ldc, int symbol, do
       f3 = zadd(f3, zdiv(zadd(zsub(zsub({-4, 0}, zsc(LR, 3)), LR2), zmul(eLR, zsub({4, 0}, LR))), LR3));
     }
     const double w = dt / M;
-    T* t = tab + (long long)f * 6 * per + r;
     t[0 * per] = (T)exp(z);
     t[1 * per] = (T)exp(0.5 * z);
     t[2 * per] = (T)(w * Q.x);
@@ -100,7 +151,7 @@ __global__ void etd_coeff_kernel(T* tab, int ny, int nx, int ldc, int symbol, do
 }
 
 // ------------------------------------------------------------------ stage column pass
-enum { E0 = 0, E1 = 1, E2S = 2, E3 = 3, E4 = 4 };
+enum { E0 = 0, E1 = 1, E2S = 2, E3 = 3, E4 = 4, E5 = 5, E6 = 6, E7 = 7 };  // E5 ETD1, E6 ETD1 + keep N^, E7 ETD2
 
 template <typename T> struct EArgs {
   int ny, log2ny, ncols, ldc, C, njobs;
@@ -133,8 +184,8 @@ __global__ void __launch_bounds__(EThreads<T>::v, 1) etd_col_kernel(const __grid
   const long long ldc = a.ldc, fo = (long long)f * a.fs, per = a.fs;
   const T* tab = a.tab + (long long)f * 6 * per;
 
-  // load the row-spectrum tile: E0 ZU, E1 ZN, E2-E4 ZX
-  const Cx* in0 = type == E0 ? a.zu : (type == E1 ? a.zn : a.zx);
+  // load the row-spectrum tile: E0 ZU, E1 and E5-E7 ZN, E2-E4 ZX
+  const Cx* in0 = type == E0 ? a.zu : ((type == E1 || type >= E5) ? a.zn : a.zx);
   for (int e = tid; e < ny * Cn; e += nth) {
     const int ky = e / Cn, c = e - ky * Cn, kx = kx0 + c;
     buf[sp(ky * W + c)] = kx < a.ncols ? in0[fo + ky * ldc + kx] : mk<Cx>((T)0, (T)0);
@@ -167,6 +218,20 @@ __global__ void __launch_bounds__(EThreads<T>::v, 1) etd_col_kernel(const __grid
       const Cx ah = a.ah[g], nu = a.nu[g], s = a.ss[g];
       a.ss[g] = cadd(s, x);
       out = mk<Cx>(e2 * ah.x + q * ((T)2 * x.x - nu.x), e2 * ah.y + q * ((T)2 * x.y - nu.y));
+    } else if (type >= E5) {
+      // ETD1 (fft_integrators.py:165-166) / ETD2 (234-236)
+      const T E = tab[0 * per + tg], p1 = tab[1 * per + tg];
+      const Cx u = a.uh[g];
+      T ox = E * u.x + p1 * x.x, oy = E * u.y + p1 * x.y;
+      if (type == E7) {
+        const T p2 = tab[2 * per + tg];
+        const Cx np = a.nu[g];
+        ox += p2 * (x.x - np.x);
+        oy += p2 * (x.y - np.y);
+      }
+      if (type != E5) a.nu[g] = x;
+      out = mk<Cx>(ox, oy);
+      a.uh[g] = out;
     } else {
       const T E = tab[0 * per + tg], f1 = tab[3 * per + tg], f2 = tab[4 * per + tg], f3 = tab[5 * per + tg];
       const Cx u = a.uh[g], nu = a.nu[g], s = a.ss[g];
@@ -178,7 +243,7 @@ __global__ void __launch_bounds__(EThreads<T>::v, 1) etd_col_kernel(const __grid
   if (type == E0) return;
   __syncthreads();
   fft_smem<T, true, true>(buf, ny, a.log2ny, Cn, 1, W, a.tw, tid);
-  Cx* dst = type == E4 ? a.zu : a.zx;
+  Cx* dst = type >= E4 ? a.zu : a.zx;
   for (int e = tid; e < ny * Cn; e += nth) {
     const int ky = e / Cn, c = e - ky * Cn, kx = kx0 + c;
     if (kx < a.ncols) dst[fo + ky * ldc + kx] = buf[sp(ky * W + c)];
@@ -212,13 +277,17 @@ static EtdLayout etd_layout(int ny, int nx, int elem) {
 
 template <typename T>
 struct EtdPlan {
-  EArgs<T> c[5];
+  EArgs<T> c[8];
+  EArgs<T> c0n;                     // forward transform of N_prev (row spectra in ZX) into N^prev
   RowArgs<T> rN, r4, rin, rout;
+  RowArgs<T> rprev, rnout;          // N_prev real -> ZX; ZU -> N(u) real
 };
 
+// nf = 2: fields u, v paired row by row; nf = 1: rows y and y + ny/2 of one field.
 template <typename T>
-static EtdPlan<T> build_etd(const void* plan, const mjx_grid2d* g, double F, double k, char* ws,
-                            const EtdLayout& L, const T* y_in, T* y_out) {
+static EtdPlan<T> build_etd(const void* plan, const mjx_grid2d* g, int nf, double F, double k, double r_,
+                            char* ws, const EtdLayout& L, const T* y_in, T* y_out, const T* nprev_in,
+                            T* n_out) {
   EtdPlan<T> P;
   const PlanView pv = plan_view(plan, g->ny, g->nx, sizeof(T));
   const int ldc = spec_ldc(g->nx);
@@ -233,7 +302,7 @@ static EtdPlan<T> build_etd(const void* plan, const mjx_grid2d* g, double F, dou
                      (size_t)sp_size(g->ny * nin * C) * 2 * sizeof(T) > 200 * 1024)) C >>= 1;
     return C;
   };
-  e.njobs = 2;
+  e.njobs = nf;
   e.zu = (cx<T>*)(ws + L.zu); e.zn = (cx<T>*)(ws + L.zn); e.zx = (cx<T>*)(ws + L.zx);
   e.uh = (cx<T>*)(ws + L.uh); e.nu = (cx<T>*)(ws + L.nu); e.ah = (cx<T>*)(ws + L.ah); e.ss = (cx<T>*)(ws + L.ss);
   e.tab = (const T*)(ws + L.tab); e.fs = L.fs; e.tw = (const cx<T>*)pv.twy;
@@ -241,29 +310,35 @@ static EtdPlan<T> build_etd(const void* plan, const mjx_grid2d* g, double F, dou
   // row-space state ZU is an unnormalised row DFT both after the initial r2c and
   // after each step
   e.scale = (T)(1.0 / (double)g->ny);
-  for (int t = E0; t <= E4; ++t) {
+  for (int t = E0; t <= E7; ++t) {
     P.c[t] = e;
     P.c[t].type = t;
     P.c[t].C = tile(1);
   }
+  P.c0n = P.c[E0];
+  P.c0n.zu = e.zx;
+  P.c0n.uh = e.nu;
 
   RowArgs<T> r;
   memset(&r, 0, sizeof(r));
-  r.n = g->nx; r.log2n = ilog2_exact(g->nx); r.ldc = ldc; r.nrows = g->ny; r.npairs = 1;
-  r.nseq = row_nseq(g->nx, g->ny); r.rstride = g->nx; r.rin_sel = -1; r.rout_sel = -1;
+  r.n = g->nx; r.log2n = ilog2_exact(g->nx); r.ldc = ldc; r.nrows = nf == 2 ? g->ny : g->ny / 2; r.npairs = 1;
+  r.nseq = row_nseq(g->nx, r.nrows); r.rstride = g->nx; r.rin_sel = -1; r.rout_sel = -1;
   r.spec = (cx<T>*)(ws + L.zu); r.tw = (const cx<T>*)pv.twx; r.inv_scale = (T)(1.0 / (double)g->nx);
-  r.F = F; r.k = k;
+  r.F = F; r.k = k; r.r = r_;
   r.rin[0] = y_in; r.rout[0] = y_out;
   const long long zx = (long long)((L.zx - L.zu) / sizeof(cx<T>)), zn = (long long)((L.zn - L.zu) / sizeof(cx<T>));
-  const long long fr = (long long)g->ny * g->nx;
+  const long long hr = nf == 2 ? (long long)g->ny * g->nx : (long long)(g->ny / 2) * g->nx;
+  const long long hs = nf == 2 ? L.fs : (long long)(g->ny / 2) * ldc;
   RowPair p;
   memset(&p, 0, sizeof(p));
-  p.ra = 0; p.rb = fr;
-  P.rN = r; p.sa = zx; p.sb = zx + L.fs; p.flags = ROW_LOAD_SPEC | ROW_NONLIN | ROW_STORE_SPEC; P.rN.pr[0] = p;
-  P.r4 = r; p.sa = 0; p.sb = L.fs; p.oa = zn; p.ob = zn + L.fs;
+  p.ra = 0; p.rb = hr;
+  P.rN = r; p.sa = zx; p.sb = zx + hs; p.flags = ROW_LOAD_SPEC | ROW_NONLIN | ROW_STORE_SPEC; P.rN.pr[0] = p;
+  P.rprev = r; P.rprev.rin[0] = nprev_in; p.flags = ROW_STORE_SPEC; P.rprev.pr[0] = p;
+  P.r4 = r; p.sa = 0; p.sb = hs; p.oa = zn; p.ob = zn + hs;
   p.flags = ROW_LOAD_SPEC | ROW_NONLIN | ROW_STORE_SPEC | ROW_SPEC_ALT; P.r4.pr[0] = p;
-  P.rin = r; p.sa = 0; p.sb = L.fs; p.flags = ROW_STORE_SPEC; P.rin.pr[0] = p;
+  P.rin = r; p.sa = 0; p.sb = hs; p.flags = ROW_STORE_SPEC; P.rin.pr[0] = p;
   P.rout = r; p.flags = ROW_LOAD_SPEC | ROW_STORE_REAL; P.rout.pr[0] = p;
+  P.rnout = r; P.rnout.rout[0] = n_out; p.flags = ROW_LOAD_SPEC | ROW_NONLIN | ROW_STORE_REAL; P.rnout.pr[0] = p;
   return P;
 }
 
@@ -277,20 +352,61 @@ static cudaError_t etd_col(const EArgs<T>& e, cudaStream_t s) {
 }
 
 template <typename T>
-static cudaError_t etd_step(const EtdPlan<T>& P, cudaStream_t s) {
+static cudaError_t etd_row(const RowArgs<T>& r, int rx, cudaStream_t s) {
+  if (rx == MJX_REACT_GRAY_SCOTT) return launch_row<T, RX_GRAY_SCOTT>(r, s);
+  if (rx == MJX_REACT_FISHER) return launch_row<T, RX_FISHER>(r, s);
+  return launch_row<T, RX_NONE>(r, s);
+}
+
+enum { K_RK4 = 0, K_ETD1 = 1, K_ETD1N = 2, K_ETD2 = 3 };
+
+template <typename T>
+static cudaError_t etd_step(const EtdPlan<T>& P, int kind, int rx, cudaStream_t s) {
   cudaError_t e;
+  if (kind != K_RK4) {
+    const int t = kind == K_ETD1 ? E5 : (kind == K_ETD1N ? E6 : E7);
+    if ((e = etd_col<T>(P.c[t], s)) != cudaSuccess) return e;
+    return etd_row<T>(P.r4, rx, s);
+  }
   for (int t = 1; t <= 4; ++t) {
     if ((e = etd_col<T>(P.c[t], s)) != cudaSuccess) return e;
-    const RowArgs<T>& r = t < 4 ? P.rN : P.r4;
-    if ((e = launch_row<T, RX_GRAY_SCOTT>(r, s)) != cudaSuccess) return e;
+    if ((e = etd_row<T>(t < 4 ? P.rN : P.r4, rx, s)) != cudaSuccess) return e;
   }
   return cudaSuccess;
 }
 
+// cnt steps of one kind: captured once into a graph, replayed cnt times.
 template <typename T>
-static mjx_status etd_run(const void* plan, const mjx_grid2d* g, int symbol, const double* D, double F,
-                          double k, double dt, double f2_factor, int n_steps, const T* y_in, T* y_out,
-                          char* ws, const EtdLayout& L, int recompute, cudaStream_t s) {
+static cudaError_t etd_replay(const EtdPlan<T>& P, int kind, int rx, int cnt, cudaStream_t s) {
+  cudaStream_t cs = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  cudaError_t ce = cudaSuccess;
+  do {
+    if ((ce = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking)) != cudaSuccess) break;
+    if ((ce = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) break;
+    const cudaError_t le = etd_step<T>(P, kind, rx, cs);
+    ce = cudaStreamEndCapture(cs, &graph);
+    if (le != cudaSuccess) { ce = le; break; }
+    if (ce != cudaSuccess) break;
+    if ((ce = cudaGraphInstantiate(&exec, graph, 0)) != cudaSuccess) break;
+    for (int i = 0; i < cnt && ce == cudaSuccess; ++i) ce = cudaGraphLaunch(exec, s);
+  } while (0);
+  if (exec) cudaGraphExecDestroy(exec);
+  if (graph) cudaGraphDestroy(graph);
+  if (cs) cudaStreamDestroy(cs);
+  return ce;
+}
+
+static int etd_form(const mjx_etd_problem* p) {
+  if (p->method != MJX_ETD_RK4) return FORM_PHI_ETD12;
+  return p->coeffs == MJX_ETD_COEFF_PHI ? FORM_PHI_RK4 : FORM_CONTOUR_RK4;
+}
+
+template <typename T>
+static mjx_status etd_run(const void* plan, const mjx_grid2d* g, const mjx_etd_problem* pb, int n_steps,
+                          const T* y_in, const T* nprev_in, T* y_out, T* n_out, char* ws, const EtdLayout& L,
+                          int recompute, cudaStream_t s) {
   static int attr = 0;
   if (!attr) {
     int dev = 0, optin = 0;
@@ -300,37 +416,73 @@ static mjx_status etd_run(const void* plan, const mjx_grid2d* g, int symbol, con
     MJX_CUDA_TRY(cudaFuncSetAttribute(etd_col_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
     attr = 1;
   }
+  const int nf = pb->nfields, rx = pb->reaction;
+  const int symbol = pb->symbol & 1, xonly = (pb->symbol & MJX_SYMBOL_X_ONLY) ? 1 : 0;
   if (recompute) {
-    etd_coeff_kernel<T><<<152 * 8, 256, 0, s>>>((T*)(ws + L.tab), g->ny, g->nx, spec_ldc(g->nx), symbol,
-                                                 g->dy, g->dx, D[0], D[1], dt, 32, f2_factor);
+    etd_coeff_kernel<T><<<152 * 8, 256, 0, s>>>((T*)(ws + L.tab), g->ny, g->nx, spec_ldc(g->nx), symbol, xonly,
+                                                 g->dy, g->dx, pb->D[0], pb->D[1], nf, pb->dt, 32,
+                                                 pb->f2_factor, etd_form(pb));
     MJX_CUDA_TRY(cudaGetLastError());
   }
-  const EtdPlan<T> P = build_etd<T>(plan, g, F, k, ws, L, y_in, y_out);
-  MJX_CUDA_TRY((launch_row<T, RX_GRAY_SCOTT>(P.rin, s)));
+  const EtdPlan<T> P = build_etd<T>(plan, g, nf, pb->F, pb->k, pb->r, ws, L, y_in, y_out, nprev_in, n_out);
+  MJX_CUDA_TRY(etd_row<T>(P.rin, rx, s));
   MJX_CUDA_TRY(etd_col<T>(P.c[E0], s));  // U^ of the initial state
-  MJX_CUDA_TRY((launch_row<T, RX_GRAY_SCOTT>(P.r4, s)));
-  if (n_steps > 0) {
-    // one step captured once, replayed n_steps times
-    cudaStream_t cs = nullptr;
-    cudaGraph_t graph = nullptr;
-    cudaGraphExec_t exec = nullptr;
-    cudaError_t ce = cudaSuccess;
-    do {
-      if ((ce = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking)) != cudaSuccess) break;
-      if ((ce = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) break;
-      const cudaError_t le = etd_step<T>(P, cs);
-      ce = cudaStreamEndCapture(cs, &graph);
-      if (le != cudaSuccess) { ce = le; break; }
-      if (ce != cudaSuccess) break;
-      if ((ce = cudaGraphInstantiate(&exec, graph, 0)) != cudaSuccess) break;
-      for (int i = 0; i < n_steps && ce == cudaSuccess; ++i) ce = cudaGraphLaunch(exec, s);
-    } while (0);
-    if (exec) cudaGraphExecDestroy(exec);
-    if (graph) cudaGraphDestroy(graph);
-    if (cs) cudaStreamDestroy(cs);
-    if (ce != cudaSuccess) { set_last_error(ce, __FILE__, __LINE__); return MJX_CUDA_ERROR; }
+  const int method = pb->method;
+  if (method == MJX_ETD_2 && nprev_in) {
+    MJX_CUDA_TRY(etd_row<T>(P.rprev, rx, s));
+    MJX_CUDA_TRY(etd_col<T>(P.c0n, s));  // N^prev
   }
-  MJX_CUDA_TRY((launch_row<T, RX_GRAY_SCOTT>(P.rout, s)));
+  MJX_CUDA_TRY(etd_row<T>(P.r4, rx, s));  // ZN = row spectra of N(u0)
+  const int regular = method == MJX_ETD_RK4 ? K_RK4 : (method == MJX_ETD_1 ? K_ETD1 : K_ETD2);
+  int i = 0;
+  while (i < n_steps) {
+    const int kind = (method == MJX_ETD_2 && i == 0 && !nprev_in) ? K_ETD1N : regular;
+    const bool last = i == n_steps - 1;
+    if (last && n_out) MJX_CUDA_TRY(etd_row<T>(P.rnout, rx, s));  // N at the start of the last step
+    const int cnt = n_steps - i - (n_out ? 1 : 0);
+    if (kind != regular || last || cnt < 3) {
+      MJX_CUDA_TRY(etd_step<T>(P, kind, rx, s));
+      ++i;
+      continue;
+    }
+    const cudaError_t ce = etd_replay<T>(P, kind, rx, cnt, s);
+    if (ce != cudaSuccess) { set_last_error(ce, __FILE__, __LINE__); return MJX_CUDA_ERROR; }
+    i += cnt;
+  }
+  MJX_CUDA_TRY(etd_row<T>(P.rout, rx, s));
+  return MJX_OK;
+}
+
+// Row pass that replaces real rows by the nonlinear term (no spectra).
+template <typename T>
+static RowArgs<T> nonlin_rows(const void* plan, const mjx_grid2d* g, int nf, double F, double k, double r_,
+                              const T* y, T* out) {
+  const PlanView pv = plan_view(plan, g->ny, g->nx, sizeof(T));
+  RowArgs<T> r;
+  memset(&r, 0, sizeof(r));
+  r.n = g->nx; r.log2n = ilog2_exact(g->nx); r.ldc = spec_ldc(g->nx); r.nrows = nf == 2 ? g->ny : g->ny / 2;
+  r.npairs = 1; r.nseq = row_nseq(g->nx, r.nrows); r.rstride = g->nx; r.rin_sel = -1; r.rout_sel = -1;
+  r.tw = (const cx<T>*)pv.twx; r.inv_scale = (T)1;
+  r.F = F; r.k = k; r.r = r_;
+  r.rin[0] = y; r.rout[0] = out;
+  r.pr[0].ra = 0;
+  r.pr[0].rb = nf == 2 ? (long long)g->ny * g->nx : (long long)(g->ny / 2) * g->nx;
+  r.pr[0].flags = ROW_NONLIN | ROW_STORE_REAL;
+  return r;
+}
+
+static mjx_status check_etd(const mjx_grid2d* g, const mjx_etd_problem* p) {
+  if (!p) return MJX_BAD_ARG;
+  if (p->method != MJX_ETD_1 && p->method != MJX_ETD_2 && p->method != MJX_ETD_RK4) return MJX_BAD_ARG;
+  if (p->coeffs != MJX_ETD_COEFF_CONTOUR && p->coeffs != MJX_ETD_COEFF_PHI) return MJX_BAD_ARG;
+  if ((p->symbol & ~MJX_SYMBOL_X_ONLY) != MJX_SYMBOL_FD && (p->symbol & ~MJX_SYMBOL_X_ONLY) != MJX_SYMBOL_SPECTRAL)
+    return MJX_BAD_ARG;
+  if (p->reaction != MJX_REACT_NONE && p->reaction != MJX_REACT_GRAY_SCOTT && p->reaction != MJX_REACT_FISHER)
+    return MJX_BAD_ARG;
+  if (p->nfields != 1 && p->nfields != 2) return MJX_BAD_ARG;
+  if (p->reaction == MJX_REACT_GRAY_SCOTT && p->nfields != 2) return MJX_BAD_ARG;
+  if (!(p->dt > 0.0)) return MJX_BAD_ARG;
+  (void)g;
   return MJX_OK;
 }
 
@@ -346,25 +498,59 @@ size_t mjx_etdrk4_ws_bytes(int ny, int nx, int dtype) {
   return etd_layout(ny, nx, e).total;
 }
 
-mjx_status mjx_etdrk4_gray_scott2d(const void* plan, const mjx_grid2d* g, int dtype, int symbol,
-                                   const double* D, double F, double k, double dt, double f2_factor,
-                                   int n_steps,
-                                   const void* y_in, void* y_out, void* ws, size_t ws_bytes,
-                                   int recompute_coeffs, void* stream) {
+mjx_status mjx_etd_integrate2d(const void* plan, const mjx_grid2d* g, int dtype, const mjx_etd_problem* p,
+                               int n_steps, const void* y_in, const void* nprev_in, void* y_out, void* n_out,
+                               void* ws, size_t ws_bytes, int recompute_coeffs, void* stream) {
   MJX_TRY(check_grid(g));
+  MJX_TRY(check_etd(g, p));
   const int e = elem_size(dtype);
   if (!e) return MJX_BAD_DTYPE;
-  if (!plan || !D || !y_in || !y_out || n_steps < 0) return MJX_BAD_ARG;
-  if (symbol != MJX_SYMBOL_FD && symbol != MJX_SYMBOL_SPECTRAL) return MJX_BAD_ARG;
+  if (!plan || !y_in || !y_out || n_steps < 0) return MJX_BAD_ARG;
+  if (n_out && n_steps < 1) return MJX_BAD_ARG;
+  if (nprev_in && p->method != MJX_ETD_2) return MJX_BAD_ARG;
   const EtdLayout L = etd_layout(g->ny, g->nx, e);
   if (!ws || ws_bytes < L.total) return MJX_WORKSPACE;
   MJX_TRY(ensure_kernel_attrs());
   cudaStream_t s = (cudaStream_t)stream;
   if (e == 4)
-    return etd_run<float>(plan, g, symbol, D, F, k, dt, f2_factor, n_steps, (const float*)y_in, (float*)y_out,
-                          (char*)ws, L, recompute_coeffs, s);
-  return etd_run<double>(plan, g, symbol, D, F, k, dt, f2_factor, n_steps, (const double*)y_in, (double*)y_out,
-                         (char*)ws, L, recompute_coeffs, s);
+    return etd_run<float>(plan, g, p, n_steps, (const float*)y_in, (const float*)nprev_in, (float*)y_out,
+                          (float*)n_out, (char*)ws, L, recompute_coeffs, s);
+  return etd_run<double>(plan, g, p, n_steps, (const double*)y_in, (const double*)nprev_in, (double*)y_out,
+                         (double*)n_out, (char*)ws, L, recompute_coeffs, s);
+}
+
+mjx_status mjx_etdrk4_gray_scott2d(const void* plan, const mjx_grid2d* g, int dtype, int symbol,
+                                   const double* D, double F, double k, double dt, double f2_factor,
+                                   int n_steps,
+                                   const void* y_in, void* y_out, void* ws, size_t ws_bytes,
+                                   int recompute_coeffs, void* stream) {
+  if (!D) return MJX_BAD_ARG;
+  mjx_etd_problem p;
+  memset(&p, 0, sizeof(p));
+  p.method = MJX_ETD_RK4; p.coeffs = MJX_ETD_COEFF_CONTOUR; p.symbol = symbol;
+  p.reaction = MJX_REACT_GRAY_SCOTT; p.nfields = 2;
+  p.D[0] = D[0]; p.D[1] = D[1]; p.F = F; p.k = k; p.dt = dt; p.f2_factor = f2_factor;
+  return mjx_etd_integrate2d(plan, g, dtype, &p, n_steps, y_in, nullptr, y_out, nullptr, ws, ws_bytes,
+                             recompute_coeffs, stream);
+}
+
+mjx_status mjx_etd_nonlinear2d(const void* plan, const mjx_grid2d* g, int dtype, int reaction, int nfields,
+                               double F, double k, double r, const void* y, void* out, void* stream) {
+  MJX_TRY(check_grid(g));
+  const int e = elem_size(dtype);
+  if (!e) return MJX_BAD_DTYPE;
+  if (!plan || !y || !out) return MJX_BAD_ARG;
+  if (nfields != 1 && nfields != 2) return MJX_BAD_ARG;
+  if (reaction == MJX_REACT_GRAY_SCOTT && nfields != 2) return MJX_BAD_ARG;
+  if (reaction != MJX_REACT_NONE && reaction != MJX_REACT_GRAY_SCOTT && reaction != MJX_REACT_FISHER)
+    return MJX_BAD_ARG;
+  MJX_TRY(ensure_kernel_attrs());
+  cudaStream_t s = (cudaStream_t)stream;
+  // one row pass, real rows in and out
+  const cudaError_t ce = e == 4
+      ? etd_row<float>(nonlin_rows<float>(plan, g, nfields, F, k, r, (const float*)y, (float*)out), reaction, s)
+      : etd_row<double>(nonlin_rows<double>(plan, g, nfields, F, k, r, (const double*)y, (double*)out), reaction, s);
+  return cuda_status(ce);
 }
 
 mjx_status mjx_etdrk4_kernel2d(const void* plan, const mjx_grid2d* g, int dtype, double F, double k,
@@ -377,11 +563,13 @@ mjx_status mjx_etdrk4_kernel2d(const void* plan, const mjx_grid2d* g, int dtype,
   cudaStream_t s = (cudaStream_t)stream;
   cudaError_t ce;
   if (e == 4) {
-    const EtdPlan<float> P = build_etd<float>(plan, g, F, k, (char*)ws, L, nullptr, nullptr);
+    const EtdPlan<float> P = build_etd<float>(plan, g, 2, F, k, 0.0, (char*)ws, L, nullptr, nullptr, nullptr,
+                                              nullptr);
     ce = (which & 1) ? etd_col<float>(P.c[(which + 1) / 2], s)
                      : launch_row<float, RX_GRAY_SCOTT>(which == 8 ? P.r4 : P.rN, s);
   } else {
-    const EtdPlan<double> P = build_etd<double>(plan, g, F, k, (char*)ws, L, nullptr, nullptr);
+    const EtdPlan<double> P = build_etd<double>(plan, g, 2, F, k, 0.0, (char*)ws, L, nullptr, nullptr, nullptr,
+                                                nullptr);
     ce = (which & 1) ? etd_col<double>(P.c[(which + 1) / 2], s)
                      : launch_row<double, RX_GRAY_SCOTT>(which == 8 ? P.r4 : P.rN, s);
   }

@@ -296,6 +296,8 @@ __device__ __forceinline__ T multiplier(int mul, T hD, T lam, int pw) {
     m = ((T)1 + x) / ((T)1 - x);
   } else if (mul == MUL_EXP) {
     m = exp(hD * lam);
+  } else if (mul == MUL_LAP) {
+    m = hD * lam;
   } else {
     m = (T)1;
   }
@@ -519,6 +521,8 @@ mjx_status spectral_apply(const void* plan, const mjx_grid2d* g, int nfields, co
   int idx[4], nd = 0;
   for (int f = 0; f < nfields; ++f) {
     if (D[f] > 1e-14 || moves(f)) idx[nd++] = f;
+    else if (mult == MUL_LAP)  // D Lap u = 0
+      MJX_CUDA_TRY(cudaMemsetAsync(out + f * fsz, 0, fsz * sizeof(T), s));
     else if (in != out)
       MJX_CUDA_TRY(cudaMemcpyAsync(out + f * fsz, in + f * fsz, fsz * sizeof(T), cudaMemcpyDeviceToDevice, s));
   }
@@ -687,7 +691,7 @@ mjx_status mjx_spectral_apply2d(const void* plan, const mjx_grid2d* g, int dtype
   MJX_TRY(check_grid(g));
   if (nfields < 1 || nfields > 4 || D == nullptr || plan == nullptr || in == nullptr || out == nullptr)
     return MJX_BAD_ARG;
-  if (mult < MJX_MULT_SCALE || mult > MJX_MULT_EXP) return MJX_BAD_ARG;
+  if ((mult < MJX_MULT_SCALE || mult > MJX_MULT_EXP) && mult != MJX_MULT_LAP) return MJX_BAD_ARG;
   const int e = elem_size(dtype);
   if (!e) return MJX_BAD_DTYPE;
   if (ws == nullptr || ws_bytes < mjx_spec2d_ws_bytes(g->ny, g->nx, nfields, dtype)) return MJX_WORKSPACE;

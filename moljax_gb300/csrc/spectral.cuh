@@ -77,7 +77,7 @@ template <typename T> struct RowArgs {
   RowPair pr[MJX_MAXPAIR];
 };
 
-enum { MUL_SCALE = 0, MUL_HELMHOLTZ = 1, MUL_CN = 2, MUL_EXP = 3, MUL_ADVDIFF = 4 };
+enum { MUL_SCALE = 0, MUL_HELMHOLTZ = 1, MUL_CN = 2, MUL_EXP = 3, MUL_ADVDIFF = 4, MUL_LAP = 5 };
 
 struct ColJob {
   long long sin;         // spectrum offset of the input column block (ky=0, kx=0)

@@ -226,3 +226,79 @@ def test_dct_oracle_pins():
     lamN = OD.laplacian_symbol_neumann(N, dx)
     np.testing.assert_allclose(OD.solve_helmholtz_neumann(v - dt * D * A @ v, lamN, dt, D), v,
                                rtol=1e-10, atol=1e-12)
+
+
+# ------------------------------------------------------------- ETD1 / ETD2 / library ETDRK4
+def _etd_case(n=128, L=1.0):
+    from oracle import etd as OT
+    dx = L / n
+    x = (np.arange(n) + 0.5) * dx  # Grid1D interior coordinates (grid.py:87-110)
+    return OT, x, dx
+
+
+def test_etd1_zero_nonlinear_matches_exponential():
+    # tests/test_fft_operators.py:393-422: ETD1 with N = 0 equals the pure exponential, < 1e-10
+    OT, x, dx = _etd_case(128)
+    lam = {"u": 0.1 * OT.fd_symbol_1d(128, dx)}
+    state = {"u": np.sin(2 * np.pi * x)}
+    for _ in range(int(0.1 / 0.01)):
+        state = OT.etd1_step(state, 0.01, lam, OT.zero)
+    pure = OT.diffusion_only_etd1(np.sin(2 * np.pi * x), 0.1, 0.01, lam["u"])
+    assert np.linalg.norm(state["u"] - pure) / np.linalg.norm(pure) < 1e-10
+
+
+def test_etd_integrate_api_pins():
+    # tests/test_fft_operators.py:424-465: 5 saves, final state within 1e-3 of the exact decay
+    OT, x, dx = _etd_case(128)
+    D = 0.05
+    t, hist = OT.etd_integrate({"u": np.sin(2 * np.pi * x)}, (0.0, 0.2), 0.01,
+                               {"u": D * OT.fd_symbol_1d(128, dx)}, OT.zero, "etd1", 5)
+    assert len(hist) == int(0.2 / 0.01 / 5) + 1
+    exact = np.exp(-4 * np.pi ** 2 * D * 0.2) * np.sin(2 * np.pi * x)
+    assert np.linalg.norm(hist[-1]["u"] - exact) / np.linalg.norm(exact) < 1e-3
+
+
+def test_etdrk4_logistic_pins():
+    # tests/test_fft_operators.py:517-559: ETDRK4 dt = 0.05 within 1 % of ETD1 dt = 0.001
+    OT, x, dx = _etd_case(256)
+    lam = {"u": 0.01 * OT.fd_symbol_1d(256, dx)}
+    u0 = {"u": 0.5 + 0.3 * np.sin(2 * np.pi * x)}
+    N_ = OT.logistic(0.1)
+    _, h4 = OT.etd_integrate(u0, (0.0, 1.0), 0.05, lam, N_, "etdrk4")
+    _, h1 = OT.etd_integrate(u0, (0.0, 1.0), 0.001, lam, N_, "etd1")
+    rel = np.sqrt(np.mean((h4[-1]["u"] - h1[-1]["u"]) ** 2)) / np.sqrt(np.mean(h1[-1]["u"] ** 2))
+    assert rel < 0.01
+
+
+def test_etdrk4_library_order_pin():
+    # tests/test_fft_operators.py:561-617: observed order > 3 (alpha = 0.5, t = 0.5)
+    OT, x, dx = _etd_case(256)
+    lam = {"u": 0.01 * OT.fd_symbol_1d(256, dx)}
+    u0 = {"u": 0.5 + 0.3 * np.sin(2 * np.pi * x)}
+    N_ = OT.logistic(0.5)
+    ref = OT.etd_integrate(u0, (0.0, 0.5), 0.0001, lam, N_, "etdrk4")[1][-1]["u"]
+    errs = [np.linalg.norm(OT.etd_integrate(u0, (0.0, 0.5), dt, lam, N_, "etdrk4")[1][-1]["u"] - ref)
+            / np.linalg.norm(ref) for dt in (0.1, 0.05, 0.025, 0.0125)]
+    orders = [np.log2(errs[i] / errs[i + 1]) for i in range(3) if errs[i + 1] > 1e-14]
+    assert np.mean(orders) > 3.0
+
+
+def test_etd2_second_order_and_phi_switch():
+    OT, x, dx = _etd_case(128)
+    lam = {"u": 0.01 * OT.fd_symbol_1d(128, dx)}
+    u0 = {"u": 0.5 + 0.3 * np.sin(2 * np.pi * x)}
+    N_ = OT.logistic(1.0)
+    ref = OT.etd_integrate(u0, (0.0, 1.0), 0.001, lam, N_, "etdrk4")[1][-1]["u"]
+    e = [np.linalg.norm(OT.etd_integrate(u0, (0.0, 1.0), dt, lam, N_, m)[1][-1]["u"] - ref)
+         for m, dt in (("etd2", 0.1), ("etd2", 0.05), ("etd1", 0.1), ("etd1", 0.05))]
+    assert 3.0 < e[0] / e[1] < 5.0   # ETD2: second order
+    assert 1.6 < e[2] / e[3] < 2.5   # ETD1: first order
+    # the Taylor branch and the closed form agree across |z| = 1e-4
+    z = np.array([-0.99e-4, -1.01e-4])
+    for f in (OT.phi1, OT.phi2):
+        v = f(z)
+        assert abs(v[0] - v[1]) < 1e-5 * abs(v[0])
+    # L = 0: ETD1 is explicit Euler, ETD2 is Adams-Bashforth 2 (fft_integrators.py:172-174, 245-247)
+    s0 = {"u": u0["u"]}
+    e1 = OT.etd1_step(s0, 0.1, {"u": np.zeros(128)}, N_)
+    assert np.allclose(e1["u"], u0["u"] + 0.1 * N_(s0)["u"], rtol=0, atol=1e-14)
