@@ -10,6 +10,7 @@ of the reaction increments (rel-L2 vs the FP64 path is reported in the line).
   python bench.py --kernels-only [--reps R]   # per-kernel CUDA-event times only
   python bench.py --workload etdrk4 --n 4096 [--etd-steps S] [--kernels-only] [--etd-method etd1|etd2]
   python bench.py --workload serve [--requests R]
+  python bench.py --workload fft3d --n 512 [--etd-steps S] [--fp32]
 
 Our arm prints one JSON line with the device-timed value, the end-to-end
 number through the public API with host buffers, the live roofline of the
@@ -27,6 +28,7 @@ from __future__ import annotations
 import argparse
 import ctypes as C
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -59,7 +61,8 @@ def parse():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp32"])
     ap.add_argument("--kernels-only", action="store_true")
-    ap.add_argument("--workload", default="imex", choices=["imex", "etdrk4", "serve"])
+    ap.add_argument("--workload", default="imex", choices=["imex", "etdrk4", "serve", "fft3d"])
+    ap.add_argument("--fp32", action="store_true", help="fft3d: FP32 instead of FP64")
     ap.add_argument("--requests", type=int, default=512)
     ap.add_argument("--etd-steps", type=int, default=100)
     ap.add_argument("--etd-method", default="etdrk4", choices=["etdrk4", "etd1", "etd2"])
@@ -517,6 +520,54 @@ def run_etdrk4(args, local):
     return out
 
 
+def run_fft3d(args, local):
+    """3D FFT-CN diffusion (benchmarks/sisc/bench_3d_feasibility.py: D = 0.1, T = 0.01 in 10
+    steps, spectral symbol) at n^3: the published case (10 steps) timed as the reference
+    times it, plus --etd-steps steps for throughput and the HBM roofline of a step (five
+    passes, each reading and writing the box: 80 B per point FP64, 40 B FP32)."""
+    import numpy as np
+    import torch
+    import moljax_gb300 as M
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    n = args.n
+    dt_ = torch.float32 if args.fp32 else torch.float64
+    x = torch.arange(n, dtype=torch.float64, device=dev) / n
+    s1 = torch.sin(2 * math.pi * x)
+    u0 = (s1[:, None, None] * s1[None, :, None] * s1[None, None, :]).to(dt_).contiguous()
+    D, T, n10 = 0.1, 0.01, 10
+    dt = T / n10
+    for _ in range(3):
+        M.fft_cn_step_3d(u0, D, 1.0 / n, dt, n10)
+    torch.cuda.synchronize(dev)
+    s = torch.cuda.current_stream(dev)
+    times = []
+    for _ in range(5):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        u = M.fft_cn_step_3d(u0, D, 1.0 / n, dt, n10)
+        e1.record(s)
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1))
+    exact = u0.double() * math.exp(-12 * math.pi ** 2 * D * T)
+    err = float((u.double() - exact).abs().max())
+    S = args.etd_steps
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    M.fft_cn_step_3d(u0, D, 1.0 / n, dt, S)
+    e1.record(s)
+    e1.synchronize()
+    t = e0.elapsed_time(e1) * 1e-3
+    per_pt = 80 if dt_ == torch.float64 else 40
+    b = per_pt * n ** 3
+    peak, peak_kind = peaks()
+    gbs = b * S / t / 1e9
+    return {"workload": f"3D FFT-CN diffusion {n}^3 {'FP32' if args.fp32 else 'FP64'}, spectral symbol",
+            "n": n, "published_case_ms": float(np.median(times)), "published_case_max_error": err,
+            "steps": S, "value": n ** 3 * S / t, "unit": UNIT, "ms_per_step": t / S * 1e3,
+            "step_alg_bytes": b, "achieved_gbs": gbs, "frac_of_" + peak_kind.replace(" ", "_"): gbs / peak}
+
+
 def run_serve(args, local):
     """The served mix (Poisson arrivals, 60 % tubular-reactor CN, 40 % Gray-Scott IMEX-Strang
     64^2..512^2): continuous-batching server vs one FP64 solve at a time (the first
@@ -615,6 +666,8 @@ def main():
         out = run_etdrk4(args, local)
     elif args.workload == "serve":
         out = run_serve(args, local)
+    elif args.workload == "fft3d":
+        out = run_fft3d(args, local)
     elif args.kernels_only:
         out = run_kernels_only(args, local)
     else:

@@ -69,6 +69,12 @@ typedef struct mjx_grid2d {
   double dy, dx;
 } mjx_grid2d;
 
+typedef struct mjx_grid3d {
+  int nz, ny, nx;      /* interior points, powers of two in [2, 4096]; arrays [nz][ny][nx] */
+  int pad;
+  double dz, dy, dx;
+} mjx_grid3d;
+
 /* moljax/core/dt_policy.py:49-78 (PIDParams) */
 typedef struct mjx_pid_params {
   double safety, kI, kP, dt_min, dt_max, max_factor, min_factor, atol, rtol;
@@ -111,6 +117,19 @@ size_t mjx_spec2d_ws_bytes(int ny, int nx, int nfields, int dtype);
 mjx_status mjx_spectral_apply2d(const void* plan, const mjx_grid2d* grid, int dtype, int nfields,
                                 const double* D, double h, int mult, const void* in, void* out,
                                 void* ws, size_t ws_bytes, void* stream);
+
+/* ---- periodic 3D boxes (benchmarks/sisc/bench_3d_feasibility.py) ------------------ */
+/* Plan: x / y / z twiddles and 1D symbols (FD or spectral) of an [nz][ny][nx] box. */
+size_t mjx_spec3d_plan_bytes(int nz, int ny, int nx, int dtype);
+mjx_status mjx_spec3d_plan_init(void* plan, const mjx_grid3d* grid, int symbol, int dtype, void* stream);
+/* Spectrum workspace: nz * ny * (nx/2+1 padded) complex. */
+size_t mjx_spec3d_ws_bytes(int nz, int ny, int nx, int dtype);
+/* n_steps times u <- real(IFFTN( m(h, D, lam_x + lam_y + lam_z) FFTN(u) )), each a full
+ * forward and inverse transform: with MJX_MULT_CN the 3D FFT-CN loop of
+ * bench_3d_feasibility.py:71-87 (cn_step_3d in a fori_loop); also Helmholtz, exp, D Lap. */
+mjx_status mjx_spectral_apply3d(const void* plan, const mjx_grid3d* grid, int dtype, double D, double h, int mult,
+                                int n_steps, const void* in, void* out, void* ws, size_t ws_bytes,
+                                void* stream);
 
 /* out_f = real(IFFT2( FFT2(in_f) / (1 - h (D_f lam - i (vx_f kx + vy_f ky))) )): the exact
  * periodic advection-diffusion inverse of FFTAdvectionDiffusionPreconditioner

@@ -37,6 +37,11 @@ class Grid2DC(C.Structure):
     _fields_ = [("ny", C.c_int), ("nx", C.c_int), ("dy", C.c_double), ("dx", C.c_double)]
 
 
+class Grid3DC(C.Structure):
+    _fields_ = [("nz", C.c_int), ("ny", C.c_int), ("nx", C.c_int), ("pad", C.c_int),
+                ("dz", C.c_double), ("dy", C.c_double), ("dx", C.c_double)]
+
+
 class ETDProblemC(C.Structure):
     _fields_ = [("method", C.c_int), ("coeffs", C.c_int), ("symbol", C.c_int), ("reaction", C.c_int),
                 ("nfields", C.c_int), ("pad", C.c_int), ("D", C.c_double * 2), ("F", C.c_double),
@@ -148,6 +153,10 @@ SIGNATURES = {
     "mjx_etdrk4_ws_bytes": (_sz, [_i, _i, _i]),
     "mjx_etdrk4_gray_scott2d": (_i, [_vp, C.POINTER(Grid2DC), _i, _i, C.POINTER(C.c_double), _d, _d,
                                      _d, _d, _i, _vp, _vp, _vp, _sz, _i, _vp]),
+    "mjx_spec3d_plan_bytes": (_sz, [_i, _i, _i, _i]),
+    "mjx_spec3d_plan_init": (_i, [_vp, C.POINTER(Grid3DC), _i, _i, _vp]),
+    "mjx_spec3d_ws_bytes": (_sz, [_i, _i, _i, _i]),
+    "mjx_spectral_apply3d": (_i, [_vp, C.POINTER(Grid3DC), _i, _d, _d, _i, _i, _vp, _vp, _vp, _sz, _vp]),
     "mjx_etd_integrate2d": (_i, [_vp, C.POINTER(Grid2DC), _i, C.POINTER(ETDProblemC), _i, _vp, _vp, _vp, _vp,
                                  _vp, _sz, _i, _vp]),
     "mjx_etd_nonlinear2d": (_i, [_vp, C.POINTER(Grid2DC), _i, _i, _i, _d, _d, _d, _vp, _vp, _vp]),

@@ -16,12 +16,13 @@ from moljax_gb300.core.stepping import (IntegratorType, AdaptiveResult, adaptive
 from moljax_gb300.core.dt_policy import CFLParams, PIDParams
 from moljax_gb300.core.fft_solvers import (create_fft_cache, solve_helmholtz_2d,
                                            apply_diffusion_inverse_fft, fft_cn_step,
-                                           laplacian_symbol_2d)
+                                           laplacian_symbol_2d, fft_cn_step_3d, solve_helmholtz_3d,
+                                           get_plan3d)
 from moljax_gb300.core.utils import StatusCode
 from moljax_gb300.core import fft_integrators, fft_operators
 from moljax_gb300.core.fft_integrators import (etdrk4_gray_scott, etdrk4_step, etd_integrate, etd1_step,
                                                etd2_step, diffusion_only_etd1, NativeNonlinear,
-                                               etd_integrate_model)
+                                               etd_integrate_model, etd_adaptive_integrate)
 from moljax_gb300.core.fft_operators import DiffusionOperator
 from moljax_gb300.core import newton_krylov, preconditioners
 from moljax_gb300.core.newton_krylov import (NKParams, NKStats, newton_krylov_solve,

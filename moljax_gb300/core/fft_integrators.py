@@ -138,15 +138,16 @@ def _grid_of(state, names, linear_ops):
 
 def _run(y: torch.Tensor, grid, symbol: int, D, nl: NativeNonlinear, method: int, coeffs: int,
          dt: float, n_steps: int, nprev: Optional[torch.Tensor] = None, want_n: bool = False,
-         f2_factor: float = 2.0):
-    """n_steps native ETD steps of packed fields y (nf, ny, nx); returns (y_out, n_out)."""
+         f2_factor: float = 2.0, tag: str = "etd"):
+    """n_steps native ETD steps of packed fields y (nf, ny, nx); returns (y_out, n_out).
+    Each workspace tag keeps its own coefficient tables (one per step size in use)."""
     nf = y.shape[0]
     if nf > 2:
         raise NotImplementedError("the native ETD path takes one or two fields per call")
     ny, nx, dy, dx = grid
     plan = get_plan(ny, nx, dy, dx, "fd", y.dtype, y.device)
     lib = N.lib()
-    ws = workspace(lib.mjx_etdrk4_ws_bytes(ny, nx, plan.code), plan.device, "etd")
+    ws = workspace(lib.mjx_etdrk4_ws_bytes(ny, nx, plan.code), plan.device, tag)
     pb = N.ETDProblemC()
     pb.method, pb.coeffs, pb.symbol, pb.reaction, pb.nfields = method, coeffs, symbol, nl.kind, nf
     pb.D[0] = float(D[0])
@@ -154,8 +155,8 @@ def _run(y: torch.Tensor, grid, symbol: int, D, nl: NativeNonlinear, method: int
     pb.F, pb.k, pb.r, pb.dt, pb.f2_factor = nl.F, nl.k, nl.r, float(dt), float(f2_factor)
     key = (ny, nx, dy, dx, symbol, y.dtype, tuple(pb.D), float(dt), method, coeffs, float(f2_factor), nf,
            ws.data_ptr())
-    recompute = int(_coeff_key.get(str(plan.device)) != key)
-    _coeff_key[str(plan.device)] = key
+    recompute = int(_coeff_key.get((str(plan.device), tag)) != key)
+    _coeff_key[(str(plan.device), tag)] = key
     out = torch.empty_like(y)
     n_out = torch.empty_like(y) if want_n else None
     cg = N.Grid2DC(ny, nx, dy, dx)
@@ -284,3 +285,78 @@ def etd_integrate_model(model, y0, t0: float, t_end: float, dt: float, symbol: s
     n = ceil((t_end - t0)/dt) steps (the benchmark's step count); returns (state, t)."""
     n = int(math.ceil((t_end - t0) / dt - 1e-12))
     return etdrk4_gray_scott(model, y0, dt, n, symbol, variant), t0 + n * dt
+
+
+def etd_adaptive_integrate(u0, t0: float, t_end: float, dt0: float, linear_ops, nonlinear_rhs,
+                           method: str = "etdrk4", pid_params=None, max_steps: int = 10000,
+                           save_every: int = 1, model=None, max_attempts: Optional[int] = None):
+    """Adaptive ETD1 / ETDRK4 by step doubling (the reference has fixed-step ETD only).
+
+    Each attempt runs one native step of dt and two of dt/2 from the same state (two
+    workspaces, so each step size keeps its coefficient tables), takes the scaled
+    RMS of their difference with the native error norm, and applies the explicit
+    branch of adaptive_integrate (moljax/core/stepping.py:723-1021): PI controller of
+    order compute_error_order (1 for ETD1, 4 for ETDRK4, dt_policy.py:178-268),
+    halving after a reject, DT_TOO_SMALL / NON_FINITE_VALUES / MAX_STEPS_REACHED.
+    No CFL limit applies: the linear part is integrated exactly.  The accepted state
+    is the two-half-step result.  Returns an AdaptiveResult (interior fields; no y
+    history)."""
+    from moljax_gb300.core.dt_policy import (PIDParams, ControllerState, pid_controller_dt,
+                                             handle_rejected_step)
+    from moljax_gb300.core.fft_solvers import workspace as _ws
+    from moljax_gb300.core.stepping import AdaptiveResult
+    from moljax_gb300.core.utils import StatusCode as S
+    if method not in ("etd1", "etdrk4"):
+        raise ValueError("adaptive ETD: method 'etd1' or 'etdrk4' (ETD2 is a multistep method)")
+    pid = pid_params or PIDParams()
+    order = 1 if method == "etd1" else 4
+    m = METHODS[method]
+    nl, names, y, is2d, grid, symbol, D = _setup(u0, linear_ops, nonlinear_rhs, model)
+    if len(names) > 2:
+        raise NotImplementedError("adaptive ETD takes one or two fields")
+    lib = N.lib()
+    ews = _ws(lib.mjx_error_norm_ws_bytes(), y.device, "errnorm")
+    res = (C.c_double * 2)()
+    max_saves = max_steps // save_every + 1
+    t_hist = torch.zeros(max_saves, dtype=torch.float64)
+    dt_hist = torch.zeros(max_saves, dtype=torch.float64)
+    t_hist[0] = t0
+    t, dt, cs = float(t0), float(dt0), ControllerState(1.0, 1.0, 0)
+    write_idx, n_acc, n_rej, status, attempts = 1, 0, 0, S.RUNNING, 0
+    while status == S.RUNNING and t < t_end and write_idx < max_saves:
+        if max_attempts is not None and attempts >= max_attempts:
+            break
+        attempts += 1
+        dtc = min(dt, t_end - t)
+        y_full, _ = _run(y, grid, symbol, D, nl, m, N.ETD_COEFF_PHI, dtc, 1, tag="etd")
+        y_half, _ = _run(y, grid, symbol, D, nl, m, N.ETD_COEFF_PHI, 0.5 * dtc, 2, tag="etd_half")
+        err = y_half - y_full
+        N.check("mjx_scaled_error_norm", lib.mjx_scaled_error_norm(
+            N.ptr(err), N.ptr(y_half), err.numel(), N.dtype_code(err.dtype), float(pid.atol),
+            float(pid.rtol), res, N.ptr(ews), ews.numel(), N.stream_ptr(y.device)))
+        e, finite = max(float(res[0]), 1e-10), res[1] != 0.0
+        if e <= 1.0:
+            dt_a, cs_new = pid_controller_dt(dtc, e, cs, pid, order)
+        else:
+            dt_a, cs_new = handle_rejected_step(dtc, e, cs, pid, order)[0], cs
+        dt_new = min(max(dt_a, pid.dt_min), pid.dt_max)
+        if e <= 1.0 and finite:
+            if n_acc % save_every == 0:
+                t_hist[write_idx] = t + dtc
+                dt_hist[write_idx - 1] = dtc
+                write_idx += 1
+            t, y, dt, cs = t + dtc, y_half, dt_new, cs_new
+            n_acc += 1
+        else:
+            dt = max(dt_new * 0.5, pid.dt_min)
+            if dt <= pid.dt_min * 1.1:
+                status = S.DT_TOO_SMALL
+            n_rej += 1
+        if not finite:
+            status = S.NON_FINITE_VALUES
+    if t >= t_end:
+        status = S.SUCCESS
+    elif write_idx >= max_saves:
+        status = S.MAX_STEPS_REACHED
+    return AdaptiveResult(t, _unpack(y, names, is2d), t_hist, None, dt_hist, write_idx, n_acc, n_rej,
+                          status)

@@ -234,3 +234,70 @@ def fft_cn_step(u0: torch.Tensor, D: float, dx: float, dt: float, n_steps: int =
         N.ptr(plan.buf), C.byref(plan.cgrid), plan.code, float(D), float(dt), int(n_steps),
         N.ptr(u), N.ptr(out), N.ptr(ws), ws.numel(), N.stream_ptr(plan.device)))
     return out
+
+
+# ----------------------------------------------------------------- periodic 3D boxes
+class SpectralPlan3D:
+    """Device tables of one periodic [nz][ny][nx] box (benchmarks/sisc/bench_3d_feasibility.py)."""
+
+    def __init__(self, nz: int, ny: int, nx: int, dz: float, dy: float, dx: float,
+                 symbol: str = "spectral", dtype: torch.dtype = torch.float64, device=None):
+        N.require_cuda()
+        self.shape = (int(nz), int(ny), int(nx))
+        self.symbol, self.dtype, self.device = symbol, dtype, _device(device)
+        self.code = N.dtype_code(dtype)
+        lib = N.lib()
+        nbytes = lib.mjx_spec3d_plan_bytes(*self.shape, self.code)
+        if nbytes == 0:
+            raise ValueError(f"unsupported box {nz}x{ny}x{nx}: sizes must be powers of two in [2, 4096]")
+        self.buf = torch.empty(nbytes, dtype=torch.uint8, device=self.device)
+        self.cgrid = N.Grid3DC(int(nz), int(ny), int(nx), 0, float(dz), float(dy), float(dx))
+        with torch.cuda.device(self.device):
+            N.check("mjx_spec3d_plan_init", lib.mjx_spec3d_plan_init(
+                N.ptr(self.buf), C.byref(self.cgrid), SYMBOLS[symbol], self.code, N.stream_ptr(self.device)))
+
+    def apply(self, u: torch.Tensor, D: float, h: float, mult: int, n_steps: int = 1) -> torch.Tensor:
+        """n_steps times u <- real(IFFTN(m(h, D, lam) FFTN(u))) on the GPU."""
+        u = u.contiguous()
+        N.require_cuda(u)
+        if tuple(u.shape) != self.shape or u.dtype != self.dtype:
+            raise ValueError(f"expected {self.shape} {self.dtype}, got {tuple(u.shape)} {u.dtype}")
+        lib = N.lib()
+        ws = workspace(lib.mjx_spec3d_ws_bytes(*self.shape, self.code), self.device, "spec3d")
+        out = torch.empty_like(u)
+        N.check("mjx_spectral_apply3d", lib.mjx_spectral_apply3d(
+            N.ptr(self.buf), C.byref(self.cgrid), self.code, float(D), float(h), int(mult), int(n_steps),
+            N.ptr(u), N.ptr(out), N.ptr(ws), ws.numel(), N.stream_ptr(self.device)))
+        return out
+
+
+_plans3d: Dict[tuple, SpectralPlan3D] = {}
+
+
+def get_plan3d(nz, ny, nx, dz, dy, dx, symbol="spectral", dtype=torch.float64, device=None) -> SpectralPlan3D:
+    dev = _device(device)
+    key = (int(nz), int(ny), int(nx), float(dz), float(dy), float(dx), symbol, dtype, str(dev))
+    p = _plans3d.get(key)
+    if p is None:
+        p = SpectralPlan3D(nz, ny, nx, dz, dy, dx, symbol, dtype, dev)
+        _plans3d[key] = p
+    return p
+
+
+def fft_cn_step_3d(u0: torch.Tensor, D: float, dx: float, dt: float, n_steps: int = 1,
+                   symbol: str = "spectral", dy: Optional[float] = None,
+                   dz: Optional[float] = None) -> torch.Tensor:
+    """3D Crank-Nicolson diffusion steps u <- real(ifftn(G fftn(u))),
+    G = (1 + dt D lam/2)/(1 - dt D lam/2), lam = -(kx^2 + ky^2 + kz^2) by default
+    (benchmarks/sisc/bench_3d_feasibility.py:71-87); each step a full transform pair."""
+    nz, ny, nx = u0.shape
+    plan = get_plan3d(nz, ny, nx, dz or dx, dy or dx, dx, symbol, u0.dtype, u0.device)
+    return plan.apply(u0, D, dt, N.MULT_CN, n_steps)
+
+
+def solve_helmholtz_3d(rhs: torch.Tensor, D: float, dt: float, dx: float, symbol: str = "fd",
+                       dy: Optional[float] = None, dz: Optional[float] = None) -> torch.Tensor:
+    """(I - dt D Lap) u = rhs on a periodic box (|denominator| clamped at 1e-14)."""
+    nz, ny, nx = rhs.shape
+    plan = get_plan3d(nz, ny, nx, dz or dx, dy or dx, dx, symbol, rhs.dtype, rhs.device)
+    return plan.apply(rhs, D, dt, N.MULT_HELMHOLTZ)

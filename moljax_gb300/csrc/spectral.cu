@@ -317,6 +317,7 @@ __global__ void __launch_bounds__(ColThreads<T>::v, 1) col_kernel(const __grid_c
   const int kx0 = blockIdx.x * Cn;
   const int ny = a.ny, tid = threadIdx.x, nth = blockDim.x;
   const long long ldc = a.ldc;
+  const long long po = (long long)blockIdx.z * a.pstride;
 
   {
     C v[16];
@@ -324,7 +325,7 @@ __global__ void __launch_bounds__(ColThreads<T>::v, 1) col_kernel(const __grid_c
     for (int m = 0; m < 16; ++m) {
       const int e = tid + m * nth;
       const int ky = e / Cn, c = e - ky * Cn, kx = kx0 + c;
-      if (e < ny * Cn) v[m] = kx < a.ncols ? a.spec[jb.sin + ky * ldc + kx] : mk<C>((T)0, (T)0);
+      if (e < ny * Cn) v[m] = kx < a.ncols ? a.spec[po + jb.sin + ky * ldc + kx] : mk<C>((T)0, (T)0);
     }
 #pragma unroll
     for (int m = 0; m < 16; ++m) {
@@ -342,7 +343,9 @@ __global__ void __launch_bounds__(ColThreads<T>::v, 1) col_kernel(const __grid_c
   const T hD0 = (T)(h * jb.hfac[0] * jb.D), hD1 = (T)(h * jb.hfac[1] * jb.D);
   for (int e = tid; e < ny * Cn; e += nth) {
     const int ky = e / Cn, c = e - ky * Cn, kx = kx0 + c;
-    const T lam = (kx < a.ncols ? a.lamx[kx] : (T)0) + a.lamy[ky];
+    T lxy = (T)0;
+    if (kx < a.ncols) lxy = a.ldc3 ? a.lamx[kx % a.ldc3] + a.lamy2[kx / a.ldc3] : a.lamx[kx];
+    const T lam = lxy + a.lamy[ky];
     const C v = buf[sp(ky * W + c)];
     if (jb.mul == MUL_ADVDIFF) {
       // m(k) = 1/(1 - h (D lam - i (vx kx + vy ky))), |denominator| < 1e-14 -> 1e-14
@@ -378,7 +381,7 @@ __global__ void __launch_bounds__(ColThreads<T>::v, 1) col_kernel(const __grid_c
   for (int e = tid; e < ny * W; e += nth) {
     const int ky = e / W, col = e - ky * W;
     const int o = col / Cn, c = col - o * Cn, kx = kx0 + c;
-    if (kx < a.ncols) a.spec[jb.sout[o] + ky * ldc + kx] = buf[sp(ky * W + col)];
+    if (kx < a.ncols) a.spec[po + jb.sout[o] + ky * ldc + kx] = buf[sp(ky * W + col)];
   }
 }
 
@@ -399,7 +402,7 @@ cudaError_t launch_col(const ColArgs<T>& a, cudaStream_t s) {
   int maxout = 1;
   for (int j = 0; j < a.njobs; ++j) maxout = a.job[j].nout > maxout ? a.job[j].nout : maxout;
   const int tps = a.ny >= 16 ? a.ny / 16 : 1;
-  dim3 grid((a.ncols + a.C - 1) / a.C, a.njobs);
+  dim3 grid((a.ncols + a.C - 1) / a.C, a.njobs, a.nplanes > 1 ? a.nplanes : 1);
   const size_t smem = (size_t)sp_size(a.ny * a.C * maxout) * sizeof(cx<T>);
   col_kernel<T><<<grid, a.C * maxout * tps, smem, s>>>(a);
   return cudaGetLastError();

@@ -102,6 +102,12 @@ template <typename T> struct ColArgs {
   double kxs, kys;       // MUL_ADVDIFF: wavenumber units 2 pi/(nx dx), 2 pi/(ny dy)
   double hfixed;
   const DevState* st;
+  // 3D grids: gridDim.z planes pstride complex elements apart; in the z pass (ldc3 > 0)
+  // column c is (ky, kx) = (c / ldc3, c % ldc3) and lam = lamx[kx] + lamy2[ky] + lamy[row]
+  long long pstride;
+  int nplanes;
+  int ldc3;
+  const T* lamy2;
   ColJob job[MJX_MAXJOB];
 };
 

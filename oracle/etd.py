@@ -172,3 +172,62 @@ def gray_scott(F, k):
 
 def zero(s):
     return {k: np.zeros_like(v) for k, v in s.items()}
+
+
+def adaptive_etd(u0, t0, t_end, dt0, lam, nonlinear, method="etdrk4", pid=None, max_steps=10000,
+                 save_every=1, coupled=False, max_attempts=None):
+    """Adaptive ETD1 / ETDRK4 by step doubling: the accept/reject flow of the explicit
+    branch of adaptive_integrate (moljax/core/stepping.py:723-1021: y_half2 - y_full as the
+    error, scaled_error_norm, PI controller with compute_error_order, halving after a
+    reject, DT_TOO_SMALL / NON_FINITE_VALUES / MAX_STEPS_REACHED) without a CFL limit
+    (the linear part is integrated exactly).  Returns an oracle.imex.AdaptiveResult."""
+    from oracle import imex as OI
+    pid = pid or OI.PIDParams()
+    order = {"etd1": 1, "etdrk4": 4}[method]
+
+    def step(y, h):
+        if method == "etd1":
+            return etd1_step(y, h, lam, nonlinear)
+        return etdrk4_step(y, h, lam, nonlinear, coupled)
+
+    max_saves = max_steps // save_every + 1
+    t_hist, dt_hist = np.zeros(max_saves), np.zeros(max_saves)
+    t_hist[0] = t0
+    t, y, dt, prev_err = float(t0), u0, float(dt0), 1.0
+    write_idx, n_acc, n_rej, status, attempts = 1, 0, 0, OI.RUNNING, 0
+    names = list(u0)
+    while status == OI.RUNNING and t < t_end and write_idx < max_saves:
+        if max_attempts is not None and attempts >= max_attempts:
+            break
+        attempts += 1
+        dtc = min(dt, t_end - t)
+        y_full = step(y, dtc)
+        y_h = step(step(y, 0.5 * dtc), 0.5 * dtc)
+        err = np.stack([y_h[k] - y_full[k] for k in names])
+        yn = np.stack([y_h[k] for k in names])
+        finite = bool(np.all(np.isfinite(yn)))
+        e = max(float(np.sqrt(np.mean((err / (pid.atol + pid.rtol * np.abs(yn))) ** 2))), 1e-10)
+        if e <= 1.0:
+            dt_a, pe_new = OI.pid_controller_dt(dtc, e, prev_err, pid, order)
+        else:
+            dt_a, pe_new = OI.handle_rejected_step(dtc, e, pid, order), prev_err
+        dt_new = min(max(dt_a, pid.dt_min), pid.dt_max)
+        if e <= 1.0 and finite:
+            if n_acc % save_every == 0:
+                t_hist[write_idx] = t + dtc
+                dt_hist[write_idx - 1] = dtc
+                write_idx += 1
+            t, y, dt, prev_err = t + dtc, y_h, dt_new, pe_new
+            n_acc += 1
+        else:
+            dt = max(dt_new * 0.5, pid.dt_min)
+            if dt <= pid.dt_min * 1.1:
+                status = OI.DT_TOO_SMALL
+            n_rej += 1
+        if not finite:
+            status = OI.NON_FINITE_VALUES
+    if t >= t_end:
+        status = OI.SUCCESS
+    elif write_idx >= max_saves:
+        status = OI.MAX_STEPS_REACHED
+    return OI.AdaptiveResult(t, y, t_hist, None, dt_hist, write_idx, n_acc, n_rej, status)

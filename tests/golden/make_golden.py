@@ -3,8 +3,9 @@
 Run in a checkout that has the reference (gogipav14/moljax) at REF (default
 /root/reference).  The fixtures hold only the numbers the tests pin:
 the FFT-CN error tables of benchmarks/results/precision_fp32_fp64.json and
-benchmarks/results/scipy_comparison.json, and the CN reactor conversions of
-benchmarks/results/method_comparison_results.json.
+benchmarks/results/scipy_comparison.json, the CN reactor conversions of
+benchmarks/results/method_comparison_results.json, and the 3D FFT-CN errors and
+times of benchmarks/results/3d_feasibility.json.
 """
 
 import json
@@ -43,6 +44,11 @@ def main():
     with open(os.path.join(HERE, "reactor_published.json"), "w") as f:
         json.dump({"source": "benchmarks/results/method_comparison_results.json",
                    "reactor_methods": reactor}, f, indent=1)
+    f3 = json.load(open(os.path.join(res, "3d_feasibility.json")))
+    with open(os.path.join(HERE, "fft3d_published.json"), "w") as f:
+        json.dump({"source": "benchmarks/results/3d_feasibility.json", "config": f3["config"],
+                   "experiments": [{k: e[k] for k in ("grid_size", "time_ms", "error")}
+                                   for e in f3["experiments"] if e.get("success")]}, f, indent=1)
 
 
 if __name__ == "__main__":

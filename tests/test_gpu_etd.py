@@ -161,3 +161,50 @@ def test_native_nonlinear_and_1d_operator(cuda):
     np.testing.assert_allclose(op.exp_matvec(ut, 0.2).cpu().numpy(), np.real(np.fft.ifft(np.exp(0.2 * lam) * uh)),
                                rtol=0, atol=1e-13)
     np.testing.assert_allclose(op.eigenvalues.numpy(), lam, rtol=1e-14)
+
+
+@pytest.mark.parametrize("method", ["etdrk4", "etd1"])
+def test_adaptive_etd_1d_vs_oracle(cuda, method):
+    import moljax_gb300 as M
+    from oracle import imex as OI
+    n = 128
+    g, x = _grid1d(n)
+    u0 = 0.5 + 0.3 * np.sin(2 * np.pi * x)
+    op = M.DiffusionOperator(g, 0.01)
+    rtol, atol = (1e-7, 1e-9) if method == "etdrk4" else (1e-4, 1e-6)
+    pid = M.PIDParams(rtol=rtol, atol=atol)
+    r = M.etd_adaptive_integrate({"u": torch.tensor(u0, device=cuda)}, 0.0, 2.0, 0.05, {"u": op},
+                                 M.NativeNonlinear.logistic(2.0), method=method, pid_params=pid)
+    o = OT.adaptive_etd({"u": u0}, 0.0, 2.0, 0.05, {"u": 0.01 * OT.fd_symbol_1d(n, g.dx)}, OT.logistic(2.0),
+                        method, OI.PIDParams(rtol=rtol, atol=atol))
+    assert (r.status, r.n_accepted, r.n_rejected) == (o.status, o.n_accepted, o.n_rejected)
+    assert r.status == 0 and r.n_accepted > 3
+    # the step-doubling estimate divides an O(rtol |u|) difference of two solutions by
+    # rtol |u|, so the ~1e-15 rounding of each solution's transforms (Stockham on the GPU,
+    # pocketfft in the oracle) reaches the error ratio as ~1e-15 / rtol and the dt
+    # sequence through the PI controller: rtol 1e-7 -> ~1e-7 relative in dt
+    np.testing.assert_allclose(r.t_history.numpy()[:r.n_steps], o.t_history[:o.n_steps], rtol=1e-5)
+    assert _rel(r.y_final["u"].cpu().numpy(), o.y_final["u"]) < 1e-9
+
+
+def test_adaptive_etdrk4_gray_scott_vs_oracle(cuda):
+    import moljax_gb300 as M
+    from oracle import imex as OI
+    n, L = 32, 2.5
+    grid = M.Grid2D(n, n, 0.0, L, 0.0, L)
+    og = mol.Grid2D(n, n, 0, L, 0, L)
+    y0 = mol.gray_scott_ic(og, 5)
+    u0, v0 = mol.interior(y0["u"], og), mol.interior(y0["v"], og)
+    Du, Dv, F, k = 2e-5, 1e-5, 0.035, 0.065
+    ops = {"u": M.DiffusionOperator(grid, Du), "v": M.DiffusionOperator(grid, Dv)}
+    st = {"u": torch.tensor(u0, device=cuda), "v": torch.tensor(v0, device=cuda)}
+    pid = dict(rtol=1e-6, atol=1e-8, dt_max=20.0)
+    r = M.etd_adaptive_integrate(st, 0.0, 200.0, 1.0, ops, M.NativeNonlinear.gray_scott(F, k),
+                                 pid_params=M.PIDParams(**pid))
+    lam = mol.fd_symbol_2d(n, n, og.dy, og.dx)
+    o = OT.adaptive_etd({"u": u0, "v": v0}, 0.0, 200.0, 1.0, {"u": Du * lam, "v": Dv * lam}, OT.gray_scott(F, k),
+                        "etdrk4", OI.PIDParams(**pid), coupled=True)
+    assert (r.status, r.n_accepted, r.n_rejected) == (o.status, o.n_accepted, o.n_rejected)
+    # v decays to ~1e-12 by t = 200 here, so compare on the O(1) scale of the fields
+    for f in ("u", "v"):
+        assert float(np.max(np.abs(r.y_final[f].cpu().numpy() - o.y_final[f]))) < 1e-9

@@ -302,3 +302,16 @@ def test_etd2_second_order_and_phi_switch():
     s0 = {"u": u0["u"]}
     e1 = OT.etd1_step(s0, 0.1, {"u": np.zeros(128)}, N_)
     assert np.allclose(e1["u"], u0["u"] + 0.1 * N_(s0)["u"], rtol=0, atol=1e-14)
+
+
+@pytest.mark.parametrize("row", [r for r in _load("fft3d_published.json")["experiments"]
+                                 if r["grid_size"] in (32, 48, 64)])
+def test_fft3d_error_pins(row):
+    # benchmarks/results/3d_feasibility.json: N^3, D = 0.1, 10 CN steps to T = 0.01, max error
+    cfg = _load("fft3d_published.json")["config"]
+    N_ = row["grid_size"]
+    u0 = fftcn.node_grid_ic_3d(N_)
+    dt = cfg["t_final"] / cfg["n_steps"]
+    u = fftcn.fft_cn_3d(u0, cfg["D"], 1.0 / N_, dt, cfg["n_steps"])
+    exact = u0 * np.exp(-12 * np.pi ** 2 * cfg["D"] * cfg["n_steps"] * dt)
+    assert float(np.max(np.abs(u - exact))) == pytest.approx(row["error"], rel=1e-8)
