@@ -114,8 +114,13 @@ __device__ __forceinline__ float4 ff_add_c(float4 X, float2 d) {
 }
 
 // One CTA: C adjacent kx columns of one job over all ny rows.  Threads per CTA
-// = 2 C ny/16, so every thread combines exactly min(8, ny/2) elements.
-__global__ void __launch_bounds__(512, 1) mcol_kernel(const __grid_constant__ MColArgs a) {
+// = 2 C ny/16, so every thread combines exactly min(8, ny/2) elements.  The state
+// operands are read in the combine loop rather than held across the forward
+// transform: 64 registers, so four 256-thread CTAs share an SM and hide each
+// other's load latency (the column passes are latency-bound at 1024^2, where the
+// whole working set sits in L2).  Only ny = 4096 needs 512-thread CTAs.
+template <int NT, int MINB>
+__global__ void __launch_bounds__(NT, MINB) mcol_kernel(const __grid_constant__ MColArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float2* buf = reinterpret_cast<float2*>(smem_raw);
   const DevState* st = a.st;
@@ -131,22 +136,6 @@ __global__ void __launch_bounds__(512, 1) mcol_kernel(const __grid_constant__ MC
   const float hA = (float)(0.5 * h * jb.D), hB = (float)(0.25 * h * jb.D);
   const float nrm = a.inv_norm;
   const int type = jb.type;
-
-  // State operands of this thread's elements, loaded first so that their
-  // latency overlaps the forward transform below.
-  float4 P[8], Q[8];
-#pragma unroll
-  for (int m = 0; m < 8; ++m) {
-    const int e = tid + m * nth;
-    const int ky = e / Cn, c = e - ky * Cn, kx = kx0 + c;
-    if (e < total && kx < a.ncols) {
-      const long long g = jb.off + ky * ldc + kx;
-      if (type == MC_SPLIT) P[m] = a.ys[cur][g];
-      else if (type == MC_FULL_END) P[m] = a.pa[g];
-      else P[m] = a.pb[g];
-      if (type == MC_HALF_END) Q[m] = a.pa[g];
-    }
-  }
 
   if (type != MC_SPLIT) {
     // load the FP32 increment tile and transform it forward along y
@@ -181,8 +170,13 @@ __global__ void __launch_bounds__(512, 1) mcol_kernel(const __grid_constant__ MC
     }
     const long long g = jb.off + ky * ldc + kx;
     const float lam = a.lamx[kx] + a.lamy[ky];
+    float4 Pm, Qm;
+    if (type == MC_SPLIT) Pm = a.ys[cur][g];
+    else if (type == MC_FULL_END) Pm = a.pa[g];
+    else Pm = a.pb[g];
+    if (type == MC_HALF_END) Qm = a.pa[g];
     if (type == MC_SPLIT) {
-      const float4 PA = ff_mstep_c(P[m], mu_of(hA, lam)), PB = ff_mstep_c(P[m], mu_of(hB, lam));
+      const float4 PA = ff_mstep_c(Pm, mu_of(hA, lam)), PB = ff_mstep_c(Pm, mu_of(hB, lam));
       a.pa[g] = PA;
       a.pb[g] = PB;
       buf[sp(ky * W + c)] = fmk(ff_scaled(ff_re(PA), nrm), ff_scaled(ff_im(PA), nrm));
@@ -190,16 +184,16 @@ __global__ void __launch_bounds__(512, 1) mcol_kernel(const __grid_constant__ MC
     } else {
       const float2 d = buf[sp(ky * W + c)];
       if (type == MC_FULL_END) {
-        a.pa[g] = ff_mstep_c(ff_add_c(P[m], d), mu_of(hA, lam));
+        a.pa[g] = ff_mstep_c(ff_add_c(Pm, d), mu_of(hA, lam));
       } else if (type == MC_HALF_MID) {
         const float mu = mu_of(hB, lam);
-        const float4 X = ff_mstep_c(ff_mstep_c(ff_add_c(P[m], d), mu), mu);
+        const float4 X = ff_mstep_c(ff_mstep_c(ff_add_c(Pm, d), mu), mu);
         a.pb[g] = X;
         buf[sp(ky * W + c)] = fmk(ff_scaled(ff_re(X), nrm), ff_scaled(ff_im(X), nrm));
       } else {  // MC_HALF_END
-        const float4 X = ff_mstep_c(ff_add_c(P[m], d), mu_of(hB, lam));
+        const float4 X = ff_mstep_c(ff_add_c(Pm, d), mu_of(hB, lam));
         a.ys[1 - cur][g] = X;
-        const float4 Fa = Q[m];
+        const float4 Fa = Qm;
         buf[sp(ky * W + c)] = fmk(ff_diff_scaled(ff_re(X), ff_re(Fa), nrm),
                                   ff_diff_scaled(ff_im(X), ff_im(Fa), nrm));
         buf[sp(ky * W + Cn + c)] = fmk(ff_scaled(ff_re(X), nrm), ff_scaled(ff_im(X), nrm));
@@ -364,7 +358,9 @@ static MixAttempt build_mix(const void* plan32, const mjx_grid2d* g, const mjx_i
 static cudaError_t mcol(const MColArgs& c, size_t smem, cudaStream_t s) {
   const int tps = c.ny >= 16 ? c.ny / 16 : 1;
   dim3 grid((c.ncols + c.C - 1) / c.C, c.njobs);
-  mcol_kernel<<<grid, 2 * c.C * tps, smem, s>>>(c);
+  const int nt = 2 * c.C * tps;
+  if (nt <= 256) mcol_kernel<256, 4><<<grid, nt, smem, s>>>(c);
+  else mcol_kernel<512, 1><<<grid, nt, smem, s>>>(c);
   return cudaGetLastError();
 }
 
@@ -372,6 +368,9 @@ static cudaError_t mrow(const RowArgs<float>& r, int rx, cudaStream_t s) {
   return rx == RX_GRAY_SCOTT ? launch_row<float, RX_GRAY_SCOTT>(r, s)
          : (rx == RX_FISHER ? launch_row<float, RX_FISHER>(r, s) : launch_row<float, RX_NONE>(r, s));
 }
+
+// attempts per iteration of the conditional while node
+static constexpr int kCondUnroll = 4;
 
 static cudaError_t launch_mix_attempt(const MixAttempt& A, cudaStream_t s) {
   cudaError_t e;
@@ -449,7 +448,8 @@ mjx_status ensure_mix_attrs() {
   int dev = 0, optin = 0;
   MJX_CUDA_TRY(cudaGetDevice(&dev));
   MJX_CUDA_TRY(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-  MJX_CUDA_TRY(cudaFuncSetAttribute(mcol_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
+  MJX_CUDA_TRY(cudaFuncSetAttribute(mcol_kernel<256, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
+  MJX_CUDA_TRY(cudaFuncSetAttribute(mcol_kernel<512, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
   done = 1;
   return MJX_OK;
 }
@@ -597,8 +597,14 @@ mjx_status mjx_imex_adaptive2d_mixed(const void* plan32, const void* plan64, con
       cudaGraph_t body = np.conditional.phGraph_out[0];
       if ((ce = cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) break;
       ca.handle = hdl; ca.use_handle = 1;
-      cudaError_t le = launch_mix_attempt(A, cs);
-      if (le == cudaSuccess) le = launch_controller(ca, cs);
+      // the body holds kCondUnroll attempts (each followed by the controller), so the
+      // conditional node is evaluated once per kCondUnroll attempts; once the
+      // controller marks the solve done, the rest of the body's kernels return at entry
+      cudaError_t le = cudaSuccess;
+      for (int u = 0; u < kCondUnroll && le == cudaSuccess; ++u) {
+        le = launch_mix_attempt(A, cs);
+        if (le == cudaSuccess) le = launch_controller(ca, cs);
+      }
       cudaGraph_t captured = nullptr;
       ce = cudaStreamEndCapture(cs, &captured);
       if (le != cudaSuccess) { ce = le; break; }
