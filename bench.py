@@ -396,11 +396,11 @@ def run_ours(args, rank, world, local):
                          "peak_kind": f"of {peak_kind}", "unit": "GB/s", "frac": achieved / peak,
                          "traffic": traffic, "alg_bytes": kb[dom],
                          "kernel_us": {k: v * 1e6 for k, v in ktimes.items()}},
-            # mixed: the graph body holds 4 attempts (6 kernels + controller each), so a solve
-            # launches its attempts rounded up to a multiple of 4 (the surplus kernels return at
-            # entry) plus 9 conversion kernels; FP32: 8 per attempt plus 3
-            "gpu_launches": (args.steps * (-(-(attempts // args.steps) // 4) * 4 * 7 + 9) if P == "mixed"
-                             else attempts * 8 + args.steps * 3),
+            # the graph body holds 4 attempts (mixed: 6 kernels + controller each; FP32: 7 + 1),
+            # so a solve launches its attempts rounded up to a multiple of 4 (the surplus
+            # kernels return at entry) plus its conversion kernels (mixed 9, FP32 3)
+            "gpu_launches": args.steps * (-(-(attempts // args.steps) // 4) * 4 * (7 if P == "mixed" else 8)
+                                          + (9 if P == "mixed" else 3)),
             "clocks": clk,
             "wall_s": wall,
         }

@@ -162,6 +162,9 @@ __global__ void __launch_bounds__(256) controller_kernel(CtlArgs a) {
   if (a.use_handle) cudaGraphSetConditional(a.handle, running ? 1u : 0u);
 }
 
+// attempts per iteration of the conditional while node of the adaptive loops
+static constexpr int kCondUnroll = 4;
+
 bool host_loop_mode() {
   static const int mode = [] {
     const char* v = getenv("MJX_HOST_LOOP");
@@ -475,14 +478,20 @@ static mjx_status adaptive_run(const void* plan, const mjx_grid2d* g, const mjx_
       cudaGraph_t body = np.conditional.phGraph_out[0];
       { const cudaError_t _e = cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal); if (_e != cudaSuccess) { set_last_error(_e, __FILE__, __LINE__); rc = MJX_CUDA_ERROR; break; } }
       ca.handle = hdl; ca.use_handle = 1;
-      cudaError_t le = launch_attempt<T>(A, cs);
-      if (le == cudaSuccess) {
-        controller_kernel<<<1, 256, 0, cs>>>(ca);
-        le = cudaGetLastError();
-      }
-      if (le == cudaSuccess && hist_y) {
-        hist_copy_kernel<T><<<304, 256, 0, cs>>>(st, (const T*)(ws + L.y0), (const T*)(ws + L.y1), hist_y, nelem);
-        le = cudaGetLastError();
+      // kCondUnroll attempts per iteration of the while node; after the controller
+      // marks the solve done the remaining kernels of the body return at entry (a
+      // repeated history copy rewrites the same slot with the same state)
+      cudaError_t le = cudaSuccess;
+      for (int u = 0; u < kCondUnroll && le == cudaSuccess; ++u) {
+        le = launch_attempt<T>(A, cs);
+        if (le == cudaSuccess) {
+          controller_kernel<<<1, 256, 0, cs>>>(ca);
+          le = cudaGetLastError();
+        }
+        if (le == cudaSuccess && hist_y) {
+          hist_copy_kernel<T><<<304, 256, 0, cs>>>(st, (const T*)(ws + L.y0), (const T*)(ws + L.y1), hist_y, nelem);
+          le = cudaGetLastError();
+        }
       }
       cudaGraph_t captured = nullptr;
       const cudaError_t ce = cudaStreamEndCapture(cs, &captured);
