@@ -273,11 +273,16 @@ static MixLayout mix_layout(int ny, int nx, int nf, int nparts) {
 
 static int mix_nparts(int ny, int nx, int nf) { return row_ctas(nx, ny, nf); }
 
+// thread caps of the C1 / C2 / C3 column tiles: 512 -> four columns per CTA at 1024 rows
+// (whole 32-byte sectors of the FP32 tile; two 64-register CTAs per SM), 256 -> two columns
+// (four CTAs per SM).  Measured at 1024^2: 881 ms per solve with 512 for all three passes,
+// 901 ms with 256; mixed choices in between.
+static constexpr int kColCap[3] = {512, 512, 512};
+
 struct MixAttempt {
   MColArgs c1, c2, c3;
   RowArgs<float> r1, r2, r3;
   int rx;
-  size_t csmem;
 };
 
 static MixAttempt build_mix(const void* plan32, const mjx_grid2d* g, const mjx_imex_problem* pb,
@@ -290,19 +295,22 @@ static MixAttempt build_mix(const void* plan32, const mjx_grid2d* g, const mjx_i
   memset(&c, 0, sizeof(c));
   c.ny = g->ny; c.log2ny = ilog2_exact(g->ny); c.ncols = g->nx / 2 + 1; c.ldc = ldc;
   const int tps = g->ny >= 16 ? g->ny / 16 : 1;
-  int C = 256 / tps;
-  if (C < 1) C = 1;
-  if (C > 8) C = 8;
-  while (C > 1 && (2 * C * tps > 256 || (size_t)sp_size(g->ny * 2 * C) * 8 > 200 * 1024)) C >>= 1;
-  c.C = C;
+  // column tile width: the widest C with 2 C ny/16 <= cap threads and <= 200 KB of smem
+  auto tile = [&](int cap) {
+    int C = 8;
+    while (C > 1 && (2 * C * tps > cap || (size_t)sp_size(g->ny * 2 * C) * 8 > 200 * 1024)) C >>= 1;
+    return C;
+  };
+  c.C = tile(kColCap[1]);
   c.ys[0] = (float4*)(ws + L.ys0); c.ys[1] = (float4*)(ws + L.ys1);
   c.pa = (float4*)(ws + L.pa); c.pb = (float4*)(ws + L.pb);
   c.za = (float2*)(ws + L.za); c.zb = (float2*)(ws + L.zb);
   c.lamx = (const float*)pv.lamx; c.lamy = (const float*)pv.lamy; c.tw = (const float2*)pv.twy;
   c.inv_norm = (float)(1.0 / ((double)g->nx * (double)g->ny));
   c.st = st;
-  A.csmem = (size_t)sp_size(g->ny * 2 * C) * sizeof(float2);
   A.c1 = c; A.c2 = c; A.c3 = c;
+  A.c1.C = tile(kColCap[0]);
+  A.c3.C = tile(kColCap[2]);
   for (int f = 0; f < nf; ++f) {
     const double D = pb->D[f] > 1e-14 ? pb->D[f] : 0.0;
     MJob j;
@@ -355,12 +363,13 @@ static MixAttempt build_mix(const void* plan32, const mjx_grid2d* g, const mjx_i
   return A;
 }
 
-static cudaError_t mcol(const MColArgs& c, size_t smem, cudaStream_t s) {
+static cudaError_t mcol(const MColArgs& c, cudaStream_t s) {
   const int tps = c.ny >= 16 ? c.ny / 16 : 1;
+  const size_t smem = (size_t)sp_size(c.ny * 2 * c.C) * sizeof(float2);
   dim3 grid((c.ncols + c.C - 1) / c.C, c.njobs);
   const int nt = 2 * c.C * tps;
   if (nt <= 256) mcol_kernel<256, 4><<<grid, nt, smem, s>>>(c);
-  else mcol_kernel<512, 1><<<grid, nt, smem, s>>>(c);
+  else mcol_kernel<512, 2><<<grid, nt, smem, s>>>(c);
   return cudaGetLastError();
 }
 
@@ -374,11 +383,11 @@ static constexpr int kCondUnroll = 4;
 
 static cudaError_t launch_mix_attempt(const MixAttempt& A, cudaStream_t s) {
   cudaError_t e;
-  if ((e = mcol(A.c1, A.csmem, s)) != cudaSuccess) return e;
+  if ((e = mcol(A.c1, s)) != cudaSuccess) return e;
   if ((e = mrow(A.r1, A.rx, s)) != cudaSuccess) return e;
-  if ((e = mcol(A.c2, A.csmem, s)) != cudaSuccess) return e;
+  if ((e = mcol(A.c2, s)) != cudaSuccess) return e;
   if ((e = mrow(A.r2, A.rx, s)) != cudaSuccess) return e;
-  if ((e = mcol(A.c3, A.csmem, s)) != cudaSuccess) return e;
+  if ((e = mcol(A.c3, s)) != cudaSuccess) return e;
   return mrow(A.r3, RX_NONE, s);
 }
 
@@ -449,7 +458,7 @@ mjx_status ensure_mix_attrs() {
   MJX_CUDA_TRY(cudaGetDevice(&dev));
   MJX_CUDA_TRY(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
   MJX_CUDA_TRY(cudaFuncSetAttribute(mcol_kernel<256, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
-  MJX_CUDA_TRY(cudaFuncSetAttribute(mcol_kernel<512, 1>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
+  MJX_CUDA_TRY(cudaFuncSetAttribute(mcol_kernel<512, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
   done = 1;
   return MJX_OK;
 }
@@ -496,11 +505,11 @@ mjx_status mjx_imex_mixed_attempt_kernel2d(const void* plan32, const void* plan6
   const MixAttempt A = build_mix(plan32, g, pb, pid, w, L, st);
   cudaError_t e;
   switch (which) {
-    case 1: e = mcol(A.c1, A.csmem, s); break;
+    case 1: e = mcol(A.c1, s); break;
     case 2: e = mrow(A.r1, A.rx, s); break;
-    case 3: e = mcol(A.c2, A.csmem, s); break;
+    case 3: e = mcol(A.c2, s); break;
     case 4: e = mrow(A.r2, A.rx, s); break;
-    case 5: e = mcol(A.c3, A.csmem, s); break;
+    case 5: e = mcol(A.c3, s); break;
     case 6: e = mrow(A.r3, RX_NONE, s); break;
     default: return MJX_BAD_ARG;
   }
