@@ -61,3 +61,23 @@ def test_etdrk4_fourth_order(cuda):
     for dt, n_st in ((2.0, 4), (1.0, 8)):
         errs.append(np.linalg.norm(M.etdrk4_gray_scott(model, ym, dt, n_st)["u"].cpu().numpy() - ref))
     assert errs[0] / errs[1] > 8.0
+
+
+@pytest.mark.parametrize("ny,nx", [(4096, 16), (16, 4096)])
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+def test_etdrk4_maximum_extent(cuda, ny, nx, dtype):
+    # 4096-point transforms along each axis (the widest column tiles and the 256-thread rows)
+    import moljax_gb300 as M
+    L = 2.5
+    grid = M.Grid2D(nx, ny, 0.0, L, 0.0, L)
+    model = M.create_gray_scott_model(grid, 2e-5, 1e-5, 0.035, 0.065, dtype=dtype)
+    og = mol.Grid2D(nx, ny, 0, L, 0, L)
+    y0 = mol.gray_scott_ic(og, 23)
+    ym = {k: torch.tensor(v, dtype=dtype, device=cuda) for k, v in y0.items()}
+    out = M.etdrk4_gray_scott(model, ym, 0.5, 6)
+    lam = mol.fd_symbol_2d(ny, nx, og.dy, og.dx)
+    ru, rv = OE.etdrk4_gray_scott(mol.interior(y0["u"], og), mol.interior(y0["v"], og), lam,
+                                  2e-5, 1e-5, 0.035, 0.065, 0.5, 6, 2.0)
+    tol = 1e-11 if dtype == torch.float64 else 3e-6
+    assert _rel(mol.interior(out["u"].cpu().numpy(), og), ru) < tol
+    assert _rel(mol.interior(out["v"].cpu().numpy(), og), rv) < tol

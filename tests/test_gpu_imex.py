@@ -234,3 +234,32 @@ def test_history_streamed_to_host_equals_device_history(cuda):
     k = rd.n_steps
     for f in ("u", "v"):
         np.testing.assert_array_equal(rh.y_history[f][:k].numpy(), rd.y_history[f][:k].cpu().numpy())
+
+
+@pytest.mark.parametrize("ny,nx", [(4096, 32), (32, 4096)])
+def test_adaptive_mixed_maximum_extent(cuda, ny, nx):
+    # the largest transform length (4096) along each axis: one-column 512-thread column
+    # tiles (ny = 4096) and 4096-point row transforms (nx = 4096)
+    import moljax_gb300 as M
+    L = 2.5
+    grid = M.Grid2D(nx, ny, 0.0, L, 0.0, L)
+    model, cache, diff = M.create_gray_scott_periodic_fft(grid, 2e-5, 1e-5, 0.035, 0.065, torch.float32, cuda)
+    og = mol.Grid2D(nx, ny, 0, L, 0, L)
+    y0 = mol.gray_scott_ic(og, 17)
+    ym = {k: torch.tensor(v, dtype=torch.float32, device=cuda) for k, v in y0.items()}
+    om, lam, od = OI.gray_scott_periodic(og, 2e-5, 1e-5, 0.035, 0.065)
+    pid = M.PIDParams(atol=1e-7, rtol=1e-5)
+    r = M.adaptive_integrate_imex(model, ym, 0.0, 12.0, 1.0, cache, diff, pid_params=pid,
+                                  save_every=100, save_y_history=False, precision="mixed")
+    ro = OI.adaptive_integrate_imex(om, y0, 0.0, 12.0, 1.0, lam, od,
+                                    pid=OI.PIDParams(atol=1e-7, rtol=1e-5), save_every=100,
+                                    keep_history=False)
+    assert r.status == ro.status == 0
+    assert (r.n_accepted, r.n_rejected) == (ro.n_accepted, ro.n_rejected)
+    for k in ("u", "v"):
+        assert _rel(r.y_final[k].cpu().numpy(), ro.y_final[k]) < 1e-6
+    rf = M.adaptive_integrate_imex(model, ym, 0.0, 12.0, 1.0, cache, diff, pid_params=pid,
+                                   save_every=100, save_y_history=False, precision="fp32")
+    assert rf.status == 0
+    for k in ("u", "v"):
+        assert _rel(rf.y_final[k].cpu().numpy(), ro.y_final[k]) < 1e-4
