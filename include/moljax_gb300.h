@@ -139,6 +139,24 @@ mjx_status mjx_advdiff_apply2d(const void* plan, const mjx_grid2d* grid, int dty
                                const double* D, const double* vx, const double* vy, double h,
                                const void* in, void* out, void* ws, size_t ws_bytes, void* stream);
 
+/* The periodic advection-diffusion operator L = D Lap - v.grad with the symbol
+ * D lam - i (vx kx + vy ky) (kx, ky = 2 pi fftfreq): op 0 solves (I - h L) u = in
+ * (as mjx_advdiff_apply2d), op 1 applies h L, op 2 applies exp(h L); out = the real part
+ * (AdvectionDiffusionOperator, moljax/core/fft_operators.py:179-260: solve, matvec with
+ * h = 1, exp_matvec).  Fields with D <= 1e-14 and |v| <= 1e-14 are copied (ops 0, 2)
+ * or zeroed (op 1). */
+mjx_status mjx_advdiff_op2d(const void* plan, const mjx_grid2d* grid, int dtype, int nfields,
+                            const double* D, const double* vx, const double* vy, double h, int op,
+                            const void* in, void* out, void* ws, size_t ws_bytes, void* stream);
+
+/* out_f = real(IFFT2( sigma * FFT2(in_f) )) with sigma a real multiplier per point of the
+ * half spectrum: table [ny][ldc] (ldc = nx/2+1 rounded up to a multiple of 4), the
+ * Hermitian part (K(k) + K(-k))/2 of a full-spectrum kernel K
+ * (apply_spectral_filter_interior, moljax/core/fft_solvers.py:534-556). */
+mjx_status mjx_spectral_filter2d(const void* plan, const mjx_grid2d* grid, int dtype, int nfields,
+                                 const void* table, const void* in, void* out, void* ws, size_t ws_bytes,
+                                 void* stream);
+
 /* n_steps Crank-Nicolson steps u <- real(IFFT2(G * FFT2(u))) executed one by one;
  * G = (1 + dt D lam/2)/(1 - dt D lam/2).  Replaces the benchmark FFT-CN step
  * (benchmarks/benchmark_vs_scipy.py:74-91) behind fft_solvers.fft_cn_step. */

@@ -17,13 +17,21 @@ from moljax_gb300.core.dt_policy import CFLParams, PIDParams
 from moljax_gb300.core.fft_solvers import (create_fft_cache, solve_helmholtz_2d,
                                            apply_diffusion_inverse_fft, fft_cn_step,
                                            laplacian_symbol_2d, fft_cn_step_3d, solve_helmholtz_3d,
-                                           get_plan3d)
+                                           get_plan3d, solve_diffusion_fft_field, apply_diffusion_fft,
+                                           diffusion_rhs_fft, exponential_filter_1d,
+                                           exponential_filter_2d, apply_spectral_filter_interior,
+                                           apply_spectral_filter_field, apply_spectral_filter_state,
+                                           create_fft_cache_1d, solve_helmholtz_1d,
+                                           build_wavenumbers_2d)
 from moljax_gb300.core.utils import StatusCode
 from moljax_gb300.core import fft_integrators, fft_operators
 from moljax_gb300.core.fft_integrators import (etdrk4_gray_scott, etdrk4_step, etd_integrate, etd1_step,
                                                etd2_step, diffusion_only_etd1, NativeNonlinear,
-                                               etd_integrate_model, etd_adaptive_integrate)
-from moljax_gb300.core.fft_operators import DiffusionOperator
+                                               etd_integrate_model, etd_adaptive_integrate,
+                                               batched_fft_matvec, batched_fft_solve,
+                                               batched_fft_exp_matvec, stacked_fft_solve_shared_op)
+from moljax_gb300.core.fft_operators import (DiffusionOperator, AdvectionDiffusionOperator,
+                                              SpectralBounds, exact_cfl_dt)
 from moljax_gb300.core import newton_krylov, preconditioners
 from moljax_gb300.core.newton_krylov import (NKParams, NKStats, newton_krylov_solve,
                                              integrate_implicit_vardiff)

@@ -246,6 +246,53 @@ def etd_integrate(u0, t_span, dt: float, linear_ops, nonlinear_rhs, method: str 
     return torch.tensor(t_hist, dtype=torch.float64), hist
 
 
+def batched_fft_matvec(state, linear_ops):
+    """L u per field; zeros without an operator (fft_integrators.py:400-420)."""
+    return {n: (linear_ops[n].matvec(u) if n in linear_ops else torch.zeros_like(u)) for n, u in state.items()}
+
+
+def batched_fft_solve(rhs, linear_ops, dt: float):
+    """(I - dt L)^-1 per field; unchanged without an operator (fft_integrators.py:423-445)."""
+    return {n: (linear_ops[n].solve(u, dt) if n in linear_ops else u) for n, u in rhs.items()}
+
+
+def batched_fft_exp_matvec(state, linear_ops, dt: float):
+    """exp(dt L) u per field; unchanged without an operator (fft_integrators.py:448-470)."""
+    return {n: (linear_ops[n].exp_matvec(u, dt) if n in linear_ops else u) for n, u in state.items()}
+
+
+def stacked_fft_solve_shared_op(rhs, op, dt: float):
+    """(I - dt L)^-1 for every field with one shared operator (fft_integrators.py:473-510);
+    a shared DiffusionOperator runs all fields through one native pass (four per launch)."""
+    from moljax_gb300.core.fft_operators import DiffusionOperator
+    names = list(rhs.keys())
+    if not names:
+        return {}
+    if not isinstance(op, DiffusionOperator):
+        return {n: op.solve(rhs[n], dt) for n in names}
+    x = torch.stack([rhs[n] for n in names]).contiguous()
+    plan = op._plan(x.dtype)
+    if op.is_1d:
+        from moljax_gb300.core.fft_solvers import _apply_1d
+        y = _apply_1d(plan, x, op.D, dt, N.MULT_HELMHOLTZ)
+    else:
+        y = plan.apply(x, op.D, dt, N.MULT_HELMHOLTZ)
+    return {n: y[i] for i, n in enumerate(names)}
+
+
+def imex_euler_step(state, t: float, dt: float, linear_ops, nonlinear_rhs, model=None):
+    """(I - dt L) u_{n+1} = u_n + dt N(u_n) (fft_integrators.py:545-585): N by the native
+    row pass, the solve by the operator's spectral pass; without an operator, explicit
+    Euler."""
+    nl = NativeNonlinear.of(model if model is not None else nonlinear_rhs)
+    Nn = nl(state, t)
+    out = {}
+    for n, u in state.items():
+        r = u + dt * Nn[n]
+        out[n] = linear_ops[n].solve(r, dt) if n in linear_ops else r
+    return out
+
+
 def diffusion_only_etd1(u0: torch.Tensor, t_end: float, dt: float, op) -> torch.Tensor:
     """fft_integrators.py:513-542: max(1, int(t_end/dt)) steps of exp(h L), h = t_end/n."""
     n = max(1, int(t_end / dt))

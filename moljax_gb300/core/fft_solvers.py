@@ -151,10 +151,38 @@ def create_fft_cache_2d(grid: Grid2D, dtype=torch.float64, device=None) -> FFTCa
     return FFTCache2D(lam, kx, ky, lam._mjx_plan)
 
 
+def build_wavenumbers_2d(ny: int, nx: int, dy: float, dx: float, dtype=torch.float64):
+    """moljax/core/fft_solvers.py:67-94: (kx, ky), each (ny, nx), 2 pi fftfreq."""
+    kx = build_wavenumbers_1d(nx, dx, dtype)[None, :].expand(ny, nx).contiguous()
+    ky = build_wavenumbers_1d(ny, dy, dtype)[:, None].expand(ny, nx).contiguous()
+    return kx, ky
+
+
+class FFTCache1D(NamedTuple):
+    """moljax/core/fft_solvers.py:31-35 plus the native plan (a 2-row grid whose rows
+    carry the same field, so that its y modes are zero)."""
+    laplacian_symbol: torch.Tensor
+    k: torch.Tensor
+    plan: SpectralPlan
+
+
+def _plan_1d(nx: int, dx: float, dtype, device=None) -> SpectralPlan:
+    return get_plan(2, nx, dx, dx, "fd", dtype, device)
+
+
+def create_fft_cache_1d(grid: Grid1D, dtype=torch.float64, device=None) -> FFTCache1D:
+    """moljax/core/fft_solvers.py:161-178."""
+    dev = _device(device)
+    lam = laplacian_symbol_1d(grid.nx, grid.dx, dtype).to(dev)
+    plan = _plan_1d(grid.nx, grid.dx, dtype, dev)
+    lam._mjx_plan = plan
+    return FFTCache1D(lam, build_wavenumbers_1d(grid.nx, grid.dx, dtype).to(dev), plan)
+
+
 def create_fft_cache(grid, dtype=torch.float64, device=None):
-    """moljax/core/fft_solvers.py:201-215 (2D grids)."""
+    """moljax/core/fft_solvers.py:201-215."""
     if isinstance(grid, Grid1D):
-        raise NotImplementedError("1D periodic FFT cache: use Grid2D (1D spectral path not built)")
+        return create_fft_cache_1d(grid, dtype, device)
     return create_fft_cache_2d(grid, dtype, device)
 
 
@@ -172,6 +200,25 @@ def _plan_of(laplacian_symbol_or_cache, ny, nx, dtype):
     return plan
 
 
+def _apply_1d(plan: SpectralPlan, u: torch.Tensor, D, h: float, mult: int) -> torch.Tensor:
+    """A multiplier on 1D fields (..., nx) through the 2-row plan (both rows the same field)."""
+    u2 = u.reshape(-1, 1, u.shape[-1]).expand(-1, 2, -1).contiguous()
+    return plan.apply(u2, D, h, mult)[:, 0].reshape(u.shape).clone()
+
+
+def solve_helmholtz_1d(rhs_interior: torch.Tensor, laplacian_symbol, dt: float, D: float):
+    """(I - dt D Lap) u = rhs on a periodic 1D interior (moljax/core/fft_solvers.py:222-258)."""
+    nx = rhs_interior.shape[-1]
+    plan = getattr(laplacian_symbol, "plan", None) or getattr(laplacian_symbol, "_mjx_plan", None)
+    if plan is None:
+        raise NotImplementedError("solve_helmholtz_1d needs a symbol made by create_fft_cache_1d")
+    if plan.nx != nx or plan.ny != 2:
+        raise ValueError("symbol/grid shape mismatch")
+    if plan.dtype != rhs_interior.dtype:
+        plan = get_plan(2, nx, plan.dy, plan.dx, plan.symbol, rhs_interior.dtype, plan.device)
+    return _apply_1d(plan, rhs_interior, D, dt, N.MULT_HELMHOLTZ)
+
+
 def solve_helmholtz_2d(rhs_interior: torch.Tensor, laplacian_symbol, dt: float, D: float):
     """(I - dt D Lap) u = rhs on the interior (moljax/core/fft_solvers.py:261-294)."""
     ny, nx = rhs_interior.shape[-2:]
@@ -180,9 +227,9 @@ def solve_helmholtz_2d(rhs_interior: torch.Tensor, laplacian_symbol, dt: float, 
 
 
 def solve_helmholtz(rhs_interior, laplacian_symbol, dt, D):
-    """moljax/core/fft_solvers.py:297-320 (2D)."""
-    if rhs_interior.ndim != 2:
-        raise NotImplementedError("1D Helmholtz: use a 2D grid")
+    """moljax/core/fft_solvers.py:297-320."""
+    if rhs_interior.ndim == 1:
+        return solve_helmholtz_1d(rhs_interior, laplacian_symbol, dt, D)
     return solve_helmholtz_2d(rhs_interior, laplacian_symbol, dt, D)
 
 
@@ -196,6 +243,12 @@ def embed_interior(u_interior, grid, padded_template):
     out = padded_template.clone()
     out[grid.interior_slice] = u_interior
     return out
+
+
+def solve_diffusion_fft_field(rhs_padded, grid, dt: float, D: float, fft_cache):
+    """(I - dt D Lap) u = rhs for one padded field; ghosts from rhs (fft_solvers.py:368-403)."""
+    u = solve_helmholtz(extract_interior(rhs_padded, grid).contiguous(), fft_cache.laplacian_symbol, dt, D)
+    return embed_interior(u, grid, rhs_padded)
 
 
 def apply_diffusion_inverse_fft(state_rhs, grid: Grid2D, dt: float, diffusivities, fft_cache):
@@ -212,6 +265,97 @@ def apply_diffusion_inverse_fft(state_rhs, grid: Grid2D, dt: float, diffusivitie
     for i, n in enumerate(names):
         out[n] = embed_interior(res[i], grid, state_rhs[n])
     return out
+
+
+def apply_diffusion_fft(state, grid, dt: float, diffusivities, fft_cache):
+    """Implicit Euler diffusion step u <- (I - dt D Lap)^-1 u (fft_solvers.py:448-474)."""
+    if isinstance(grid, Grid1D):
+        return {n: (solve_diffusion_fft_field(f, grid, dt, diffusivities[n], fft_cache)
+                    if diffusivities.get(n, 0.0) > 1e-14 else f) for n, f in state.items()}
+    return apply_diffusion_inverse_fft(state, grid, dt, diffusivities, fft_cache)
+
+
+def diffusion_rhs_fft(state, grid, diffusivities, fft_cache):
+    """D Lap u of each field through the FFT symbol, ghosts zero (fft_solvers.py:619-660)."""
+    out = {}
+    for n, f in state.items():
+        D = diffusivities.get(n, 0.0)
+        if D > 1e-14:
+            fi = extract_interior(f, grid).contiguous()
+            if fi.ndim == 1:
+                lap = _apply_1d(_plan_of(fft_cache, 2, fi.shape[-1], fi.dtype), fi, D, 1.0, N.MULT_LAP)
+            else:
+                lap = _plan_of(fft_cache, fi.shape[0], fi.shape[1], fi.dtype).apply(fi, D, 1.0, N.MULT_LAP)
+            out[n] = embed_interior(lap, grid, torch.zeros_like(f))
+        else:
+            out[n] = torch.zeros_like(f)
+    return out
+
+
+# ----------------------------------------------------------------- spectral filters
+def exponential_filter_1d(nx: int, strength: float = 36.0, order: int = 36, dtype=torch.float64):
+    """sigma(k) = exp(-strength (|k|/k_max)^order), |k| = min(k, n - k) (fft_solvers.py:477-503)."""
+    k = torch.arange(nx, dtype=torch.float64)
+    kn = torch.minimum(k, nx - k) / (nx // 2)
+    kn = torch.clamp(kn, max=1.0)
+    return torch.exp(-strength * kn ** order).to(dtype)
+
+
+def exponential_filter_2d(ny: int, nx: int, strength: float = 36.0, order: int = 36, dtype=torch.float64):
+    """Outer product of the 1D filters (fft_solvers.py:506-531)."""
+    return torch.outer(exponential_filter_1d(ny, strength, order, dtype),
+                       exponential_filter_1d(nx, strength, order, dtype))
+
+
+def _half_table(kernel: torch.Tensor, ny: int, nx: int, dtype, device) -> torch.Tensor:
+    """The real multiplier on the half spectrum equivalent to real(ifft2(K fft2(u))):
+    (K(k) + K(-k)) / 2 for kx = 0..nx/2, padded to the plan's row length."""
+    K = kernel.to(torch.float64).cpu()
+    if K.is_complex():
+        raise NotImplementedError("complex filter kernels are not supported")
+    if K.ndim == 1:
+        K = K[None, :].expand(ny, nx)
+    iy = (-torch.arange(ny)) % ny
+    ix = (-torch.arange(nx)) % nx
+    Km = K[iy][:, ix]
+    half = 0.5 * (K + Km)[:, : nx // 2 + 1]
+    ldc = ((nx // 2 + 1) + 3) & ~3
+    tab = torch.zeros(ny, ldc, dtype=torch.float64)
+    tab[:, : nx // 2 + 1] = half
+    return tab.to(dtype).to(device).contiguous()
+
+
+def apply_spectral_filter_interior(u_interior: torch.Tensor, filter_kernel) -> torch.Tensor:
+    """real(ifft(sigma * fft(u))) on a 1D or 2D interior (fft_solvers.py:534-556)."""
+    u = u_interior.contiguous()
+    N.require_cuda(u)
+    if u.ndim == 1:
+        ny, nx = 2, u.shape[0]
+        x = torch.stack([u, u])
+    else:
+        ny, nx = u.shape
+        x = u
+    kern = filter_kernel if torch.is_tensor(filter_kernel) else torch.as_tensor(filter_kernel)
+    plan = get_plan(ny, nx, 1.0 / ny, 1.0 / nx, "fd", u.dtype, u.device)
+    tab = _half_table(kern, ny, nx, u.dtype, u.device)
+    out = torch.empty_like(x)
+    ws = workspace(plan.ws_bytes(1), plan.device)
+    N.check("mjx_spectral_filter2d", N.lib().mjx_spectral_filter2d(
+        N.ptr(plan.buf), C.byref(plan.cgrid), plan.code, 1, N.ptr(tab), N.ptr(x), N.ptr(out),
+        N.ptr(ws), ws.numel(), N.stream_ptr(plan.device)))
+    return out[0].clone() if u.ndim == 1 else out
+
+
+def apply_spectral_filter_field(f_padded, grid, filter_kernel):
+    """fft_solvers.py:559-581: filter the interior, ghosts kept."""
+    return embed_interior(apply_spectral_filter_interior(extract_interior(f_padded, grid), filter_kernel),
+                          grid, f_padded)
+
+
+def apply_spectral_filter_state(state, grid, filter_kernel, filter_fields=None):
+    """fft_solvers.py:584-616: fields with filter_fields[name] False (default True) pass through."""
+    return {n: (apply_spectral_filter_field(f, grid, filter_kernel)
+                if filter_fields is None or filter_fields.get(n, True) else f) for n, f in state.items()}
 
 
 def fft_cn_step(u0: torch.Tensor, D: float, dx: float, dt: float, n_steps: int = 1,

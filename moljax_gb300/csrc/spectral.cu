@@ -347,29 +347,49 @@ __global__ void __launch_bounds__(ColThreads<T>::v, 1) col_kernel(const __grid_c
     if (kx < a.ncols) lxy = a.ldc3 ? a.lamx[kx % a.ldc3] + a.lamy2[kx / a.ldc3] : a.lamx[kx];
     const T lam = lxy + a.lamy[ky];
     const C v = buf[sp(ky * W + c)];
-    if (jb.mul == MUL_ADVDIFF) {
-      // m(k) = 1/(1 - h (D lam - i (vx kx + vy ky))), |denominator| < 1e-14 -> 1e-14
-      // (FFTAdvectionDiffusionPreconditioner, moljax/core/preconditioners.py:297-420),
-      // kx, ky = 2 pi fftfreq (the Nyquist index negative).  The reference keeps
-      // real(ifft2(.)); on the half spectrum that is the multiplier (m(k) + conj(m(-k)))/2,
-      // which equals m(k) except on the Nyquist lines, where fftfreq breaks the oddness
-      // of the advection term.
+    if (jb.mul == MUL_ADVDIFF || jb.mul == MUL_ADV_LAP || jb.mul == MUL_ADV_EXP) {
+      // z = h (D lam - i (vx kx + vy ky)), kx, ky = 2 pi fftfreq (the Nyquist index
+      // negative); m = 1/(1 - z) with |1 - z| < 1e-14 -> 1e-14 (the solve of
+      // FFTAdvectionDiffusionPreconditioner, moljax/core/preconditioners.py:297-420, and of
+      // AdvectionDiffusionOperator, fft_operators.py:179-260), z itself (matvec) or exp(z)
+      // (exp_matvec).  The reference keeps real(ifft(.)); on the half spectrum that is the
+      // multiplier (m(k) + conj(m(-k)))/2, which equals m(k) except on the Nyquist lines,
+      // where fftfreq breaks the oddness of the advection term.
       const int nxl = 2 * (a.ncols - 1);
       const int mx = kx < nxl / 2 ? kx : kx - nxl, my = ky < ny / 2 ? ky : ky - ny;
       const int nmx = mx == -nxl / 2 ? mx : -mx, nmy = my == -ny / 2 ? my : -my;
       const double hh = h * jb.hfac[0];
-      const double dr0 = 1.0 - (double)hD0 * (double)lam;
+      const double zr = (double)hD0 * (double)lam;
       double mre = 0.0, mim = 0.0;
       for (int side = 0; side < 2; ++side) {
         const int qx = side ? nmx : mx, qy = side ? nmy : my;
-        double dr = dr0, di = hh * (jb.vx * a.kxs * qx + jb.vy * a.kys * qy);
-        if (sqrt(dr * dr + di * di) < 1e-14) { dr = 1e-14; di = 0.0; }
-        const double den = dr * dr + di * di;
-        mre += 0.5 * dr / den;
-        mim += side ? 0.5 * di / den : -0.5 * di / den;  // conj(m(-k)) on the second side
+        const double zi = -hh * (jb.vx * a.kxs * qx + jb.vy * a.kys * qy);
+        double fr, fi;
+        if (jb.mul == MUL_ADVDIFF) {
+          double dr = 1.0 - zr, di = -zi;
+          if (sqrt(dr * dr + di * di) < 1e-14) { dr = 1e-14; di = 0.0; }
+          const double den = dr * dr + di * di;
+          fr = dr / den;
+          fi = -di / den;
+        } else if (jb.mul == MUL_ADV_LAP) {
+          fr = zr;
+          fi = zi;
+        } else {
+          double sn, cs;
+          sincos(zi, &sn, &cs);
+          const double ez = exp(zr);
+          fr = ez * cs;
+          fi = ez * sn;
+        }
+        mre += 0.5 * fr;
+        mim += side ? -0.5 * fi : 0.5 * fi;  // conj(m(-k)) on the second side
       }
       const T mr = (T)mre, mi = (T)mim;
       buf[sp(ky * W + c)] = cscale(mk<C>(v.x * mr - v.y * mi, v.x * mi + v.y * mr), jscale);
+      continue;
+    }
+    if (jb.mul == MUL_TABLE) {
+      buf[sp(ky * W + c)] = cscale(v, jscale * a.mtab[(long long)ky * ldc + kx]);
       continue;
     }
     buf[sp(ky * W + c)] = cscale(v, jscale * multiplier<T>(jb.mul, hD0, lam, jb.pow[0]));
@@ -515,7 +535,8 @@ ColArgs<T> field_cols(const mjx_grid2d* g, const PlanView& pv, cx<T>* spec, int 
 template <typename T>
 mjx_status spectral_apply(const void* plan, const mjx_grid2d* g, int nfields, const double* D,
                           double h, int mult, const T* in, T* out, void* ws, cudaStream_t s,
-                          const double* vx = nullptr, const double* vy = nullptr) {
+                          const double* vx = nullptr, const double* vy = nullptr,
+                          const T* mtab = nullptr) {
   const PlanView pv = plan_view(plan, g->ny, g->nx, sizeof(T));
   cx<T>* spec = (cx<T>*)ws;
   const size_t fsz = (size_t)g->ny * g->nx;
@@ -523,8 +544,8 @@ mjx_status spectral_apply(const void* plan, const mjx_grid2d* g, int nfields, co
   auto moves = [&](int f) { return vx && vy && (fabs(vx[f]) > 1e-14 || fabs(vy[f]) > 1e-14); };
   int idx[4], nd = 0;
   for (int f = 0; f < nfields; ++f) {
-    if (D[f] > 1e-14 || moves(f)) idx[nd++] = f;
-    else if (mult == MUL_LAP)  // D Lap u = 0
+    if (mult == MUL_TABLE || D[f] > 1e-14 || moves(f)) idx[nd++] = f;
+    else if (mult == MUL_LAP || mult == MUL_ADV_LAP)  // L u = 0
       MJX_CUDA_TRY(cudaMemsetAsync(out + f * fsz, 0, fsz * sizeof(T), s));
     else if (in != out)
       MJX_CUDA_TRY(cudaMemcpyAsync(out + f * fsz, in + f * fsz, fsz * sizeof(T), cudaMemcpyDeviceToDevice, s));
@@ -540,7 +561,7 @@ mjx_status spectral_apply(const void* plan, const mjx_grid2d* g, int nfields, co
   for (int i = 0; i < nd; ++i) r.pr[i].flags = ROW_STORE_SPEC;
   MJX_CUDA_TRY((launch_row<T, RX_NONE>(r, s)));
   ColArgs<T> c = field_cols<T>(g, pv, spec, 1);
-  c.hfixed = h; c.njobs = nd;
+  c.hfixed = h; c.njobs = nd; c.mtab = mtab;
   c.kxs = 6.283185307179586476925286766559 / ((double)g->nx * g->dx);
   c.kys = 6.283185307179586476925286766559 / ((double)g->ny * g->dy);
   for (int i = 0; i < nd; ++i) {
@@ -702,6 +723,43 @@ mjx_status mjx_spectral_apply2d(const void* plan, const mjx_grid2d* g, int dtype
   cudaStream_t s = (cudaStream_t)stream;
   if (e == 4) return spectral_apply<float>(plan, g, nfields, D, h, mult, (const float*)in, (float*)out, ws, s);
   return spectral_apply<double>(plan, g, nfields, D, h, mult, (const double*)in, (double*)out, ws, s);
+}
+
+mjx_status mjx_advdiff_op2d(const void* plan, const mjx_grid2d* g, int dtype, int nfields,
+                            const double* D, const double* vx, const double* vy, double h, int op,
+                            const void* in, void* out, void* ws, size_t ws_bytes, void* stream) {
+  MJX_TRY(check_grid(g));
+  if (nfields < 1 || nfields > 4 || D == nullptr || vx == nullptr || vy == nullptr || plan == nullptr ||
+      in == nullptr || out == nullptr || op < 0 || op > 2)
+    return MJX_BAD_ARG;
+  const int e = elem_size(dtype);
+  if (!e) return MJX_BAD_DTYPE;
+  if (ws == nullptr || ws_bytes < mjx_spec2d_ws_bytes(g->ny, g->nx, nfields, dtype)) return MJX_WORKSPACE;
+  MJX_TRY(ensure_kernel_attrs());
+  cudaStream_t s = (cudaStream_t)stream;
+  const int mul = op == 0 ? MUL_ADVDIFF : (op == 1 ? MUL_ADV_LAP : MUL_ADV_EXP);
+  if (e == 4)
+    return spectral_apply<float>(plan, g, nfields, D, h, mul, (const float*)in, (float*)out, ws, s, vx, vy);
+  return spectral_apply<double>(plan, g, nfields, D, h, mul, (const double*)in, (double*)out, ws, s, vx, vy);
+}
+
+mjx_status mjx_spectral_filter2d(const void* plan, const mjx_grid2d* g, int dtype, int nfields,
+                                 const void* table, const void* in, void* out, void* ws, size_t ws_bytes,
+                                 void* stream) {
+  MJX_TRY(check_grid(g));
+  if (nfields < 1 || nfields > 4 || plan == nullptr || table == nullptr || in == nullptr || out == nullptr)
+    return MJX_BAD_ARG;
+  const int e = elem_size(dtype);
+  if (!e) return MJX_BAD_DTYPE;
+  if (ws == nullptr || ws_bytes < mjx_spec2d_ws_bytes(g->ny, g->nx, nfields, dtype)) return MJX_WORKSPACE;
+  MJX_TRY(ensure_kernel_attrs());
+  cudaStream_t s = (cudaStream_t)stream;
+  const double D[4] = {1.0, 1.0, 1.0, 1.0};
+  if (e == 4)
+    return spectral_apply<float>(plan, g, nfields, D, 1.0, MUL_TABLE, (const float*)in, (float*)out, ws, s,
+                                 nullptr, nullptr, (const float*)table);
+  return spectral_apply<double>(plan, g, nfields, D, 1.0, MUL_TABLE, (const double*)in, (double*)out, ws, s,
+                                nullptr, nullptr, (const double*)table);
 }
 
 mjx_status mjx_advdiff_apply2d(const void* plan, const mjx_grid2d* g, int dtype, int nfields,

@@ -77,7 +77,10 @@ template <typename T> struct RowArgs {
   RowPair pr[MJX_MAXPAIR];
 };
 
-enum { MUL_SCALE = 0, MUL_HELMHOLTZ = 1, MUL_CN = 2, MUL_EXP = 3, MUL_ADVDIFF = 4, MUL_LAP = 5 };
+enum { MUL_SCALE = 0, MUL_HELMHOLTZ = 1, MUL_CN = 2, MUL_EXP = 3, MUL_ADVDIFF = 4, MUL_LAP = 5,
+       MUL_ADV_LAP = 6,   // h (D lam - i v.k): the advection-diffusion operator itself
+       MUL_ADV_EXP = 7,   // exp(h (D lam - i v.k))
+       MUL_TABLE = 8 };   // a real multiplier per half-spectrum point (ColArgs::mtab)
 
 struct ColJob {
   long long sin;         // spectrum offset of the input column block (ky=0, kx=0)
@@ -108,6 +111,7 @@ template <typename T> struct ColArgs {
   int nplanes;
   int ldc3;
   const T* lamy2;
+  const T* mtab;         // MUL_TABLE: [ny][ldc] real multipliers
   ColJob job[MJX_MAXJOB];
 };
 
