@@ -209,9 +209,16 @@ mjx_status mjx_unpad2d(const void* padded, void* interior, int nfields, int ny, 
 mjx_status mjx_laplacian2d(const void* padded_in, void* padded_out, int nfields, int ny, int nx,
                            int n_ghost, const double* coef, int fill_bc, const int* kinds,
                            const double* values, double dy, double dx, int dtype, void* stream);
-/* 2D first derivative on padded fields, ghosts read as stored, output ghosts zero:
- * op 1 upwind along axis with scalar velocity v (d1_upwind_2d, operators.py:200-268),
- * op 2 central (d1_central_2d, 155-197); axis 0 = y, 1 = x; d = spacing along axis. */
+/* div(D grad u) with face-averaged D on the interior of one padded field, ghosts zero
+ * (apply_variable_diffusion_2d, moljax/core/variable_coeff.py:232-287).  D is padded like u,
+ * or interior-shaped [ny][nx] (d_interior = 1) and edge-extended.  out must not alias u. */
+mjx_status mjx_variable_diffusion2d(const void* u_padded, const void* D, int d_interior, void* out_padded,
+                                    int ny, int nx, int n_ghost, double dy, double dx, int dtype, void* stream);
+
+/* 2D one-axis differences on padded fields, ghosts read as stored, output ghosts zero:
+ * op 1 upwind first derivative along axis with scalar velocity v (d1_upwind_2d,
+ * operators.py:200-268), op 2 central first derivative (d1_central_2d, 155-197), op 3
+ * central second derivative (d2_central_2d, 271-308); axis 0 = y, 1 = x; d = spacing. */
 mjx_status mjx_stencil2d(const void* padded_in, void* padded_out, int nfields, int ny, int nx,
                         int n_ghost, int op, int axis, double v, double d, int dtype, void* stream);
 /* result[0] = sqrt(sum((err/(atol + rtol |y|))^2) / n) (scaled_error_norm, state.py:312-343),

@@ -51,3 +51,28 @@ from moljax_gb300.core.fft_nonperiodic import (dst_I_fast, idst_I_fast, laplacia
                                                solve_poisson_neumann, solve_helmholtz_neumann,
                                                etd1_neumann, check_compatibility_neumann,
                                                project_to_compatible)
+from moljax_gb300.core import state, variable_coeff
+from moljax_gb300.core.state import (tree_add, tree_sub, tree_scale, tree_axpy, tree_zeros_like,
+                                     tree_ones_like, tree_norm2, tree_norm_inf, tree_vdot,
+                                     flatten_to_vec, unflatten_from_vec, state_total_size,
+                                     state_interior_size, create_state_from_interior,
+                                     get_interior_state)
+from moljax_gb300.core.variable_coeff import apply_variable_diffusion_2d
+from moljax_gb300.core.operators import (d2_central_1d, d2_central_2d, d1_central_1d, op_sum,
+                                        state_zero_like, make_diffusion_op_1d, make_diffusion_op_2d,
+                                        make_advection_op_1d, make_advection_op_2d, make_reaction_op,
+                                        fd_laplacian_symbol_1d, fd_laplacian_symbol_2d,
+                                        gray_scott_reaction_op, fisher_kpp_reaction_op)
+from moljax_gb300.core.stepping import (AdaptiveState, estimate_error_doubling,
+                                        estimate_error_implicit, estimate_error_imex_doubling,
+                                        step_explicit, step_explicit_with_error)
+from moljax_gb300.core.newton_krylov import create_implicit_residual, create_bdf2_residual
+from moljax_gb300.core.preconditioners import (create_gray_scott_preconditioner,
+                                               create_advdiff_preconditioner,
+                                               create_diffusion_preconditioner,
+                                               create_fft_preconditioner,
+                                               create_gray_scott_fft_preconditioner,
+                                               create_advdiff_fft_preconditioner)
+from moljax_gb300.core.dt_policy import estimate_reaction_stiffness
+from moljax_gb300.core.fft_operators import FFTLinearOperator
+from moljax_gb300.core.fft_integrators import ETDStepResult

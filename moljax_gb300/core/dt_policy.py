@@ -192,3 +192,19 @@ def propose_dt(method: int, grid, params, state, t, dt_old, err_ratio,
     if nk_stats is not None and method >= 3:
         dt_a = implicit_robustness_dt(dt_a, nk_stats)
     return _clip(dt_a, pid_params.dt_min, pid_params.dt_max), st
+
+
+def estimate_reaction_stiffness(state, params) -> float:
+    """Reaction stiffness bound (dt_policy.py:505-541): Gray-Scott max(F + k, v^2 + F,
+    2 u v + F + k) from the state's maxima; Fisher-KPP r."""
+    s = 0.0
+    if "F" in params and "k" in params:
+        F, k = float(params["F"]), float(params["k"])
+        s = max(s, F + k)
+        if "u" in state and "v" in state:
+            vm = float(state["v"].abs().max())
+            um = float(state["u"].abs().max())
+            s = max(s, vm ** 2 + F, 2 * um * vm + F + k)
+    if "r" in params:
+        s = max(s, float(params["r"]))
+    return s

@@ -28,7 +28,7 @@ from __future__ import annotations
 
 import ctypes as C
 import math
-from typing import Dict, Optional
+from typing import Dict, NamedTuple, Optional
 
 import torch
 
@@ -39,6 +39,13 @@ from moljax_gb300.core.fft_solvers import get_plan, workspace
 _coeff_key = {}
 
 METHODS = {"etd1": N.ETD_1, "etd2": N.ETD_2, "etdrk4": N.ETD_RK4}
+
+
+class ETDStepResult(NamedTuple):
+    """fft_integrators.py:31-35."""
+    state: Dict[str, torch.Tensor]
+    t: float
+    diagnostics: dict
 
 
 def _symbol_code(symbol):

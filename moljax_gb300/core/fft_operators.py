@@ -14,12 +14,28 @@ from __future__ import annotations
 
 import ctypes as C
 from dataclasses import dataclass, field
-from typing import Dict, List, NamedTuple, Tuple, Union
+from typing import Dict, List, NamedTuple, Protocol, Tuple, Union, runtime_checkable
 
 import torch
 
 from moljax_gb300 import _native as N
 from moljax_gb300.core.grid import Grid1D, Grid2D
+
+
+@runtime_checkable
+class FFTLinearOperator(Protocol):
+    """fft_operators.py:42-77: what the ETD integrators and FFT solves need of an operator."""
+    name: str
+    grid: Union[Grid1D, Grid2D]
+
+    @property
+    def eigenvalues(self) -> torch.Tensor: ...
+
+    def matvec(self, u: torch.Tensor) -> torch.Tensor: ...
+
+    def solve(self, rhs: torch.Tensor, dt: float) -> torch.Tensor: ...
+
+    def exp_matvec(self, u: torch.Tensor, dt: float) -> torch.Tensor: ...
 
 
 @dataclass(frozen=True)

@@ -214,3 +214,36 @@ def newton_krylov_solve(residual_fn: Callable, x0, grid=None, params: Optional[D
         it += 1
     sol = _unflat(x, keys, shapes)
     return NKResult(sol["x"] if single else sol, NKStats(bool(converged), it, lits, res))
+
+
+def create_implicit_residual(model, y_old, t_new: float, dt: float, method: str = "be"):
+    """R(y) = y - y_old - dt F(y) ("be") or y - y_old - dt/2 (F(y_old) + F(y)) ("cn")
+    (newton_krylov.py:362-403); F is the model's fused native rhs."""
+    t_old = t_new - dt
+    if method == "be":
+        def residual(y_new):
+            F = model.rhs(y_new, t_new)
+            return {k: y_new[k] - y_old[k] - dt * F[k] for k in y_new}
+    elif method == "cn":
+        F_old = model.rhs(y_old, t_old)
+
+        def residual(y_new):
+            F = model.rhs(y_new, t_new)
+            return {k: y_new[k] - y_old[k] - 0.5 * dt * (F_old[k] + F[k]) for k in y_new}
+    else:
+        raise ValueError(f"Unknown method: {method}")
+    return residual
+
+
+def create_bdf2_residual(model, y_n, y_nm1, t_new: float, dt: float, dt_prev: float):
+    """Variable-step BDF2 residual a0 y + a1 y_n + a2 y_nm1 - beta F(y), omega = dt/dt_prev,
+    a0 = (1+2w)/(1+w), a1 = -(1+w), a2 = w^2/(1+w), beta = dt (1+w)/(1+2w)
+    (newton_krylov.py:406-448)."""
+    w = dt / dt_prev
+    a0, a1, a2 = (1.0 + 2.0 * w) / (1.0 + w), -(1.0 + w), w ** 2 / (1.0 + w)
+    beta = dt * (1.0 + w) / (1.0 + 2.0 * w)
+
+    def residual(y_new):
+        F = model.rhs(y_new, t_new)
+        return {k: a0 * y_new[k] + a1 * y_n[k] + a2 * y_nm1[k] - beta * F[k] for k in y_new}
+    return residual

@@ -66,6 +66,24 @@ def d1_central_2d(f, grid: Grid2D, axis: int):
     return _d1_2d(f, grid, 2, axis)
 
 
+def d2_central_2d(f, grid: Grid2D, axis: int):
+    """(f[+1] - 2 f + f[-1]) / d^2 along axis (0: y, 1: x) on the interior, ghosts zero
+    (operators.py:271-308)."""
+    return _d1_2d(f, grid, 3, axis)
+
+
+def d2_central_1d(f, grid: Grid1D):
+    """(f[i+1] - 2 f[i] + f[i-1]) / dx^2 on the interior (operators.py:113-138)."""
+    from moljax_gb300.core import stencil1d
+    return stencil1d.laplacian_1d(f, grid)
+
+
+def d1_central_1d(f, grid: Grid1D):
+    """(f[i+1] - f[i-1]) / (2 dx) on the interior."""
+    from moljax_gb300.core import stencil1d
+    return stencil1d.d1_central_1d(f, grid)
+
+
 def laplacian_1d(f_or_grid, grid=None, order: int = 2):
     """``laplacian_1d(f, grid)`` (operators.py:141-152) or the README factory form
     ``laplacian_1d(grid, order=2)`` returning an operator usable with ``@``."""
@@ -129,3 +147,103 @@ def fd_laplacian_symbol_2d(ny, nx, dy, dx, dtype=None):
 
 
 Params = Dict[str, Any]
+
+
+# ----------------------------------------------------------------- operator factories
+def state_zero_like(state):
+    """Zeros shaped like each field (operators.py:383-385)."""
+    return {k: torch.zeros_like(v) for k, v in state.items()}
+
+
+def op_sum(ops):
+    """(state, grid, t, params) -> the sum of the ops' outputs (operators.py:364-380)."""
+    def combined_apply(state, grid, t, params):
+        result = ops[0].apply(state, grid, t, params)
+        for op in ops[1:]:
+            r = op.apply(state, grid, t, params)
+            result = {k: result[k] + r[k] for k in result}
+        return result
+    return combined_apply
+
+
+def make_diffusion_op_1d(field_name: str, D_param: str = "D") -> LinearOp:
+    """D Lap of one field, zeros elsewhere; dt bound 0.5 dx^2 / D (operators.py:392-417)."""
+    def apply(state, grid, t, params):
+        out = state_zero_like(state)
+        out[field_name] = params.get(D_param, 1.0) * laplacian_1d(state[field_name], grid)
+        return out
+
+    def dt_bound(grid, params):
+        return 0.5 * grid.min_dx2 / (params.get(D_param, 1.0) + 1e-14)
+
+    return LinearOp(f"diffusion_{field_name}", apply, dt_bound, "diffusion")
+
+
+def make_diffusion_op_2d(field_name: str, D_param: str = "D") -> LinearOp:
+    """D Lap of one field, zeros elsewhere; dt bound 0.25 min(dx,dy)^2 / D (operators.py:420-444)."""
+    def apply(state, grid, t, params):
+        out = state_zero_like(state)
+        out[field_name] = params.get(D_param, 1.0) * laplacian_2d(state[field_name], grid)
+        return out
+
+    def dt_bound(grid, params):
+        return 0.25 * grid.min_dx2 / (params.get(D_param, 1.0) + 1e-14)
+
+    return LinearOp(f"diffusion_{field_name}", apply, dt_bound, "diffusion")
+
+
+def make_advection_op_1d(field_name: str, vx_param: str = "vx", use_upwind: bool = True) -> LinearOp:
+    """-vx df/dx (upwind or central), zeros elsewhere; dt bound dx / |vx| (operators.py:447-481)."""
+    def apply(state, grid, t, params):
+        vx = params.get(vx_param, 0.0)
+        f = state[field_name]
+        d = d1_upwind_1d(f, vx, grid) if use_upwind else d1_central_1d(f, grid)
+        out = state_zero_like(state)
+        out[field_name] = -vx * d
+        return out
+
+    def dt_bound(grid, params):
+        return grid.min_dx / (abs(params.get(vx_param, 0.0)) + 1e-14)
+
+    return LinearOp(f"advection_{field_name}", apply, dt_bound, "advection")
+
+
+def make_advection_op_2d(field_name: str, vx_param: str = "vx", vy_param: str = "vy",
+                         use_upwind: bool = True) -> LinearOp:
+    """-(vx df/dx + vy df/dy), zeros elsewhere; dt bound min(dx,dy) / (|vx| + |vy|)
+    (operators.py:484-527)."""
+    def apply(state, grid, t, params):
+        vx, vy = params.get(vx_param, 0.0), params.get(vy_param, 0.0)
+        f = state[field_name]
+        if use_upwind:
+            dx_, dy_ = d1_upwind_2d(f, vx, grid, 1), d1_upwind_2d(f, vy, grid, 0)
+        else:
+            dx_, dy_ = d1_central_2d(f, grid, 1), d1_central_2d(f, grid, 0)
+        out = state_zero_like(state)
+        out[field_name] = -vx * dx_ - vy * dy_
+        return out
+
+    def dt_bound(grid, params):
+        v = abs(params.get(vx_param, 0.0)) + abs(params.get(vy_param, 0.0))
+        return grid.min_dx / (v + 1e-14)
+
+    return LinearOp(f"advection_{field_name}", apply, dt_bound, "advection")
+
+
+def make_reaction_op(reactions) -> NonlinearOp:
+    """Per-field reaction functions (state, params) -> rate, zeros elsewhere
+    (operators.py:623-641).  User callables: usable through ``apply`` and the generic
+    Newton-Krylov path; the fused drivers take the built-in reactions only."""
+    def apply(state, grid, t, params):
+        out = state_zero_like(state)
+        for name, fn in reactions.items():
+            out[name] = fn(state, params)
+        return out
+
+    return NonlinearOp("reactions", apply, None, None)
+
+
+def fd_laplacian_symbol_1d(nx: int, dx: float, dtype=None):
+    """(2 cos(k dx) - 2) / dx^2, k = 2 pi fftfreq (operators.py:708-731)."""
+    from moljax_gb300.core.fft_solvers import laplacian_symbol_1d
+    return laplacian_symbol_1d(nx, dx, dtype or torch.float64)

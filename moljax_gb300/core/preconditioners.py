@@ -203,9 +203,40 @@ class FFTAdvectionDiffusionPreconditioner:
         return out
 
 
-def create_gray_scott_preconditioner(Du_key="Du", Dv_key="Dv") -> DiffusionPreconditioner:
-    """preconditioners.py:423-446."""
-    return DiffusionPreconditioner(field_diffusivities={"u": Du_key, "v": Dv_key})
+def create_gray_scott_preconditioner() -> BlockJacobiPreconditioner:
+    """Block-Jacobi on u (Du) and v (Dv) (preconditioners.py:423-427)."""
+    return BlockJacobiPreconditioner(diffusion_keys={"u": "Du", "v": "Dv"})
+
+
+def create_advdiff_preconditioner(field_names) -> BlockJacobiPreconditioner:
+    """Block-Jacobi with diffusivity key 'D' and velocity key 'vx' per field
+    (preconditioners.py:430-437)."""
+    return BlockJacobiPreconditioner(diffusion_keys={n: "D" for n in field_names},
+                                     advection_keys={n: "vx" for n in field_names})
+
+
+def create_diffusion_preconditioner(field_diffusivities: Dict[str, str], n_iterations: int = 5):
+    """preconditioners.py:440-457."""
+    return DiffusionPreconditioner(field_diffusivities=field_diffusivities, n_iterations=n_iterations)
+
+
+def create_fft_preconditioner(field_diffusivity_keys: Dict[str, str], fft_cache, fallback=None):
+    """preconditioners.py:460-480."""
+    return FFTDiffusionPreconditioner(field_diffusivity_keys=field_diffusivity_keys, fft_cache=fft_cache,
+                                      fallback=fallback)
+
+
+def create_gray_scott_fft_preconditioner(fft_cache):
+    """FFT preconditioner on u (Du) and v (Dv) (preconditioners.py:483-488)."""
+    return FFTDiffusionPreconditioner(field_diffusivity_keys={"u": "Du", "v": "Dv"}, fft_cache=fft_cache)
+
+
+def create_advdiff_fft_preconditioner(field_diffusivity_keys: Dict[str, str],
+                                      field_velocity_keys: Dict[str, str], fft_cache, fallback=None):
+    """preconditioners.py:491-514."""
+    return FFTAdvectionDiffusionPreconditioner(field_diffusivity_keys=field_diffusivity_keys,
+                                               field_velocity_keys=field_velocity_keys,
+                                               fft_cache=fft_cache, fallback=fallback)
 
 
 Preconditioner = Any

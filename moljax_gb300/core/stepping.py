@@ -551,3 +551,63 @@ def adaptive_integrate(model, y0=None, t0: float = 0.0, t_end: Optional[float] =
                                        method == IntegratorType.IMEX_STRANG, max_steps,
                                        cfl_params, pid_params, save_every, **kw)
     raise NotImplementedError(f"{method.name} adaptive driver is not built on the GPU path")
+
+
+# ------------------------------------------------------------------ step-doubling helpers
+class AdaptiveState(NamedTuple):
+    """moljax/core/stepping.py:683-707: the loop state of the reference's adaptive
+    while_loop.  The native drivers keep it on the device (DevState); this record is the
+    host-side mirror for callers that build their own loops."""
+    t: float
+    y: Dict[str, torch.Tensor]
+    dt: float
+    y_prev: Optional[Dict[str, torch.Tensor]]
+    dt_prev: float
+    step_count: int
+    controller: object
+    t_history: torch.Tensor
+    y_history: Optional[Dict[str, torch.Tensor]]
+    dt_history: torch.Tensor
+    write_idx: int
+    n_accepted: int
+    n_rejected: int
+    status: int
+
+
+def _sub(a, b):
+    return {k: a[k] - b[k] for k in a}
+
+
+def estimate_error_doubling(model, y, t, dt, step_fn):
+    """(y_half2, y_half2 - y_full) from one step of dt and two of dt/2 (stepping.py:502-536)."""
+    y_full = step_fn(model, y, t, dt)
+    y_half2 = step_fn(model, step_fn(model, y, t, dt / 2.0), t + dt / 2.0, dt / 2.0)
+    return y_half2, _sub(y_half2, y_full)
+
+
+def estimate_error_implicit(model, y, t, dt, y_be, y_cn):
+    """y_cn - y_be (stepping.py:539-563)."""
+    return _sub(y_cn, y_be)
+
+
+def estimate_error_imex_doubling(model, y, t, dt, fft_cache, diffusivities, use_strang: bool = True):
+    """Step doubling with IMEX-Strang (or IMEX-Euler) steps (stepping.py:566-608); each step
+    is one native fused call.  The adaptive drivers fuse the three steps of an attempt and
+    the error norm into one pass sequence instead."""
+    fn = imex_strang_step if use_strang else imex_euler_step
+    return estimate_error_doubling(model, y, t, dt,
+                                   lambda m, yy, tt, h: fn(m, yy, tt, h, fft_cache, diffusivities))
+
+
+_EXPLICIT_STEPS = {0: "euler_step", 1: "ssprk3_step", 2: "rk4_step"}
+
+
+def step_explicit(model, y, t, dt, method: int):
+    """Euler / SSPRK3 / RK4 by index 0 / 1 / 2 (stepping.py:615-643)."""
+    return globals()[_EXPLICIT_STEPS[int(method)]](model, y, t, dt)
+
+
+def step_explicit_with_error(model, y, t, dt, method: int):
+    """Step doubling with the explicit method of index 0 / 1 / 2 (stepping.py:646-676)."""
+    fn = globals()[_EXPLICIT_STEPS[int(method)]]
+    return estimate_error_doubling(model, y, t, dt, fn)

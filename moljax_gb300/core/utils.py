@@ -57,3 +57,73 @@ def is_finite(state) -> bool:
         if res[1] == 0.0:
             return False
     return True
+
+
+# ---------------------------------------------------------------- small helpers (utils.py:20-261)
+def eps_for_dtype(dtype=None) -> float:
+    """1e-10 for FP32, else 1e-14 (utils.py:20-27)."""
+    import torch
+    return 1e-10 if dtype == torch.float32 else 1e-14
+
+
+def safe_eps(dtype=None) -> float:
+    return eps_for_dtype(dtype)
+
+
+def set_interior(padded, interior, grid):
+    """A copy of padded with its interior replaced (utils.py:44-60)."""
+    out = padded.clone()
+    out[grid.interior_slice] = interior
+    return out
+
+
+def allocate_scalar_history(max_steps: int, dtype=None, device=None):
+    import torch
+    return torch.zeros(max_steps, dtype=dtype or torch.float64, device=device)
+
+
+def allocate_field_history(field_shape, max_steps: int, dtype=None, device=None):
+    import torch
+    return torch.zeros((max_steps,) + tuple(field_shape), dtype=dtype or torch.float64, device=device)
+
+
+def allocate_state_history(state, grid, max_steps: int, interior_only: bool = True, dtype=None):
+    """utils.py:96-123."""
+    return {n: allocate_field_history((f[grid.interior_slice] if interior_only else f).shape, max_steps,
+                                      dtype or f.dtype, f.device) for n, f in state.items()}
+
+
+def save_to_history(history, state, grid, idx: int, interior_only: bool = True):
+    """Writes the state into slot idx (in place) and returns the history (utils.py:126-153)."""
+    for n, f in state.items():
+        history[n][idx] = f[grid.interior_slice] if interior_only else f
+    return history
+
+
+def safe_divide(numerator, denominator, eps: float = 1e-14):
+    return numerator / (denominator + eps)
+
+
+def clip_array(x, x_min: float, x_max: float):
+    import torch
+    return torch.clamp(x, x_min, x_max)
+
+
+def create_padded_array(grid, fill_value: float = 0.0, dtype=None, device=None):
+    """utils.py:200-219."""
+    import torch
+    from moljax_gb300.core.grid import Grid1D
+    shape = (grid.nx_total,) if isinstance(grid, Grid1D) else (grid.ny_total, grid.nx_total)
+    return torch.full(shape, fill_value, dtype=dtype or torch.float64, device=device)
+
+
+def max_abs_interior(field, grid):
+    return field[grid.interior_slice].abs().max()
+
+
+def mean_interior(field, grid):
+    return field[grid.interior_slice].mean()
+
+
+def sum_interior(field, grid):
+    return field[grid.interior_slice].sum()

@@ -213,7 +213,37 @@ __global__ void stencil2d_kernel(const T* __restrict__ in, T* __restrict__ out, 
     if (y < g || y >= ny + g || x < g || x >= nx + g) { out[i] = (T)0; continue; }
     const T c = in[i], lo = in[i - step], hi = in[i + step];
     if (op == 1) out[i] = v >= 0 ? (c - lo) / (T)d : (hi - c) / (T)d;
-    else out[i] = (hi - lo) / (T)(2.0 * d);
+    else if (op == 2) out[i] = (hi - lo) / (T)(2.0 * d);
+    else out[i] = (hi - (T)2 * c + lo) / (T)(d * d);
+  }
+}
+
+// div(D grad u) with face averages D_{i+1/2} = (D_i + D_{i+1})/2 on the interior, ghosts zero
+// (apply_variable_diffusion_2d, moljax/core/variable_coeff.py:232-287).  D is padded like u, or
+// interior-shaped (d_interior != 0) and then edge-extended as jnp.pad(mode='edge') does.
+template <typename T>
+__global__ void vardiff2d_kernel(const T* __restrict__ u, const T* __restrict__ D, T* __restrict__ out,
+                                 int ny, int nx, int g, int d_interior, double dy, double dx) {
+  const int ldx = nx + 2 * g, ldy = ny + 2 * g;
+  const long long total = (long long)ldx * ldy;
+  const T idx2 = (T)(1.0 / (dx * dx)), idy2 = (T)(1.0 / (dy * dy));
+  auto Dat = [&](int y, int x) -> T {
+    if (!d_interior) return D[(long long)y * ldx + x];
+    int yi = y - g, xi = x - g;
+    yi = yi < 0 ? 0 : (yi >= ny ? ny - 1 : yi);
+    xi = xi < 0 ? 0 : (xi >= nx ? nx - 1 : xi);
+    return D[(long long)yi * nx + xi];
+  };
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+       i += (long long)gridDim.x * blockDim.x) {
+    const int y = (int)(i / ldx), x = (int)(i - (long long)y * ldx);
+    if (y < g || y >= ny + g || x < g || x >= nx + g) { out[i] = (T)0; continue; }
+    const T c = u[i], Dc = Dat(y, x);
+    const T dxp = (T)0.5 * (Dc + Dat(y, x + 1)), dxm = (T)0.5 * (Dc + Dat(y, x - 1));
+    const T dyp = (T)0.5 * (Dc + Dat(y + 1, x)), dym = (T)0.5 * (Dc + Dat(y - 1, x));
+    const T Lx = (dxp * (u[i + 1] - c) - dxm * (c - u[i - 1])) * idx2;
+    const T Ly = (dyp * (u[i + ldx] - c) - dym * (c - u[i - ldx])) * idy2;
+    out[i] = Lx + Ly;
   }
 }
 
@@ -259,11 +289,29 @@ mjx_status mjx_stencil2d(const void* padded_in, void* padded_out, int nfields, i
   const int e = elem_size(dtype);
   if (!e) return MJX_BAD_DTYPE;
   if (!padded_in || !padded_out || padded_in == padded_out) return MJX_BAD_ARG;
-  if (op < 1 || op > 2 || axis < 0 || axis > 1 || !(d > 0)) return MJX_BAD_ARG;
+  if (op < 1 || op > 3 || axis < 0 || axis > 1 || !(d > 0)) return MJX_BAD_ARG;
   const long long total = (long long)nfields * (ny + 2 * n_ghost) * (nx + 2 * n_ghost);
   cudaStream_t s = (cudaStream_t)stream;
   if (e == 4) stencil2d_kernel<float><<<grid_for(total), 256, 0, s>>>((const float*)padded_in, (float*)padded_out, nfields, ny, nx, n_ghost, op, axis, v, d);
   else stencil2d_kernel<double><<<grid_for(total), 256, 0, s>>>((const double*)padded_in, (double*)padded_out, nfields, ny, nx, n_ghost, op, axis, v, d);
+  return cuda_status(cudaGetLastError());
+}
+
+mjx_status mjx_variable_diffusion2d(const void* u_padded, const void* D, int d_interior, void* out_padded,
+                                    int ny, int nx, int n_ghost, double dy, double dx, int dtype, void* stream) {
+  const int e = elem_size(dtype);
+  if (!e) return MJX_BAD_DTYPE;
+  if (!u_padded || !D || !out_padded || u_padded == out_padded || ny < 1 || nx < 1 || n_ghost < 1 ||
+      !(dx > 0) || !(dy > 0))
+    return MJX_BAD_ARG;
+  const long long total = (long long)(ny + 2 * n_ghost) * (nx + 2 * n_ghost);
+  cudaStream_t s = (cudaStream_t)stream;
+  if (e == 4)
+    vardiff2d_kernel<float><<<grid_for(total), 256, 0, s>>>((const float*)u_padded, (const float*)D,
+                                                            (float*)out_padded, ny, nx, n_ghost, d_interior, dy, dx);
+  else
+    vardiff2d_kernel<double><<<grid_for(total), 256, 0, s>>>((const double*)u_padded, (const double*)D,
+                                                             (double*)out_padded, ny, nx, n_ghost, d_interior, dy, dx);
   return cuda_status(cudaGetLastError());
 }
 
