@@ -65,7 +65,7 @@ from moljax_gb300.core.operators import (d2_central_1d, d2_central_2d, d1_centra
                                         gray_scott_reaction_op, fisher_kpp_reaction_op)
 from moljax_gb300.core.stepping import (AdaptiveState, estimate_error_doubling,
                                         estimate_error_implicit, estimate_error_imex_doubling,
-                                        step_explicit, step_explicit_with_error)
+                                        step_explicit, step_explicit_with_error, imex_ssprk2_step)
 from moljax_gb300.core.newton_krylov import create_implicit_residual, create_bdf2_residual
 from moljax_gb300.core.preconditioners import (create_gray_scott_preconditioner,
                                                create_advdiff_preconditioner,

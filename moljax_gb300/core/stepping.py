@@ -611,3 +611,32 @@ def step_explicit_with_error(model, y, t, dt, method: int):
     """Step doubling with the explicit method of index 0 / 1 / 2 (stepping.py:646-676)."""
     fn = globals()[_EXPLICIT_STEPS[int(method)]]
     return estimate_error_doubling(model, y, t, dt, fn)
+
+
+def imex_ssprk2_step(model, y, t, dt, fft_cache, diffusivities):
+    """IMEX-SSPRK2 (stepping.py:438-495): y1 = H(dt)(y + dt N(y)), y2 = H(dt)(y1 + dt N(y1)),
+    y_new = (y + y2)/2, the BCs applied after each stage.  N is the model's reaction by the
+    native row pass (on the interiors; every ghost is refilled by the BCs), H the native
+    Helmholtz pass."""
+    from moljax_gb300.core.fft_integrators import NativeNonlinear
+    from moljax_gb300.core.fft_solvers import apply_diffusion_inverse_fft
+    grid = model.grid
+    nl = NativeNonlinear.of(model)
+    sl = grid.interior_slice
+
+    def N(state):
+        r = nl({k: v[sl] for k, v in state.items()})
+        out = {k: torch.zeros_like(v) for k, v in state.items()}
+        for k in out:
+            out[k][sl] = r[k]
+        return out
+
+    def stage(z, tt):
+        n = N(z)
+        rhs = {k: z[k] + dt * n[k] for k in z}
+        return model.apply_bcs(apply_diffusion_inverse_fft(rhs, grid, dt, diffusivities, fft_cache), tt)
+
+    y = model.apply_bcs(y, t)
+    y1 = stage(y, t + dt)
+    y2 = stage(y1, t + dt)
+    return model.apply_bcs({k: 0.5 * y[k] + 0.5 * y2[k] for k in y}, t + dt)

@@ -80,6 +80,18 @@ def imex_euler_step(model, y, dt, lam, diff):
     return model.apply_bcs(y_new)
 
 
+def imex_ssprk2_step(model, y, dt, lam, diff):
+    """moljax/core/stepping.py:438-495: y1 = H(dt)(y + dt N(y)); y2 = H(dt)(y1 + dt N(y1));
+    y_new = (y + y2)/2, BCs applied after each stage."""
+    y = model.apply_bcs(y)
+
+    def N(z):
+        return model.nonlinear_rhs(z) if model.reaction else {k: np.zeros_like(f) for k, f in z.items()}
+    y1 = model.apply_bcs(mol.apply_diffusion_inverse_fft(_axpy(y, dt, N(y)), model.grid, dt, diff, lam))
+    y2 = model.apply_bcs(mol.apply_diffusion_inverse_fft(_axpy(y1, dt, N(y1)), model.grid, dt, diff, lam))
+    return model.apply_bcs({k: 0.5 * y[k] + 0.5 * y2[k] for k in y})
+
+
 def imex_strang_step(model, y, dt, lam, diff):
     """moljax/core/stepping.py:370-435: H(dt/2) -> Heun reaction(dt) -> H(dt/2)."""
     h = dt / 2.0

@@ -148,3 +148,23 @@ def test_implicit_residual_factories(cuda):
         np.testing.assert_allclose(r2[k].cpu().numpy(), ya[k] - yb[k] - 0.05 * (Fb[k] + Fa[k]), rtol=0, atol=1e-14)
         np.testing.assert_allclose(r3[k].cpu().numpy(), a0 * ya[k] + a1 * yb[k] + a2 * yc[k] - beta * Fa[k],
                                    rtol=0, atol=1e-13)
+
+
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+def test_imex_ssprk2_step_vs_oracle(cuda, dtype):
+    import moljax_gb300 as M
+    n = 64
+    grid = M.Grid2D(n, n, 0.0, 2.5, 0.0, 2.5)
+    model, cache, diff = M.create_gray_scott_periodic_fft(grid, 2e-5, 1e-5, 0.035, 0.065, dtype, cuda)
+    og = mol.Grid2D(n, n, 0, 2.5, 0, 2.5)
+    y0 = mol.gray_scott_ic(og, 13)
+    om, lam, od = OI.gray_scott_periodic(og, 2e-5, 1e-5, 0.035, 0.065)
+    y = {k: torch.tensor(v, dtype=dtype, device=cuda) for k, v in y0.items()}
+    yo = y0
+    for _ in range(3):
+        y = M.imex_ssprk2_step(model, y, 0.0, 0.7, cache, diff)
+        yo = OI.imex_ssprk2_step(om, yo, 0.7, lam, od)
+    tol = 1e-13 if dtype == torch.float64 else 2e-6
+    for k in ("u", "v"):
+        r = float(np.linalg.norm(y[k].cpu().double().numpy() - yo[k]) / np.linalg.norm(yo[k]))
+        assert r < tol  # ghosts included (periodic fill)
