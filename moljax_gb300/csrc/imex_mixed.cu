@@ -126,7 +126,10 @@ __global__ void __launch_bounds__(NT, MINB) mcol_kernel(const __grid_constant__ 
   const DevState* st = a.st;
   if (st != nullptr && st->done) return;
   const MJob jb = a.job[blockIdx.y];
-  const int Cn = a.C, W = 2 * Cn;
+  // the tile holds two outputs side by side (W = 2C) where a job writes two transforms
+  // (C1 split, C3 end); the single-output jobs of C2 use a compact tile (W = C), whose
+  // column transforms then walk shared memory with half the stride
+  const int Cn = a.C, W = (jb.type == MC_FULL_END || jb.type == MC_HALF_MID) ? Cn : 2 * Cn;
   const int kx0 = blockIdx.x * Cn;
   const int ny = a.ny, tid = threadIdx.x, nth = blockDim.x;
   const int total = ny * Cn;
@@ -165,7 +168,7 @@ __global__ void __launch_bounds__(NT, MINB) mcol_kernel(const __grid_constant__ 
     const int ky = e / Cn, c = e - ky * Cn, kx = kx0 + c;
     if (kx >= a.ncols) {
       buf[sp(ky * W + c)] = fmk(0.f, 0.f);
-      buf[sp(ky * W + Cn + c)] = fmk(0.f, 0.f);
+      if (W > Cn) buf[sp(ky * W + Cn + c)] = fmk(0.f, 0.f);
       continue;
     }
     const long long g = jb.off + ky * ldc + kx;
