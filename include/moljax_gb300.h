@@ -52,7 +52,12 @@ typedef enum mjx_mult {
   MJX_MULT_HELMHOLTZ = 1,  /* 1/(1 - h D lam), |denominator| clamped at 1e-14 */
   MJX_MULT_CN = 2,         /* (1 + h D lam/2)/(1 - h D lam/2) */
   MJX_MULT_EXP = 3,        /* exp(h D lam) */
-  MJX_MULT_LAP = 5         /* h D lam (the operator itself, DiffusionOperator.matvec) */
+  MJX_MULT_LAP = 5,        /* h D lam (the operator itself, DiffusionOperator.matvec) */
+  /* general-size path only (mjx_spectral_apply_general2d), z = h (D lam - i (vx kx + vy ky)): */
+  MJX_MULT_ADV_SOLVE = 16, /* 1/(1 - z), |1 - z| clamped at 1e-14 */
+  MJX_MULT_ADV_LAP = 17,   /* z */
+  MJX_MULT_ADV_EXP = 18,   /* exp(z) */
+  MJX_MULT_TABLE = 19      /* a real table [ny][nx] on the full spectrum */
 } mjx_mult;
 
 typedef enum mjx_reaction {
@@ -117,6 +122,32 @@ size_t mjx_spec2d_ws_bytes(int ny, int nx, int nfields, int dtype);
 mjx_status mjx_spectral_apply2d(const void* plan, const mjx_grid2d* grid, int dtype, int nfields,
                                 const double* D, double h, int mult, const void* in, void* out,
                                 void* ws, size_t ws_bytes, void* stream);
+
+/* ---- periodic grids of any size (numpy / jnp.fft lengths) ------------------------- */
+/* Plan of a length-n DFT: n a power of two <= 4096 (Stockham) or any n <= 2048
+ * (Bluestein chirp-z with a power-of-two convolution <= 4096); 0 bytes if unsupported. */
+size_t mjx_dftn_plan_bytes(int n, int dtype);
+mjx_status mjx_dftn_plan_init(void* plan, int n, int dtype, void* stream);
+size_t mjx_spectral_general2d_ws_bytes(int ny, int nx, int nfields, int dtype);
+/* out_f = real(IFFT2( m FFT2(in_f) )) for ny x nx interiors of any supported size, on the
+ * full complex spectrum (row DFTs, transpose, column DFTs, multiplier, and back).  mult:
+ * MJX_MULT_SCALE/HELMHOLTZ/CN/EXP/LAP with lam the FD or spectral symbol and D_f, the
+ * advection forms MJX_MULT_ADV_* with vx_f, vy_f (may be NULL: zero), or MJX_MULT_TABLE with
+ * table [ny][nx].  The same operations as mjx_spectral_apply2d / mjx_advdiff_op2d /
+ * mjx_spectral_filter2d (fft_solvers.py:222-616, fft_operators.py:80-260). */
+mjx_status mjx_spectral_apply_general2d(const void* plan_y, const void* plan_x, const mjx_grid2d* grid, int symbol,
+                                        int dtype, int nfields, const double* D, const double* vx,
+                                        const double* vy, double h, int mult, const void* table,
+                                        const void* in, void* out, void* ws, size_t ws_bytes, void* stream);
+
+size_t mjx_spectral_general3d_ws_bytes(int nz, int ny, int nx, int dtype);
+/* n_steps times u <- real(IFFTN( m(h, D, lam) FFTN(u) )) on an [nz][ny][nx] box of any
+ * supported lengths (the general form of mjx_spectral_apply3d; the 3D FFT-CN of
+ * bench_3d_feasibility.py at its 48^3, 80^3, 100^3 cases).  mult: SCALE/HELMHOLTZ/CN/EXP/LAP. */
+mjx_status mjx_spectral_apply_general3d(const void* plan_z, const void* plan_y, const void* plan_x,
+                                        const mjx_grid3d* grid, int symbol, int dtype, double D, double h, int mult,
+                                        int n_steps, const void* in, void* out, void* ws, size_t ws_bytes,
+                                        void* stream);
 
 /* ---- periodic 3D boxes (benchmarks/sisc/bench_3d_feasibility.py) ------------------ */
 /* Plan: x / y / z twiddles and 1D symbols (FD or spectral) of an [nz][ny][nx] box. */

@@ -27,6 +27,7 @@ STATUS_NAMES = {
 F32, F64 = 0, 1
 SYMBOL_FD, SYMBOL_SPECTRAL = 0, 1
 MULT_SCALE, MULT_HELMHOLTZ, MULT_CN, MULT_EXP, MULT_LAP = 0, 1, 2, 3, 5
+MULT_ADV_SOLVE, MULT_ADV_LAP, MULT_ADV_EXP, MULT_TABLE = 16, 17, 18, 19
 REACT_NONE, REACT_GRAY_SCOTT, REACT_FISHER = 0, 1, 2
 SYMBOL_X_ONLY = 0x10
 ETD_1, ETD_2, ETD_RK4 = 1, 2, 4
@@ -157,6 +158,15 @@ SIGNATURES = {
     "mjx_advdiff_op2d": (_i, [_vp, C.POINTER(Grid2DC), _i, _i, C.POINTER(C.c_double), C.POINTER(C.c_double),
                               C.POINTER(C.c_double), _d, _i, _vp, _vp, _vp, _sz, _vp]),
     "mjx_spectral_filter2d": (_i, [_vp, C.POINTER(Grid2DC), _i, _i, _vp, _vp, _vp, _vp, _sz, _vp]),
+    "mjx_dftn_plan_bytes": (_sz, [_i, _i]),
+    "mjx_dftn_plan_init": (_i, [_vp, _i, _i, _vp]),
+    "mjx_spectral_general2d_ws_bytes": (_sz, [_i, _i, _i, _i]),
+    "mjx_spectral_apply_general2d": (_i, [_vp, _vp, C.POINTER(Grid2DC), _i, _i, _i, C.POINTER(C.c_double),
+                                          C.POINTER(C.c_double), C.POINTER(C.c_double), _d, _i, _vp, _vp, _vp,
+                                          _vp, _sz, _vp]),
+    "mjx_spectral_general3d_ws_bytes": (_sz, [_i, _i, _i, _i]),
+    "mjx_spectral_apply_general3d": (_i, [_vp, _vp, _vp, C.POINTER(Grid3DC), _i, _i, _d, _d, _i, _i, _vp, _vp,
+                                          _vp, _sz, _vp]),
     "mjx_spec3d_plan_bytes": (_sz, [_i, _i, _i, _i]),
     "mjx_spec3d_plan_init": (_i, [_vp, C.POINTER(Grid3DC), _i, _i, _vp]),
     "mjx_spec3d_ws_bytes": (_sz, [_i, _i, _i, _i]),

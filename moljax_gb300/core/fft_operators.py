@@ -169,6 +169,10 @@ class AdvectionDiffusionOperator:
             plan = get_plan(g.ny, g.nx, g.dy, g.dx, "fd", u.dtype, u.device)
             x = u
         vx, vy = self._velocity()
+        if getattr(plan, "general", False):
+            mult = (N.MULT_ADV_SOLVE, N.MULT_ADV_LAP, N.MULT_ADV_EXP)[op]
+            out = plan.apply(x, float(self.D), h, mult, vx=vx, vy=vy)
+            return out[0].clone() if self.is_1d else out
         out = torch.empty_like(x)
         ws = workspace(plan.ws_bytes(1), plan.device)
         D_ = (C.c_double * 1)(float(self.D))

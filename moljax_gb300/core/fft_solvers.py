@@ -96,12 +96,81 @@ class SpectralPlan:
         return out3.reshape(x.shape)
 
 
-def get_plan(ny, nx, dy, dx, symbol="fd", dtype=torch.float64, device=None) -> SpectralPlan:
+def _pow2(n: int) -> bool:
+    return n >= 1 and (n & (n - 1)) == 0
+
+
+class GeneralSpectralPlan:
+    """Periodic (ny, nx) grid of any supported size (powers of two up to 4096, other sizes up
+    to 2048): the full-spectrum path of ``mjx_spectral_apply_general2d`` (row DFTs by
+    Stockham or Bluestein, transposes, column DFTs and the multiplier).  Same ``apply`` as
+    ``SpectralPlan``; the fused drivers (IMEX, ETD, explicit steppers) take powers of two."""
+
+    general = True
+
+    def __init__(self, ny: int, nx: int, dy: float, dx: float, symbol: str = "fd",
+                 dtype: torch.dtype = torch.float64, device=None):
+        N.require_cuda()
+        self.ny, self.nx, self.dy, self.dx = int(ny), int(nx), float(dy), float(dx)
+        self.symbol, self.dtype, self.device = symbol, dtype, _device(device)
+        self.code = N.dtype_code(dtype)
+        lib = N.lib()
+        self.cgrid = N.Grid2DC(self.ny, self.nx, self.dy, self.dx)
+        bufs = []
+        for n in (self.ny, self.nx):
+            nb = lib.mjx_dftn_plan_bytes(n, self.code)
+            if nb == 0:
+                raise ValueError(f"unsupported grid {ny}x{nx}: lengths must be powers of two <= 4096 or <= 2048")
+            b = torch.empty(nb, dtype=torch.uint8, device=self.device)
+            with torch.cuda.device(self.device):
+                N.check("mjx_dftn_plan_init", lib.mjx_dftn_plan_init(N.ptr(b), n, self.code,
+                                                                     N.stream_ptr(self.device)))
+            bufs.append(b)
+        self.buf_y, self.buf_x = bufs
+        self.buf = self.buf_y  # the power-of-two entry points reject this grid by its shape
+
+    def ws_bytes(self, nfields: int) -> int:
+        return N.lib().mjx_spectral_general2d_ws_bytes(self.ny, self.nx, nfields, self.code)
+
+    def apply(self, x: torch.Tensor, D, h: float, mult: int, out: Optional[torch.Tensor] = None,
+              vx=None, vy=None, table: Optional[torch.Tensor] = None):
+        """out_f = real(IFFT2(m(h, D_f, ...) FFT2(x_f))) for x of shape (ny, nx) or (nf, ny, nx)."""
+        x3 = x.reshape(-1, self.ny, self.nx).contiguous()
+        N.require_cuda(x3)
+        if x3.dtype != self.dtype:
+            raise TypeError(f"plan dtype {self.dtype} does not match {x3.dtype}")
+        nf = x3.shape[0]
+
+        def per_field(v):
+            if v is None:
+                return [0.0] * nf
+            return [float(v)] * nf if not isinstance(v, (list, tuple)) else [float(t) for t in v]
+        Ds, vxs, vys = per_field(D), per_field(vx), per_field(vy)
+        out3 = torch.empty_like(x3) if out is None else out.reshape(-1, self.ny, self.nx)
+        sym = SYMBOLS[self.symbol]
+        for i in range(0, nf, 4):
+            j = min(nf, i + 4)
+            ws = workspace(self.ws_bytes(j - i), self.device, "general")
+            arr = lambda v: (C.c_double * (j - i))(*v[i:j])  # noqa: E731
+            N.check("mjx_spectral_apply_general2d", N.lib().mjx_spectral_apply_general2d(
+                N.ptr(self.buf_y), N.ptr(self.buf_x), C.byref(self.cgrid), sym, self.code, j - i,
+                arr(Ds), arr(vxs), arr(vys), float(h), int(mult),
+                N.ptr(table) if table is not None else None, N.ptr(x3[i:j]), N.ptr(out3[i:j]),
+                N.ptr(ws), ws.numel(), N.stream_ptr(self.device)))
+        return out3.reshape(x.shape)
+
+
+def get_plan(ny, nx, dy, dx, symbol="fd", dtype=torch.float64, device=None):
+    """The spectral plan of a periodic (ny, nx) grid: the fused power-of-two passes, or the
+    general full-spectrum path for other sizes."""
     dev = _device(device)
     key = (int(ny), int(nx), float(dy), float(dx), symbol, dtype, str(dev))
     p = _plans.get(key)
     if p is None:
-        p = SpectralPlan(ny, nx, dy, dx, symbol, dtype, dev)
+        if _pow2(int(ny)) and _pow2(int(nx)) and ny >= 2 and nx >= 2:
+            p = SpectralPlan(ny, nx, dy, dx, symbol, dtype, dev)
+        else:
+            p = GeneralSpectralPlan(ny, nx, dy, dx, symbol, dtype, dev)
         _plans[key] = p
     return p
 
@@ -337,6 +406,13 @@ def apply_spectral_filter_interior(u_interior: torch.Tensor, filter_kernel) -> t
         x = u
     kern = filter_kernel if torch.is_tensor(filter_kernel) else torch.as_tensor(filter_kernel)
     plan = get_plan(ny, nx, 1.0 / ny, 1.0 / nx, "fd", u.dtype, u.device)
+    if getattr(plan, "general", False):
+        K = kern.to(torch.float64)
+        if K.ndim == 1:
+            K = K[None, :].expand(ny, nx)
+        tab = K.to(u.dtype).to(u.device).contiguous()
+        out = plan.apply(x, 1.0, 1.0, N.MULT_TABLE, table=tab)
+        return out[0].clone() if u.ndim == 1 else out
     tab = _half_table(kern, ny, nx, u.dtype, u.device)
     out = torch.empty_like(x)
     ws = workspace(plan.ws_bytes(1), plan.device)
@@ -372,6 +448,10 @@ def fft_cn_step(u0: torch.Tensor, D: float, dx: float, dt: float, n_steps: int =
     ny, nx = u.shape[-2:]
     dy = dx if dy is None else dy
     plan = get_plan(ny, nx, dy, dx, symbol, u.dtype, u.device)
+    if getattr(plan, "general", False):
+        for _ in range(int(n_steps)):  # each step a full transform pair
+            u = plan.apply(u, D, dt, N.MULT_CN)
+        return u
     out = torch.empty_like(u)
     ws = workspace(plan.ws_bytes(1), plan.device)
     N.check("mjx_fft_cn2d", N.lib().mjx_fft_cn2d(
@@ -391,11 +471,26 @@ class SpectralPlan3D:
         self.symbol, self.dtype, self.device = symbol, dtype, _device(device)
         self.code = N.dtype_code(dtype)
         lib = N.lib()
+        self.cgrid = N.Grid3DC(int(nz), int(ny), int(nx), 0, float(dz), float(dy), float(dx))
+        # powers of two >= 2: the fused five-pass form; other lengths: the general path
+        self.general = not all(_pow2(n) and n >= 2 for n in self.shape)
+        if self.general:
+            self.bufs = []
+            for n in self.shape:
+                nb = lib.mjx_dftn_plan_bytes(n, self.code)
+                if nb == 0:
+                    raise ValueError(f"unsupported box {nz}x{ny}x{nx}: lengths must be powers of two <= 4096 "
+                                     "or <= 2048")
+                b = torch.empty(nb, dtype=torch.uint8, device=self.device)
+                with torch.cuda.device(self.device):
+                    N.check("mjx_dftn_plan_init", lib.mjx_dftn_plan_init(N.ptr(b), n, self.code,
+                                                                         N.stream_ptr(self.device)))
+                self.bufs.append(b)
+            return
         nbytes = lib.mjx_spec3d_plan_bytes(*self.shape, self.code)
         if nbytes == 0:
             raise ValueError(f"unsupported box {nz}x{ny}x{nx}: sizes must be powers of two in [2, 4096]")
         self.buf = torch.empty(nbytes, dtype=torch.uint8, device=self.device)
-        self.cgrid = N.Grid3DC(int(nz), int(ny), int(nx), 0, float(dz), float(dy), float(dx))
         with torch.cuda.device(self.device):
             N.check("mjx_spec3d_plan_init", lib.mjx_spec3d_plan_init(
                 N.ptr(self.buf), C.byref(self.cgrid), SYMBOLS[symbol], self.code, N.stream_ptr(self.device)))
@@ -407,8 +502,15 @@ class SpectralPlan3D:
         if tuple(u.shape) != self.shape or u.dtype != self.dtype:
             raise ValueError(f"expected {self.shape} {self.dtype}, got {tuple(u.shape)} {u.dtype}")
         lib = N.lib()
-        ws = workspace(lib.mjx_spec3d_ws_bytes(*self.shape, self.code), self.device, "spec3d")
         out = torch.empty_like(u)
+        if self.general:
+            ws = workspace(lib.mjx_spectral_general3d_ws_bytes(*self.shape, self.code), self.device, "general3d")
+            N.check("mjx_spectral_apply_general3d", lib.mjx_spectral_apply_general3d(
+                N.ptr(self.bufs[0]), N.ptr(self.bufs[1]), N.ptr(self.bufs[2]), C.byref(self.cgrid),
+                SYMBOLS[self.symbol], self.code, float(D), float(h), int(mult), int(n_steps), N.ptr(u),
+                N.ptr(out), N.ptr(ws), ws.numel(), N.stream_ptr(self.device)))
+            return out
+        ws = workspace(lib.mjx_spec3d_ws_bytes(*self.shape, self.code), self.device, "spec3d")
         N.check("mjx_spectral_apply3d", lib.mjx_spectral_apply3d(
             N.ptr(self.buf), C.byref(self.cgrid), self.code, float(D), float(h), int(mult), int(n_steps),
             N.ptr(u), N.ptr(out), N.ptr(ws), ws.numel(), N.stream_ptr(self.device)))

@@ -305,7 +305,7 @@ def test_etd2_second_order_and_phi_switch():
 
 
 @pytest.mark.parametrize("row", [r for r in _load("fft3d_published.json")["experiments"]
-                                 if r["grid_size"] in (32, 48, 64)])
+                                 if r["grid_size"] in (32, 48, 64, 80, 100)])
 def test_fft3d_error_pins(row):
     # benchmarks/results/3d_feasibility.json: N^3, D = 0.1, 10 CN steps to T = 0.01, max error
     cfg = _load("fft3d_published.json")["config"]
