@@ -140,15 +140,19 @@ __global__ void transpose_kernel(const cx<T>* __restrict__ in, cx<T>* __restrict
   const long long b = blockIdx.z;
   const cx<T>* src = in + b * (long long)rows * cols;
   cx<T>* dst = out + b * (long long)rows * cols;
-  const int c0 = blockIdx.x * 32, r0 = blockIdx.y * 32;
-  for (int i = threadIdx.y; i < 32; i += 8) {
-    const int r = r0 + i, c = c0 + threadIdx.x;
-    if (r < rows && c < cols) tile[i][threadIdx.x] = src[(long long)r * cols + c];
-  }
-  __syncthreads();
-  for (int i = threadIdx.y; i < 32; i += 8) {
-    const int c = c0 + i, r = r0 + threadIdx.x;
-    if (r < rows && c < cols) dst[(long long)c * rows + r] = tile[threadIdx.x][i];
+  const int c0 = blockIdx.x * 32;
+  // row tiles in a grid-stride loop (gridDim.y is capped at 65535)
+  for (int r0 = blockIdx.y * 32; r0 < rows; r0 += gridDim.y * 32) {
+    for (int i = threadIdx.y; i < 32; i += 8) {
+      const int r = r0 + i, c = c0 + threadIdx.x;
+      if (r < rows && c < cols) tile[i][threadIdx.x] = src[(long long)r * cols + c];
+    }
+    __syncthreads();
+    for (int i = threadIdx.y; i < 32; i += 8) {
+      const int c = c0 + i, r = r0 + threadIdx.x;
+      if (r < rows && c < cols) dst[(long long)c * rows + r] = tile[threadIdx.x][i];
+    }
+    __syncthreads();
   }
 }
 
@@ -254,7 +258,8 @@ static cudaError_t dft_rows(const DftArgs<T>& a, cudaStream_t s) {
 
 template <typename T>
 static cudaError_t transpose(const cx<T>* in, cx<T>* out, int rows, int cols, int batch, cudaStream_t s) {
-  dim3 grid((cols + 31) / 32, (rows + 31) / 32, batch), block(32, 8);
+  const int ty = (rows + 31) / 32;
+  dim3 grid((cols + 31) / 32, ty < 65535 ? ty : 65535, batch), block(32, 8);
   transpose_kernel<T><<<grid, block, 0, s>>>(in, out, rows, cols);
   return cudaGetLastError();
 }
