@@ -6,7 +6,8 @@
 //   T   transpose                                        [f][x][y]
 //   C   row DFTs of length ny, multiplier, inverse DFTs  [f][x][y]
 //   T   transpose back, inverse row DFTs of length nx, real part
-// A DFT of length n is the shared-memory Stockham FFT when n is a power of two and
+// A DFT of length n is the shared-memory Stockham FFT when n is a power of two, a
+// mixed-radix (2, 3, 4, 5) Stockham FFT when n has no other prime factor, and
 // Bluestein's chirp-z form otherwise: with c[j] = exp(-i pi j^2 / n),
 //   DFT_n(z)[k] = c[k] * IFFT_L( FFT_L(z c) * FFT_L(b) )[k],  b[j] = conj(c[|j|]),
 // a circular convolution of length L = 2^ceil(log2(2n - 1)) <= 4096 (n <= 2048).
@@ -29,21 +30,34 @@ void set_last_error(cudaError_t e, const char* file, int line);
 static inline size_t g256(size_t b) { return (b + 255) & ~size_t(255); }
 
 struct DftGeom {
-  int n, L, log2L, bluestein;
+  int n, L, log2L, bluestein, mixed, nrad;
+  int rad[16];
   size_t tw, chirp, bhat, total;
 };
+
+// radices 4, 2, 3, 5 covering n, or 0 if n has another prime factor
+static int radix_plan(int n, int* rad) {
+  int m = n, k = 0;
+  const int rs[4] = {4, 2, 3, 5};
+  for (int i = 0; i < 4; ++i)
+    while (m % rs[i] == 0 && k < 16) { rad[k++] = rs[i]; m /= rs[i]; }
+  return m == 1 ? k : 0;
+}
 
 static DftGeom dft_geom(int n, int elem) {
   DftGeom g;
   memset(&g, 0, sizeof(g));
   g.n = n;
-  g.bluestein = ilog2_exact(n) < 0;
+  const bool pow2 = ilog2_exact(n) >= 0;
+  g.nrad = pow2 ? 0 : radix_plan(n, g.rad);
+  g.mixed = !pow2 && g.nrad > 0;
+  g.bluestein = !pow2 && !g.mixed;
   g.L = n;
   if (g.bluestein) {
     g.L = 1;
     while (g.L < 2 * n - 1) g.L <<= 1;
   }
-  g.log2L = ilog2_exact(g.L);
+  g.log2L = g.mixed ? 0 : ilog2_exact(g.L);
   const size_t c = 2 * (size_t)elem;
   size_t o = 0;
   g.tw = o; o += g256(g.L * c);
@@ -85,12 +99,99 @@ template <typename T>
 struct DftArgs {
   cx<T>* data;        // rows of n complex values, row stride ld
   long long nrows, ld;
-  const cx<T>* tw;    // length-L twiddles
+  const cx<T>* tw;    // length-L twiddles (mixed radix: exp(-2 pi i m / n), m < n)
   const cx<T>* chirp; // length n
   const cx<T>* bhat;  // length L, FFT_L(b) / L
   int n, L, log2L, bluestein, nseq, inverse;
+  int mixed, nrad, tpsm;  // mixed radix: passes and threads per sequence
+  int rad[16];
   T scale;
 };
+
+// small forward DFTs in registers (w = exp(-2 pi i / r)); the constants are cos/sin of
+// 2 pi/3, 2 pi/5, 4 pi/5
+template <typename C>
+__device__ __forceinline__ void sdft(C* v, int r) {
+  typedef decltype(C::x) R;
+  if (r == 2) {
+    const C a = v[0], b = v[1];
+    v[0] = cadd(a, b); v[1] = csub(a, b);
+  } else if (r == 3) {
+    const R h = (R)0.86602540378443864676;  // sin(2 pi / 3)
+    const C a = v[0], t = cadd(v[1], v[2]), d = csub(v[1], v[2]);
+    const C m = mk<C>(a.x - (R)0.5 * t.x, a.y - (R)0.5 * t.y);
+    const C q = mk<C>(h * d.y, -h * d.x);  // -i h d
+    v[0] = cadd(a, t); v[1] = cadd(m, q); v[2] = csub(m, q);
+  } else if (r == 4) {
+    const C a = v[0], b = v[1], c = v[2], d = v[3];
+    const C s0 = cadd(a, c), s1 = csub(a, c), t0 = cadd(b, d), t1 = csub(b, d);
+    const C jt1 = mk<C>(t1.y, -t1.x);  // -i (b - d)
+    v[0] = cadd(s0, t0); v[2] = csub(s0, t0); v[1] = cadd(s1, jt1); v[3] = csub(s1, jt1);
+  } else {  // r == 5
+    const R c1 = (R)0.30901699437494742410, c2 = (R)-0.80901699437494742410;
+    const R s1 = (R)0.95105651629515357212, s2 = (R)0.58778525229247312917;
+    const C a = v[0];
+    const C t1 = cadd(v[1], v[4]), t2 = cadd(v[2], v[3]), t3 = csub(v[1], v[4]), t4 = csub(v[2], v[3]);
+    const C m1 = mk<C>(a.x + c1 * t1.x + c2 * t2.x, a.y + c1 * t1.y + c2 * t2.y);
+    const C m2 = mk<C>(a.x + c2 * t1.x + c1 * t2.x, a.y + c2 * t1.y + c1 * t2.y);
+    const C n1 = mk<C>(s1 * t3.x + s2 * t4.x, s1 * t3.y + s2 * t4.y);
+    const C n2 = mk<C>(s2 * t3.x - s1 * t4.x, s2 * t3.y - s1 * t4.y);
+    v[0] = mk<C>(a.x + t1.x + t2.x, a.y + t1.y + t2.y);
+    v[1] = mk<C>(m1.x + n1.y, m1.y - n1.x);  // m1 - i n1
+    v[4] = mk<C>(m1.x - n1.y, m1.y + n1.x);  // m1 + i n1
+    v[2] = mk<C>(m2.x + n2.y, m2.y - n2.x);
+    v[3] = mk<C>(m2.x - n2.y, m2.y + n2.x);
+  }
+}
+
+// Mixed-radix Stockham DFT of lengths n = 2^a 3^b 5^c: pass (r, p) maps butterfly j
+// (k = j mod p) from src[j + t n/r] to dst[(j - k) r + k + t p] after the twiddles
+// w^(k t), w = exp(-2 pi i / (p r)); two shared buffers alternate between passes.
+template <typename T>
+__global__ void __launch_bounds__(256) dft_mixed_kernel(const __grid_constant__ DftArgs<T> a) {
+  typedef cx<T> C;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int n = a.n, T_ = a.tpsm, tid = threadIdx.x;
+  C* b0 = reinterpret_cast<C*>(smem_raw);
+  C* b1 = b0 + (long long)a.nseq * n;
+  const int s = tid / T_, lt = tid - s * T_;
+  const long long row = (long long)blockIdx.x * a.nseq + s;
+  const bool active = s < a.nseq && row < a.nrows;
+  C* x = a.data + row * a.ld;
+  C* src = b0 + s * n;
+  C* dst = b1 + s * n;
+  if (active)
+    for (int j = lt; j < n; j += T_) {
+      C v = x[j];
+      if (a.inverse) v.y = -v.y;
+      src[j] = v;
+    }
+  __syncthreads();
+  int p = 1;
+  for (int q = 0; q < a.nrad; ++q) {
+    const int r = a.rad[q], nb = n / r, step = n / (p * r);
+    if (active)
+      for (int j = lt; j < nb; j += T_) {
+        const int k = j % p;
+        C v[5];
+        for (int t = 0; t < r; ++t) v[t] = src[j + t * nb];
+        if (p > 1)
+          for (int t = 1; t < r; ++t) v[t] = cmul(v[t], __ldg(&a.tw[k * t * step]));
+        sdft(v, r);
+        const int base = (j - k) * r + k;
+        for (int t = 0; t < r; ++t) dst[base + t * p] = v[t];
+      }
+    __syncthreads();
+    C* tmp = src; src = dst; dst = tmp;
+    p *= r;
+  }
+  if (active)
+    for (int j = lt; j < n; j += T_) {
+      C v = src[j];
+      if (a.inverse) v.y = -v.y;
+      x[j] = mk<C>(v.x * a.scale, v.y * a.scale);
+    }
+}
 
 // nseq rows per CTA, each in its own shared-memory segment of length L
 template <typename T>
@@ -241,14 +342,34 @@ static DftArgs<T> dft_args(const void* plan, int n, cx<T>* data, long long nrows
   a.data = data; a.nrows = nrows; a.ld = ld;
   a.tw = (const cx<T>*)(p + g.tw); a.chirp = (const cx<T>*)(p + g.chirp); a.bhat = (const cx<T>*)(p + g.bhat);
   a.n = n; a.L = g.L; a.log2L = g.log2L; a.bluestein = g.bluestein; a.inverse = inverse;
-  const int tps = g.L >= 16 ? g.L / 16 : 1;
-  a.nseq = tps >= 256 ? 1 : 256 / tps;
+  a.mixed = g.mixed; a.nrad = g.nrad;
+  for (int i = 0; i < 16; ++i) a.rad[i] = g.rad[i];
+  if (g.mixed) {
+    // threads per sequence n/8 in [1, 256]; sequences per CTA within 256 threads and 96 KB
+    int T_ = n / 8;
+    if (T_ < 1) T_ = 1;
+    if (T_ > 256) T_ = 256;
+    a.tpsm = T_;
+    int ns = 256 / T_;
+    const int cap = (int)((96 * 1024) / (2 * (size_t)n * sizeof(cx<T>)));
+    if (ns > cap) ns = cap;
+    a.nseq = ns < 1 ? 1 : ns;
+  } else {
+    const int tps = g.L >= 16 ? g.L / 16 : 1;
+    a.nseq = tps >= 256 ? 1 : 256 / tps;
+  }
   a.scale = (T)(inverse ? 1.0 / n : 1.0);
   return a;
 }
 
 template <typename T>
 static cudaError_t dft_rows(const DftArgs<T>& a, cudaStream_t s) {
+  if (a.mixed) {
+    const long long grid = (a.nrows + a.nseq - 1) / a.nseq;
+    const size_t smem = (size_t)2 * a.nseq * a.n * sizeof(cx<T>);
+    dft_mixed_kernel<T><<<(unsigned)grid, a.nseq * a.tpsm, smem, s>>>(a);
+    return cudaGetLastError();
+  }
   const int tps = a.L >= 16 ? a.L / 16 : 1;
   const long long grid = (a.nrows + a.nseq - 1) / a.nseq;
   const size_t smem = (size_t)sp_size(a.nseq * a.L) * sizeof(cx<T>);
@@ -380,6 +501,8 @@ static mjx_status set_dft_attrs() {
   MJX_CUDA_TRY(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
   MJX_CUDA_TRY(cudaFuncSetAttribute(dft_rows_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
   MJX_CUDA_TRY(cudaFuncSetAttribute(dft_rows_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
+  MJX_CUDA_TRY(cudaFuncSetAttribute(dft_mixed_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
+  MJX_CUDA_TRY(cudaFuncSetAttribute(dft_mixed_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
   done = 1;
   return MJX_OK;
 }
@@ -407,7 +530,7 @@ mjx_status mjx_dftn_plan_init(void* plan, int n, int dtype, void* stream) {
     else { double* q = (double*)(host.data() + off); q[2 * i] = re; q[2 * i + 1] = im; }
   };
   const double twopi = 6.283185307179586476925286766559, pi = 0.5 * twopi;
-  for (int j = 0; j < g.L; ++j) put(g.tw, j, cos(twopi * j / g.L), -sin(twopi * j / g.L));
+  for (int j = 0; j < g.L; ++j) put(g.tw, j, cos(twopi * j / g.L), -sin(twopi * j / g.L));  // L = n when mixed
   if (g.bluestein) {
     std::vector<double> cre(n), cim(n);
     for (int j = 0; j < n; ++j) {  // exp(-i pi j^2 / n), j^2 reduced mod 2n to keep the angle exact
