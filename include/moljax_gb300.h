@@ -240,6 +240,13 @@ mjx_status mjx_unpad2d(const void* padded, void* interior, int nfields, int ny, 
 mjx_status mjx_laplacian2d(const void* padded_in, void* padded_out, int nfields, int ny, int nx,
                            int n_ghost, const double* coef, int fill_bc, const int* kinds,
                            const double* values, double dy, double dx, int dtype, void* stream);
+/* Reaction step of length h on interior fields [nfields][n]: Heun (euler = 0, the reaction
+ * stage of imex_strang_step, moljax/core/stepping.py:370-435), explicit Euler (euler = 1,
+ * imex_euler_step 317-367) or the rates N(y) themselves (euler = 2); Gray-Scott (nfields 2),
+ * Fisher-KPP r u (1-u) per field, or none (a copy; rates zero).  in may equal out. */
+mjx_status mjx_reaction_step2d(const void* in, void* out, int nfields, long long n, int reaction, double F,
+                               double k, double r, double h, int euler, int dtype, void* stream);
+
 /* div(D grad u) with face-averaged D on the interior of one padded field, ghosts zero
  * (apply_variable_diffusion_2d, moljax/core/variable_coeff.py:232-287).  D is padded like u,
  * or interior-shaped [ny][nx] (d_interior = 1) and edge-extended.  out must not alias u. */

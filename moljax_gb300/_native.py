@@ -154,6 +154,7 @@ SIGNATURES = {
     "mjx_etdrk4_ws_bytes": (_sz, [_i, _i, _i]),
     "mjx_etdrk4_gray_scott2d": (_i, [_vp, C.POINTER(Grid2DC), _i, _i, C.POINTER(C.c_double), _d, _d,
                                      _d, _d, _i, _vp, _vp, _vp, _sz, _i, _vp]),
+    "mjx_reaction_step2d": (_i, [_vp, _vp, _i, C.c_longlong, _i, _d, _d, _d, _d, _i, _i, _vp]),
     "mjx_variable_diffusion2d": (_i, [_vp, _vp, _i, _vp, _i, _i, _i, _d, _d, _i, _vp]),
     "mjx_advdiff_op2d": (_i, [_vp, C.POINTER(Grid2DC), _i, _i, C.POINTER(C.c_double), C.POINTER(C.c_double),
                               C.POINTER(C.c_double), _d, _i, _vp, _vp, _vp, _sz, _vp]),

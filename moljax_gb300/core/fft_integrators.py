@@ -89,19 +89,15 @@ class NativeNonlinear:
             "a Gray-Scott or Fisher-KPP reaction); arbitrary Python callables are not run")
 
     def __call__(self, state: Dict[str, torch.Tensor], t: float = 0.0) -> Dict[str, torch.Tensor]:
+        """N on the fields (any shape), one pointwise native kernel."""
         names = _field_order(state, self)
-        y, is2d = _pack(state, names)
+        y = torch.stack([state[n] for n in names]).contiguous()
         N.require_cuda(y)
-        (ny, nx, dy, dx), _ = _grid_of(state, names, {})
-        plan = get_plan(ny, nx, dy, dx, "fd", y.dtype, y.device)
         out = torch.empty_like(y)
-        cg = N.Grid2DC(ny, nx, dy, dx)
-        for g in _groups(names):
-            sl = slice(g[0], g[-1] + 1)
-            N.check("mjx_etd_nonlinear2d", N.lib().mjx_etd_nonlinear2d(
-                N.ptr(plan.buf), C.byref(cg), plan.code, self.kind, len(g), self.F, self.k, self.r,
-                N.ptr(y[sl]), N.ptr(out[sl]), N.stream_ptr(plan.device)))
-        return _unpack(out, names, is2d)
+        N.check("mjx_reaction_step2d", N.lib().mjx_reaction_step2d(
+            N.ptr(y), N.ptr(out), len(names), y[0].numel(), self.kind, self.F, self.k, self.r, 0.0, 2,
+            N.dtype_code(y.dtype), N.stream_ptr(y.device)))
+        return {n: out[i] for i, n in enumerate(names)}
 
 
 def _field_order(state, nl: NativeNonlinear):

@@ -93,12 +93,54 @@ def imex_euler_step(model, y, t, dt, fft_cache, diffusivities):
     return _imex_step(model, y, t, dt, fft_cache, diffusivities, False)
 
 
+# ------------------------------------------------------------------ grids of any size
+def _reaction_args(model):
+    rx = model.reaction_kind
+    p = model.params
+    return rx, float(p.get("F", 0.0)), float(p.get("k", 0.0)), float(p.get("r", 1.0))
+
+
+def _imex_interior_general(model, plan, interior, dt, diffusivities, use_strang):
+    """One IMEX step on interiors (nf, ny, nx) of a grid of any size: the general spectral
+    plan for H, the native Heun / Euler reaction kernels for R (the reaction is pointwise and
+    H acts on interiors, so the intermediate ghost fills of the reference change nothing)."""
+    names = model.field_names
+    D = [float(diffusivities.get(n, 0.0)) for n in names]
+    diffusive = [i for i, d in enumerate(D) if d > 1e-14]
+
+    def H(x, h):
+        out = x.clone()
+        if diffusive:
+            sel = torch.tensor(diffusive, device=x.device)
+            out[sel] = plan.apply(x[sel].contiguous(), [D[i] for i in diffusive], h, N.MULT_HELMHOLTZ)
+        return out
+
+    rx, F, k, r = _reaction_args(model)
+    nf = interior.shape[0]
+    npts = interior[0].numel()
+
+    def react(x, h, euler):
+        out = torch.empty_like(x)
+        N.check("mjx_reaction_step2d", N.lib().mjx_reaction_step2d(
+            N.ptr(x), N.ptr(out), nf, npts, rx, F, k, r, float(h), int(euler), N.dtype_code(x.dtype),
+            N.stream_ptr(x.device)))
+        return out
+
+    if use_strang:  # H(dt/2) R_heun(dt) H(dt/2)
+        return H(react(H(interior, 0.5 * dt), dt, 0), 0.5 * dt)
+    return H(react(interior, dt, 1), dt)  # H(dt) (y + dt N(y))
+
+
 def _imex_step(model, y, t, dt, fft_cache, diffusivities, use_strang):
     _periodic_only(model)
     grid = model.grid
     names = model.field_names
     interior = stencil.unpad(stencil.stack(y, names), grid)
     plan = _plan_of(fft_cache, grid.ny, grid.nx, interior.dtype)
+    if getattr(plan, "general", False):
+        out = _imex_interior_general(model, plan, interior, dt, diffusivities, use_strang)
+        padded = stencil.pad_interior(out, grid, model.bc_spec, names, t + dt, model.params)
+        return {n: padded[i] for i, n in enumerate(names)}
     prob = _problem(model, diffusivities, CFLParams(), use_strang=use_strang)
     lib = N.lib()
     ws = workspace(lib.mjx_imex2d_ws_bytes(grid.ny, grid.nx, len(names), plan.code), plan.device,
@@ -163,6 +205,12 @@ def adaptive_integrate_imex(model, y0, t0, t_end, dt0, fft_cache=None, diffusivi
         fft_cache = model.metadata.get("fft_cache") or create_fft_cache(grid, model.dtype)
     interior = stencil.unpad(stencil.stack(y0, names), grid)
     plan = _plan_of(fft_cache, grid.ny, grid.nx, interior.dtype)
+    if getattr(plan, "general", False):
+        if precision == "mixed":
+            raise NotImplementedError("the mixed-precision form needs a power-of-two grid")
+        return _adaptive_imex_general(model, interior, plan, diffusivities, use_strang, t0, t_end, dt0,
+                                      max_steps, cfl_params, pid_params, save_every, save_y_history,
+                                      max_attempts)
     prob = _problem(model, diffusivities, cfl_params, max_attempts, use_strang)
     if precision is None:
         precision = "fp64" if interior.dtype == torch.float64 else "fp32"
@@ -204,6 +252,77 @@ def adaptive_integrate_imex(model, y0, t0, t_end, dt0, fft_cache=None, diffusivi
     y_history = ({n: y_hist[:, i] for i, n in enumerate(names)} if y_hist is not None else None)
     return AdaptiveResult(res.t_final, y_fin, t_hist, y_history, dt_hist, res.n_saved,
                           res.n_accepted, res.n_rejected, res.status)
+
+
+def _adaptive_imex_general(model, interior, plan, diffusivities, use_strang, t0, t_end, dt0, max_steps,
+                           cfl_params, pid_params, save_every, save_y_history, max_attempts):
+    """The adaptive IMEX loop on a grid of any size: the same step doubling, error norm, PI
+    controller with the IMEX CFL limit and accept/reject rules as the device loop
+    (stepping.py:1146-1371), with the native general-size steps; the controller runs on the
+    host (one scalar read per attempt)."""
+    from moljax_gb300.core.dt_policy import ControllerState, imex_cfl_dt, propose_dt_imex
+    from moljax_gb300.core.utils import StatusCode as S
+    grid, names = model.grid, model.field_names
+    order = 2 if use_strang else 1
+    dev = interior.device
+    dt = min(float(dt0), imex_cfl_dt(grid, model.params, cfl_params))
+    max_saves = max_steps // save_every + 1
+    t_hist = torch.zeros(max_saves, dtype=torch.float64, device=dev)
+    dt_hist = torch.zeros(max_saves, dtype=torch.float64, device=dev)
+    if save_y_history == "host":
+        y_hist = torch.empty((max_saves,) + tuple(interior.shape), dtype=interior.dtype, pin_memory=True)
+    elif save_y_history:
+        y_hist = torch.empty((max_saves,) + tuple(interior.shape), dtype=interior.dtype, device=dev)
+    else:
+        y_hist = None
+    t_hist[0] = t0
+    if y_hist is not None:
+        y_hist[0].copy_(interior)
+    lib = N.lib()
+    ews = workspace(lib.mjx_error_norm_ws_bytes(), dev, "errnorm")
+    res = (C.c_double * 2)()
+    cap = max_attempts if max_attempts and max_attempts > 0 else 20 * max_steps + 1000
+
+    def step(x, h):
+        return _imex_interior_general(model, plan, x, h, diffusivities, use_strang)
+
+    t, y, cs = float(t0), interior, ControllerState(1.0, 1.0, 0)
+    write_idx, n_acc, n_rej, status, attempts = 1, 0, 0, S.RUNNING, 0
+    while status == S.RUNNING and t < t_end and write_idx < max_saves and attempts < cap:
+        attempts += 1
+        dtc = min(dt, t_end - t)
+        y_full = step(y, dtc)
+        y_half = step(step(y, 0.5 * dtc), 0.5 * dtc)
+        err = y_half - y_full
+        N.check("mjx_scaled_error_norm", lib.mjx_scaled_error_norm(
+            N.ptr(err), N.ptr(y_half), err.numel(), N.dtype_code(err.dtype), float(pid_params.atol),
+            float(pid_params.rtol), res, N.ptr(ews), ews.numel(), N.stream_ptr(dev)))
+        e, finite = max(float(res[0]), 1e-10), res[1] != 0.0
+        dt_new, cs_new = propose_dt_imex(grid, model.params, None, t, dtc, e, cs, cfl_params, pid_params, order)
+        if e <= 1.0 and finite:
+            if n_acc % save_every == 0:
+                t_hist[write_idx] = t + dtc
+                dt_hist[write_idx - 1] = dtc
+                if y_hist is not None:
+                    y_hist[write_idx].copy_(y_half)
+                write_idx += 1
+            t, y, dt, cs = t + dtc, y_half, dt_new, cs_new
+            n_acc += 1
+        else:
+            dt = max(dt_new * 0.5, pid_params.dt_min)
+            if dt <= pid_params.dt_min * 1.1:
+                status = S.DT_TOO_SMALL
+            n_rej += 1
+        if not finite:
+            status = S.NON_FINITE_VALUES
+    if t >= t_end:  # as the device controller ends the loop
+        status = S.SUCCESS
+    elif write_idx >= max_saves or status == S.RUNNING:
+        status = S.MAX_STEPS_REACHED
+    padded = stencil.pad_interior(y, grid, model.bc_spec, names, t, model.params)
+    y_fin = {n: padded[i] for i, n in enumerate(names)}
+    y_history = ({n: y_hist[:, i] for i, n in enumerate(names)} if y_hist is not None else None)
+    return AdaptiveResult(t, y_fin, t_hist, y_history, dt_hist, write_idx, n_acc, n_rej, status)
 
 
 def _adaptive_mixed(model, interior, plan, prob, pid_params, t0, t_end, dt0, max_steps,
@@ -615,28 +734,28 @@ def step_explicit_with_error(model, y, t, dt, method: int):
 
 def imex_ssprk2_step(model, y, t, dt, fft_cache, diffusivities):
     """IMEX-SSPRK2 (stepping.py:438-495): y1 = H(dt)(y + dt N(y)), y2 = H(dt)(y1 + dt N(y1)),
-    y_new = (y + y2)/2, the BCs applied after each stage.  N is the model's reaction by the
-    native row pass (on the interiors; every ghost is refilled by the BCs), H the native
-    Helmholtz pass."""
-    from moljax_gb300.core.fft_integrators import NativeNonlinear
+    y_new = (y + y2)/2, the BCs applied after each stage.  y + dt N(y) is the native
+    Euler reaction kernel (on the interiors; every ghost is refilled by the BCs), H the
+    Helmholtz pass of the grid's spectral plan (any size)."""
     from moljax_gb300.core.fft_solvers import apply_diffusion_inverse_fft
     grid = model.grid
-    nl = NativeNonlinear.of(model)
-    sl = grid.interior_slice
-
-    def N(state):
-        r = nl({k: v[sl] for k, v in state.items()})
-        out = {k: torch.zeros_like(v) for k, v in state.items()}
-        for k in out:
-            out[k][sl] = r[k]
-        return out
+    names = model.field_names
+    rx, F, k, r = _reaction_args(model)
 
     def stage(z, tt):
-        n = N(z)
-        rhs = {k: z[k] + dt * n[k] for k in z}
+        inter = stencil.unpad(stencil.stack(z, names), grid)
+        out = torch.empty_like(inter)
+        N.check("mjx_reaction_step2d", N.lib().mjx_reaction_step2d(
+            N.ptr(inter), N.ptr(out), len(names), inter[0].numel(), rx, F, k, r, float(dt), 1,
+            N.dtype_code(out.dtype), N.stream_ptr(out.device)))
+        rhs = dict(z)
+        for i, n in enumerate(names):
+            rr = z[n].clone()
+            rr[grid.interior_slice] = out[i]
+            rhs[n] = rr
         return model.apply_bcs(apply_diffusion_inverse_fft(rhs, grid, dt, diffusivities, fft_cache), tt)
 
     y = model.apply_bcs(y, t)
     y1 = stage(y, t + dt)
     y2 = stage(y1, t + dt)
-    return model.apply_bcs({k: 0.5 * y[k] + 0.5 * y2[k] for k in y}, t + dt)
+    return model.apply_bcs({k_: 0.5 * y[k_] + 0.5 * y2[k_] for k_ in y}, t + dt)

@@ -247,6 +247,42 @@ __global__ void vardiff2d_kernel(const T* __restrict__ u, const T* __restrict__ 
   }
 }
 
+// Reaction step of length h on interior fields [nf][n]: Heun R1 = N(y), R2 = N(y + h R1),
+// y + h/2 (R1 + R2) (the reaction stage of imex_strang_step, moljax/core/stepping.py:370-435),
+// explicit Euler y + h N(y) (imex_euler_step, 317-367), or the rates N(y) (mode 2);
+// Gray-Scott couples fields 0 and 1, Fisher-KPP acts on each field, none has N = 0.
+template <typename T>
+__global__ void heun2d_kernel(const T* __restrict__ in, T* __restrict__ out, int nf, long long n, int rx,
+                              double F, double k, double r, double h, int euler) {
+  const T pF = (T)F, pK = (T)k, pR = (T)r, th = (T)h, hh = (T)(0.5 * h);
+  const long long total = rx == MJX_REACT_GRAY_SCOTT ? n : n * nf;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+       i += (long long)gridDim.x * blockDim.x) {
+    if (rx == MJX_REACT_GRAY_SCOTT) {
+      const T u = in[i], v = in[n + i];
+      const T a = u * v * v;
+      const T r1u = -a + pF * ((T)1 - u), r1v = a - (pF + pK) * v;
+      if (euler == 2) { out[i] = r1u; out[n + i] = r1v; continue; }
+      const T ut = u + th * r1u, vt = v + th * r1v;
+      if (euler) { out[i] = ut; out[n + i] = vt; continue; }
+      const T b = ut * vt * vt;
+      const T r2u = -b + pF * ((T)1 - ut), r2v = b - (pF + pK) * vt;
+      out[i] = u + hh * (r1u + r2u);
+      out[n + i] = v + hh * (r1v + r2v);
+    } else if (rx == MJX_REACT_FISHER) {
+      const T u = in[i];
+      const T r1 = pR * u * ((T)1 - u);
+      if (euler == 2) { out[i] = r1; continue; }
+      const T ut = u + th * r1;
+      if (euler) { out[i] = ut; continue; }
+      const T r2 = pR * ut * ((T)1 - ut);
+      out[i] = u + hh * (r1 + r2);
+    } else {
+      out[i] = euler == 2 ? (T)0 : in[i];
+    }
+  }
+}
+
 // scaled error partials over n values: sum (e / (atol + rtol |y|))^2 and non-finite flags of y
 template <typename T>
 __global__ void errnorm_partials(const T* __restrict__ e, const T* __restrict__ y, long long n,
@@ -312,6 +348,25 @@ mjx_status mjx_variable_diffusion2d(const void* u_padded, const void* D, int d_i
   else
     vardiff2d_kernel<double><<<grid_for(total), 256, 0, s>>>((const double*)u_padded, (const double*)D,
                                                              (double*)out_padded, ny, nx, n_ghost, d_interior, dy, dx);
+  return cuda_status(cudaGetLastError());
+}
+
+mjx_status mjx_reaction_step2d(const void* in, void* out, int nfields, long long n, int reaction, double F,
+                               double k, double r, double h, int euler, int dtype, void* stream) {
+  const int e = elem_size(dtype);
+  if (!e) return MJX_BAD_DTYPE;
+  if (!in || !out || nfields < 1 || n < 1) return MJX_BAD_ARG;
+  if (reaction != MJX_REACT_NONE && reaction != MJX_REACT_GRAY_SCOTT && reaction != MJX_REACT_FISHER)
+    return MJX_BAD_ARG;
+  if (reaction == MJX_REACT_GRAY_SCOTT && nfields != 2) return MJX_BAD_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  const long long total = (long long)nfields * n;
+  if (e == 4)
+    heun2d_kernel<float><<<grid_for(total), 256, 0, s>>>((const float*)in, (float*)out, nfields, n, reaction, F, k, r, h,
+                                                         euler);
+  else
+    heun2d_kernel<double><<<grid_for(total), 256, 0, s>>>((const double*)in, (double*)out, nfields, n, reaction, F, k, r,
+                                                          h, euler);
   return cuda_status(cudaGetLastError());
 }
 

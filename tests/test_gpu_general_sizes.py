@@ -93,10 +93,36 @@ def test_general_1d_operators(cuda, n):
                                atol=1e-11 * max(1.0, float(np.max(np.abs(lam_a)))))
 
 
-def test_fused_drivers_reject_general_sizes(cuda):
+@pytest.mark.parametrize("shape", [(48, 48), (30, 50)])
+def test_imex_general_size_vs_oracle(cuda, shape):
+    """adaptive_integrate_imex and the Strang / Euler / SSPRK2 steps on grids of other sizes
+    against the FP64 oracle (identical accept/reject counts)."""
     import moljax_gb300 as M
-    grid = M.Grid2D(48, 48, 0.0, 2.5, 0.0, 2.5)
+    from oracle import imex as OI
+    from oracle import mol
+    ny, nx = shape
+    grid = M.Grid2D(nx, ny, 0.0, 2.5, 0.0, 2.5)
     model, cache, diff = M.create_gray_scott_periodic_fft(grid, 2e-5, 1e-5, 0.035, 0.065, torch.float64, cuda)
-    y = model.create_initial_state(fill_values={"u": 1.0, "v": 0.0}, device=cuda)
-    with pytest.raises(Exception):
-        M.adaptive_integrate_imex(model, y, 0.0, 1.0, 0.1, cache, diff)
+    og = mol.Grid2D(nx, ny, 0, 2.5, 0, 2.5)
+    y0 = mol.gray_scott_ic(og, 4)
+    ym = {k: torch.tensor(v, device=cuda) for k, v in y0.items()}
+    om, lam, od = OI.gray_scott_periodic(og, 2e-5, 1e-5, 0.035, 0.065)
+    for fn, ofn in ((M.imex_strang_step, OI.imex_strang_step), (M.imex_euler_step, OI.imex_euler_step),
+                    (M.imex_ssprk2_step, OI.imex_ssprk2_step)):
+        a = fn(model, ym, 0.0, 0.8, cache, diff)
+        b = ofn(om, y0, 0.8, lam, od)
+        for k in ("u", "v"):
+            assert float(np.max(np.abs(a[k].cpu().numpy() - b[k]))) < 1e-13
+    pid = M.PIDParams(atol=1e-7, rtol=1e-5)
+    r = M.adaptive_integrate_imex(model, ym, 0.0, 30.0, 1.0, cache, diff, pid_params=pid, save_every=1,
+                                  max_steps=2000)
+    ro = OI.adaptive_integrate_imex(om, y0, 0.0, 30.0, 1.0, lam, od, pid=OI.PIDParams(atol=1e-7, rtol=1e-5),
+                                    save_every=1, max_steps=2000)
+    assert r.status == ro.status == 0
+    assert (r.n_accepted, r.n_rejected) == (ro.n_accepted, ro.n_rejected)
+    for k in ("u", "v"):
+        assert float(np.max(np.abs(r.y_final[k].cpu().numpy() - ro.y_final[k]))) < 1e-10
+    nh = ro.n_steps
+    np.testing.assert_allclose(r.t_history.cpu().numpy()[:nh], ro.t_history[:nh], rtol=1e-9)
+    with pytest.raises(NotImplementedError):
+        M.adaptive_integrate_imex(model, ym, 0.0, 1.0, 0.1, cache, diff, precision="mixed")
