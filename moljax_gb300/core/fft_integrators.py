@@ -149,6 +149,8 @@ def _run(y: torch.Tensor, grid, symbol: int, D, nl: NativeNonlinear, method: int
         raise NotImplementedError("the native ETD path takes one or two fields per call")
     ny, nx, dy, dx = grid
     plan = get_plan(ny, nx, dy, dx, "fd", y.dtype, y.device)
+    if getattr(plan, "general", False):
+        return _run_general(plan, y, grid, symbol, D, nl, method, coeffs, dt, n_steps, nprev, want_n, f2_factor)
     lib = N.lib()
     ws = workspace(lib.mjx_etdrk4_ws_bytes(ny, nx, plan.code), plan.device, tag)
     pb = N.ETDProblemC()
@@ -170,6 +172,104 @@ def _run(y: torch.Tensor, grid, symbol: int, D, nl: NativeNonlinear, method: int
         N.ptr(nprev) if nprev is not None else None, N.ptr(out), N.ptr(n_out) if want_n else None,
         N.ptr(ws), ws.numel(), recompute, N.stream_ptr(plan.device)))
     return out, n_out
+
+
+# ------------------------------------------------------------------ grids of any size
+def _phi_ref(z: torch.Tensor):
+    """phi1, phi2, phi3 as fft_integrators.py:39-78 evaluates them (Taylor below |z| = 1e-4)."""
+    small = z.abs() < 1e-4
+    zs = torch.where(small, torch.ones_like(z), z)  # keeps the unused branch finite
+    ez = torch.exp(z)
+    p1 = torch.where(small, 1.0 + z / 2.0 + z ** 2 / 6.0 + z ** 3 / 24.0, (ez - 1.0) / zs)
+    p2 = torch.where(small, 0.5 + z / 6.0 + z ** 2 / 24.0 + z ** 3 / 120.0, (ez - 1.0 - z) / (zs * zs))
+    p3 = torch.where(small, 1.0 / 6.0 + z / 24.0 + z ** 2 / 120.0 + z ** 3 / 720.0,
+                     (ez - 1.0 - z - z ** 2 / 2.0) / (zs * zs * zs))
+    return p1, p2, p3
+
+
+def _symbol_full(ny, nx, dy, dx, symbol, device):
+    """The Laplacian symbol on the full (ny, nx) spectrum in FFT order (FD or spectral;
+    with MJX_SYMBOL_X_ONLY no y part)."""
+    kind = symbol & 1
+    kx = 2 * math.pi * torch.fft.fftfreq(nx, d=dx, dtype=torch.float64, device=device)
+    ky = 2 * math.pi * torch.fft.fftfreq(ny, d=dy, dtype=torch.float64, device=device)
+    if kind == N.SYMBOL_FD:
+        lx, ly = (2.0 * torch.cos(kx * dx) - 2.0) / dx ** 2, (2.0 * torch.cos(ky * dy) - 2.0) / dy ** 2
+    else:
+        lx, ly = -kx ** 2, -ky ** 2
+    if symbol & N.SYMBOL_X_ONLY:
+        ly = torch.zeros_like(ly)
+    return ly[:, None] + lx[None, :]
+
+
+def _etd_tables(lam, Df, dt, method, coeffs, f2_factor):
+    """Per-field coefficient tables on the full spectrum: ETD1/ETD2 (E, dt phi1, dt phi2);
+    ETDRK4 (E, E2, Q, f1, f2, f3) from the phi functions or the 32-point contour mean."""
+    z = dt * Df * lam
+    if method != N.ETD_RK4:
+        p1, p2, _ = _phi_ref(z)
+        return torch.exp(z), dt * p1, dt * p2
+    if coeffs == N.ETD_COEFF_PHI:
+        p1, p2, p3 = _phi_ref(z)
+        h1, _, _ = _phi_ref(z / 2.0)
+        return (torch.exp(z), torch.exp(z / 2.0), dt / 2.0 * h1, dt * (p1 - 3.0 * p2 + 4.0 * p3),
+                dt * (2.0 * p2 - 4.0 * p3), dt * (-p2 + 4.0 * p3))
+    M = 32
+    r = torch.exp(1j * math.pi * (torch.arange(1, M + 1, dtype=torch.float64, device=lam.device) - 0.5) / M)
+    LR = z.to(torch.complex128)[..., None] + r
+    mean = lambda x: torch.real(x.mean(dim=-1))  # noqa: E731
+    Q = dt * mean((torch.exp(LR / 2) - 1) / LR)
+    f1 = dt * mean((-4 - LR + torch.exp(LR) * (4 - 3 * LR + LR ** 2)) / LR ** 3)
+    f2 = dt * mean((2 + LR + torch.exp(LR) * (-2 + LR)) / LR ** 3)
+    f3 = dt * mean((-4 - 3 * LR - LR ** 2 + torch.exp(LR) * (4 - LR)) / LR ** 3)
+    return torch.exp(z), torch.exp(z / 2.0), Q, f1, f2_factor * f2, f3
+
+
+def _run_general(plan, y, grid, symbol, D, nl, method, coeffs, dt, n_steps, nprev, want_n, f2_factor):
+    """ETD steps on a grid of any size: each spectral product real(ifft2(T fft2(x))) is one
+    native table-multiplier pass of the general plan, the nonlinear term the pointwise
+    reaction kernel; the updates combine the passes as fft_integrators.py:119-341 combine
+    the spectra."""
+    ny, nx, dy, dx = grid
+    nf = y.shape[0]
+    lam = _symbol_full(ny, nx, dy, dx, symbol, y.device)
+    tabs = [tuple(t.to(y.dtype).contiguous() for t in _etd_tables(lam, float(D[f]), dt, method, coeffs, f2_factor))
+            for f in range(nf)]
+
+    def mul(x, idx):  # x (nf, ny, nx): field f times table idx of field f
+        return torch.stack([plan.apply(x[f].contiguous(), 1.0, 1.0, N.MULT_TABLE, table=tabs[f][idx])
+                            for f in range(nf)])
+
+    def Nf(x):
+        out = torch.empty_like(x)
+        N.check("mjx_reaction_step2d", N.lib().mjx_reaction_step2d(
+            N.ptr(x), N.ptr(out), nf, x[0].numel(), nl.kind, nl.F, nl.k, nl.r, 0.0, 2, N.dtype_code(x.dtype),
+            N.stream_ptr(x.device)))
+        return out
+
+    u = y.contiguous()
+    Np = nprev.contiguous() if nprev is not None else None
+    n_out = None
+    for i in range(int(n_steps)):
+        Nu = Nf(u)
+        if want_n and i == n_steps - 1:
+            n_out = Nu.clone()
+        if method == N.ETD_1 or (method == N.ETD_2 and Np is None):
+            u_new = mul(u, 0) + mul(Nu, 1)
+        elif method == N.ETD_2:
+            u_new = mul(u, 0) + mul(Nu, 1) + mul(Nu - Np, 2)
+        else:
+            a = mul(u, 1) + mul(Nu, 2)
+            Na = Nf(a)
+            b = mul(u, 1) + mul(Na, 2)
+            Nb = Nf(b)
+            c = mul(a, 1) + mul(2.0 * Nb - Nu, 2)
+            Nc = Nf(c)
+            u_new = mul(u, 0) + mul(Nu, 3) + mul(Na + Nb, 4) + mul(Nc, 5)
+        if method == N.ETD_2:
+            Np = Nu
+        u = u_new
+    return u, n_out
 
 
 def _setup(state, linear_ops, nonlinear_rhs, model=None):

@@ -104,7 +104,8 @@ class GeneralSpectralPlan:
     """Periodic (ny, nx) grid of any supported size (powers of two up to 4096, other sizes up
     to 2048): the full-spectrum path of ``mjx_spectral_apply_general2d`` (row DFTs by
     Stockham or Bluestein, transposes, column DFTs and the multiplier).  Same ``apply`` as
-    ``SpectralPlan``; the FFT-fused drivers (IMEX, ETD) take powers of two."""
+    ``SpectralPlan``; the fused device loops (IMEX, ETD) take powers of two, their
+    host-driven forms run on this plan."""
 
     general = True
 

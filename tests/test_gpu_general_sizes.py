@@ -126,3 +126,41 @@ def test_imex_general_size_vs_oracle(cuda, shape):
     np.testing.assert_allclose(r.t_history.cpu().numpy()[:nh], ro.t_history[:nh], rtol=1e-9)
     with pytest.raises(NotImplementedError):
         M.adaptive_integrate_imex(model, ym, 0.0, 1.0, 0.1, cache, diff, precision="mixed")
+
+
+@pytest.mark.parametrize("method", ["etd1", "etd2", "etdrk4"])
+def test_etd_general_sizes_vs_oracle(cuda, method):
+    import moljax_gb300 as M
+    from oracle import etd as OT
+    from oracle import etdrk4 as OE
+    from oracle import mol
+    # 1D logistic, n = 100
+    g = M.Grid1D.uniform(100, x_min=0.0, x_max=1.0)
+    x = g.x_coords().numpy()
+    u0 = 0.5 + 0.3 * np.sin(2 * np.pi * x)
+    _, h = M.etd_integrate({"u": torch.tensor(u0, device=cuda)}, (0.0, 0.5), 0.05, {"u": M.DiffusionOperator(g, 0.01)},
+                           M.NativeNonlinear.logistic(0.5), method=method, save_every=5)
+    _, ho = OT.etd_integrate({"u": u0}, (0.0, 0.5), 0.05, {"u": 0.01 * OT.fd_symbol_1d(100, g.dx)},
+                             OT.logistic(0.5), method, 5)
+    assert float(np.max(np.abs(h[-1]["u"].cpu().numpy() - ho[-1]["u"]))) < 1e-12
+    # 2D coupled Gray-Scott on 40 x 48
+    ny, nx, L = 40, 48, 2.5
+    grid = M.Grid2D(nx, ny, 0.0, L, 0.0, L)
+    og = mol.Grid2D(nx, ny, 0, L, 0, L)
+    y0 = mol.gray_scott_ic(og, 6)
+    ui, vi = mol.interior(y0["u"], og), mol.interior(y0["v"], og)
+    ops = {"u": M.DiffusionOperator(grid, 2e-5), "v": M.DiffusionOperator(grid, 1e-5)}
+    _, h2 = M.etd_integrate({"u": torch.tensor(ui, device=cuda), "v": torch.tensor(vi, device=cuda)}, (0.0, 4.0), 1.0,
+                            ops, M.NativeNonlinear.gray_scott(0.035, 0.065), method=method, save_every=4)
+    lam = mol.fd_symbol_2d(ny, nx, og.dy, og.dx)
+    _, h2o = OT.etd_integrate({"u": ui, "v": vi}, (0.0, 4.0), 1.0, {"u": 2e-5 * lam, "v": 1e-5 * lam},
+                              OT.gray_scott(0.035, 0.065), method, 4, coupled=True)
+    for f in ("u", "v"):
+        assert float(np.max(np.abs(h2[-1][f].cpu().numpy() - h2o[-1][f]))) < 1e-12
+    if method == "etdrk4":  # the benchmark's contour form on the MOLModel
+        model = M.create_gray_scott_model(grid, 2e-5, 1e-5, 0.035, 0.065)
+        out = M.etdrk4_gray_scott(model, {k: torch.tensor(v, device=cuda) for k, v in y0.items()}, 1.0, 4,
+                                  variant="benchmark")
+        ru, rv = OE.etdrk4_gray_scott(ui, vi, lam, 2e-5, 1e-5, 0.035, 0.065, 1.0, 4, 1.0)
+        assert float(np.max(np.abs(mol.interior(out["u"].cpu().numpy(), og) - ru))) < 1e-12
+        assert float(np.max(np.abs(mol.interior(out["v"].cpu().numpy(), og) - rv))) < 1e-12
