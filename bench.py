@@ -11,6 +11,8 @@ of the reaction increments (rel-L2 vs the FP64 path is reported in the line).
   python bench.py --workload etdrk4 --n 4096 [--etd-steps S] [--kernels-only] [--etd-method etd1|etd2]
   python bench.py --workload serve [--requests R]
   python bench.py --workload fft3d --n 512 [--etd-steps S] [--fp32]
+  python bench.py --workload explicit --n 4096 [--etd-steps S]      (RK4 advection-diffusion)
+  python bench.py --workload nk --n 512 [--etd-steps S]             (BDF2 Newton-Krylov)
 
 Our arm prints one JSON line with the device-timed value, the end-to-end
 number through the public API with host buffers, the live roofline of the
@@ -61,7 +63,7 @@ def parse():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp32"])
     ap.add_argument("--kernels-only", action="store_true")
-    ap.add_argument("--workload", default="imex", choices=["imex", "etdrk4", "serve", "fft3d"])
+    ap.add_argument("--workload", default="imex", choices=["imex", "etdrk4", "serve", "fft3d", "explicit", "nk"])
     ap.add_argument("--fp32", action="store_true", help="fft3d: FP32 instead of FP64")
     ap.add_argument("--requests", type=int, default=512)
     ap.add_argument("--etd-steps", type=int, default=100)
@@ -572,6 +574,81 @@ def run_fft3d(args, local):
             "step_alg_bytes": b, "achieved_gbs": gbs, "frac_of_" + peak_kind.replace(" ", "_"): gbs / peak}
 
 
+def run_explicit(args, local):
+    """Fixed-step RK4 of the two-species advection-diffusion model (examples/advdiff_multispecies.py
+    shape: D = 1e-4, v = (0.5, -0.3), upwind, periodic) at n^2 in FP32: grid-pt-steps/s over
+    --etd-steps steps and the HBM roofline of a step.  Per field and point an RK4 step makes
+    16 buffer accesses in its four fused stage kernels (3 + 5 + 5 + 3: stage input, step
+    start, running sum; outputs), 64 B in FP32."""
+    import numpy as np
+    import torch
+    import moljax_gb300 as M
+    from moljax_gb300.core.stepping import _explicit_steps
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    n, S = args.n, args.etd_steps
+    grid = M.Grid2D(n, n, 0.0, 1.0, 0.0, 1.0)
+    model = M.create_advection_diffusion_model(grid, field_names=("c1", "c2"), D=1e-4, vx=0.5, vy=-0.3,
+                                               dtype=torch.float32)
+    rng = np.random.default_rng(SEED)
+    y0 = {k: torch.tensor(rng.uniform(0, 1, (n + 2, n + 2)), dtype=torch.float32, device=dev) for k in ("c1", "c2")}
+    dt = 0.2 * min(grid.dx / 0.8, grid.dx ** 2 / (4 * 1e-4))
+    _explicit_steps(model, y0, 0.0, dt, 2, 3)
+    torch.cuda.synchronize(dev)
+    s = torch.cuda.current_stream(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    _explicit_steps(model, y0, 0.0, dt, 2, S)
+    e1.record(s)
+    e1.synchronize()
+    t = e0.elapsed_time(e1) * 1e-3
+    b = 2 * n * n * 64
+    peak, peak_kind = peaks()
+    gbs = b * S / t / 1e9
+    return {"workload": f"advection-diffusion RK4 2 fields {n}x{n} FP32, upwind, periodic", "n": n, "steps": S,
+            "value": n * n * S / t, "unit": UNIT, "ms_per_step": t / S * 1e3, "step_alg_bytes": b,
+            "achieved_gbs": gbs, "frac_of_" + peak_kind.replace(" ", "_"): gbs / peak}
+
+
+def run_nk(args, local):
+    """Fixed-step BDF2 (BE first step) of u_t = div((1 + u^2) grad u) - u^3 on the unit square
+    with Dirichlet walls at n^2 cell centres, u0 a seeded sum of 8 Gaussians (A ~ U[0,1],
+    w ~ U[0.02,0.1]), dt = 100 dx^2, GMRES(30), Newton rtol 1e-8: FP64 state and residual,
+    FP32 Krylov, through the native Newton-Krylov driver.  Reports ms per step and the
+    Newton / GMRES iterations per step."""
+    import numpy as np
+    import torch
+    import moljax_gb300 as M
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    n, S = args.n, args.etd_steps
+    dx = 1.0 / n
+    rng = np.random.default_rng(SEED)
+    x = (np.arange(n) + 0.5) / n
+    X, Y = np.meshgrid(x, x, indexing="xy")
+    u0 = np.zeros((n, n))
+    for _ in range(8):
+        A, w = rng.uniform(0.0, 1.0), rng.uniform(0.02, 0.1)
+        cx, cy = rng.uniform(0.0, 1.0, 2)
+        u0 += A * np.exp(-((X - cx) ** 2 + (Y - cy) ** 2) / (2 * w * w))
+    u0 = torch.tensor(u0, device=dev)
+    dt = 100 * dx * dx
+    nkp = M.NKParams(gmres_restart=30)
+    M.integrate_implicit_vardiff(u0, dx, dt, 3, method="bdf2", nk_params=nkp, be_guess="previous")
+    torch.cuda.synchronize(dev)
+    s = torch.cuda.current_stream(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    u, st = M.integrate_implicit_vardiff(u0, dx, dt, S, method="bdf2", nk_params=nkp, be_guess="previous")
+    e1.record(s)
+    e1.synchronize()
+    t = e0.elapsed_time(e1) * 1e-3
+    return {"workload": f"variable-diffusion BDF2 Newton-Krylov {n}x{n} FP64/FP32-Krylov (Dirichlet), dt=100dx^2",
+            "n": n, "steps": S, "value": n * n * S / t, "unit": UNIT, "ms_per_step": t / S * 1e3,
+            "newton_per_step": float(st[:, 0].double().mean()), "gmres_per_step": float(st[:, 1].double().mean()),
+            "all_converged": bool((st[:, 2] != 0).all())}
+
+
 def run_serve(args, local):
     """The served mix (Poisson arrivals, 60 % tubular-reactor CN, 40 % Gray-Scott IMEX-Strang
     64^2..512^2): continuous-batching server vs one FP64 solve at a time (the first
@@ -672,6 +749,10 @@ def main():
         out = run_serve(args, local)
     elif args.workload == "fft3d":
         out = run_fft3d(args, local)
+    elif args.workload == "explicit":
+        out = run_explicit(args, local)
+    elif args.workload == "nk":
+        out = run_nk(args, local)
     elif args.kernels_only:
         out = run_kernels_only(args, local)
     else:

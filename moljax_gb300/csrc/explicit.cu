@@ -41,9 +41,23 @@ struct XModel {
   double F, k, r, vx, vy, dy, dx;
 };
 
+// The coefficients of a stage in the state type, converted on the host: FP64 arithmetic
+// is rare on this part, so an FP32 stage kernel performs none per point.
+template <typename T>
+struct XCoef {
+  T idx2, idy2, idx, idy, vx, vy, F, Fk, r;
+  T D[4];
+  T gv[4][4];  // ghost constants per field and side (left, right, bottom, top):
+               // Dirichlet 2 b, Neumann 2 d b
+  T cp1, cq1, cf1, cp2, cq2, cf2, hfac, hfixed;  // hfixed = fixed h * hfac
+  T atol, rtol;
+  int vxpos, vypos;
+};
+
 template <typename T>
 struct XStage {
   XModel m;
+  XCoef<T> k;
   T* buf[XB_NBUF];
   int w, p, q, o1, o2;
   double cp1, cq1, cf1, cp2, cq2, cf2;
@@ -62,110 +76,172 @@ __device__ __forceinline__ T* xbuf(const XStage<T>& a, int id, int cur) {
   return a.buf[id];
 }
 
-// w at (y, x) for interior or one-cell ghost positions of field f
+// Tiles of 32 columns x XTILE_ROWS rows; block (32, 8): each warp owns a strip of
+// XROWS rows and slides a three-row window down it.  The loads of a row are issued one
+// row ahead (row y+2 of the stage input and row y+1 of the combine operands while row y
+// is computed), with the BC ghosts applied by selects after branch-free index choices;
+// the x-neighbours come from the lanes by shuffle (lanes 0 and 31 and the grid edges
+// read theirs directly).  Coefficients arrive in the state type (XCoef).
+enum { XROWS = 8, XWARPS = 8, XTILE_ROWS = XROWS * XWARPS };
+
+// the ghost formula of moljax/core/bc.py:202-307 on the boundary-adjacent value s
 template <typename T>
-__device__ __forceinline__ T xat(const T* w, int y, int x, const XModel& m, int f) {
-  const int ny = m.ny, nx = m.nx, kind = m.kind[f];
-  if (x < 0 || x >= nx) {
-    const bool lo = x < 0;
-    const int xs = kind == MJX_BC_PERIODIC ? (lo ? nx - 1 : 0) : (lo ? 0 : nx - 1);
-    const T s = w[(long long)y * nx + xs];
-    const double b = lo ? m.bv[f][0] : m.bv[f][1];
-    if (kind == MJX_BC_DIRICHLET) return (T)(2.0 * b) - s;
-    if (kind == MJX_BC_NEUMANN) return lo ? s - (T)(2.0 * m.dx * b) : s + (T)(2.0 * m.dx * b);
-    return s;
-  }
-  if (y < 0 || y >= ny) {
-    const bool lo = y < 0;
-    const int ys = kind == MJX_BC_PERIODIC ? (lo ? ny - 1 : 0) : (lo ? 0 : ny - 1);
-    const T s = w[(long long)ys * nx + x];
-    const double b = lo ? m.bv[f][2] : m.bv[f][3];
-    if (kind == MJX_BC_DIRICHLET) return (T)(2.0 * b) - s;
-    if (kind == MJX_BC_NEUMANN) return lo ? s - (T)(2.0 * m.dy * b) : s + (T)(2.0 * m.dy * b);
-    return s;
-  }
-  return w[(long long)y * nx + x];
+__device__ __forceinline__ T xghost(T s, int kind, T g, bool lo) {
+  if (kind == MJX_BC_DIRICHLET) return g - s;
+  if (kind == MJX_BC_NEUMANN) return lo ? s - g : s + g;
+  return s;
 }
 
-template <typename T, int RX>
-__global__ void __launch_bounds__(256) rk_stage_kernel(const __grid_constant__ XStage<T> a) {
+// row yy in [-1, ny] of field f at column xc (ghost rows from the BC formulas)
+template <typename T>
+__device__ __forceinline__ T xrow(const T* wf, int yy, int xc, const XModel& m, const XCoef<T>& k, int f) {
+  const int ny = m.ny, kind = m.kind[f];
+  const bool lo = yy < 0, hi = yy >= ny;
+  const int ys = lo ? (kind == MJX_BC_PERIODIC ? ny - 1 : 0) : (hi ? (kind == MJX_BC_PERIODIC ? 0 : ny - 1) : yy);
+  const T s = wf[(long long)ys * m.nx + xc];
+  return (lo || hi) ? xghost(s, kind, lo ? k.gv[f][2] : k.gv[f][3], lo) : s;
+}
+
+template <typename T, int RX, int NF>
+__global__ void __launch_bounds__(256, sizeof(T) == 8 ? 2 : (NF == 4 ? 3 : 4)) rk_stage_kernel(const __grid_constant__ XStage<T> a) {
   const DevState* st = a.st;
   if (st != nullptr && st->done) return;
   const XModel& m = a.m;
   const int cur = st != nullptr ? st->cur : 0;
-  const T h = (T)((st != nullptr ? st->dtc : a.hfixed) * a.hfac);
+  const XCoef<T>& k = a.k;
+  const T h = st != nullptr ? (T)st->dtc * k.hfac : k.hfixed;  // hfac is 1 or 1/2: exact
   const T* W = xbuf(a, a.w, cur);
-  const T* P = a.p >= 0 ? xbuf(a, a.p, cur) : nullptr;
-  const T* Q = a.q >= 0 ? xbuf(a, a.q, cur) : nullptr;
+  const bool hasP = a.p >= 0, hasQ = a.q >= 0;
+  const T* P = hasP ? xbuf(a, a.p, cur) : W;  // an absent operand reads W (cached) and is zeroed
+  const T* Q = hasQ ? xbuf(a, a.q, cur) : W;
   T* O1 = xbuf(a, a.o1, cur);
   T* O2 = a.o2 >= 0 ? xbuf(a, a.o2, cur) : nullptr;
   const T* YF = a.buf[XB_YF];
-  const long long per = (long long)m.ny * m.nx;
-  const T idx2 = (T)(1.0 / (m.dx * m.dx)), idy2 = (T)(1.0 / (m.dy * m.dy));
-  const T idx = (T)(1.0 / m.dx), idy = (T)(1.0 / m.dy);
-  double esum = 0.0;
+  const int nf = m.nf, ny = m.ny, nx = m.nx, adv = m.advection;
+  const long long per = (long long)ny * nx;
+  const T idx2 = k.idx2, idy2 = k.idy2, idx = k.idx, idy = k.idy, vx = k.vx, vy = k.vy;
+  const bool vxpos = k.vxpos != 0, vypos = k.vypos != 0;
+  const T cp1 = k.cp1, cq1 = k.cq1, cf1h = k.cf1 * h;
+  const T cp2 = k.cp2, cq2 = k.cq2, cf2h = k.cf2 * h;
+  const T rF = k.F, rFk = k.Fk, rr = k.r;
+  const int lane = threadIdx.x;
+  const int ntx = (nx + 31) >> 5, nty = (ny + XTILE_ROWS - 1) / XTILE_ROWS;
+  const int ntiles = ntx * nty;
+  T esum = (T)0;  // per thread in the state type; FP64 across threads (as the row kernels)
   int bad = 0;
-  for (long long pt = blockIdx.x * (long long)blockDim.x + threadIdx.x; pt < per;
-       pt += (long long)gridDim.x * blockDim.x) {
-    const int y = (int)(pt / m.nx), x = (int)(pt - (long long)y * m.nx);
-    T c[4], Fv[4];
+  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const int ty = tile / ntx, tx = tile - ty * ntx;
+    const int x = tx * 32 + lane;
+    const int xc = x < nx ? x : nx - 1;
+    const int y0 = ty * XTILE_ROWS + threadIdx.y * XROWS;
+    if (y0 >= ny) continue;  // warp-uniform: a warp is one threadIdx.y
+    const int y1 = y0 + XROWS < ny ? y0 + XROWS : ny;
+    // x-neighbour columns of the lane that reads one directly (lane 0: left, others: right)
+    T up[NF], cc[NF], dn[NF], pn[NF], qn[NF];
 #pragma unroll
-    for (int f = 0; f < 4; ++f) {
-      if (f >= m.nf) break;
+    for (int f = 0; f < NF; ++f) {
+      if (f >= nf) break;
       const T* wf = W + f * per;
-      const T cc = wf[pt];
-      const T xm = xat(wf, y, x - 1, m, f), xp = xat(wf, y, x + 1, m, f);
-      const T ym = xat(wf, y - 1, x, m, f), yp = xat(wf, y + 1, x, m, f);
-      T v = (T)m.D[f] * ((xp - (T)2 * cc + xm) * idx2 + (yp - (T)2 * cc + ym) * idy2);
-      if (m.advection == 1) {  // d1_upwind_2d: v >= 0 backward, else forward
-        const T gx = m.vx >= 0.0 ? (cc - xm) * idx : (xp - cc) * idx;
-        const T gy = m.vy >= 0.0 ? (cc - ym) * idy : (yp - cc) * idy;
-        v = v - (T)m.vx * gx - (T)m.vy * gy;
-      } else if (m.advection == 2) {
-        v = v - (T)m.vx * (xp - xm) * (T)0.5 * idx - (T)m.vy * (yp - ym) * (T)0.5 * idy;
-      }
-      c[f] = cc;
-      Fv[f] = v;
+      up[f] = xrow(wf, y0 - 1, xc, m, k, f);
+      cc[f] = wf[(long long)y0 * nx + xc];
+      dn[f] = xrow(wf, y0 + 1, xc, m, k, f);
+      const long long i0 = f * per + (long long)y0 * nx + xc;
+      pn[f] = P[i0];
+      qn[f] = Q[i0];
     }
-    if (RX == RX_GRAY_SCOTT) {  // operators.py:644-667
-      const T uvv = c[0] * c[1] * c[1];
-      Fv[0] += -uvv + (T)m.F * ((T)1 - c[0]);
-      Fv[1] += uvv - (T)(m.F + m.k) * c[1];
-    } else if (RX == RX_FISHER) {  // operators.py:680-705
+    for (int y = y0; y < y1; ++y) {
+      const long long row = (long long)y * nx;
+      const int yn = y + 1 < y1 ? y + 1 : y;         // the next row of this strip (or y again)
+      const int y2 = y + 2 <= ny ? y + 2 : ny;       // two rows down, clamped to the ghost row
+      T c[NF], Fv[NF], pc[NF], qc[NF], d2[NF];
 #pragma unroll
-      for (int f = 0; f < 4; ++f) {
-        if (f >= m.nf) break;
-        Fv[f] += (T)m.r * c[f] * ((T)1 - c[f]);
+      for (int f = 0; f < NF; ++f) {  // the loads of the next row, issued first
+        if (f >= nf) break;
+        const T* wf = W + f * per;
+        pc[f] = pn[f];
+        qc[f] = qn[f];
+        d2[f] = xrow(wf, y2, xc, m, k, f);
+        const long long i1 = f * per + (long long)yn * nx + xc;
+        pn[f] = P[i1];
+        qn[f] = Q[i1];
       }
-    }
 #pragma unroll
-    for (int f = 0; f < 4; ++f) {
-      if (f >= m.nf) break;
-      const long long i = f * per + pt;
-      const T pv = P ? P[i] : (T)0, qv = Q ? Q[i] : (T)0;
-      const T o1 = (T)a.cp1 * pv + (T)a.cq1 * qv + (T)a.cf1 * h * Fv[f];
-      if (O2) O2[i] = (T)a.cp2 * pv + (T)a.cq2 * qv + (T)a.cf2 * h * Fv[f];
-      O1[i] = o1;
-      if (a.err) {  // moljax/core/state.py:335-339
-        const double e = ((double)o1 - (double)YF[i]) / (a.atol + a.rtol * fabs((double)o1));
-        esum += e * e;
-        bad |= !isfinite(o1);
+      for (int f = 0; f < NF; ++f) {
+        if (f >= nf) break;
+        const T* wf = W + f * per;
+        const int kind = m.kind[f];
+        const T cv = cc[f], ym = up[f], yp = dn[f];
+        // lane 0 reads its left neighbour, the other lanes their right one (only lane 31
+        // and the last column use it); edges take the BC ghost
+        const bool left = lane == 0;
+        const int xn = left ? (xc > 0 ? xc - 1 : (kind == MJX_BC_PERIODIC ? nx - 1 : 0))
+                            : (xc < nx - 1 ? xc + 1 : (kind == MJX_BC_PERIODIC ? 0 : nx - 1));
+        T e = wf[row + xn];
+        if (left ? xc == 0 : xc >= nx - 1) e = xghost(e, kind, left ? k.gv[f][0] : k.gv[f][1], left);
+        T xm = __shfl_up_sync(0xffffffffu, cv, 1), xp = __shfl_down_sync(0xffffffffu, cv, 1);
+        if (left) xm = e;
+        else if (lane == 31 || xc >= nx - 1) xp = e;
+        if (left && xc >= nx - 1) {  // a one-lane last tile: the right ghost as well
+          const int xr = kind == MJX_BC_PERIODIC ? 0 : nx - 1;
+          xp = xghost(wf[row + xr], kind, k.gv[f][1], false);
+        }
+        T v = k.D[f] * ((xp - (T)2 * cv + xm) * idx2 + (yp - (T)2 * cv + ym) * idy2);
+        if (adv == 1) {  // d1_upwind_2d: v >= 0 backward, else forward
+          const T gx = vxpos ? (cv - xm) * idx : (xp - cv) * idx;
+          const T gy = vypos ? (cv - ym) * idy : (yp - cv) * idy;
+          v = v - vx * gx - vy * gy;
+        } else if (adv == 2) {
+          v = v - vx * (xp - xm) * (T)0.5 * idx - vy * (yp - ym) * (T)0.5 * idy;
+        }
+        c[f] = cv;
+        Fv[f] = v;
+        up[f] = cv;
+        cc[f] = yp;
+        dn[f] = d2[f];
+      }
+      if (RX == RX_GRAY_SCOTT) {  // operators.py:644-667
+        const T uvv = c[0] * c[1] * c[1];
+        Fv[0] += -uvv + rF * ((T)1 - c[0]);
+        Fv[1] += uvv - rFk * c[1];
+      } else if (RX == RX_FISHER) {  // operators.py:680-705
+#pragma unroll
+        for (int f = 0; f < NF; ++f) {
+          if (f >= nf) break;
+          Fv[f] += rr * c[f] * ((T)1 - c[f]);
+        }
+      }
+      if (x < nx) {
+#pragma unroll
+        for (int f = 0; f < NF; ++f) {
+          if (f >= nf) break;
+          const long long i = f * per + row + x;
+          const T pv = hasP ? pc[f] : (T)0, qv = hasQ ? qc[f] : (T)0;
+          const T o1 = cp1 * pv + cq1 * qv + cf1h * Fv[f];
+          if (O2) O2[i] = cp2 * pv + cq2 * qv + cf2h * Fv[f];
+          O1[i] = o1;
+          if (a.err) {  // moljax/core/state.py:335-339
+            const T e = (o1 - YF[i]) / (k.atol + k.rtol * (o1 < (T)0 ? -o1 : o1));
+            esum += e * e;
+            bad |= !isfinite(o1);
+          }
+        }
       }
     }
   }
   if (a.err) {
-    __shared__ double red[8];
-    __shared__ int redb[8];
+    __shared__ double red[XWARPS];
+    __shared__ int redb[XWARPS];
+    double esd = (double)esum;
     for (int o = 16; o > 0; o >>= 1) {
-      esum += __shfl_xor_sync(0xffffffffu, esum, o);
+      esd += __shfl_xor_sync(0xffffffffu, esd, o);
       bad |= __shfl_xor_sync(0xffffffffu, bad, o);
     }
-    if ((threadIdx.x & 31) == 0) { red[threadIdx.x >> 5] = esum; redb[threadIdx.x >> 5] = bad; }
+    if (lane == 0) { red[threadIdx.y] = esd; redb[threadIdx.y] = bad; }
     __syncthreads();
-    if (threadIdx.x == 0) {
+    if (lane == 0 && threadIdx.y == 0) {
       double s = 0.0, cc = 0.0;
       int b = 0;
-      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {  // Kahan
+      for (int w = 0; w < XWARPS; ++w) {  // Kahan
         const double yv = red[w] - cc, tv = s + yv;
         cc = (tv - s) - yv;
         s = tv;
@@ -292,14 +368,46 @@ static XAttempt<T> build_x(const XModel& m, int method, char* ws, const XLayout&
   return A;
 }
 
+// the state-type coefficients of a stage (XCoef), from its FP64 description
 template <typename T>
-static cudaError_t launch_stage(const XStage<T>& s, int rx, cudaStream_t st) {
-  const long long per = (long long)s.m.ny * s.m.nx;
-  long long blocks = (per + 255) / 256;
-  if (s.err || blocks > XNPARTS) blocks = XNPARTS;  // the error pass always fills XNPARTS partials
-  if (rx == RX_GRAY_SCOTT) rk_stage_kernel<T, RX_GRAY_SCOTT><<<(int)blocks, 256, 0, st>>>(s);
-  else if (rx == RX_FISHER) rk_stage_kernel<T, RX_FISHER><<<(int)blocks, 256, 0, st>>>(s);
-  else rk_stage_kernel<T, RX_NONE><<<(int)blocks, 256, 0, st>>>(s);
+static void x_coef(XStage<T>& s) {
+  const XModel& m = s.m;
+  XCoef<T>& k = s.k;
+  memset(&k, 0, sizeof(k));
+  k.idx2 = (T)(1.0 / (m.dx * m.dx)); k.idy2 = (T)(1.0 / (m.dy * m.dy));
+  k.idx = (T)(1.0 / m.dx); k.idy = (T)(1.0 / m.dy);
+  k.vx = (T)m.vx; k.vy = (T)m.vy; k.vxpos = m.vx >= 0.0; k.vypos = m.vy >= 0.0;
+  k.F = (T)m.F; k.Fk = (T)(m.F + m.k); k.r = (T)m.r;
+  for (int f = 0; f < 4; ++f) {
+    k.D[f] = (T)m.D[f];
+    for (int side = 0; side < 4; ++side) {
+      const double d = side < 2 ? m.dx : m.dy, b = m.bv[f][side];
+      k.gv[f][side] = m.kind[f] == MJX_BC_NEUMANN ? (T)(2.0 * d * b) : (T)(2.0 * b);
+    }
+  }
+  k.cp1 = (T)s.cp1; k.cq1 = (T)s.cq1; k.cf1 = (T)s.cf1;
+  k.cp2 = (T)s.cp2; k.cq2 = (T)s.cq2; k.cf2 = (T)s.cf2;
+  k.hfac = (T)s.hfac; k.hfixed = (T)(s.hfixed * s.hfac);
+  k.atol = (T)s.atol; k.rtol = (T)s.rtol;
+}
+
+template <typename T>
+static cudaError_t launch_stage(const XStage<T>& s0, int rx, cudaStream_t st) {
+  XStage<T> s = s0;
+  x_coef(s);
+  const long long tiles = (long long)((s.m.nx + 31) / 32) * ((s.m.ny + XTILE_ROWS - 1) / XTILE_ROWS);
+  // one resident wave (4 blocks of 256 threads per SM) looping over the tiles; the error
+  // pass always fills XNPARTS partials
+  const int blocks = s.err ? XNPARTS : (int)(tiles < XNPARTS ? tiles : XNPARTS);
+  const dim3 blk(32, XWARPS);
+  if (rx == RX_GRAY_SCOTT) rk_stage_kernel<T, RX_GRAY_SCOTT, 2><<<blocks, blk, 0, st>>>(s);
+  else if (s.m.nf <= 2) {
+    if (rx == RX_FISHER) rk_stage_kernel<T, RX_FISHER, 2><<<blocks, blk, 0, st>>>(s);
+    else rk_stage_kernel<T, RX_NONE, 2><<<blocks, blk, 0, st>>>(s);
+  } else {
+    if (rx == RX_FISHER) rk_stage_kernel<T, RX_FISHER, 4><<<blocks, blk, 0, st>>>(s);
+    else rk_stage_kernel<T, RX_NONE, 4><<<blocks, blk, 0, st>>>(s);
+  }
   return cudaGetLastError();
 }
 
@@ -310,6 +418,274 @@ static cudaError_t launch_x_attempt(const XAttempt<T>& A, cudaStream_t s) {
     if (e != cudaSuccess) return e;
   }
   return cudaSuccess;
+}
+
+// ---------------------------------------------------------------------------
+// One whole SSPRK3 or RK4 step per kernel (temporal blocking).  A block owns an
+// FTX x FTY tile of the output; it stages the step's input over the tile plus a halo
+// of NST cells (one per stage: every stage's 5-point stencil eats one ring) in shared
+// memory and runs the stages there, each over the region its successors still need,
+// so that the step reads the state once and writes it once (8 B per point and field in
+// FP32 instead of the 64 B of four separate RK4 stage passes).  The stage table is the
+// one the separate passes use (add_step), with buffer ids mapped to shared memory:
+// 0 step input, 1 and 2 the stage ping-pong, 3 the RK4 running sum, -2 the output.
+// Periodic halos wrap; for Dirichlet and Neumann fields the ring of ghost cells just
+// outside the domain is refilled from the BC formula after every stage, and cells
+// further out are never read by a domain point.
+enum { FTX = 64, FTY = 32, FOUT = -2 };
+
+template <typename T>
+struct XFused {
+  XModel m;
+  XCoef<T> k;
+  const T* in;
+  T* out;
+  int nst;
+  int w[4], p[4], q[4], o1[4], o2[4];
+  T cp1[4], cq1[4], cf1[4], cp2[4], cq2[4], cf2[4];
+  int any_bc;  // some field is Dirichlet or Neumann
+};
+
+// periodic index: one add or subtract within a halo of the domain, a remainder beyond
+__device__ __forceinline__ int xwrap(int v, int n) {
+  v = v < 0 ? v + n : (v >= n ? v - n : v);
+  return (v >= 0 && v < n) ? v : ((v % n) + n) % n;
+}
+
+enum { FTHREADS = 512 };
+
+// one region cell of the step input: a wrapped periodic cell, a domain cell, a ghost of
+// the ring (the BC formula on its adjacent domain cell) or an unused outer cell (0)
+template <typename T>
+__device__ __forceinline__ long long fcell_src(int gy, int gx, const XModel& m, int kind, int* side) {
+  const int ny = m.ny, nx = m.nx;
+  *side = -1;
+  if (kind == MJX_BC_PERIODIC) return (long long)xwrap(gy, ny) * nx + xwrap(gx, nx);
+  const bool iny = gy >= 0 && gy < ny, inx = gx >= 0 && gx < nx;
+  if (iny && inx) return (long long)gy * nx + gx;
+  if (iny && (gx == -1 || gx == nx)) { *side = gx < 0 ? 0 : 1; return (long long)gy * nx + (gx < 0 ? 0 : nx - 1); }
+  if (inx && (gy == -1 || gy == ny)) { *side = gy < 0 ? 2 : 3; return (long long)(gy < 0 ? 0 : ny - 1) * nx + gx; }
+  *side = 4;
+  return -1;
+}
+
+template <typename T, int RX, int NF, int NST>
+__global__ void __launch_bounds__(FTHREADS, (sizeof(T) * NF <= 8) ? 2 : 1)
+fused_step_kernel(const __grid_constant__ XFused<T> a) {
+  extern __shared__ __align__(16) unsigned char fsm_raw[];
+  T* sm = reinterpret_cast<T*>(fsm_raw);
+  const XModel& m = a.m;
+  const XCoef<T>& k = a.k;
+  constexpr int R = NST, RW = FTX + 2 * R, RH = FTY + 2 * R, RS = RW * RH;
+  constexpr int NL = (RS + FTHREADS - 1) / FTHREADS;
+  const int nf = m.nf, ny = m.ny, nx = m.nx, adv = m.advection;
+  const long long per = (long long)ny * nx;
+  const int ntx = (nx + FTX - 1) / FTX;
+  const int ty = blockIdx.x / ntx, tx = blockIdx.x - ty * ntx;
+  const int X0 = tx * FTX - R, Y0 = ty * FTY - R;  // domain coordinates of region cell (0, 0)
+  const int tid = threadIdx.x;
+  const T h = k.hfixed;
+  const T idx2 = k.idx2, idy2 = k.idy2, idx = k.idx, idy = k.idy, vx = k.vx, vy = k.vy;
+  const bool vxpos = k.vxpos != 0, vypos = k.vypos != 0;
+  auto buf = [&](int b, int f) -> T* { return sm + (size_t)(b * NF + f) * RS; };
+
+  // 1. the step input over the region: all loads of a thread are issued before any store
+  {
+    T v[NL][NF];
+#pragma unroll
+    for (int j = 0; j < NL; ++j) {
+      const int i = tid + j * FTHREADS;
+      const int ry = i / RW, rx = i - ry * RW;
+#pragma unroll
+      for (int f = 0; f < NF; ++f) {
+        v[j][f] = (T)0;
+        if (f >= nf || i >= RS) continue;
+        int side;
+        const long long si = fcell_src<T>(Y0 + ry, X0 + rx, m, m.kind[f], &side);
+        if (si >= 0) v[j][f] = a.in[f * per + si];
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < NL; ++j) {
+      const int i = tid + j * FTHREADS;
+      if (i >= RS) continue;
+      const int ry = i / RW, rx = i - ry * RW;
+#pragma unroll
+      for (int f = 0; f < NF; ++f) {
+        if (f >= nf) break;
+        int side;
+        const int kind = m.kind[f];
+        (void)fcell_src<T>(Y0 + ry, X0 + rx, m, kind, &side);
+        T x = v[j][f];
+        if (side >= 0 && side < 4) x = xghost(x, kind, k.gv[f][side], side == 0 || side == 2);
+        buf(0, f)[i] = x;
+      }
+    }
+  }
+  __syncthreads();
+
+#pragma unroll
+  for (int s = 0; s < NST; ++s) {
+    const int lo = s + 1;
+    const int SW = RW - 2 * lo, SH = RH - 2 * lo;  // this stage's output region (compile time)
+    const int wb = a.w[s], pb = a.p[s], qb = a.q[s], o1b = a.o1[s], o2b = a.o2[s];
+    const T cp1 = a.cp1[s], cq1 = a.cq1[s], cf1h = a.cf1[s] * h;
+    const T cp2 = a.cp2[s], cq2 = a.cq2[s], cf2h = a.cf2[s] * h;
+    for (int i = tid; i < SW * SH; i += FTHREADS) {
+      const int sy = i / SW, sx = i - sy * SW;
+      const int ry = sy + lo, rx = sx + lo;
+      const int gy = Y0 + ry, gx = X0 + rx;
+      const int c0 = ry * RW + rx;
+      T c[NF], Fv[NF];
+#pragma unroll
+      for (int f = 0; f < NF; ++f) {
+        if (f >= nf) break;
+        const T* wv = buf(wb, f);
+        const T cv = wv[c0], xm = wv[c0 - 1], xp = wv[c0 + 1], ym = wv[c0 - RW], yp = wv[c0 + RW];
+        T v = k.D[f] * ((xp - (T)2 * cv + xm) * idx2 + (yp - (T)2 * cv + ym) * idy2);
+        if (adv == 1) {  // d1_upwind_2d
+          const T gxv = vxpos ? (cv - xm) * idx : (xp - cv) * idx;
+          const T gyv = vypos ? (cv - ym) * idy : (yp - cv) * idy;
+          v = v - vx * gxv - vy * gyv;
+        } else if (adv == 2) {
+          v = v - vx * (xp - xm) * (T)0.5 * idx - vy * (yp - ym) * (T)0.5 * idy;
+        }
+        c[f] = cv;
+        Fv[f] = v;
+      }
+      if (RX == RX_GRAY_SCOTT) {  // operators.py:644-667
+        const T uvv = c[0] * c[1] * c[1];
+        Fv[0] += -uvv + k.F * ((T)1 - c[0]);
+        Fv[1] += uvv - k.Fk * c[1];
+      } else if (RX == RX_FISHER) {  // operators.py:680-705
+#pragma unroll
+        for (int f = 0; f < NF; ++f) {
+          if (f >= nf) break;
+          Fv[f] += k.r * c[f] * ((T)1 - c[f]);
+        }
+      }
+#pragma unroll
+      for (int f = 0; f < NF; ++f) {
+        if (f >= nf) break;
+        const T pv = pb >= 0 ? buf(pb, f)[c0] : (T)0, qv = qb >= 0 ? buf(qb, f)[c0] : (T)0;
+        const T o1 = cp1 * pv + cq1 * qv + cf1h * Fv[f];
+        if (o2b >= 0) buf(o2b, f)[c0] = cp2 * pv + cq2 * qv + cf2h * Fv[f];
+        if (o1b == FOUT) {
+          if (gy < ny && gx < nx) a.out[f * per + (long long)gy * nx + gx] = o1;
+        } else {
+          buf(o1b, f)[c0] = o1;
+        }
+      }
+    }
+    if (s + 1 < NST) {
+      __syncthreads();
+      if (a.any_bc) {  // the ghost ring of the new stage values
+        for (int i = tid; i < SW * SH; i += FTHREADS) {
+          const int sy = i / SW, sx = i - sy * SW;
+          const int ry = sy + lo, rx = sx + lo;
+          const int gy = Y0 + ry, gx = X0 + rx;
+          const bool iny = gy >= 0 && gy < ny, inx = gx >= 0 && gx < nx;
+          const bool gxr = iny && (gx == -1 || gx == nx), gyr = inx && (gy == -1 || gy == ny);
+          if (!gxr && !gyr) continue;
+          const int c0 = ry * RW + rx;
+          // the adjacent domain cell lies one step inward, inside this stage's region
+          const int cin = gxr ? (gx < 0 ? c0 + 1 : c0 - 1) : (gy < 0 ? c0 + RW : c0 - RW);
+#pragma unroll
+          for (int f = 0; f < NF; ++f) {
+            if (f >= nf) break;
+            const int kind = m.kind[f];
+            if (kind == MJX_BC_PERIODIC) continue;
+            T* ob = buf(o1b, f);
+            ob[c0] = gxr ? xghost(ob[cin], kind, gx < 0 ? k.gv[f][0] : k.gv[f][1], gx < 0)
+                         : xghost(ob[cin], kind, gy < 0 ? k.gv[f][2] : k.gv[f][3], gy < 0);
+          }
+        }
+        __syncthreads();
+      }
+    }
+  }
+}
+
+template <typename T>
+static size_t fused_smem(int nst, int nfa) {
+  const int nbuf = nst == 4 ? 4 : 3;
+  return (size_t)nbuf * nfa * (FTX + 2 * nst) * (FTY + 2 * nst) * sizeof(T);
+}
+
+// whether a fused step of `method` fits the shared memory of a block
+template <typename T>
+static bool fused_ok(const XModel& m, int method) {
+  if (method != 1 && method != 2) return false;
+  const int nfa = m.nf <= 2 ? 2 : 4;
+  return fused_smem<T>(method == 2 ? 4 : 3, nfa) <= 200 * 1024;
+}
+
+template <typename T, int RX, int NF, int NST>
+static cudaError_t launch_fused_t(const XFused<T>& f, size_t smem, unsigned blocks, cudaStream_t s) {
+  static bool attr = false;
+  if (!attr) {
+    const cudaError_t e = cudaFuncSetAttribute(fused_step_kernel<T, RX, NF, NST>,
+                                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    attr = true;
+  }
+  fused_step_kernel<T, RX, NF, NST><<<blocks, FTHREADS, smem, s>>>(f);
+  return cudaGetLastError();
+}
+
+template <typename T, int RX>
+static cudaError_t launch_fused_rx(const XFused<T>& f, cudaStream_t s) {
+  const int nfa = f.m.nf <= 2 ? 2 : 4;
+  const size_t smem = fused_smem<T>(f.nst, nfa);
+  const unsigned blocks = (unsigned)(((f.m.nx + FTX - 1) / FTX) * ((f.m.ny + FTY - 1) / FTY));
+  if (f.nst == 4) {
+    return nfa == 2 ? launch_fused_t<T, RX, 2, 4>(f, smem, blocks, s) : launch_fused_t<T, RX, 4, 4>(f, smem, blocks, s);
+  }
+  return nfa == 2 ? launch_fused_t<T, RX, 2, 3>(f, smem, blocks, s) : launch_fused_t<T, RX, 4, 3>(f, smem, blocks, s);
+}
+
+template <typename T>
+static cudaError_t launch_fused(const XFused<T>& f, cudaStream_t s) {
+  if (f.m.reaction == MJX_REACT_GRAY_SCOTT) return launch_fused_rx<T, RX_GRAY_SCOTT>(f, s);
+  if (f.m.reaction == MJX_REACT_FISHER) return launch_fused_rx<T, RX_FISHER>(f, s);
+  return launch_fused_rx<T, RX_NONE>(f, s);
+}
+
+// the fused step of `method` with the stage table of add_step (in / out set per step)
+template <typename T>
+static XFused<T> make_fused(const XModel& m, int method, double dt) {
+  XAttempt<T> A;
+  memset(&A, 0, sizeof(A));
+  XStage<T> base;
+  memset(&base, 0, sizeof(base));
+  base.m = m;
+  base.hfixed = dt;
+  add_step(A, base, method, XB_YCUR, XB_YNEXT, 1.0, 0);
+  XFused<T> f;
+  memset(&f, 0, sizeof(f));
+  f.m = m;
+  XStage<T> s0 = A.s[0];
+  x_coef(s0);
+  f.k = s0.k;
+  f.nst = A.n;
+  auto map = [](int id) -> int {
+    switch (id) {
+      case XB_YCUR: return 0;
+      case XB_W1: return 1;
+      case XB_W2: return 2;
+      case XB_ACC: return 3;
+      case XB_YNEXT: return FOUT;
+      default: return -1;
+    }
+  };
+  for (int i = 0; i < A.n; ++i) {
+    const XStage<T>& st = A.s[i];
+    f.w[i] = map(st.w); f.p[i] = map(st.p); f.q[i] = map(st.q); f.o1[i] = map(st.o1); f.o2[i] = map(st.o2);
+    f.cp1[i] = (T)st.cp1; f.cq1[i] = (T)st.cq1; f.cf1[i] = (T)st.cf1;
+    f.cp2[i] = (T)st.cp2; f.cq2[i] = (T)st.cq2; f.cf2[i] = (T)st.cf2;
+  }
+  for (int q = 0; q < m.nf; ++q) f.any_bc |= m.kind[q] != MJX_BC_PERIODIC;
+  return f;
 }
 
 template <typename T>
@@ -326,6 +702,18 @@ static mjx_status x_integrate(const XModel& m, int method, double dt, int n_step
   A.rx = m.reaction == MJX_REACT_GRAY_SCOTT ? RX_GRAY_SCOTT : (m.reaction == MJX_REACT_FISHER ? RX_FISHER : RX_NONE);
   MJX_CUDA_TRY(cudaMemcpyAsync(base.buf[0], y0, nelem * sizeof(T), cudaMemcpyDeviceToDevice, s));
   int src = 0;
+  if (fused_ok<T>(m, method)) {  // SSPRK3 / RK4: one kernel per step
+    XFused<T> f = make_fused<T>(m, method, dt);
+    for (int step = 0; step < n_steps; ++step) {
+      f.in = base.buf[src];
+      f.out = base.buf[1 - src];
+      const cudaError_t e = launch_fused<T>(f, s);
+      if (e != cudaSuccess) { set_last_error(e, __FILE__, __LINE__); return MJX_CUDA_ERROR; }
+      src = 1 - src;
+    }
+    MJX_CUDA_TRY(cudaMemcpyAsync(y_out, base.buf[src], nelem * sizeof(T), cudaMemcpyDeviceToDevice, s));
+    return MJX_OK;
+  }
   for (int step = 0; step < n_steps; ++step) {
     A.n = 0;
     // with st == nullptr the buffer ids XB_YCUR/XB_YNEXT address buf[0]/buf[1] directly

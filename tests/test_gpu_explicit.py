@@ -190,3 +190,70 @@ def test_2d_derivatives_error_norm_is_finite(cuda):
     y["v"] = y["v"].clone()
     y["v"][3, 4] = float("nan")
     assert not M.is_finite(y)
+
+
+@pytest.mark.parametrize("shape", [(70, 33), (5, 1), (3, 65), (97, 129), (130, 64)])
+@pytest.mark.parametrize("kind", [mol.PERIODIC, mol.DIRICHLET, mol.NEUMANN])
+def test_stage_tiles_any_shape(cuda, shape, kind):
+    """The stage kernel's 32 x 64 tiles on grids that leave partial tiles, a one-column last
+    tile (nx = 33, 65, 129) and single-column grids; three fields (the four-field build),
+    SSPRK3 and RK4, BC values on every side."""
+    import moljax_gb300 as M
+    from moljax_gb300.core.bc import FieldBCSpec, BCType
+    ny, nx = shape
+    names = ("c1", "c2", "c3")
+    grid = M.Grid2D(nx, ny, 0.0, 1.0, 0.0, 0.8)
+    og = mol.Grid2D(nx, ny, 0, 1, 0, 0.8)
+    model = M.create_advection_diffusion_model(grid, names, 0.01, 0.7, -0.4, BCType(kind), True)
+    vals = {}
+    if kind != mol.PERIODIC:
+        fn = (lambda X, Y, t, p: dict(SIDES))
+        spec = FieldBCSpec(kind=BCType(kind), value=fn) if kind == mol.DIRICHLET else \
+            FieldBCSpec(kind=BCType(kind), flux=fn)
+        model = M.MOLModel(model.grid, {k: spec for k in names}, model.params, model.linear_ops,
+                           model.nonlinear_ops, model.metadata)
+        vals = {k: dict(SIDES) for k in names}
+    om = OX.ExplicitModel(og, {k: kind for k in names}, {k: 0.01 for k in names}, vals,
+                          advection="upwind", vx=0.7, vy=-0.4, params={"D": 0.01, "vx": 0.7, "vy": -0.4})
+    rng = np.random.default_rng(ny * 131 + nx)
+    y0 = {k: mol.pad(rng.uniform(0, 1, (ny, nx)), og) for k in names}
+    ym = {k: torch.tensor(v, device=cuda) for k, v in y0.items()}
+    c = (slice(1, ny + 1), slice(1, nx + 1))
+    for method, step in ((1, "ssprk3_step"), (2, "rk4_step")):
+        out = getattr(M, step)(model, ym, 0.0, 1e-3)
+        ref = OX.STEPS[method](om, y0, 1e-3)
+        for k in names:
+            np.testing.assert_allclose(out[k].cpu().numpy()[c], ref[k][c], rtol=0, atol=1e-12)
+    # FP32 state: the same RK4 step within single-precision rounding
+    m32 = M.create_advection_diffusion_model(grid, names, 0.01, 0.7, -0.4, BCType(kind), True,
+                                             dtype=torch.float32)
+    if kind != mol.PERIODIC:
+        m32 = M.MOLModel(m32.grid, model.bc_spec, m32.params, m32.linear_ops, m32.nonlinear_ops, m32.metadata)
+    out = M.rk4_step(m32, {k: v.float() for k, v in ym.items()}, 0.0, 1e-3)
+    ref = OX.STEPS[2](om, y0, 1e-3)
+    for k in names:
+        np.testing.assert_allclose(out[k].cpu().double().numpy()[c], ref[k][c], rtol=0, atol=2e-5)
+
+
+def test_gray_scott_stage_rectangular(cuda):
+    """Gray-Scott (the two-field reaction build) on a 48 x 80 grid with Dirichlet values."""
+    import moljax_gb300 as M
+    from moljax_gb300.core.bc import FieldBCSpec, BCType
+    ny, nx = 48, 80
+    grid = M.Grid2D(nx, ny, 0.0, 2.5, 0.0, 1.5)
+    model = M.create_gray_scott_model(grid, 2e-5, 1e-5, 0.035, 0.065, BCType(mol.DIRICHLET))
+    fn = (lambda X, Y, t, p: dict(SIDES))
+    spec = FieldBCSpec(kind=BCType(mol.DIRICHLET), value=fn)
+    model = M.MOLModel(model.grid, {"u": spec, "v": spec}, model.params, model.linear_ops,
+                       model.nonlinear_ops, model.metadata)
+    og = mol.Grid2D(nx, ny, 0, 2.5, 0, 1.5)
+    y0 = mol.gray_scott_ic(og, 9)
+    om = OX.ExplicitModel(og, {"u": mol.DIRICHLET, "v": mol.DIRICHLET}, {"u": 2e-5, "v": 1e-5},
+                          {"u": dict(SIDES), "v": dict(SIDES)}, lambda y: mol.gray_scott_reaction(y, 0.035, 0.065),
+                          params={"Du": 2e-5, "Dv": 1e-5, "F": 0.035, "k": 0.065})
+    ym = {k: torch.tensor(v, device=cuda) for k, v in y0.items()}
+    c = (slice(1, ny + 1), slice(1, nx + 1))
+    out = M.rk4_step(model, ym, 0.0, 0.5)
+    ref = OX.STEPS[2](om, y0, 0.5)
+    for k in ("u", "v"):
+        np.testing.assert_allclose(out[k].cpu().numpy()[c], ref[k][c], rtol=0, atol=1e-13)
