@@ -572,6 +572,45 @@ mjx_status mjx_imex_attempt_kernel2d(const void* plan, const mjx_grid2d* grid, i
                                      int which, double dt, const void* y, void* ws,
                                      size_t ws_bytes, void* stream);
 
+/* ---- Autotuning --------------------------------------------------------------
+ * No reference counterpart: under jax.jit XLA chooses its own FFT and fusion
+ * strategies (moljax/core/fft_solvers.py:33-80 calls jnp.fft.fft2 / ifft2 and
+ * moljax/core/stepping.py:126-163 leaves the stencil passes to XLA).  Here the
+ * tunable launch choices are timed on the device and the fastest is kept in a
+ * process-wide registry that the launchers read. */
+
+/* Candidate radix schedules of a mixed-radix DFT length n = 2^a 3^b 5^c (not a power of
+ * two): up to max rows of 17 ints [nrad, r0 .. r15] (radices 2, 3, 4, 5 in pass order)
+ * written to out; returns the count (0 for other lengths).  Host only. */
+int mjx_dft_schedule_candidates(int n, int* out, int max);
+/* Installs the radix schedule (nrad radices whose product is n) and the threads per
+ * sequence (tpsm in [1, 256], 0 = n/8) used for length n in dtype; nrad = 0 clears the
+ * entry (back to the default schedule 4s, 2s, 3s, 5s). */
+mjx_status mjx_dft_schedule_set(int n, int dtype, int nrad, const int* rad, int tpsm);
+/* The schedule in use for length n (tuned or default): nrad (0 for power-of-two and
+ * Bluestein lengths), rad[16], tpsm. */
+mjx_status mjx_dft_schedule_get(int n, int dtype, int* nrad, int* rad, int* tpsm);
+/* Times every candidate schedule of length n with threads per sequence n/4, n/8, n/16
+ * on nrows rows of scratch (>= nrows * n complex values of dtype; overwritten) with
+ * CUDA events, reps launches each after a warm-up launch, installs the fastest and
+ * returns the candidate count, the winner's index and up to max_times times (ms per
+ * launch, candidate order: schedule-major).  plan is a mjx_dftn_plan_init plan of n.
+ * Lengths without a schedule (powers of two, Bluestein) return n_cand = 0. */
+mjx_status mjx_autotune_dft(const void* plan, int n, int dtype, long long nrows, void* scratch,
+                            size_t scratch_bytes, int reps, double* times, int max_times, int* n_cand,
+                            int* best, void* stream);
+/* Installs the rows per warp strip (2, 4, 8, 16 or 32; 0 = default 8) of the explicit
+ * stage kernel for this grid size, field count and dtype. */
+mjx_status mjx_stencil_rows_set(int ny, int nx, int nfields, int dtype, int rows);
+/* The installed rows per warp strip (0 when untuned). */
+int mjx_stencil_rows_get(int ny, int nx, int nfields, int dtype);
+/* Times an RK4 middle stage of prob on grid for strips of 2, 4, 8, 16 and 32 rows
+ * (reps launches each, CUDA events) in ws (mjx_explicit_ws_bytes; overwritten),
+ * installs the fastest and returns it with up to max_times times (ms per launch). */
+mjx_status mjx_autotune_stencil2d(const mjx_grid2d* grid, int dtype, const mjx_explicit_problem* prob,
+                                  void* ws, size_t ws_bytes, int reps, double* times, int max_times,
+                                  int* best_rows, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

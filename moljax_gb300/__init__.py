@@ -6,6 +6,7 @@ tensors as the device buffers.  There is no CPU or library fallback.
 """
 
 from moljax_gb300.core import *  # noqa: F401,F403
+from moljax_gb300.core import autotune  # noqa: F401
 
 
 __version__ = "0.1.0"

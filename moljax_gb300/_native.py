@@ -185,6 +185,15 @@ SIGNATURES = {
                                              C.POINTER(PIDParamsC), _i, _d, _vp, _vp, _sz, _vp]),
     "mjx_imex_attempt_kernel2d": (_i, [_vp, C.POINTER(Grid2DC), _i, C.POINTER(ImexProblemC),
                                        C.POINTER(PIDParamsC), _i, _d, _vp, _vp, _sz, _vp]),
+    "mjx_dft_schedule_candidates": (_i, [_i, C.POINTER(C.c_int), _i]),
+    "mjx_dft_schedule_set": (_i, [_i, _i, _i, C.POINTER(C.c_int), _i]),
+    "mjx_dft_schedule_get": (_i, [_i, _i, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
+    "mjx_autotune_dft": (_i, [_vp, _i, _i, C.c_longlong, _vp, _sz, _i, C.POINTER(C.c_double), _i,
+                              C.POINTER(C.c_int), C.POINTER(C.c_int), _vp]),
+    "mjx_stencil_rows_set": (_i, [_i, _i, _i, _i, _i]),
+    "mjx_stencil_rows_get": (_i, [_i, _i, _i, _i]),
+    "mjx_autotune_stencil2d": (_i, [C.POINTER(Grid2DC), _i, C.POINTER(ExplicitProblemC), _vp, _sz, _i,
+                                    C.POINTER(C.c_double), _i, C.POINTER(C.c_int), _vp]),
 }
 
 

@@ -129,6 +129,8 @@ class GeneralSpectralPlan:
             bufs.append(b)
         self.buf_y, self.buf_x = bufs
         self.buf = self.buf_y  # the power-of-two entry points reject this grid by its shape
+        from moljax_gb300.core import autotune
+        autotune.tune_lengths([(self.nx, self.ny, self.buf_x), (self.ny, self.nx, self.buf_y)], dtype, self.device)
 
     def ws_bytes(self, nfields: int) -> int:
         return N.lib().mjx_spectral_general2d_ws_bytes(self.ny, self.nx, nfields, self.code)
@@ -487,6 +489,10 @@ class SpectralPlan3D:
                     N.check("mjx_dftn_plan_init", lib.mjx_dftn_plan_init(N.ptr(b), n, self.code,
                                                                          N.stream_ptr(self.device)))
                 self.bufs.append(b)
+            from moljax_gb300.core import autotune
+            nz_, ny_, nx_ = self.shape
+            autotune.tune_lengths([(nx_, nz_ * ny_, self.bufs[2]), (ny_, nz_ * nx_, self.bufs[1]),
+                                   (nz_, ny_ * nx_, self.bufs[0])], dtype, self.device)
             return
         nbytes = lib.mjx_spec3d_plan_bytes(*self.shape, self.code)
         if nbytes == 0:

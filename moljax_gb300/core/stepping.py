@@ -433,6 +433,8 @@ def _adaptive_explicit(model, y0, t0, t_end, dt0, method, max_steps, cfl_params,
     pid_params = pid_params or PIDParams()
     interior = stencil.unpad(stencil.stack(y0, names), grid)
     N.require_cuda(interior)
+    from moljax_gb300.core import autotune
+    autotune.tune_stencil_once(model, interior.dtype)  # tile height of the stage kernel, once per size
     prob = explicit_problem(model, _EXPLICIT[method], cfl_params, t0, max_attempts)
     lib = N.lib()
     dev = interior.device

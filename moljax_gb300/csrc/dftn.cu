@@ -20,6 +20,7 @@
 #include <vector>
 
 #include "fft.cuh"
+#include "autotune.cuh"
 
 namespace mjx {
 
@@ -51,6 +52,11 @@ static DftGeom dft_geom(int n, int elem) {
   const bool pow2 = ilog2_exact(n) >= 0;
   g.nrad = pow2 ? 0 : radix_plan(n, g.rad);
   g.mixed = !pow2 && g.nrad > 0;
+  DftTune t;
+  if (g.mixed && tune_dft_get(n, elem, &t) && t.nrad > 0) {  // an autotuned schedule
+    g.nrad = t.nrad;
+    for (int i = 0; i < 16; ++i) g.rad[i] = t.rad[i];
+  }
   g.bluestein = !pow2 && !g.mixed;
   g.L = n;
   if (g.bluestein) {
@@ -333,6 +339,20 @@ __global__ void general_mult_kernel(cx<T>* __restrict__ s, const T* __restrict__
   }
 }
 
+// threads per sequence tp in [1, 256] (default n/8); sequences per CTA within 256
+// threads and 96 KB of shared memory
+template <typename T>
+static void mixed_launch(DftArgs<T>& a, int tp) {
+  int T_ = tp;
+  if (T_ < 1) T_ = 1;
+  if (T_ > 256) T_ = 256;
+  a.tpsm = T_;
+  int ns = 256 / T_;
+  const int cap = (int)((96 * 1024) / (2 * (size_t)a.n * sizeof(cx<T>)));
+  if (ns > cap) ns = cap;
+  a.nseq = ns < 1 ? 1 : ns;
+}
+
 template <typename T>
 static DftArgs<T> dft_args(const void* plan, int n, cx<T>* data, long long nrows, long long ld, int inverse) {
   const DftGeom g = dft_geom(n, sizeof(T));
@@ -345,15 +365,9 @@ static DftArgs<T> dft_args(const void* plan, int n, cx<T>* data, long long nrows
   a.mixed = g.mixed; a.nrad = g.nrad;
   for (int i = 0; i < 16; ++i) a.rad[i] = g.rad[i];
   if (g.mixed) {
-    // threads per sequence n/8 in [1, 256]; sequences per CTA within 256 threads and 96 KB
-    int T_ = n / 8;
-    if (T_ < 1) T_ = 1;
-    if (T_ > 256) T_ = 256;
-    a.tpsm = T_;
-    int ns = 256 / T_;
-    const int cap = (int)((96 * 1024) / (2 * (size_t)n * sizeof(cx<T>)));
-    if (ns > cap) ns = cap;
-    a.nseq = ns < 1 ? 1 : ns;
+    DftTune t;
+    const int tp = (tune_dft_get(n, (int)sizeof(T), &t) && t.tpsm > 0) ? t.tpsm : n / 8;
+    mixed_launch(a, tp);
   } else {
     const int tps = g.L >= 16 ? g.L / 16 : 1;
     a.nseq = tps >= 256 ? 1 : 256 / tps;
@@ -617,3 +631,95 @@ mjx_status mjx_spectral_apply_general3d(const void* plan_z, const void* plan_y, 
 }
 
 }  // extern "C"
+
+// Autotuner of the mixed-radix row DFT of length n: every candidate schedule
+// (dft_schedules) with threads per sequence n/4, n/8 and n/16 is timed on nrows rows of
+// scratch (one warm-up launch, then reps launches between CUDA events); the fastest is
+// installed in the registry for n and this element size.
+template <typename T>
+static mjx_status tune_dft(const void* plan, int n, long long nrows, cx<T>* data, int reps, double* times,
+                           int max_times, int* n_cand, int* best, cudaStream_t s) {
+  int sched[64 * 17];
+  const int ns = dft_schedules(n, sched, 64);
+  if (ns == 0) return MJX_BAD_ARG;
+  int tps[3] = {n / 4, n / 8, n / 16}, ntp = 0;
+  int uniq[3];
+  for (int i = 0; i < 3; ++i) {
+    int v = tps[i] < 1 ? 1 : (tps[i] > 256 ? 256 : tps[i]);
+    bool dup = false;
+    for (int j = 0; j < ntp; ++j) dup |= uniq[j] == v;
+    if (!dup) uniq[ntp++] = v;
+  }
+  tune_dft_clear(n, (int)sizeof(T));
+  DftArgs<T> a = dft_args<T>(plan, n, data, nrows, n, 0);
+  cudaEvent_t e0, e1;
+  MJX_CUDA_TRY(cudaEventCreate(&e0));
+  MJX_CUDA_TRY(cudaEventCreate(&e1));
+  double best_t = 1e300;
+  int best_i = -1, k = 0;
+  mjx_status st = MJX_OK;
+  for (int i = 0; i < ns && st == MJX_OK; ++i) {
+    for (int j = 0; j < ntp && st == MJX_OK; ++j, ++k) {
+      a.nrad = sched[17 * i];
+      for (int q = 0; q < 16; ++q) a.rad[q] = sched[17 * i + 1 + q];
+      mixed_launch(a, uniq[j]);
+      cudaError_t ce = dft_rows<T>(a, s);
+      if (ce == cudaSuccess) ce = cudaEventRecord(e0, s);
+      for (int r = 0; r < reps && ce == cudaSuccess; ++r) ce = dft_rows<T>(a, s);
+      if (ce == cudaSuccess) ce = cudaEventRecord(e1, s);
+      if (ce == cudaSuccess) ce = cudaEventSynchronize(e1);
+      float ms = 0.f;
+      if (ce == cudaSuccess) ce = cudaEventElapsedTime(&ms, e0, e1);
+      if (ce != cudaSuccess) { set_last_error(ce, __FILE__, __LINE__); st = MJX_CUDA_ERROR; break; }
+      const double tpl = (double)ms / reps;
+      if (times && k < max_times) times[k] = tpl;
+      if (tpl < best_t) { best_t = tpl; best_i = k; }
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (st != MJX_OK) return st;
+  const int bi = best_i / ntp, bj = best_i - bi * ntp;
+  DftTune t;
+  memset(&t, 0, sizeof(t));
+  t.nrad = sched[17 * bi];
+  for (int q = 0; q < 16; ++q) t.rad[q] = sched[17 * bi + 1 + q];
+  t.tpsm = uniq[bj];
+  tune_dft_put(n, (int)sizeof(T), t);
+  if (n_cand) *n_cand = ns * ntp;
+  if (best) *best = best_i;
+  return MJX_OK;
+}
+
+mjx_status mjx_autotune_dft(const void* plan, int n, int dtype, long long nrows, void* scratch,
+                            size_t scratch_bytes, int reps, double* times, int max_times, int* n_cand,
+                            int* best, void* stream) {
+  const int e = elem_size(dtype);
+  if (!e) return MJX_BAD_DTYPE;
+  if (!plan || !scratch || !dft_len_ok(n) || nrows < 1 || reps < 1) return MJX_BAD_ARG;
+  if (scratch_bytes < (size_t)nrows * n * 2 * e) return MJX_WORKSPACE;
+  const DftGeom g = dft_geom(n, e);
+  if (!g.mixed) {
+    if (n_cand) *n_cand = 0;  // powers of two and Bluestein lengths have no schedule to tune
+    if (best) *best = -1;
+    return MJX_OK;
+  }
+  MJX_TRY(set_dft_attrs());
+  cudaStream_t s = (cudaStream_t)stream;
+  MJX_CUDA_TRY(cudaMemsetAsync(scratch, 0, (size_t)nrows * n * 2 * e, s));
+  if (e == 4)
+    return tune_dft<float>(plan, n, nrows, (cx<float>*)scratch, reps, times, max_times, n_cand, best, s);
+  return tune_dft<double>(plan, n, nrows, (cx<double>*)scratch, reps, times, max_times, n_cand, best, s);
+}
+
+mjx_status mjx_dft_schedule_get(int n, int dtype, int* nrad, int* rad, int* tpsm) {
+  const int e = elem_size(dtype);
+  if (!e) return MJX_BAD_DTYPE;
+  if (!nrad || !rad || !tpsm || !dft_len_ok(n)) return MJX_BAD_ARG;
+  const DftGeom g = dft_geom(n, e);
+  *nrad = g.mixed ? g.nrad : 0;
+  for (int i = 0; i < 16; ++i) rad[i] = g.mixed ? g.rad[i] : 0;
+  DftTune t;
+  *tpsm = g.mixed ? ((tune_dft_get(n, e, &t) && t.tpsm > 0) ? t.tpsm : (n / 8 < 1 ? 1 : (n / 8 > 256 ? 256 : n / 8))) : 0;
+  return MJX_OK;
+}

@@ -23,6 +23,7 @@
 #include <string.h>
 
 #include "spectral.cuh"
+#include "autotune.cuh"
 
 namespace mjx {
 
@@ -67,6 +68,7 @@ struct XStage {
   double atol, rtol;
   double* partial;
   int* nonfinite;
+  int rows;  // rows per warp strip (tile height / XWARPS); 0: the tuned or default value
 };
 
 template <typename T>
@@ -76,13 +78,13 @@ __device__ __forceinline__ T* xbuf(const XStage<T>& a, int id, int cur) {
   return a.buf[id];
 }
 
-// Tiles of 32 columns x XTILE_ROWS rows; block (32, 8): each warp owns a strip of
-// XROWS rows and slides a three-row window down it.  The loads of a row are issued one
+// Tiles of 32 columns x (rows x XWARPS) rows; block (32, 8): each warp owns a strip of
+// `rows` rows (autotuned per grid size, default 8) and slides a three-row window down it.  The loads of a row are issued one
 // row ahead (row y+2 of the stage input and row y+1 of the combine operands while row y
 // is computed), with the BC ghosts applied by selects after branch-free index choices;
 // the x-neighbours come from the lanes by shuffle (lanes 0 and 31 and the grid edges
 // read theirs directly).  Coefficients arrive in the state type (XCoef).
-enum { XROWS = 8, XWARPS = 8, XTILE_ROWS = XROWS * XWARPS };
+enum { XROWS_DEFAULT = 8, XWARPS = 8 };
 
 // the ghost formula of moljax/core/bc.py:202-307 on the boundary-adjacent value s
 template <typename T>
@@ -125,7 +127,8 @@ __global__ void __launch_bounds__(256, sizeof(T) == 8 ? 2 : (NF == 4 ? 3 : 4)) r
   const T cp2 = k.cp2, cq2 = k.cq2, cf2h = k.cf2 * h;
   const T rF = k.F, rFk = k.Fk, rr = k.r;
   const int lane = threadIdx.x;
-  const int ntx = (nx + 31) >> 5, nty = (ny + XTILE_ROWS - 1) / XTILE_ROWS;
+  const int rows = a.rows, tile_rows = rows * XWARPS;
+  const int ntx = (nx + 31) >> 5, nty = (ny + tile_rows - 1) / tile_rows;
   const int ntiles = ntx * nty;
   T esum = (T)0;  // per thread in the state type; FP64 across threads (as the row kernels)
   int bad = 0;
@@ -133,9 +136,9 @@ __global__ void __launch_bounds__(256, sizeof(T) == 8 ? 2 : (NF == 4 ? 3 : 4)) r
     const int ty = tile / ntx, tx = tile - ty * ntx;
     const int x = tx * 32 + lane;
     const int xc = x < nx ? x : nx - 1;
-    const int y0 = ty * XTILE_ROWS + threadIdx.y * XROWS;
+    const int y0 = ty * tile_rows + threadIdx.y * rows;
     if (y0 >= ny) continue;  // warp-uniform: a warp is one threadIdx.y
-    const int y1 = y0 + XROWS < ny ? y0 + XROWS : ny;
+    const int y1 = y0 + rows < ny ? y0 + rows : ny;
     // x-neighbour columns of the lane that reads one directly (lane 0: left, others: right)
     T up[NF], cc[NF], dn[NF], pn[NF], qn[NF];
 #pragma unroll
@@ -395,7 +398,12 @@ template <typename T>
 static cudaError_t launch_stage(const XStage<T>& s0, int rx, cudaStream_t st) {
   XStage<T> s = s0;
   x_coef(s);
-  const long long tiles = (long long)((s.m.nx + 31) / 32) * ((s.m.ny + XTILE_ROWS - 1) / XTILE_ROWS);
+  if (s.rows <= 0) {
+    const int tuned = tune_rows_get(s.m.ny, s.m.nx, s.m.nf, (int)sizeof(T));
+    s.rows = tuned > 0 ? tuned : XROWS_DEFAULT;
+  }
+  const int tile_rows = s.rows * XWARPS;
+  const long long tiles = (long long)((s.m.nx + 31) / 32) * ((s.m.ny + tile_rows - 1) / tile_rows);
   // one resident wave (4 blocks of 256 threads per SM) looping over the tiles; the error
   // pass always fills XNPARTS partials
   const int blocks = s.err ? XNPARTS : (int)(tiles < XNPARTS ? tiles : XNPARTS);
@@ -638,10 +646,14 @@ static cudaError_t launch_fused_rx(const XFused<T>& f, cudaStream_t s) {
   const int nfa = f.m.nf <= 2 ? 2 : 4;
   const size_t smem = fused_smem<T>(f.nst, nfa);
   const unsigned blocks = (unsigned)(((f.m.nx + FTX - 1) / FTX) * ((f.m.ny + FTY - 1) / FTY));
-  if (f.nst == 4) {
-    return nfa == 2 ? launch_fused_t<T, RX, 2, 4>(f, smem, blocks, s) : launch_fused_t<T, RX, 4, 4>(f, smem, blocks, s);
+  if constexpr (RX == RX_GRAY_SCOTT) {  // two fields only
+    return f.nst == 4 ? launch_fused_t<T, RX, 2, 4>(f, smem, blocks, s) : launch_fused_t<T, RX, 2, 3>(f, smem, blocks, s);
+  } else {
+    if (f.nst == 4) {
+      return nfa == 2 ? launch_fused_t<T, RX, 2, 4>(f, smem, blocks, s) : launch_fused_t<T, RX, 4, 4>(f, smem, blocks, s);
+    }
+    return nfa == 2 ? launch_fused_t<T, RX, 2, 3>(f, smem, blocks, s) : launch_fused_t<T, RX, 4, 3>(f, smem, blocks, s);
   }
-  return nfa == 2 ? launch_fused_t<T, RX, 2, 3>(f, smem, blocks, s) : launch_fused_t<T, RX, 4, 3>(f, smem, blocks, s);
 }
 
 template <typename T>
@@ -907,3 +919,64 @@ mjx_status mjx_explicit_adaptive2d(const mjx_grid2d* grid, int dtype, const mjx_
 }
 
 }  // extern "C"
+
+// Autotuner of the stencil stage's tile height: one RK4 middle stage (stage input,
+// step start and running sum read; two outputs) of the problem is timed for strips of
+// 2, 4, 8, 16 and 32 rows per warp (one warm-up launch, then reps launches between
+// CUDA events) on the workspace buffers, and the fastest is installed for this grid
+// size, field count and element size.
+template <typename T>
+static mjx_status tune_stencil(const XModel& m, char* ws, const XLayout& L, int reps, double* times, int max_times,
+                               int* best_rows, cudaStream_t s) {
+  static const int cand[5] = {2, 4, 8, 16, 32};
+  XStage<T> st;
+  memset(&st, 0, sizeof(st));
+  st.m = m;
+  for (int i = 0; i < 7; ++i) st.buf[i] = (T*)(ws + L.b[i]);
+  st.w = XB_W1; st.p = XB_YCUR; st.q = XB_ACC; st.o1 = XB_W2; st.o2 = XB_ACC;
+  st.cp1 = 1; st.cf1 = 0.5; st.cq2 = 1; st.cf2 = 1.0 / 3.0;
+  st.hfac = 1.0; st.hfixed = 1e-6;
+  const int rx = m.reaction == MJX_REACT_GRAY_SCOTT ? RX_GRAY_SCOTT : (m.reaction == MJX_REACT_FISHER ? RX_FISHER : RX_NONE);
+  cudaEvent_t e0, e1;
+  MJX_CUDA_TRY(cudaEventCreate(&e0));
+  MJX_CUDA_TRY(cudaEventCreate(&e1));
+  double best_t = 1e300;
+  int bi = -1;
+  cudaError_t ce = cudaSuccess;
+  for (int i = 0; i < 5 && ce == cudaSuccess; ++i) {
+    st.rows = cand[i];
+    ce = launch_stage<T>(st, rx, s);
+    if (ce == cudaSuccess) ce = cudaEventRecord(e0, s);
+    for (int r = 0; r < reps && ce == cudaSuccess; ++r) ce = launch_stage<T>(st, rx, s);
+    if (ce == cudaSuccess) ce = cudaEventRecord(e1, s);
+    if (ce == cudaSuccess) ce = cudaEventSynchronize(e1);
+    float ms = 0.f;
+    if (ce == cudaSuccess) ce = cudaEventElapsedTime(&ms, e0, e1);
+    if (ce != cudaSuccess) break;
+    const double tpl = (double)ms / reps;
+    if (times && i < max_times) times[i] = tpl;
+    if (tpl < best_t) { best_t = tpl; bi = i; }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (ce != cudaSuccess) { set_last_error(ce, __FILE__, __LINE__); return MJX_CUDA_ERROR; }
+  tune_rows_put(m.ny, m.nx, m.nf, (int)sizeof(T), cand[bi]);
+  if (best_rows) *best_rows = cand[bi];
+  return MJX_OK;
+}
+
+mjx_status mjx_autotune_stencil2d(const mjx_grid2d* grid, int dtype, const mjx_explicit_problem* prob, void* ws,
+                                  size_t ws_bytes, int reps, double* times, int max_times, int* best_rows,
+                                  void* stream) {
+  XModel m;
+  MJX_TRY(x_model(prob, grid, &m));
+  const int e = elem_size(dtype);
+  if (!e) return MJX_BAD_DTYPE;
+  if (reps < 1) return MJX_BAD_ARG;
+  const XLayout L = x_layout(m.nf, m.ny, m.nx, e);
+  if (ws == nullptr || ws_bytes < L.total) return MJX_WORKSPACE;
+  cudaStream_t s = (cudaStream_t)stream;
+  MJX_CUDA_TRY(cudaMemsetAsync(ws, 0, L.part, s));  // the state buffers: finite values to time on
+  if (e == 4) return tune_stencil<float>(m, (char*)ws, L, reps, times, max_times, best_rows, s);
+  return tune_stencil<double>(m, (char*)ws, L, reps, times, max_times, best_rows, s);
+}
