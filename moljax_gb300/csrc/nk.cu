@@ -59,6 +59,18 @@ __device__ __forceinline__ T dval(const T* u, int i, int j, int n) {
   return ((i < 0) != (i >= n)) || ((j < 0) != (j >= n)) ? -v : v;
 }
 
+// (row, column) of flat index p in rows of length n: 32-bit division whenever p fits
+__device__ __forceinline__ void nk_rowcol(long long p, int n, int& i, int& j) {
+  if (p < 4294967296LL) {
+    const unsigned q = (unsigned)p / (unsigned)n;
+    i = (int)q;
+    j = (int)((unsigned)p - q * (unsigned)n);
+  } else {
+    i = (int)(p / n);
+    j = (int)(p - (long long)i * n);
+  }
+}
+
 // R = a0 y + cst - beta F(y); part[block] = sum R^2; b32 = -R (optional)
 __global__ void vd_residual_kernel(const double* __restrict__ y, const double* __restrict__ cst,
                                    double* __restrict__ R, float* __restrict__ b32,
@@ -69,7 +81,8 @@ __global__ void vd_residual_kernel(const double* __restrict__ y, const double* _
   const long long N2 = (long long)n * n;
   for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < N2;
        p += (long long)gridDim.x * blockDim.x) {
-    const int i = (int)(p / n), j = (int)(p - (long long)i * n);
+    int i, j;
+    nk_rowcol(p, n, i, j);
     const double uc = y[p];
     const double ue = dval(y, i, j + 1, n), uw = dval(y, i, j - 1, n);
     const double un = dval(y, i + 1, j, n), us = dval(y, i - 1, j, n);
@@ -100,7 +113,8 @@ __global__ void vd_rhs_kernel(const double* __restrict__ y, double* __restrict__
   const long long N2 = (long long)n * n;
   for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < N2;
        p += (long long)gridDim.x * blockDim.x) {
-    const int i = (int)(p / n), j = (int)(p - (long long)i * n);
+    int i, j;
+    nk_rowcol(p, n, i, j);
     const double uc = y[p];
     const double ue = dval(y, i, j + 1, n), uw = dval(y, i, j - 1, n);
     const double un = dval(y, i + 1, j, n), us = dval(y, i - 1, j, n);
@@ -113,17 +127,20 @@ __global__ void vd_rhs_kernel(const double* __restrict__ y, double* __restrict__
 }
 
 // odd extension N x N -> 2N x 2N (Dirichlet cell-centred <-> periodic)
+// rows 0..n-1 of the 2n x 2n cell-centred odd extension (each row [r_i, -reverse(r_i)]);
+// rows n..2n-1, the negated mirror, are synthesised by the column pass (ColArgs::oddy)
 __global__ void oddext_kernel(const float* __restrict__ r, float* __restrict__ e, int n,
                               const GmresState* gs) {
   if (gs && gs->converged) return;
   const int m = 2 * n;
-  const long long M2 = (long long)m * m;
+  const long long M2 = (long long)n * m;
   for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < M2;
        p += (long long)gridDim.x * blockDim.x) {
-    const int i = (int)(p / m), j = (int)(p - (long long)i * m);
-    const int ii = i < n ? i : 2 * n - 1 - i, jj = j < n ? j : 2 * n - 1 - j;
-    const float sgn = ((i < n) == (j < n)) ? 1.f : -1.f;
-    e[p] = sgn * r[(long long)ii * n + jj];
+    int i, j;
+    nk_rowcol(p, m, i, j);
+    const int jj = j < n ? j : 2 * n - 1 - j;
+    const float sgn = j < n ? 1.f : -1.f;
+    e[p] = sgn * r[(long long)i * n + jj];
   }
 }
 
@@ -134,7 +151,8 @@ __global__ void restrict_kernel(const float* __restrict__ e, float* __restrict__
   const long long N2 = (long long)n * n;
   for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < N2;
        p += (long long)gridDim.x * blockDim.x) {
-    const int i = (int)(p / n), j = (int)(p - (long long)i * n);
+    int i, j;
+    nk_rowcol(p, n, i, j);
     w[p] = s * e[(long long)i * 2 * n + j];
   }
 }
@@ -422,7 +440,8 @@ __global__ void vd_jvp_j_kernel(const float* y32, float* V, const GmresState* gs
   const float s = gs ? (float)gs->hnext_inv : 1.0f;
   for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < N2;
        p += (long long)gridDim.x * blockDim.x) {
-    const int i = (int)(p / n), jj = (int)(p - (long long)i * n);
+    int i, jj;
+    nk_rowcol(p, n, i, jj);
     const float uc = y32[p], ue = dval(y32, i, jj + 1, n), uw = dval(y32, i, jj - 1, n);
     const float un = dval(y32, i + 1, jj, n), us = dval(y32, i - 1, jj, n);
     const float vc = s * vin[p], ve = s * dval(vin, i, jj + 1, n), vw = s * dval(vin, i, jj - 1, n);
@@ -509,11 +528,13 @@ static cudaError_t precond(NKRun& r, const float* src, float* w, const GmresStat
   cx<float>* spec = (cx<float>*)(r.ws + r.L.spec);
   RowArgs<float> ro;
   memset(&ro, 0, sizeof(ro));
-  ro.n = 2 * n; ro.log2n = ilog2_exact(2 * n); ro.ldc = spec_ldc(2 * n); ro.nrows = n; ro.npairs = 1;
-  ro.nseq = row_nseq(2 * n, n); ro.rstride = 2 * n; ro.rin_sel = -1; ro.rout_sel = -1;
+  // the n distinct rows of the extension as n/2 pairs (i, i + n/2)
+  const int hn = n / 2;
+  ro.n = 2 * n; ro.log2n = ilog2_exact(2 * n); ro.ldc = spec_ldc(2 * n); ro.nrows = hn; ro.npairs = 1;
+  ro.nseq = row_nseq(2 * n, hn); ro.rstride = 2 * n; ro.rin_sel = -1; ro.rout_sel = -1;
   ro.rin[0] = P32(r, r.L.e); ro.rout[0] = P32(r, r.L.e); ro.spec = spec; ro.tw = (const cx<float>*)pv.twx;
   ro.inv_scale = 1.0f;
-  ro.pr[0].ra = 0; ro.pr[0].rb = (long long)n * 2 * n; ro.pr[0].sa = 0; ro.pr[0].sb = (long long)n * ro.ldc;
+  ro.pr[0].ra = 0; ro.pr[0].rb = (long long)hn * 2 * n; ro.pr[0].sa = 0; ro.pr[0].sb = (long long)hn * ro.ldc;
   ro.pr[0].flags = ROW_STORE_SPEC;
   // converged Arnoldi steps skip the pass through the state flag of the spectral kernels
   ro.st = (const DevState*)(r.ws + r.L.pst);
@@ -523,7 +544,7 @@ static cudaError_t precond(NKRun& r, const float* src, float* w, const GmresStat
   c.ny = 2 * n; c.log2ny = ilog2_exact(2 * n); c.ncols = n + 1; c.ldc = ro.ldc;
   c.C = col_tile(2 * n, c.ncols, 1, 4); c.spec = spec; c.lamx = (const float*)pv.lamx;
   c.lamy = (const float*)pv.lamy; c.tw = (const cx<float>*)pv.twy;
-  c.scale = (float)(1.0 / (4.0 * n * n)); c.st = ro.st; c.njobs = 1;
+  c.scale = (float)(1.0 / (4.0 * n * n)); c.st = ro.st; c.njobs = 1; c.oddy = 1;
   c.job[0].nout = 1; c.job[0].mul = MUL_HELMHOLTZ; c.job[0].D = 1.0; c.job[0].hfac[0] = c.job[0].hfac[1] = 1.0;
   c.job[0].pow[0] = c.job[0].pow[1] = 1;
   if ((e = launch_col<float>(c, r.s)) != cudaSuccess) return e;

@@ -325,7 +325,12 @@ __global__ void __launch_bounds__(ColThreads<T>::v, 1) col_kernel(const __grid_c
     for (int m = 0; m < 16; ++m) {
       const int e = tid + m * nth;
       const int ky = e / Cn, c = e - ky * Cn, kx = kx0 + c;
-      if (e < ny * Cn) v[m] = kx < a.ncols ? a.spec[po + jb.sin + ky * ldc + kx] : mk<C>((T)0, (T)0);
+      const bool mir = a.oddy && ky >= (ny >> 1);
+      const int kyl = mir ? ny - 1 - ky : ky;
+      if (e < ny * Cn) {
+        v[m] = kx < a.ncols ? a.spec[po + jb.sin + kyl * ldc + kx] : mk<C>((T)0, (T)0);
+        if (mir) v[m] = mk<C>(-v[m].x, -v[m].y);
+      }
     }
 #pragma unroll
     for (int m = 0; m < 16; ++m) {
@@ -401,7 +406,7 @@ __global__ void __launch_bounds__(ColThreads<T>::v, 1) col_kernel(const __grid_c
   for (int e = tid; e < ny * W; e += nth) {
     const int ky = e / W, col = e - ky * W;
     const int o = col / Cn, c = col - o * Cn, kx = kx0 + c;
-    if (kx < a.ncols) a.spec[po + jb.sout[o] + ky * ldc + kx] = buf[sp(ky * W + col)];
+    if (kx < a.ncols && !(a.oddy && ky >= (ny >> 1))) a.spec[po + jb.sout[o] + ky * ldc + kx] = buf[sp(ky * W + col)];
   }
 }
 

@@ -112,6 +112,10 @@ template <typename T> struct ColArgs {
   int ldc3;
   const T* lamy2;
   const T* mtab;         // MUL_TABLE: [ny][ldc] real multipliers
+  // odd extension along the column: rows ky >= ny/2 are not stored; they are loaded as
+  // the negated mirror -row(ny-1-ky) and only rows ky < ny/2 are written back (the
+  // cell-centred odd extension of a Dirichlet DST-II solve)
+  int oddy;
   ColJob job[MJX_MAXJOB];
 };
 
