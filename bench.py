@@ -13,6 +13,7 @@ of the reaction increments (rel-L2 vs the FP64 path is reported in the line).
   python bench.py --workload fft3d --n 512 [--etd-steps S] [--fp32]
   python bench.py --workload explicit --n 4096 [--etd-steps S]      (RK4 advection-diffusion)
   python bench.py --workload nk --n 512 [--etd-steps S]             (BDF2 Newton-Krylov)
+  python bench.py --workload stencil --n 4096 [--fp32]               (stencil stage kernel roofline)
 
 Our arm prints one JSON line with the device-timed value, the end-to-end
 number through the public API with host buffers, the live roofline of the
@@ -63,7 +64,7 @@ def parse():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp32"])
     ap.add_argument("--kernels-only", action="store_true")
-    ap.add_argument("--workload", default="imex", choices=["imex", "etdrk4", "serve", "fft3d", "explicit", "nk"])
+    ap.add_argument("--workload", default="imex", choices=["imex", "etdrk4", "serve", "fft3d", "explicit", "nk", "stencil"])
     ap.add_argument("--fp32", action="store_true", help="fft3d: FP32 instead of FP64")
     ap.add_argument("--requests", type=int, default=512)
     ap.add_argument("--etd-steps", type=int, default=100)
@@ -637,6 +638,36 @@ def explicit_cpu_baseline(n=1024, steps=48):
             "sample": f"{steps} RK4 steps of the same model at {n}^2 in {d:.1f} s (NumPy FP64 restatement)"}
 
 
+def run_stencil(args, local):
+    """The stencil stage kernel alone (rk_stage_vec_kernel / rk_stage_kernel): one RK4
+    middle stage of the two-field advection-diffusion model of the explicit workload at
+    n^2, timed by the autotuner for each tile height (CUDA events, 20 launches each after
+    a warm-up launch).  Algorithmic bytes per point and field: stage input, step start and
+    running sum read, two outputs written = 5 accesses (20 B in FP32, 40 B in FP64); the
+    5-point neighbours come from cache."""
+    import torch
+    import moljax_gb300 as M
+    from moljax_gb300.core import autotune as AT
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    n = args.n
+    dtype = torch.float32 if args.fp32 else torch.float64
+    grid = M.Grid2D(n, n, 0.0, 1.0, 0.0, 1.0)
+    model = M.create_advection_diffusion_model(grid, ("c1", "c2"), D=1e-4, vx=0.5, vy=-0.3, dtype=dtype)
+    res = AT.autotune_stencil(model, dtype, reps=20)
+    esz = 4 if dtype == torch.float32 else 8
+    b = 2 * n * n * 5 * esz
+    peak, peak_kind = peaks()
+    t = min(res.times_ms) * 1e-3
+    return {"workload": f"stencil stage (RK4 middle stage) advection-diffusion 2 fields {n}x{n} "
+                        f"{'FP32' if dtype == torch.float32 else 'FP64'}",
+            "n": n, "kernel": "rk_stage_vec_kernel" if n % (16 // esz) == 0 else "rk_stage_kernel",
+            "tile_heights": [c[0] for c in res.candidates], "ms_per_launch": res.times_ms,
+            "best_rows": res.choice[0], "alg_bytes": b,
+            "roofline": {"bound": "hbm", "achieved": b / t / 1e9, "peak": peak, "peak_kind": peak_kind,
+                         "unit": "GB/s", "frac": b / t / 1e9 / peak}}
+
+
 def run_nk(args, local):
     """Fixed-step BDF2 (BE first step) of u_t = div((1 + u^2) grad u) - u^3 on the unit square
     with Dirichlet walls at n^2 cell centres, u0 a seeded sum of 8 Gaussians (A ~ U[0,1],
@@ -792,6 +823,8 @@ def main():
         out = run_explicit(args, local)
     elif args.workload == "nk":
         out = run_nk(args, local)
+    elif args.workload == "stencil":
+        out = run_stencil(args, local)
     elif args.kernels_only:
         out = run_kernels_only(args, local)
     else:

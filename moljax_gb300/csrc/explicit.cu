@@ -21,6 +21,7 @@
 // IMEX driver.
 #include <math.h>
 #include <string.h>
+#include <stdint.h>
 
 #include "spectral.cuh"
 #include "autotune.cuh"
@@ -371,6 +372,220 @@ static XAttempt<T> build_x(const XModel& m, int method, char* ws, const XLayout&
   return A;
 }
 
+// 128-bit form of rk_stage_kernel: a thread owns V = 16 / sizeof(T) consecutive columns
+// (one float4 / double2 per row, field and operand), a warp 32 V columns; the x-neighbours
+// of a lane's first and last column come from the neighbouring lanes by shuffle (lanes 0
+// and 31 and the grid edges read theirs, or the BC ghost, directly).  Used when nx is a
+// multiple of V and every buffer is 16-byte aligned; same arithmetic per point as the
+// scalar kernel, so the results are identical.
+template <typename T> struct Vec16;
+template <> struct Vec16<float> { typedef float4 t; enum { V = 4 }; };
+template <> struct Vec16<double> { typedef double2 t; enum { V = 2 }; };
+
+template <typename T, int V>
+__device__ __forceinline__ void vload(const T* p, T (&v)[V]) {
+  typedef typename Vec16<T>::t VT;
+  const VT q = *reinterpret_cast<const VT*>(p);
+  const T* e = reinterpret_cast<const T*>(&q);
+#pragma unroll
+  for (int k = 0; k < V; ++k) v[k] = e[k];
+}
+
+template <typename T, int V>
+__device__ __forceinline__ void vstore(T* p, const T (&v)[V]) {
+  typedef typename Vec16<T>::t VT;
+  VT q;
+  T* e = reinterpret_cast<T*>(&q);
+#pragma unroll
+  for (int k = 0; k < V; ++k) e[k] = v[k];
+  *reinterpret_cast<VT*>(p) = q;
+}
+
+// row yy in [-1, ny] of field f at columns xb .. xb+V-1 (ghost rows from the BC formulas)
+template <typename T, int V>
+__device__ __forceinline__ void xrow_v(const T* wf, int yy, int xb, const XModel& m, const XCoef<T>& k, int f,
+                                       T (&v)[V]) {
+  const int ny = m.ny, kind = m.kind[f];
+  const bool lo = yy < 0, hi = yy >= ny;
+  const int ys = lo ? (kind == MJX_BC_PERIODIC ? ny - 1 : 0) : (hi ? (kind == MJX_BC_PERIODIC ? 0 : ny - 1) : yy);
+  vload<T, V>(wf + (long long)ys * m.nx + xb, v);
+  if (lo || hi) {
+    const T g = lo ? k.gv[f][2] : k.gv[f][3];
+#pragma unroll
+    for (int q = 0; q < V; ++q) v[q] = xghost(v[q], kind, g, lo);
+  }
+}
+
+template <typename T, int RX, int NF>
+__global__ void __launch_bounds__(256, NF == 4 ? 1 : 2)
+rk_stage_vec_kernel(const __grid_constant__ XStage<T> a) {
+  constexpr int V = Vec16<T>::V;
+  const DevState* st = a.st;
+  if (st != nullptr && st->done) return;
+  const XModel& m = a.m;
+  const int cur = st != nullptr ? st->cur : 0;
+  const XCoef<T>& k = a.k;
+  const T h = st != nullptr ? (T)st->dtc * k.hfac : k.hfixed;
+  const T* W = xbuf(a, a.w, cur);
+  const bool hasP = a.p >= 0, hasQ = a.q >= 0;
+  const T* P = hasP ? xbuf(a, a.p, cur) : W;
+  const T* Q = hasQ ? xbuf(a, a.q, cur) : W;
+  T* O1 = xbuf(a, a.o1, cur);
+  T* O2 = a.o2 >= 0 ? xbuf(a, a.o2, cur) : nullptr;
+  const T* YF = a.buf[XB_YF];
+  const int nf = m.nf, ny = m.ny, nx = m.nx, adv = m.advection;
+  const long long per = (long long)ny * nx;
+  const T idx2 = k.idx2, idy2 = k.idy2, idx = k.idx, idy = k.idy, vx = k.vx, vy = k.vy;
+  const bool vxpos = k.vxpos != 0, vypos = k.vypos != 0;
+  const T cp1 = k.cp1, cq1 = k.cq1, cf1h = k.cf1 * h;
+  const T cp2 = k.cp2, cq2 = k.cq2, cf2h = k.cf2 * h;
+  const T rF = k.F, rFk = k.Fk, rr = k.r;
+  const int lane = threadIdx.x;
+  const int rows = a.rows, tile_rows = rows * XWARPS, tcols = 32 * V;
+  const int ntx = (nx + tcols - 1) / tcols, nty = (ny + tile_rows - 1) / tile_rows;
+  const int ntiles = ntx * nty;
+  T esum = (T)0;
+  int bad = 0;
+  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const int ty = tile / ntx, tx = tile - ty * ntx;
+    const int xb0 = (tx * 32 + lane) * V;
+    const bool valid = xb0 < nx;
+    const int xb = valid ? xb0 : nx - V;  // nx is a multiple of V
+    const int y0 = ty * tile_rows + threadIdx.y * rows;
+    if (y0 >= ny) continue;  // warp-uniform
+    const int y1 = y0 + rows < ny ? y0 + rows : ny;
+    T up[NF][V], cc[NF][V], dn[NF][V], pn[NF][V], qn[NF][V];
+#pragma unroll
+    for (int f = 0; f < NF; ++f) {
+      if (f >= nf) break;
+      const T* wf = W + f * per;
+      xrow_v<T, V>(wf, y0 - 1, xb, m, k, f, up[f]);
+      vload<T, V>(wf + (long long)y0 * nx + xb, cc[f]);
+      xrow_v<T, V>(wf, y0 + 1, xb, m, k, f, dn[f]);
+      const long long i0 = f * per + (long long)y0 * nx + xb;
+      vload<T, V>(P + i0, pn[f]);
+      vload<T, V>(Q + i0, qn[f]);
+    }
+    for (int y = y0; y < y1; ++y) {
+      const long long row = (long long)y * nx;
+      const int yn = y + 1 < y1 ? y + 1 : y;
+      const int y2 = y + 2 <= ny ? y + 2 : ny;
+      T c[NF][V], Fv[NF][V], pc[NF][V], qc[NF][V], d2[NF][V];
+#pragma unroll
+      for (int f = 0; f < NF; ++f) {  // the loads of the next row, issued first
+        if (f >= nf) break;
+        const T* wf = W + f * per;
+#pragma unroll
+        for (int q = 0; q < V; ++q) { pc[f][q] = pn[f][q]; qc[f][q] = qn[f][q]; }
+        xrow_v<T, V>(wf, y2, xb, m, k, f, d2[f]);
+        const long long i1 = f * per + (long long)yn * nx + xb;
+        vload<T, V>(P + i1, pn[f]);
+        vload<T, V>(Q + i1, qn[f]);
+      }
+#pragma unroll
+      for (int f = 0; f < NF; ++f) {
+        if (f >= nf) break;
+        const T* wf = W + f * per;
+        const int kind = m.kind[f];
+        // left neighbour of column xb and right neighbour of column xb + V - 1
+        T lft = __shfl_up_sync(0xffffffffu, cc[f][V - 1], 1);
+        T rgt = __shfl_down_sync(0xffffffffu, cc[f][0], 1);
+        if (lane == 0 || xb == 0) {
+          const int xl = xb > 0 ? xb - 1 : (kind == MJX_BC_PERIODIC ? nx - 1 : 0);
+          lft = wf[row + xl];
+          if (xb == 0) lft = xghost(lft, kind, k.gv[f][0], true);
+        }
+        if (lane == 31 || xb + V >= nx) {
+          const int xr = xb + V < nx ? xb + V : (kind == MJX_BC_PERIODIC ? 0 : nx - 1);
+          rgt = wf[row + xr];
+          if (xb + V >= nx) rgt = xghost(rgt, kind, k.gv[f][1], false);
+        }
+#pragma unroll
+        for (int q = 0; q < V; ++q) {
+          const T cv = cc[f][q], ym = up[f][q], yp = dn[f][q];
+          const T xm = q > 0 ? cc[f][q > 0 ? q - 1 : 0] : lft;
+          const T xp = q < V - 1 ? cc[f][q < V - 1 ? q + 1 : 0] : rgt;
+          T v = k.D[f] * ((xp - (T)2 * cv + xm) * idx2 + (yp - (T)2 * cv + ym) * idy2);
+          if (adv == 1) {
+            const T gx = vxpos ? (cv - xm) * idx : (xp - cv) * idx;
+            const T gy = vypos ? (cv - ym) * idy : (yp - cv) * idy;
+            v = v - vx * gx - vy * gy;
+          } else if (adv == 2) {
+            v = v - vx * (xp - xm) * (T)0.5 * idx - vy * (yp - ym) * (T)0.5 * idy;
+          }
+          c[f][q] = cv;
+          Fv[f][q] = v;
+        }
+#pragma unroll
+        for (int q = 0; q < V; ++q) { up[f][q] = cc[f][q]; cc[f][q] = dn[f][q]; dn[f][q] = d2[f][q]; }
+      }
+#pragma unroll
+      for (int q = 0; q < V; ++q) {
+        if (RX == RX_GRAY_SCOTT) {  // operators.py:644-667
+          const T uvv = c[0][q] * c[1][q] * c[1][q];
+          Fv[0][q] += -uvv + rF * ((T)1 - c[0][q]);
+          Fv[1][q] += uvv - rFk * c[1][q];
+        } else if (RX == RX_FISHER) {  // operators.py:680-705
+#pragma unroll
+          for (int f = 0; f < NF; ++f) {
+            if (f >= nf) break;
+            Fv[f][q] += rr * c[f][q] * ((T)1 - c[f][q]);
+          }
+        }
+      }
+      if (valid) {
+#pragma unroll
+        for (int f = 0; f < NF; ++f) {
+          if (f >= nf) break;
+          const long long i = f * per + row + xb;
+          T o1[V], o2[V];
+#pragma unroll
+          for (int q = 0; q < V; ++q) {
+            const T pv = hasP ? pc[f][q] : (T)0, qv = hasQ ? qc[f][q] : (T)0;
+            o1[q] = cp1 * pv + cq1 * qv + cf1h * Fv[f][q];
+            o2[q] = cp2 * pv + cq2 * qv + cf2h * Fv[f][q];
+          }
+          if (O2) vstore<T, V>(O2 + i, o2);
+          vstore<T, V>(O1 + i, o1);
+          if (a.err) {  // moljax/core/state.py:335-339
+            T yf[V];
+            vload<T, V>(YF + i, yf);
+#pragma unroll
+            for (int q = 0; q < V; ++q) {
+              const T e = (o1[q] - yf[q]) / (k.atol + k.rtol * (o1[q] < (T)0 ? -o1[q] : o1[q]));
+              esum += e * e;
+              bad |= !isfinite(o1[q]);
+            }
+          }
+        }
+      }
+    }
+  }
+  if (a.err) {
+    __shared__ double red[XWARPS];
+    __shared__ int redb[XWARPS];
+    double esd = (double)esum;
+    for (int o = 16; o > 0; o >>= 1) {
+      esd += __shfl_xor_sync(0xffffffffu, esd, o);
+      bad |= __shfl_xor_sync(0xffffffffu, bad, o);
+    }
+    if (lane == 0) { red[threadIdx.y] = esd; redb[threadIdx.y] = bad; }
+    __syncthreads();
+    if (lane == 0 && threadIdx.y == 0) {
+      double s = 0.0, cc = 0.0;
+      int b = 0;
+      for (int w = 0; w < XWARPS; ++w) {  // Kahan
+        const double yv = red[w] - cc, tv = s + yv;
+        cc = (tv - s) - yv;
+        s = tv;
+        b |= redb[w];
+      }
+      a.partial[blockIdx.x] = s;
+      a.nonfinite[blockIdx.x] = b;
+    }
+  }
+}
+
 // the state-type coefficients of a stage (XCoef), from its FP64 description
 template <typename T>
 static void x_coef(XStage<T>& s) {
@@ -403,11 +618,31 @@ static cudaError_t launch_stage(const XStage<T>& s0, int rx, cudaStream_t st) {
     s.rows = tuned > 0 ? tuned : XROWS_DEFAULT;
   }
   const int tile_rows = s.rows * XWARPS;
-  const long long tiles = (long long)((s.m.nx + 31) / 32) * ((s.m.ny + tile_rows - 1) / tile_rows);
+  // the 128-bit form when nx is a multiple of the vector width and every buffer is
+  // 16-byte aligned (offsets f * ny * nx elements keep the alignment then)
+  constexpr int V = Vec16<T>::V;
+  bool vec = s.m.nx % V == 0;
+  for (int i = 0; i < XB_NBUF && vec; ++i) vec = ((uintptr_t)s.buf[i] & 15) == 0;
+  const int tcols = vec ? 32 * V : 32;
+  const long long tiles = (long long)((s.m.nx + tcols - 1) / tcols) * ((s.m.ny + tile_rows - 1) / tile_rows);
   // one resident wave (4 blocks of 256 threads per SM) looping over the tiles; the error
   // pass always fills XNPARTS partials
   const int blocks = s.err ? XNPARTS : (int)(tiles < XNPARTS ? tiles : XNPARTS);
   const dim3 blk(32, XWARPS);
+  if (vec) {
+    // two resident blocks per SM (one with four fields): one wave looping over the tiles
+    const int res = (s.m.nf <= 2 ? 2 : 1) * 152;
+    const int vblocks = s.err ? XNPARTS : (int)(tiles < res ? tiles : res);
+    if (rx == RX_GRAY_SCOTT) rk_stage_vec_kernel<T, RX_GRAY_SCOTT, 2><<<vblocks, blk, 0, st>>>(s);
+    else if (s.m.nf <= 2) {
+      if (rx == RX_FISHER) rk_stage_vec_kernel<T, RX_FISHER, 2><<<vblocks, blk, 0, st>>>(s);
+      else rk_stage_vec_kernel<T, RX_NONE, 2><<<vblocks, blk, 0, st>>>(s);
+    } else {
+      if (rx == RX_FISHER) rk_stage_vec_kernel<T, RX_FISHER, 4><<<vblocks, blk, 0, st>>>(s);
+      else rk_stage_vec_kernel<T, RX_NONE, 4><<<vblocks, blk, 0, st>>>(s);
+    }
+    return cudaGetLastError();
+  }
   if (rx == RX_GRAY_SCOTT) rk_stage_kernel<T, RX_GRAY_SCOTT, 2><<<blocks, blk, 0, st>>>(s);
   else if (s.m.nf <= 2) {
     if (rx == RX_FISHER) rk_stage_kernel<T, RX_FISHER, 2><<<blocks, blk, 0, st>>>(s);

@@ -192,7 +192,7 @@ def test_2d_derivatives_error_norm_is_finite(cuda):
     assert not M.is_finite(y)
 
 
-@pytest.mark.parametrize("shape", [(70, 33), (5, 1), (3, 65), (97, 129), (130, 64)])
+@pytest.mark.parametrize("shape", [(70, 33), (5, 1), (3, 65), (97, 129), (130, 64), (40, 70), (12, 36)])
 @pytest.mark.parametrize("kind", [mol.PERIODIC, mol.DIRICHLET, mol.NEUMANN])
 def test_stage_tiles_any_shape(cuda, shape, kind):
     """The stage kernel's 32 x 64 tiles on grids that leave partial tiles, a one-column last
