@@ -70,6 +70,7 @@ def parse():
     ap.add_argument("--etd-steps", type=int, default=100)
     ap.add_argument("--etd-method", default="etdrk4", choices=["etdrk4", "etd1", "etd2"])
     ap.add_argument("--reps", type=int, default=30)
+    ap.add_argument("--adaptive", action="store_true", help="explicit: adaptive RK4 (step doubling, PI controller)")
     return ap.parse_args()
 
 
@@ -594,6 +595,8 @@ def run_explicit(args, local):
     rng = np.random.default_rng(SEED)
     y0 = {k: torch.tensor(rng.uniform(0, 1, (n + 2, n + 2)), dtype=torch.float32, device=dev) for k in ("c1", "c2")}
     dt = 0.2 * min(grid.dx / 0.8, grid.dx ** 2 / (4 * 1e-4))
+    if args.adaptive:
+        return run_explicit_adaptive(args, model, y0, dt, n, S, dev)
     _explicit_steps(model, y0, 0.0, dt, 2, 3)
     torch.cuda.synchronize(dev)
     s = torch.cuda.current_stream(dev)
@@ -617,6 +620,38 @@ def run_explicit(args, local):
     if not args.no_cpu_baseline:
         out["cpu_baseline"] = explicit_cpu_baseline()
     return out
+
+
+def run_explicit_adaptive(args, model, y0, dt, n, S, dev):
+    """adaptive_integrate with RK4 (step doubling: a full step and two half steps per
+    attempt, 12 stencil-stage launches, the error fused into the last; PI controller and
+    CFL limit on the device in a conditional graph) for S attempts from t = 0, no state
+    history.  Reports attempts/s, accepted pt-steps/s and the stage kernels' HBM rate
+    (12 stages x 16/4 accesses: 48 accesses = 192 B per point and field per attempt in
+    FP32)."""
+    import torch
+    import moljax_gb300 as M
+    pid = M.PIDParams(atol=1e-7, rtol=1e-5)
+    kw = dict(method=M.IntegratorType.RK4, max_steps=10 * S + 10, pid_params=pid, save_every=1,
+              save_y_history=False)
+    M.adaptive_integrate(model, y0, 0.0, 1e9, dt, max_attempts=8, **kw)  # tunes and captures
+    torch.cuda.synchronize(dev)
+    s = torch.cuda.current_stream(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    r = M.adaptive_integrate(model, y0, 0.0, 1e9, dt, max_attempts=S, **kw)
+    e1.record(s)
+    e1.synchronize()
+    t = e0.elapsed_time(e1) * 1e-3
+    att = r.n_accepted + r.n_rejected
+    b = 2 * n * n * 192
+    peak, peak_kind = peaks()
+    return {"workload": f"advection-diffusion adaptive RK4 (step doubling) 2 fields {n}x{n} FP32, upwind, periodic, "
+                        f"rtol=1e-5, atol=1e-7", "n": n, "attempts": att, "n_accepted": r.n_accepted,
+            "n_rejected": r.n_rejected, "t_reached": float(r.t_final), "ms_per_attempt": t / max(att, 1) * 1e3,
+            "value": n * n * r.n_accepted / t, "unit": UNIT, "attempt_alg_bytes": b,
+            "achieved_gbs": b * att / t / 1e9, "frac_of_" + peak_kind: b * att / t / 1e9 / peak,
+            "stencil_rows": M.autotune.stencil_rows(n, n, 2, torch.float32)}
 
 
 def explicit_cpu_baseline(n=1024, steps=48):
