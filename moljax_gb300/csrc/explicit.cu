@@ -669,9 +669,10 @@ static cudaError_t launch_x_attempt(const XAttempt<T>& A, cudaStream_t s) {
 // of NST cells (one per stage: every stage's 5-point stencil eats one ring) in shared
 // memory and runs the stages there, each over the region its successors still need,
 // so that the step reads the state once and writes it once (8 B per point and field in
-// FP32 instead of the 64 B of four separate RK4 stage passes).  The stage table is the
-// one the separate passes use (add_step), with buffer ids mapped to shared memory:
-// 0 step input, 1 and 2 the stage ping-pong, 3 the RK4 running sum, -2 the output.
+// FP32 instead of the 64 B of four separate RK4 stage passes).  The stage formulas are
+// those of the separate passes (add_step) compiled in per method, with the buffers in
+// shared memory: 0 step input, 1 and 2 the stage ping-pong, 3 the RK4 running sum (kept
+// on the tile only, where the last stage reads it).
 // Periodic halos wrap; for Dirichlet and Neumann fields the ring of ghost cells just
 // outside the domain is refilled from the BC formula after every stage, and cells
 // further out are never read by a domain point.
@@ -683,9 +684,7 @@ struct XFused {
   XCoef<T> k;
   const T* in;
   T* out;
-  int nst;
-  int w[4], p[4], q[4], o1[4], o2[4];
-  T cp1[4], cq1[4], cf1[4], cp2[4], cq2[4], cf2[4];
+  int nst;     // 3: SSPRK3, 4: RK4 (the stage formulas are compiled in per method)
   int any_bc;  // some field is Dirichlet or Neumann
 };
 
@@ -767,18 +766,25 @@ fused_step_kernel(const __grid_constant__ XFused<T> a) {
   }
   __syncthreads();
 
+  // stage constants of add_step's SSPRK3 (NST 3) and RK4 (NST 4) tables, in the state type
+  const T h2 = (T)0.5 * h, h3 = (T)(1.0 / 3.0) * h, h6 = (T)(1.0 / 6.0) * h;
+  const T c75 = (T)0.75, c25 = (T)0.25, h25 = (T)0.25 * h;
+  const T c13 = (T)(1.0 / 3.0), c23 = (T)(2.0 / 3.0), h23 = (T)(2.0 / 3.0) * h;
 #pragma unroll
   for (int s = 0; s < NST; ++s) {
     const int lo = s + 1;
     const int SW = RW - 2 * lo, SH = RH - 2 * lo;  // this stage's output region (compile time)
-    const int wb = a.w[s], pb = a.p[s], qb = a.q[s], o1b = a.o1[s], o2b = a.o2[s];
-    const T cp1 = a.cp1[s], cq1 = a.cq1[s], cf1h = a.cf1[s] * h;
-    const T cp2 = a.cp2[s], cq2 = a.cq2[s], cf2h = a.cf2[s] * h;
+    // stage input: buffer 0 (step input), then 1, 2, 1 (RK4) or 1, 2 (SSPRK3); output the
+    // other ping-pong buffer, the RK4 running sum in buffer 3, the last stage to global
+    const int wb = s == 0 ? 0 : (s == 2 ? 2 : 1);
+    const int o1b = s == NST - 1 ? FOUT : (s == 1 ? 2 : 1);
     for (int i = tid; i < SW * SH; i += FTHREADS) {
       const int sy = i / SW, sx = i - sy * SW;
       const int ry = sy + lo, rx = sx + lo;
       const int gy = Y0 + ry, gx = X0 + rx;
       const int c0 = ry * RW + rx;
+      // the running sum is read only on the tile (the last stage's region)
+      const bool tile = ry >= R && ry < R + FTY && rx >= R && rx < R + FTX;
       T c[NF], Fv[NF];
 #pragma unroll
       for (int f = 0; f < NF; ++f) {
@@ -810,9 +816,21 @@ fused_step_kernel(const __grid_constant__ XFused<T> a) {
 #pragma unroll
       for (int f = 0; f < NF; ++f) {
         if (f >= nf) break;
-        const T pv = pb >= 0 ? buf(pb, f)[c0] : (T)0, qv = qb >= 0 ? buf(qb, f)[c0] : (T)0;
-        const T o1 = cp1 * pv + cq1 * qv + cf1h * Fv[f];
-        if (o2b >= 0) buf(o2b, f)[c0] = cp2 * pv + cq2 * qv + cf2h * Fv[f];
+        const T F = Fv[f];
+        T o1;
+        if (NST == 4) {  // rk4_step (stepping.py:126-163), running sum in buffer 3
+          T* acc = buf(3, f);
+          if (s == 3) {
+            o1 = acc[c0] + h6 * F;
+          } else {
+            const T y0v = buf(0, f)[c0];
+            o1 = y0v + (s == 2 ? h : h2) * F;
+            if (tile) acc[c0] = s == 0 ? y0v + h6 * F : acc[c0] + h3 * F;
+          }
+        } else {  // ssprk3_step (stepping.py:87-123), Shu-Osher form
+          const T y0v = buf(0, f)[c0];
+          o1 = s == 0 ? y0v + h * F : (s == 1 ? c75 * y0v + c25 * c[f] + h25 * F : c13 * y0v + c23 * c[f] + h23 * F);
+        }
         if (o1b == FOUT) {
           if (gy < ny && gx < nx) a.out[f * per + (long long)gy * nx + gx] = o1;
         } else {
@@ -898,39 +916,20 @@ static cudaError_t launch_fused(const XFused<T>& f, cudaStream_t s) {
   return launch_fused_rx<T, RX_NONE>(f, s);
 }
 
-// the fused step of `method` with the stage table of add_step (in / out set per step)
+// the fused step of `method` (1 SSPRK3, 2 RK4; in / out set per step)
 template <typename T>
 static XFused<T> make_fused(const XModel& m, int method, double dt) {
-  XAttempt<T> A;
-  memset(&A, 0, sizeof(A));
-  XStage<T> base;
-  memset(&base, 0, sizeof(base));
-  base.m = m;
-  base.hfixed = dt;
-  add_step(A, base, method, XB_YCUR, XB_YNEXT, 1.0, 0);
+  XStage<T> s0;
+  memset(&s0, 0, sizeof(s0));
+  s0.m = m;
+  s0.hfixed = dt;
+  s0.hfac = 1.0;
+  x_coef(s0);
   XFused<T> f;
   memset(&f, 0, sizeof(f));
   f.m = m;
-  XStage<T> s0 = A.s[0];
-  x_coef(s0);
   f.k = s0.k;
-  f.nst = A.n;
-  auto map = [](int id) -> int {
-    switch (id) {
-      case XB_YCUR: return 0;
-      case XB_W1: return 1;
-      case XB_W2: return 2;
-      case XB_ACC: return 3;
-      case XB_YNEXT: return FOUT;
-      default: return -1;
-    }
-  };
-  for (int i = 0; i < A.n; ++i) {
-    const XStage<T>& st = A.s[i];
-    f.w[i] = map(st.w); f.p[i] = map(st.p); f.q[i] = map(st.q); f.o1[i] = map(st.o1); f.o2[i] = map(st.o2);
-    f.cp1[i] = (T)st.cp1; f.cq1[i] = (T)st.cq1; f.cf1[i] = (T)st.cf1;
-    f.cp2[i] = (T)st.cp2; f.cq2[i] = (T)st.cq2; f.cf2[i] = (T)st.cf2;
-  }
+  f.nst = method == 2 ? 4 : 3;
   for (int q = 0; q < m.nf; ++q) f.any_bc |= m.kind[q] != MJX_BC_PERIODIC;
   return f;
 }
