@@ -22,6 +22,7 @@
 #include <math.h>
 #include <string.h>
 #include <stdint.h>
+#include <type_traits>
 
 #include "spectral.cuh"
 #include "autotune.cuh"
@@ -778,63 +779,113 @@ fused_step_kernel(const __grid_constant__ XFused<T> a) {
     // other ping-pong buffer, the RK4 running sum in buffer 3, the last stage to global
     const int wb = s == 0 ? 0 : (s == 2 ? 2 : 1);
     const int o1b = s == NST - 1 ? FOUT : (s == 1 ? 2 : 1);
-    for (int i = tid; i < SW * SH; i += FTHREADS) {
-      const int sy = i / SW, sx = i - sy * SW;
-      const int ry = sy + lo, rx = sx + lo;
+    // cells in pairs (rx, rx + 1) from an even column (64-bit shared-memory accesses; RW and
+    // every buffer offset are even): when lo is odd the pairs start one column left of the
+    // region and may end one right of it; those extra cells are read by no later stage and
+    // write no output (the global store is limited to the tile)
+    const int x0 = lo & ~1;
+    const int SWP = (RW - lo - x0 + 1) >> 1;
+    typedef typename Vec16<T>::t V16;
+    typedef typename std::conditional<sizeof(T) == 4, float2, double2>::type T2;
+    (void)sizeof(V16);
+    for (int i = tid; i < SWP * SH; i += FTHREADS) {
+      const int sy = i / SWP, sp = i - sy * SWP;
+      const int ry = sy + lo, rx = x0 + 2 * sp;
       const int gy = Y0 + ry, gx = X0 + rx;
       const int c0 = ry * RW + rx;
       // the running sum is read only on the tile (the last stage's region)
-      const bool tile = ry >= R && ry < R + FTY && rx >= R && rx < R + FTX;
-      T c[NF], Fv[NF];
+      const bool rin = ry >= R && ry < R + FTY;
+      const bool t0 = rin && rx >= R && rx < R + FTX, t1 = rin && rx + 1 >= R && rx + 1 < R + FTX;
+      T c[NF][2], Fv[NF][2];
 #pragma unroll
       for (int f = 0; f < NF; ++f) {
         if (f >= nf) break;
         const T* wv = buf(wb, f);
-        const T cv = wv[c0], xm = wv[c0 - 1], xp = wv[c0 + 1], ym = wv[c0 - RW], yp = wv[c0 + RW];
-        T v = k.D[f] * ((xp - (T)2 * cv + xm) * idx2 + (yp - (T)2 * cv + ym) * idy2);
-        if (adv == 1) {  // d1_upwind_2d
-          const T gxv = vxpos ? (cv - xm) * idx : (xp - cv) * idx;
-          const T gyv = vypos ? (cv - ym) * idy : (yp - cv) * idy;
-          v = v - vx * gxv - vy * gyv;
-        } else if (adv == 2) {
-          v = v - vx * (xp - xm) * (T)0.5 * idx - vy * (yp - ym) * (T)0.5 * idy;
-        }
-        c[f] = cv;
-        Fv[f] = v;
-      }
-      if (RX == RX_GRAY_SCOTT) {  // operators.py:644-667
-        const T uvv = c[0] * c[1] * c[1];
-        Fv[0] += -uvv + k.F * ((T)1 - c[0]);
-        Fv[1] += uvv - k.Fk * c[1];
-      } else if (RX == RX_FISHER) {  // operators.py:680-705
+        const T2 cc = *reinterpret_cast<const T2*>(wv + c0);
+        const T2 up = *reinterpret_cast<const T2*>(wv + c0 - RW);
+        const T2 dn = *reinterpret_cast<const T2*>(wv + c0 + RW);
+        const T xl = wv[c0 - 1], xr = wv[c0 + 2];
+        const T cvs[2] = {cc.x, cc.y}, xms[2] = {xl, cc.x}, xps[2] = {cc.y, xr};
+        const T yms[2] = {up.x, up.y}, yps[2] = {dn.x, dn.y};
 #pragma unroll
-        for (int f = 0; f < NF; ++f) {
-          if (f >= nf) break;
-          Fv[f] += k.r * c[f] * ((T)1 - c[f]);
+        for (int q = 0; q < 2; ++q) {
+          const T cv = cvs[q], xm = xms[q], xp = xps[q], ym = yms[q], yp = yps[q];
+          T v = k.D[f] * ((xp - (T)2 * cv + xm) * idx2 + (yp - (T)2 * cv + ym) * idy2);
+          if (adv == 1) {  // d1_upwind_2d
+            const T gxv = vxpos ? (cv - xm) * idx : (xp - cv) * idx;
+            const T gyv = vypos ? (cv - ym) * idy : (yp - cv) * idy;
+            v = v - vx * gxv - vy * gyv;
+          } else if (adv == 2) {
+            v = v - vx * (xp - xm) * (T)0.5 * idx - vy * (yp - ym) * (T)0.5 * idy;
+          }
+          c[f][q] = cv;
+          Fv[f][q] = v;
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < 2; ++q) {
+        if (RX == RX_GRAY_SCOTT) {  // operators.py:644-667
+          const T uvv = c[0][q] * c[1][q] * c[1][q];
+          Fv[0][q] += -uvv + k.F * ((T)1 - c[0][q]);
+          Fv[1][q] += uvv - k.Fk * c[1][q];
+        } else if (RX == RX_FISHER) {  // operators.py:680-705
+#pragma unroll
+          for (int f = 0; f < NF; ++f) {
+            if (f >= nf) break;
+            Fv[f][q] += k.r * c[f][q] * ((T)1 - c[f][q]);
+          }
         }
       }
 #pragma unroll
       for (int f = 0; f < NF; ++f) {
         if (f >= nf) break;
-        const T F = Fv[f];
-        T o1;
+        T o1[2];
         if (NST == 4) {  // rk4_step (stepping.py:126-163), running sum in buffer 3
           T* acc = buf(3, f);
+          const T2 av = *reinterpret_cast<const T2*>(acc + c0);
+          const T avs[2] = {av.x, av.y};
           if (s == 3) {
-            o1 = acc[c0] + h6 * F;
+#pragma unroll
+            for (int q = 0; q < 2; ++q) o1[q] = avs[q] + h6 * Fv[f][q];
           } else {
-            const T y0v = buf(0, f)[c0];
-            o1 = y0v + (s == 2 ? h : h2) * F;
-            if (tile) acc[c0] = s == 0 ? y0v + h6 * F : acc[c0] + h3 * F;
+            const T2 yv = *reinterpret_cast<const T2*>(buf(0, f) + c0);
+            const T ys[2] = {yv.x, yv.y};
+            T an[2];
+#pragma unroll
+            for (int q = 0; q < 2; ++q) {
+              o1[q] = ys[q] + (s == 2 ? h : h2) * Fv[f][q];
+              an[q] = s == 0 ? ys[q] + h6 * Fv[f][q] : avs[q] + h3 * Fv[f][q];
+            }
+            if (t0 && t1) {
+              T2 w2;
+              w2.x = an[0];
+              w2.y = an[1];
+              *reinterpret_cast<T2*>(acc + c0) = w2;
+            } else {
+              if (t0) acc[c0] = an[0];
+              if (t1) acc[c0 + 1] = an[1];
+            }
           }
         } else {  // ssprk3_step (stepping.py:87-123), Shu-Osher form
-          const T y0v = buf(0, f)[c0];
-          o1 = s == 0 ? y0v + h * F : (s == 1 ? c75 * y0v + c25 * c[f] + h25 * F : c13 * y0v + c23 * c[f] + h23 * F);
+          const T2 yv = *reinterpret_cast<const T2*>(buf(0, f) + c0);
+          const T ys[2] = {yv.x, yv.y};
+#pragma unroll
+          for (int q = 0; q < 2; ++q)
+            o1[q] = s == 0 ? ys[q] + h * Fv[f][q]
+                           : (s == 1 ? c75 * ys[q] + c25 * c[f][q] + h25 * Fv[f][q]
+                                     : c13 * ys[q] + c23 * c[f][q] + h23 * Fv[f][q]);
         }
         if (o1b == FOUT) {
-          if (gy < ny && gx < nx) a.out[f * per + (long long)gy * nx + gx] = o1;
+          T* orow = a.out + f * per + (long long)gy * nx;
+          if (gy < ny) {
+            if (t0 && gx < nx) orow[gx] = o1[0];
+            if (t1 && gx + 1 < nx) orow[gx + 1] = o1[1];
+          }
         } else {
-          buf(o1b, f)[c0] = o1;
+          T2 w2;
+          w2.x = o1[0];
+          w2.y = o1[1];
+          *reinterpret_cast<T2*>(buf(o1b, f) + c0) = w2;
         }
       }
     }
