@@ -128,6 +128,11 @@ __device__ __forceinline__ void apply_twiddles(cx<T>* x, int t, const cx<T>* __r
   }
 }
 
+// a / b and a % b for a >= 0, b > 0: a shift and a mask when b is a power of two (every
+// length, thread count and sequence count of the transforms here), a division otherwise
+__device__ __forceinline__ int pdiv(int a, int b) { return (b & (b - 1)) == 0 ? a >> (__ffs(b) - 1) : a / b; }
+__device__ __forceinline__ int pmod(int a, int b) { return (b & (b - 1)) == 0 ? a & (b - 1) : a % b; }
+
 // One Stockham pass of radix R with current sub-length p (p*R divides n).
 // Element j of this thread's sequence is buf[base + j * es]; ES1 fixes es = 1.
 template <typename T, int R, bool INV, bool ES1>
@@ -136,8 +141,8 @@ __device__ __forceinline__ void stockham_pass(cx<T>* buf, int n, int p, int tps,
                                               const cx<T>* __restrict__ tw) {
   typedef cx<T> C;
   const int es = ES1 ? 1 : es_rt;
-  const int Tn = n / R;                       // butterflies per sequence
-  const int nb = (Tn >= tps) ? Tn / tps : 1;  // butterflies per thread (<= 16/R)
+  const int Tn = pdiv(n, R);                       // butterflies per sequence
+  const int nb = (Tn >= tps) ? pdiv(Tn, tps) : 1;  // butterflies per thread (<= 16/R)
   constexpr int NBMAX = 16 / R;
   C x[16];
   if (active) {
@@ -152,7 +157,7 @@ __device__ __forceinline__ void stockham_pass(cx<T>* buf, int n, int p, int tps,
   }
   __syncthreads();
   if (active) {
-    const int twstep = n / (p * R);
+    const int twstep = pdiv(n, p * R);
 #pragma unroll
     for (int m = 0; m < NBMAX; ++m) {
       if (m < nb) {
@@ -175,11 +180,11 @@ __device__ __forceinline__ void stockham_pass(cx<T>* buf, int n, int p, int tps,
 template <typename T, bool INV, bool COLMAJOR>
 __device__ void fft_smem(cx<T>* buf, int n, int log2n, int nseq, int ss, int es,
                          const cx<T>* __restrict__ tw, int tid) {
-  const int tps = n >= 16 ? n / 16 : 1;
+  const int tps = n >= 16 ? pdiv(n, 16) : 1;
   const bool active = tid < nseq * tps;
   int lt, s;
-  if (COLMAJOR) { s = tid % nseq; lt = tid / nseq; }
-  else { lt = tid % tps; s = tid / tps; }
+  if (COLMAJOR) { s = pmod(tid, nseq); lt = pdiv(tid, nseq); }
+  else { lt = pmod(tid, tps); s = pdiv(tid, tps); }
   const int base = s * ss;
   // straight-line schedule: up to three radix-16 passes (n <= 4096), then radix 2/4/8
   int p = 1, rem = log2n;

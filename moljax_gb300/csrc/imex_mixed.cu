@@ -133,6 +133,7 @@ __global__ void __launch_bounds__(NT, MINB) mcol_kernel(const __grid_constant__ 
   const int kx0 = blockIdx.x * Cn;
   const int ny = a.ny, tid = threadIdx.x, nth = blockDim.x;
   const int total = ny * Cn;
+  const int lc = __ffs(Cn) - 1;  // the tile width is a power of two (col_tile / tile halve from one)
   const long long ldc = a.ldc;
   const int cur = st != nullptr ? st->cur : 0;
   const double h = st != nullptr ? st->dtc : a.hfixed;
@@ -147,13 +148,13 @@ __global__ void __launch_bounds__(NT, MINB) mcol_kernel(const __grid_constant__ 
 #pragma unroll
     for (int m = 0; m < 8; ++m) {
       const int e = tid + m * nth;
-      const int ky = e / Cn, c = e - ky * Cn, kx = kx0 + c;
+      const int ky = e >> lc, c = e & (Cn - 1), kx = kx0 + c;
       if (e < total) v[m] = kx < a.ncols ? zin[jb.off + ky * ldc + kx] : fmk(0.f, 0.f);
     }
 #pragma unroll
     for (int m = 0; m < 8; ++m) {
       const int e = tid + m * nth;
-      const int ky = e / Cn, c = e - ky * Cn;
+      const int ky = e >> lc, c = e & (Cn - 1);
       if (e < total) buf[sp(ky * W + c)] = v[m];
     }
     __syncthreads();
@@ -165,7 +166,7 @@ __global__ void __launch_bounds__(NT, MINB) mcol_kernel(const __grid_constant__ 
   for (int m = 0; m < 8; ++m) {
     const int e = tid + m * nth;
     if (e >= total) continue;
-    const int ky = e / Cn, c = e - ky * Cn, kx = kx0 + c;
+    const int ky = e >> lc, c = e & (Cn - 1), kx = kx0 + c;
     if (kx >= a.ncols) {
       buf[sp(ky * W + c)] = fmk(0.f, 0.f);
       if (W > Cn) buf[sp(ky * W + Cn + c)] = fmk(0.f, 0.f);
@@ -207,9 +208,10 @@ __global__ void __launch_bounds__(NT, MINB) mcol_kernel(const __grid_constant__ 
   __syncthreads();
   const int nseq = (type == MC_HALF_MID) ? Cn : W;
   fft_smem<float, true, true>(buf, ny, a.log2ny, nseq, 1, W, a.tw, tid);
+  const int lns = __ffs(nseq) - 1;
   for (int e = tid; e < ny * nseq; e += nth) {
-    const int ky = e / nseq, col = e - ky * nseq;
-    const int half = col / Cn, c = col - half * Cn, kx = kx0 + c;
+    const int ky = e >> lns, col = e & (nseq - 1);
+    const int half = col >> lc, c = col & (Cn - 1), kx = kx0 + c;
     if (kx >= a.ncols) continue;
     const long long g = jb.off + ky * ldc + kx;
     const float2 v = buf[sp(ky * W + col)];

@@ -316,6 +316,7 @@ __global__ void __launch_bounds__(ColThreads<T>::v, 1) col_kernel(const __grid_c
   const int Cn = a.C, nout = jb.nout, W = Cn * nout;
   const int kx0 = blockIdx.x * Cn;
   const int ny = a.ny, tid = threadIdx.x, nth = blockDim.x;
+  const int lc = __ffs(Cn) - 1;  // the tile width is a power of two (col_tile / tile halve from one)
   const long long ldc = a.ldc;
   const long long po = (long long)blockIdx.z * a.pstride;
 
@@ -324,7 +325,7 @@ __global__ void __launch_bounds__(ColThreads<T>::v, 1) col_kernel(const __grid_c
 #pragma unroll
     for (int m = 0; m < 16; ++m) {
       const int e = tid + m * nth;
-      const int ky = e / Cn, c = e - ky * Cn, kx = kx0 + c;
+      const int ky = e >> lc, c = e & (Cn - 1), kx = kx0 + c;
       const bool mir = a.oddy && ky >= (ny >> 1);
       const int kyl = mir ? ny - 1 - ky : ky;
       if (e < ny * Cn) {
@@ -335,7 +336,7 @@ __global__ void __launch_bounds__(ColThreads<T>::v, 1) col_kernel(const __grid_c
 #pragma unroll
     for (int m = 0; m < 16; ++m) {
       const int e = tid + m * nth;
-      const int ky = e / Cn, c = e - ky * Cn;
+      const int ky = e >> lc, c = e & (Cn - 1);
       if (e < ny * Cn) buf[sp(ky * W + c)] = v[m];
     }
   }
@@ -347,7 +348,7 @@ __global__ void __launch_bounds__(ColThreads<T>::v, 1) col_kernel(const __grid_c
   const double h = a.st != nullptr ? a.st->dtc : a.hfixed;
   const T hD0 = (T)(h * jb.hfac[0] * jb.D), hD1 = (T)(h * jb.hfac[1] * jb.D);
   for (int e = tid; e < ny * Cn; e += nth) {
-    const int ky = e / Cn, c = e - ky * Cn, kx = kx0 + c;
+    const int ky = e >> lc, c = e & (Cn - 1), kx = kx0 + c;
     T lxy = (T)0;
     if (kx < a.ncols) lxy = a.ldc3 ? a.lamx[kx % a.ldc3] + a.lamy2[kx / a.ldc3] : a.lamx[kx];
     const T lam = lxy + a.lamy[ky];
@@ -403,9 +404,10 @@ __global__ void __launch_bounds__(ColThreads<T>::v, 1) col_kernel(const __grid_c
   __syncthreads();
   if (dirs & 2) fft_smem<T, true, true>(buf, ny, a.log2ny, W, 1, W, a.tw, tid);
 
+  const int lw = __ffs(W) - 1;  // W = Cn or 2 Cn
   for (int e = tid; e < ny * W; e += nth) {
-    const int ky = e / W, col = e - ky * W;
-    const int o = col / Cn, c = col - o * Cn, kx = kx0 + c;
+    const int ky = e >> lw, col = e & (W - 1);
+    const int o = col >> lc, c = col & (Cn - 1), kx = kx0 + c;
     if (kx < a.ncols && !(a.oddy && ky >= (ny >> 1))) a.spec[po + jb.sout[o] + ky * ldc + kx] = buf[sp(ky * W + col)];
   }
 }
