@@ -179,6 +179,7 @@ __global__ void __launch_bounds__(EThreads<T>::v, 1) etd_col_kernel(const __grid
   const int f = blockIdx.y;
   const int type = a.type;
   const int Cn = a.C, W = Cn;
+  const int lc = __ffs(Cn) - 1;  // the tile width is a power of two (halved from 16)
   const int kx0 = blockIdx.x * Cn;
   const int ny = a.ny, tid = threadIdx.x, nth = blockDim.x;
   const long long ldc = a.ldc, fo = (long long)f * a.fs, per = a.fs;
@@ -187,14 +188,14 @@ __global__ void __launch_bounds__(EThreads<T>::v, 1) etd_col_kernel(const __grid
   // load the row-spectrum tile: E0 ZU, E1 and E5-E7 ZN, E2-E4 ZX
   const Cx* in0 = type == E0 ? a.zu : ((type == E1 || type >= E5) ? a.zn : a.zx);
   for (int e = tid; e < ny * Cn; e += nth) {
-    const int ky = e / Cn, c = e - ky * Cn, kx = kx0 + c;
+    const int ky = e >> lc, c = e & (Cn - 1), kx = kx0 + c;
     buf[sp(ky * W + c)] = kx < a.ncols ? in0[fo + ky * ldc + kx] : mk<Cx>((T)0, (T)0);
   }
   __syncthreads();
   fft_smem<T, false, true>(buf, ny, a.log2ny, Cn, 1, W, a.tw, tid);
 
   for (int e = tid; e < ny * Cn; e += nth) {
-    const int ky = e / Cn, c = e - ky * Cn, kx = kx0 + c;
+    const int ky = e >> lc, c = e & (Cn - 1), kx = kx0 + c;
     if (kx >= a.ncols) { buf[sp(ky * W + c)] = mk<Cx>((T)0, (T)0); continue; }
     const long long g = fo + ky * ldc + kx, tg = ky * ldc + kx;
     const Cx x = buf[sp(ky * W + c)];
@@ -245,7 +246,7 @@ __global__ void __launch_bounds__(EThreads<T>::v, 1) etd_col_kernel(const __grid
   fft_smem<T, true, true>(buf, ny, a.log2ny, Cn, 1, W, a.tw, tid);
   Cx* dst = type >= E4 ? a.zu : a.zx;
   for (int e = tid; e < ny * Cn; e += nth) {
-    const int ky = e / Cn, c = e - ky * Cn, kx = kx0 + c;
+    const int ky = e >> lc, c = e & (Cn - 1), kx = kx0 + c;
     if (kx < a.ncols) dst[fo + ky * ldc + kx] = buf[sp(ky * W + c)];
   }
 }
