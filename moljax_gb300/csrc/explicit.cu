@@ -934,12 +934,17 @@ static bool fused_ok(const XModel& m, int method) {
 
 template <typename T, int RX, int NF, int NST>
 static cudaError_t launch_fused_t(const XFused<T>& f, size_t smem, unsigned blocks, cudaStream_t s) {
-  static bool attr = false;
-  if (!attr) {
-    const cudaError_t e = cudaFuncSetAttribute(fused_step_kernel<T, RX, NF, NST>,
-                                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  // the dynamic shared-memory limit is a per-device function attribute: set it once for
+  // each device this instantiation runs on (a repeated set from two threads is harmless)
+  static int attr_mask = 0;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  const int bit = dev < 31 ? (1 << dev) : 0;
+  if (bit == 0 || !(attr_mask & bit)) {
+    e = cudaFuncSetAttribute(fused_step_kernel<T, RX, NF, NST>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    attr = true;
+    attr_mask |= bit;
   }
   fused_step_kernel<T, RX, NF, NST><<<blocks, FTHREADS, smem, s>>>(f);
   return cudaGetLastError();
