@@ -206,8 +206,12 @@ mjx_status mjx_fft_cn2d(const void* plan, const mjx_grid2d* grid, int dtype, dou
  * loads the library until process exit), so the grid must satisfy
  * mjx_spec2d_ws_bytes(ny, nx, 1, dtype) <= MJX_NOALLOC_SCRATCH_BYTES (e.g.
  * 1024^2 FP32, 512^2 FP64); larger grids return MJX_WORKSPACE.  The first call
- * on a device looks up the scratch address once (make that call before any
- * stream capture).  No device memory is allocated or freed.  All calls share
+ * in each CUDA context looks up the scratch address of that context (make that
+ * call before any stream capture): the array has its own address in the
+ * device's primary context, in a driver-API context that an embedding host
+ * made current, and in the new primary context after cudaDeviceReset, and the
+ * lookup is cached per context, never per device.  No device memory is
+ * allocated or freed.  All calls share
  * the one scratch array, so calls that overlap on the GPU (different streams,
  * or different host threads without ordering) race; nothing in the scratch
  * needs to start at zero, because each step writes every spectrum entry it

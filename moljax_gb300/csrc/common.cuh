@@ -4,6 +4,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <mutex>
+
 #include "../../include/moljax_gb300.h"
 
 namespace mjx {
@@ -55,6 +57,40 @@ static inline int ilog2_exact(long long n) {
     mjx_status _s = (expr);                             \
     if (_s != MJX_OK) return _s;                        \
   } while (0)
+
+namespace mjx {
+
+// Process-unique identity (cuCtxGetId) of the CUDA context current on the
+// calling thread.  When no context is current yet, the device's primary
+// context is made current first (cudaSetDevice), as any runtime call would.
+// Function attributes and __device__ symbol addresses belong to a context, so
+// one-time set-up is keyed on this id, not on the device number: a context
+// created by a driver-API host, or the new primary context after
+// cudaDeviceReset, gets its own set-up.
+mjx_status current_context_id(unsigned long long* id);
+
+// Runs a set-up function once per CUDA context (thread-safe).  A failed
+// set-up leaves the context unmarked, so the next call retries it.
+struct ContextOnce {
+  std::mutex mu;
+  unsigned long long ids[32] = {};
+  int n = 0;
+  template <class F>
+  mjx_status run(F&& setup) {
+    unsigned long long id = 0;
+    MJX_TRY(current_context_id(&id));
+    std::lock_guard<std::mutex> lk(mu);
+    const int m = n < 32 ? n : 32;
+    for (int i = 0; i < m; ++i)
+      if (ids[i] == id) return MJX_OK;
+    MJX_TRY(setup());
+    ids[n % 32] = id;  // oldest entry replaced after 32 contexts
+    ++n;
+    return MJX_OK;
+  }
+};
+
+}  // namespace mjx
 
 #define MJX_CUDA_TRY(expr)                                          \
   do {                                                              \

@@ -508,17 +508,17 @@ static mjx_status general_apply3(const void* pz, const void* py, const void* px,
 }
 
 static mjx_status set_dft_attrs() {
-  static int done = 0;
-  if (done) return MJX_OK;
-  int dev = 0, optin = 0;
-  MJX_CUDA_TRY(cudaGetDevice(&dev));
-  MJX_CUDA_TRY(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-  MJX_CUDA_TRY(cudaFuncSetAttribute(dft_rows_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
-  MJX_CUDA_TRY(cudaFuncSetAttribute(dft_rows_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
-  MJX_CUDA_TRY(cudaFuncSetAttribute(dft_mixed_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
-  MJX_CUDA_TRY(cudaFuncSetAttribute(dft_mixed_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
-  done = 1;
-  return MJX_OK;
+  static ContextOnce once;
+  return once.run([]() -> mjx_status {
+    int dev = 0, optin = 0;
+    MJX_CUDA_TRY(cudaGetDevice(&dev));
+    MJX_CUDA_TRY(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    MJX_CUDA_TRY(cudaFuncSetAttribute(dft_rows_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
+    MJX_CUDA_TRY(cudaFuncSetAttribute(dft_rows_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
+    MJX_CUDA_TRY(cudaFuncSetAttribute(dft_mixed_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
+    MJX_CUDA_TRY(cudaFuncSetAttribute(dft_mixed_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
+    return MJX_OK;
+  });
 }
 
 }  // namespace mjx

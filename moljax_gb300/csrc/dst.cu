@@ -346,17 +346,17 @@ static mjx_status dst1_run(const void* plan, int N, long long nrows, int mode, c
 }
 
 static mjx_status dst1_attrs() {
-  static int done = 0;
-  if (done) return MJX_OK;
-  int dev = 0, optin = 0;
-  MJX_CUDA_TRY(cudaGetDevice(&dev));
-  MJX_CUDA_TRY(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-  MJX_CUDA_TRY(cudaFuncSetAttribute(dst1_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
-  MJX_CUDA_TRY(cudaFuncSetAttribute(dst1_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
-  MJX_CUDA_TRY(cudaFuncSetAttribute(dct2_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
-  MJX_CUDA_TRY(cudaFuncSetAttribute(dct2_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
-  done = 1;
-  return MJX_OK;
+  static ContextOnce once;
+  return once.run([]() -> mjx_status {
+    int dev = 0, optin = 0;
+    MJX_CUDA_TRY(cudaGetDevice(&dev));
+    MJX_CUDA_TRY(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    MJX_CUDA_TRY(cudaFuncSetAttribute(dst1_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
+    MJX_CUDA_TRY(cudaFuncSetAttribute(dst1_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
+    MJX_CUDA_TRY(cudaFuncSetAttribute(dct2_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
+    MJX_CUDA_TRY(cudaFuncSetAttribute(dct2_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
+    return MJX_OK;
+  });
 }
 
 template <typename T>

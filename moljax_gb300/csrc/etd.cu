@@ -408,15 +408,15 @@ template <typename T>
 static mjx_status etd_run(const void* plan, const mjx_grid2d* g, const mjx_etd_problem* pb, int n_steps,
                           const T* y_in, const T* nprev_in, T* y_out, T* n_out, char* ws, const EtdLayout& L,
                           int recompute, cudaStream_t s) {
-  static int attr = 0;
-  if (!attr) {
+  static ContextOnce attr;
+  MJX_TRY(attr.run([]() -> mjx_status {
     int dev = 0, optin = 0;
     MJX_CUDA_TRY(cudaGetDevice(&dev));
     MJX_CUDA_TRY(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
     MJX_CUDA_TRY(cudaFuncSetAttribute(etd_col_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
     MJX_CUDA_TRY(cudaFuncSetAttribute(etd_col_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
-    attr = 1;
-  }
+    return MJX_OK;
+  }));
   const int nf = pb->nfields, rx = pb->reaction;
   const int symbol = pb->symbol & 1, xonly = (pb->symbol & MJX_SYMBOL_X_ONLY) ? 1 : 0;
   if (recompute) {

@@ -934,18 +934,15 @@ static bool fused_ok(const XModel& m, int method) {
 
 template <typename T, int RX, int NF, int NST>
 static cudaError_t launch_fused_t(const XFused<T>& f, size_t smem, unsigned blocks, cudaStream_t s) {
-  // the dynamic shared-memory limit is a per-device function attribute: set it once for
-  // each device this instantiation runs on (a repeated set from two threads is harmless)
-  static int attr_mask = 0;
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return e;
-  const int bit = dev < 31 ? (1 << dev) : 0;
-  if (bit == 0 || !(attr_mask & bit)) {
+  // the dynamic shared-memory limit is a function attribute of the CUDA context: set it
+  // once for each context this instantiation runs in
+  static ContextOnce attr;
+  cudaError_t e = cudaSuccess;
+  const mjx_status st = attr.run([&]() -> mjx_status {
     e = cudaFuncSetAttribute(fused_step_kernel<T, RX, NF, NST>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    attr_mask |= bit;
-  }
+    return e == cudaSuccess ? MJX_OK : MJX_CUDA_ERROR;
+  });
+  if (st != MJX_OK) return e != cudaSuccess ? e : cudaErrorDeviceUninitialized;
   fused_step_kernel<T, RX, NF, NST><<<blocks, FTHREADS, smem, s>>>(f);
   return cudaGetLastError();
 }

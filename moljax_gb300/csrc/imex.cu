@@ -21,6 +21,7 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include "controller.cuh"
 #include "spectral.cuh"
 
 namespace mjx {
@@ -69,11 +70,6 @@ static ImexLayout imex_layout(int ny, int nx, int nf, int elem, int nrows, int n
 // ------------------------------------------------------------------ controller
 
 
-// NaN-propagating min/max (jnp.minimum/maximum semantics).
-__device__ __forceinline__ double jmax(double a, double b) { return (a != a || b != b) ? (a + b) : (a > b ? a : b); }
-__device__ __forceinline__ double jmin(double a, double b) { return (a != a || b != b) ? (a + b) : (a < b ? a : b); }
-__device__ __forceinline__ double jclip(double x, double lo, double hi) { return jmin(jmax(x, lo), hi); }
-
 __global__ void __launch_bounds__(256) controller_kernel(CtlArgs a) {
   DevState* st = a.st;
   if (st->done) {
@@ -102,63 +98,7 @@ __global__ void __launch_bounds__(256) controller_kernel(CtlArgs a) {
   double tot = 0.0;
   for (int i = 0; i < (int)(blockDim.x >> 5); ++i) { tot += red[i]; bad |= redbad[i]; }
 
-  const mjx_pid_params& P = a.pid;
-  const double order = (double)st->order;
-  const double dtc = st->dtc;
-  // stepping.py:1246-1247
-  const double e = jmax(sqrt(tot / a.n_dof), 1e-10);
-  const int finite = !bad;
-  const bool accept = (e <= 1.0) && finite;
-  // dt_policy.py:544-610 (propose_dt_imex)
-  double dt_a, pe_new;
-  if (e <= 1.0) {  // pid_controller_dt (178-227)
-    const double kI = P.kI / order, kP = P.kP / order;
-    const double es = jmax(e, 1e-10), pes = jmax(st->prev_err, 1e-10);
-    double fac = pow(1.0 / es, kI) * pow(pes / es, kP);
-    fac = jclip(fac * P.safety, P.min_factor, P.max_factor);
-    dt_a = jclip(dtc * fac, P.dt_min, P.dt_max);
-    pe_new = e;
-  } else {  // handle_rejected_step (230-268)
-    const double kI = P.kI / order;
-    double fac = P.safety * pow(1.0 / jmax(e, 1.0), kI);
-    fac = jclip(fac, P.min_factor, 1.0);
-    dt_a = jclip(dtc * fac, P.dt_min, P.dt_max);
-    pe_new = st->prev_err;
-  }
-  const double dt_new = jclip(jmin(dt_a, st->dt_cfl), P.dt_min, P.dt_max);
-  st->err_last = e;
-  st->save_slot = -1;
-  if (accept) {  // stepping.py:1271-1309
-    if (st->n_acc % st->save_every == 0) {
-      if (a.hist_t) a.hist_t[st->write_idx] = st->t + dtc;
-      if (a.hist_dt) a.hist_dt[st->write_idx - 1] = dtc;
-      st->save_slot = st->write_idx;
-      st->write_idx += 1;
-    }
-    st->t = st->t + dtc;
-    st->cur = 1 - st->cur;
-    st->dt = dt_new;
-    st->prev_err = pe_new;
-    st->dt_last_accepted = dtc;
-    st->n_acc += 1;
-  } else {  // stepping.py:1311-1334
-    const double dtr = jmax(dt_new * 0.5, P.dt_min);
-    st->dt = dtr;
-    if (dtr <= P.dt_min * 1.1) st->status = MJX_STATUS_DT_TOO_SMALL_CODE;
-    st->n_rej += 1;
-  }
-  if (!finite) { st->status = MJX_STATUS_NON_FINITE_CODE; st->finite = 0; }
-  st->attempts += 1;
-  const bool running = st->status == MJX_STATUS_RUNNING_CODE && st->t < st->t_end &&
-                       st->write_idx < st->max_saves && st->attempts < st->max_attempts;
-  if (running) {
-    st->dtc = jmin(st->dt, st->t_end - st->t);
-  } else {
-    st->done = 1;
-    if (st->t >= st->t_end) st->status = MJX_STATUS_SUCCESS_CODE;             // 1351-1359
-    else if (st->write_idx >= st->max_saves) st->status = MJX_STATUS_MAX_STEPS_CODE;
-    else if (st->status == MJX_STATUS_RUNNING_CODE) st->status = MJX_STATUS_MAX_STEPS_CODE;
-  }
+  const bool running = ctl_update(st, tot, bad, a.n_dof, a.pid, a.hist_t, a.hist_dt);
   if (a.use_handle) cudaGraphSetConditional(a.handle, running ? 1u : 0u);
 }
 

@@ -25,7 +25,7 @@
 #include <math.h>
 #include <string.h>
 
-#include "spectral.cuh"
+#include "mixed.cuh"
 
 namespace mjx {
 
@@ -33,8 +33,6 @@ mjx_status ensure_kernel_attrs();
 mjx_status check_grid(const mjx_grid2d* g);
 int elem_size(int dtype);
 void set_last_error(cudaError_t e, const char* file, int line);
-
-enum { MC_SPLIT = 0, MC_FULL_END = 1, MC_HALF_MID = 2, MC_HALF_END = 3 };
 
 struct MJob {
   int type;
@@ -60,65 +58,6 @@ struct MColArgs {
   MJob job[8];
 };
 
-__device__ __forceinline__ float2 fmk(float x, float y) { float2 r; r.x = x; r.y = y; return r; }
-
-// ---- float-float arithmetic (error-free transformations: Knuth's two-sum,
-// Dekker's fast two-sum, the FMA two-product).  The _rn intrinsics are never
-// contracted into FMAs or reassociated, which the transformations rely on.
-struct FF { float h, l; };
-
-__device__ __forceinline__ FF ff_fast2sum(float a, float b) {  // |a| >= |b| or a == 0
-  const float s = __fadd_rn(a, b);
-  FF r; r.h = s; r.l = __fsub_rn(b, __fsub_rn(s, a));
-  return r;
-}
-__device__ __forceinline__ float ff_2sum_err(float a, float b, float s) {  // s = fl(a + b)
-  const float bb = __fsub_rn(s, a);
-  return __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
-}
-// x + d, d an FP32 number
-__device__ __forceinline__ FF ff_add_f(FF x, float d) {
-  const float s = __fadd_rn(x.h, d);
-  return ff_fast2sum(s, __fadd_rn(ff_2sum_err(x.h, d, s), x.l));
-}
-// x + x * mu
-__device__ __forceinline__ FF ff_mstep(FF x, float mu) {
-  const float p = __fmul_rn(x.h, mu);
-  const float pe = __fmaf_rn(x.l, mu, __fmaf_rn(x.h, mu, -p));  // x*mu - p
-  const float s = __fadd_rn(x.h, p);
-  return ff_fast2sum(s, __fadd_rn(ff_2sum_err(x.h, p, s), __fadd_rn(x.l, pe)));
-}
-// s * (x - y) rounded to FP32 (the hi difference is exact when x, y are close)
-__device__ __forceinline__ float ff_diff_scaled(FF x, FF y, float s) {
-  return __fmul_rn(__fadd_rn(__fsub_rn(x.h, y.h), __fsub_rn(x.l, y.l)), s);
-}
-// s * x rounded to FP32
-__device__ __forceinline__ float ff_scaled(FF x, float s) { return __fmaf_rn(x.l, s, __fmul_rn(x.h, s)); }
-
-__device__ __forceinline__ FF ff_re(float4 v) { FF r; r.h = v.x; r.l = v.z; return r; }
-__device__ __forceinline__ FF ff_im(float4 v) { FF r; r.h = v.y; r.l = v.w; return r; }
-__device__ __forceinline__ float4 ff_pack(FF re, FF im) { return make_float4(re.h, im.h, re.l, im.l); }
-
-// mu = x/(1-x), x = hD * lam (FP32, |1-x| clamped at 1e-14 like the reference)
-__device__ __forceinline__ float mu_of(float hD, float lam) {
-  const float x = hD * lam;
-  float den = 1.0f - x;
-  if (fabsf(den) < 1e-14f) den = 1e-14f;
-  return x / den;
-}
-__device__ __forceinline__ float4 ff_mstep_c(float4 X, float mu) {
-  return ff_pack(ff_mstep(ff_re(X), mu), ff_mstep(ff_im(X), mu));
-}
-__device__ __forceinline__ float4 ff_add_c(float4 X, float2 d) {
-  return ff_pack(ff_add_f(ff_re(X), d.x), ff_add_f(ff_im(X), d.y));
-}
-
-// One CTA: C adjacent kx columns of one job over all ny rows.  Threads per CTA
-// = 2 C ny/16, so every thread combines exactly min(8, ny/2) elements.  The state
-// operands are read in the combine loop rather than held across the forward
-// transform: 64 registers, so four 256-thread CTAs share an SM and hide each
-// other's load latency (the column passes are latency-bound at 1024^2, where the
-// whole working set sits in L2).  Only ny = 4096 needs 512-thread CTAs.
 template <int NT, int MINB>
 __global__ void __launch_bounds__(NT, MINB) mcol_kernel(const __grid_constant__ MColArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -126,99 +65,17 @@ __global__ void __launch_bounds__(NT, MINB) mcol_kernel(const __grid_constant__ 
   const DevState* st = a.st;
   if (st != nullptr && st->done) return;
   const MJob jb = a.job[blockIdx.y];
-  // the tile holds two outputs side by side (W = 2C) where a job writes two transforms
-  // (C1 split, C3 end); the single-output jobs of C2 use a compact tile (W = C), whose
-  // column transforms then walk shared memory with half the stride
-  const int Cn = a.C, W = (jb.type == MC_FULL_END || jb.type == MC_HALF_MID) ? Cn : 2 * Cn;
-  const int kx0 = blockIdx.x * Cn;
-  const int ny = a.ny, tid = threadIdx.x, nth = blockDim.x;
-  const int total = ny * Cn;
-  const int lc = __ffs(Cn) - 1;  // the tile width is a power of two (col_tile / tile halve from one)
-  const long long ldc = a.ldc;
   const int cur = st != nullptr ? st->cur : 0;
   const double h = st != nullptr ? st->dtc : a.hfixed;
-  const float hA = (float)(0.5 * h * jb.D), hB = (float)(0.25 * h * jb.D);
-  const float nrm = a.inv_norm;
-  const int type = jb.type;
-
-  if (type != MC_SPLIT) {
-    // load the FP32 increment tile and transform it forward along y
-    const float2* zin = type == MC_FULL_END ? a.za : a.zb;
-    float2 v[8];
-#pragma unroll
-    for (int m = 0; m < 8; ++m) {
-      const int e = tid + m * nth;
-      const int ky = e >> lc, c = e & (Cn - 1), kx = kx0 + c;
-      if (e < total) v[m] = kx < a.ncols ? zin[jb.off + ky * ldc + kx] : fmk(0.f, 0.f);
-    }
-#pragma unroll
-    for (int m = 0; m < 8; ++m) {
-      const int e = tid + m * nth;
-      const int ky = e >> lc, c = e & (Cn - 1);
-      if (e < total) buf[sp(ky * W + c)] = v[m];
-    }
-    __syncthreads();
-    fft_smem<float, false, true>(buf, ny, a.log2ny, Cn, 1, W, a.tw, tid);
-  }
-
-  // float-float combine, element by element
-#pragma unroll
-  for (int m = 0; m < 8; ++m) {
-    const int e = tid + m * nth;
-    if (e >= total) continue;
-    const int ky = e >> lc, c = e & (Cn - 1), kx = kx0 + c;
-    if (kx >= a.ncols) {
-      buf[sp(ky * W + c)] = fmk(0.f, 0.f);
-      if (W > Cn) buf[sp(ky * W + Cn + c)] = fmk(0.f, 0.f);
-      continue;
-    }
-    const long long g = jb.off + ky * ldc + kx;
-    const float lam = a.lamx[kx] + a.lamy[ky];
-    float4 Pm, Qm;
-    if (type == MC_SPLIT) Pm = a.ys[cur][g];
-    else if (type == MC_FULL_END) Pm = a.pa[g];
-    else Pm = a.pb[g];
-    if (type == MC_HALF_END) Qm = a.pa[g];
-    if (type == MC_SPLIT) {
-      const float4 PA = ff_mstep_c(Pm, mu_of(hA, lam)), PB = ff_mstep_c(Pm, mu_of(hB, lam));
-      a.pa[g] = PA;
-      a.pb[g] = PB;
-      buf[sp(ky * W + c)] = fmk(ff_scaled(ff_re(PA), nrm), ff_scaled(ff_im(PA), nrm));
-      buf[sp(ky * W + Cn + c)] = fmk(ff_scaled(ff_re(PB), nrm), ff_scaled(ff_im(PB), nrm));
-    } else {
-      const float2 d = buf[sp(ky * W + c)];
-      if (type == MC_FULL_END) {
-        a.pa[g] = ff_mstep_c(ff_add_c(Pm, d), mu_of(hA, lam));
-      } else if (type == MC_HALF_MID) {
-        const float mu = mu_of(hB, lam);
-        const float4 X = ff_mstep_c(ff_mstep_c(ff_add_c(Pm, d), mu), mu);
-        a.pb[g] = X;
-        buf[sp(ky * W + c)] = fmk(ff_scaled(ff_re(X), nrm), ff_scaled(ff_im(X), nrm));
-      } else {  // MC_HALF_END
-        const float4 X = ff_mstep_c(ff_add_c(Pm, d), mu_of(hB, lam));
-        a.ys[1 - cur][g] = X;
-        const float4 Fa = Qm;
-        buf[sp(ky * W + c)] = fmk(ff_diff_scaled(ff_re(X), ff_re(Fa), nrm),
-                                  ff_diff_scaled(ff_im(X), ff_im(Fa), nrm));
-        buf[sp(ky * W + Cn + c)] = fmk(ff_scaled(ff_re(X), nrm), ff_scaled(ff_im(X), nrm));
-      }
-    }
-  }
-  if (type == MC_FULL_END) return;
-  __syncthreads();
-  const int nseq = (type == MC_HALF_MID) ? Cn : W;
-  fft_smem<float, true, true>(buf, ny, a.log2ny, nseq, 1, W, a.tw, tid);
-  const int lns = __ffs(nseq) - 1;
-  for (int e = tid; e < ny * nseq; e += nth) {
-    const int ky = e >> lns, col = e & (nseq - 1);
-    const int half = col >> lc, c = col & (Cn - 1), kx = kx0 + c;
-    if (kx >= a.ncols) continue;
-    const long long g = jb.off + ky * ldc + kx;
-    const float2 v = buf[sp(ky * W + col)];
-    if (type == MC_HALF_MID) a.zb[g] = v;
-    else if (half == 0) a.za[g] = v;
-    else a.zb[g] = v;
-  }
+  MColTile t;
+  t.ny = a.ny; t.log2ny = a.log2ny; t.ncols = a.ncols; t.C = a.C; t.type = jb.type;
+  t.kx0 = blockIdx.x * a.C;
+  t.ldc = a.ldc; t.off = jb.off;
+  t.ys_cur = a.ys[cur]; t.ys_next = a.ys[1 - cur];
+  t.pa = a.pa; t.pb = a.pb; t.za = a.za; t.zb = a.zb;
+  t.lamx = a.lamx; t.lamy = a.lamy; t.tw = a.tw;
+  t.hA = (float)(0.5 * h * jb.D); t.hB = (float)(0.25 * h * jb.D); t.nrm = a.inv_norm;
+  mcol_tile(buf, t, threadIdx.x, blockDim.x);
 }
 
 __global__ void f32_to_f64(const float* in, double* out, long long n) {
@@ -240,7 +97,7 @@ __global__ void c64_to_ff(double2* data, long long n) {
 }
 // current float-float state -> FP64 complex
 __global__ void select_state_kernel(const DevState* st, const float4* y0, const float4* y1, double2* out, long long n) {
-  const float4* src = st->cur == 0 ? y0 : y1;
+  const float4* src = (st == nullptr || st->cur == 0) ? y0 : y1;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
     const float4 v = src[i];
     double2 z; z.x = (double)v.x + (double)v.z; z.y = (double)v.y + (double)v.w;
@@ -456,16 +313,47 @@ static mjx_status from_spectrum64(const void* plan64, const mjx_grid2d* g, int n
   return MJX_OK;
 }
 
-mjx_status ensure_mix_attrs() {
-  static int done = 0;
-  if (done) return MJX_OK;
-  int dev = 0, optin = 0;
-  MJX_CUDA_TRY(cudaGetDevice(&dev));
-  MJX_CUDA_TRY(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-  MJX_CUDA_TRY(cudaFuncSetAttribute(mcol_kernel<256, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
-  MJX_CUDA_TRY(cudaFuncSetAttribute(mcol_kernel<512, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
-  done = 1;
+mjx_status mix_state_from_real(const void* plan64, const mjx_grid2d* g, int nf, int io_dtype, const void* y,
+                               double* real64, float4* ys, cudaStream_t s) {
+  const long long nelem = (long long)nf * g->ny * g->nx;
+  if (io_dtype == MJX_F32) {
+    f32_to_f64<<<304, 256, 0, s>>>((const float*)y, real64, nelem);
+    MJX_CUDA_TRY(cudaGetLastError());
+  } else {
+    MJX_CUDA_TRY(cudaMemcpyAsync(real64, y, nelem * 8, cudaMemcpyDeviceToDevice, s));
+  }
+  MJX_TRY(to_spectrum64(plan64, g, nf, real64, (double2*)ys, s));
+  c64_to_ff<<<304, 256, 0, s>>>((double2*)ys, (long long)nf * g->ny * spec_ldc(g->nx));
+  MJX_CUDA_TRY(cudaGetLastError());
   return MJX_OK;
+}
+
+mjx_status mix_real_from_state(const void* plan64, const mjx_grid2d* g, int nf, const DevState* st,
+                               const float4* ys0, const float4* ys1, double2* spec64, double* real64,
+                               int io_dtype, void* y_out, cudaStream_t s) {
+  const long long nelem = (long long)nf * g->ny * g->nx;
+  select_state_kernel<<<304, 256, 0, s>>>(st, ys0, ys1, spec64, (long long)nf * g->ny * spec_ldc(g->nx));
+  MJX_CUDA_TRY(cudaGetLastError());
+  MJX_TRY(from_spectrum64(plan64, g, nf, spec64, real64, s));
+  if (io_dtype == MJX_F32) {
+    f64_to_f32<<<304, 256, 0, s>>>(real64, (float*)y_out, nelem);
+    MJX_CUDA_TRY(cudaGetLastError());
+  } else if ((void*)real64 != y_out) {
+    MJX_CUDA_TRY(cudaMemcpyAsync(y_out, real64, nelem * 8, cudaMemcpyDeviceToDevice, s));
+  }
+  return MJX_OK;
+}
+
+mjx_status ensure_mix_attrs() {
+  static ContextOnce once;
+  return once.run([]() -> mjx_status {
+    int dev = 0, optin = 0;
+    MJX_CUDA_TRY(cudaGetDevice(&dev));
+    MJX_CUDA_TRY(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    MJX_CUDA_TRY(cudaFuncSetAttribute(mcol_kernel<256, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
+    MJX_CUDA_TRY(cudaFuncSetAttribute(mcol_kernel<512, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
+    return MJX_OK;
+  });
 }
 
 }  // namespace mjx
@@ -553,15 +441,7 @@ mjx_status mjx_imex_adaptive2d_mixed(const void* plan32, const void* plan64, con
 
   // initial spectral state in FP64 (real input staged in PA)
   double* real64 = (double*)(w + L.pa);
-  if (e == 4) {
-    f32_to_f64<<<304, 256, 0, s>>>((const float*)y0, real64, nelem);
-    MJX_CUDA_TRY(cudaGetLastError());
-  } else {
-    MJX_CUDA_TRY(cudaMemcpyAsync(real64, y0, nelem * 8, cudaMemcpyDeviceToDevice, s));
-  }
-  MJX_TRY(to_spectrum64(plan64, g, nf, real64, (double2*)(w + L.ys0), s));
-  c64_to_ff<<<304, 256, 0, s>>>((double2*)(w + L.ys0), (long long)nf * L.fs);
-  MJX_CUDA_TRY(cudaGetLastError());
+  MJX_TRY(mix_state_from_real(plan64, g, nf, io_dtype, y0, real64, (float4*)(w + L.ys0), s));
 
   DevState h;
   memset(&h, 0, sizeof(h));
@@ -632,17 +512,8 @@ mjx_status mjx_imex_adaptive2d_mixed(const void* plan32, const void* plan64, con
     if (ce != cudaSuccess) { set_last_error(ce, __FILE__, __LINE__); return MJX_CUDA_ERROR; }
   }
   // final real state: select Y^[cur] into PB, inverse FP64 transform, write real into PA
-  double2* spec = (double2*)(w + L.pb);
-  select_state_kernel<<<304, 256, 0, s>>>(st, (const float4*)(w + L.ys0), (const float4*)(w + L.ys1), spec,
-                                          (long long)nf * L.fs);
-  MJX_CUDA_TRY(cudaGetLastError());
-  MJX_TRY(from_spectrum64(plan64, g, nf, spec, real64, s));
-  if (e == 4) {
-    f64_to_f32<<<304, 256, 0, s>>>(real64, (float*)y_final, nelem);
-    MJX_CUDA_TRY(cudaGetLastError());
-  } else {
-    MJX_CUDA_TRY(cudaMemcpyAsync(y_final, real64, nelem * 8, cudaMemcpyDeviceToDevice, s));
-  }
+  MJX_TRY(mix_real_from_state(plan64, g, nf, st, (const float4*)(w + L.ys0), (const float4*)(w + L.ys1),
+                              (double2*)(w + L.pb), real64, io_dtype, y_final, s));
   DevState out;
   MJX_CUDA_TRY(cudaMemcpyAsync(&out, st, sizeof(out), cudaMemcpyDeviceToHost, s));
   MJX_CUDA_TRY(cudaStreamSynchronize(s));

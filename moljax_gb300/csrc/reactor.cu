@@ -197,15 +197,15 @@ mjx_status mjx_reactor_cn_batch(const mjx_reactor_instance* inst_dev, int n_inst
   if (!inst_dev || !out || n_inst < 0 || max_n < 2) return MJX_BAD_ARG;
   if (n_inst == 0) return MJX_OK;
   const size_t smem = mjx_reactor_smem_bytes(max_n, dtype);
-  static int attr_done = 0;
-  if (!attr_done) {
+  static ContextOnce attr;
+  MJX_TRY(attr.run([]() -> mjx_status {
     int dev = 0, optin = 0;
     MJX_CUDA_TRY(cudaGetDevice(&dev));
     MJX_CUDA_TRY(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
     MJX_CUDA_TRY(cudaFuncSetAttribute(reactor_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
     MJX_CUDA_TRY(cudaFuncSetAttribute(reactor_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
-    attr_done = 1;
-  }
+    return MJX_OK;
+  }));
   if (smem > 227 * 1024) return MJX_BAD_SHAPE;
   ReactorArgs A;
   A.inst = inst_dev; A.out = out; A.n_inst = n_inst;

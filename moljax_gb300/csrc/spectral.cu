@@ -11,6 +11,8 @@
 
 #include "spectral.cuh"
 
+struct CUctx_st;  // driver-API context (opaque)
+
 namespace mjx {
 
 static inline size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
@@ -471,23 +473,54 @@ static mjx_status raise_smem(K kernel, int optin) {
   return MJX_OK;
 }
 
-// Raise the dynamic shared-memory limit of every kernel once per device.
+// Raise the dynamic shared-memory limit of every kernel once per CUDA context
+// (function attributes belong to the context the kernels are loaded in).
 mjx_status ensure_kernel_attrs() {
-  static int done_mask = 0;
-  int dev = 0;
-  MJX_CUDA_TRY(cudaGetDevice(&dev));
-  if (dev < 31 && (done_mask & (1 << dev))) return MJX_OK;
-  int optin = 0;
-  MJX_CUDA_TRY(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-  MJX_TRY(raise_smem(row_kernel<float, RX_NONE>, optin));
-  MJX_TRY(raise_smem(row_kernel<float, RX_GRAY_SCOTT>, optin));
-  MJX_TRY(raise_smem(row_kernel<float, RX_FISHER>, optin));
-  MJX_TRY(raise_smem(row_kernel<double, RX_NONE>, optin));
-  MJX_TRY(raise_smem(row_kernel<double, RX_GRAY_SCOTT>, optin));
-  MJX_TRY(raise_smem(row_kernel<double, RX_FISHER>, optin));
-  MJX_TRY(raise_smem(col_kernel<float>, optin));
-  MJX_TRY(raise_smem(col_kernel<double>, optin));
-  if (dev < 31) done_mask |= 1 << dev;
+  static ContextOnce once;
+  return once.run([]() -> mjx_status {
+    int dev = 0, optin = 0;
+    MJX_CUDA_TRY(cudaGetDevice(&dev));
+    MJX_CUDA_TRY(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    MJX_TRY(raise_smem(row_kernel<float, RX_NONE>, optin));
+    MJX_TRY(raise_smem(row_kernel<float, RX_GRAY_SCOTT>, optin));
+    MJX_TRY(raise_smem(row_kernel<float, RX_FISHER>, optin));
+    MJX_TRY(raise_smem(row_kernel<double, RX_NONE>, optin));
+    MJX_TRY(raise_smem(row_kernel<double, RX_GRAY_SCOTT>, optin));
+    MJX_TRY(raise_smem(row_kernel<double, RX_FISHER>, optin));
+    MJX_TRY(raise_smem(col_kernel<float>, optin));
+    MJX_TRY(raise_smem(col_kernel<double>, optin));
+    return MJX_OK;
+  });
+}
+
+typedef int (*PfnCtxGetCurrent)(CUctx_st**);
+typedef int (*PfnCtxGetId)(CUctx_st*, unsigned long long*);
+
+mjx_status current_context_id(unsigned long long* id) {
+  static PfnCtxGetCurrent get_current = nullptr;
+  static PfnCtxGetId get_id = nullptr;
+  static std::once_flag resolved;
+  std::call_once(resolved, []() {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_current = (PfnCtxGetCurrent)f;
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = (PfnCtxGetId)f;
+  });
+  if (get_current == nullptr || get_id == nullptr) return cuda_status(cudaErrorNotSupported);
+  CUctx_st* ctx = nullptr;
+  if (get_current(&ctx) != 0) return cuda_status(cudaErrorDeviceUninitialized);
+  if (ctx == nullptr) {  // nothing current yet: the runtime's default is the primary context
+    int dev = 0;
+    MJX_CUDA_TRY(cudaGetDevice(&dev));
+    MJX_CUDA_TRY(cudaSetDevice(dev));
+    if (get_current(&ctx) != 0 || ctx == nullptr) return cuda_status(cudaErrorDeviceUninitialized);
+  }
+  if (get_id(ctx, id) != 0) return cuda_status(cudaErrorDeviceUninitialized);
   return MJX_OK;
 }
 
@@ -615,23 +648,34 @@ mjx_status fft_cn(const void* plan, const mjx_grid2d* g, double D, double dt, in
 // own device memory: every GPU that loads the library holds these bytes until
 // the process exits.  Host code must not pass the symbol itself to a kernel
 // (in host code it is only a stand-in); the device address comes from
-// cudaGetSymbolAddress, once per device.
+// cudaGetSymbolAddress, once per CUDA context.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[MJX_NOALLOC_SCRATCH_BYTES];
 
+// Scratch addresses by CUDA context.  A __device__ array has a separate
+// address in every context that loads the library (the primary context, a
+// driver-API context of an embedding host, the new primary context after
+// cudaDeviceReset), so the lookup is cached per context id, never per device.
 static std::mutex g_noalloc_mu;
-static void* g_noalloc_ptr[64];
+static unsigned long long g_noalloc_ctx[32];
+static void* g_noalloc_ptr[32];
+static int g_noalloc_n = 0;
 
 static mjx_status noalloc_scratch(void** out) {
-  int dev = 0;
-  MJX_CUDA_TRY(cudaGetDevice(&dev));
-  if (dev < 0 || dev >= 64) return MJX_BAD_ARG;
+  unsigned long long ctx = 0;
+  MJX_TRY(current_context_id(&ctx));
   std::lock_guard<std::mutex> lk(g_noalloc_mu);
-  if (g_noalloc_ptr[dev] == nullptr) {
-    void* p = nullptr;
-    MJX_CUDA_TRY(cudaGetSymbolAddress(&p, g_noalloc_scratch));
-    g_noalloc_ptr[dev] = p;
-  }
-  *out = g_noalloc_ptr[dev];
+  const int m = g_noalloc_n < 32 ? g_noalloc_n : 32;
+  for (int i = 0; i < m; ++i)
+    if (g_noalloc_ctx[i] == ctx) {
+      *out = g_noalloc_ptr[i];
+      return MJX_OK;
+    }
+  void* p = nullptr;
+  MJX_CUDA_TRY(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+  g_noalloc_ctx[g_noalloc_n % 32] = ctx;
+  g_noalloc_ptr[g_noalloc_n % 32] = p;
+  ++g_noalloc_n;
+  *out = p;
   return MJX_OK;
 }
 

@@ -1,7 +1,7 @@
 """Writes tests/golden/*.json from the reference's own published result files.
 
-Run in a checkout that has the reference (gogipav14/moljax) at REF (default
-/root/reference).  The fixtures hold only the numbers the tests pin:
+Usage: python tests/golden/make_golden.py <path of a gogipav14/moljax checkout>.
+The fixtures hold only the numbers the tests pin:
 the FFT-CN error tables of benchmarks/results/precision_fp32_fp64.json and
 benchmarks/results/scipy_comparison.json, the CN reactor conversions of
 benchmarks/results/method_comparison_results.json, and the 3D FFT-CN errors and
@@ -12,12 +12,11 @@ import json
 import os
 import sys
 
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
 HERE = os.path.dirname(os.path.abspath(__file__))
 
 
-def main():
-    res = os.path.join(REF, "benchmarks", "results")
+def main(ref):
+    res = os.path.join(ref, "benchmarks", "results")
     prec = json.load(open(os.path.join(res, "precision_fp32_fp64.json")))
     sc = json.load(open(os.path.join(res, "scipy_comparison.json")))
     out = {
@@ -52,4 +51,6 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_golden.py <path of the gogipav14/moljax checkout>")
+    main(sys.argv[1])
