@@ -576,6 +576,66 @@ mjx_status mjx_imex_attempt_kernel2d(const void* plan, const mjx_grid2d* grid, i
                                      int which, double dt, const void* y, void* ws,
                                      size_t ws_bytes, void* stream);
 
+/* ---- batched adaptive IMEX-Strang: many Gray-Scott solves in one engine ------------ */
+/* One Gray-Scott solve of the batch: grid, parameters, time span and controller
+ * settings of adaptive_integrate_imex (moljax/core/stepping.py:1146-1371) for the
+ * periodic model of create_gray_scott_periodic_fft (moljax/core/model.py:529-584). */
+typedef struct mjx_gs_instance {
+  int ny, nx;           /* powers of two, 16 <= ny <= 2048, 16 <= nx <= 4096 */
+  double dy, dx;
+  double Du, Dv, F, k;
+  double t0, t_end, dt0;
+  double dt_cfl;        /* imex_cfl_dt (moljax/core/dt_policy.py:430-502), host-computed */
+  int max_steps, save_every, max_attempts, pad;  /* max_attempts <= 0: 20 max_steps + 1000 */
+  mjx_pid_params pid;
+} mjx_gs_instance;
+
+/* Engine device bytes for up to max_instances solves and max_work work items per
+ * pass (sum of mjx_gsbatch_work_items over the solves in flight). */
+size_t mjx_gsbatch_bytes(int max_instances, int max_work);
+/* Device bytes of one solve's workspace (float-float spectral state, FP32 and FP64
+ * plans, error partials, t/dt history of max_saves = max_steps / save_every + 1). */
+size_t mjx_gsbatch_instance_bytes(int ny, int nx, int max_saves);
+/* Work items of one solve in the largest pass. */
+int mjx_gsbatch_work_items(int ny, int nx);
+
+/* Creates a batch engine in the caller's device workspace ws (mjx_gsbatch_bytes).
+ * Every solve runs the mixed-precision attempt of mjx_imex_adaptive2d_mixed with
+ * its own dt, controller state, accept mask and status; one persistent kernel per
+ * attempt stage covers every solve in flight, and a batched controller (one warp per
+ * solve) applies the PI / accept-reject update of each.  The attempt loop is a CUDA
+ * graph with a conditional while node, captured once here; admissions and retirements
+ * change only device memory.  The engine also holds one mapped pinned host flag
+ * (mjx_gsbatch_request_stop).  Thread-compatible: one thread drives an engine.
+ * The reference's only batching is stacking and vmap (moljax/core/jit_kernels.py:422-441,
+ * fft_integrators.py:473-510); there is no engine counterpart. */
+mjx_status mjx_gsbatch_create(void** batch, int max_instances, int max_work, void* ws, size_t ws_bytes);
+mjx_status mjx_gsbatch_destroy(void* batch);
+/* Admits one solve: y0 is [2][ny][nx] (u then v, io_dtype) and goes through an FP64
+ * transform into the solve's float-float spectral state in ws
+ * (mjx_gsbatch_instance_bytes); returns its slot.  MJX_OOM when no slot or no work-list
+ * room is free.  Synchronises the stream. */
+mjx_status mjx_gsbatch_admit(void* batch, const mjx_gs_instance* inst, int io_dtype, const void* y0, void* ws,
+                             size_t ws_bytes, int* slot, void* stream);
+/* Runs attempts of every admitted solve (one epoch) until none is running, until
+ * stop_after_finished solves finished in this epoch (0: no such stop), after
+ * max_attempts attempts, or when the stop flag is raised; blocks until the epoch ends.
+ * n_running / n_finished (optional): solves still running, and finished solves waiting
+ * for mjx_gsbatch_retire. */
+mjx_status mjx_gsbatch_run(void* batch, int max_attempts, int stop_after_finished, int* n_running,
+                           int* n_finished, void* stream);
+/* Slots of the finished solves (up to cap of them) and their count. */
+mjx_status mjx_gsbatch_finished(void* batch, int* slots, int cap, int* n);
+/* Writes a finished solve's final state y_final ([2][ny][nx], io_dtype, by an FP64
+ * inverse transform), its t/dt history (HOST arrays of n_saved doubles, may be NULL)
+ * and its result (AdaptiveResult scalars), then frees the slot.  The solve's workspace
+ * may be released afterwards. */
+mjx_status mjx_gsbatch_retire(void* batch, int slot, int io_dtype, void* y_final, double* hist_t, double* hist_dt,
+                              mjx_adaptive_result* res, void* stream);
+/* Raises (stop != 0) or clears the stop flag from any host thread: a running epoch
+ * ends at its next attempt boundary (the server uses it to admit arrivals). */
+void mjx_gsbatch_request_stop(void* batch, int stop);
+
 /* ---- Autotuning --------------------------------------------------------------
  * No reference counterpart: under jax.jit XLA chooses its own FFT and fusion
  * strategies (moljax/core/fft_solvers.py:33-80 calls jnp.fft.fft2 / ifft2 and

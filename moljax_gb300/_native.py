@@ -88,6 +88,14 @@ class AdaptiveResultC(C.Structure):
                 ("finite", C.c_int)]
 
 
+class GsInstanceC(C.Structure):
+    _fields_ = [("ny", C.c_int), ("nx", C.c_int), ("dy", C.c_double), ("dx", C.c_double),
+                ("Du", C.c_double), ("Dv", C.c_double), ("F", C.c_double), ("k", C.c_double),
+                ("t0", C.c_double), ("t_end", C.c_double), ("dt0", C.c_double), ("dt_cfl", C.c_double),
+                ("max_steps", C.c_int), ("save_every", C.c_int), ("max_attempts", C.c_int),
+                ("pad", C.c_int), ("pid", PIDParamsC)]
+
+
 _vp, _sz, _i, _d = C.c_void_p, C.c_size_t, C.c_int, C.c_double
 # name -> (restype, argtypes); the list is the exported C ABI
 SIGNATURES = {
@@ -185,6 +193,17 @@ SIGNATURES = {
                                              C.POINTER(PIDParamsC), _i, _d, _vp, _vp, _sz, _vp]),
     "mjx_imex_attempt_kernel2d": (_i, [_vp, C.POINTER(Grid2DC), _i, C.POINTER(ImexProblemC),
                                        C.POINTER(PIDParamsC), _i, _d, _vp, _vp, _sz, _vp]),
+    "mjx_gsbatch_bytes": (_sz, [_i, _i]),
+    "mjx_gsbatch_instance_bytes": (_sz, [_i, _i, _i]),
+    "mjx_gsbatch_work_items": (_i, [_i, _i]),
+    "mjx_gsbatch_create": (_i, [C.POINTER(C.c_void_p), _i, _i, _vp, _sz]),
+    "mjx_gsbatch_destroy": (_i, [_vp]),
+    "mjx_gsbatch_admit": (_i, [_vp, C.POINTER(GsInstanceC), _i, _vp, _vp, _sz, C.POINTER(C.c_int), _vp]),
+    "mjx_gsbatch_run": (_i, [_vp, _i, _i, C.POINTER(C.c_int), C.POINTER(C.c_int), _vp]),
+    "mjx_gsbatch_finished": (_i, [_vp, C.POINTER(C.c_int), _i, C.POINTER(C.c_int)]),
+    "mjx_gsbatch_retire": (_i, [_vp, _i, _i, _vp, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                C.POINTER(AdaptiveResultC), _vp]),
+    "mjx_gsbatch_request_stop": (None, [_vp, _i]),
     "mjx_dft_schedule_candidates": (_i, [_i, C.POINTER(C.c_int), _i]),
     "mjx_dft_schedule_set": (_i, [_i, _i, _i, C.POINTER(C.c_int), _i]),
     "mjx_dft_schedule_get": (_i, [_i, _i, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),

@@ -76,3 +76,5 @@ from moljax_gb300.core.preconditioners import (create_gray_scott_preconditioner,
 from moljax_gb300.core.dt_policy import estimate_reaction_stiffness
 from moljax_gb300.core.fft_operators import FFTLinearOperator
 from moljax_gb300.core.fft_integrators import ETDStepResult
+from moljax_gb300.core import batch
+from moljax_gb300.core.batch import GrayScottBatch, GrayScottProblem, adaptive_integrate_imex_batch

@@ -76,6 +76,13 @@ def _problem(model, diffusivities, cfl_params, max_attempts=0, use_strang=True):
     return p
 
 
+def _pid_c(pid_params):
+    """PIDParams -> the C struct (moljax/core/dt_policy.py:49-78 fields)."""
+    return N.PIDParamsC(pid_params.safety, pid_params.kI, pid_params.kP, pid_params.dt_min,
+                        pid_params.dt_max, pid_params.max_factor, pid_params.min_factor,
+                        pid_params.atol, pid_params.rtol)
+
+
 def _periodic_only(model):
     from moljax_gb300.core.bc import BCType
     for n, s in model.bc_spec.items():
@@ -223,9 +230,7 @@ def adaptive_integrate_imex(model, y0, t0, t_end, dt0, fft_cache=None, diffusivi
         raise ValueError(f"precision must be 'fp32', 'fp64' or 'mixed', not {precision!r}")
     if (precision == "fp64") != (interior.dtype == torch.float64):
         raise TypeError(f"precision {precision!r} needs a {'float64' if precision == 'fp64' else 'float32'} state")
-    pid = N.PIDParamsC(pid_params.safety, pid_params.kI, pid_params.kP, pid_params.dt_min,
-                       pid_params.dt_max, pid_params.max_factor, pid_params.min_factor,
-                       pid_params.atol, pid_params.rtol)
+    pid = _pid_c(pid_params)
     lib = N.lib()
     dev = plan.device
     max_saves = max_steps // save_every + 1
@@ -332,9 +337,7 @@ def _adaptive_mixed(model, interior, plan, prob, pid_params, t0, t_end, dt0, max
     names = model.field_names
     p32 = get_plan(plan.ny, plan.nx, plan.dy, plan.dx, plan.symbol, torch.float32, plan.device)
     p64 = get_plan(plan.ny, plan.nx, plan.dy, plan.dx, plan.symbol, torch.float64, plan.device)
-    pid = N.PIDParamsC(pid_params.safety, pid_params.kI, pid_params.kP, pid_params.dt_min,
-                       pid_params.dt_max, pid_params.max_factor, pid_params.min_factor,
-                       pid_params.atol, pid_params.rtol)
+    pid = _pid_c(pid_params)
     lib = N.lib()
     dev = plan.device
     max_saves = max_steps // save_every + 1
@@ -451,9 +454,7 @@ def _adaptive_explicit(model, y0, t0, t_end, dt0, method, max_steps, cfl_params,
         y_hist = torch.empty((max_saves,) + tuple(interior.shape), dtype=interior.dtype, device=dev)
     else:
         y_hist = None
-    pid = N.PIDParamsC(pid_params.safety, pid_params.kI, pid_params.kP, pid_params.dt_min,
-                       pid_params.dt_max, pid_params.max_factor, pid_params.min_factor,
-                       pid_params.atol, pid_params.rtol)
+    pid = _pid_c(pid_params)
     res = N.AdaptiveResultC()
     N.check("mjx_explicit_adaptive2d", lib.mjx_explicit_adaptive2d(
         C.byref(N.Grid2DC(grid.ny, grid.nx, grid.dy, grid.dx)), code, C.byref(prob), C.byref(pid),
@@ -603,9 +604,7 @@ def _adaptive_implicit(model, y0, t0, t_end, dt0, method, max_steps, pid_params,
     log_cap = 20 * max_steps + 1000 if attempt_log is not None else 0
     log = (C.c_double * (6 * max(log_cap, 1)))() if attempt_log is not None else None
     res = N.AdaptiveResultC()
-    pid = N.PIDParamsC(pid_params.safety, pid_params.kI, pid_params.kP, pid_params.dt_min,
-                       pid_params.dt_max, pid_params.max_factor, pid_params.min_factor,
-                       pid_params.atol, pid_params.rtol)
+    pid = _pid_c(pid_params)
     N.check("mjx_nk_vardiff_adaptive2d", lib.mjx_nk_vardiff_adaptive2d(
         N.ptr(plan2.buf), n, float(g.dy), float(g.dx), abc, _IMPLICIT[method], C.byref(pid),
         float(t0), float(t_end), float(dt0), int(max_steps), int(save_every),

@@ -90,31 +90,6 @@ __device__ __forceinline__ void react_euler(T& a, T& b, T h, T F, T k, T r) {
 
 template <typename T> __device__ __forceinline__ bool finite_(T v) { return isfinite(v); }
 
-// The Heun increment y** - y* computed without forming y** (no cancellation).
-template <typename T, int RX>
-__device__ __forceinline__ void react_delta(T& a, T& b, T h, T F, T k, T r) {
-  const T hh = (T)0.5 * h;
-  if (RX == RX_GRAY_SCOTT) {
-    const T uvv = a * b * b;
-    const T fu = -uvv + F * ((T)1 - a);
-    const T fv = uvv - (F + k) * b;
-    const T ua = a + h * fu, va = b + h * fv;
-    const T uvv2 = ua * va * va;
-    const T gu = -uvv2 + F * ((T)1 - ua);
-    const T gv = uvv2 - (F + k) * va;
-    a = hh * (fu + gu);
-    b = hh * (fv + gv);
-  } else if (RX == RX_FISHER) {
-    const T fa = r * a * ((T)1 - a), fb = r * b * ((T)1 - b);
-    const T ta = a + h * fa, tb = b + h * fb;
-    a = hh * (fa + r * ta * ((T)1 - ta));
-    b = hh * (fb + r * tb * ((T)1 - tb));
-  } else {
-    a = (T)0;
-    b = (T)0;
-  }
-}
-
 // ------------------------------------------------------------------ row pass
 template <typename T> struct Occ { static constexpr int row = sizeof(T) == 4 ? 4 : 2, col = sizeof(T) == 4 ? 2 : 1; };
 

@@ -49,6 +49,31 @@ enum {
 // pointwise reaction kinds (compile-time)
 enum { RX_NONE = 0, RX_GRAY_SCOTT = 1, RX_FISHER = 2, RX_LINEAR = 3 };
 
+// The Heun increment y** - y* computed without forming y** (no cancellation).
+template <typename T, int RX>
+__device__ __forceinline__ void react_delta(T& a, T& b, T h, T F, T k, T r) {
+  const T hh = (T)0.5 * h;
+  if (RX == RX_GRAY_SCOTT) {
+    const T uvv = a * b * b;
+    const T fu = -uvv + F * ((T)1 - a);
+    const T fv = uvv - (F + k) * b;
+    const T ua = a + h * fu, va = b + h * fv;
+    const T uvv2 = ua * va * va;
+    const T gu = -uvv2 + F * ((T)1 - ua);
+    const T gv = uvv2 - (F + k) * va;
+    a = hh * (fu + gu);
+    b = hh * (fv + gv);
+  } else if (RX == RX_FISHER) {
+    const T fa = r * a * ((T)1 - a), fb = r * b * ((T)1 - b);
+    const T ta = a + h * fa, tb = b + h * fb;
+    a = hh * (fa + r * ta * ((T)1 - ta));
+    b = hh * (fb + r * tb * ((T)1 - tb));
+  } else {
+    a = (T)0;
+    b = (T)0;
+  }
+}
+
 struct RowPair {
   long long ra, rb;    // real row offsets (elements) of rows a and b at y = 0
   long long sa, sb;    // spectrum offsets (complex elements) at ky = 0
