@@ -66,7 +66,8 @@ def parse():
     ap.add_argument("--kernels-only", action="store_true")
     ap.add_argument("--workload", default="imex", choices=["imex", "etdrk4", "serve", "fft3d", "explicit", "nk", "stencil"])
     ap.add_argument("--fp32", action="store_true", help="fft3d: FP32 instead of FP64")
-    ap.add_argument("--requests", type=int, default=512)
+    ap.add_argument("--requests", type=int, default=256)
+    ap.add_argument("--no-configs", action="store_true", help="skip the configs 1, 3, 4, 5 legs of the default line")
     ap.add_argument("--etd-steps", type=int, default=100)
     ap.add_argument("--etd-method", default="etdrk4", choices=["etdrk4", "etd1", "etd2"])
     ap.add_argument("--reps", type=int, default=30)
@@ -408,8 +409,12 @@ def run_ours(args, rank, world, local):
             "clocks": clk,
             "wall_s": wall,
         }
+        if not args.no_configs:
+            # the other benchmark configurations, each measured on its own terms
+            out["configs"] = {"fft_cn_128": fftcn_leg(dev), "etdrk4_4096": etdrk4_leg(dev),
+                              "nk_bdf2_512": nk_leg(dev), "served_mix": served_mix(dev, args.requests)}
         if not args.no_cpu_baseline and world == 1:
-            out["cpu_baseline"] = cpu_baseline(args, sample_attempts=None)
+            out["cpu_baseline"] = cpu_baseline(args)
     return out
 
 
@@ -754,24 +759,115 @@ def run_nk(args, local):
     return out
 
 
-def run_serve(args, local):
-    """The served mix (Poisson arrivals, 60 % tubular-reactor CN, 40 % Gray-Scott IMEX-Strang
-    64^2..512^2): continuous-batching server vs one FP64 solve at a time (the first
-    min(128, requests) requests for the plain comparator)."""
+def fftcn_leg(dev):
+    """Config 1: FFT-CN 128^2 on [0,1)^2 (node grid), FP64, D = 0.1, dt = 0.01, 100 steps one
+    by one through fft_solvers.fft_cn_step, pseudo-spectral symbol; absolute pt-steps/s (the
+    128^2 field sits on chip, so the pass is latency-bound and no roofline applies) and the
+    error against the analytic decay exp(-8 pi^2 D t) (CN truncation 4.1e-3 relative)."""
+    import torch
+    import moljax_gb300 as M
+    n, D, dt, S = 128, 0.1, 0.01, 100
+    x = torch.arange(n, dtype=torch.float64, device=dev) / n
+    u0 = (torch.sin(2 * math.pi * x)[:, None] * torch.sin(2 * math.pi * x)[None, :]).contiguous()
+    for _ in range(3):
+        M.fft_cn_step(u0, D, 1.0 / n, dt, S)
+    torch.cuda.synchronize(dev)
+    s = torch.cuda.current_stream(dev)
+    ts = []
+    for _ in range(5):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        u = M.fft_cn_step(u0, D, 1.0 / n, dt, S)
+        e1.record(s)
+        e1.synchronize()
+        ts.append(e0.elapsed_time(e1) * 1e-3)
+    t = min(ts)
+    exact = u0 * math.exp(-8 * math.pi ** 2 * D * dt * S)
+    rel = float(torch.linalg.norm(u - exact) / torch.linalg.norm(exact))
+    return {"workload": "FFT-CN 2D periodic diffusion 128x128 FP64, D=0.1, dt=0.01, 100 steps (fft_cn_step)",
+            "value": n * n * S / t, "unit": UNIT, "ms_per_solve": t * 1e3, "us_per_step": t / S * 1e6,
+            "rel_l2_vs_analytic_decay": rel, "gpu_launches_per_solve": 3 * S,
+            "roofline": "latency-bound (128^2 FP64 field, 128 KB, on chip): absolute throughput only"}
+
+
+def nk_leg(dev, n=512, steps=20):
+    """Config 4: NK-BDF2 at 512^2 (run_nk) plus the achieved bandwidth by the byte
+    convention per GMRES iteration j of a cycle, (11 + 2 j) b per point (JVP 3b, DST
+    preconditioner 6b, Arnoldi (2j + 2) b, b = 4), and 32 B per point per Newton residual."""
+    import types
+    out = run_nk(types.SimpleNamespace(n=n, etd_steps=steps, no_cpu_baseline=True), dev.index or 0)
+    g_per_newton = out["gmres_per_step"] / max(out["newton_per_step"], 1e-9)
+    jbar = max(g_per_newton - 1.0, 0.0) / 2.0
+    bytes_step = n * n * (out["gmres_per_step"] * (11 + 2 * jbar) * 4 + out["newton_per_step"] * 32)
+    peak, peak_kind = peaks()
+    gbs = bytes_step / (out["ms_per_step"] * 1e-3) / 1e9
+    out["alg_bytes_per_step"] = bytes_step
+    out["achieved_gbs"] = gbs
+    out["frac_of_" + peak_kind] = gbs / peak
+    out["bound"] = "launch/sync: ~11 kernels per GMRES iteration plus host reads of Newton norms"
+    return out
+
+
+def etdrk4_leg(dev, n=4096, steps=100, err_steps=10):
+    """Config 3: coupled Gray-Scott ETDRK4 at 4096^2, FP32 state with FP64 contour
+    coefficients, dt = 1 (run_etdrk4: throughput and per-pass roofline), plus the FP32
+    against FP64 relative L2 error after err_steps steps from the same initial state."""
+    import types
+    import torch
+    import moljax_gb300 as M
+    from moljax_gb300.workloads import gray_scott_initial_condition
+    out = run_etdrk4(types.SimpleNamespace(n=n, etd_steps=steps, kernels_only=False, reps=10,
+                                           etd_method="etdrk4"), dev.index or 0)
+    grid = M.Grid2D(n, n, 0.0, L_BOX, 0.0, L_BOX)
+    y32 = gray_scott_initial_condition(grid, SEED, torch.float32, dev)
+    y64 = {k: v.double() for k, v in y32.items()}
+    r32 = M.etdrk4_gray_scott(M.create_gray_scott_model(grid, DU, DV, F, K, dtype=torch.float32), y32, 1.0, err_steps)
+    r64 = M.etdrk4_gray_scott(M.create_gray_scott_model(grid, DU, DV, F, K, dtype=torch.float64), y64, 1.0, err_steps)
+    num = sum(float(torch.linalg.norm(r32[k].double() - r64[k])) ** 2 for k in ("u", "v"))
+    den = sum(float(torch.linalg.norm(r64[k])) ** 2 for k in ("u", "v"))
+    out["fp32_rel_l2_vs_fp64"] = (num / den) ** 0.5
+    out["error_steps"] = err_steps
+    return out
+
+
+def served_mix(dev, n_requests, realtime=True, slots=64):
+    """The served mix (config 5's Poisson arrivals at 2000/s, seed 5, its first n_requests
+    requests): the continuous-batching server (FP32 + float-float Gray-Scott batch engine,
+    batched reactor kernel) against the same requests solved one at a time in FP64 (the
+    plain form of the same kernels), FIFO, no arrival waits.  Reports p50/p99 latency,
+    solves/s and grid-point-steps/s of both, their ratio, and the largest rel-L2 of a
+    served Gray-Scott result against its plain FP64 result."""
     import torch
     from moljax_gb300.serve import make_mix, Server, run_plain, summarize
+    Server(dev, slots=8).run(make_mix(12, seed=99, gs_sizes=(64, 128)), realtime=False)  # warm kernels
+    mix = make_mix(n_requests)
+    srv = Server(dev, slots=slots)
+    done = srv.run(mix, realtime=realtime)
+    served = summarize(done, srv.makespan)
+    served.update({"reactor_batches": srv.batches, "gs_epochs": srv.epochs, "slots": slots})
+    plain = run_plain(mix, torch.float64, dev, realtime=False)
+    pl = summarize(plain, max(c.end for c in plain))
+    by_id = {c.rid: c for c in plain}
+    err = 0.0
+    for c in done:
+        if c.kind == "gs":
+            ref = by_id[c.rid].output
+            err = max(err, float(torch.linalg.norm(c.output.double() - ref) / torch.linalg.norm(ref)))
+    n_gs = sum(1 for r in mix if r.kind == "gs")
+    return {"workload": f"served mix: first {n_requests} requests of the config-5 stream (Poisson 2000/s, seed 5; "
+                        f"{n_gs} Gray-Scott 64^2..512^2 t_end=100, {n_requests - n_gs} reactor CN n=64..4096)",
+            "served": served, "plain_fp64": pl,
+            "speedup_pt_steps": served["pt_steps_per_s"] / pl["pt_steps_per_s"],
+            "speedup_solves": served["solves_per_s"] / pl["solves_per_s"],
+            "gs_max_rel_l2_vs_plain_fp64": err}
+
+
+def run_serve(args, local):
+    """--workload serve: the served mix with --requests requests (see served_mix)."""
+    import torch
     dev = torch.device("cuda", local)
     torch.cuda.set_device(dev)
-    Server(dev, slots=8).run(make_mix(16, seed=99), realtime=False)  # warm plans and kernels
-    mix = make_mix(args.requests)
-    srv = Server(dev, slots=8)
-    done = srv.run(mix)
-    out = {"workload": f"served mix, {args.requests} requests, Poisson 2000/s", "served": summarize(done, srv.makespan)}
-    out["served"]["batches"] = srv.batches
-    k = min(args.requests, 128)
-    plain = run_plain(mix[:k], torch.float64, dev, realtime=False)
-    out[f"plain_fp64_first{k}"] = summarize(plain, max(c.end for c in plain))
-    return out
+    return served_mix(dev, args.requests)
 
 
 def run_kernels_only(args, local):
@@ -803,16 +899,20 @@ def cpu_sample(n, attempts, workers):
     return n * n * r.n_accepted / dt, r, dt
 
 
-def cpu_baseline(args, sample_attempts=None):
+CPU_ATTEMPTS = 16  # attempts per CPU sample (about 2.5 s of the 1024^2 oracle on 16 Arm cores)
+
+
+def cpu_baseline(args):
+    """The oracle on the host cores: one untimed warm-up attempt, then one sample of
+    CPU_ATTEMPTS attempts from t = 0 -- the same sampler and sample length as each step
+    of the reference arm, so both report the same CPU figure."""
     workers = os.cpu_count() or 1
-    # size the sample to ~10-20 s of CPU work
-    v1, r1, d1 = cpu_sample(args.n, 1, workers)
-    att = sample_attempts or max(1, min(40, int(12.0 / max(d1, 1e-3))))
-    v, r, d = cpu_sample(args.n, att, workers)
+    cpu_sample(args.n, 1, workers)
+    v, r, d = cpu_sample(args.n, CPU_ATTEMPTS, workers)
     return {"value": v, "unit": UNIT, "cores": workers, "kind": "port",
-            "sample": f"{r.n_accepted + r.n_rejected} attempts of the same {args.n}^2 solve "
-                      f"({r.n_accepted} accepted, t reached {r.t_final:.3g}) in {d:.1f} s; "
-                      f"NumPy/SciPy FP64 restatement, scipy.fft workers={workers}"}
+            "sample": f"{r.n_accepted + r.n_rejected} attempts of the same {args.n}^2 solve from t=0 "
+                      f"({r.n_accepted} accepted, t reached {r.t_final:.3g}) in {d:.1f} s after a 1-attempt "
+                      f"warm-up; NumPy/SciPy FP64 restatement, scipy.fft workers={workers}"}
 
 
 def run_reference(args, rank, world):
@@ -821,10 +921,9 @@ def run_reference(args, rank, world):
     workers = os.cpu_count() or 1
     for _ in range(max(1, args.warmup)):  # untimed: warms the FFT plans and caches
         cpu_sample(args.n, 1, workers)
-    vals, tot_units, tot_t = [], 0, 0.0
-    att = 8
+    tot_units, tot_t = 0, 0.0
     for _ in range(args.steps):
-        v, r, d = cpu_sample(args.n, att, workers)
+        v, r, d = cpu_sample(args.n, CPU_ATTEMPTS, workers)
         tot_units += args.n * args.n * r.n_accepted
         tot_t += d
     value = tot_units / tot_t
@@ -834,11 +933,11 @@ def run_reference(args, rank, world):
             "data": "synthetic", "impl": "reference",
             "config": {"workload": f"gray-scott IMEX-Strang adaptive {args.n}x{args.n}, "
                                    f"t_span=(0,{T_END:g}), rtol={RTOL}, atol={ATOL}",
-                       "step": f"{att} attempts of the adaptive solve (bounded CPU sample)"},
+                       "step": f"{CPU_ATTEMPTS} attempts of the adaptive solve from t=0 (bounded CPU sample)"},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": workers, "kind": "port",
-                             "sample": f"{att} attempts per step, NumPy/SciPy FP64 restatement of "
-                                       "the reference (JAX is not installed), scipy.fft "
-                                       f"workers={workers}"},
+                             "sample": f"{CPU_ATTEMPTS} attempts per step from t=0, NumPy/SciPy FP64 restatement "
+                                       "of the reference (JAX is not installed here or on the GPU host), "
+                                       f"scipy.fft workers={workers}"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
 

@@ -63,8 +63,24 @@ typedef enum mjx_mult {
 typedef enum mjx_reaction {
   MJX_REACT_NONE = 0,
   MJX_REACT_GRAY_SCOTT = 1, /* u: -uv^2 + F(1-u); v: uv^2 - (F+k)v  (operators.py:644-677) */
-  MJX_REACT_FISHER = 2      /* r u (1-u) on every field          (operators.py:680-705) */
+  MJX_REACT_FISHER = 2,     /* r u (1-u) on every field          (operators.py:680-705) */
+  MJX_REACT_KINETICS = 3    /* a mass-action network (mjx_kinetics): the multispecies reaction
+                               terms of make_reaction_op (operators.py:623-641) in native form */
 } mjx_reaction;
+
+/* Mass-action kinetics of up to 4 species (the fields, in order) and up to 8 reactions:
+ *   dc_s/dt += source[s] + sum_j linear[s][j] c_j + sum_r stoich[r][s] rate[r] prod_q c_q^order[r][q]
+ * First-order networks need only `linear`; a zeroth-order feed goes in `source`. */
+#define MJX_KIN_MAXR 8
+typedef struct mjx_kinetics {
+  int nreactions;        /* 0..8 */
+  int pad;
+  int order[8][4];       /* reactant order of each species in each reaction, 0..3 */
+  double rate[8];        /* rate constant of each reaction */
+  double stoich[8][4];   /* net change of each species per reaction event (products - reactants) */
+  double linear[4][4];   /* first-order rate matrix */
+  double source[4];      /* zeroth-order source of each species */
+} mjx_kinetics;
 
 /* Ghost-cell BC kinds (moljax/core/bc.py:26-30 BCType). */
 typedef enum mjx_bc_kind { MJX_BC_PERIODIC = 0, MJX_BC_DIRICHLET = 1, MJX_BC_NEUMANN = 2 } mjx_bc_kind;
@@ -194,6 +210,25 @@ mjx_status mjx_spectral_filter2d(const void* plan, const mjx_grid2d* grid, int d
 mjx_status mjx_fft_cn2d(const void* plan, const mjx_grid2d* grid, int dtype, double D, double dt,
                         int n_steps, const void* u_in, void* u_out, void* ws, size_t ws_bytes,
                         void* stream);
+
+/* Workspace of mjx_gs_cn_newton2d: the two fields' row spectra, c_old, w and the residual
+ * maxima (nx >= 16). */
+size_t mjx_gs_cn_ws_bytes(int ny, int nx, int dtype);
+/* n_steps Crank-Nicolson steps of periodic Gray-Scott (fields u then v, [2][ny][nx]; D =
+ * {Du, Dv}) solved by the preconditioned Newton iteration of the reference's Gray-Scott
+ * benchmark (benchmarks/benchmark_gray_scott.py:162-228, cn_newton_step_jit): residual
+ * u - u_old - dt/2 (D Lap u + D Lap u_old + R(u) + R(u_old)), update by the exact periodic
+ * inverse of (I - dt/2 D Lap) applied to -res, while max|res_u| + max|res_v| > tol and
+ * fewer than max_iter iterations ran.  The Laplacian is the plan's symbol (the benchmark
+ * uses the pseudo-spectral -(kx^2 + ky^2)).  The Newton loop of each step is a CUDA graph
+ * with a conditional while node (no host synchronisation per iteration or step).  iters
+ * (optional, DEVICE int[n_steps]): Newton iterations per step; iters_total / last_res
+ * (optional, host): their sum and the last residual norm.  y_in may equal y_out.  FP64 is
+ * the benchmark's precision; in FP32 the residual cannot fall below ~1e-7 relative. */
+mjx_status mjx_gs_cn_newton2d(const void* plan, const mjx_grid2d* grid, int dtype, const double* D, double F,
+                              double k, double dt, int n_steps, double tol, int max_iter, const void* y_in,
+                              void* y_out, int* iters, int* iters_total, double* last_res, void* ws,
+                              size_t ws_bytes, void* stream);
 
 /* Size of the fixed device scratch used by mjx_fft_cn2d_noalloc (8 MiB). */
 #define MJX_NOALLOC_SCRATCH_BYTES (8u << 20)
@@ -346,6 +381,13 @@ mjx_status mjx_nk_vardiff_integrate2d(const void* plan2, int n, double dy, doubl
 mjx_status mjx_vardiff_rhs2d(int n, double dy, double dx, const double* model_abc, const double* y,
                              double* out, void* stream);
 
+/* out = a0 v - beta J_F(u) v in FP64: the hand-written Jacobian-vector product of
+ * F(u) = div((a + b u^2) grad u) - c u^3 (homogeneous Dirichlet ghosts), i.e. the JVP of
+ * the residual a0 y + cst - beta F(y) at u (newton_krylov.py:61-80, _jvp_matvec, which
+ * takes it with jax.jvp); a0 = 0, beta = -1 gives J_F(u) v.  u, v, out: n x n FP64. */
+mjx_status mjx_vardiff_jvp2d(int n, double dy, double dx, const double* model_abc, double a0, double beta,
+                             const double* u, const double* v, double* out, void* stream);
+
 /* One implicit step of this model: be_step (moljax/core/stepping.py:170-214), cn_step
  * (217-260) or bdf2_step (263-310, omega = dt/dt_prev, y_prev = y_{n-1}), solved as in
  * mjx_nk_vardiff_integrate2d.  stats (optional): Newton iterations, GMRES iterations,
@@ -396,6 +438,7 @@ typedef struct mjx_explicit_problem {
   double dt_cfl;         /* heisenberg_cfl_dt (moljax/core/dt_policy.py:104-175), host-computed */
   int max_attempts;      /* <= 0 -> 20 * max_steps + 1000 */
   int pad;
+  mjx_kinetics kin;      /* the network when reaction == MJX_REACT_KINETICS */
 } mjx_explicit_problem;
 
 /* Workspace of the explicit steppers: 7 state-sized buffers plus partials and the state. */
@@ -452,8 +495,12 @@ mjx_status mjx_dct2(const void* plan, int n, long long nrows, int dtype, int mod
 
 /* ---- 1D tubular reactor, Crank-Nicolson, batched --------------------------------- */
 typedef enum mjx_reactor_variant {
-  MJX_REACTOR_DANCKWERTS = 0, /* benchmarks/benchmark_reactor_vs_diffrax.py:40-138 */
-  MJX_REACTOR_DIRICHLET = 1   /* benchmarks/benchmark_method_comparison.py:56-160 */
+  MJX_REACTOR_DANCKWERTS = 0, /* benchmarks/benchmark_reactor_vs_diffrax.py:40-138 (dispersion CN,
+                                 upwind advection and reaction explicit: needs dt <= dz) */
+  MJX_REACTOR_DIRICHLET = 1,  /* benchmarks/benchmark_method_comparison.py:56-160 */
+  MJX_REACTOR_DANCKWERTS_CN = 2 /* the Danckwerts discretisation of variant 0 advanced by the fully
+                                   implicit CN of benchmark_method_comparison.py:134-160 (stable at
+                                   its CN step dt = min(10 dz, 0.05, t_final/100), line 216) */
 } mjx_reactor_variant;
 
 /* One reactor solve of c_t = c_zz/Pe - c_z - Da c: n points, n_steps fixed CN
@@ -557,6 +604,27 @@ mjx_status mjx_imex_adaptive2d_mixed(const void* plan32, const void* plan64, con
                                      int max_steps, int save_every, const void* y0, void* y_final,
                                      double* hist_t, double* hist_dt, void* ws, size_t ws_bytes,
                                      mjx_adaptive_result* result, void* stream);
+
+/* Persistent plan of the mixed-precision adaptive loop for one problem: the attempt
+ * kernels and controller of mjx_imex_adaptive2d_mixed captured ONCE into a CUDA graph
+ * with a conditional while node and instantiated; every mjx_imex_plan_run replays it
+ * (no graph capture, instantiation or device allocation per call).  The plan owns the
+ * graph; the caller owns ws (mjx_imex_plan_ws_bytes: the mixed workspace plus the t/dt
+ * history of max_saves = max_steps / save_every + 1 steps) and the FP32/FP64 grid plans,
+ * which must outlive the plan.  The grid, problem, PID settings, max_steps and save_every
+ * are fixed at creation; t0, t_end, dt0 and the state vary per run.  Runs of one plan
+ * must not overlap (they share ws).  The steady loop of adaptive_integrate_imex
+ * (moljax/core/stepping.py:1146-1371) as a reusable object; JAX re-traces per shape. */
+size_t mjx_imex_plan_ws_bytes(int ny, int nx, int nfields, int max_saves);
+mjx_status mjx_imex_plan_create(void** plan, const void* plan32, const void* plan64, const mjx_grid2d* grid,
+                                const mjx_imex_problem* prob, const mjx_pid_params* pid, int max_steps,
+                                int save_every, void* ws, size_t ws_bytes);
+/* One adaptive solve from y0 ([nfields][ny][nx], io_dtype) to y_final; hist_t/hist_dt
+ * (optional, device or host arrays of max_saves doubles) receive the t/dt history. */
+mjx_status mjx_imex_plan_run(void* plan, int io_dtype, double t0, double t_end, double dt0, const void* y0,
+                             void* y_final, double* hist_t, double* hist_dt, mjx_adaptive_result* result,
+                             void* stream);
+mjx_status mjx_imex_plan_destroy(void* plan);
 
 /* Launches a single kernel of one mixed-precision attempt (timing/profiling):
  * which = 0 seeds the workspace from the FP32 state y with step dt; 1..6 launch

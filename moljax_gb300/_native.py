@@ -28,7 +28,7 @@ F32, F64 = 0, 1
 SYMBOL_FD, SYMBOL_SPECTRAL = 0, 1
 MULT_SCALE, MULT_HELMHOLTZ, MULT_CN, MULT_EXP, MULT_LAP = 0, 1, 2, 3, 5
 MULT_ADV_SOLVE, MULT_ADV_LAP, MULT_ADV_EXP, MULT_TABLE = 16, 17, 18, 19
-REACT_NONE, REACT_GRAY_SCOTT, REACT_FISHER = 0, 1, 2
+REACT_NONE, REACT_GRAY_SCOTT, REACT_FISHER, REACT_KINETICS = 0, 1, 2, 3
 SYMBOL_X_ONLY = 0x10
 ETD_1, ETD_2, ETD_RK4 = 1, 2, 4
 ETD_COEFF_CONTOUR, ETD_COEFF_PHI = 0, 1
@@ -73,12 +73,18 @@ class ReactorInstanceC(C.Structure):
                 ("dt", C.c_double), ("c_init", C.c_double), ("c_inlet", C.c_double)]
 
 
+class KineticsC(C.Structure):
+    _fields_ = [("nreactions", C.c_int), ("pad", C.c_int), ("order", (C.c_int * 4) * 8),
+                ("rate", C.c_double * 8), ("stoich", (C.c_double * 4) * 8), ("linear", (C.c_double * 4) * 4),
+                ("source", C.c_double * 4)]
+
+
 class ExplicitProblemC(C.Structure):
     _fields_ = [("reaction", C.c_int), ("nfields", C.c_int), ("D", C.c_double * 4),
                 ("F", C.c_double), ("k", C.c_double), ("r", C.c_double), ("vx", C.c_double),
                 ("vy", C.c_double), ("advection", C.c_int), ("method", C.c_int),
                 ("bc_kind", C.c_int * 4), ("bc_values", C.c_double * 16), ("dt_cfl", C.c_double),
-                ("max_attempts", C.c_int), ("pad", C.c_int)]
+                ("max_attempts", C.c_int), ("pad", C.c_int), ("kin", KineticsC)]
 
 
 class AdaptiveResultC(C.Structure):
@@ -112,6 +118,9 @@ SIGNATURES = {
                                  _sz, _vp]),
     "mjx_fft_cn2d": (_i, [_vp, C.POINTER(Grid2DC), _i, _d, _d, _i, _vp, _vp, _vp, _sz, _vp]),
     "mjx_fft_cn2d_noalloc": (_i, [_vp, C.POINTER(Grid2DC), _i, _d, _d, _i, _vp, _vp, _vp]),
+    "mjx_gs_cn_ws_bytes": (_sz, [_i, _i, _i]),
+    "mjx_gs_cn_newton2d": (_i, [_vp, C.POINTER(Grid2DC), _i, C.POINTER(C.c_double), _d, _d, _d, _i, _d, _i, _vp,
+                                _vp, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_double), _vp, _sz, _vp]),
     "mjx_bc_pad2d": (_i, [_vp, _vp, _i, _i, _i, _i, _vp, _vp, _d, _d, _i, _vp]),
     "mjx_bc_fill2d": (_i, [_vp, _vp, _i, _i, _i, _i, _vp, _vp, _d, _d, _i, _vp]),
     "mjx_unpad2d": (_i, [_vp, _vp, _i, _i, _i, _i, _i, _vp]),
@@ -136,6 +145,7 @@ SIGNATURES = {
                                         C.POINTER(NKParamsC), _vp, _vp, C.POINTER(C.c_int), _vp, _sz,
                                         _vp]),
     "mjx_vardiff_rhs2d": (_i, [_i, _d, _d, C.POINTER(C.c_double), _vp, _vp, _vp]),
+    "mjx_vardiff_jvp2d": (_i, [_i, _d, _d, C.POINTER(C.c_double), _d, _d, _vp, _vp, _vp, _vp]),
     "mjx_nk_vardiff_step2d": (_i, [_vp, _i, _d, _d, C.POINTER(C.c_double), _i, _d, _d, _i,
                                    C.POINTER(NKParamsC), _vp, _vp, _vp, C.POINTER(C.c_int),
                                    C.POINTER(C.c_double), _vp, _sz, _vp]),
@@ -193,6 +203,12 @@ SIGNATURES = {
                                              C.POINTER(PIDParamsC), _i, _d, _vp, _vp, _sz, _vp]),
     "mjx_imex_attempt_kernel2d": (_i, [_vp, C.POINTER(Grid2DC), _i, C.POINTER(ImexProblemC),
                                        C.POINTER(PIDParamsC), _i, _d, _vp, _vp, _sz, _vp]),
+    "mjx_imex_plan_ws_bytes": (_sz, [_i, _i, _i, _i]),
+    "mjx_imex_plan_create": (_i, [C.POINTER(C.c_void_p), _vp, _vp, C.POINTER(Grid2DC), C.POINTER(ImexProblemC),
+                                  C.POINTER(PIDParamsC), _i, _i, _vp, _sz]),
+    "mjx_imex_plan_run": (_i, [_vp, _i, _d, _d, _d, _vp, _vp, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                               C.POINTER(AdaptiveResultC), _vp]),
+    "mjx_imex_plan_destroy": (_i, [_vp]),
     "mjx_gsbatch_bytes": (_sz, [_i, _i]),
     "mjx_gsbatch_instance_bytes": (_sz, [_i, _i, _i]),
     "mjx_gsbatch_work_items": (_i, [_i, _i]),

@@ -78,3 +78,5 @@ from moljax_gb300.core.fft_operators import FFTLinearOperator
 from moljax_gb300.core.fft_integrators import ETDStepResult
 from moljax_gb300.core import batch
 from moljax_gb300.core.batch import GrayScottBatch, GrayScottProblem, adaptive_integrate_imex_batch
+from moljax_gb300.core.fft_solvers import gray_scott_cn_newton
+from moljax_gb300.core.operators import make_kinetics_op

@@ -463,6 +463,37 @@ def fft_cn_step(u0: torch.Tensor, D: float, dx: float, dt: float, n_steps: int =
     return out
 
 
+def gray_scott_cn_newton(u0: torch.Tensor, v0: torch.Tensor, Du: float, Dv: float, F: float, k: float,
+                         dt: float, n_steps: int, dx: float, dy: Optional[float] = None, tol: float = 1e-8,
+                         max_iter: int = 10, symbol: str = "spectral"):
+    """Crank-Nicolson Gray-Scott steps solved by the preconditioned Newton iteration of
+    benchmarks/benchmark_gray_scott.py:162-228 (cn_newton_step_jit / cn_solve_jit):
+    residual of the CN step, the exact periodic inverse of (I - dt/2 D Lap) as the
+    preconditioner, while max|res_u| + max|res_v| > tol and fewer than max_iter
+    iterations ran.  The Newton loop of every step runs on the device
+    (``mjx_gs_cn_newton2d``); pseudo-spectral Laplacian by default, as the benchmark.
+    Returns (u, v, per-step Newton iteration counts)."""
+    u0 = u0.contiguous()
+    N.require_cuda(u0, v0)
+    ny, nx = u0.shape
+    dy = dx if dy is None else dy
+    plan = get_plan(ny, nx, dy, dx, symbol, u0.dtype, u0.device)
+    if getattr(plan, "general", False):
+        raise NotImplementedError("gray_scott_cn_newton needs a power-of-two grid")
+    y = torch.stack([u0, v0.to(u0.dtype)]).contiguous()
+    out = torch.empty_like(y)
+    iters = torch.zeros(max(int(n_steps), 1), dtype=torch.int32, device=u0.device)
+    lib = N.lib()
+    ws = workspace(lib.mjx_gs_cn_ws_bytes(ny, nx, plan.code), plan.device, "gs_cn")
+    D = (C.c_double * 2)(float(Du), float(Dv))
+    tot, last = C.c_int(0), C.c_double(0.0)
+    N.check("mjx_gs_cn_newton2d", lib.mjx_gs_cn_newton2d(
+        N.ptr(plan.buf), C.byref(plan.cgrid), plan.code, D, float(F), float(k), float(dt), int(n_steps),
+        float(tol), int(max_iter), N.ptr(y), N.ptr(out), C.cast(C.c_void_p(iters.data_ptr()), C.POINTER(C.c_int)),
+        C.byref(tot), C.byref(last), N.ptr(ws), ws.numel(), N.stream_ptr(plan.device)))
+    return out[0], out[1], iters[:int(n_steps)]
+
+
 # ----------------------------------------------------------------- periodic 3D boxes
 class SpectralPlan3D:
     """Device tables of one periodic [nz][ny][nx] box (benchmarks/sisc/bench_3d_feasibility.py)."""

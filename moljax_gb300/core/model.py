@@ -154,11 +154,14 @@ def create_fisher_kpp_model(grid: Grid2D, D: float = 0.01, r: float = 1.0,
 def create_advection_diffusion_model(grid: Grid2D, field_names=("c1", "c2"), D: float = 0.01,
                                      vx: float = 1.0, vy: float = 0.0,
                                      bc_type: BCType = BCType.PERIODIC, use_upwind: bool = True,
-                                     dtype: torch.dtype = torch.float64) -> MOLModel:
+                                     dtype: torch.dtype = torch.float64,
+                                     reactions: Optional[NonlinearOp] = None) -> MOLModel:
     """dc_i/dt = D Lap(c_i) - vx dc_i/dx - vy dc_i/dy (moljax/core/model.py:295-370).
 
     The operator is one linear op, as in the reference (upwind d1_upwind_2d or
     central differences); the explicit steppers evaluate it in fused native kernels.
+    ``reactions`` (an extension of the reference signature): a native reaction op of the
+    species, e.g. ``make_kinetics_op``, added to the model's nonlinear ops.
     """
     names = list(field_names)
     bc_spec = {n: FieldBCSpec(kind=bc_type) for n in names}
@@ -172,7 +175,9 @@ def create_advection_diffusion_model(grid: Grid2D, field_names=("c1", "c2"), D: 
         return min(g.min_dx / (vmax + 1e-14), 0.25 * g.min_dx2 / (p["D"] + 1e-14))
 
     op = LinearOp("advection_diffusion", advdiff_apply, advdiff_dt_bound, "advection_diffusion")
-    return MOLModel(grid, bc_spec, params, (op,), (),
+    if reactions is not None and reactions.native is not None and list(reactions.native[0]) != names:
+        raise ValueError("the reaction network's species must be the model's fields, in order")
+    return MOLModel(grid, bc_spec, params, (op,), (reactions,) if reactions is not None else (),
                     {"field_names": names, "pde_type": "advection_diffusion",
                      "advection": 1 if use_upwind else 2,
                      "diffusivities": {n: D for n in names}})
@@ -257,6 +262,24 @@ def _vardiff_rhs_raw(state, grid, params):
     padded = torch.zeros_like(u, dtype=torch.float64)
     padded[grid.interior_slice] = out
     return {"u": padded.to(u.dtype)}
+
+
+def vardiff_jvp(model: MOLModel, u, v, a0: float = 0.0, beta: float = -1.0):
+    """a0 v - beta J_F(u) v for the variable-diffusion model, with the hand-written native
+    JVP (``mjx_vardiff_jvp2d``): J_F(u) v by default, the JVP of an implicit residual
+    a0 y + cst - beta F(y) otherwise (moljax/core/newton_krylov.py:61-80 takes it with
+    jax.jvp).  u, v: interior (n, n) tensors; FP64 result."""
+    import ctypes as C
+    grid = model.grid
+    N.require_cuda(u, v)
+    u64, v64 = u.to(torch.float64).contiguous(), v.to(torch.float64).contiguous()
+    out = torch.empty_like(u64)
+    a, b, c = model.metadata["abc"]
+    abc = (C.c_double * 3)(a, b, c)
+    N.check("mjx_vardiff_jvp2d", N.lib().mjx_vardiff_jvp2d(
+        grid.nx, float(grid.dy), float(grid.dx), abc, float(a0), float(beta), N.ptr(u64), N.ptr(v64), N.ptr(out),
+        N.stream_ptr(u.device)))
+    return out
 
 
 def _vardiff_rhs(model: MOLModel, state):

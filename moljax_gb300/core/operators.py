@@ -33,6 +33,7 @@ class NonlinearOp:
     apply: Callable
     dt_bound: Optional[Callable] = None
     kind: Optional[int] = None  # native reaction id (MJX_REACT_*)
+    native: Any = None          # the native description (MJX_REACT_KINETICS: (species, KineticsC))
 
 
 def laplacian_2d(f, grid: Grid2D):
@@ -241,6 +242,63 @@ def make_reaction_op(reactions) -> NonlinearOp:
         return out
 
     return NonlinearOp("reactions", apply, None, None)
+
+
+def make_kinetics_op(species, reactions=(), linear=None, source=None) -> NonlinearOp:
+    """A mass-action reaction network over the named species (at most 4, the model's
+    fields in order, at most 8 reactions) in native form: the multispecies reaction
+    terms that make_reaction_op (operators.py:623-641) takes as Python callables, here
+    evaluated inside the fused stencil stage kernels (``MJX_REACT_KINETICS``).
+
+    reactions: (rate, reactants, products) with reactants {species: order (1..3)} and
+    products {species: count}; rate * prod c^order is the reaction's rate.
+    linear: {(target, species): k}, the first-order terms dc_target/dt += k c_species.
+    source: {species: s}, zeroth-order feeds.
+    ``apply`` evaluates the same rates with torch (the generic paths)."""
+    from moljax_gb300 import _native as N
+    names = list(species)
+    if not 1 <= len(names) <= 4:
+        raise ValueError("a native network takes 1 to 4 species")
+    reactions = [(float(r), dict(a), dict(b)) for r, a, b in reactions]
+    if len(reactions) > 8:
+        raise ValueError("a native network takes at most 8 reactions")
+    idx = {n: i for i, n in enumerate(names)}
+    kin = N.KineticsC()
+    kin.nreactions = len(reactions)
+    for r, (rate, reac, prod) in enumerate(reactions):
+        kin.rate[r] = rate
+        for n, o in reac.items():
+            if int(o) != o or not 1 <= o <= 3:
+                raise ValueError("reactant orders are 1, 2 or 3")
+            kin.order[r][idx[n]] = int(o)
+            kin.stoich[r][idx[n]] -= float(o)
+        for n, c in prod.items():
+            kin.stoich[r][idx[n]] += float(c)
+    for (t, sname), kv in (linear or {}).items():
+        kin.linear[idx[t]][idx[sname]] = float(kv)
+    for n, v in (source or {}).items():
+        kin.source[idx[n]] = float(v)
+
+    def apply(state, grid, t, params):
+        c = [state[n] for n in names]
+        out = state_zero_like(state)
+        for i, n in enumerate(names):
+            acc = torch.zeros_like(c[i]) + kin.source[i]
+            for j in range(len(names)):
+                if kin.linear[i][j] != 0.0:
+                    acc = acc + kin.linear[i][j] * c[j]
+            out[n] = acc
+        for r in range(kin.nreactions):
+            w = kin.rate[r]
+            for j in range(len(names)):
+                for _ in range(kin.order[r][j]):
+                    w = w * c[j]
+            for i, n in enumerate(names):
+                if kin.stoich[r][i] != 0.0:
+                    out[n] = out[n] + kin.stoich[r][i] * w
+        return out
+
+    return NonlinearOp("kinetics", apply, None, N.REACT_KINETICS, (names, kin))
 
 
 def fd_laplacian_symbol_1d(nx: int, dx: float, dtype=None):

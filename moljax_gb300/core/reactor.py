@@ -17,7 +17,7 @@ import torch
 
 from moljax_gb300 import _native as N
 
-DANCKWERTS, DIRICHLET = 0, 1
+DANCKWERTS, DIRICHLET, DANCKWERTS_CN = 0, 1, 2
 
 
 @dataclass

@@ -330,29 +330,88 @@ def _adaptive_imex_general(model, interior, plan, diffusivities, use_strang, t0,
     return AdaptiveResult(t, y_fin, t_hist, y_history, dt_hist, write_idx, n_acc, n_rej, status)
 
 
+class ImexPlan:
+    """Persistent native plan of the mixed-precision adaptive IMEX-Strang loop
+    (``mjx_imex_plan_*``): the attempt kernels and controller are captured once into a
+    CUDA graph with a conditional while node and every ``run`` replays it, with no
+    capture, instantiation or allocation per solve.  Fixed at creation: the grid, the
+    native problem (reaction, D, F, k, CFL limit), the PID settings, max_steps and
+    save_every; ``run`` takes the state and t0, t_end, dt0.  Runs of one plan must not
+    overlap (one thread, one stream at a time)."""
+
+    def __init__(self, grid_plan, prob, pid_params, max_steps: int, save_every: int, nfields: int):
+        from moljax_gb300.core.fft_solvers import get_plan
+        p = grid_plan
+        self.p32 = get_plan(p.ny, p.nx, p.dy, p.dx, p.symbol, torch.float32, p.device)
+        self.p64 = get_plan(p.ny, p.nx, p.dy, p.dx, p.symbol, torch.float64, p.device)
+        self.device = p.device
+        self.max_saves = max_steps // save_every + 1
+        lib = N.lib()
+        nbytes = lib.mjx_imex_plan_ws_bytes(p.ny, p.nx, nfields, self.max_saves)
+        self.ws = torch.empty(nbytes, dtype=torch.uint8, device=self.device)
+        self._prob, self._pid = prob, _pid_c(pid_params)
+        h = C.c_void_p()
+        with torch.cuda.device(self.device):
+            N.check("mjx_imex_plan_create", lib.mjx_imex_plan_create(
+                C.byref(h), N.ptr(self.p32.buf), N.ptr(self.p64.buf), C.byref(self.p32.cgrid), C.byref(prob),
+                C.byref(self._pid), int(max_steps), int(save_every), N.ptr(self.ws), nbytes))
+        self._h = h
+
+    def run(self, interior, t0: float, t_end: float, dt0: float):
+        """(y_final interior, t history, dt history, native result) of one solve."""
+        y_final = torch.empty_like(interior)
+        t_hist = torch.empty(self.max_saves, dtype=torch.float64, device=self.device)
+        dt_hist = torch.empty(self.max_saves, dtype=torch.float64, device=self.device)
+        res = N.AdaptiveResultC()
+        dp = C.POINTER(C.c_double)
+        N.check("mjx_imex_plan_run", N.lib().mjx_imex_plan_run(
+            self._h, N.dtype_code(interior.dtype), float(t0), float(t_end), float(dt0), N.ptr(interior),
+            N.ptr(y_final), C.cast(C.c_void_p(t_hist.data_ptr()), dp), C.cast(C.c_void_p(dt_hist.data_ptr()), dp),
+            C.byref(res), N.stream_ptr(self.device)))
+        return y_final, t_hist, dt_hist, res
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            N.lib().mjx_imex_plan_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:  # noqa: BLE001 - interpreter shutdown
+            pass
+
+
+_imex_plans: "OrderedDict" = None
+_IMEX_PLAN_CACHE = 16  # plans kept per process (least recently used dropped first)
+
+
+def _cached_imex_plan(grid_plan, prob, pid_params, max_steps, save_every, nfields):
+    """The persistent plan for this problem (one per host thread: runs must not overlap)."""
+    global _imex_plans
+    import threading
+    from collections import OrderedDict
+    if _imex_plans is None:
+        _imex_plans = OrderedDict()
+    key = (threading.get_ident(), str(grid_plan.device), grid_plan.ny, grid_plan.nx, grid_plan.dy, grid_plan.dx,
+           grid_plan.symbol, nfields, bytes(prob), bytes(_pid_c(pid_params)), int(max_steps), int(save_every))
+    plan = _imex_plans.get(key)
+    if plan is None:
+        plan = ImexPlan(grid_plan, prob, pid_params, max_steps, save_every, nfields)
+        _imex_plans[key] = plan
+        while len(_imex_plans) > _IMEX_PLAN_CACHE:
+            _imex_plans.popitem(last=False)[1].close()
+    else:
+        _imex_plans.move_to_end(key)
+    return plan
+
+
 def _adaptive_mixed(model, interior, plan, prob, pid_params, t0, t_end, dt0, max_steps,
                     save_every) -> AdaptiveResult:
-    from moljax_gb300.core.fft_solvers import get_plan
     grid = model.grid
     names = model.field_names
-    p32 = get_plan(plan.ny, plan.nx, plan.dy, plan.dx, plan.symbol, torch.float32, plan.device)
-    p64 = get_plan(plan.ny, plan.nx, plan.dy, plan.dx, plan.symbol, torch.float64, plan.device)
-    pid = _pid_c(pid_params)
-    lib = N.lib()
-    dev = plan.device
-    max_saves = max_steps // save_every + 1
-    ws = workspace(lib.mjx_imex2d_mixed_ws_bytes(grid.ny, grid.nx, len(names)), dev, "imex_mixed")
-    y_final = torch.empty_like(interior)
-    t_hist = torch.empty(max_saves, dtype=torch.float64, device=dev)
-    dt_hist = torch.empty(max_saves, dtype=torch.float64, device=dev)
-    res = N.AdaptiveResultC()
-    N.check("mjx_imex_adaptive2d_mixed", lib.mjx_imex_adaptive2d_mixed(
-        N.ptr(p32.buf), N.ptr(p64.buf), C.byref(p32.cgrid), N.dtype_code(interior.dtype),
-        C.byref(prob), C.byref(pid), float(t0), float(t_end), float(dt0), int(max_steps),
-        int(save_every), N.ptr(interior), N.ptr(y_final),
-        C.cast(C.c_void_p(t_hist.data_ptr()), C.POINTER(C.c_double)),
-        C.cast(C.c_void_p(dt_hist.data_ptr()), C.POINTER(C.c_double)),
-        N.ptr(ws), ws.numel(), C.byref(res), N.stream_ptr(dev)))
+    ip = _cached_imex_plan(plan, prob, pid_params, max_steps, save_every, len(names))
+    y_final, t_hist, dt_hist, res = ip.run(interior, t0, t_end, dt0)
     padded = stencil.pad_interior(y_final, grid, model.bc_spec, names, res.t_final, model.params)
     y_fin = {n: padded[i] for i, n in enumerate(names)}
     return AdaptiveResult(res.t_final, y_fin, t_hist, None, dt_hist, res.n_saved, res.n_accepted,
@@ -390,6 +449,8 @@ def explicit_problem(model, method: int = 2, cfl_params: Optional[CFLParams] = N
     p.vx = float(model.params.get("vx", 0.0)) if p.advection else 0.0
     p.vy = float(model.params.get("vy", 0.0)) if p.advection else 0.0
     p.method = int(method)
+    if p.reaction == N.REACT_KINETICS:
+        p.kin = model.nonlinear_ops[0].native[1]
     p.dt_cfl = heisenberg_cfl_dt(model.grid, model.params, cfl_params or CFLParams())
     p.max_attempts = int(max_attempts)
     return p

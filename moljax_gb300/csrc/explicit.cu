@@ -42,7 +42,47 @@ struct XModel {
   double bv[4][4];  // per field: left, right, bottom, top
   double D[4];
   double F, k, r, vx, vy, dy, dx;
+  mjx_kinetics kin;  // MJX_REACT_KINETICS
 };
+
+// A mass-action network in the state type.
+template <typename T>
+struct XKin {
+  int nr;
+  int order[MJX_KIN_MAXR][4];
+  T rate[MJX_KIN_MAXR];
+  T stoich[MJX_KIN_MAXR][4];
+  T linear[4][4];
+  T source[4];
+};
+
+// Adds the network's rates at concentrations c (NF fields, nf used) to Fv.
+template <typename T, int NF>
+__device__ __forceinline__ void kinetics_add(T* Fv, const T* c, int nf, const XKin<T>& q) {
+#pragma unroll
+  for (int s = 0; s < NF; ++s) {
+    if (s >= nf) break;
+    T acc = q.source[s];
+#pragma unroll
+    for (int j = 0; j < NF; ++j)
+      if (j < nf) acc += q.linear[s][j] * c[j];
+    Fv[s] += acc;
+  }
+  for (int r = 0; r < q.nr; ++r) {
+    T w = q.rate[r];
+#pragma unroll
+    for (int j = 0; j < NF; ++j) {
+      if (j >= nf) break;
+      const int o = q.order[r][j];
+      if (o >= 1) w *= c[j];
+      if (o >= 2) w *= c[j];
+      if (o >= 3) w *= c[j];
+    }
+#pragma unroll
+    for (int s = 0; s < NF; ++s)
+      if (s < nf) Fv[s] += q.stoich[r][s] * w;
+  }
+}
 
 // The coefficients of a stage in the state type, converted on the host: FP64 arithmetic
 // is rare on this part, so an FP32 stage kernel performs none per point.
@@ -55,6 +95,7 @@ struct XCoef {
   T cp1, cq1, cf1, cp2, cq2, cf2, hfac, hfixed;  // hfixed = fixed h * hfac
   T atol, rtol;
   int vxpos, vypos;
+  XKin<T> kin;
 };
 
 template <typename T>
@@ -214,6 +255,8 @@ __global__ void __launch_bounds__(256, sizeof(T) == 8 ? 2 : (NF == 4 ? 3 : 4)) r
           if (f >= nf) break;
           Fv[f] += rr * c[f] * ((T)1 - c[f]);
         }
+      } else if (RX == RX_KINETICS) {
+        kinetics_add<T, NF>(Fv, c, nf, k.kin);
       }
       if (x < nx) {
 #pragma unroll
@@ -301,7 +344,13 @@ static mjx_status x_model(const mjx_explicit_problem* pb, const mjx_grid2d* g, X
   if (pb == nullptr || g == nullptr) return MJX_BAD_ARG;
   if (pb->nfields < 1 || pb->nfields > 4 || g->ny < 1 || g->nx < 1 || !(g->dx > 0) || !(g->dy > 0))
     return MJX_BAD_SHAPE;
-  if (pb->reaction < MJX_REACT_NONE || pb->reaction > MJX_REACT_FISHER) return MJX_BAD_ARG;
+  if (pb->reaction < MJX_REACT_NONE || pb->reaction > MJX_REACT_KINETICS) return MJX_BAD_ARG;
+  if (pb->reaction == MJX_REACT_KINETICS) {
+    if (pb->kin.nreactions < 0 || pb->kin.nreactions > MJX_KIN_MAXR) return MJX_BAD_ARG;
+    for (int r = 0; r < pb->kin.nreactions; ++r)
+      for (int j = 0; j < 4; ++j)
+        if (pb->kin.order[r][j] < 0 || pb->kin.order[r][j] > 3) return MJX_BAD_ARG;
+  }
   if (pb->reaction == MJX_REACT_GRAY_SCOTT && pb->nfields != 2) return MJX_BAD_ARG;
   if (pb->advection < 0 || pb->advection > 2) return MJX_BAD_ARG;
   if (pb->method < 0 || pb->method > 2) return MJX_BAD_ARG;
@@ -316,7 +365,18 @@ static mjx_status x_model(const mjx_explicit_problem* pb, const mjx_grid2d* g, X
   }
   m->F = pb->F; m->k = pb->k; m->r = pb->r; m->vx = pb->vx; m->vy = pb->vy;
   m->dy = g->dy; m->dx = g->dx;
+  if (pb->reaction == MJX_REACT_KINETICS) m->kin = pb->kin;
   return MJX_OK;
+}
+
+// compile-time reaction kind of an mjx_reaction
+static int rx_of(int reaction) {
+  switch (reaction) {
+    case MJX_REACT_GRAY_SCOTT: return RX_GRAY_SCOTT;
+    case MJX_REACT_FISHER: return RX_FISHER;
+    case MJX_REACT_KINETICS: return RX_KINETICS;
+    default: return RX_NONE;
+  }
 }
 
 template <typename T>
@@ -365,7 +425,7 @@ static XAttempt<T> build_x(const XModel& m, int method, char* ws, const XLayout&
   base.st = st;
   base.atol = atol; base.rtol = rtol;
   base.partial = (double*)(ws + L.part); base.nonfinite = (int*)(ws + L.bad);
-  A.rx = m.reaction == MJX_REACT_GRAY_SCOTT ? RX_GRAY_SCOTT : (m.reaction == MJX_REACT_FISHER ? RX_FISHER : RX_NONE);
+  A.rx = rx_of(m.reaction);
   // estimate_error_doubling: full step -> YF; half steps -> YH -> Y[1-cur] (+ error)
   add_step(A, base, method, XB_YCUR, XB_YF, 1.0, 0);
   add_step(A, base, method, XB_YCUR, XB_YH, 0.5, 0);
@@ -532,6 +592,13 @@ rk_stage_vec_kernel(const __grid_constant__ XStage<T> a) {
             if (f >= nf) break;
             Fv[f][q] += rr * c[f][q] * ((T)1 - c[f][q]);
           }
+        } else if (RX == RX_KINETICS) {
+          T cq[NF], fq[NF];
+#pragma unroll
+          for (int f = 0; f < NF; ++f) { cq[f] = c[f][q]; fq[f] = Fv[f][q]; }
+          kinetics_add<T, NF>(fq, cq, nf, k.kin);
+#pragma unroll
+          for (int f = 0; f < NF; ++f) Fv[f][q] = fq[f];
         }
       }
       if (valid) {
@@ -608,6 +675,17 @@ static void x_coef(XStage<T>& s) {
   k.cp2 = (T)s.cp2; k.cq2 = (T)s.cq2; k.cf2 = (T)s.cf2;
   k.hfac = (T)s.hfac; k.hfixed = (T)(s.hfixed * s.hfac);
   k.atol = (T)s.atol; k.rtol = (T)s.rtol;
+  if (m.reaction == MJX_REACT_KINETICS) {
+    k.kin.nr = m.kin.nreactions;
+    for (int r = 0; r < MJX_KIN_MAXR; ++r) {
+      k.kin.rate[r] = (T)m.kin.rate[r];
+      for (int j = 0; j < 4; ++j) { k.kin.order[r][j] = m.kin.order[r][j]; k.kin.stoich[r][j] = (T)m.kin.stoich[r][j]; }
+    }
+    for (int i = 0; i < 4; ++i) {
+      k.kin.source[i] = (T)m.kin.source[i];
+      for (int j = 0; j < 4; ++j) k.kin.linear[i][j] = (T)m.kin.linear[i][j];
+    }
+  }
 }
 
 template <typename T>
@@ -637,9 +715,11 @@ static cudaError_t launch_stage(const XStage<T>& s0, int rx, cudaStream_t st) {
     if (rx == RX_GRAY_SCOTT) rk_stage_vec_kernel<T, RX_GRAY_SCOTT, 2><<<vblocks, blk, 0, st>>>(s);
     else if (s.m.nf <= 2) {
       if (rx == RX_FISHER) rk_stage_vec_kernel<T, RX_FISHER, 2><<<vblocks, blk, 0, st>>>(s);
+      else if (rx == RX_KINETICS) rk_stage_vec_kernel<T, RX_KINETICS, 2><<<vblocks, blk, 0, st>>>(s);
       else rk_stage_vec_kernel<T, RX_NONE, 2><<<vblocks, blk, 0, st>>>(s);
     } else {
       if (rx == RX_FISHER) rk_stage_vec_kernel<T, RX_FISHER, 4><<<vblocks, blk, 0, st>>>(s);
+      else if (rx == RX_KINETICS) rk_stage_vec_kernel<T, RX_KINETICS, 4><<<vblocks, blk, 0, st>>>(s);
       else rk_stage_vec_kernel<T, RX_NONE, 4><<<vblocks, blk, 0, st>>>(s);
     }
     return cudaGetLastError();
@@ -647,9 +727,11 @@ static cudaError_t launch_stage(const XStage<T>& s0, int rx, cudaStream_t st) {
   if (rx == RX_GRAY_SCOTT) rk_stage_kernel<T, RX_GRAY_SCOTT, 2><<<blocks, blk, 0, st>>>(s);
   else if (s.m.nf <= 2) {
     if (rx == RX_FISHER) rk_stage_kernel<T, RX_FISHER, 2><<<blocks, blk, 0, st>>>(s);
+    else if (rx == RX_KINETICS) rk_stage_kernel<T, RX_KINETICS, 2><<<blocks, blk, 0, st>>>(s);
     else rk_stage_kernel<T, RX_NONE, 2><<<blocks, blk, 0, st>>>(s);
   } else {
     if (rx == RX_FISHER) rk_stage_kernel<T, RX_FISHER, 4><<<blocks, blk, 0, st>>>(s);
+    else if (rx == RX_KINETICS) rk_stage_kernel<T, RX_KINETICS, 4><<<blocks, blk, 0, st>>>(s);
     else rk_stage_kernel<T, RX_NONE, 4><<<blocks, blk, 0, st>>>(s);
   }
   return cudaGetLastError();
@@ -928,6 +1010,7 @@ static size_t fused_smem(int nst, int nfa) {
 template <typename T>
 static bool fused_ok(const XModel& m, int method) {
   if (method != 1 && method != 2) return false;
+  if (m.reaction == MJX_REACT_KINETICS) return false;  // the stage kernels take the network
   const int nfa = m.nf <= 2 ? 2 : 4;
   return fused_smem<T>(method == 2 ? 4 : 3, nfa) <= 200 * 1024;
 }
@@ -998,7 +1081,7 @@ static mjx_status x_integrate(const XModel& m, int method, double dt, int n_step
   base.m = m;
   for (int i = 0; i < 7; ++i) base.buf[i] = (T*)(ws + L.b[i]);
   base.hfixed = dt;
-  A.rx = m.reaction == MJX_REACT_GRAY_SCOTT ? RX_GRAY_SCOTT : (m.reaction == MJX_REACT_FISHER ? RX_FISHER : RX_NONE);
+  A.rx = rx_of(m.reaction);
   MJX_CUDA_TRY(cudaMemcpyAsync(base.buf[0], y0, nelem * sizeof(T), cudaMemcpyDeviceToDevice, s));
   int src = 0;
   if (fused_ok<T>(m, method)) {  // SSPRK3 / RK4: one kernel per step
@@ -1166,7 +1249,7 @@ mjx_status mjx_explicit_rhs2d(const mjx_grid2d* grid, int dtype, const mjx_expli
   const int e = elem_size(dtype);
   if (!e) return MJX_BAD_DTYPE;
   if (y == nullptr || out == nullptr || y == out) return MJX_BAD_ARG;
-  const int rx = m.reaction == MJX_REACT_GRAY_SCOTT ? RX_GRAY_SCOTT : (m.reaction == MJX_REACT_FISHER ? RX_FISHER : RX_NONE);
+  const int rx = rx_of(m.reaction);
   cudaStream_t s = (cudaStream_t)stream;
   auto run = [&](auto tag) -> cudaError_t {
     typedef decltype(tag) T;
@@ -1223,7 +1306,7 @@ static mjx_status tune_stencil(const XModel& m, char* ws, const XLayout& L, int 
   st.w = XB_W1; st.p = XB_YCUR; st.q = XB_ACC; st.o1 = XB_W2; st.o2 = XB_ACC;
   st.cp1 = 1; st.cf1 = 0.5; st.cq2 = 1; st.cf2 = 1.0 / 3.0;
   st.hfac = 1.0; st.hfixed = 1e-6;
-  const int rx = m.reaction == MJX_REACT_GRAY_SCOTT ? RX_GRAY_SCOTT : (m.reaction == MJX_REACT_FISHER ? RX_FISHER : RX_NONE);
+  const int rx = rx_of(m.reaction);
   cudaEvent_t e0, e1;
   MJX_CUDA_TRY(cudaEventCreate(&e0));
   MJX_CUDA_TRY(cudaEventCreate(&e1));

@@ -414,106 +414,141 @@ size_t mjx_imex2d_mixed_ws_bytes(int ny, int nx, int nfields) {
   return mix_layout(ny, nx, nfields, mix_nparts(ny, nx, nfields)).total;
 }
 
-mjx_status mjx_imex_adaptive2d_mixed(const void* plan32, const void* plan64, const mjx_grid2d* g,
-                                     int io_dtype, const mjx_imex_problem* pb,
-                                     const mjx_pid_params* pid, double t0, double t_end, double dt0,
-                                     int max_steps, int save_every, const void* y0, void* y_final,
-                                     double* hist_t, double* hist_dt, void* ws, size_t ws_bytes,
-                                     mjx_adaptive_result* res, void* stream) {
+}  // extern "C"
+
+namespace mjx {
+
+// The captured adaptive loop of one mixed-precision problem: the workspace layout, the
+// attempt kernels' arguments and the instantiated conditional graph, built once and
+// replayed by every run.  The t/dt history lives in the plan's workspace (after the
+// mixed layout) so the captured controller writes a fixed address.
+struct ImexMixedPlan {
+  const void* plan32;
+  const void* plan64;
+  mjx_grid2d g;
+  mjx_imex_problem pb;
+  mjx_pid_params pid;
+  int max_steps, save_every, max_saves;
+  char* ws;
+  MixLayout L;
+  double* ht = nullptr;     // t/dt history written by the captured controller (may be null)
+  double* hdt = nullptr;
+  bool own_hist = false;    // the history lives in the plan's workspace (copied out per run)
+  cudaStream_t cap = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+};
+
+static size_t plan_hist_offset(const MixLayout& L) { return L.total; }
+
+static void free_mixed_plan(ImexMixedPlan* P) {
+  if (P->exec) cudaGraphExecDestroy(P->exec);
+  if (P->graph) cudaGraphDestroy(P->graph);
+  if (P->cap) cudaStreamDestroy(P->cap);
+  delete P;
+}
+
+static mjx_status check_mixed_problem(const mjx_grid2d* g, const mjx_imex_problem* pb, const mjx_pid_params* pid,
+                                      const void* plan32, const void* plan64, int max_steps, int save_every) {
   MJX_TRY(check_grid(g));
-  if (pb == nullptr || pid == nullptr || plan32 == nullptr || plan64 == nullptr || !y0 || !y_final)
-    return MJX_BAD_ARG;
+  if (pb == nullptr || pid == nullptr || plan32 == nullptr || plan64 == nullptr) return MJX_BAD_ARG;
   if (pb->nfields < 1 || pb->nfields > 4 || !pb->use_strang) return MJX_BAD_ARG;
   if (pb->reaction == MJX_REACT_GRAY_SCOTT && pb->nfields != 2) return MJX_BAD_ARG;
   if (max_steps < 0 || save_every < 1) return MJX_BAD_ARG;
-  const int e = elem_size(io_dtype);
-  if (!e) return MJX_BAD_DTYPE;
-  const int nf = pb->nfields;
-  const MixLayout L = mix_layout(g->ny, g->nx, nf, mix_nparts(g->ny, g->nx, nf));
-  if (ws == nullptr || ws_bytes < L.total) return MJX_WORKSPACE;
-  MJX_TRY(ensure_kernel_attrs());
-  MJX_TRY(ensure_mix_attrs());
-  cudaStream_t s = (cudaStream_t)stream;
-  char* w = (char*)ws;
-  DevState* st = (DevState*)(w + L.st);
-  const long long nelem = (long long)nf * g->ny * g->nx;
-  const int max_saves = max_steps / save_every + 1;
+  return MJX_OK;
+}
 
+// Captures kCondUnroll attempts (each followed by the controller) into the body of a
+// conditional while node and instantiates the graph.
+static mjx_status capture_mixed(ImexMixedPlan& P) {
+  DevState* st = (DevState*)(P.ws + P.L.st);
+  const MixAttempt A = build_mix(P.plan32, &P.g, &P.pb, &P.pid, P.ws, P.L, st);
+  CtlArgs ca;
+  memset(&ca, 0, sizeof(ca));
+  ca.st = st; ca.partial = (const double*)(P.ws + P.L.part); ca.nonfinite = (const int*)(P.ws + P.L.bad);
+  ca.nparts = P.L.nparts; ca.n_dof = (double)P.pb.nfields * P.g.ny * P.g.nx; ca.pid = P.pid;
+  ca.hist_t = P.ht; ca.hist_dt = P.hdt;
+  cudaError_t ce = cudaSuccess;
+  do {
+    if ((ce = cudaStreamCreateWithFlags(&P.cap, cudaStreamNonBlocking)) != cudaSuccess) break;
+    if ((ce = cudaGraphCreate(&P.graph, 0)) != cudaSuccess) break;
+    cudaGraphConditionalHandle hdl;
+    if ((ce = cudaGraphConditionalHandleCreate(&hdl, P.graph, 1, cudaGraphCondAssignDefault)) != cudaSuccess) break;
+    cudaGraphNodeParams np = {cudaGraphNodeTypeConditional};
+    np.conditional.handle = hdl;
+    np.conditional.type = cudaGraphCondTypeWhile;
+    np.conditional.size = 1;
+    cudaGraphNode_t node;
+    if ((ce = cudaGraphAddNode(&node, P.graph, nullptr, nullptr, 0, &np)) != cudaSuccess) break;
+    cudaGraph_t body = np.conditional.phGraph_out[0];
+    if ((ce = cudaStreamBeginCaptureToGraph(P.cap, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) break;
+    ca.handle = hdl; ca.use_handle = 1;
+    // the body holds kCondUnroll attempts (each followed by the controller), so the
+    // conditional node is evaluated once per kCondUnroll attempts; once the
+    // controller marks the solve done, the rest of the body's kernels return at entry
+    cudaError_t le = cudaSuccess;
+    for (int u = 0; u < kCondUnroll && le == cudaSuccess; ++u) {
+      le = launch_mix_attempt(A, P.cap);
+      if (le == cudaSuccess) le = launch_controller(ca, P.cap);
+    }
+    cudaGraph_t captured = nullptr;
+    ce = cudaStreamEndCapture(P.cap, &captured);
+    if (le != cudaSuccess) { ce = le; break; }
+    if (ce != cudaSuccess) break;
+    ce = cudaGraphInstantiate(&P.exec, P.graph, 0);
+  } while (0);
+  if (ce != cudaSuccess) { set_last_error(ce, __FILE__, __LINE__); return MJX_CUDA_ERROR; }
+  return MJX_OK;
+}
+
+static mjx_status run_mixed(ImexMixedPlan& P, int io_dtype, double t0, double t_end, double dt0, const void* y0,
+                            void* y_final, double* hist_t, double* hist_dt, mjx_adaptive_result* res,
+                            cudaStream_t s, bool host_loop) {
+  const int nf = P.pb.nfields;
+  char* w = P.ws;
+  DevState* st = (DevState*)(w + P.L.st);
+  const int max_saves = P.max_saves;
+  double* real64 = (double*)(w + P.L.pa);
+  double* ht = P.ht;
+  double* hdt = P.hdt;
   // initial spectral state in FP64 (real input staged in PA)
-  double* real64 = (double*)(w + L.pa);
-  MJX_TRY(mix_state_from_real(plan64, g, nf, io_dtype, y0, real64, (float4*)(w + L.ys0), s));
-
+  MJX_TRY(mix_state_from_real(P.plan64, &P.g, nf, io_dtype, y0, real64, (float4*)(w + P.L.ys0), s));
   DevState h;
   memset(&h, 0, sizeof(h));
-  const double dt_init = (dt0 < pb->dt_cfl || dt0 != dt0) ? dt0 : pb->dt_cfl;
-  h.t = t0; h.dt = dt_init; h.t_end = t_end; h.prev_err = 1.0; h.dt_cfl = pb->dt_cfl;
+  const double dt_init = (dt0 < P.pb.dt_cfl || dt0 != dt0) ? dt0 : P.pb.dt_cfl;
+  h.t = t0; h.dt = dt_init; h.t_end = t_end; h.prev_err = 1.0; h.dt_cfl = P.pb.dt_cfl;
   h.status = MJX_STATUS_RUNNING_CODE; h.write_idx = 1; h.finite = 1;
-  h.max_saves = max_saves; h.save_every = save_every; h.order = 2; h.save_slot = -1;
-  h.max_attempts = pb->max_attempts > 0 ? pb->max_attempts : 20 * max_steps + 1000;
+  h.max_saves = max_saves; h.save_every = P.save_every; h.order = 2; h.save_slot = -1;
+  h.max_attempts = P.pb.max_attempts > 0 ? P.pb.max_attempts : 20 * P.max_steps + 1000;
   const bool running = (t0 < t_end) && (1 < max_saves);
   if (running) h.dtc = dt_init < t_end - t0 ? dt_init : t_end - t0;
   else { h.done = 1; h.status = (t0 >= t_end) ? MJX_STATUS_SUCCESS_CODE : MJX_STATUS_MAX_STEPS_CODE; }
   MJX_CUDA_TRY(cudaMemcpyAsync(st, &h, sizeof(h), cudaMemcpyHostToDevice, s));
-  if (hist_t) {
-    MJX_CUDA_TRY(cudaMemsetAsync(hist_t, 0, sizeof(double) * max_saves, s));
-    MJX_CUDA_TRY(cudaMemcpyAsync(hist_t, &t0, sizeof(double), cudaMemcpyHostToDevice, s));
+  if (ht) {
+    MJX_CUDA_TRY(cudaMemsetAsync(ht, 0, sizeof(double) * max_saves, s));
+    MJX_CUDA_TRY(cudaMemcpyAsync(ht, &t0, sizeof(double), cudaMemcpyHostToDevice, s));
   }
-  if (hist_dt) MJX_CUDA_TRY(cudaMemsetAsync(hist_dt, 0, sizeof(double) * max_saves, s));
-  MJX_CUDA_TRY(cudaStreamSynchronize(s));
-
-  const MixAttempt A = build_mix(plan32, g, pb, pid, w, L, st);
-  CtlArgs ca;
-  memset(&ca, 0, sizeof(ca));
-  ca.st = st; ca.partial = (const double*)(w + L.part); ca.nonfinite = (const int*)(w + L.bad);
-  ca.nparts = L.nparts; ca.n_dof = (double)nelem; ca.pid = *pid; ca.hist_t = hist_t; ca.hist_dt = hist_dt;
-  if (running && host_loop_mode()) {
+  if (hdt) MJX_CUDA_TRY(cudaMemsetAsync(hdt, 0, sizeof(double) * max_saves, s));
+  MJX_CUDA_TRY(cudaStreamSynchronize(s));  // h and t0 are host stack values
+  if (running && host_loop) {
+    const MixAttempt A = build_mix(P.plan32, &P.g, &P.pb, &P.pid, w, P.L, st);
+    CtlArgs ca;
+    memset(&ca, 0, sizeof(ca));
+    ca.st = st; ca.partial = (const double*)(w + P.L.part); ca.nonfinite = (const int*)(w + P.L.bad);
+    ca.nparts = P.L.nparts; ca.n_dof = (double)nf * P.g.ny * P.g.nx; ca.pid = P.pid; ca.hist_t = ht; ca.hist_dt = hdt;
     const cudaError_t he = run_host_loop([&](cudaStream_t ls) -> cudaError_t {
       const cudaError_t le = launch_mix_attempt(A, ls);
       return le == cudaSuccess ? launch_controller(ca, ls) : le;
     }, st, h.max_attempts, s);
     MJX_CUDA_TRY(he);
   } else if (running) {
-    cudaStream_t cs = nullptr;
-    cudaGraph_t graph = nullptr;
-    cudaGraphExec_t exec = nullptr;
-    cudaError_t ce = cudaSuccess;
-    do {
-      if ((ce = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking)) != cudaSuccess) break;
-      if ((ce = cudaGraphCreate(&graph, 0)) != cudaSuccess) break;
-      cudaGraphConditionalHandle hdl;
-      if ((ce = cudaGraphConditionalHandleCreate(&hdl, graph, 1, cudaGraphCondAssignDefault)) != cudaSuccess) break;
-      cudaGraphNodeParams np = {cudaGraphNodeTypeConditional};
-      np.conditional.handle = hdl;
-      np.conditional.type = cudaGraphCondTypeWhile;
-      np.conditional.size = 1;
-      cudaGraphNode_t node;
-      if ((ce = cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, &np)) != cudaSuccess) break;
-      cudaGraph_t body = np.conditional.phGraph_out[0];
-      if ((ce = cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) break;
-      ca.handle = hdl; ca.use_handle = 1;
-      // the body holds kCondUnroll attempts (each followed by the controller), so the
-      // conditional node is evaluated once per kCondUnroll attempts; once the
-      // controller marks the solve done, the rest of the body's kernels return at entry
-      cudaError_t le = cudaSuccess;
-      for (int u = 0; u < kCondUnroll && le == cudaSuccess; ++u) {
-        le = launch_mix_attempt(A, cs);
-        if (le == cudaSuccess) le = launch_controller(ca, cs);
-      }
-      cudaGraph_t captured = nullptr;
-      ce = cudaStreamEndCapture(cs, &captured);
-      if (le != cudaSuccess) { ce = le; break; }
-      if (ce != cudaSuccess) break;
-      if ((ce = cudaGraphInstantiate(&exec, graph, 0)) != cudaSuccess) break;
-      ce = cudaGraphLaunch(exec, s);
-    } while (0);
-    if (exec) cudaGraphExecDestroy(exec);
-    if (graph) cudaGraphDestroy(graph);
-    if (cs) cudaStreamDestroy(cs);
-    if (ce != cudaSuccess) { set_last_error(ce, __FILE__, __LINE__); return MJX_CUDA_ERROR; }
+    MJX_CUDA_TRY(cudaGraphLaunch(P.exec, s));
   }
   // final real state: select Y^[cur] into PB, inverse FP64 transform, write real into PA
-  MJX_TRY(mix_real_from_state(plan64, g, nf, st, (const float4*)(w + L.ys0), (const float4*)(w + L.ys1),
-                              (double2*)(w + L.pb), real64, io_dtype, y_final, s));
+  MJX_TRY(mix_real_from_state(P.plan64, &P.g, nf, st, (const float4*)(w + P.L.ys0), (const float4*)(w + P.L.ys1),
+                              (double2*)(w + P.L.pb), real64, io_dtype, y_final, s));
+  if (P.own_hist && hist_t) MJX_CUDA_TRY(cudaMemcpyAsync(hist_t, ht, sizeof(double) * max_saves, cudaMemcpyDefault, s));
+  if (P.own_hist && hist_dt) MJX_CUDA_TRY(cudaMemcpyAsync(hist_dt, hdt, sizeof(double) * max_saves, cudaMemcpyDefault, s));
   DevState out;
   MJX_CUDA_TRY(cudaMemcpyAsync(&out, st, sizeof(out), cudaMemcpyDeviceToHost, s));
   MJX_CUDA_TRY(cudaStreamSynchronize(s));
@@ -523,6 +558,94 @@ mjx_status mjx_imex_adaptive2d_mixed(const void* plan32, const void* plan64, con
     res->n_saved = out.write_idx; res->status = out.status; res->finite = out.finite;
   }
   return MJX_OK;
+}
+
+// hist_t / hist_dt: the caller's history arrays for a one-shot plan; null for a
+// persistent plan, whose history lives after the mixed layout in its workspace.
+static mjx_status make_mixed_plan(ImexMixedPlan** out, const void* plan32, const void* plan64, const mjx_grid2d* g,
+                                  const mjx_imex_problem* pb, const mjx_pid_params* pid, int max_steps,
+                                  int save_every, void* ws, size_t ws_bytes, bool persistent, double* hist_t,
+                                  double* hist_dt) {
+  MJX_TRY(check_mixed_problem(g, pb, pid, plan32, plan64, max_steps, save_every));
+  const int nf = pb->nfields;
+  const MixLayout L = mix_layout(g->ny, g->nx, nf, mix_nparts(g->ny, g->nx, nf));
+  const int max_saves = max_steps / save_every + 1;
+  const size_t ht = plan_hist_offset(L), hdt = ht + al256m(sizeof(double) * (size_t)max_saves);
+  const size_t total = persistent ? hdt + al256m(sizeof(double) * (size_t)max_saves) : L.total;
+  if (ws == nullptr || ws_bytes < total) return MJX_WORKSPACE;
+  MJX_TRY(ensure_kernel_attrs());
+  MJX_TRY(ensure_mix_attrs());
+  ImexMixedPlan* P = new ImexMixedPlan();
+  P->plan32 = plan32; P->plan64 = plan64; P->g = *g; P->pb = *pb; P->pid = *pid;
+  P->max_steps = max_steps; P->save_every = save_every; P->max_saves = max_saves;
+  P->ws = (char*)ws; P->L = L;
+  if (persistent) {
+    P->ht = (double*)((char*)ws + ht); P->hdt = (double*)((char*)ws + hdt); P->own_hist = true;
+  } else {
+    P->ht = hist_t; P->hdt = hist_dt;
+  }
+  if (persistent || !host_loop_mode()) {
+    const mjx_status st = capture_mixed(*P);
+    if (st != MJX_OK) { free_mixed_plan(P); return st; }
+  }
+  *out = P;
+  return MJX_OK;
+}
+
+}  // namespace mjx
+
+extern "C" {
+
+size_t mjx_imex_plan_ws_bytes(int ny, int nx, int nfields, int max_saves) {
+  if (ilog2_exact(nx) < 1 || ilog2_exact(ny) < 1 || nfields < 1 || nfields > 4 || max_saves < 1) return 0;
+  const MixLayout L = mix_layout(ny, nx, nfields, mix_nparts(ny, nx, nfields));
+  return plan_hist_offset(L) + 2 * al256m(sizeof(double) * (size_t)max_saves);
+}
+
+mjx_status mjx_imex_plan_create(void** plan, const void* plan32, const void* plan64, const mjx_grid2d* g,
+                                const mjx_imex_problem* pb, const mjx_pid_params* pid, int max_steps,
+                                int save_every, void* ws, size_t ws_bytes) {
+  if (plan == nullptr) return MJX_BAD_ARG;
+  *plan = nullptr;
+  ImexMixedPlan* P = nullptr;
+  MJX_TRY(make_mixed_plan(&P, plan32, plan64, g, pb, pid, max_steps, save_every, ws, ws_bytes, true, nullptr,
+                          nullptr));
+  *plan = P;
+  return MJX_OK;
+}
+
+mjx_status mjx_imex_plan_run(void* plan, int io_dtype, double t0, double t_end, double dt0, const void* y0,
+                             void* y_final, double* hist_t, double* hist_dt, mjx_adaptive_result* res,
+                             void* stream) {
+  ImexMixedPlan* P = (ImexMixedPlan*)plan;
+  if (P == nullptr || y0 == nullptr || y_final == nullptr) return MJX_BAD_ARG;
+  if (!elem_size(io_dtype)) return MJX_BAD_DTYPE;
+  return run_mixed(*P, io_dtype, t0, t_end, dt0, y0, y_final, hist_t, hist_dt, res, (cudaStream_t)stream,
+                   host_loop_mode());
+}
+
+mjx_status mjx_imex_plan_destroy(void* plan) {
+  if (plan == nullptr) return MJX_BAD_ARG;
+  free_mixed_plan((ImexMixedPlan*)plan);
+  return MJX_OK;
+}
+
+mjx_status mjx_imex_adaptive2d_mixed(const void* plan32, const void* plan64, const mjx_grid2d* g,
+                                     int io_dtype, const mjx_imex_problem* pb,
+                                     const mjx_pid_params* pid, double t0, double t_end, double dt0,
+                                     int max_steps, int save_every, const void* y0, void* y_final,
+                                     double* hist_t, double* hist_dt, void* ws, size_t ws_bytes,
+                                     mjx_adaptive_result* res, void* stream) {
+  if (!y0 || !y_final) return MJX_BAD_ARG;
+  if (!elem_size(io_dtype)) return MJX_BAD_DTYPE;
+  // one shot: capture, run once, release (the persistent form is mjx_imex_plan_create)
+  ImexMixedPlan* P = nullptr;
+  MJX_TRY(make_mixed_plan(&P, plan32, plan64, g, pb, pid, max_steps, save_every, ws, ws_bytes, false, hist_t,
+                          hist_dt));
+  const mjx_status st = run_mixed(*P, io_dtype, t0, t_end, dt0, y0, y_final, nullptr, nullptr, res,
+                                  (cudaStream_t)stream, host_loop_mode());
+  free_mixed_plan(P);
+  return st;
 }
 
 }  // extern "C"

@@ -458,6 +458,30 @@ __global__ void vd_jvp_j_kernel(const float* y32, float* V, const GmresState* gs
   }
 }
 
+// out = a0 v - beta J_F(u) v in FP64 (the exported JVP; J_F v itself with a0 = 0, beta = -1)
+__global__ void vd_jvp64_kernel(const double* __restrict__ u, const double* __restrict__ v, double* __restrict__ out,
+                                double a, double b, double c, double a0, double beta, int n, double idx2,
+                                double idy2, long long N2) {
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < N2;
+       p += (long long)gridDim.x * blockDim.x) {
+    int i, jj;
+    nk_rowcol(p, n, i, jj);
+    const double uc = u[p], ue = dval(u, i, jj + 1, n), uw = dval(u, i, jj - 1, n);
+    const double un = dval(u, i + 1, jj, n), us = dval(u, i - 1, jj, n);
+    const double vc = v[p], ve = dval(v, i, jj + 1, n), vw = dval(v, i, jj - 1, n);
+    const double vn = dval(v, i + 1, jj, n), vs = dval(v, i - 1, jj, n);
+    const double Dc = a + b * uc * uc, De = a + b * ue * ue, Dw = a + b * uw * uw;
+    const double Dn = a + b * un * un, Ds = a + b * us * us;
+    const double dc = 2.0 * b * uc * vc, de = 2.0 * b * ue * ve, dw = 2.0 * b * uw * vw;
+    const double dn = 2.0 * b * un * vn, ds = 2.0 * b * us * vs;
+    const double gx = 0.5 * (Dc + De) * (ve - vc) + 0.5 * (dc + de) * (ue - uc)
+                    - 0.5 * (Dw + Dc) * (vc - vw) - 0.5 * (dw + dc) * (uc - uw);
+    const double gy = 0.5 * (Dc + Dn) * (vn - vc) + 0.5 * (dc + dn) * (un - uc)
+                    - 0.5 * (Ds + Dc) * (vc - vs) - 0.5 * (ds + dc) * (uc - us);
+    out[p] = a0 * vc - beta * (gx * idx2 + gy * idy2 - 3.0 * c * uc * uc * vc);
+  }
+}
+
 __global__ void nk_scale_j_kernel(float* V, const GmresState* gs, long long N2) {
   if (gs->converged) return;
   float* v = V + (long long)gs->j * N2;
@@ -871,6 +895,16 @@ mjx_status mjx_vardiff_rhs2d(int n, double dy, double dx, const double* model_ab
   if (n < 1 || !(dx > 0) || !(dy > 0)) return MJX_BAD_SHAPE;
   vd_rhs_kernel<<<152 * 4, 256, 0, (cudaStream_t)stream>>>(y, out, model_abc[0], model_abc[1], model_abc[2],
                                                            1.0, n, 1.0 / (dx * dx), 1.0 / (dy * dy));
+  return cuda_status(cudaGetLastError());
+}
+
+mjx_status mjx_vardiff_jvp2d(int n, double dy, double dx, const double* model_abc, double a0, double beta,
+                             const double* u, const double* v, double* out, void* stream) {
+  if (model_abc == nullptr || u == nullptr || v == nullptr || out == nullptr) return MJX_BAD_ARG;
+  if (n < 1 || !(dx > 0) || !(dy > 0)) return MJX_BAD_SHAPE;
+  vd_jvp64_kernel<<<152 * 4, 256, 0, (cudaStream_t)stream>>>(u, v, out, model_abc[0], model_abc[1], model_abc[2],
+                                                             a0, beta, n, 1.0 / (dx * dx), 1.0 / (dy * dy),
+                                                             (long long)n * n);
   return cuda_status(cudaGetLastError());
 }
 

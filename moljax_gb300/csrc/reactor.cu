@@ -8,6 +8,13 @@
 //  MJX_REACTOR_DIRICHLET   benchmarks/benchmark_method_comparison.py:56-160:
 //    N nodes, dz = 1/(N-1), fully implicit CN of L = D2/Pe - D1 - Da with a
 //    Dirichlet inlet row and the one-sided outlet row.
+//  MJX_REACTOR_DANCKWERTS_CN  the Danckwerts discretisation above, advanced by
+//    the fully implicit CN of benchmark_method_comparison.py:134-160: the whole
+//    operator M c + s (dispersion, upwind advection with the inlet flux, and
+//    reaction; s = e_0/dz) is implicit, so the step is stable at the CN step
+//    size of that benchmark, dt = min(10 dz, 0.05, t_final/100) (line 216),
+//    which the semi-implicit form above is not (its explicit upwind advection
+//    needs dt <= dz).
 // The reference solves with a dense inverse / LU (O(N^2) per step); the system
 // matrix is tridiagonal and constant in time, so each CTA factorises it once
 // (Thomas) and runs every step's two substitution sweeps as parallel affine
@@ -99,11 +106,18 @@ __global__ void __launch_bounds__(256) reactor_kernel(ReactorArgs A) {
   const int tid = threadIdx.x, nt = blockDim.x;
   const double Pe = I.Pe, Da = I.Da, dt = I.dt;
   const bool dk = I.variant == MJX_REACTOR_DANCKWERTS;
-  const double dz = dk ? 1.0 / n : 1.0 / (n - 1);
+  const bool dkcn = I.variant == MJX_REACTOR_DANCKWERTS_CN;
+  const double dz = (dk || dkcn) ? 1.0 / n : 1.0 / (n - 1);
   // tridiagonal entries of the implicit matrix and of the explicit operator
   double kap = 0, Ls = 0, Ld = 0, Lp = 0, Lsl = 0, Ldl = 0;
   if (dk) {
     kap = 0.5 * dt / (Pe * dz * dz);
+  } else if (dkcn) {
+    // M: row 0 (-2q - 1/dz - Da, q), rows 1..N-2 (q + 1/dz, -2q - 1/dz - Da, q),
+    // row N-1 (2q + 1/dz, -2q - 1/dz - Da)
+    const double q = (1.0 / Pe) / (dz * dz);
+    Ls = q + 1.0 / dz; Ld = -2.0 * q - 1.0 / dz - Da; Lp = q;
+    Lsl = 2.0 * q + 1.0 / dz; Ldl = Ld;
   } else {
     const double q = (1.0 / Pe) / (dz * dz);
     Ls = q + 1.0 / dz; Ld = -2.0 * q - 1.0 / dz - Da; Lp = q;   // rows 1..N-2
@@ -116,12 +130,12 @@ __global__ void __launch_bounds__(256) reactor_kernel(ReactorArgs A) {
   };
   auto dia = [&](int i) -> double {
     if (dk) return 1.0 + 2.0 * kap;
-    if (i == 0) return 1.0;
+    if (i == 0) return dkcn ? 1.0 - 0.5 * dt * Ld : 1.0;
     return i == n - 1 ? 1.0 - 0.5 * dt * Ldl : 1.0 - 0.5 * dt * Ld;
   };
   auto sup = [&](int i) -> double {  // A[i][i+1]
     if (dk) return i == n - 1 ? 0.0 : -kap;
-    if (i == 0 || i == n - 1) return 0.0;
+    if (i == n - 1 || (i == 0 && !dkcn)) return 0.0;
     return -0.5 * dt * Lp;
   };
   // Thomas factorisation once (sequential, FP64)
@@ -136,7 +150,7 @@ __global__ void __launch_bounds__(256) reactor_kernel(ReactorArgs A) {
     }
   }
   for (int i = tid; i < n; i += nt) c[pz(i)] = (T)I.c_init;
-  if (!dk && tid == 0) c[pz(0)] = (T)I.c_inlet;
+  if (!dk && !dkcn && tid == 0) c[pz(0)] = (T)I.c_inlet;
   __syncthreads();
   const T idz = (T)(1.0 / dz), Dat = (T)Da, dtt = (T)dt, kp = (T)kap;
   const T half_dt = (T)(0.5 * dt);
@@ -152,6 +166,13 @@ __global__ void __launch_bounds__(256) reactor_kernel(ReactorArgs A) {
         else lap = cl - (T)2 * ci + cr;
         const T adv = i == 0 ? -(ci - (T)1) * idz : -(ci - cl) * idz;
         r = ci + kp * lap + dtt * (adv - Dat * ci);
+      } else if (dkcn) {  // c + dt/2 M c + dt s
+        const T cl = i > 0 ? c[pz(i - 1)] : (T)0, cr = i < n - 1 ? c[pz(i + 1)] : (T)0;
+        T Mc;
+        if (i == 0) Mc = (T)Ld * ci + (T)Lp * cr;
+        else if (i == n - 1) Mc = (T)Lsl * cl + (T)Ldl * ci;
+        else Mc = (T)Ls * cl + (T)Ld * ci + (T)Lp * cr;
+        r = ci + half_dt * Mc + (i == 0 ? dtt * idz : (T)0);
       } else {
         if (i == 0) {
           r = (T)I.c_inlet;

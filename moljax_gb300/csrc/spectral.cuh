@@ -47,7 +47,7 @@ enum {
 };
 
 // pointwise reaction kinds (compile-time)
-enum { RX_NONE = 0, RX_GRAY_SCOTT = 1, RX_FISHER = 2, RX_LINEAR = 3 };
+enum { RX_NONE = 0, RX_GRAY_SCOTT = 1, RX_FISHER = 2, RX_LINEAR = 3, RX_KINETICS = 4 };
 
 // The Heun increment y** - y* computed without forming y** (no cancellation).
 template <typename T, int RX>

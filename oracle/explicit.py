@@ -173,3 +173,27 @@ def fft_advdiff_inverse(r, grid, dt, D, vx, vy):
     den = 1.0 - dt * (D * lam - 1j * (vx * kx + vy * ky))
     den = np.where(np.abs(den) < 1e-14, 1e-14, den)
     return np.real(np.fft.ifft2(np.fft.fft2(r) / den))
+
+
+def mass_action(species, reactions=(), linear=None, source=None):
+    """Reaction callable (padded state -> rates) of a mass-action network: for each
+    species source + sum_j linear[(s, j)] c_j + sum_r (products - reactants)_s rate_r
+    prod c^order (the native network of make_kinetics_op, restated in NumPy)."""
+    def R(y):
+        out = {}
+        for s in species:
+            acc = np.zeros_like(y[s], dtype=np.float64) + (source or {}).get(s, 0.0)
+            for (t, j), kv in (linear or {}).items():
+                if t == s:
+                    acc = acc + kv * y[j]
+            out[s] = acc
+        for rate, reac, prod in reactions:
+            w = float(rate)
+            for j, o in reac.items():
+                w = w * y[j] ** int(o)
+            for s in species:
+                nu = prod.get(s, 0) - reac.get(s, 0)
+                if nu:
+                    out[s] = out[s] + nu * w
+        return out
+    return R

@@ -1,0 +1,61 @@
+"""Oracle: Crank-Nicolson Gray-Scott by the preconditioned Newton iteration.
+
+TEST INFRASTRUCTURE ONLY (see ``oracle/__init__.py``).  NumPy FP64 restatement
+of benchmarks/benchmark_gray_scott.py:162-228 (cn_newton_step_jit): per step the
+CN residual with pseudo-spectral (or any given) Laplacian eigenvalues, the exact
+periodic inverse of (I - dt/2 D Lap) as the preconditioner, u <- u + M^-1(-res),
+while max|res_u| + max|res_v| > tol and i < max_iter, starting from u_old with
+res_norm = 1.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+
+
+def spectral_symbol(n, dx):
+    """benchmarks/benchmark_gray_scott.py:53-56: -(kx^2 + ky^2), k = 2 pi fftfreq(n, dx)."""
+    k = np.fft.fftfreq(n, dx) * 2 * np.pi
+    KX, KY = np.meshgrid(k, k, indexing="ij")
+    return -(KX ** 2 + KY ** 2)
+
+
+def benchmark_ic(n):
+    """benchmarks/benchmark_gray_scott.py:60-62 (numpy's legacy seed 42 stream)."""
+    rs = np.random.RandomState(42)
+    u0 = np.ones((n, n)) - 0.5 * rs.rand(n, n) * 0.1
+    v0 = 0.25 * np.ones((n, n)) + 0.5 * rs.rand(n, n) * 0.1
+    return u0, v0
+
+
+def cn_newton_step(u_old, v_old, lam, Du, Dv, F, k, dt, tol=1e-8, max_iter=10):
+    """One step; returns (u, v, iterations)."""
+    fft2, ifft2 = np.fft.fft2, np.fft.ifft2
+    pu = 1.0 / (1.0 - 0.5 * dt * Du * lam)
+    pv = 1.0 / (1.0 - 0.5 * dt * Dv * lam)
+    lap_uo = np.real(ifft2(lam * fft2(u_old)))
+    lap_vo = np.real(ifft2(lam * fft2(v_old)))
+    uvv_o = u_old * v_old * v_old
+    Ruo, Rvo = -uvv_o + F * (1 - u_old), uvv_o - (F + k) * v_old
+    u, v = u_old.copy(), v_old.copy()
+    res_norm, i = 1.0, 0
+    while res_norm > tol and i < max_iter:
+        lap_u = np.real(ifft2(lam * fft2(u)))
+        lap_v = np.real(ifft2(lam * fft2(v)))
+        uvv = u * v * v
+        res_u = u - u_old - 0.5 * dt * (Du * (lap_u + lap_uo) + (-uvv + F * (1 - u)) + Ruo)
+        res_v = v - v_old - 0.5 * dt * (Dv * (lap_v + lap_vo) + (uvv - (F + k) * v) + Rvo)
+        u = u + np.real(ifft2(pu * fft2(-res_u)))
+        v = v + np.real(ifft2(pv * fft2(-res_v)))
+        res_norm = np.max(np.abs(res_u)) + np.max(np.abs(res_v))
+        i += 1
+    return u, v, i
+
+
+def cn_solve(u0, v0, lam, Du, Dv, F, k, dt, n_steps, tol=1e-8, max_iter=10):
+    """n_steps steps (cn_solve_jit, 216-221); returns (u, v, per-step iteration counts)."""
+    u, v, its = u0, v0, []
+    for _ in range(n_steps):
+        u, v, it = cn_newton_step(u, v, lam, Du, Dv, F, k, dt, tol, max_iter)
+        its.append(it)
+    return u, v, its

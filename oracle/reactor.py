@@ -40,6 +40,32 @@ def danckwerts_cn(N, Pe, Da, dt, n_steps, c_init=1.0):
     return c
 
 
+def danckwerts_full_cn(N, Pe, Da, dt, n_steps, c_init=0.0):
+    """The Danckwerts discretisation of danckwerts_cn (benchmark_reactor_vs_diffrax.py:40-138:
+    N cells, dz = 1/N, Neumann outlet row, inlet flux -(c0 - 1)/dz) advanced by the fully
+    implicit Crank-Nicolson of benchmark_method_comparison.py:134-160: with M the whole
+    operator (dispersion, upwind advection, reaction) and s = e0/dz the inlet source,
+    (I - dt/2 M) c' = (I + dt/2 M) c + dt s.  Dense FP64."""
+    dz = 1.0 / N
+    L = (np.diag(-2.0 * np.ones(N)) + np.diag(np.ones(N - 1), 1) + np.diag(np.ones(N - 1), -1))
+    L[-1, -1] = -2.0
+    L[-1, -2] = 2.0
+    L /= dz ** 2
+    G = np.diag(np.ones(N)) + np.diag(-np.ones(N - 1), -1)
+    G /= dz                      # row 0: c0/dz (the inlet flux without its source)
+    M = L / Pe - G - Da * np.eye(N)
+    s = np.zeros(N)
+    s[0] = 1.0 / dz
+    I = np.eye(N)
+    A = I - 0.5 * dt * M
+    B = I + 0.5 * dt * M
+    Ainv = np.linalg.inv(A)
+    c = np.full(N, float(c_init))
+    for _ in range(n_steps):
+        c = Ainv @ (B @ c + dt * s)
+    return c
+
+
 def dirichlet_system(N, Pe, Da):
     """benchmarks/benchmark_method_comparison.py:56-110 (the full operator L)."""
     dz = 1.0 / (N - 1)

@@ -257,3 +257,62 @@ def test_gray_scott_stage_rectangular(cuda):
     ref = OX.STEPS[2](om, y0, 0.5)
     for k in ("u", "v"):
         np.testing.assert_allclose(out[k].cpu().numpy()[c], ref[k][c], rtol=0, atol=1e-13)
+
+
+def _kinetics_case(n, nspecies, kind, cuda, dtype=torch.float64):
+    """A mass-action network on an advection-diffusion model (the multispecies caller of
+    make_reaction_op, examples/advdiff_multispecies.py, with native reactions)."""
+    import moljax_gb300 as M
+    from moljax_gb300.core.bc import BCType
+    names = ["a", "b", "c", "d"][:nspecies]
+    reactions = [(2.0, {"a": 1, "b": 1}, {"c": 1}) if nspecies >= 3 else (2.0, {"a": 1, "b": 1}, {}),
+                 (0.7, {"b": 2}, {"a": 1}), (0.25, {"a": 1}, {"a": 2}), (0.1, {"a": 3}, {})]
+    if nspecies == 4:
+        reactions.append((1.3, {"c": 1, "d": 1}, {"d": 2}))
+    linear = {("a", "b"): 0.3, ("b", "b"): -0.3}
+    source = {"b": 0.05}
+    op = M.make_kinetics_op(names, reactions, linear, source)
+    grid = M.Grid2D(n, n, 0.0, 1.0, 0.0, 1.0)
+    model = M.create_advection_diffusion_model(grid, names, 0.01, 0.6, -0.4, BCType(kind), True, dtype,
+                                               reactions=op)
+    og = mol.Grid2D(n, n, 0, 1, 0, 1)
+    rng = np.random.default_rng(17)
+    y0 = {k: mol.pad(rng.uniform(0.2, 1.0, (n, n)), og) for k in names}
+    om = OX.ExplicitModel(og, {k: kind for k in names}, {k: 0.01 for k in names}, advection="upwind",
+                          vx=0.6, vy=-0.4, reaction=OX.mass_action(names, reactions, linear, source),
+                          params={"D": 0.01, "vx": 0.6, "vy": -0.4})
+    ym = {k: torch.tensor(v, dtype=dtype, device=cuda) for k, v in y0.items()}
+    return M, model, ym, om, y0, names
+
+
+@pytest.mark.parametrize("nspecies", [2, 3, 4])
+@pytest.mark.parametrize("kind", [mol.PERIODIC, mol.NEUMANN])
+def test_kinetics_network_vs_oracle(cuda, nspecies, kind):
+    """The native mass-action network in the RHS, in SSPRK3 / RK4 steps (scalar and 128-bit
+    stage kernels: n = 32 and 34 columns) and in the adaptive loop, against the oracle."""
+    for n in (32, 34):
+        M, model, ym, om, y0, names = _kinetics_case(n, nspecies, kind, cuda)
+        F = model.rhs(ym)
+        R = om.rhs(y0)
+        for k in names:
+            assert _rel(_interior(F[k].cpu().numpy(), n), _interior(R[k], n)) < 1e-12
+        # the torch form of the op (generic paths) gives the same rates
+        Rt = model.nonlinear_ops[0].apply(ym, model.grid, 0.0, model.params)
+        Ro = om.reaction(y0)
+        for k in names:
+            assert _rel(_interior(Rt[k].cpu().numpy(), n), _interior(Ro[k], n)) < 1e-13
+        for method in (1, 2):
+            step = {1: "ssprk3_step", 2: "rk4_step"}[method]
+            out = getattr(M, step)(model, ym, 0.0, 5e-3)
+            ref = OX.STEPS[method](om, y0, 5e-3)
+            for k in names:
+                assert _rel(_interior(out[k].cpu().numpy(), n), _interior(ref[k], n)) < 1e-13
+    pid = M.PIDParams(atol=1e-6, rtol=1e-4)
+    r = M.adaptive_integrate(model, ym, 0.0, 0.3, 0.01, M.IntegratorType.RK4, max_steps=2000, pid_params=pid,
+                             save_every=1)
+    ro = OX.adaptive_integrate_explicit(om, y0, 0.0, 0.3, 0.01, 2, max_steps=2000,
+                                        pid=OI.PIDParams(atol=1e-6, rtol=1e-4), save_every=1)
+    assert r.status == ro.status == 0
+    assert (r.n_accepted, r.n_rejected) == (ro.n_accepted, ro.n_rejected)
+    for k in names:
+        assert _rel(_interior(r.y_final[k].cpu().numpy(), n), _interior(ro.y_final[k], n)) < 1e-10

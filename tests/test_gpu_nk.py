@@ -176,3 +176,27 @@ def test_adaptive_implicit_vs_oracle(cuda, method):
     assert abs(r.n_accepted - ro["n_acc"]) <= 0.25 * ro["n_acc"] + 2
     # both runs meet rtol = 1e-2 per step; their final states agree far inside that
     assert _rel(r.y_final["u"][1:-1, 1:-1].cpu().numpy(), ro["u"]) < 5e-3
+
+
+def test_vardiff_jvp_vs_oracle_and_difference_quotient(cuda):
+    """The exported hand-written JVP equals the oracle's JVP and the central difference
+    of the native F (jax.jvp's role in newton_krylov.py:61-80)."""
+    import moljax_gb300 as M
+    from moljax_gb300.core.model import vardiff_jvp
+    n = 48
+    g = M.Grid2D(n, n, 0.0, 1.0, 0.0, 1.0)
+    m = M.create_variable_diffusion_model(g, 1.0, 1.0, 1.0)
+    rng = np.random.default_rng(9)
+    u = ONK.gaussians_ic(n)
+    v = rng.standard_normal((n, n))
+    ut, vt = torch.tensor(u, device=cuda), torch.tensor(v, device=cuda)
+    jv = vardiff_jvp(m, ut, vt).cpu().numpy()
+    ref = ONK.vardiff_JF(u, v, 1.0 / n, 1.0 / n)
+    assert _rel(jv, ref) < 1e-13
+    # the residual form a0 v - beta J v
+    jr = vardiff_jvp(m, ut, vt, a0=1.5, beta=0.01).cpu().numpy()
+    assert _rel(jr, 1.5 * v - 0.01 * ref) < 1e-13
+    eps = 1e-6
+    Fp = ONK.vardiff_F(u + eps * v, 1.0 / n, 1.0 / n)
+    Fm = ONK.vardiff_F(u - eps * v, 1.0 / n, 1.0 / n)
+    assert _rel(jv, (Fp - Fm) / (2 * eps)) < 1e-7

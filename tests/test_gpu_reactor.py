@@ -24,23 +24,29 @@ def test_reactor_published_conversions(cuda):
         assert 1 - float(c[-1]) == pytest.approx(v["CN"]["conversion"], rel=1e-10)
 
 
-@pytest.mark.parametrize("variant", ["danckwerts", "dirichlet"])
+@pytest.mark.parametrize("variant", ["danckwerts", "dirichlet", "danckwerts_cn"])
 def test_reactor_batch_uneven_vs_oracle(cuda, variant):
     from moljax_gb300.core import reactor as R
     rng = np.random.default_rng(5)
+    kind = {"danckwerts": R.DANCKWERTS, "dirichlet": R.DIRICHLET, "danckwerts_cn": R.DANCKWERTS_CN}[variant]
     cases = []
     for n in (64, 100, 257, 1000, 4096):
         dt, ns = R.served_dt(n)
+        if variant == "danckwerts":  # explicit upwind advection: stable for dt <= dz only
+            dt = 0.5 / n
         ns = min(ns, 60)
-        cases.append(R.ReactorCase(n, float(rng.uniform(10, 200)), float(rng.uniform(0.5, 5)), dt, ns,
-                                   R.DANCKWERTS if variant == "danckwerts" else R.DIRICHLET, 0.0))
+        cases.append(R.ReactorCase(n, float(rng.uniform(10, 200)), float(rng.uniform(0.5, 5)), dt, ns, kind, 0.0))
     for dtype, tol in ((torch.float64, 1e-11), (torch.float32, 1e-4)):
         outs = R.solve_batch(cases, dtype)
         for c, o in zip(cases, outs):
             if variant == "danckwerts":
                 ref = OR.danckwerts_cn(c.n, c.Pe, c.Da, c.dt, c.n_steps, c.c_init)
+            elif variant == "danckwerts_cn":
+                ref = OR.danckwerts_full_cn(c.n, c.Pe, c.Da, c.dt, c.n_steps, c.c_init)
             else:
                 ref = OR.dirichlet_cn(c.n, c.Pe, c.Da, c.dt, c.n_steps, 1.0, c.c_init)
+            # a stable run stays O(1) (CN overshoots the inlet value slightly, never grows)
+            assert np.all(np.isfinite(ref)) and np.max(np.abs(ref)) <= 1.5
             err = np.linalg.norm(o.double().cpu().numpy() - ref) / np.linalg.norm(ref)
             assert err < tol, (c.n, err)
 
