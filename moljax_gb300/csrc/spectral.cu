@@ -10,8 +10,7 @@
 #include <vector>
 
 #include "spectral.cuh"
-
-struct CUctx_st;  // driver-API context (opaque)
+#include "tma.cuh"
 
 namespace mjx {
 
@@ -468,8 +467,40 @@ mjx_status ensure_kernel_attrs() {
   });
 }
 
-typedef int (*PfnCtxGetCurrent)(CUctx_st**);
-typedef int (*PfnCtxGetId)(CUctx_st*, unsigned long long*);
+typedef CUresult (*PfnTensorMapEncodeTiled)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                            const cuuint64_t*, const cuuint32_t*, const cuuint32_t*,
+                                            CUtensorMapInterleave, CUtensorMapSwizzle, CUtensorMapL2promotion,
+                                            CUtensorMapFloatOOBfill);
+
+mjx_status make_tmap_2d_f32(CUtensorMap* map, const void* base, unsigned long long inner, unsigned long long rows,
+                            unsigned long long row_bytes, unsigned box_inner, unsigned box_rows) {
+  static PfnTensorMapEncodeTiled encode = nullptr;
+  static std::once_flag resolved;
+  std::call_once(resolved, []() {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess && q == cudaDriverEntryPointSuccess)
+      encode = (PfnTensorMapEncodeTiled)f;
+  });
+  if (encode == nullptr) return cuda_status(cudaErrorNotSupported);
+  // the copy rules: 16-byte aligned base and row stride, inner box a multiple of 16 bytes
+  if (((uintptr_t)base & 15) || (row_bytes & 15) || ((box_inner * 4) & 15) || box_rows < 1 || box_rows > 256 ||
+      box_inner < 1 || box_inner > 256)
+    return MJX_BAD_ARG;
+  const cuuint64_t dims[2] = {inner, rows};
+  const cuuint64_t strides[1] = {row_bytes};
+  const cuuint32_t box[2] = {box_inner, box_rows};
+  const cuuint32_t estr[2] = {1, 1};
+  const CUresult r = encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void*>(base), dims, strides, box,
+                            estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return cuda_status(cudaErrorInvalidValue);
+  return MJX_OK;
+}
+
+typedef CUresult (*PfnCtxGetCurrent)(CUcontext*);
+typedef CUresult (*PfnCtxGetId)(CUcontext, unsigned long long*);
 
 mjx_status current_context_id(unsigned long long* id) {
   static PfnCtxGetCurrent get_current = nullptr;
@@ -487,7 +518,7 @@ mjx_status current_context_id(unsigned long long* id) {
       get_id = (PfnCtxGetId)f;
   });
   if (get_current == nullptr || get_id == nullptr) return cuda_status(cudaErrorNotSupported);
-  CUctx_st* ctx = nullptr;
+  CUcontext ctx = nullptr;
   if (get_current(&ctx) != 0) return cuda_status(cudaErrorDeviceUninitialized);
   if (ctx == nullptr) {  // nothing current yet: the runtime's default is the primary context
     int dev = 0;
