@@ -115,7 +115,6 @@ __device__ __forceinline__ void bcol_item(float2* buf, const BInst* I, unsigned 
   t.pa = I->pa; t.pb = I->pb; t.za = I->za; t.zb = I->zb;
   t.lamx = I->lamx; t.lamy = I->lamy; t.tw = I->twy;
   t.hA = (float)(0.5 * h * I->D[f]); t.hB = (float)(0.25 * h * I->D[f]); t.nrm = I->inv_norm;
-  t.sp_p = nullptr; t.sp_q = nullptr; t.bar = nullptr; t.err = nullptr;  // operands from global memory
   mcol_tile(buf, t, threadIdx.x, BT);
 }
 

@@ -23,8 +23,6 @@
 //   C3 col  Y^[1-cur] = M(dt/4)(PB + FFT_y ZB);  ZA = IFFT_y(Y^[1-cur] - PA), ZB = IFFT_y(Y^[1-cur])
 //   R3 row  c2r of (ZA, ZB) pairs -> scaled error partials
 #include <math.h>
-#include <stdio.h>
-#include <stdlib.h>
 #include <string.h>
 
 #include "mixed.cuh"
@@ -45,16 +43,6 @@ struct MJob {
 
 // Float-float complex element in HBM: {re_hi, im_hi, re_lo, im_lo}.
 struct MColArgs {
-  // TMA maps of the float-float arrays (viewed as FP32 rows of 4 ldc floats, fields stacked),
-  // boxes of C columns by brows rows: the state operands are staged in shared memory
-  // while the forward transform runs (stage != 0)
-  CUtensorMap tm_ys[2];
-  CUtensorMap tm_pa;
-  CUtensorMap tm_pb;
-  int stage, brows;
-  int stage_ops;   // operand tiles reserved in shared memory (the largest job's count)
-  int wide;        // 1: some job writes two transforms (tile width 2C), 0: C
-  int* err;
   int ny, log2ny, ncols, ldc, C, njobs;
   float4* ys[2];
   float4* pa;
@@ -70,45 +58,15 @@ struct MColArgs {
   MJob job[8];
 };
 
-// operands a job stages: the state operand, plus pa for the end of the half-step branch
-__host__ __device__ __forceinline__ int mc_nops(int type) { return type == MC_HALF_END ? 2 : 1; }
-
 template <int NT, int MINB>
 __global__ void __launch_bounds__(NT, MINB) mcol_kernel(const __grid_constant__ MColArgs a) {
-  extern __shared__ __align__(128) unsigned char smem_raw[];
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  float2* buf = reinterpret_cast<float2*>(smem_raw);
   const DevState* st = a.st;
   if (st != nullptr && st->done) return;
   const MJob jb = a.job[blockIdx.y];
   const int cur = st != nullptr ? st->cur : 0;
   const double h = st != nullptr ? st->dtc : a.hfixed;
-  // shared memory: [barrier (128 B)][staged operands][transform tile]
-  const size_t tile_elems = (size_t)a.ny * a.C;
-  unsigned long long* bar = reinterpret_cast<unsigned long long*>(smem_raw);
-  float4* stg = reinterpret_cast<float4*>(smem_raw + 128);
-  float2* buf = reinterpret_cast<float2*>(smem_raw + (a.stage ? 128 + a.stage_ops * tile_elems * sizeof(float4) : 0));
-  const float4* sp_p = nullptr;
-  const float4* sp_q = nullptr;
-  if (a.stage) {
-    const int nops = mc_nops(jb.type);
-    if (threadIdx.x == 0) mbar_init(bar, 1);
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      const CUtensorMap* mp = jb.type == MC_SPLIT ? &a.tm_ys[cur]
-                              : (jb.type == MC_FULL_END ? &a.tm_pa : &a.tm_pb);
-      const int nb = a.ny / a.brows;
-      const unsigned box_bytes = (unsigned)(a.brows * a.C * sizeof(float4));
-      mbar_arrive_expect_tx(bar, box_bytes * nb * nops);
-      const int x = blockIdx.x * a.C * 4;             // float column of the tile (a multiple of 16 B)
-      const int y0 = (int)(jb.off / a.ldc);           // first row of the job's field
-      for (int b = 0; b < nb; ++b)
-        tma_load_2d(stg + (size_t)b * a.brows * a.C, mp, x, y0 + b * a.brows, bar);
-      if (nops == 2)
-        for (int b = 0; b < nb; ++b)
-          tma_load_2d(stg + tile_elems + (size_t)b * a.brows * a.C, &a.tm_pa, x, y0 + b * a.brows, bar);
-    }
-    sp_p = stg;
-    sp_q = nops == 2 ? stg + tile_elems : nullptr;
-  }
   MColTile t;
   t.ny = a.ny; t.log2ny = a.log2ny; t.ncols = a.ncols; t.C = a.C; t.type = jb.type;
   t.kx0 = blockIdx.x * a.C;
@@ -117,7 +75,6 @@ __global__ void __launch_bounds__(NT, MINB) mcol_kernel(const __grid_constant__ 
   t.pa = a.pa; t.pb = a.pb; t.za = a.za; t.zb = a.zb;
   t.lamx = a.lamx; t.lamy = a.lamy; t.tw = a.tw;
   t.hA = (float)(0.5 * h * jb.D); t.hB = (float)(0.25 * h * jb.D); t.nrm = a.inv_norm;
-  t.sp_p = sp_p; t.sp_q = sp_q; t.bar = a.stage ? bar : nullptr; t.err = a.err;
   mcol_tile(buf, t, threadIdx.x, blockDim.x);
 }
 
@@ -184,57 +141,6 @@ static int mix_nparts(int ny, int nx, int nf) { return row_ctas(nx, ny, nf); }
 // 901 ms with 256; mixed choices in between.
 static constexpr int kColCap[3] = {512, 512, 512};
 
-static size_t mcol_smem(const MColArgs& c) {
-  return (c.stage ? 128 + (size_t)c.stage_ops * c.ny * c.C * sizeof(float4) : 0) +
-         (size_t)sp_size(c.ny * (c.wide ? 2 : 1) * c.C) * sizeof(float2);
-}
-
-// Column tile width and operand staging of the three column passes.  The MJX_MIX_TILES
-// environment variable ("C1,S1;C2,S2;C3,S3": columns per tile, 1 = stage the operands
-// by TMA) overrides the defaults for measurements.
-struct MixTiles { int C[3]; int stage[3]; };
-
-static const MixTiles& mix_tiles() {
-  static const MixTiles t = [] {
-    MixTiles r = {{0, 0, 0}, {0, 0, 0}};
-    const char* v = getenv("MJX_MIX_TILES");
-    if (v != nullptr) {
-      int c[3], s3[3];
-      if (sscanf(v, "%d,%d;%d,%d;%d,%d", &c[0], &s3[0], &c[1], &s3[1], &c[2], &s3[2]) == 6)
-        for (int i = 0; i < 3; ++i)
-          if (c[i] >= 1 && c[i] <= 16 && (c[i] & (c[i] - 1)) == 0) { r.C[i] = c[i]; r.stage[i] = s3[i] != 0; }
-    }
-    return r;
-  }();
-  return t;
-}
-
-// Staging needs whole 16-byte box rows (C * 16 bytes), at most 256 rows per box, and
-// room for the operands next to the transform tile.
-static bool stage_ok(const MColArgs& c, char* ws, const MixLayout& L, int nf) {
-  (void)ws; (void)L; (void)nf;
-  if (2 * c.C * (c.ny >= 16 ? c.ny / 16 : 1) > 512) return false;
-  MColArgs t = c;
-  t.stage = 1;
-  return mcol_smem(t) <= 220 * 1024;
-}
-
-static void stage_maps(MColArgs& c, char* ws, const MixLayout& L, int nf) {
-  const unsigned long long inner = (unsigned long long)c.ldc * 4, rows = (unsigned long long)nf * c.ny;
-  const unsigned long long rb = (unsigned long long)c.ldc * sizeof(float4);
-  const unsigned brows = c.ny < 256 ? c.ny : 256;
-  const unsigned bi = (unsigned)c.C * 4;
-  if (make_tmap_2d_f32(&c.tm_ys[0], ws + L.ys0, inner, rows, rb, bi, brows) != MJX_OK ||
-      make_tmap_2d_f32(&c.tm_ys[1], ws + L.ys1, inner, rows, rb, bi, brows) != MJX_OK ||
-      make_tmap_2d_f32(&c.tm_pa, ws + L.pa, inner, rows, rb, bi, brows) != MJX_OK ||
-      make_tmap_2d_f32(&c.tm_pb, ws + L.pb, inner, rows, rb, bi, brows) != MJX_OK) {
-    c.stage = 0;  // no tensor maps: the operands come from global memory
-    return;
-  }
-  c.stage = 1;
-  c.brows = (int)brows;
-}
-
 struct MixAttempt {
   MColArgs c1, c2, c3;
   RowArgs<float> r1, r2, r3;
@@ -258,7 +164,6 @@ static MixAttempt build_mix(const void* plan32, const mjx_grid2d* g, const mjx_i
     return C;
   };
   c.C = tile(kColCap[1]);
-  c.err = &st->pad0;
   c.ys[0] = (float4*)(ws + L.ys0); c.ys[1] = (float4*)(ws + L.ys1);
   c.pa = (float4*)(ws + L.pa); c.pb = (float4*)(ws + L.pb);
   c.za = (float2*)(ws + L.za); c.zb = (float2*)(ws + L.zb);
@@ -277,22 +182,6 @@ static MixAttempt build_mix(const void* plan32, const mjx_grid2d* g, const mjx_i
     j.type = MC_FULL_END; A.c2.job[A.c2.njobs++] = j;
     j.type = MC_HALF_MID; A.c2.job[A.c2.njobs++] = j;
     j.type = MC_HALF_END; A.c3.job[A.c3.njobs++] = j;
-  }
-  for (MColArgs* ci : {&A.c1, &A.c2, &A.c3}) {
-    ci->stage_ops = 0;
-    ci->wide = 0;
-    for (int q = 0; q < ci->njobs; ++q) {
-      const int ty = ci->job[q].type;
-      ci->stage_ops = mc_nops(ty) > ci->stage_ops ? mc_nops(ty) : ci->stage_ops;
-      ci->wide |= (ty == MC_SPLIT || ty == MC_HALF_END) ? 1 : 0;
-    }
-  }
-  const MixTiles& tc = mix_tiles();
-  MColArgs* cs[3] = {&A.c1, &A.c2, &A.c3};
-  for (int i = 0; i < 3; ++i) {
-    MColArgs& ci = *cs[i];
-    if (tc.C[i] > 0 && 2 * tc.C[i] * (g->ny >= 16 ? g->ny / 16 : 1) <= 512) ci.C = tc.C[i];
-    if (tc.stage[i] && stage_ok(ci, ws, L, nf)) stage_maps(ci, ws, L, nf);
   }
   // row passes over the FP32 row spectra ZA/ZB (contiguous: ZB = ZA + zoff)
   const long long zoff = (long long)((L.zb - L.za) / sizeof(float2));
@@ -338,7 +227,7 @@ static MixAttempt build_mix(const void* plan32, const mjx_grid2d* g, const mjx_i
 
 static cudaError_t mcol(const MColArgs& c, cudaStream_t s) {
   const int tps = c.ny >= 16 ? c.ny / 16 : 1;
-  const size_t smem = mcol_smem(c);
+  const size_t smem = (size_t)sp_size(c.ny * 2 * c.C) * sizeof(float2);
   dim3 grid((c.ncols + c.C - 1) / c.C, c.njobs);
   const int nt = 2 * c.C * tps;
   if (nt <= 256) mcol_kernel<256, 4><<<grid, nt, smem, s>>>(c);
@@ -663,8 +552,6 @@ static mjx_status run_mixed(ImexMixedPlan& P, int io_dtype, double t0, double t_
   DevState out;
   MJX_CUDA_TRY(cudaMemcpyAsync(&out, st, sizeof(out), cudaMemcpyDeviceToHost, s));
   MJX_CUDA_TRY(cudaStreamSynchronize(s));
-  // a staged-operand wait that ran out (the pass fell back to global loads): report it
-  if (out.pad0) { set_last_error(cudaErrorTimeout, __FILE__, __LINE__); return MJX_CUDA_ERROR; }
   if (res) {
     res->t_final = out.t; res->dt_next = out.dt; res->prev_err = out.prev_err; res->last_err = out.err_last;
     res->n_accepted = out.n_acc; res->n_rejected = out.n_rej; res->n_attempts = out.attempts;

@@ -5,7 +5,6 @@
 #pragma once
 
 #include "spectral.cuh"
-#include "tma.cuh"
 
 namespace mjx {
 
@@ -80,12 +79,6 @@ struct MColTile {
   const float* lamy;
   const float2* tw;
   float hA, hB, nrm;        // dt/2 D, dt/4 D, 1/(nx ny)
-  // operands staged in shared memory by TMA (element e of the tile at index e), or null:
-  // the combine then reads global memory.  bar completes when they have arrived.
-  const float4* sp_p;       // the state operand (ys_cur, pa or pb)
-  const float4* sp_q;       // HALF_END: pa
-  unsigned long long* bar;
-  int* err;                 // set when the staged wait runs out (the global operands are used)
 };
 
 // One tile: C adjacent kx columns of one job over all ny rows.  Threads per CTA
@@ -128,14 +121,6 @@ __device__ __forceinline__ void mcol_tile(float2* buf, const MColTile& t, int ti
     fft_smem<float, false, true>(buf, ny, t.log2ny, Cn, 1, W, t.tw, tid);
   }
 
-  // the staged operands (issued by the kernel before the forward transform) must have arrived
-  const float4* sp_p = t.sp_p;
-  const float4* sp_q = t.sp_q;
-  if (t.bar != nullptr && !mbar_wait(t.bar, 0, 1 << 22)) {
-    if (tid == 0) atomicOr(t.err, 1);
-    sp_p = nullptr;
-    sp_q = nullptr;
-  }
   // float-float combine, element by element
 #pragma unroll
   for (int m = 0; m < 8; ++m) {
@@ -150,11 +135,10 @@ __device__ __forceinline__ void mcol_tile(float2* buf, const MColTile& t, int ti
     const long long g = t.off + ky * ldc + kx;
     const float lam = t.lamx[kx] + t.lamy[ky];
     float4 Pm, Qm;
-    if (sp_p != nullptr) Pm = sp_p[e];
-    else if (type == MC_SPLIT) Pm = t.ys_cur[g];
+    if (type == MC_SPLIT) Pm = t.ys_cur[g];
     else if (type == MC_FULL_END) Pm = t.pa[g];
     else Pm = t.pb[g];
-    if (type == MC_HALF_END) Qm = sp_q != nullptr ? sp_q[e] : t.pa[g];
+    if (type == MC_HALF_END) Qm = t.pa[g];
     if (type == MC_SPLIT) {
       const float4 PA = ff_mstep_c(Pm, mu_of(hA, lam)), PB = ff_mstep_c(Pm, mu_of(hB, lam));
       t.pa[g] = PA;

@@ -392,7 +392,16 @@ __global__ void __launch_bounds__(ColThreads<T>::v, 1) col_kernel(const __grid_c
 static size_t row_smem(int n, int nseq, int elem) { return (size_t)sp_size(nseq * n) * 2 * elem; }
 
 template <typename T, int RX>
-cudaError_t launch_row(const RowArgs<T>& a, cudaStream_t s) {
+cudaError_t launch_row(const RowArgs<T>& a0, cudaStream_t s) {
+  // Small grids: fewer row pairs per CTA until the pass covers every SM (the partial-sum
+  // passes keep their CTA count, which sizes the controller's reduction).  FP64 transforms
+  // are bound by the FP64 units, so a pass on a few SMs is a few times slower.
+  RowArgs<T> a = a0;
+  bool partials = false;
+  for (int q = 0; q < a.npairs && q < MJX_MAXPAIR; ++q)
+    partials |= (a.pr[q].flags & (ROW_ERRNORM | ROW_ERRPAIR)) != 0;
+  if (!partials)
+    while (a.nseq > 1 && a.npairs * a.nrows / a.nseq < 152) a.nseq >>= 1;
   const int tps = a.n >= 16 ? a.n / 16 : 1;
   const int grid = a.npairs * a.nrows / a.nseq;
   const size_t smem = row_smem(a.n, a.nseq, sizeof(T));
@@ -401,10 +410,14 @@ cudaError_t launch_row(const RowArgs<T>& a, cudaStream_t s) {
 }
 
 template <typename T>
-cudaError_t launch_col(const ColArgs<T>& a, cudaStream_t s) {
+cudaError_t launch_col(const ColArgs<T>& a0, cudaStream_t s) {
+  ColArgs<T> a = a0;
   int maxout = 1;
   for (int j = 0; j < a.njobs; ++j) maxout = a.job[j].nout > maxout ? a.job[j].nout : maxout;
   const int tps = a.ny >= 16 ? a.ny / 16 : 1;
+  // small grids: narrower tiles until the pass covers every SM (as launch_row)
+  const long long planes = a.nplanes > 1 ? a.nplanes : 1;
+  while (a.C > 1 && (long long)((a.ncols + a.C - 1) / a.C) * a.njobs * planes < 152) a.C >>= 1;
   dim3 grid((a.ncols + a.C - 1) / a.C, a.njobs, a.nplanes > 1 ? a.nplanes : 1);
   const size_t smem = (size_t)sp_size(a.ny * a.C * maxout) * sizeof(cx<T>);
   col_kernel<T><<<grid, a.C * maxout * tps, smem, s>>>(a);
