@@ -679,10 +679,10 @@ def explicit_cpu_baseline(n=1024, steps=48):
 
 
 def run_stencil(args, local):
-    """The stencil stage kernel alone (rk_stage_vec_kernel / rk_stage_kernel): one RK4
-    middle stage of the two-field advection-diffusion model of the explicit workload at
-    n^2, timed by the autotuner for each tile height (CUDA events, 20 launches each after
-    a warm-up launch).  Algorithmic bytes per point and field: stage input, step start and
+    """The stencil stage kernel alone (rk_stage_tma_kernel / rk_stage_vec_kernel /
+    rk_stage_kernel): one RK4 middle stage of the two-field advection-diffusion model of
+    the explicit workload at n^2, timed by the autotuner for each tile height and the
+    TMA-staged form (64; FP32) (CUDA events, 20 launches each after a warm-up launch).  Algorithmic bytes per point and field: stage input, step start and
     running sum read, two outputs written = 5 accesses (20 B in FP32, 40 B in FP64); the
     5-point neighbours come from cache."""
     import torch
@@ -701,7 +701,8 @@ def run_stencil(args, local):
     t = min(res.times_ms) * 1e-3
     return {"workload": f"stencil stage (RK4 middle stage) advection-diffusion 2 fields {n}x{n} "
                         f"{'FP32' if dtype == torch.float32 else 'FP64'}",
-            "n": n, "kernel": "rk_stage_vec_kernel" if n % (16 // esz) == 0 else "rk_stage_kernel",
+            "n": n, "kernel": ("rk_stage_tma_kernel" if res.choice[0] == 64 else
+                               "rk_stage_vec_kernel" if n % (16 // esz) == 0 else "rk_stage_kernel"),
             "tile_heights": [c[0] for c in res.candidates], "ms_per_launch": res.times_ms,
             "best_rows": res.choice[0], "alg_bytes": b,
             "roofline": {"bound": "hbm", "achieved": b / t / 1e9, "peak": peak, "peak_kind": peak_kind,

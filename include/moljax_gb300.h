@@ -57,6 +57,7 @@ typedef enum mjx_mult {
   MJX_MULT_ADV_SOLVE = 16, /* 1/(1 - z), |1 - z| clamped at 1e-14 */
   MJX_MULT_ADV_LAP = 17,   /* z */
   MJX_MULT_ADV_EXP = 18,   /* exp(z) */
+  MJX_MULT_ADV_CN = 20,    /* (1 + z/2)/(1 - z/2) */
   MJX_MULT_TABLE = 19      /* a real table [ny][nx] on the full spectrum */
 } mjx_mult;
 
@@ -188,9 +189,11 @@ mjx_status mjx_advdiff_apply2d(const void* plan, const mjx_grid2d* grid, int dty
 
 /* The periodic advection-diffusion operator L = D Lap - v.grad with the symbol
  * D lam - i (vx kx + vy ky) (kx, ky = 2 pi fftfreq): op 0 solves (I - h L) u = in
- * (as mjx_advdiff_apply2d), op 1 applies h L, op 2 applies exp(h L); out = the real part
+ * (as mjx_advdiff_apply2d), op 1 applies h L, op 2 applies exp(h L), op 3 one
+ * Crank-Nicolson step (I - h L/2)^-1 (I + h L/2); out = the real part
  * (AdvectionDiffusionOperator, moljax/core/fft_operators.py:179-260: solve, matvec with
- * h = 1, exp_matvec).  Fields with D <= 1e-14 and |v| <= 1e-14 are copied (ops 0, 2)
+ * h = 1, exp_matvec; the 1D advective FFT-CN of
+ * benchmarks/benchmark_solver_comparison.py:152-163).  Fields with D <= 1e-14 and |v| <= 1e-14 are copied (ops 0, 2)
  * or zeroed (op 1). */
 mjx_status mjx_advdiff_op2d(const void* plan, const mjx_grid2d* grid, int dtype, int nfields,
                             const double* D, const double* vx, const double* vy, double h, int op,
@@ -498,9 +501,15 @@ typedef enum mjx_reactor_variant {
   MJX_REACTOR_DANCKWERTS = 0, /* benchmarks/benchmark_reactor_vs_diffrax.py:40-138 (dispersion CN,
                                  upwind advection and reaction explicit: needs dt <= dz) */
   MJX_REACTOR_DIRICHLET = 1,  /* benchmarks/benchmark_method_comparison.py:56-160 */
-  MJX_REACTOR_DANCKWERTS_CN = 2 /* the Danckwerts discretisation of variant 0 advanced by the fully
+  MJX_REACTOR_DANCKWERTS_CN = 2, /* the Danckwerts discretisation of variant 0 advanced by the fully
                                    implicit CN of benchmark_method_comparison.py:134-160 (stable at
                                    its CN step dt = min(10 dz, 0.05, t_final/100), line 216) */
+  /* benchmarks/benchmark_tubular_reactor.py:57-200: N nodes, dz = 1/(N-1), classical RK4 of
+     (1/Pe) D2 c - D1 c - Da c with the end rows replaced by penalties 100 (target - c)
+     (mjx_reactor_rk4_batch only) */
+  MJX_REACTOR_RK4_DANCKWERTS = 3, /* inlet (c_in + k c1)/(1 + k), k = 1/(Pe dz); outlet c_{N-2} */
+  MJX_REACTOR_RK4_ROBIN = 4,      /* alpha_in = 1, beta_in = 1/Pe, alpha_out = 0, beta_out = 1 */
+  MJX_REACTOR_RK4_NEUMANN = 5     /* inlet c1, outlet c_{N-2} */
 } mjx_reactor_variant;
 
 /* One reactor solve of c_t = c_zz/Pe - c_z - Da c: n points, n_steps fixed CN
@@ -523,6 +532,15 @@ size_t mjx_reactor_smem_bytes(int n, int dtype);
  * a tridiagonal factorisation plus two parallel substitution scans per step. */
 mjx_status mjx_reactor_cn_batch(const mjx_reactor_instance* inst_dev, int n_inst, int max_n,
                                 int dtype, void* out, void* stream);
+/* n_inst penalty-BC RK4 reactor solves (variants MJX_REACTOR_RK4_*; c_init the uniform
+ * initial state, c_inlet the inlet value c_in; 3 <= n <= max_n, max_n <= 1024 FP32 or 512
+ * FP64) in one launch, one warp per instance with the whole state in registers.  Replaces
+ * solve_rk4 with
+ * create_rhs_danckwerts / create_rhs_robin / create_rhs_neumann
+ * (benchmarks/benchmark_tubular_reactor.py:84-192, 254-301), whose RHS is a dense n x n
+ * matvec.  An instance of another variant or an n outside [3, max_n] comes back as NaN. */
+mjx_status mjx_reactor_rk4_batch(const mjx_reactor_instance* inst_dev, int n_inst, int max_n,
+                                 int dtype, void* out, void* stream);
 
 /* ---- ETDRK4 (Cox-Matthews) for coupled Gray-Scott ------------------------------ */
 /* Workspace: row spectra ZU/ZN/ZX, 2D spectra U^/N^u/a^/S and the coefficient tables. */
@@ -732,13 +750,16 @@ mjx_status mjx_autotune_dft(const void* plan, int n, int dtype, long long nrows,
                             size_t scratch_bytes, int reps, double* times, int max_times, int* n_cand,
                             int* best, void* stream);
 /* Installs the rows per warp strip (2, 4, 8, 16 or 32; 0 = default 8) of the explicit
- * stage kernel for this grid size, field count and dtype. */
+ * stage kernel for this grid size, field count and dtype; 64 selects the TMA-staged
+ * form (shared-memory tiles of 32 x 128 points loaded by cp.async.bulk.tensor), used
+ * for FP32 stages whose rows are a multiple of 4 points (others run with 8). */
 mjx_status mjx_stencil_rows_set(int ny, int nx, int nfields, int dtype, int rows);
 /* The installed rows per warp strip (0 when untuned). */
 int mjx_stencil_rows_get(int ny, int nx, int nfields, int dtype);
-/* Times an RK4 middle stage of prob on grid for strips of 2, 4, 8, 16 and 32 rows
- * (reps launches each, CUDA events) in ws (mjx_explicit_ws_bytes; overwritten),
- * installs the fastest and returns it with up to max_times times (ms per launch). */
+/* Times an RK4 middle stage of prob on grid for strips of 2, 4, 8, 16 and 32 rows and,
+ * for FP32 with nx a multiple of 4, the TMA-staged form (64) (reps launches each, CUDA
+ * events) in ws (mjx_explicit_ws_bytes; overwritten), installs the fastest and returns
+ * it with up to max_times times (ms per launch, candidate order). */
 mjx_status mjx_autotune_stencil2d(const mjx_grid2d* grid, int dtype, const mjx_explicit_problem* prob,
                                   void* ws, size_t ws_bytes, int reps, double* times, int max_times,
                                   int* best_rows, void* stream);

@@ -27,7 +27,7 @@ STATUS_NAMES = {
 F32, F64 = 0, 1
 SYMBOL_FD, SYMBOL_SPECTRAL = 0, 1
 MULT_SCALE, MULT_HELMHOLTZ, MULT_CN, MULT_EXP, MULT_LAP = 0, 1, 2, 3, 5
-MULT_ADV_SOLVE, MULT_ADV_LAP, MULT_ADV_EXP, MULT_TABLE = 16, 17, 18, 19
+MULT_ADV_SOLVE, MULT_ADV_LAP, MULT_ADV_EXP, MULT_TABLE, MULT_ADV_CN = 16, 17, 18, 19, 20
 REACT_NONE, REACT_GRAY_SCOTT, REACT_FISHER, REACT_KINETICS = 0, 1, 2, 3
 SYMBOL_X_ONLY = 0x10
 ETD_1, ETD_2, ETD_RK4 = 1, 2, 4
@@ -140,6 +140,7 @@ SIGNATURES = {
                                  C.POINTER(AdaptiveResultC), _vp]),
     "mjx_reactor_smem_bytes": (_sz, [_i, _i]),
     "mjx_reactor_cn_batch": (_i, [_vp, _i, _i, _i, _vp, _vp]),
+    "mjx_reactor_rk4_batch": (_i, [_vp, _i, _i, _i, _vp, _vp]),
     "mjx_nk_vardiff_ws_bytes": (_sz, [_i, _i]),
     "mjx_nk_vardiff_integrate2d": (_i, [_vp, _i, _d, _d, C.POINTER(C.c_double), _i, _d, _i, _i,
                                         C.POINTER(NKParamsC), _vp, _vp, C.POINTER(C.c_int), _vp, _sz,

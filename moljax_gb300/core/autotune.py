@@ -164,7 +164,8 @@ def set_stencil_rows(ny: int, nx: int, nfields: int, dtype: torch.dtype, rows: i
 def autotune_stencil(model, dtype: Optional[torch.dtype] = None, reps: int = 5, method: int = 2,
                      device=None) -> TuneResult:
     """Time the stage kernel of ``model`` (an explicit-stepper MOLModel) for strips of
-    2, 4, 8, 16 and 32 rows and install the fastest for its grid size."""
+    2, 4, 8, 16 and 32 rows and, for FP32 grids whose rows are a multiple of 4 points,
+    the TMA-staged form (64), and install the fastest for its grid size."""
     from moljax_gb300.core.fft_solvers import workspace
     from moljax_gb300.core.stepping import explicit_problem
     N.require_cuda()
@@ -176,16 +177,17 @@ def autotune_stencil(model, dtype: Optional[torch.dtype] = None, reps: int = 5, 
     code = N.dtype_code(dtype)
     prob = explicit_problem(model, method, t=0.0)
     ws = workspace(lib.mjx_explicit_ws_bytes(grid.ny, grid.nx, len(names), code), dev, "explicit")
-    times = (C.c_double * 5)()
+    times = (C.c_double * 6)()
     best = C.c_int()
     with torch.cuda.device(dev):
         N.check("mjx_autotune_stencil2d", lib.mjx_autotune_stencil2d(
             C.byref(N.Grid2DC(grid.ny, grid.nx, grid.dy, grid.dx)), code, C.byref(prob), N.ptr(ws), ws.numel(),
-            int(reps), times, 5, C.byref(best), N.stream_ptr(dev)))
-    cands = [(r,) for r in (2, 4, 8, 16, 32)]
+            int(reps), times, 6, C.byref(best), N.stream_ptr(dev)))
+    tma = dtype == torch.float32 and grid.nx % 4 == 0
+    cands = [(r,) for r in ((2, 4, 8, 16, 32, 64) if tma else (2, 4, 8, 16, 32))]
     _RECORD[f"rows/{grid.ny}/{grid.nx}/{len(names)}/{code}"] = {"rows": best.value}
     _STENCIL_DONE.add((grid.ny, grid.nx, len(names), code))
-    return TuneResult((best.value,), cands, list(times), cands.index((best.value,)))
+    return TuneResult((best.value,), cands, list(times)[:len(cands)], cands.index((best.value,)))
 
 
 def tune_stencil_once(model, dtype: torch.dtype) -> None:

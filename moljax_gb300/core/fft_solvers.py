@@ -463,6 +463,60 @@ def fft_cn_step(u0: torch.Tensor, D: float, dx: float, dt: float, n_steps: int =
     return out
 
 
+def _advdiff_1d_apply(plan, x, D: float, v: float, h: float, op: int, out: torch.Tensor):
+    """One mjx_advdiff_op2d call on the two identical rows of a 1D field (op 0 solve, 1 h L,
+    2 exp(h L), 3 one CN step); the general-size path for other lengths."""
+    if getattr(plan, "general", False):
+        mult = (N.MULT_ADV_SOLVE, N.MULT_ADV_LAP, N.MULT_ADV_EXP, N.MULT_ADV_CN)[op]
+        return plan.apply(x, float(D), h, mult, out=out, vx=float(v), vy=0.0)
+    ws = workspace(plan.ws_bytes(1), plan.device)
+    D_ = (C.c_double * 1)(float(D))
+    vx_ = (C.c_double * 1)(float(v))
+    vy_ = (C.c_double * 1)(0.0)
+    N.check("mjx_advdiff_op2d", N.lib().mjx_advdiff_op2d(
+        N.ptr(plan.buf), C.byref(plan.cgrid), plan.code, 1, D_, vx_, vy_, float(h), int(op),
+        N.ptr(x), N.ptr(out), N.ptr(ws), ws.numel(), N.stream_ptr(plan.device)))
+    return out
+
+
+def fft_cn_advdiff_1d(u0: torch.Tensor, D: float, v: float, dx: float, dt: float, n_steps: int = 1,
+                      symbol: str = "spectral") -> torch.Tensor:
+    """Crank-Nicolson steps of the periodic 1D advection-diffusion u_t = D u_xx - v u_x,
+    u <- real(ifft(G fft(u))), G = (1 + dt L/2)/(1 - dt L/2), L = D lam - i v k
+    (benchmarks/benchmark_solver_comparison.py:145-176, fft_cn_step / fft_cn_solve;
+    pseudo-spectral lam = -k^2 by default, as the benchmark).  One native transform pair per
+    step (``mjx_advdiff_op2d`` op 3)."""
+    u = u0.contiguous()
+    N.require_cuda(u)
+    if u.ndim != 1:
+        raise ValueError("fft_cn_advdiff_1d: a field of shape (nx,)")
+    plan = get_plan(2, u.shape[0], dx, dx, symbol, u.dtype, u.device)
+    a, b = torch.stack([u, u]), torch.empty(2, u.shape[0], dtype=u.dtype, device=u.device)
+    for _ in range(int(n_steps)):
+        _advdiff_1d_apply(plan, a, D, v, dt, 3, b)
+        a, b = b, a
+    return a[0].clone()
+
+
+def imex_advdiff_1d(u0: torch.Tensor, D: float, v: float, dx: float, dt: float, n_steps: int = 1,
+                    symbol: str = "spectral") -> torch.Tensor:
+    """Exponential Strang steps of u_t = D u_xx - v u_x: exp(dt/2 (-i v k)), exp(dt D lam),
+    exp(dt/2 (-i v k)), each a transform pair keeping the real part
+    (benchmarks/benchmark_solver_comparison.py:184-215, imex_step / imex_solve)."""
+    u = u0.contiguous()
+    N.require_cuda(u)
+    if u.ndim != 1:
+        raise ValueError("imex_advdiff_1d: a field of shape (nx,)")
+    plan = get_plan(2, u.shape[0], dx, dx, symbol, u.dtype, u.device)
+    a, b = torch.stack([u, u]), torch.empty(2, u.shape[0], dtype=u.dtype, device=u.device)
+    for _ in range(int(n_steps)):
+        _advdiff_1d_apply(plan, a, 0.0, v, 0.5 * dt, 2, b)
+        _advdiff_1d_apply(plan, b, D, 0.0, dt, 2, a)
+        _advdiff_1d_apply(plan, a, 0.0, v, 0.5 * dt, 2, b)
+        a, b = b, a
+    return a[0].clone()
+
+
 def gray_scott_cn_newton(u0: torch.Tensor, v0: torch.Tensor, Du: float, Dv: float, F: float, k: float,
                          dt: float, n_steps: int, dx: float, dy: Optional[float] = None, tol: float = 1e-8,
                          max_iter: int = 10, symbol: str = "spectral"):

@@ -18,6 +18,8 @@ import torch
 from moljax_gb300 import _native as N
 
 DANCKWERTS, DIRICHLET, DANCKWERTS_CN = 0, 1, 2
+RK4_DANCKWERTS, RK4_ROBIN, RK4_NEUMANN = 3, 4, 5
+RK4_VARIANTS = {"danckwerts": RK4_DANCKWERTS, "robin": RK4_ROBIN, "neumann": RK4_NEUMANN}
 
 
 @dataclass
@@ -40,9 +42,14 @@ def served_dt(n: int, t_final: float = 5.0):
 
 
 def solve_batch(cases: Sequence[ReactorCase], dtype=torch.float32, device="cuda", stream=None):
-    """All cases in one launch; returns a list of final concentration profiles."""
+    """All cases in one launch; returns a list of final concentration profiles.  Cases of
+    the penalty-RK4 variants (RK4_*) go through ``mjx_reactor_rk4_batch`` (all cases of
+    one call must then be RK4 ones), the others through ``mjx_reactor_cn_batch``."""
     if not cases:
         return []
+    rk4 = [c.variant >= RK4_DANCKWERTS for c in cases]
+    if any(rk4) and not all(rk4):
+        raise ValueError("solve_batch: RK4 and CN reactor cases go in separate batches")
     offs, o = [], 0
     arr = (N.ReactorInstanceC * len(cases))()
     for i, c in enumerate(cases):
@@ -55,7 +62,8 @@ def solve_batch(cases: Sequence[ReactorCase], dtype=torch.float32, device="cuda"
     inst = raw.to(dev, non_blocking=False)
     out = torch.empty(o, dtype=dtype, device=dev)
     s = C.c_void_p(stream if stream is not None else torch.cuda.current_stream(dev).cuda_stream)
-    N.check("mjx_reactor_cn_batch", N.lib().mjx_reactor_cn_batch(
+    entry = "mjx_reactor_rk4_batch" if rk4[0] else "mjx_reactor_cn_batch"
+    N.check(entry, getattr(N.lib(), entry)(
         N.ptr(inst), len(cases), max(c.n for c in cases), N.dtype_code(dtype), N.ptr(out), s))
     res = [out[offs[i]:offs[i] + c.n] for i, c in enumerate(cases)]
     return res
@@ -66,3 +74,64 @@ def tubular_reactor_cn(n: int, Pe: float, Da: float, dt: float, n_steps: int,
     """One solve (solve_reactor_cn_jit / run_reactor_cn semantics)."""
     v = DANCKWERTS if variant == "danckwerts" else DIRICHLET
     return solve_batch([ReactorCase(n, Pe, Da, dt, n_steps, v, c_init)], dtype)[0]
+
+
+def tubular_rk4_dt(n: int, Pe: float, t_final: float):
+    """dt = min(0.5 dz, 0.25 Pe dz^2, 0.01), n_steps = int(t_final / dt), dz = 1/(n-1)
+    (benchmarks/benchmark_tubular_reactor.py:283-286)."""
+    dz = 1.0 / (n - 1)
+    dt = min(0.5 * dz, 0.25 * Pe * dz ** 2, 0.01)
+    return dt, int(t_final / dt)
+
+
+def tubular_rk4_case(Pe: float, Da: float, bc_type: str, N: int = 128, t_final: float = 10.0,
+                     c_in: float = 1.0) -> ReactorCase:
+    """The case ``run_single_benchmark(Pe, Da, bc_type, N, t_final)`` of
+    benchmarks/benchmark_tubular_reactor.py:254-301 runs: zeros (Danckwerts, Robin) or ones
+    (Neumann) at t = 0, the CFL step, RK4 to t_final."""
+    if bc_type not in RK4_VARIANTS:
+        raise ValueError(f"Unknown BC type: {bc_type}")
+    dt, n_steps = tubular_rk4_dt(N, Pe, t_final)
+    return ReactorCase(N, Pe, Da, dt, n_steps, RK4_VARIANTS[bc_type],
+                       1.0 if bc_type == "neumann" else 0.0, c_in)
+
+
+def reactor_summary(c: torch.Tensor, Pe: float, Da: float, bc_type: str, t_final: float):
+    """conversion (1 - outlet; the mean for Neumann), max error against the analytic
+    profile (Danckwerts steady state, or e^{-Da t} for Neumann) and the outlet value
+    (benchmarks/benchmark_tubular_reactor.py:207-235, 294-296), computed on the host in FP64."""
+    import numpy as np
+    c = c.detach().double().cpu().numpy()
+    n = c.shape[-1]
+    z = np.linspace(0, 1, n)
+    if bc_type == "neumann":
+        ref = np.exp(-Da * t_final) * np.ones(n)
+        conv = float(c.mean())
+    else:
+        disc = Pe ** 2 + 4 * Pe * Da
+        r1, r2 = (Pe + np.sqrt(disc)) / 2, (Pe - np.sqrt(disc)) / 2
+        a, b = np.linalg.solve(np.array([[r1 / Pe - 1, r2 / Pe - 1], [r1 * np.exp(r1), r2 * np.exp(r2)]]),
+                               np.array([-1.0, 0.0]))
+        ref = a * np.exp(r1 * z) + b * np.exp(r2 * z)
+        conv = float(1.0 - c[-1])
+    return {"conversion": conv, "error": float(np.max(np.abs(c - ref))), "final_outlet_c": float(c[-1])}
+
+
+def run_tubular_sweep(bc_types=("danckwerts", "robin", "neumann"), Pe_values=(1, 10, 100),
+                      Da_values=(0.1, 1, 10), N: int = 128, t_final: float = 15.0, dtype=torch.float64,
+                      device="cuda"):
+    """Every (BC, Pe, Da) case of run_full_sweep (benchmarks/benchmark_tubular_reactor.py:304-329)
+    in one launch; returns {"<bc>_Pe<Pe>_Da<Da>": summary + dt + n_steps}."""
+    keys, cases = [], []
+    for bc in bc_types:
+        for Pe in Pe_values:
+            for Da in Da_values:
+                keys.append((bc, Pe, Da))
+                cases.append(tubular_rk4_case(Pe, Da, bc, N, t_final))
+    outs = solve_batch(cases, dtype, device)
+    res = {}
+    for (bc, Pe, Da), case, c in zip(keys, cases, outs):
+        r = reactor_summary(c, Pe, Da, bc, t_final)
+        r.update(bc_type=bc, Pe=Pe, Da=Da, dt=case.dt, n_steps=case.n_steps)
+        res[f"{bc}_Pe{Pe}_Da{Da}"] = r
+    return res

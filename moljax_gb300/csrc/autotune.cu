@@ -129,7 +129,9 @@ mjx_status mjx_stencil_rows_set(int ny, int nx, int nfields, int dtype, int rows
   const int e = elem_size(dtype);
   if (!e) return MJX_BAD_DTYPE;
   if (ny < 1 || nx < 1 || nfields < 1 || nfields > 4) return MJX_BAD_ARG;
-  if (rows != 0 && rows != 2 && rows != 4 && rows != 8 && rows != 16 && rows != 32) return MJX_BAD_ARG;
+  // 64 selects the TMA-staged form (FP32 with 16-byte rows; other stages fall back to 8)
+  if (rows != 0 && rows != 2 && rows != 4 && rows != 8 && rows != 16 && rows != 32 && rows != 64)
+    return MJX_BAD_ARG;
   tune_rows_put(ny, nx, nfields, e, rows);
   return MJX_OK;
 }

@@ -319,7 +319,8 @@ __global__ void general_mult_kernel(cx<T>* __restrict__ s, const T* __restrict__
         fr = dr / den; fi = -di / den;
         break;
       }
-      case MJX_MULT_CN: {
+      case MJX_MULT_CN:
+      case MJX_MULT_ADV_CN: {
         const double nr = 1.0 + 0.5 * zr, ni = 0.5 * zi, dr = 1.0 - 0.5 * zr, di = -0.5 * zi;
         const double den = dr * dr + di * di;
         fr = (nr * dr + ni * di) / den; fi = (ni * dr - nr * di) / den;
@@ -585,7 +586,8 @@ mjx_status mjx_spectral_apply_general2d(const void* plan_y, const void* plan_x, 
   if (symbol != MJX_SYMBOL_FD && symbol != MJX_SYMBOL_SPECTRAL) return MJX_BAD_ARG;
   const bool ok_mult = mult == MJX_MULT_SCALE || mult == MJX_MULT_HELMHOLTZ || mult == MJX_MULT_CN ||
                        mult == MJX_MULT_EXP || mult == MJX_MULT_LAP || mult == MJX_MULT_TABLE ||
-                       mult == MJX_MULT_ADV_SOLVE || mult == MJX_MULT_ADV_LAP || mult == MJX_MULT_ADV_EXP;
+                       mult == MJX_MULT_ADV_SOLVE || mult == MJX_MULT_ADV_LAP || mult == MJX_MULT_ADV_EXP ||
+                       mult == MJX_MULT_ADV_CN;
   if (!ok_mult || (mult == MJX_MULT_TABLE && !table)) return MJX_BAD_ARG;
   if (!ws || ws_bytes < mjx_spectral_general2d_ws_bytes(g->ny, g->nx, nfields, dtype)) return MJX_WORKSPACE;
   MJX_TRY(set_dft_attrs());

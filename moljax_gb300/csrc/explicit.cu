@@ -26,6 +26,7 @@
 
 #include "spectral.cuh"
 #include "autotune.cuh"
+#include "tma.cuh"
 
 namespace mjx {
 
@@ -688,6 +689,293 @@ static void x_coef(XStage<T>& s) {
   }
 }
 
+// TMA-staged form of the stage kernel (FP32, nx a multiple of 4): a CTA loops over tiles of
+// XT_H rows by XT_W columns; the stage input W of every field comes into shared memory as one
+// 3D box per field with a one-row and a four-column halo (four columns keep the box start on a
+// 16-byte boundary), two tiles in flight (the next tile's copies are issued before the
+// current one is computed).  Boxes that reach past the grid are zero-filled by the copy; the
+// ghost cells the 5-point stencil needs there are written from the BC formulas (periodic:
+// the wrapped row or column from global memory).  The combine operands and the outputs use
+// 128-bit loads and stores.  Same arithmetic per point as the scalar kernel.  A tile whose
+// copies never arrive (a bounded wait) produces NaN, which the error norm reports.
+enum { XT_W = 128, XT_H = 32, XT_SW = XT_W + 8, XT_SH = XT_H + 2, XT_TMA_ROWS = 64 };
+// a tensor copy writes shared memory at 128-byte aligned addresses: each field's box
+// (XT_SH x XT_SW floats, 18 496 bytes) sits in a slot rounded up to 128 bytes
+enum { XT_BOX = XT_SH * XT_SW, XT_SLOT = (XT_BOX + 31) / 32 * 32 };
+static_assert((XT_SLOT * 4) % 128 == 0, "TMA slots must keep 128-byte alignment");
+
+struct XTmaMaps {
+  CUtensorMap m[XB_NBUF];  // [nf][ny][nx] FP32 views of the stage buffers, boxes XT_SW x XT_SH x 1
+};
+
+// 128 bytes of alignment slack, 128 for the barriers, two tiles of NF field slots
+static size_t x_tma_smem(int NF) { return 256 + 2 * (size_t)NF * XT_SLOT * sizeof(float); }
+
+template <int RX, int NF>
+__global__ void __launch_bounds__(256, NF == 2 ? 3 : 1)
+rk_stage_tma_kernel(const __grid_constant__ XStage<float> a, const __grid_constant__ XTmaMaps tm) {
+  typedef float T;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
+  // the dynamic region follows the static arrays: align its use to 128 bytes explicitly
+  unsigned char* smem_base = smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u);
+  unsigned long long* bar = reinterpret_cast<unsigned long long*>(smem_base);  // two barriers
+  float* stg = reinterpret_cast<float*>(smem_base + 128);  // [2][NF] slots of [XT_SH][XT_SW]
+  const DevState* st = a.st;
+  if (st != nullptr && st->done) return;
+  const XModel& m = a.m;
+  const int cur = st != nullptr ? st->cur : 0;
+  const XCoef<T>& k = a.k;
+  const T h = st != nullptr ? (T)st->dtc * k.hfac : k.hfixed;
+  const T* W = xbuf(a, a.w, cur);
+  const int wid = a.w == XB_YCUR ? cur : (a.w == XB_YNEXT ? 1 - cur : a.w);
+  const bool hasP = a.p >= 0, hasQ = a.q >= 0;
+  const T* P = hasP ? xbuf(a, a.p, cur) : W;
+  const T* Q = hasQ ? xbuf(a, a.q, cur) : W;
+  T* O1 = xbuf(a, a.o1, cur);
+  T* O2 = a.o2 >= 0 ? xbuf(a, a.o2, cur) : nullptr;
+  const T* YF = a.buf[XB_YF];
+  const int nf = m.nf, ny = m.ny, nx = m.nx, adv = m.advection;
+  const long long per = (long long)ny * nx;
+  const T idx2 = k.idx2, idy2 = k.idy2, idx = k.idx, idy = k.idy, vx = k.vx, vy = k.vy;
+  const bool vxpos = k.vxpos != 0, vypos = k.vypos != 0;
+  const T cp1 = k.cp1, cq1 = k.cq1, cf1h = k.cf1 * h;
+  const T cp2 = k.cp2, cq2 = k.cq2, cf2h = k.cf2 * h;
+  const T rF = k.F, rFk = k.Fk, rr = k.r;
+  const int lane = threadIdx.x, warp = threadIdx.y, tid = warp * 32 + lane;
+  const int ntx = (nx + XT_W - 1) / XT_W, nty = (ny + XT_H - 1) / XT_H, ntiles = ntx * nty;
+  const int fsz = XT_SLOT;
+  const CUtensorMap* mw = &tm.m[wid];
+  if ((smem_u32(stg) & 127u) != 0) {  // guard: no tensor copy to a misaligned slot
+    if (a.err && tid == 0) {
+      a.partial[blockIdx.x] = __longlong_as_double(0x7ff8000000000000ll);
+      a.nonfinite[blockIdx.x] = 1;
+    }
+    return;
+  }
+  if (tid == 0) { mbar_init(&bar[0], 1); mbar_init(&bar[1], 1); }
+  __syncthreads();
+  auto issue = [&](int tile, int sb) {  // thread 0: the boxes of every field of a tile
+    const int ty = tile / ntx, tx = tile - ty * ntx;
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // earlier ghost stores first
+    mbar_arrive_expect_tx(&bar[sb], (unsigned)(nf * XT_BOX * sizeof(float)));
+    for (int f = 0; f < nf; ++f)
+      tma_load_3d(stg + (size_t)(sb * NF + f) * fsz, mw, tx * XT_W - 4, ty * XT_H - 1, f, &bar[sb]);
+  };
+  if (tid == 0 && (int)blockIdx.x < ntiles) issue(blockIdx.x, 0);
+  T esum = (T)0;
+  int bad = 0;
+  int it = 0;
+  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
+    const int sb = it & 1;
+    if (tid == 0 && tile + (int)gridDim.x < ntiles) issue(tile + gridDim.x, sb ^ 1);
+    // block-uniform: every thread leaves the loop together when the copies never land
+    const bool arrived = __syncthreads_and(mbar_wait(&bar[sb], (it >> 1) & 1, 1 << 22)) != 0;
+    const int ty = tile / ntx, tx = tile - ty * ntx;
+    const int x0 = tx * XT_W, y0 = ty * XT_H;
+    const int lxe = nx - x0 < XT_W ? nx - x0 : XT_W;  // valid columns / rows of the tile
+    const int lye = ny - y0 < XT_H ? ny - y0 : XT_H;
+    // ghost cells at the grid edges (the box holds zeros there)
+    for (int f = 0; f < nf && arrived; ++f) {
+      T* S = stg + (size_t)(sb * NF + f) * fsz;
+      const int kind = m.kind[f];
+      const T* wf = W + f * per;
+      if (y0 == 0 && tid < lxe) {  // row -1
+        const T v = kind == MJX_BC_PERIODIC ? wf[(long long)(ny - 1) * nx + x0 + tid] : S[XT_SW + 4 + tid];
+        S[4 + tid] = kind == MJX_BC_PERIODIC ? v : xghost(v, kind, k.gv[f][2], true);
+      }
+      if (y0 + lye == ny && tid >= 128 && tid - 128 < lxe) {  // row ny
+        const int c = tid - 128;
+        const T v = kind == MJX_BC_PERIODIC ? wf[x0 + c] : S[lye * XT_SW + 4 + c];
+        S[(lye + 1) * XT_SW + 4 + c] = kind == MJX_BC_PERIODIC ? v : xghost(v, kind, k.gv[f][3], false);
+      }
+      if (x0 == 0 && tid < lye) {  // column -1
+        const T v = kind == MJX_BC_PERIODIC ? wf[(long long)(y0 + tid) * nx + nx - 1] : S[(tid + 1) * XT_SW + 4];
+        S[(tid + 1) * XT_SW + 3] = kind == MJX_BC_PERIODIC ? v : xghost(v, kind, k.gv[f][0], true);
+      }
+      if (x0 + lxe == nx && tid >= 64 && tid - 64 < lye) {  // column nx
+        const int r = tid - 64;
+        const T v = kind == MJX_BC_PERIODIC ? wf[(long long)(y0 + r) * nx] : S[(r + 1) * XT_SW + 4 + lxe - 1];
+        S[(r + 1) * XT_SW + 4 + lxe] = kind == MJX_BC_PERIODIC ? v : xghost(v, kind, k.gv[f][1], false);
+      }
+    }
+    __syncthreads();
+    const int lx = lane * 4;
+    const bool colv = lx < lxe;
+    const T nanv = __int_as_float(0x7fc00000);
+#pragma unroll
+    for (int j = 0; j < XT_H / XWARPS; ++j) {
+      const int ly = warp * (XT_H / XWARPS) + j;
+      const bool valid = colv && ly < lye;
+      const long long row = (long long)(y0 + ly) * nx;
+      T c[NF][4], Fv[NF][4];
+#pragma unroll
+      for (int f = 0; f < NF; ++f) {
+        if (f >= nf) break;
+        const T* S = stg + (size_t)(sb * NF + f) * fsz;
+        const float4 cv4 = *reinterpret_cast<const float4*>(S + (ly + 1) * XT_SW + 4 + lx);
+        const float4 up4 = *reinterpret_cast<const float4*>(S + ly * XT_SW + 4 + lx);
+        const float4 dn4 = *reinterpret_cast<const float4*>(S + (ly + 2) * XT_SW + 4 + lx);
+        T lft = __shfl_up_sync(0xffffffffu, cv4.w, 1);
+        T rgt = __shfl_down_sync(0xffffffffu, cv4.x, 1);
+        if (lane == 0) lft = S[(ly + 1) * XT_SW + 3];
+        if (lane == 31 || lx + 4 >= lxe) rgt = S[(ly + 1) * XT_SW + 4 + lx + 4];
+        const T cc[4] = {cv4.x, cv4.y, cv4.z, cv4.w};
+        const T uu[4] = {up4.x, up4.y, up4.z, up4.w};
+        const T dd[4] = {dn4.x, dn4.y, dn4.z, dn4.w};
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const T cvq = cc[q], ym = uu[q], yp = dd[q];
+          const T xm = q > 0 ? cc[q > 0 ? q - 1 : 0] : lft;
+          const T xp = q < 3 ? cc[q < 3 ? q + 1 : 0] : rgt;
+          T v = k.D[f] * ((xp - (T)2 * cvq + xm) * idx2 + (yp - (T)2 * cvq + ym) * idy2);
+          if (adv == 1) {
+            const T gx = vxpos ? (cvq - xm) * idx : (xp - cvq) * idx;
+            const T gy = vypos ? (cvq - ym) * idy : (yp - cvq) * idy;
+            v = v - vx * gx - vy * gy;
+          } else if (adv == 2) {
+            v = v - vx * (xp - xm) * (T)0.5 * idx - vy * (yp - ym) * (T)0.5 * idy;
+          }
+          c[f][q] = arrived ? cvq : nanv;
+          Fv[f][q] = arrived ? v : nanv;
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        if (RX == RX_GRAY_SCOTT) {  // operators.py:644-667
+          const T uvv = c[0][q] * c[1][q] * c[1][q];
+          Fv[0][q] += -uvv + rF * ((T)1 - c[0][q]);
+          Fv[1][q] += uvv - rFk * c[1][q];
+        } else if (RX == RX_FISHER) {  // operators.py:680-705
+#pragma unroll
+          for (int f = 0; f < NF; ++f) {
+            if (f >= nf) break;
+            Fv[f][q] += rr * c[f][q] * ((T)1 - c[f][q]);
+          }
+        } else if (RX == RX_KINETICS) {
+          T cq[NF], fq[NF];
+#pragma unroll
+          for (int f = 0; f < NF; ++f) { cq[f] = c[f][q]; fq[f] = Fv[f][q]; }
+          kinetics_add<T, NF>(fq, cq, nf, k.kin);
+#pragma unroll
+          for (int f = 0; f < NF; ++f) Fv[f][q] = fq[f];
+        }
+      }
+      if (valid) {
+#pragma unroll
+        for (int f = 0; f < NF; ++f) {
+          if (f >= nf) break;
+          const long long i = f * per + row + x0 + lx;
+          T pc[4], qc[4], o1[4], o2[4];
+          vload<T, 4>(P + i, pc);
+          vload<T, 4>(Q + i, qc);
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            const T pv = hasP ? pc[q] : (T)0, qv = hasQ ? qc[q] : (T)0;
+            o1[q] = cp1 * pv + cq1 * qv + cf1h * Fv[f][q];
+            o2[q] = cp2 * pv + cq2 * qv + cf2h * Fv[f][q];
+          }
+          if (O2) vstore<T, 4>(O2 + i, o2);
+          vstore<T, 4>(O1 + i, o1);
+          if (a.err) {  // moljax/core/state.py:335-339
+            T yf[4];
+            vload<T, 4>(YF + i, yf);
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+              const T e = (o1[q] - yf[q]) / (k.atol + k.rtol * (o1[q] < (T)0 ? -o1[q] : o1[q]));
+              esum += e * e;
+              bad |= !isfinite(o1[q]);
+            }
+          }
+        }
+      }
+    }
+    __syncthreads();  // the buffer is refilled by the copy issued two tiles later
+    if (!arrived) {
+      // the next tile's copies may still be in flight into the other buffer: wait for
+      // them (bounded) before the block's shared memory is released
+      if (tile + (int)gridDim.x < ntiles) mbar_wait(&bar[sb ^ 1], ((it + 1) >> 1) & 1, 1 << 22);
+      break;
+    }
+  }
+  if (a.err) {
+    __shared__ double red[XWARPS];
+    __shared__ int redb[XWARPS];
+    double esd = (double)esum;
+    for (int o = 16; o > 0; o >>= 1) {
+      esd += __shfl_xor_sync(0xffffffffu, esd, o);
+      bad |= __shfl_xor_sync(0xffffffffu, bad, o);
+    }
+    if (lane == 0) { red[warp] = esd; redb[warp] = bad; }
+    __syncthreads();
+    if (tid == 0) {
+      double s2 = 0.0, cc = 0.0;  // Kahan
+      int b = 0;
+      for (int w = 0; w < XWARPS; ++w) {
+        const double yv = red[w] - cc;
+        const double tv = s2 + yv;
+        cc = (tv - s2) - yv;
+        s2 = tv;
+        b |= redb[w];
+      }
+      a.partial[blockIdx.x] = s2;
+      a.nonfinite[blockIdx.x] = b;
+    }
+  }
+}
+
+// The TMA form applies when the stage is FP32, nx is a multiple of 4 (16-byte rows) and
+// every buffer is 16-byte aligned; the maps cover the buffers the stage can read as W.
+static bool x_tma_ok(const XStage<float>& s) {
+  if (s.m.nx % 4 != 0) return false;
+  for (int i = 0; i < XB_NBUF; ++i)
+    if (s.buf[i] && ((uintptr_t)s.buf[i] & 15)) return false;
+  return true;
+}
+
+template <int RX>
+static cudaError_t launch_stage_tma_rx(const XStage<float>& s, cudaStream_t st) {
+  XTmaMaps tm;
+  memset(&tm, 0, sizeof(tm));
+  // maps of the buffers the stage can read as W (the current state resolves on the device)
+  for (int i = 0; i < XB_NBUF; ++i) {
+    const bool wcand = s.w == XB_YCUR || s.w == XB_YNEXT ? i <= XB_YNEXT : i == s.w;
+    if (wcand && s.buf[i] != nullptr &&
+        make_tmap_3d_f32(&tm.m[i], s.buf[i], s.m.nx, s.m.ny, s.m.nf, XT_SW, XT_SH) != MJX_OK)
+      return cudaErrorInvalidValue;
+  }
+  const int NFa = s.m.nf <= 2 ? 2 : 4;
+  const size_t smem = x_tma_smem(NFa);
+  const long long tiles = (long long)((s.m.nx + XT_W - 1) / XT_W) * ((s.m.ny + XT_H - 1) / XT_H);
+  // one resident wave over the tiles; the error pass fills every partial slot
+  const int res = (NFa == 2 ? 3 : 1) * 152;
+  const int blocks = s.err ? XNPARTS : (int)(tiles < res ? tiles : res);
+  const dim3 blk(32, XWARPS);
+  static ContextOnce attr;
+  cudaError_t e = cudaSuccess;
+  const mjx_status as = attr.run([&]() -> mjx_status {
+    e = cudaFuncSetAttribute(rk_stage_tma_kernel<RX, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)x_tma_smem(2));
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(rk_stage_tma_kernel<RX, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)x_tma_smem(4));
+    return e == cudaSuccess ? MJX_OK : MJX_CUDA_ERROR;
+  });
+  if (as != MJX_OK) return e != cudaSuccess ? e : cudaErrorInvalidValue;
+  if (NFa == 2) rk_stage_tma_kernel<RX, 2><<<blocks, blk, smem, st>>>(s, tm);
+  else rk_stage_tma_kernel<RX, 4><<<blocks, blk, smem, st>>>(s, tm);
+  return cudaGetLastError();
+}
+
+static cudaError_t x_launch_tma(const XStage<float>& s, int rx, cudaStream_t st) {
+  switch (rx) {
+    case RX_GRAY_SCOTT: return launch_stage_tma_rx<RX_GRAY_SCOTT>(s, st);
+    case RX_FISHER: return launch_stage_tma_rx<RX_FISHER>(s, st);
+    case RX_KINETICS: return launch_stage_tma_rx<RX_KINETICS>(s, st);
+    default: return launch_stage_tma_rx<RX_NONE>(s, st);
+  }
+}
+static cudaError_t x_launch_tma(const XStage<double>&, int, cudaStream_t) { return cudaErrorInvalidValue; }
+static bool x_tma_able(const XStage<float>& s) { return x_tma_ok(s); }
+static bool x_tma_able(const XStage<double>&) { return false; }
+
 template <typename T>
 static cudaError_t launch_stage(const XStage<T>& s0, int rx, cudaStream_t st) {
   XStage<T> s = s0;
@@ -695,6 +983,10 @@ static cudaError_t launch_stage(const XStage<T>& s0, int rx, cudaStream_t st) {
   if (s.rows <= 0) {
     const int tuned = tune_rows_get(s.m.ny, s.m.nx, s.m.nf, (int)sizeof(T));
     s.rows = tuned > 0 ? tuned : XROWS_DEFAULT;
+  }
+  if (s.rows == XT_TMA_ROWS) {  // the TMA-staged form (selected by the autotuner)
+    if (x_tma_able(s)) return x_launch_tma(s, rx, st);
+    s.rows = XROWS_DEFAULT;
   }
   const int tile_rows = s.rows * XWARPS;
   // the 128-bit form when nx is a multiple of the vector width and every buffer is
@@ -1292,13 +1584,13 @@ mjx_status mjx_explicit_adaptive2d(const mjx_grid2d* grid, int dtype, const mjx_
 
 // Autotuner of the stencil stage's tile height: one RK4 middle stage (stage input,
 // step start and running sum read; two outputs) of the problem is timed for strips of
-// 2, 4, 8, 16 and 32 rows per warp (one warm-up launch, then reps launches between
-// CUDA events) on the workspace buffers, and the fastest is installed for this grid
-// size, field count and element size.
+// 2, 4, 8, 16 and 32 rows per warp and, for FP32 with 16-byte rows, the TMA-staged form
+// (one warm-up launch, then reps launches between CUDA events) on the workspace
+// buffers, and the fastest is installed for this grid size, field count and element size.
 template <typename T>
 static mjx_status tune_stencil(const XModel& m, char* ws, const XLayout& L, int reps, double* times, int max_times,
                                int* best_rows, cudaStream_t s) {
-  static const int cand[5] = {2, 4, 8, 16, 32};
+  static const int cand[6] = {2, 4, 8, 16, 32, XT_TMA_ROWS};
   XStage<T> st;
   memset(&st, 0, sizeof(st));
   st.m = m;
@@ -1313,7 +1605,8 @@ static mjx_status tune_stencil(const XModel& m, char* ws, const XLayout& L, int 
   double best_t = 1e300;
   int bi = -1;
   cudaError_t ce = cudaSuccess;
-  for (int i = 0; i < 5 && ce == cudaSuccess; ++i) {
+  const int ncand = x_tma_able(st) ? 6 : 5;  // the TMA form: FP32 with aligned 16-byte rows
+  for (int i = 0; i < ncand && ce == cudaSuccess; ++i) {
     st.rows = cand[i];
     ce = launch_stage<T>(st, rx, s);
     if (ce == cudaSuccess) ce = cudaEventRecord(e0, s);

@@ -15,6 +15,8 @@
 //    size of that benchmark, dt = min(10 dz, 0.05, t_final/100) (line 216),
 //    which the semi-implicit form above is not (its explicit upwind advection
 //    needs dt <= dz).
+//  MJX_REACTOR_RK4_DANCKWERTS / _ROBIN / _NEUMANN  benchmarks/benchmark_tubular_reactor.py:
+//    N nodes, dz = 1/(N-1), explicit RK4 with penalty end rows (reactor_rk4_kernel).
 // The reference solves with a dense inverse / LU (O(N^2) per step); the system
 // matrix is tridiagonal and constant in time, so each CTA factorises it once
 // (Thomas) and runs every step's two substitution sweeps as parallel affine
@@ -96,6 +98,11 @@ __global__ void __launch_bounds__(256) reactor_kernel(ReactorArgs A) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const mjx_reactor_instance I = A.inst[blockIdx.x];
   const int n = I.n;
+  if (I.variant < MJX_REACTOR_DANCKWERTS || I.variant > MJX_REACTOR_DANCKWERTS_CN) {  // an RK4 instance
+    T* o = reinterpret_cast<T*>(A.out) + I.offset;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) o[i] = (T)NAN;
+    return;
+  }
   const int np = pz_size(n);               // padded length (index through pz)
   T* c = reinterpret_cast<T*>(smem_raw);   // state
   T* d = c + np;                           // rhs / scan values
@@ -199,6 +206,84 @@ __global__ void __launch_bounds__(256) reactor_kernel(ReactorArgs A) {
   for (int i = tid; i < n; i += nt) out[i] = c[pz(i)];
 }
 
+// Penalty-BC RK4 of benchmarks/benchmark_tubular_reactor.py (57-200, 254-301): n nodes,
+// dz = 1/(n-1), interior rows (1/Pe) D2 c - D1 c - Da c with central D1, and the end rows
+// replaced by relaxations 100 (target - c) toward the BC value (Danckwerts / Robin inlet
+// (c_in + k c_1)/(1 + k), k = (1/Pe)/dz; Neumann c_1; outlet c_{n-2}, Robin written as
+// (c_{n-2}/dz)/(1/dz) like the reference).  The RHS is a 3-point stencil, so one warp
+// holds a whole instance in registers (P contiguous nodes per lane, n <= 32 P) and the
+// four stages of a step exchange only the lane-boundary nodes by shuffle: no shared
+// memory and no block barrier in the time loop.  Four instances per CTA.
+// f(s) in place: each node's left neighbour is carried from the previous iteration
+// (the value before it was overwritten), so one array holds both the stage input and k.
+template <typename T, int P>
+__device__ __forceinline__ void rk4_rhs(T (&s)[P], int i0, int n, int bc, T iPe, T idz2, T hidz, T Da, T kin,
+                                        T cin, T idz) {
+  const T sl = __shfl_up_sync(0xffffffffu, s[P - 1], 1);
+  const T sr = __shfl_down_sync(0xffffffffu, s[0], 1);
+  T cm = sl;
+#pragma unroll
+  for (int q = 0; q < P; ++q) {
+    const int i = i0 + q;
+    const T cc = s[q];
+    const T cp = q < P - 1 ? s[q < P - 1 ? q + 1 : 0] : sr;
+    T v = iPe * ((cm - (T)2 * cc + cp) * idz2) - (cp - cm) * hidz - Da * cc;
+    if (i == 0) {
+      const T tgt = bc == MJX_REACTOR_RK4_NEUMANN ? cp : (cin + kin * cp) / ((T)1 + kin);
+      v = (T)100 * (tgt - cc);
+    } else if (i == n - 1) {
+      const T tgt = bc == MJX_REACTOR_RK4_ROBIN ? (idz * cm) / idz : cm;
+      v = (T)100 * (tgt - cc);
+    } else if (i >= n) {
+      v = (T)0;
+    }
+    s[q] = v;
+    cm = cc;
+  }
+}
+
+template <typename T, int P>
+__global__ void __launch_bounds__(128) reactor_rk4_kernel(ReactorArgs A) {
+  const int w = blockIdx.x * 4 + (threadIdx.x >> 5);
+  if (w >= A.n_inst) return;  // warp-uniform
+  const int lane = threadIdx.x & 31;
+  const mjx_reactor_instance I = A.inst[w];
+  const int n = I.n, bc = I.variant;
+  T* out = reinterpret_cast<T*>(A.out) + I.offset;
+  const bool ok = n >= 3 && n <= 32 * P && bc >= MJX_REACTOR_RK4_DANCKWERTS && bc <= MJX_REACTOR_RK4_NEUMANN;
+  if (!ok) {  // not this kernel's instance: NaN, never an out-of-range write
+    for (int i = lane; i < n && i < 32 * P; i += 32) out[i] = (T)NAN;
+    return;
+  }
+  const double dz = 1.0 / (n - 1);
+  const T iPe = (T)(1.0 / I.Pe), idz2 = (T)(1.0 / (dz * dz)), hidz = (T)(0.5 / dz), Da = (T)I.Da;
+  const T idz = (T)(1.0 / dz), kin = (T)((1.0 / I.Pe) / dz), cin = (T)I.c_inlet;
+  const T dt = (T)I.dt, hdt = (T)(0.5 * I.dt), dt6 = (T)(I.dt / 6.0);
+  const int i0 = lane * P;
+  T c[P], acc[P], y[P];
+#pragma unroll
+  for (int q = 0; q < P; ++q) c[q] = i0 + q < n ? (T)I.c_init : (T)0;
+  for (int step = 0; step < I.n_steps; ++step) {
+#pragma unroll
+    for (int q = 0; q < P; ++q) y[q] = c[q];
+    rk4_rhs<T, P>(y, i0, n, bc, iPe, idz2, hidz, Da, kin, cin, idz);  // k1
+#pragma unroll
+    for (int q = 0; q < P; ++q) { acc[q] = y[q]; y[q] = c[q] + hdt * y[q]; }
+    rk4_rhs<T, P>(y, i0, n, bc, iPe, idz2, hidz, Da, kin, cin, idz);  // k2
+#pragma unroll
+    for (int q = 0; q < P; ++q) { acc[q] += (T)2 * y[q]; y[q] = c[q] + hdt * y[q]; }
+    rk4_rhs<T, P>(y, i0, n, bc, iPe, idz2, hidz, Da, kin, cin, idz);  // k3
+#pragma unroll
+    for (int q = 0; q < P; ++q) { acc[q] += (T)2 * y[q]; y[q] = c[q] + dt * y[q]; }
+    rk4_rhs<T, P>(y, i0, n, bc, iPe, idz2, hidz, Da, kin, cin, idz);  // k4
+#pragma unroll
+    for (int q = 0; q < P; ++q) c[q] = c[q] + dt6 * (acc[q] + y[q]);
+  }
+#pragma unroll
+  for (int q = 0; q < P; ++q)
+    if (i0 + q < n) out[i0 + q] = c[q];
+}
+
 }  // namespace mjx
 
 using namespace mjx;
@@ -233,6 +318,31 @@ mjx_status mjx_reactor_cn_batch(const mjx_reactor_instance* inst_dev, int n_inst
   cudaStream_t s = (cudaStream_t)stream;
   if (e == 4) reactor_kernel<float><<<n_inst, 256, smem, s>>>(A);
   else reactor_kernel<double><<<n_inst, 256, smem, s>>>(A);
+  return cuda_status(cudaGetLastError());
+}
+
+mjx_status mjx_reactor_rk4_batch(const mjx_reactor_instance* inst_dev, int n_inst, int max_n, int dtype,
+                                 void* out, void* stream) {
+  const int e = elem_size(dtype);
+  if (!e) return MJX_BAD_DTYPE;
+  if (!inst_dev || !out || n_inst < 0 || max_n < 3) return MJX_BAD_ARG;
+  if (max_n > (e == 4 ? 1024 : 512)) return MJX_BAD_SHAPE;  // 32 (FP32) / 16 (FP64) nodes per lane
+  if (n_inst == 0) return MJX_OK;
+  ReactorArgs A;
+  A.inst = inst_dev; A.out = out; A.n_inst = n_inst;
+  cudaStream_t s = (cudaStream_t)stream;
+  const int blocks = (n_inst + 3) / 4;
+  const int per = (max_n + 31) / 32;  // nodes per lane
+#define MJX_RK4_LAUNCH(PP)                                                         \
+  do {                                                                             \
+    if (e == 4) reactor_rk4_kernel<float, PP><<<blocks, 128, 0, s>>>(A);           \
+    else reactor_rk4_kernel<double, PP><<<blocks, 128, 0, s>>>(A);                 \
+  } while (0)
+  if (per <= 4) MJX_RK4_LAUNCH(4);
+  else if (per <= 8) MJX_RK4_LAUNCH(8);
+  else if (per <= 16) MJX_RK4_LAUNCH(16);
+  else if (e == 4) reactor_rk4_kernel<float, 32><<<blocks, 128, 0, s>>>(A);
+#undef MJX_RK4_LAUNCH
   return cuda_status(cudaGetLastError());
 }
 

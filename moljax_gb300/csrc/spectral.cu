@@ -329,12 +329,14 @@ __global__ void __launch_bounds__(ColThreads<T>::v, 1) col_kernel(const __grid_c
     if (kx < a.ncols) lxy = a.ldc3 ? a.lamx[kx % a.ldc3] + a.lamy2[kx / a.ldc3] : a.lamx[kx];
     const T lam = lxy + a.lamy[ky];
     const C v = buf[sp(ky * W + c)];
-    if (jb.mul == MUL_ADVDIFF || jb.mul == MUL_ADV_LAP || jb.mul == MUL_ADV_EXP) {
+    if (jb.mul == MUL_ADVDIFF || jb.mul == MUL_ADV_LAP || jb.mul == MUL_ADV_EXP || jb.mul == MUL_ADV_CN) {
       // z = h (D lam - i (vx kx + vy ky)), kx, ky = 2 pi fftfreq (the Nyquist index
       // negative); m = 1/(1 - z) with |1 - z| < 1e-14 -> 1e-14 (the solve of
       // FFTAdvectionDiffusionPreconditioner, moljax/core/preconditioners.py:297-420, and of
       // AdvectionDiffusionOperator, fft_operators.py:179-260), z itself (matvec) or exp(z)
-      // (exp_matvec).  The reference keeps real(ifft(.)); on the half spectrum that is the
+      // (exp_matvec), or the Crank-Nicolson factor (1 + z/2)/(1 - z/2) of the 1D advective
+      // FFT-CN (benchmarks/benchmark_solver_comparison.py:152-163).  The reference keeps
+      // real(ifft(.)); on the half spectrum that is the
       // multiplier (m(k) + conj(m(-k)))/2, which equals m(k) except on the Nyquist lines,
       // where fftfreq breaks the oddness of the advection term.
       const int nxl = 2 * (a.ncols - 1);
@@ -356,6 +358,11 @@ __global__ void __launch_bounds__(ColThreads<T>::v, 1) col_kernel(const __grid_c
         } else if (jb.mul == MUL_ADV_LAP) {
           fr = zr;
           fi = zi;
+        } else if (jb.mul == MUL_ADV_CN) {
+          const double nr = 1.0 + 0.5 * zr, ni = 0.5 * zi, dr = 1.0 - 0.5 * zr, di = -0.5 * zi;
+          const double den = dr * dr + di * di;
+          fr = (nr * dr + ni * di) / den;
+          fi = (ni * dr - nr * di) / den;
         } else {
           double sn, cs;
           sincos(zi, &sn, &cs);
@@ -506,6 +513,32 @@ mjx_status make_tmap_2d_f32(CUtensorMap* map, const void* base, unsigned long lo
   const cuuint32_t box[2] = {box_inner, box_rows};
   const cuuint32_t estr[2] = {1, 1};
   const CUresult r = encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<void*>(base), dims, strides, box,
+                            estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return cuda_status(cudaErrorInvalidValue);
+  return MJX_OK;
+}
+
+mjx_status make_tmap_3d_f32(CUtensorMap* map, const void* base, unsigned long long nx, unsigned long long ny,
+                            unsigned long long nz, unsigned box_x, unsigned box_y) {
+  static PfnTensorMapEncodeTiled encode = nullptr;
+  static std::once_flag resolved;
+  std::call_once(resolved, []() {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess && q == cudaDriverEntryPointSuccess)
+      encode = (PfnTensorMapEncodeTiled)f;
+  });
+  if (encode == nullptr) return cuda_status(cudaErrorNotSupported);
+  if (((uintptr_t)base & 15) || ((nx * 4) & 15) || ((box_x * 4) & 15) || box_x < 1 || box_x > 256 || box_y < 1 ||
+      box_y > 256)
+    return MJX_BAD_ARG;
+  const cuuint64_t dims[3] = {nx, ny, nz};
+  const cuuint64_t strides[2] = {nx * 4, nx * ny * 4};
+  const cuuint32_t box[3] = {box_x, box_y, 1};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  const CUresult r = encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<void*>(base), dims, strides, box,
                             estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                             CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) return cuda_status(cudaErrorInvalidValue);
@@ -800,14 +833,14 @@ mjx_status mjx_advdiff_op2d(const void* plan, const mjx_grid2d* g, int dtype, in
                             const void* in, void* out, void* ws, size_t ws_bytes, void* stream) {
   MJX_TRY(check_grid(g));
   if (nfields < 1 || nfields > 4 || D == nullptr || vx == nullptr || vy == nullptr || plan == nullptr ||
-      in == nullptr || out == nullptr || op < 0 || op > 2)
+      in == nullptr || out == nullptr || op < 0 || op > 3)
     return MJX_BAD_ARG;
   const int e = elem_size(dtype);
   if (!e) return MJX_BAD_DTYPE;
   if (ws == nullptr || ws_bytes < mjx_spec2d_ws_bytes(g->ny, g->nx, nfields, dtype)) return MJX_WORKSPACE;
   MJX_TRY(ensure_kernel_attrs());
   cudaStream_t s = (cudaStream_t)stream;
-  const int mul = op == 0 ? MUL_ADVDIFF : (op == 1 ? MUL_ADV_LAP : MUL_ADV_EXP);
+  const int mul = op == 0 ? MUL_ADVDIFF : (op == 1 ? MUL_ADV_LAP : (op == 2 ? MUL_ADV_EXP : MUL_ADV_CN));
   if (e == 4)
     return spectral_apply<float>(plan, g, nfields, D, h, mul, (const float*)in, (float*)out, ws, s, vx, vy);
   return spectral_apply<double>(plan, g, nfields, D, h, mul, (const double*)in, (double*)out, ws, s, vx, vy);

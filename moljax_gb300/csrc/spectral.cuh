@@ -105,7 +105,8 @@ template <typename T> struct RowArgs {
 enum { MUL_SCALE = 0, MUL_HELMHOLTZ = 1, MUL_CN = 2, MUL_EXP = 3, MUL_ADVDIFF = 4, MUL_LAP = 5,
        MUL_ADV_LAP = 6,   // h (D lam - i v.k): the advection-diffusion operator itself
        MUL_ADV_EXP = 7,   // exp(h (D lam - i v.k))
-       MUL_TABLE = 8 };   // a real multiplier per half-spectrum point (ColArgs::mtab)
+       MUL_TABLE = 8,     // a real multiplier per half-spectrum point (ColArgs::mtab)
+       MUL_ADV_CN = 9 };  // (1 + z/2)/(1 - z/2), z = h (D lam - i v.k): one Crank-Nicolson step
 
 struct ColJob {
   long long sin;         // spectrum offset of the input column block (ky=0, kx=0)

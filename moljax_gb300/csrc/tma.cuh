@@ -16,6 +16,11 @@ namespace mjx {
 mjx_status make_tmap_2d_f32(CUtensorMap* map, const void* base, unsigned long long inner, unsigned long long rows,
                             unsigned long long row_bytes, unsigned box_inner, unsigned box_rows);
 
+// 3D tensor map of FP32 data [nz][ny][nx] (rows nx floats, planes ny rows; nx * 4 a
+// multiple of 16), boxes of box_x x box_y x 1 (box_x * 4 a multiple of 16, box sides <= 256).
+mjx_status make_tmap_3d_f32(CUtensorMap* map, const void* base, unsigned long long nx, unsigned long long ny,
+                            unsigned long long nz, unsigned box_x, unsigned box_y);
+
 __device__ __forceinline__ unsigned smem_u32(const void* p) {
   return (unsigned)__cvta_generic_to_shared(p);
 }
@@ -38,6 +43,16 @@ __device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, i
   asm volatile(
       "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
       ::"r"(smem_u32(dst)), "l"(reinterpret_cast<unsigned long long>(map)), "r"(x), "r"(y), "r"(smem_u32(bar))
+      : "memory");
+}
+
+// one 3D box at element coordinates (x, y, z) of the map into shared memory dst
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, int x, int y, int z,
+                                            unsigned long long* bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];"
+      ::"r"(smem_u32(dst)), "l"(reinterpret_cast<unsigned long long>(map)), "r"(x), "r"(y), "r"(z),
+        "r"(smem_u32(bar))
       : "memory");
 }
 

@@ -9,7 +9,8 @@ package itself):
   ``real(ifft2(fft2(u) * cn_factor))``;
 * ``benchmarks/sisc/bench_precision_fp32_fp64.py:41-100`` -- the same at
   128^2, D=0.1, T=0.1 for a range of dt (the published error table);
-* ``benchmarks/benchmark_solver_comparison.py:152-163`` -- the 1D form;
+* ``benchmarks/benchmark_solver_comparison.py:152-163`` -- the 1D form with advection,
+  and its exponential Strang splitting (190-215) and SciPy Radau comparison (67-121);
 * ``benchmarks/sisc/bench_3d_feasibility.py:56-87`` -- 3D, N^3 points of
   x = j L/N, D = 0.1, 10 steps to T = 0.01, max error vs the analytic decay
   exp(-12 pi^2 D T) sin sin sin.
@@ -62,6 +63,46 @@ def fft_cn_1d(u0, D, dx, dt, n_steps, kind="spectral", v=0.0):
     for _ in range(n_steps):
         u = np.real(np.fft.ifft(np.fft.fft(u) * G))
     return u
+
+
+def solver_comparison_ic(n=1024):
+    """u0 = exp(-100 (x - 0.5)^2) on x = j/n (benchmarks/benchmark_solver_comparison.py:55-58)."""
+    x = np.linspace(0, 1, n, endpoint=False)
+    return np.exp(-100 * (x - 0.5) ** 2)
+
+
+def strang_exp_1d(u0, D, v, dx, dt, n_steps):
+    """benchmarks/benchmark_solver_comparison.py:190-215 (imex_step / imex_solve): per step
+    exp(dt/2 v (-i k)), exp(dt D (-k^2)), exp(dt/2 v (-i k)), each a transform pair keeping
+    the real part."""
+    n = u0.shape[0]
+    k = 2 * np.pi * np.fft.fftfreq(n, dx)
+    ea = np.exp(0.5 * dt * v * (-1j * k))
+    ed = np.exp(dt * D * (-(k * k)))
+    u = np.array(u0, dtype=np.float64, copy=True)
+    for _ in range(n_steps):
+        u = np.real(np.fft.ifft(np.fft.fft(u) * ea))
+        u = np.real(np.fft.ifft(np.fft.fft(u) * ed))
+        u = np.real(np.fft.ifft(np.fft.fft(u) * ea))
+    return u
+
+
+def radau_advdiff_1d(u0, D, v, t_final, rtol=1e-6, atol=1e-8):
+    """The comparison solution of benchmarks/benchmark_solver_comparison.py:67-121: SciPy
+    Radau on the periodic FD semi-discretisation D D2 u - v D1 u (central D1), dense
+    matrices; returns (final state, number of output times)."""
+    from scipy.integrate import solve_ivp
+    n = u0.shape[0]
+    dx = 1.0 / n
+    D2 = np.zeros((n, n))
+    D1 = np.zeros((n, n))
+    for i in range(n):
+        D2[i, (i - 1) % n], D2[i, i], D2[i, (i + 1) % n] = 1.0, -2.0, 1.0
+        D1[i, (i - 1) % n], D1[i, (i + 1) % n] = -1.0, 1.0
+    D2 /= dx ** 2
+    D1 /= 2 * dx
+    sol = solve_ivp(lambda t, u: D * D2 @ u - v * D1 @ u, [0, t_final], u0, method="Radau", rtol=rtol, atol=atol)
+    return sol.y[:, -1], len(sol.t)
 
 
 def analytic_decay(u0, D, T):

@@ -108,3 +108,114 @@ def served_dt(N, t_final=5.0):
     dz = 1.0 / (N - 1)
     dt = min(10 * dz, 0.05, t_final / 100)
     return dt, int(t_final / dt)
+
+
+# --- penalty-BC RK4 (benchmarks/benchmark_tubular_reactor.py) ---------------------------
+
+TUBULAR_BCS = ("danckwerts", "robin", "neumann")
+
+
+def tubular_dt(N, Pe, t_final):
+    """dt = min(0.5 dz, 0.25 Pe dz^2, 0.01), n_steps = int(t_final / dt), dz = 1/(N-1)
+    (benchmark_tubular_reactor.py:254-256, 283-286)."""
+    dz = 1.0 / (N - 1)
+    dt = min(0.5 * dz, 0.25 * Pe * dz ** 2, 0.01)
+    return dt, int(t_final / dt)
+
+
+def tubular_rhs(c, N, Pe, Da, bc, c_in=1.0):
+    """dc/dt of benchmark_tubular_reactor.py:57-160 on N nodes (dz = 1/(N-1)): the interior
+    rows (1/Pe) D2 c - D1 c - Da c (D2 central with zero end rows, D1 central with one-sided
+    end rows, 57-81), then the two end rows replaced by penalty relaxations 100 (target - c):
+    Danckwerts inlet target (c_in + k c1) / (1 + k), k = (1/Pe)/dz (84-110); Robin with
+    alpha_in = 1, beta_in = 1/Pe, alpha_out = 0, beta_out = 1 (113-144, 269); Neumann
+    c1 / c_{N-2} (147-167).  Written out per row, in the reference's operation order."""
+    dz = 1.0 / (N - 1)
+    d2 = np.zeros_like(c)
+    d2[1:-1] = (c[:-2] - 2.0 * c[1:-1] + c[2:]) / dz ** 2
+    d1 = np.empty_like(c)
+    d1[1:-1] = (-0.5 * c[:-2] + 0.5 * c[2:]) / dz
+    d1[0] = (-c[0] + c[1]) / dz
+    d1[-1] = (-c[-2] + c[-1]) / dz
+    f = (1.0 / Pe) * d2 - d1 - Da * c
+    if bc == "danckwerts":
+        k = (1.0 / Pe) / dz
+        f[0] = 100.0 * ((c_in + k * c[1]) / (1.0 + k) - c[0])
+        f[-1] = 100.0 * (c[-2] - c[-1])
+    elif bc == "robin":
+        b_in, b_out = 1.0 / Pe, 1.0
+        f[0] = 100.0 * ((c_in + b_in / dz * c[1]) / (1.0 + b_in / dz) - c[0])
+        f[-1] = 100.0 * ((b_out / dz * c[-2]) / (0.0 + b_out / dz) - c[-1])
+    elif bc == "neumann":
+        f[0] = 100.0 * (c[1] - c[0])
+        f[-1] = 100.0 * (c[-2] - c[-1])
+    else:
+        raise ValueError(bc)
+    return f
+
+
+def tubular_initial(N, bc):
+    """Zeros (Danckwerts, Robin) or ones (Neumann) (benchmark_tubular_reactor.py:258-262)."""
+    return np.ones(N) if bc == "neumann" else np.zeros(N)
+
+
+def tubular_rk4_loop(N, Pe, Da, bc, dt, n_steps, c0=None):
+    """Classical RK4 (benchmark_tubular_reactor.py:181-192), step by step."""
+    c = tubular_initial(N, bc) if c0 is None else np.array(c0, dtype=np.float64)
+    f = lambda y: tubular_rhs(y, N, Pe, Da, bc)
+    for _ in range(n_steps):
+        k1 = f(c)
+        k2 = f(c + 0.5 * dt * k1)
+        k3 = f(c + 0.5 * dt * k2)
+        k4 = f(c + dt * k3)
+        c = c + (dt / 6.0) * (k1 + 2 * k2 + 2 * k3 + k4)
+    return c
+
+
+def tubular_rk4(N, Pe, Da, bc, dt, n_steps):
+    """The same RK4 recurrence for long runs: the RHS is affine, f(c) = A c + b, so one step
+    is c <- P c + q with P = I + hA + (hA)^2/2 + (hA)^3/6 + (hA)^4/24 and
+    q = h (I + hA/2 + (hA)^2/6 + (hA)^3/24) b (exact algebra of the four stages); n steps are
+    the n-th power of the affine map, by repeated squaring (FP64)."""
+    I = np.eye(N)
+    b = tubular_rhs(np.zeros(N), N, Pe, Da, bc)
+    A = np.stack([tubular_rhs(I[:, j], N, Pe, Da, bc) - b for j in range(N)], axis=1)
+    hA = dt * A
+    hA2 = hA @ hA
+    hA3 = hA2 @ hA
+    P = I + hA + hA2 / 2 + hA3 / 6 + hA3 @ hA / 24
+    q = dt * ((I + hA / 2 + hA2 / 6 + hA3 / 24) @ b)
+    T = np.eye(N + 1)
+    T[:N, :N] = P
+    T[:N, N] = q
+    R = np.eye(N + 1)
+    n = int(n_steps)
+    while n:
+        if n & 1:
+            R = T @ R
+        T = T @ T
+        n >>= 1
+    c0 = np.append(tubular_initial(N, bc), 1.0)
+    return (R @ c0)[:N]
+
+
+def tubular_analytic_danckwerts(z, Pe, Da):
+    """Steady state of the Danckwerts problem (benchmark_tubular_reactor.py:207-235):
+    c = A e^{r1 z} + B e^{r2 z}, r = (Pe +- sqrt(Pe^2 + 4 Pe Da))/2."""
+    disc = Pe ** 2 + 4 * Pe * Da
+    r1 = (Pe + np.sqrt(disc)) / 2
+    r2 = (Pe - np.sqrt(disc)) / 2
+    M = np.array([[r1 / Pe - 1, r2 / Pe - 1], [r1 * np.exp(r1), r2 * np.exp(r2)]])
+    A, B = np.linalg.solve(M, np.array([-1.0, 0.0]))
+    return A * np.exp(r1 * z) + B * np.exp(r2 * z)
+
+
+def tubular_summary(c, Pe, Da, bc, t_final):
+    """conversion (1 - outlet, or the mean for Neumann), the max error against the
+    analytic profile (the Danckwerts steady state, or e^{-Da t} for Neumann) and the outlet
+    value (benchmark_tubular_reactor.py:263-268, 294-296)."""
+    N = c.shape[-1]
+    z = np.linspace(0, 1, N)
+    ref = tubular_analytic_danckwerts(z, Pe, Da) if bc != "neumann" else np.exp(-Da * t_final) * np.ones(N)
+    conv = 1.0 - c[-1] if bc != "neumann" else float(c.mean())
+    return {"conversion": float(conv), "error": float(np.max(np.abs(c - ref))), "final_outlet_c": float(c[-1])}

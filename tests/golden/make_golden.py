@@ -5,7 +5,9 @@ The fixtures hold only the numbers the tests pin:
 the FFT-CN error tables of benchmarks/results/precision_fp32_fp64.json and
 benchmarks/results/scipy_comparison.json, the CN reactor conversions of
 benchmarks/results/method_comparison_results.json, and the 3D FFT-CN errors and
-times of benchmarks/results/3d_feasibility.json.
+times of benchmarks/results/3d_feasibility.json, the penalty-RK4 reactor sweep of
+benchmarks/results/reactor_results.json and the 1D solver comparison of
+benchmarks/results/solver_comparison.json.
 """
 
 import json
@@ -48,6 +50,19 @@ def main(ref):
         json.dump({"source": "benchmarks/results/3d_feasibility.json", "config": f3["config"],
                    "experiments": [{k: e[k] for k in ("grid_size", "time_ms", "error")}
                                    for e in f3["experiments"] if e.get("success")]}, f, indent=1)
+
+    rr = json.load(open(os.path.join(res, "reactor_results.json")))
+    with open(os.path.join(HERE, "tubular_published.json"), "w") as f:
+        json.dump({"source": "benchmarks/results/reactor_results.json", "N": 128, "t_final": 15.0,
+                   "config": rr["config"],
+                   "results": {k: {kk: v[kk] for kk in ("bc_type", "Pe", "Da", "conversion", "error", "dt",
+                                                          "n_steps", "final_outlet_c")}
+                               for k, v in rr["results"].items()}}, f, indent=1)
+    so = json.load(open(os.path.join(res, "solver_comparison.json")))
+    with open(os.path.join(HERE, "solver_comparison_published.json"), "w") as f:
+        json.dump({"source": "benchmarks/results/solver_comparison.json", "config": so["config"],
+                   "solvers": [{k: s_[k] for k in ("name", "steps", "dt", "rtol", "atol", "error_vs_scipy")
+                                if k in s_} for s_ in so["solvers"]]}, f, indent=1)
 
 
 if __name__ == "__main__":

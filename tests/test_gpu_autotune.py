@@ -74,7 +74,7 @@ def test_fp32_schedules_and_3d_plan(cuda):
     assert AT.dft_schedule(48, torch.float64)[0]
 
 
-@pytest.mark.parametrize("shape", [(96, 160), (37, 70)])
+@pytest.mark.parametrize("shape", [(96, 160), (37, 70), (70, 300)])
 def test_stencil_tile_heights_bit_identical(cuda, shape):
     import moljax_gb300 as M
     from moljax_gb300.core import autotune as AT
@@ -88,14 +88,16 @@ def test_stencil_tile_heights_bit_identical(cuda, shape):
          for k in ("c1", "c2")}
     try:
         outs = []
-        for rows in (2, 4, 8, 16, 32):
+        for rows in (2, 4, 8, 16, 32, 64):  # 64: the TMA-staged form where nx % 4 == 0
             AT.set_stencil_rows(ny, nx, 2, torch.float32, rows)
             F = model.rhs(y)
             outs.append(torch.stack([F["c1"], F["c2"]]).cpu())
         for o in outs[1:]:
             assert torch.equal(o, outs[0])
         res = AT.autotune_stencil(model, torch.float32)
-        assert res.choice[0] in (2, 4, 8, 16, 32) and len(res.times_ms) == 5
+        tma = nx % 4 == 0
+        assert res.choice[0] in ((2, 4, 8, 16, 32, 64) if tma else (2, 4, 8, 16, 32))
+        assert len(res.times_ms) == (6 if tma else 5)
         assert AT.stencil_rows(ny, nx, 2, torch.float32) == res.choice[0]
         F = model.rhs(y)
         assert torch.equal(torch.stack([F["c1"], F["c2"]]).cpu(), outs[0])

@@ -316,3 +316,71 @@ def test_kinetics_network_vs_oracle(cuda, nspecies, kind):
     assert (r.n_accepted, r.n_rejected) == (ro.n_accepted, ro.n_rejected)
     for k in names:
         assert _rel(_interior(r.y_final[k].cpu().numpy(), n), _interior(ro.y_final[k], n)) < 1e-10
+
+
+@pytest.mark.parametrize("shape", [(70, 300), (33, 132), (5, 4), (1, 8), (64, 256)])
+@pytest.mark.parametrize("kind", [mol.PERIODIC, mol.DIRICHLET, mol.NEUMANN])
+def test_tma_stage_form(cuda, shape, kind):
+    """The TMA-staged stage kernel (FP32, rows a multiple of 4 points; selected by
+    installing 64 as the tile height): partial tiles in x and y, grids narrower than one
+    box, a single row; three fields (the four-field build) and Gray-Scott (the two-field
+    reaction build); BC values on every side.  Its RHS equals the 128-bit register form bit
+    for bit and the oracle within FP32 rounding; the adaptive RK4 loop (the error fused into
+    the last stage) takes the same accept/reject sequence to the same state within FP32
+    rounding (the error partials are summed in another order, so dt may differ in the last
+    bit)."""
+    import moljax_gb300 as M
+    from moljax_gb300.core import autotune as AT
+    from moljax_gb300.core.bc import FieldBCSpec, BCType
+    ny, nx = shape
+    names = ("c1", "c2", "c3")
+    grid = M.Grid2D(nx, ny, 0.0, 1.0, 0.0, 0.8)
+    og = mol.Grid2D(nx, ny, 0, 1, 0, 0.8)
+    model = M.create_advection_diffusion_model(grid, names, 0.01, 0.7, -0.4, BCType(kind), True,
+                                               dtype=torch.float32)
+    vals = {}
+    if kind != mol.PERIODIC:
+        fn = (lambda X, Y, t, p: dict(SIDES))
+        spec = FieldBCSpec(kind=BCType(kind), value=fn) if kind == mol.DIRICHLET else \
+            FieldBCSpec(kind=BCType(kind), flux=fn)
+        model = M.MOLModel(model.grid, {k: spec for k in names}, model.params, model.linear_ops,
+                           model.nonlinear_ops, model.metadata)
+        vals = {k: dict(SIDES) for k in names}
+    om = OX.ExplicitModel(og, {k: kind for k in names}, {k: 0.01 for k in names}, vals,
+                          advection="upwind", vx=0.7, vy=-0.4, params={"D": 0.01, "vx": 0.7, "vy": -0.4})
+    rng = np.random.default_rng(ny * 7 + nx)
+    y0 = {k: mol.pad(rng.uniform(0, 1, (ny, nx)), og) for k in names}
+    ym = {k: torch.tensor(v, dtype=torch.float32, device=cuda) for k, v in y0.items()}
+    c = (slice(1, ny + 1), slice(1, nx + 1))
+    gs_grid = M.Grid2D(nx, ny, 0.0, 2.5, 0.0, 2.0)
+    gs = M.create_gray_scott_model(gs_grid, 2e-5, 1e-5, 0.035, 0.065, BCType(kind), torch.float32)
+    if kind != mol.PERIODIC:
+        gs = M.MOLModel(gs.grid, {k: model.bc_spec["c1"] for k in ("u", "v")}, gs.params, gs.linear_ops,
+                        gs.nonlinear_ops, gs.metadata)
+    yg = {k: torch.tensor(v, dtype=torch.float32, device=cuda)
+          for k, v in mol.gray_scott_ic(mol.Grid2D(nx, ny, 0, 2.5, 0, 2.0), 4).items()}
+    pid = M.PIDParams(atol=1e-5, rtol=1e-3)
+    runs = {}
+    try:
+        for rows in (64, 8):
+            AT.set_stencil_rows(ny, nx, 3, torch.float32, rows)
+            AT.set_stencil_rows(ny, nx, 2, torch.float32, rows)
+            out = {"rhs": model.rhs(ym), "gs": gs.rhs(yg)}
+            r = M.adaptive_integrate(model, ym, 0.0, 0.02, 1e-3, M.IntegratorType.RK4, max_steps=500,
+                                     pid_params=pid, save_every=1)
+            out["adaptive"] = (r.status, r.n_accepted, r.n_rejected, r.y_final)
+            runs[rows] = out
+    finally:
+        AT.set_stencil_rows(ny, nx, 3, torch.float32, 0)
+        AT.set_stencil_rows(ny, nx, 2, torch.float32, 0)
+    t, v = runs[64], runs[8]
+    for key in ("rhs", "gs"):
+        for k in t[key]:
+            assert torch.equal(t[key][k], v[key][k]), (key, k)
+    assert t["adaptive"][:3] == v["adaptive"][:3] and t["adaptive"][0] == 0
+    for k in names:
+        torch.testing.assert_close(t["adaptive"][3][k], v["adaptive"][3][k], rtol=1e-5, atol=1e-6)
+    R = om.rhs(y0)
+    for k in names:
+        F = t["rhs"][k].cpu().double().numpy()[c]
+        assert _rel(F, R[k][c]) < 2e-5, k

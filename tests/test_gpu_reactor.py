@@ -77,3 +77,35 @@ def test_stencil1d_vs_oracle(cuda):
     c = torch.linspace(1, 0, 128, dtype=torch.float64, device=cuda)
     assert (D2 @ c).shape == (128,) and (D1 @ c).shape == (128,)
     assert float((D1 @ c)[0]) == pytest.approx((1.0 - 1.0) / gr.dx, abs=1e-9)
+
+
+def test_tubular_rk4_sweep_published(cuda):
+    """The 27-case penalty-RK4 sweep of benchmark_tubular_reactor.py (N = 128, t_final = 15, up
+    to 967 740 RK4 steps per case) in one launch, FP64: every published conversion, error and
+    outlet value (benchmarks/results/reactor_results.json) within 1e-8 relative, and the
+    final profiles against the oracle within 1e-10."""
+    from moljax_gb300.core import reactor as R
+    g = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "tubular_published.json")))
+    res = R.run_tubular_sweep(N=g["N"], t_final=g["t_final"], dtype=torch.float64)
+    assert set(res) == set(g["results"])
+    for key, v in g["results"].items():
+        r = res[key]
+        assert r["n_steps"] == v["n_steps"]
+        for k in ("conversion", "error", "final_outlet_c"):
+            assert r[k] == pytest.approx(v[k], rel=1e-8, abs=1e-40), (key, k, r[k], v[k])
+    # profiles against the oracle on uneven sizes (one warp holds 4 to 32 nodes per lane;
+    # FP64 up to 512 nodes, FP32 up to 1024)
+    cases, refs = [], []
+    for n, bc, Pe, Da in ((3, "danckwerts", 5.0, 1.0), (37, "robin", 20.0, 2.0), (128, "neumann", 1.0, 0.5),
+                          (257, "danckwerts", 50.0, 3.0), (512, "robin", 30.0, 1.5), (1000, "neumann", 200.0, 0.7),
+                          (1024, "robin", 10.0, 4.0)):
+        c = R.tubular_rk4_case(Pe, Da, bc, n, 0.5)
+        c.n_steps = min(c.n_steps, 3000)
+        cases.append(c)
+        refs.append(OR.tubular_rk4_loop(n, Pe, Da, bc, c.dt, c.n_steps))
+    for dtype, tol, nmax in ((torch.float64, 1e-12, 512), (torch.float32, 2e-5, 1024)):
+        sel = [i for i, c in enumerate(cases) if c.n <= nmax]
+        outs = R.solve_batch([cases[i] for i in sel], dtype)
+        for c, o, ref in zip([cases[i] for i in sel], outs, [refs[i] for i in sel]):
+            err = float(np.max(np.abs(o.double().cpu().numpy() - ref)))
+            assert err < tol * max(1.0, float(np.max(np.abs(ref)))), (c.n, c.variant, dtype, err)

@@ -84,3 +84,36 @@ def test_fft_cn_fd_symbol(cuda):
     u = fft_solvers.fft_cn_step(torch.tensor(u0, device=cuda), 0.1, 1 / 64, 0.01, 10, symbol="fd")
     ref = fftcn.fft_cn_2d(u0, 0.1, 1 / 64, 0.01, 10, kind="fd")
     assert _rel(u.cpu().numpy(), ref) < 1e-12
+
+
+def test_solver_comparison_1d_published(cuda):
+    """benchmarks/results/solver_comparison.json through the native 1D advection-diffusion
+    path (N = 1024, D = 0.01, v = 1, t = 10, FP64): FFT-CN (dt 1e-3, 10 000 steps) and the
+    exponential Strang IMEX (dt 5e-3, 2 000 steps) reproduce the published max differences
+    from SciPy Radau (tests/golden/radau_advdiff1d.npy) and the oracle's final states."""
+    import json
+    import os
+    import moljax_gb300 as M
+    gold = os.path.join(os.path.dirname(__file__), "golden")
+    g = json.load(open(os.path.join(gold, "solver_comparison_published.json")))
+    ref = np.load(os.path.join(gold, "radau_advdiff1d.npy"))
+    cfg = g["config"]
+    n, D, v, T = cfg["N"], cfg["D"], cfg["v"], cfg["t_final"]
+    u0 = fftcn.solver_comparison_ic(n)
+    cn, im = g["solvers"][1], g["solvers"][2]
+    ut = torch.tensor(u0, device=cuda)
+    u = M.fft_cn_advdiff_1d(ut, D, v, 1.0 / n, cn["dt"], cn["steps"]).cpu().numpy()
+    assert float(np.max(np.abs(u - ref))) == pytest.approx(cn["error_vs_scipy"], rel=1e-5)
+    o = fftcn.fft_cn_1d(u0, D, 1.0 / n, cn["dt"], cn["steps"], "spectral", v=v)
+    assert float(np.max(np.abs(u - o))) < 1e-12
+    u = M.imex_advdiff_1d(ut, D, v, 1.0 / n, im["dt"], im["steps"]).cpu().numpy()
+    assert float(np.max(np.abs(u - ref))) == pytest.approx(im["error_vs_scipy"], rel=1e-5)
+    o = fftcn.strang_exp_1d(u0, D, v, 1.0 / n, im["dt"], im["steps"])
+    assert float(np.max(np.abs(u - o))) < 1e-12
+    # a length that is not a power of two takes the general path with the same results
+    m = 768
+    w0 = fftcn.solver_comparison_ic(m)
+    w = M.fft_cn_advdiff_1d(torch.tensor(w0, device=cuda), D, v, 1.0 / m, 1e-3, 200).cpu().numpy()
+    assert float(np.max(np.abs(w - fftcn.fft_cn_1d(w0, D, 1.0 / m, 1e-3, 200, "spectral", v=v)))) < 1e-12
+    w = M.imex_advdiff_1d(torch.tensor(w0, device=cuda), D, v, 1.0 / m, 5e-3, 100).cpu().numpy()
+    assert float(np.max(np.abs(w - fftcn.strang_exp_1d(w0, D, v, 1.0 / m, 5e-3, 100)))) < 1e-12

@@ -315,3 +315,42 @@ def test_fft3d_error_pins(row):
     u = fftcn.fft_cn_3d(u0, cfg["D"], 1.0 / N_, dt, cfg["n_steps"])
     exact = u0 * np.exp(-12 * np.pi ** 2 * cfg["D"] * cfg["n_steps"] * dt)
     assert float(np.max(np.abs(u - exact))) == pytest.approx(row["error"], rel=1e-8)
+
+
+def test_tubular_rk4_pins():
+    # benchmarks/results/reactor_results.json: the penalty-BC RK4 sweep of
+    # benchmark_tubular_reactor.py (N = 128, t_final = 15, 27 cases; the Robin cases equal the
+    # Danckwerts ones).  The oracle's affine-power form is checked against its step loop, then
+    # reproduces every published conversion, error and outlet value.
+    from oracle import reactor as OR
+    g = _load("tubular_published.json")
+    dt, n = OR.tubular_dt(128, 10, 15.0)
+    for bc in OR.TUBULAR_BCS:
+        a = OR.tubular_rk4_loop(128, 10, 1.0, bc, dt, 300)
+        b = OR.tubular_rk4(128, 10, 1.0, bc, dt, 300)
+        assert np.max(np.abs(a - b)) < 1e-12
+    for key, v in g["results"].items():
+        dt, n = OR.tubular_dt(g["N"], v["Pe"], g["t_final"])
+        assert n == v["n_steps"] and dt == pytest.approx(v["dt"], rel=1e-15)
+        s = OR.tubular_summary(OR.tubular_rk4(g["N"], v["Pe"], v["Da"], v["bc_type"], dt, n),
+                               v["Pe"], v["Da"], v["bc_type"], g["t_final"])
+        for k in ("conversion", "error", "final_outlet_c"):
+            assert s[k] == pytest.approx(v[k], rel=1e-8, abs=1e-40), (key, k)
+
+
+def test_solver_comparison_1d_pins():
+    # benchmarks/results/solver_comparison.json: 1D u_t = 0.01 u_xx - u_x, N = 1024, t in
+    # [0, 10]; the max difference of FFT-CN (dt 1e-3) and of the exponential Strang IMEX
+    # (dt 5e-3) from SciPy Radau (tests/golden/radau_advdiff1d.npy, made by
+    # make_radau_advdiff1d.py; 568 output times, as published).
+    g = _load("solver_comparison_published.json")
+    ref = np.load(os.path.join(GOLD, "radau_advdiff1d.npy"))
+    cfg = g["config"]
+    n, D, v, T = cfg["N"], cfg["D"], cfg["v"], cfg["t_final"]
+    u0 = fftcn.solver_comparison_ic(n)
+    cn, imex_ = g["solvers"][1], g["solvers"][2]
+    assert g["solvers"][0]["steps"] == 568
+    u = fftcn.fft_cn_1d(u0, D, 1.0 / n, cn["dt"], cn["steps"], "spectral", v=v)
+    assert float(np.max(np.abs(u - ref))) == pytest.approx(cn["error_vs_scipy"], rel=1e-6)
+    u = fftcn.strang_exp_1d(u0, D, v, 1.0 / n, imex_["dt"], imex_["steps"])
+    assert float(np.max(np.abs(u - ref))) == pytest.approx(imex_["error_vs_scipy"], rel=1e-6)
