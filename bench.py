@@ -14,6 +14,8 @@ of the reaction increments (rel-L2 vs the FP64 path is reported in the line).
   python bench.py --workload explicit --n 4096 [--etd-steps S]      (RK4 advection-diffusion)
   python bench.py --workload nk --n 512 [--etd-steps S]             (BDF2 Newton-Krylov)
   python bench.py --workload stencil --n 4096 [--fp32]               (stencil stage kernel roofline)
+  python bench.py --workload gs256        (the reference's Gray-Scott method benchmark, 256^2 FP64)
+  python bench.py --workload tubular      (the reference's 27-case penalty-RK4 reactor sweep, FP64)
 
 Our arm prints one JSON line with the device-timed value, the end-to-end
 number through the public API with host buffers, the live roofline of the
@@ -64,7 +66,8 @@ def parse():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp32"])
     ap.add_argument("--kernels-only", action="store_true")
-    ap.add_argument("--workload", default="imex", choices=["imex", "etdrk4", "serve", "fft3d", "explicit", "nk", "stencil"])
+    ap.add_argument("--workload", default="imex", choices=["imex", "etdrk4", "serve", "fft3d", "explicit", "nk", "stencil",
+                                                          "gs256", "tubular"])
     ap.add_argument("--fp32", action="store_true", help="fft3d: FP32 instead of FP64")
     ap.add_argument("--requests", type=int, default=256)
     ap.add_argument("--no-configs", action="store_true", help="skip the configs 1, 3, 4, 5 legs of the default line")
@@ -412,7 +415,9 @@ def run_ours(args, rank, world, local):
         if not args.no_configs:
             # the other benchmark configurations, each measured on its own terms
             out["configs"] = {"fft_cn_128": fftcn_leg(dev), "etdrk4_4096": etdrk4_leg(dev),
-                              "nk_bdf2_512": nk_leg(dev), "served_mix": served_mix(dev, args.requests)}
+                              "nk_bdf2_512": nk_leg(dev), "served_mix": served_mix(dev, args.requests),
+                              "stencil_gs_4096": stencil_gs_leg(dev), "tubular_rk4_sweep": tubular_leg(dev),
+                              "gray_scott_256_methods": gs_methods_leg(dev)}
         if not args.no_cpu_baseline and world == 1:
             out["cpu_baseline"] = cpu_baseline(args)
     return out
@@ -831,6 +836,126 @@ def etdrk4_leg(dev, n=4096, steps=100, err_steps=10):
     return out
 
 
+def stencil_gs_leg(dev, n=4096):
+    """The fused 5-point stencil + Gray-Scott reaction stage of the explicit steppers (an RK4
+    middle stage: stage input, step start and running sum read, two outputs written =
+    20 B per point and field in FP32) on a 4096^2 two-field grid, periodic, timed by the
+    autotuner for every tile height and the TMA-staged form (20 launches each, CUDA
+    events); the fastest candidate's rate against the measured HBM peak."""
+    import torch
+    import moljax_gb300 as M
+    from moljax_gb300.core import autotune as AT
+    grid = M.Grid2D(n, n, 0.0, L_BOX, 0.0, L_BOX)
+    model = M.create_gray_scott_model(grid, DU, DV, F, K, dtype=torch.float32)
+    with torch.cuda.device(dev):
+        res = AT.autotune_stencil(model, torch.float32, reps=20, device=dev)
+    b = 2 * n * n * 5 * 4
+    t = min(res.times_ms) * 1e-3
+    peak, peak_kind = peaks()
+    best = res.choice[0]
+    return {"workload": f"stencil + Gray-Scott reaction stage (RK4 middle stage) 2 fields {n}x{n} FP32, periodic",
+            "kernel": "rk_stage_tma_kernel" if best == 64 else "rk_stage_vec_kernel", "best_rows": best,
+            "candidates": [c[0] for c in res.candidates], "ms_per_launch": res.times_ms, "alg_bytes": b,
+            "roofline": {"bound": "hbm", "achieved": b / t / 1e9, "peak": peak, "unit": "GB/s",
+                         "peak_kind": peak_kind, "frac": b / t / 1e9 / peak}}
+
+
+def gs_methods_leg(dev, steps_frac=1.0):
+    """The reference's Gray-Scott method benchmark (benchmarks/benchmark_gray_scott.py,
+    published in benchmarks/results/gray_scott.json): 256^2 on [0,1]^2, Du=2e-5, Dv=1e-5,
+    F=0.035, k=0.065, pseudo-spectral Laplacian, its seed-42 initial condition, FP64, to
+    t = 10 000: CN with the FFT-preconditioned Newton iteration (dt 0.5, 20 000 steps, tol
+    1e-8, at most 10 iterations), the Strang exp-diffusion IMEX (dt 0.5, 20 000 steps) and
+    the benchmark's ETDRK4 (dt 1, 10 000 steps, 32-point contour coefficients).  Each method
+    timed with CUDA events after a 10-step warm-up, against the published wall time of the
+    reference on its own GPU (one run, the median of 10 there)."""
+    import json
+    import torch
+    import moljax_gb300 as M
+    from moljax_gb300.core import stencil
+    from moljax_gb300.workloads import gray_scott_benchmark_ic
+    g = json.load(open(os.path.join(ROOT, "tests", "golden", "gray_scott_published.json")))
+    cfg = g["config"]
+    n = cfg["N"]
+    pub = {m_["name"]: m_ for m_ in g["methods"]}
+    Du, Dv, Fp, Kp = cfg["Du"], cfg["Dv"], cfg["F"], cfg["k"]
+    dx = 1.0 / n
+    u0, v0 = gray_scott_benchmark_ic(n, torch.float64, dev)
+    grid = M.Grid2D(n, n, 0.0, 1.0, 0.0, 1.0)
+    model = M.create_gray_scott_model(grid, Du, Dv, Fp, Kp, dtype=torch.float64)
+    s = torch.cuda.current_stream(dev)
+
+    def timed(fn):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(s)
+        r = fn()
+        e1.record(s)
+        e1.synchronize()
+        return r, e0.elapsed_time(e1) * 1e-3
+
+    def padded(u, v):
+        return {k: t for k, t in zip(("u", "v"), stencil.pad_interior(torch.stack([u, v]), grid, model.bc_spec,
+                                                                        ("u", "v")))}
+    out = {"workload": "Gray-Scott 256^2 method benchmark (benchmark_gray_scott.py), FP64, pseudo-spectral, "
+                       "t_final=10000", "published_hw": "reference's own GPU (RTX 5060), JAX FP64",
+           "methods": {}}
+    st = max(1, int(steps_frac * pub["CN (Newton-Krylov)"]["steps"]))
+    M.gray_scott_cn_newton(u0, v0, Du, Dv, Fp, Kp, dt=0.5, n_steps=10, dx=dx)
+    (u, v, its), t = timed(lambda: M.gray_scott_cn_newton(u0, v0, Du, Dv, Fp, Kp, dt=0.5, n_steps=st, dx=dx))
+    its = its.cpu()
+    out["methods"]["CN (Newton-Krylov)"] = {"steps": st, "time_s": t, "newton_per_step": float(its.double().mean()),
+                                            "published_time_s": pub["CN (Newton-Krylov)"]["time_s"],
+                                            "u_mean": float(u.mean())}
+    st = max(1, int(steps_frac * pub["IMEX-Strang"]["steps"]))
+    M.gray_scott_strang_exp(u0, v0, Du, Dv, Fp, Kp, 0.5, 10, dx)
+    (u, v), t = timed(lambda: M.gray_scott_strang_exp(u0, v0, Du, Dv, Fp, Kp, 0.5, st, dx))
+    out["methods"]["IMEX-Strang"] = {"steps": st, "time_s": t, "published_time_s": pub["IMEX-Strang"]["time_s"],
+                                     "u_mean": float(u.mean())}
+    st = max(1, int(steps_frac * pub["ETDRK4"]["steps"]))
+    y0 = padded(u0, v0)
+    M.etdrk4_gray_scott(model, y0, 1.0, 10, symbol="spectral", variant="benchmark")
+    y, t = timed(lambda: M.etdrk4_gray_scott(model, y0, 1.0, st, symbol="spectral", variant="benchmark"))
+    out["methods"]["ETDRK4"] = {"steps": st, "time_s": t, "published_time_s": pub["ETDRK4"]["time_s"],
+                                "u_mean": float(y["u"][1:-1, 1:-1].mean())}
+    for m_ in out["methods"].values():
+        m_["value"] = n * n * m_["steps"] / m_["time_s"]
+        m_["unit"] = UNIT
+        m_["speedup_vs_published"] = m_["published_time_s"] / m_["time_s"] if steps_frac == 1.0 else None
+    out["not_built"] = {"RK4 (explicit)": "pseudo-spectral RK4 (102 669 steps, published 99.6 s) has no native "
+                                          "driver yet"}
+    return out
+
+
+def tubular_leg(dev):
+    """The 27-case penalty-RK4 tubular-reactor sweep of benchmark_tubular_reactor.py (N = 128,
+    t_final = 15, up to 967 740 RK4 steps per case, FP64) in one launch of the batched
+    reactor kernel, timed with CUDA events after one warm-up sweep, against the sum of the
+    reference's published per-case times (its own GPU, one case at a time); max relative
+    deviation of the conversions from the published ones."""
+    import json
+    import torch
+    from moljax_gb300.core import reactor as R
+    g = json.load(open(os.path.join(ROOT, "tests", "golden", "tubular_published.json")))
+    R.run_tubular_sweep(t_final=0.5, device=dev)
+    s = torch.cuda.current_stream(dev)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    res = R.run_tubular_sweep(N=g["N"], t_final=g["t_final"], dtype=torch.float64, device=dev)
+    e1.record(s)
+    e1.synchronize()
+    t = e0.elapsed_time(e1) * 1e-3
+    pub = g["results"]
+    dev_max = max(abs(res[k]["conversion"] - v["conversion"]) / max(abs(v["conversion"]), 1e-300)
+                  for k, v in pub.items())
+    steps = sum(v["n_steps"] for v in pub.values())
+    return {"workload": "tubular reactor penalty-RK4 sweep, 27 cases (Danckwerts/Robin/Neumann x Pe 1,10,100 x "
+                        "Da 0.1,1,10), N=128, t_final=15, FP64, one launch",
+            "sweep_s": t, "published_sweep_s": sum(v["mean_time"] for v in pub.values()),
+            "published_hw": "reference's own GPU (RTX 5060), one case at a time", "rk4_steps": steps,
+            "value": g["N"] * steps / t, "unit": UNIT, "max_rel_dev_conversion_vs_published": dev_max,
+            "gpu_launches": 1}
+
+
 def served_mix(dev, n_requests, realtime=True, slots=64):
     """The served mix (config 5's Poisson arrivals at 2000/s, seed 5, its first n_requests
     requests): the continuous-batching server (FP32 + float-float Gray-Scott batch engine,
@@ -960,6 +1085,11 @@ def main():
         out = run_nk(args, local)
     elif args.workload == "stencil":
         out = run_stencil(args, local)
+    elif args.workload in ("gs256", "tubular"):
+        import torch
+        dev = torch.device("cuda", local)
+        torch.cuda.set_device(dev)
+        out = gs_methods_leg(dev) if args.workload == "gs256" else tubular_leg(dev)
     elif args.kernels_only:
         out = run_kernels_only(args, local)
     else:

@@ -233,6 +233,17 @@ mjx_status mjx_gs_cn_newton2d(const void* plan, const mjx_grid2d* grid, int dtyp
                               void* y_out, int* iters, int* iters_total, double* last_res, void* ws,
                               size_t ws_bytes, void* stream);
 
+/* Workspace of mjx_gs_strang_exp2d: the two fields' half spectra. */
+size_t mjx_gs_strang_exp_ws_bytes(int ny, int nx, int dtype);
+/* n_steps fixed Strang steps of periodic Gray-Scott (imex_step / imex_solve of
+ * benchmarks/benchmark_gray_scott.py:268-296): explicit Euler half step of the reaction,
+ * exact exp(dt D lam) diffusion (lam from plan: FD or pseudo-spectral), explicit Euler half
+ * step.  y_in / y_out: [u; v] interiors [2][ny][nx] (may alias); D[2] = (Du, Dv).  One row
+ * and one column pass per step (nx >= 16, powers of two). */
+mjx_status mjx_gs_strang_exp2d(const void* plan, const mjx_grid2d* grid, int dtype, const double* D, double F,
+                               double k, double dt, int n_steps, const void* y_in, void* y_out, void* ws,
+                               size_t ws_bytes, void* stream);
+
 /* Size of the fixed device scratch used by mjx_fft_cn2d_noalloc (8 MiB). */
 #define MJX_NOALLOC_SCRATCH_BYTES (8u << 20)
 

@@ -517,6 +517,32 @@ def imex_advdiff_1d(u0: torch.Tensor, D: float, v: float, dx: float, dt: float, 
     return a[0].clone()
 
 
+def gray_scott_strang_exp(u0: torch.Tensor, v0: torch.Tensor, Du: float, Dv: float, F: float, k: float,
+                          dt: float, n_steps: int, dx: float, dy: Optional[float] = None,
+                          symbol: str = "spectral"):
+    """Fixed Strang steps of periodic Gray-Scott as benchmarks/benchmark_gray_scott.py:268-296
+    (imex_step / imex_solve): explicit Euler half step of the reaction, exact exponential
+    diffusion exp(dt D lam) by FFT, explicit Euler half step; pseudo-spectral Laplacian by
+    default, as the benchmark.  One row and one column pass per step (``mjx_gs_strang_exp2d``).
+    Returns (u, v)."""
+    u0 = u0.contiguous()
+    N.require_cuda(u0, v0)
+    ny, nx = u0.shape
+    dy = dx if dy is None else dy
+    plan = get_plan(ny, nx, dy, dx, symbol, u0.dtype, u0.device)
+    if getattr(plan, "general", False):
+        raise ValueError("gray_scott_strang_exp: grid sides must be powers of two")
+    lib = N.lib()
+    y = torch.stack([u0, v0.to(u0.dtype)]).contiguous()
+    out = torch.empty_like(y)
+    ws = workspace(lib.mjx_gs_strang_exp_ws_bytes(ny, nx, plan.code), plan.device, "gs_strang")
+    Dc = (C.c_double * 2)(float(Du), float(Dv))
+    N.check("mjx_gs_strang_exp2d", lib.mjx_gs_strang_exp2d(
+        N.ptr(plan.buf), C.byref(plan.cgrid), plan.code, Dc, float(F), float(k), float(dt), int(n_steps),
+        N.ptr(y), N.ptr(out), N.ptr(ws), ws.numel(), N.stream_ptr(plan.device)))
+    return out[0], out[1]
+
+
 def gray_scott_cn_newton(u0: torch.Tensor, v0: torch.Tensor, Du: float, Dv: float, F: float, k: float,
                          dt: float, n_steps: int, dx: float, dy: Optional[float] = None, tol: float = 1e-8,
                          max_iter: int = 10, symbol: str = "spectral"):

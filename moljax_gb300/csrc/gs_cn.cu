@@ -336,6 +336,81 @@ static mjx_status gcn_run(const void* plan, const mjx_grid2d* g, const double* D
   return cuda_status(ce);
 }
 
+// Fixed-step Strang splitting of the same benchmark (benchmarks/benchmark_gray_scott.py:
+// 268-296): explicit Euler half step of the reaction, exact exponential diffusion
+// exp(dt D lam) by FFT, explicit Euler half step.  The second half step of step i and
+// the first of step i+1 are two consecutive pointwise Euler steps, so a step is one column
+// pass (forward, times exp(dt D lam), inverse) and one row pass (c2r, two Euler half
+// steps, r2c); the first half step rides the initial r2c and the last step's row pass
+// stores the real fields.  The middle steps are replayed from a graph of up to 64 steps.
+template <typename T>
+static mjx_status gse_run(const void* plan, const mjx_grid2d* g, const double* D, double F, double k, double dt,
+                          int n_steps, const T* y_in, T* y_out, char* ws, cudaStream_t s) {
+  const int ny = g->ny, nx = g->nx, ldc = spec_ldc(nx);
+  const long long fr = (long long)ny * nx, fs = (long long)ny * ldc;
+  const PlanView pv = plan_view(plan, ny, nx, sizeof(T));
+  cx<T>* spec = (cx<T>*)ws;
+  if (y_out != y_in) MJX_CUDA_TRY(cudaMemcpyAsync(y_out, y_in, sizeof(T) * 2 * fr, cudaMemcpyDeviceToDevice, s));
+  if (n_steps <= 0) return cuda_status(cudaStreamSynchronize(s));
+  RowArgs<T> r;
+  memset(&r, 0, sizeof(r));
+  r.n = nx; r.log2n = ilog2_exact(nx); r.ldc = ldc; r.nrows = ny; r.npairs = 1;
+  r.nseq = row_nseq(nx, ny); r.rstride = nx; r.rin_sel = -1; r.rout_sel = -1;
+  r.rin[0] = y_out; r.rout[0] = y_out; r.spec = spec; r.tw = (const cx<T>*)pv.twx; r.inv_scale = (T)1;
+  r.hfixed = dt; r.F = F; r.k = k;
+  r.pr[0].ra = 0; r.pr[0].rb = fr; r.pr[0].sa = 0; r.pr[0].sb = fs; r.pr[0].hfac = 0.5;
+  const int RE = ROW_REACT | ROW_EULER;
+  RowArgs<T> first = r, mid = r, last = r;
+  first.pr[0].flags = RE | ROW_STORE_SPEC;
+  mid.pr[0].flags = ROW_LOAD_SPEC | RE | ROW_EULER2 | ROW_STORE_SPEC;
+  last.pr[0].flags = ROW_LOAD_SPEC | RE | ROW_STORE_REAL;
+  ColArgs<T> c;
+  memset(&c, 0, sizeof(c));
+  c.ny = ny; c.log2ny = ilog2_exact(ny); c.ncols = nx / 2 + 1; c.ldc = ldc;
+  c.C = col_tile(ny, c.ncols, 1, sizeof(T)); c.spec = spec; c.lamx = (const T*)pv.lamx;
+  c.lamy = (const T*)pv.lamy; c.tw = (const cx<T>*)pv.twy; c.scale = (T)(1.0 / ((double)nx * ny));
+  c.njobs = 2; c.hfixed = dt;
+  for (int f = 0; f < 2; ++f) {
+    ColJob& j = c.job[f];
+    j.sin = j.sout[0] = j.sout[1] = f * fs;
+    j.nout = 1; j.D = D[f]; j.pow[0] = j.pow[1] = 1; j.mul = MUL_EXP; j.hfac[0] = j.hfac[1] = 1.0;
+  }
+  cudaError_t ce = launch_row<T, RX_GRAY_SCOTT>(first, s);
+  const int nmid = n_steps - 1;
+  const int B = nmid < 64 ? nmid : 64;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  cudaStream_t cs = nullptr;
+  if (ce == cudaSuccess && B > 0 && nmid / B > 1) {  // a graph of B middle steps
+    ce = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+    if (ce == cudaSuccess) ce = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+    if (ce == cudaSuccess) {
+      cudaError_t le = cudaSuccess;
+      for (int i = 0; i < B && le == cudaSuccess; ++i) {
+        le = launch_col<T>(c, cs);
+        if (le == cudaSuccess) le = launch_row<T, RX_GRAY_SCOTT>(mid, cs);
+      }
+      ce = cudaStreamEndCapture(cs, &graph);
+      if (le != cudaSuccess) ce = le;
+    }
+    if (ce == cudaSuccess) ce = cudaGraphInstantiate(&exec, graph, 0);
+  }
+  int done = 0;
+  if (exec != nullptr)
+    for (; done + B <= nmid && ce == cudaSuccess; done += B) ce = cudaGraphLaunch(exec, s);
+  for (; done < nmid && ce == cudaSuccess; ++done) {
+    ce = launch_col<T>(c, s);
+    if (ce == cudaSuccess) ce = launch_row<T, RX_GRAY_SCOTT>(mid, s);
+  }
+  if (ce == cudaSuccess) ce = launch_col<T>(c, s);
+  if (ce == cudaSuccess) ce = launch_row<T, RX_GRAY_SCOTT>(last, s);
+  if (ce == cudaSuccess) ce = cudaStreamSynchronize(s);
+  if (exec) cudaGraphExecDestroy(exec);
+  if (graph) cudaGraphDestroy(graph);
+  if (cs) cudaStreamDestroy(cs);
+  return cuda_status(ce);
+}
+
 }  // namespace mjx
 
 using namespace mjx;
@@ -376,6 +451,28 @@ mjx_status mjx_gs_cn_newton2d(const void* plan, const mjx_grid2d* g, int dtype, 
   if (iters_total) *iters_total = out.iters_sum;
   if (last_res) *last_res = out.res;
   return MJX_OK;
+}
+
+size_t mjx_gs_strang_exp_ws_bytes(int ny, int nx, int dtype) {
+  const int e = elem_size(dtype);
+  if (!e || ilog2_exact(nx) < 4 || ilog2_exact(ny) < 1) return 0;
+  return (size_t)2 * ny * spec_ldc(nx) * 2 * e;
+}
+
+mjx_status mjx_gs_strang_exp2d(const void* plan, const mjx_grid2d* g, int dtype, const double* D, double F,
+                               double k, double dt, int n_steps, const void* y_in, void* y_out, void* ws,
+                               size_t ws_bytes, void* stream) {
+  MJX_TRY(check_grid(g));
+  if (g->nx < 16) return MJX_BAD_SHAPE;
+  if (plan == nullptr || D == nullptr || y_in == nullptr || y_out == nullptr || n_steps < 0) return MJX_BAD_ARG;
+  const int e = elem_size(dtype);
+  if (!e) return MJX_BAD_DTYPE;
+  if (ws == nullptr || ws_bytes < mjx_gs_strang_exp_ws_bytes(g->ny, g->nx, dtype)) return MJX_WORKSPACE;
+  MJX_TRY(ensure_kernel_attrs());
+  cudaStream_t s = (cudaStream_t)stream;
+  if (e == 4)
+    return gse_run<float>(plan, g, D, F, k, dt, n_steps, (const float*)y_in, (float*)y_out, (char*)ws, s);
+  return gse_run<double>(plan, g, D, F, k, dt, n_steps, (const double*)y_in, (double*)y_out, (char*)ws, s);
 }
 
 }  // extern "C"

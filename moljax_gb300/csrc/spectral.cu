@@ -194,7 +194,10 @@ __global__ void __launch_bounds__(256, Occ<T>::row) row_kernel(const __grid_cons
     }
     if (flags & ROW_REACT) {
       if (flags & ROW_DELTA) react_delta<T, RX>(va, vb, h, pF, pK, pR);
-      else if (flags & ROW_EULER) react_euler<T, RX>(va, vb, h, pF, pK, pR);
+      else if (flags & ROW_EULER) {
+        react_euler<T, RX>(va, vb, h, pF, pK, pR);
+        if (flags & ROW_EULER2) react_euler<T, RX>(va, vb, h, pF, pK, pR);
+      }
       else react_heun<T, RX>(va, vb, h, pF, pK, pR);
     }
     if (flags & ROW_STORE_REAL) { oa[x] = va; ob[x] = vb; }

@@ -44,6 +44,7 @@ enum {
   ROW_NONLIN = 128,    // replace (a, b) by the reaction terms N(a, b) (exponential integrators)
   ROW_SPEC_ALT = 256,  // store the spectrum at (oa, ob) instead of (sa, sb)
   ROW_EULER = 512,     // with ROW_REACT: explicit Euler reaction step instead of Heun
+  ROW_EULER2 = 1024,   // with ROW_EULER: a second Euler step of the same length after the first
 };
 
 // pointwise reaction kinds (compile-time)

@@ -5,6 +5,10 @@ examples/gray_scott_2d.py:42-73: u = 1, v = 0 except the central square
 |x-cx| < 0.1 Lx, |y-cy| < 0.1 Ly where u = 0.5, v = 0.25, plus 0.01*U[-1,1]
 noise on the padded arrays.  The reference draws the noise from
 jax.random.PRNGKey(42); here it comes from numpy.random.default_rng(seed).
+
+``gray_scott_benchmark_ic`` is the initial condition of the reference's Gray-Scott
+method benchmark (benchmarks/benchmark_gray_scott.py:59-68), drawn from numpy's
+legacy seed-42 stream exactly as the script does.
 """
 
 from __future__ import annotations
@@ -28,3 +32,16 @@ def gray_scott_initial_condition(grid, seed: int = 20261203, dtype=torch.float32
     v = v + noise * rng.uniform(-1.0, 1.0, v.shape)
     return {"u": torch.tensor(u, dtype=dtype, device=device),
             "v": torch.tensor(v, dtype=dtype, device=device)}
+
+
+def gray_scott_benchmark_ic(n: int = 256, dtype=torch.float64, device="cuda"):
+    """(u0, v0) interiors of benchmarks/benchmark_gray_scott.py:59-68: 1 - 0.05 U[0,1) and
+    0.25 + 0.05 U[0,1) from numpy.random.seed(42), and a 20 x 20 square of (0.5, 0.25) at
+    the centre."""
+    rs = np.random.RandomState(42)
+    u0 = np.ones((n, n)) - 0.5 * rs.rand(n, n) * 0.1
+    v0 = 0.25 * np.ones((n, n)) + 0.5 * rs.rand(n, n) * 0.1
+    c, r = n // 2, 10
+    u0[c - r:c + r, c - r:c + r] = 0.5
+    v0[c - r:c + r, c - r:c + r] = 0.25
+    return (torch.tensor(u0, dtype=dtype, device=device), torch.tensor(v0, dtype=dtype, device=device))

@@ -1,11 +1,14 @@
-"""Oracle: Crank-Nicolson Gray-Scott by the preconditioned Newton iteration.
+"""Oracle: the Gray-Scott benchmark's fixed-step methods.
 
-TEST INFRASTRUCTURE ONLY (see ``oracle/__init__.py``).  NumPy FP64 restatement
-of benchmarks/benchmark_gray_scott.py:162-228 (cn_newton_step_jit): per step the
-CN residual with pseudo-spectral (or any given) Laplacian eigenvalues, the exact
-periodic inverse of (I - dt/2 D Lap) as the preconditioner, u <- u + M^-1(-res),
-while max|res_u| + max|res_v| > tol and i < max_iter, starting from u_old with
-res_norm = 1.
+TEST INFRASTRUCTURE ONLY (see ``oracle/__init__.py``).  NumPy FP64 restatements
+of benchmarks/benchmark_gray_scott.py:
+* 162-228 (cn_newton_step_jit): per step the CN residual with pseudo-spectral (or
+  any given) Laplacian eigenvalues, the exact periodic inverse of
+  (I - dt/2 D Lap) as the preconditioner, u <- u + M^-1(-res), while
+  max|res_u| + max|res_v| > tol and i < max_iter, starting from u_old with
+  res_norm = 1;
+* 268-296 (imex_step / imex_solve): explicit Euler half step of the reaction,
+  exact exponential diffusion by FFT, explicit Euler half step.
 """
 
 from __future__ import annotations
@@ -21,10 +24,14 @@ def spectral_symbol(n, dx):
 
 
 def benchmark_ic(n):
-    """benchmarks/benchmark_gray_scott.py:60-62 (numpy's legacy seed 42 stream)."""
+    """benchmarks/benchmark_gray_scott.py:59-68 (numpy's legacy seed 42 stream): noise about
+    (1, 0.25) and a 2r x 2r square (r = 10) of (0.5, 0.25) at the centre."""
     rs = np.random.RandomState(42)
     u0 = np.ones((n, n)) - 0.5 * rs.rand(n, n) * 0.1
     v0 = 0.25 * np.ones((n, n)) + 0.5 * rs.rand(n, n) * 0.1
+    c, r = n // 2, 10
+    u0[c - r:c + r, c - r:c + r] = 0.5
+    v0[c - r:c + r, c - r:c + r] = 0.25
     return u0, v0
 
 
@@ -59,3 +66,24 @@ def cn_solve(u0, v0, lam, Du, Dv, F, k, dt, n_steps, tol=1e-8, max_iter=10):
         u, v, it = cn_newton_step(u, v, lam, Du, Dv, F, k, dt, tol, max_iter)
         its.append(it)
     return u, v, its
+
+
+def strang_exp_step(u, v, lam, Du, Dv, F, k, dt):
+    """benchmarks/benchmark_gray_scott.py:268-289."""
+    uvv = u * v * v
+    u = u + 0.5 * dt * (-uvv + F * (1 - u))
+    v = v + 0.5 * dt * (uvv - (F + k) * v)
+    u = np.real(np.fft.ifft2(np.fft.fft2(u) * np.exp(dt * Du * lam)))
+    v = np.real(np.fft.ifft2(np.fft.fft2(v) * np.exp(dt * Dv * lam)))
+    uvv = u * v * v
+    u = u + 0.5 * dt * (-uvv + F * (1 - u))
+    v = v + 0.5 * dt * (uvv - (F + k) * v)
+    return u, v
+
+
+def strang_exp_solve(u0, v0, lam, Du, Dv, F, k, dt, n_steps):
+    """imex_solve (291-296): n_steps steps."""
+    u, v = u0, v0
+    for _ in range(n_steps):
+        u, v = strang_exp_step(u, v, lam, Du, Dv, F, k, dt)
+    return u, v

@@ -5,7 +5,8 @@ The fixtures hold only the numbers the tests pin:
 the FFT-CN error tables of benchmarks/results/precision_fp32_fp64.json and
 benchmarks/results/scipy_comparison.json, the CN reactor conversions of
 benchmarks/results/method_comparison_results.json, and the 3D FFT-CN errors and
-times of benchmarks/results/3d_feasibility.json, the penalty-RK4 reactor sweep of
+times of benchmarks/results/3d_feasibility.json, the Gray-Scott method timings of
+benchmarks/results/gray_scott.json, the penalty-RK4 reactor sweep of
 benchmarks/results/reactor_results.json and the 1D solver comparison of
 benchmarks/results/solver_comparison.json.
 """
@@ -56,8 +57,13 @@ def main(ref):
         json.dump({"source": "benchmarks/results/reactor_results.json", "N": 128, "t_final": 15.0,
                    "config": rr["config"],
                    "results": {k: {kk: v[kk] for kk in ("bc_type", "Pe", "Da", "conversion", "error", "dt",
-                                                          "n_steps", "final_outlet_c")}
+                                                          "n_steps", "final_outlet_c", "mean_time")}
                                for k, v in rr["results"].items()}}, f, indent=1)
+    gsb = json.load(open(os.path.join(res, "gray_scott.json")))
+    with open(os.path.join(HERE, "gray_scott_published.json"), "w") as f:
+        json.dump({"source": "benchmarks/results/gray_scott.json", "config": gsb["config"],
+                   "methods": [{k: m_[k] for k in ("name", "time_s", "steps", "dt", "t_final")}
+                               for m_ in gsb["methods"]]}, f, indent=1)
     so = json.load(open(os.path.join(res, "solver_comparison.json")))
     with open(os.path.join(HERE, "solver_comparison_published.json"), "w") as f:
         json.dump({"source": "benchmarks/results/solver_comparison.json", "config": so["config"],

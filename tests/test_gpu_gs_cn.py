@@ -38,3 +38,23 @@ def test_gs_cn_newton_iteration_cap_and_fd_symbol(cuda):
     ru, rv, rits = G.cn_solve(u0, v0, lam, P["Du"], P["Dv"], P["F"], P["k"], 0.5, 3, max_iter=2)
     assert its.cpu().tolist() == rits == [2, 2, 2]
     assert float(np.linalg.norm(u.cpu().numpy() - ru) / np.linalg.norm(ru)) < 1e-11
+
+
+@pytest.mark.parametrize("n,steps", [(64, 40), (256, 12)])
+def test_gs_strang_exp_vs_oracle(cuda, n, steps):
+    """The benchmark's Strang exp-diffusion IMEX (imex_step, benchmark_gray_scott.py:268-296)
+    against the oracle, FP64, pseudo-spectral; steps beyond one graph of 64 and below it."""
+    import moljax_gb300 as M
+    u0, v0 = G.benchmark_ic(n)
+    dx = 1.0 / n
+    lam = G.spectral_symbol(n, dx)
+    for st in (1, steps, 130):
+        u, v = M.gray_scott_strang_exp(torch.tensor(u0, device=cuda), torch.tensor(v0, device=cuda),
+                                       P["Du"], P["Dv"], P["F"], P["k"], 0.5, st, dx)
+        ru, rv = G.strang_exp_solve(u0, v0, lam, P["Du"], P["Dv"], P["F"], P["k"], 0.5, st)
+        for a, b in ((u, ru), (v, rv)):
+            assert float(np.linalg.norm(a.cpu().numpy() - b) / np.linalg.norm(b)) < 1e-12, st
+    # the benchmark's initial condition as the package builds it equals the oracle's
+    from moljax_gb300.workloads import gray_scott_benchmark_ic
+    uu, vv = gray_scott_benchmark_ic(n, torch.float64, cuda)
+    assert np.array_equal(uu.cpu().numpy(), u0) and np.array_equal(vv.cpu().numpy(), v0)
