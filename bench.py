@@ -865,8 +865,9 @@ def gs_methods_leg(dev, steps_frac=1.0):
     published in benchmarks/results/gray_scott.json): 256^2 on [0,1]^2, Du=2e-5, Dv=1e-5,
     F=0.035, k=0.065, pseudo-spectral Laplacian, its seed-42 initial condition, FP64, to
     t = 10 000: CN with the FFT-preconditioned Newton iteration (dt 0.5, 20 000 steps, tol
-    1e-8, at most 10 iterations), the Strang exp-diffusion IMEX (dt 0.5, 20 000 steps) and
-    the benchmark's ETDRK4 (dt 1, 10 000 steps, 32-point contour coefficients).  Each method
+    1e-8, at most 10 iterations), the Strang exp-diffusion IMEX (dt 0.5, 20 000 steps), the
+    benchmark's ETDRK4 (dt 1, 10 000 steps, 32-point contour coefficients) and the
+    pseudo-spectral RK4 (dt 0.0974 = 0.9 of its stability limit, 102 669 steps).  Each method
     timed with CUDA events after a 10-step warm-up, against the published wall time of the
     reference on its own GPU (one run, the median of 10 there)."""
     import json
@@ -917,12 +918,16 @@ def gs_methods_leg(dev, steps_frac=1.0):
     y, t = timed(lambda: M.etdrk4_gray_scott(model, y0, 1.0, st, symbol="spectral", variant="benchmark"))
     out["methods"]["ETDRK4"] = {"steps": st, "time_s": t, "published_time_s": pub["ETDRK4"]["time_s"],
                                 "u_mean": float(y["u"][1:-1, 1:-1].mean())}
+    rk = pub["RK4 (explicit)"]
+    st = max(1, int(steps_frac * rk["steps"]))
+    M.gray_scott_rk4_spectral(u0, v0, Du, Dv, Fp, Kp, rk["dt"], 10, dx)
+    (u, v), t = timed(lambda: M.gray_scott_rk4_spectral(u0, v0, Du, Dv, Fp, Kp, rk["dt"], st, dx))
+    out["methods"]["RK4 (explicit)"] = {"steps": st, "time_s": t, "published_time_s": rk["time_s"],
+                                        "u_mean": float(u.mean())}
     for m_ in out["methods"].values():
         m_["value"] = n * n * m_["steps"] / m_["time_s"]
         m_["unit"] = UNIT
         m_["speedup_vs_published"] = m_["published_time_s"] / m_["time_s"] if steps_frac == 1.0 else None
-    out["not_built"] = {"RK4 (explicit)": "pseudo-spectral RK4 (102 669 steps, published 99.6 s) has no native "
-                                          "driver yet"}
     return out
 
 

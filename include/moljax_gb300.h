@@ -244,6 +244,17 @@ mjx_status mjx_gs_strang_exp2d(const void* plan, const mjx_grid2d* grid, int dty
                                double k, double dt, int n_steps, const void* y_in, void* y_out, void* ws,
                                size_t ws_bytes, void* stream);
 
+/* Workspace of mjx_gs_rk4_spectral2d: half spectra, stage input and running sum. */
+size_t mjx_gs_rk4_spectral_ws_bytes(int ny, int nx, int dtype);
+/* n_steps classical RK4 steps of periodic Gray-Scott with the Laplacian by FFT
+ * (rk4_rhs / rk4_step / rk4_solve of benchmarks/benchmark_gray_scott.py:93-131; lam from
+ * plan: pseudo-spectral as the benchmark, or FD).  Per stage one column pass (D lam) and
+ * one row pass (inverse, reaction, running sum, next stage input, forward).  Same
+ * arguments as mjx_gs_strang_exp2d. */
+mjx_status mjx_gs_rk4_spectral2d(const void* plan, const mjx_grid2d* grid, int dtype, const double* D, double F,
+                                 double k, double dt, int n_steps, const void* y_in, void* y_out, void* ws,
+                                 size_t ws_bytes, void* stream);
+
 /* Size of the fixed device scratch used by mjx_fft_cn2d_noalloc (8 MiB). */
 #define MJX_NOALLOC_SCRATCH_BYTES (8u << 20)
 
@@ -544,9 +555,8 @@ size_t mjx_reactor_smem_bytes(int n, int dtype);
 mjx_status mjx_reactor_cn_batch(const mjx_reactor_instance* inst_dev, int n_inst, int max_n,
                                 int dtype, void* out, void* stream);
 /* n_inst penalty-BC RK4 reactor solves (variants MJX_REACTOR_RK4_*; c_init the uniform
- * initial state, c_inlet the inlet value c_in; 3 <= n <= max_n, max_n <= 1024 FP32 or 512
- * FP64) in one launch, one warp per instance with the whole state in registers.  Replaces
- * solve_rk4 with
+ * initial state, c_inlet the inlet value c_in; 3 <= n <= max_n <= 1024) in one launch, one
+ * CTA of four warps per instance with the whole state in registers.  Replaces solve_rk4 with
  * create_rhs_danckwerts / create_rhs_robin / create_rhs_neumann
  * (benchmarks/benchmark_tubular_reactor.py:84-192, 254-301), whose RHS is a dense n x n
  * matvec.  An instance of another variant or an n outside [3, max_n] comes back as NaN. */

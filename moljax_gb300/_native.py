@@ -120,6 +120,9 @@ SIGNATURES = {
     "mjx_fft_cn2d_noalloc": (_i, [_vp, C.POINTER(Grid2DC), _i, _d, _d, _i, _vp, _vp, _vp]),
     "mjx_gs_cn_ws_bytes": (_sz, [_i, _i, _i]),
     "mjx_gs_strang_exp_ws_bytes": (_sz, [_i, _i, _i]),
+    "mjx_gs_rk4_spectral_ws_bytes": (_sz, [_i, _i, _i]),
+    "mjx_gs_rk4_spectral2d": (_i, [_vp, C.POINTER(Grid2DC), _i, C.POINTER(C.c_double), _d, _d, _d, _i, _vp, _vp,
+                                   _vp, _sz, _vp]),
     "mjx_gs_strang_exp2d": (_i, [_vp, C.POINTER(Grid2DC), _i, C.POINTER(C.c_double), _d, _d, _d, _i, _vp, _vp,
                                  _vp, _sz, _vp]),
     "mjx_gs_cn_newton2d": (_i, [_vp, C.POINTER(Grid2DC), _i, C.POINTER(C.c_double), _d, _d, _d, _i, _d, _i, _vp,

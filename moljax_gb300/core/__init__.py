@@ -23,7 +23,7 @@ from moljax_gb300.core.fft_solvers import (create_fft_cache, solve_helmholtz_2d,
                                            apply_spectral_filter_field, apply_spectral_filter_state,
                                            create_fft_cache_1d, solve_helmholtz_1d,
                                            build_wavenumbers_2d, fft_cn_advdiff_1d, imex_advdiff_1d,
-                                           gray_scott_strang_exp)
+                                           gray_scott_strang_exp, gray_scott_rk4_spectral)
 from moljax_gb300.core.utils import StatusCode
 from moljax_gb300.core import fft_integrators, fft_operators
 from moljax_gb300.core.fft_integrators import (etdrk4_gray_scott, etdrk4_step, etd_integrate, etd1_step,

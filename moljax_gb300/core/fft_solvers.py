@@ -543,6 +543,31 @@ def gray_scott_strang_exp(u0: torch.Tensor, v0: torch.Tensor, Du: float, Dv: flo
     return out[0], out[1]
 
 
+def gray_scott_rk4_spectral(u0: torch.Tensor, v0: torch.Tensor, Du: float, Dv: float, F: float, k: float,
+                            dt: float, n_steps: int, dx: float, dy: Optional[float] = None,
+                            symbol: str = "spectral"):
+    """Classical RK4 of periodic Gray-Scott with the Laplacian by FFT, as
+    benchmarks/benchmark_gray_scott.py:93-131 (rk4_rhs / rk4_step / rk4_solve); pseudo-spectral
+    by default.  Per stage one column and one row pass (``mjx_gs_rk4_spectral2d``).
+    Returns (u, v)."""
+    u0 = u0.contiguous()
+    N.require_cuda(u0, v0)
+    ny, nx = u0.shape
+    dy = dx if dy is None else dy
+    plan = get_plan(ny, nx, dy, dx, symbol, u0.dtype, u0.device)
+    if getattr(plan, "general", False):
+        raise ValueError("gray_scott_rk4_spectral: grid sides must be powers of two")
+    lib = N.lib()
+    y = torch.stack([u0, v0.to(u0.dtype)]).contiguous()
+    out = torch.empty_like(y)
+    ws = workspace(lib.mjx_gs_rk4_spectral_ws_bytes(ny, nx, plan.code), plan.device, "gs_rk4")
+    Dc = (C.c_double * 2)(float(Du), float(Dv))
+    N.check("mjx_gs_rk4_spectral2d", lib.mjx_gs_rk4_spectral2d(
+        N.ptr(plan.buf), C.byref(plan.cgrid), plan.code, Dc, float(F), float(k), float(dt), int(n_steps),
+        N.ptr(y), N.ptr(out), N.ptr(ws), ws.numel(), N.stream_ptr(plan.device)))
+    return out[0], out[1]
+
+
 def gray_scott_cn_newton(u0: torch.Tensor, v0: torch.Tensor, Du: float, Dv: float, F: float, k: float,
                          dt: float, n_steps: int, dx: float, dy: Optional[float] = None, tol: float = 1e-8,
                          max_iter: int = 10, symbol: str = "spectral"):

@@ -210,17 +210,28 @@ __global__ void __launch_bounds__(256) reactor_kernel(ReactorArgs A) {
 // dz = 1/(n-1), interior rows (1/Pe) D2 c - D1 c - Da c with central D1, and the end rows
 // replaced by relaxations 100 (target - c) toward the BC value (Danckwerts / Robin inlet
 // (c_in + k c_1)/(1 + k), k = (1/Pe)/dz; Neumann c_1; outlet c_{n-2}, Robin written as
-// (c_{n-2}/dz)/(1/dz) like the reference).  The RHS is a 3-point stencil, so one warp
-// holds a whole instance in registers (P contiguous nodes per lane, n <= 32 P) and the
-// four stages of a step exchange only the lane-boundary nodes by shuffle: no shared
-// memory and no block barrier in the time loop.  Four instances per CTA.
-// f(s) in place: each node's left neighbour is carried from the previous iteration
-// (the value before it was overwritten), so one array holds both the stage input and k.
+// (c_{n-2}/dz)/(1/dz) like the reference).  The RHS is a 3-point stencil and the state fits
+// in registers: one CTA of RW warps per instance, P contiguous nodes per lane
+// (n <= 32 RW P).  The stages exchange only boundary nodes: by shuffle inside a warp and
+// through two shared-memory slots (alternating by stage, one barrier per stage) between
+// warps.  FP64 runs at a low rate on this part and each warp issues to one SM sub-
+// partition, so spreading an instance over four warps uses all four FP64 units of the SM.
+enum { RW = 4 };
+
 template <typename T, int P>
 __device__ __forceinline__ void rk4_rhs(T (&s)[P], int i0, int n, int bc, T iPe, T idz2, T hidz, T Da, T kin,
-                                        T cin, T idz) {
-  const T sl = __shfl_up_sync(0xffffffffu, s[P - 1], 1);
-  const T sr = __shfl_down_sync(0xffffffffu, s[0], 1);
+                                        T cin, T idz, T* xch, int stage) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  T sl = __shfl_up_sync(0xffffffffu, s[P - 1], 1);
+  T sr = __shfl_down_sync(0xffffffffu, s[0], 1);
+  T* slot = xch + (stage & 1) * 2 * RW;
+  if (lane == 0) slot[2 * warp] = s[0];
+  if (lane == 31) slot[2 * warp + 1] = s[P - 1];
+  __syncthreads();
+  if (lane == 0 && warp > 0) sl = slot[2 * (warp - 1) + 1];
+  if (lane == 31 && warp < RW - 1) sr = slot[2 * (warp + 1)];
+  // f(s) in place: each node's left neighbour is carried from the previous iteration
+  // (the value before it was overwritten), so one array holds both the stage input and k
   T cm = sl;
 #pragma unroll
   for (int q = 0; q < P; ++q) {
@@ -243,39 +254,37 @@ __device__ __forceinline__ void rk4_rhs(T (&s)[P], int i0, int n, int bc, T iPe,
 }
 
 template <typename T, int P>
-__global__ void __launch_bounds__(128) reactor_rk4_kernel(ReactorArgs A) {
-  const int w = blockIdx.x * 4 + (threadIdx.x >> 5);
-  if (w >= A.n_inst) return;  // warp-uniform
-  const int lane = threadIdx.x & 31;
-  const mjx_reactor_instance I = A.inst[w];
+__global__ void __launch_bounds__(32 * RW) reactor_rk4_kernel(ReactorArgs A) {
+  __shared__ T xch[2 * 2 * RW];
+  const mjx_reactor_instance I = A.inst[blockIdx.x];
   const int n = I.n, bc = I.variant;
   T* out = reinterpret_cast<T*>(A.out) + I.offset;
-  const bool ok = n >= 3 && n <= 32 * P && bc >= MJX_REACTOR_RK4_DANCKWERTS && bc <= MJX_REACTOR_RK4_NEUMANN;
+  const bool ok = n >= 3 && n <= 32 * RW * P && bc >= MJX_REACTOR_RK4_DANCKWERTS && bc <= MJX_REACTOR_RK4_NEUMANN;
   if (!ok) {  // not this kernel's instance: NaN, never an out-of-range write
-    for (int i = lane; i < n && i < 32 * P; i += 32) out[i] = (T)NAN;
+    for (int i = threadIdx.x; i < n && i < 32 * RW * P; i += blockDim.x) out[i] = (T)NAN;
     return;
   }
   const double dz = 1.0 / (n - 1);
   const T iPe = (T)(1.0 / I.Pe), idz2 = (T)(1.0 / (dz * dz)), hidz = (T)(0.5 / dz), Da = (T)I.Da;
   const T idz = (T)(1.0 / dz), kin = (T)((1.0 / I.Pe) / dz), cin = (T)I.c_inlet;
   const T dt = (T)I.dt, hdt = (T)(0.5 * I.dt), dt6 = (T)(I.dt / 6.0);
-  const int i0 = lane * P;
+  const int i0 = threadIdx.x * P;
   T c[P], acc[P], y[P];
 #pragma unroll
   for (int q = 0; q < P; ++q) c[q] = i0 + q < n ? (T)I.c_init : (T)0;
   for (int step = 0; step < I.n_steps; ++step) {
 #pragma unroll
     for (int q = 0; q < P; ++q) y[q] = c[q];
-    rk4_rhs<T, P>(y, i0, n, bc, iPe, idz2, hidz, Da, kin, cin, idz);  // k1
+    rk4_rhs<T, P>(y, i0, n, bc, iPe, idz2, hidz, Da, kin, cin, idz, xch, 0);  // k1
 #pragma unroll
     for (int q = 0; q < P; ++q) { acc[q] = y[q]; y[q] = c[q] + hdt * y[q]; }
-    rk4_rhs<T, P>(y, i0, n, bc, iPe, idz2, hidz, Da, kin, cin, idz);  // k2
+    rk4_rhs<T, P>(y, i0, n, bc, iPe, idz2, hidz, Da, kin, cin, idz, xch, 1);  // k2
 #pragma unroll
     for (int q = 0; q < P; ++q) { acc[q] += (T)2 * y[q]; y[q] = c[q] + hdt * y[q]; }
-    rk4_rhs<T, P>(y, i0, n, bc, iPe, idz2, hidz, Da, kin, cin, idz);  // k3
+    rk4_rhs<T, P>(y, i0, n, bc, iPe, idz2, hidz, Da, kin, cin, idz, xch, 0);  // k3
 #pragma unroll
     for (int q = 0; q < P; ++q) { acc[q] += (T)2 * y[q]; y[q] = c[q] + dt * y[q]; }
-    rk4_rhs<T, P>(y, i0, n, bc, iPe, idz2, hidz, Da, kin, cin, idz);  // k4
+    rk4_rhs<T, P>(y, i0, n, bc, iPe, idz2, hidz, Da, kin, cin, idz, xch, 1);  // k4
 #pragma unroll
     for (int q = 0; q < P; ++q) c[q] = c[q] + dt6 * (acc[q] + y[q]);
   }
@@ -326,22 +335,21 @@ mjx_status mjx_reactor_rk4_batch(const mjx_reactor_instance* inst_dev, int n_ins
   const int e = elem_size(dtype);
   if (!e) return MJX_BAD_DTYPE;
   if (!inst_dev || !out || n_inst < 0 || max_n < 3) return MJX_BAD_ARG;
-  if (max_n > (e == 4 ? 1024 : 512)) return MJX_BAD_SHAPE;  // 32 (FP32) / 16 (FP64) nodes per lane
+  if (max_n > 32 * RW * 8) return MJX_BAD_SHAPE;  // at most 8 nodes per lane
   if (n_inst == 0) return MJX_OK;
   ReactorArgs A;
   A.inst = inst_dev; A.out = out; A.n_inst = n_inst;
   cudaStream_t s = (cudaStream_t)stream;
-  const int blocks = (n_inst + 3) / 4;
-  const int per = (max_n + 31) / 32;  // nodes per lane
+  const int per = (max_n + 32 * RW - 1) / (32 * RW);  // nodes per lane
 #define MJX_RK4_LAUNCH(PP)                                                         \
   do {                                                                             \
-    if (e == 4) reactor_rk4_kernel<float, PP><<<blocks, 128, 0, s>>>(A);           \
-    else reactor_rk4_kernel<double, PP><<<blocks, 128, 0, s>>>(A);                 \
+    if (e == 4) reactor_rk4_kernel<float, PP><<<n_inst, 32 * RW, 0, s>>>(A);       \
+    else reactor_rk4_kernel<double, PP><<<n_inst, 32 * RW, 0, s>>>(A);             \
   } while (0)
-  if (per <= 4) MJX_RK4_LAUNCH(4);
-  else if (per <= 8) MJX_RK4_LAUNCH(8);
-  else if (per <= 16) MJX_RK4_LAUNCH(16);
-  else if (e == 4) reactor_rk4_kernel<float, 32><<<blocks, 128, 0, s>>>(A);
+  if (per <= 1) MJX_RK4_LAUNCH(1);
+  else if (per <= 2) MJX_RK4_LAUNCH(2);
+  else if (per <= 4) MJX_RK4_LAUNCH(4);
+  else MJX_RK4_LAUNCH(8);
 #undef MJX_RK4_LAUNCH
   return cuda_status(cudaGetLastError());
 }

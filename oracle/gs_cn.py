@@ -8,7 +8,8 @@ of benchmarks/benchmark_gray_scott.py:
   max|res_u| + max|res_v| > tol and i < max_iter, starting from u_old with
   res_norm = 1;
 * 268-296 (imex_step / imex_solve): explicit Euler half step of the reaction,
-  exact exponential diffusion by FFT, explicit Euler half step.
+  exact exponential diffusion by FFT, explicit Euler half step;
+* 93-131 (rk4_rhs / rk4_step / rk4_solve): classical RK4 with the Laplacian by FFT.
 """
 
 from __future__ import annotations
@@ -87,3 +88,31 @@ def strang_exp_solve(u0, v0, lam, Du, Dv, F, k, dt, n_steps):
     for _ in range(n_steps):
         u, v = strang_exp_step(u, v, lam, Du, Dv, F, k, dt)
     return u, v
+
+
+def rk4_rhs(u, v, lam, Du, Dv, F, k):
+    """benchmarks/benchmark_gray_scott.py:93-106."""
+    lap_u = np.real(np.fft.ifft2(lam * np.fft.fft2(u)))
+    lap_v = np.real(np.fft.ifft2(lam * np.fft.fft2(v)))
+    uvv = u * v * v
+    return Du * lap_u - uvv + F * (1 - u), Dv * lap_v + uvv - (F + k) * v
+
+
+def rk4_solve(u0, v0, lam, Du, Dv, F, k, dt, n_steps):
+    """rk4_step / rk4_solve (108-125)."""
+    u, v = u0, v0
+    f = lambda a, b: rk4_rhs(a, b, lam, Du, Dv, F, k)  # noqa: E731
+    for _ in range(n_steps):
+        k1u, k1v = f(u, v)
+        k2u, k2v = f(u + 0.5 * dt * k1u, v + 0.5 * dt * k1v)
+        k3u, k3v = f(u + 0.5 * dt * k2u, v + 0.5 * dt * k2v)
+        k4u, k4v = f(u + dt * k3u, v + dt * k3v)
+        u = u + dt / 6 * (k1u + 2 * k2u + 2 * k3u + k4u)
+        v = v + dt / 6 * (k1v + 2 * k2v + 2 * k3v + k4v)
+    return u, v
+
+
+def rk4_dt(n, Du, Dv, dx):
+    """0.9 of the RK4 stability limit 2.8 / (max(Du, Dv) max|lam|) (79-90)."""
+    lam = spectral_symbol(n, dx)
+    return 0.9 * 2.8 / (max(Du, Dv) * float(np.max(-lam)))

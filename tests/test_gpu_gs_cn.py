@@ -58,3 +58,21 @@ def test_gs_strang_exp_vs_oracle(cuda, n, steps):
     from moljax_gb300.workloads import gray_scott_benchmark_ic
     uu, vv = gray_scott_benchmark_ic(n, torch.float64, cuda)
     assert np.array_equal(uu.cpu().numpy(), u0) and np.array_equal(vv.cpu().numpy(), v0)
+
+
+@pytest.mark.parametrize("n,steps", [(64, 40), (256, 20)])
+def test_gs_rk4_spectral_vs_oracle(cuda, n, steps):
+    """The benchmark's pseudo-spectral RK4 (rk4_step, benchmark_gray_scott.py:93-131) at
+    0.9 of its stability limit against the oracle, FP64; a run longer than one 16-step graph
+    and one shorter."""
+    import moljax_gb300 as M
+    u0, v0 = G.benchmark_ic(n)
+    dx = 1.0 / n
+    lam = G.spectral_symbol(n, dx)
+    dt = G.rk4_dt(n, P["Du"], P["Dv"], dx)
+    for st in (3, steps):
+        u, v = M.gray_scott_rk4_spectral(torch.tensor(u0, device=cuda), torch.tensor(v0, device=cuda),
+                                         P["Du"], P["Dv"], P["F"], P["k"], dt, st, dx)
+        ru, rv = G.rk4_solve(u0, v0, lam, P["Du"], P["Dv"], P["F"], P["k"], dt, st)
+        for a, b in ((u, ru), (v, rv)):
+            assert float(np.linalg.norm(a.cpu().numpy() - b) / np.linalg.norm(b)) < 1e-12, st
