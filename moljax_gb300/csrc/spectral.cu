@@ -398,6 +398,210 @@ __global__ void __launch_bounds__(ColThreads<T>::v, 1) col_kernel(const __grid_c
   }
 }
 
+// ------------------------------------------------------------------ warp row pass (n = 1024)
+// A 1024-point row transform held by one warp: lane l keeps the 32 elements l + 32 j in
+// registers.  Four-step split 1024 = 32 x 32: a 32-point DFT per lane over j, the twiddles
+// w^(l k1) (the row table, w = exp(-2 pi i/1024)), one transpose through a 32 x 33 shared
+// tile of the warp (only __syncwarp, no block barrier), and a second 32-point DFT per lane;
+// element k1 + 32 k2 of the result ends in register k2 of lane k1, which is again the
+// layout "lane = index mod 32", so the inverse transform's output feeds the pointwise work
+// and the forward transform without any reordering.  The two-for-one packing of two real
+// rows pairs index k with 1024 - k, which lives in lane (32 - l) mod 32: one shuffle each.
+
+// cos / sin of 2 pi k / 32, k = 0..15
+__constant__ const float kW32C[16] = {1.0f, 0.98078528040323044913f, 0.92387953251128675613f,
+                                      0.83146961230254523708f, 0.70710678118654752440f, 0.55557023301960222474f,
+                                      0.38268343236508977173f, 0.19509032201612826785f, 0.0f,
+                                      -0.19509032201612826785f, -0.38268343236508977173f, -0.55557023301960222474f,
+                                      -0.70710678118654752440f, -0.83146961230254523708f, -0.92387953251128675613f,
+                                      -0.98078528040323044913f};
+__constant__ const float kW32S[16] = {0.0f, 0.19509032201612826785f, 0.38268343236508977173f,
+                                      0.55557023301960222474f, 0.70710678118654752440f, 0.83146961230254523708f,
+                                      0.92387953251128675613f, 0.98078528040323044913f, 1.0f,
+                                      0.98078528040323044913f, 0.92387953251128675613f, 0.83146961230254523708f,
+                                      0.70710678118654752440f, 0.55557023301960222474f, 0.38268343236508977173f,
+                                      0.19509032201612826785f};
+
+// 32-point DFT in registers, natural order in and out: 16-point DFTs of the even and odd
+// samples and one radix-2 step with w32^k
+template <bool INV>
+__device__ __forceinline__ void dft32(float2 (&a)[32]) {
+  float2 e[16], o[16];
+#pragma unroll
+  for (int m = 0; m < 16; ++m) { e[m] = a[2 * m]; o[m] = a[2 * m + 1]; }
+  dft16<INV>(e);
+  dft16<INV>(o);
+#pragma unroll
+  for (int k = 0; k < 16; ++k) {
+    const float c = kW32C[k], sn = INV ? kW32S[k] : -kW32S[k];
+    const float2 t = mk<float2>(o[k].x * c - o[k].y * sn, o[k].x * sn + o[k].y * c);
+    a[k] = cadd(e[k], t);
+    a[k + 16] = csub(e[k], t);
+  }
+}
+
+template <bool INV>
+__device__ __forceinline__ void wfft1024(float2 (&z)[32], float2* tile, const float2* __restrict__ tw, int lane) {
+  dft32<INV>(z);
+#pragma unroll
+  for (int k1 = 1; k1 < 32; ++k1) {
+    const float2 w = __ldg(&tw[lane * k1]);
+    z[k1] = INV ? cmulc(z[k1], w) : cmul(z[k1], w);
+  }
+#pragma unroll
+  for (int k1 = 0; k1 < 32; ++k1) tile[k1 * 33 + lane] = z[k1];
+  __syncwarp();
+#pragma unroll
+  for (int j2 = 0; j2 < 32; ++j2) z[j2] = tile[lane * 33 + j2];
+  __syncwarp();
+  dft32<INV>(z);
+}
+
+__device__ __forceinline__ float2 shfl2(float2 v, int src) {
+  return mk<float2>(__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src));
+}
+
+// The row pass of row_kernel (same flags, pair table, pointwise work and error partials) for
+// FP32 rows of 1024 points, one warp per sequence.
+template <int RX>
+__global__ void __launch_bounds__(128) row_kernel_w32(const __grid_constant__ RowArgs<float> a) {
+  typedef float2 C;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const DevState* st = a.st;
+  if (st != nullptr && st->done) return;
+  const int lane = threadIdx.x & 31, s_loc = threadIdx.x >> 5;
+  C* tile = reinterpret_cast<C*>(smem_raw) + s_loc * (32 * 33);
+  const int seq0 = blockIdx.x * a.nseq;
+  const int q = seq0 / a.nrows;  // uniform within the CTA (nrows % nseq == 0)
+  const RowPair pr = a.pr[q];
+  const int flags = pr.flags;
+  const long long y = (seq0 % a.nrows) + s_loc;
+  const int cur = st != nullptr ? st->cur : 0;
+  const float* rin = a.rin_sel < 0 ? a.rin[0] : a.rin[a.rin_sel == 0 ? cur : 1 - cur];
+  float* rout = a.rout_sel < 0 ? a.rout[0] : a.rout[a.rout_sel == 0 ? cur : 1 - cur];
+  const int src = (32 - lane) & 31;  // the lane holding index 1024 - k of this lane's k
+  C z[32];
+  // 1. load: spectrum rows (c2r) or real rows, element lane + 32 j in z[j]
+  if (flags & ROW_LOAD_SPEC) {
+    const C* A = a.spec + pr.sa + y * a.ldc;
+    const C* B = a.spec + pr.sb + y * a.ldc;
+    C Ar[17], Br[17];
+#pragma unroll
+    for (int j = 0; j < 16; ++j) { Ar[j] = A[32 * j + lane]; Br[j] = B[32 * j + lane]; }
+    Ar[16] = lane == 0 ? A[512] : mk<C>(0.f, 0.f);
+    Br[16] = lane == 0 ? B[512] : mk<C>(0.f, 0.f);
+#pragma unroll
+    for (int j = 0; j < 16; ++j) z[j] = mk<C>(Ar[j].x - Br[j].y, Ar[j].y + Br[j].x);  // A_k + i B_k
+#pragma unroll
+    for (int j = 16; j < 32; ++j) {  // k = 32 j + lane > 512 (and k = 512 on lane 0)
+      C av = shfl2(Ar[31 - j], src), bv = shfl2(Br[31 - j], src);
+      if (lane == 0) { av = Ar[32 - j]; bv = Br[32 - j]; }
+      if (lane == 0 && j == 16) z[j] = mk<C>(av.x - bv.y, av.y + bv.x);
+      else z[j] = mk<C>(av.x + bv.y, bv.x - av.y);  // conj(A_k') + i conj(B_k'), k' = 1024 - k
+    }
+    wfft1024<true>(z, tile, a.tw, lane);
+  } else {
+    const float* ra = rin + pr.ra + y * a.rstride;
+    const float* rb = rin + pr.rb + y * a.rstride;
+#pragma unroll
+    for (int j = 0; j < 32; ++j) z[j] = mk<C>(ra[32 * j + lane], rb[32 * j + lane]);
+  }
+
+  // 2. pointwise work on element x = lane + 32 j (as row_kernel)
+  const float sc = (flags & ROW_LOAD_SPEC) ? a.inv_scale : 1.0f;
+  float h = 0.f;
+  if (flags & ROW_REACT) h = (float)((st != nullptr ? st->dtc : a.hfixed) * pr.hfac);
+  float esum = 0.f;
+  int bad = 0;
+  float* oa = rout + pr.ra + y * a.rstride;
+  float* ob = rout + pr.rb + y * a.rstride;
+  const float* ea = a.eref + pr.ra + y * a.rstride;
+  const float* eb = a.eref + pr.rb + y * a.rstride;
+  const float pF = (float)a.F, pK = (float)a.k, pR = (float)a.r, pFK = (float)(a.F + a.k);
+  const float pAtol = (float)a.atol, pRtol = (float)a.rtol;
+#pragma unroll
+  for (int j = 0; j < 32; ++j) {
+    const int x = lane + 32 * j;
+    float va = z[j].x * sc, vb = z[j].y * sc;
+    if (flags & ROW_NONLIN) {
+      if (RX == RX_GRAY_SCOTT) {
+        const float uvv = va * vb * vb;
+        const float nu = -uvv + pF * (1.f - va), nv = uvv - pFK * vb;
+        va = nu; vb = nv;
+      } else if (RX == RX_FISHER) {
+        va = pR * va * (1.f - va); vb = pR * vb * (1.f - vb);
+      } else {
+        va = 0.f; vb = 0.f;
+      }
+    }
+    if (flags & ROW_REACT) {
+      if (flags & ROW_DELTA) react_delta<float, RX>(va, vb, h, pF, pK, pR);
+      else if (flags & ROW_EULER) {
+        react_euler<float, RX>(va, vb, h, pF, pK, pR);
+        if (flags & ROW_EULER2) react_euler<float, RX>(va, vb, h, pF, pK, pR);
+      }
+      else react_heun<float, RX>(va, vb, h, pF, pK, pR);
+    }
+    if (flags & ROW_STORE_REAL) { oa[x] = va; ob[x] = vb; }
+    if (flags & ROW_ERRNORM) {
+      const float da = (va - ea[x]) / (pAtol + pRtol * fabsf(va));
+      const float db = (vb - eb[x]) / (pAtol + pRtol * fabsf(vb));
+      esum += da * da + db * db;
+      bad |= !(finite_(va) && finite_(vb));
+    }
+    if (flags & ROW_ERRPAIR) {
+      const float da = va / (pAtol + pRtol * fabsf(vb));
+      esum += da * da;
+      bad |= !(finite_(va) && finite_(vb));
+    }
+    z[j] = mk<C>(va, vb);
+  }
+
+  // 3. r2c and split into the two half spectra: X_k in z[k2] of lane k1, k = k1 + 32 k2
+  if (flags & ROW_STORE_SPEC) {
+    wfft1024<false>(z, tile, a.tw, lane);
+    C* A = a.spec + ((flags & ROW_SPEC_ALT) ? pr.oa : pr.sa) + y * a.ldc;
+    C* B = a.spec + ((flags & ROW_SPEC_ALT) ? pr.ob : pr.sb) + y * a.ldc;
+#pragma unroll
+    for (int k2 = 0; k2 <= 16; ++k2) {
+      C Zm = shfl2(z[k2 <= 15 ? 31 - k2 : 15], src);  // X_{1024-k} (lanes > 0)
+      if (lane == 0) Zm = z[(32 - k2) & 31];
+      const int k = lane + 32 * k2;
+      if (k2 == 16 && lane != 0) continue;
+      const C Zk = z[k2];
+      A[k] = mk<C>(0.5f * (Zk.x + Zm.x), 0.5f * (Zk.y - Zm.y));
+      B[k] = mk<C>(0.5f * (Zk.y + Zm.y), 0.5f * (Zm.x - Zk.x));
+    }
+  }
+
+  // 4. block reduction of the error partials (FP64 across warps)
+  if (flags & (ROW_ERRNORM | ROW_ERRPAIR)) {
+    __shared__ double red[4];
+    __shared__ int redbad[4];
+    double v = (double)esum;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      v += __shfl_xor_sync(0xffffffffu, v, o);
+      bad |= __shfl_xor_sync(0xffffffffu, bad, o);
+    }
+    if (lane == 0) { red[s_loc] = v; redbad[s_loc] = bad; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double sum = 0.0, c = 0.0;  // Kahan
+      int b2 = 0;
+      for (int i = 0; i < a.nseq; ++i) {
+        const double yv = red[i] - c;
+        const double tv = sum + yv;
+        c = (tv - sum) - yv;
+        sum = tv;
+        b2 |= redbad[i];
+      }
+      a.partial[blockIdx.x] = sum;
+      a.nonfinite[blockIdx.x] = b2;
+    }
+  }
+}
+
 // ------------------------------------------------------------------ launchers
 static size_t row_smem(int n, int nseq, int elem) { return (size_t)sp_size(nseq * n) * 2 * elem; }
 
@@ -414,6 +618,12 @@ cudaError_t launch_row(const RowArgs<T>& a0, cudaStream_t s) {
     while (a.nseq > 1 && a.npairs * a.nrows / a.nseq < 152) a.nseq >>= 1;
   const int tps = a.n >= 16 ? a.n / 16 : 1;
   const int grid = a.npairs * a.nrows / a.nseq;
+  if constexpr (sizeof(T) == 4) {
+    if (a.n == 1024 && a.nseq <= 4) {  // one warp per 1024-point row
+      row_kernel_w32<RX><<<grid, 32 * a.nseq, (size_t)a.nseq * 32 * 33 * sizeof(float2), s>>>(a);
+      return cudaGetLastError();
+    }
+  }
   const size_t smem = row_smem(a.n, a.nseq, sizeof(T));
   row_kernel<T, RX><<<grid, a.nseq * tps, smem, s>>>(a);
   return cudaGetLastError();

@@ -25,9 +25,10 @@ def _rel(a, b):
     return float(np.linalg.norm(a - b) / np.linalg.norm(b))
 
 
-@pytest.mark.parametrize("n", [16, 64, 256])
+@pytest.mark.parametrize("n", [16, 64, 256, 1024])
 @pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
 def test_strang_step_vs_oracle(cuda, n, dtype):
+    """One IMEX-Strang step; at 1024 the FP32 row passes take the one-warp-per-row form."""
     M, grid, model, cache, diff, ym, og, y0, om, lam, od = _setup(n, dtype, cuda)
     out = M.imex_strang_step(model, ym, 0.0, 0.8, cache, diff)
     ref = OI.imex_strang_step(om, y0, 0.8, lam, od)
