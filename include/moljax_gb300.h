@@ -667,7 +667,8 @@ mjx_status mjx_imex_plan_destroy(void* plan);
 
 /* Launches a single kernel of one mixed-precision attempt (timing/profiling):
  * which = 0 seeds the workspace from the FP32 state y with step dt; 1..6 launch
- * C1, R1, C2, R2, C3, R3 (see csrc/imex_mixed.cu).  No reference counterpart. */
+ * C1, R1, C2, R2, C3, R3 (see csrc/imex_mixed.cu); 7 the controller (it advances the
+ * seeded state as an attempt would).  No reference counterpart. */
 mjx_status mjx_imex_mixed_attempt_kernel2d(const void* plan32, const void* plan64,
                                            const mjx_grid2d* grid, const mjx_imex_problem* prob,
                                            const mjx_pid_params* pid, int which, double dt,

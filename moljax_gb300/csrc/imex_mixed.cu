@@ -179,8 +179,7 @@ static MixAttempt build_mix(const void* plan32, const mjx_grid2d* g, const mjx_i
     memset(&j, 0, sizeof(j));
     j.off = (long long)f * L.fs; j.D = D;
     j.type = MC_SPLIT; A.c1.job[A.c1.njobs++] = j;
-    j.type = MC_FULL_END; A.c2.job[A.c2.njobs++] = j;
-    j.type = MC_HALF_MID; A.c2.job[A.c2.njobs++] = j;
+    j.type = MC_MID_BOTH; A.c2.job[A.c2.njobs++] = j;  // MC_FULL_END + MC_HALF_MID, one tile
     j.type = MC_HALF_END; A.c3.job[A.c3.njobs++] = j;
   }
   // row passes over the FP32 row spectra ZA/ZB (contiguous: ZB = ZA + zoff)
@@ -404,6 +403,14 @@ mjx_status mjx_imex_mixed_attempt_kernel2d(const void* plan32, const void* plan6
     case 4: e = mrow(A.r2, A.rx, s); break;
     case 5: e = mcol(A.c3, s); break;
     case 6: e = mrow(A.r3, RX_NONE, s); break;
+    case 7: {  // the controller
+      CtlArgs ca;
+      memset(&ca, 0, sizeof(ca));
+      ca.st = st; ca.partial = (const double*)(w + L.part); ca.nonfinite = (const int*)(w + L.bad);
+      ca.nparts = L.nparts; ca.n_dof = (double)nf * g->ny * g->nx; ca.pid = *pid;
+      e = launch_controller(ca, s);
+      break;
+    }
     default: return MJX_BAD_ARG;
   }
   return cuda_status(e);

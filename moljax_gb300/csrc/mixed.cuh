@@ -8,7 +8,9 @@
 
 namespace mjx {
 
-enum { MC_SPLIT = 0, MC_FULL_END = 1, MC_HALF_MID = 2, MC_HALF_END = 3 };
+// MC_MID_BOTH is MC_FULL_END and MC_HALF_MID of the same columns in one tile (ZA in the
+// left half, ZB in the right half): the C2 pass then needs half the CTAs
+enum { MC_SPLIT = 0, MC_FULL_END = 1, MC_HALF_MID = 2, MC_HALF_END = 3, MC_MID_BOTH = 4 };
 
 __device__ __forceinline__ float2 fmk(float x, float y) { float2 r; r.x = x; r.y = y; return r; }
 
@@ -102,23 +104,26 @@ __device__ __forceinline__ void mcol_tile(float2* buf, const MColTile& t, int ti
   const float hA = t.hA, hB = t.hB, nrm = t.nrm;
 
   if (type != MC_SPLIT) {
-    // load the FP32 increment tile and transform it forward along y
-    const float2* zin = type == MC_FULL_END ? t.za : t.zb;
-    float2 v[8];
+    // load the FP32 increment tile(s) and transform them forward along y
+    const int halves = type == MC_MID_BOTH ? 2 : 1;
+    for (int hf = 0; hf < halves; ++hf) {
+      const float2* zin = (type == MC_FULL_END || (type == MC_MID_BOTH && hf == 0)) ? t.za : t.zb;
+      float2 v[8];
 #pragma unroll
-    for (int m = 0; m < 8; ++m) {
-      const int e = tid + m * nth;
-      const int ky = e >> lc, c = e & (Cn - 1), kx = kx0 + c;
-      if (e < total) v[m] = kx < t.ncols ? zin[t.off + ky * ldc + kx] : fmk(0.f, 0.f);
-    }
+      for (int m = 0; m < 8; ++m) {
+        const int e = tid + m * nth;
+        const int ky = e >> lc, c = e & (Cn - 1), kx = kx0 + c;
+        if (e < total) v[m] = kx < t.ncols ? zin[t.off + ky * ldc + kx] : fmk(0.f, 0.f);
+      }
 #pragma unroll
-    for (int m = 0; m < 8; ++m) {
-      const int e = tid + m * nth;
-      const int ky = e >> lc, c = e & (Cn - 1);
-      if (e < total) buf[sp(ky * W + c)] = v[m];
+      for (int m = 0; m < 8; ++m) {
+        const int e = tid + m * nth;
+        const int ky = e >> lc, c = e & (Cn - 1);
+        if (e < total) buf[sp(ky * W + hf * Cn + c)] = v[m];
+      }
     }
     __syncthreads();
-    fft_smem<float, false, true>(buf, ny, t.log2ny, Cn, 1, W, t.tw, tid);
+    fft_smem<float, false, true>(buf, ny, t.log2ny, type == MC_MID_BOTH ? W : Cn, 1, W, t.tw, tid);
   }
 
   // float-float combine, element by element
@@ -136,10 +141,18 @@ __device__ __forceinline__ void mcol_tile(float2* buf, const MColTile& t, int ti
     const float lam = t.lamx[kx] + t.lamy[ky];
     float4 Pm, Qm;
     if (type == MC_SPLIT) Pm = t.ys_cur[g];
-    else if (type == MC_FULL_END) Pm = t.pa[g];
+    else if (type == MC_FULL_END || type == MC_MID_BOTH) Pm = t.pa[g];
     else Pm = t.pb[g];
     if (type == MC_HALF_END) Qm = t.pa[g];
-    if (type == MC_SPLIT) {
+    if (type == MC_MID_BOTH) Qm = t.pb[g];
+    if (type == MC_MID_BOTH) {  // MC_FULL_END on the left half, MC_HALF_MID on the right
+      const float2 d = buf[sp(ky * W + c)], d2 = buf[sp(ky * W + Cn + c)];
+      t.pa[g] = ff_mstep_c(ff_add_c(Pm, d), mu_of(hA, lam));
+      const float mu = mu_of(hB, lam);
+      const float4 X = ff_mstep_c(ff_mstep_c(ff_add_c(Qm, d2), mu), mu);
+      t.pb[g] = X;
+      buf[sp(ky * W + Cn + c)] = fmk(ff_scaled(ff_re(X), nrm), ff_scaled(ff_im(X), nrm));
+    } else if (type == MC_SPLIT) {
       const float4 PA = ff_mstep_c(Pm, mu_of(hA, lam)), PB = ff_mstep_c(Pm, mu_of(hB, lam));
       t.pa[g] = PA;
       t.pb[g] = PB;
@@ -174,6 +187,7 @@ __device__ __forceinline__ void mcol_tile(float2* buf, const MColTile& t, int ti
     const int half = col >> lc, c = col & (Cn - 1), kx = kx0 + c;
     if (kx >= t.ncols) continue;
     const long long g = t.off + ky * ldc + kx;
+    if (type == MC_MID_BOTH && half == 0) continue;  // only the MC_HALF_MID half goes back
     const float2 v = buf[sp(ky * W + col)];
     if (type == MC_HALF_MID) t.zb[g] = v;
     else if (half == 0) t.za[g] = v;
