@@ -415,8 +415,11 @@ mjx_status mjx_vardiff_jvp2d(int n, double dy, double dx, const double* model_ab
 
 /* One implicit step of this model: be_step (moljax/core/stepping.py:170-214), cn_step
  * (217-260) or bdf2_step (263-310, omega = dt/dt_prev, y_prev = y_{n-1}), solved as in
- * mjx_nk_vardiff_integrate2d.  stats (optional): Newton iterations, GMRES iterations,
- * converged; res_norm (optional): final residual norm (NKStats, newton_krylov.py:41-46). */
+ * mjx_nk_vardiff_integrate2d.  be_guess_previous: 0 the reference's guess (explicit Euler;
+ * BDF2 2 y_n - y_{n-1}), 1 y_n, 2 the values y_out holds on entry (newton_krylov_solve's x0
+ * for a residual of create_implicit_residual / create_bdf2_residual, newton_krylov.py:
+ * 171-359).  stats (optional): Newton iterations, GMRES iterations, converged; res_norm
+ * (optional): final residual norm (NKStats, newton_krylov.py:41-46). */
 mjx_status mjx_nk_vardiff_step2d(const void* plan2, int n, double dy, double dx,
                                  const double* model_abc, int method, double dt, double dt_prev,
                                  int be_guess_previous, const mjx_nk_params* nkp, const double* y_n,

@@ -107,7 +107,12 @@ def _unflat(vec, keys, shapes):
 
 
 def _gmres(matvec, b, tol, restart, maxiter, M=None):
-    """Left-preconditioned restarted GMRES (MGS, Givens) on flat torch vectors."""
+    """Left-preconditioned restarted GMRES on flat torch vectors: classical Gram-Schmidt
+    with one re-orthogonalisation pass, as jax.scipy.sparse.linalg.gmres orthogonalises
+    (the Arnoldi basis is the rows of one device matrix, so a step is four matrix-vector
+    products), Givens rotations and the small triangular solve on the host in FP64; one host
+    synchronisation per Arnoldi step (its new Hessenberg column)."""
+    import numpy as np
     Mf = M or (lambda v: v)
     bp = Mf(b)
     bnorm = float(torch.linalg.norm(bp))
@@ -120,39 +125,69 @@ def _gmres(matvec, b, tol, restart, maxiter, M=None):
         beta = float(torch.linalg.norm(r))
         if beta <= tol * bnorm:
             break
-        V = [r / beta]
-        H = torch.zeros(restart + 1, restart, dtype=torch.float64)
-        cs, sn = torch.zeros(restart, dtype=torch.float64), torch.zeros(restart, dtype=torch.float64)
-        g = torch.zeros(restart + 1, dtype=torch.float64)
+        V = torch.empty(restart + 1, b.numel(), dtype=b.dtype, device=b.device)
+        V[0] = r / beta
+        H = np.zeros((restart + 1, restart))
+        cs, sn = np.zeros(restart), np.zeros(restart)
+        g = np.zeros(restart + 1)
         g[0] = beta
         k = 0
         for j in range(restart):
             w = Mf(matvec(V[j]))
-            for i in range(j + 1):
-                H[i, j] = float(torch.dot(V[i], w))
-                w = w - H[i, j].item() * V[i]
-            hn = float(torch.linalg.norm(w))
-            H[j + 1, j] = hn
+            Vj = V[:j + 1]
+            h = Vj @ w
+            w = w - Vj.T @ h
+            h2 = Vj @ w
+            w = w - Vj.T @ h2
+            col = torch.cat([h + h2, torch.linalg.norm(w)[None]]).double().cpu().numpy()
+            hn = float(col[j + 1])
+            H[:j + 2, j] = col
             for i in range(j):
                 t = cs[i] * H[i, j] + sn[i] * H[i + 1, j]
                 H[i + 1, j] = -sn[i] * H[i, j] + cs[i] * H[i + 1, j]
                 H[i, j] = t
-            den = math.hypot(float(H[j, j]), float(H[j + 1, j]))
+            den = math.hypot(H[j, j], H[j + 1, j])
             cs[j], sn[j] = H[j, j] / den, H[j + 1, j] / den
             H[j, j], H[j + 1, j] = den, 0.0
             g[j + 1] = -sn[j] * g[j]
             g[j] = cs[j] * g[j]
             its += 1
             k = j + 1
-            if abs(float(g[j + 1])) <= tol * bnorm or hn == 0.0:
+            if abs(g[j + 1]) <= tol * bnorm or hn == 0.0:
                 break
-            V.append(w / hn)
-        y = torch.linalg.solve_triangular(H[:k, :k], g[:k, None], upper=True)[:, 0]
-        for i in range(k):
-            x = x + float(y[i]) * V[i]
-        if abs(float(g[k])) <= tol * bnorm:
+            V[j + 1] = w / hn
+        y = np.zeros(k)
+        for i in range(k - 1, -1, -1):  # back substitution (upper triangular)
+            y[i] = (g[i] - H[i, i + 1:k] @ y[i + 1:k]) / H[i, i]
+        x = x + V[:k].T @ torch.tensor(y, dtype=b.dtype, device=b.device)
+        if abs(g[k]) <= tol * bnorm:
             break
     return x, its
+
+
+def _native_solve(nat, x0, p: NKParams):
+    """The solve of a create_implicit_residual / create_bdf2_residual residual over the
+    variable-diffusion model on the native Newton-Krylov solver (mjx_nk_vardiff_step2d, guess
+    x0): FP64 residual and Newton updates, FP32 JVP and GMRES, its DST preconditioner."""
+    from moljax_gb300.core import stepping as S
+    from moljax_gb300.core.fft_solvers import get_plan, workspace
+    model = nat["model"]
+    _, cp, abc, g = S._nk_setup(model, p)
+    yn = S._interior64(model, nat["y_n"])
+    yp = S._interior64(model, nat["y_prev"]) if nat["y_prev"] is not None else yn
+    out = S._interior64(model, x0).clone()  # the guess, replaced by the root
+    n = g.nx
+    plan2 = get_plan(2 * n, 2 * n, g.dy, g.dx, "fd", torch.float32, yn.device)
+    lib = N.lib()
+    ws = workspace(lib.mjx_nk_vardiff_ws_bytes(n, p.gmres_restart), plan2.device, "nk")
+    st = (C.c_int * 3)()
+    rn = C.c_double(0.0)
+    N.check("mjx_nk_vardiff_step2d", lib.mjx_nk_vardiff_step2d(
+        N.ptr(plan2.buf), n, float(g.dy), float(g.dx), abc, int(nat["method"]), float(nat["dt"]),
+        float(nat["dt_prev"]), 2, C.byref(cp), N.ptr(yn), N.ptr(yp), N.ptr(out), st, C.byref(rn), N.ptr(ws),
+        ws.numel(), N.stream_ptr(plan2.device)))
+    return NKResult({"u": S._padded(model, out, x0["u"])},
+                    NKStats(bool(st[2]), int(st[0]), int(st[1]), float(rn.value)))
 
 
 def newton_krylov_solve(residual_fn: Callable, x0, grid=None, params: Optional[Dict] = None,
@@ -160,7 +195,11 @@ def newton_krylov_solve(residual_fn: Callable, x0, grid=None, params: Optional[D
                         *, gmres_restart: Optional[int] = None, rtol: Optional[float] = None):
     """Reference signature (newton_krylov.py:171-359) and README kwargs.
 
-    ``rtol`` (README) sets newton_tol; ``gmres_restart`` sets the restart length.
+    ``rtol`` (README) sets newton_tol; ``gmres_restart`` sets the restart length.  A residual
+    made by create_implicit_residual / create_bdf2_residual over the variable-diffusion model
+    is solved by the native Newton-Krylov solver from x0 (its own preconditioner; the root is
+    the same, GMRES counts differ); any other residual runs the torch form below (JVPs by
+    torch.func, GMRES with one host synchronisation per Arnoldi step).
     """
     from moljax_gb300.core.preconditioners import PrecondContext, IdentityPreconditioner
     p = nk_params or NKParams()
@@ -168,6 +207,10 @@ def newton_krylov_solve(residual_fn: Callable, x0, grid=None, params: Optional[D
         p = p._replace(newton_tol=rtol)
     if gmres_restart is not None:
         p = p._replace(gmres_restart=gmres_restart)
+    nat = getattr(residual_fn, "native", None)
+    if (nat is not None and isinstance(x0, dict) and set(x0) == {"u"}
+            and "abc" in getattr(nat["model"], "metadata", {})):
+        return _native_solve(nat, x0, p)
     single = not isinstance(x0, dict)
     x0d = {"x": x0} if single else x0
     res_fn = (lambda d: {"x": residual_fn(d["x"])}) if single else residual_fn
@@ -232,6 +275,9 @@ def create_implicit_residual(model, y_old, t_new: float, dt: float, method: str 
             return {k: y_new[k] - y_old[k] - 0.5 * dt * (F_old[k] + F[k]) for k in y_new}
     else:
         raise ValueError(f"Unknown method: {method}")
+    # what newton_krylov_solve needs to hand the solve to the native solver
+    residual.native = {"model": model, "method": 3 if method == "be" else 4, "y_n": y_old, "y_prev": None,
+                       "dt": dt, "dt_prev": dt}
     return residual
 
 
@@ -246,4 +292,5 @@ def create_bdf2_residual(model, y_n, y_nm1, t_new: float, dt: float, dt_prev: fl
     def residual(y_new):
         F = model.rhs(y_new, t_new)
         return {k: a0 * y_new[k] + a1 * y_n[k] + a2 * y_nm1[k] - beta * F[k] for k in y_new}
+    residual.native = {"model": model, "method": 5, "y_n": y_n, "y_prev": y_nm1, "dt": dt, "dt_prev": dt_prev}
     return residual

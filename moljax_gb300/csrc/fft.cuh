@@ -174,18 +174,18 @@ __device__ __forceinline__ void stockham_pass(cx<T>* buf, int n, int p, int tps,
   __syncthreads();
 }
 
-// In-place FFT of nseq sequences (see file comment).  All threads of the block
-// must call it; threads with tid >= nseq*tps only join the barriers.  The caller
-// must __syncthreads() after filling buf; on return buf is complete.
+// In-place FFT of nseq sequences (see file comment), sequences s0 .. s0 + nseq - 1.
+// All threads of the block must call it; threads with tid >= nseq*tps only join the
+// barriers.  The caller must __syncthreads() after filling buf; on return buf is complete.
 template <typename T, bool INV, bool COLMAJOR>
 __device__ void fft_smem(cx<T>* buf, int n, int log2n, int nseq, int ss, int es,
-                         const cx<T>* __restrict__ tw, int tid) {
+                         const cx<T>* __restrict__ tw, int tid, int s0 = 0) {
   const int tps = n >= 16 ? pdiv(n, 16) : 1;
   const bool active = tid < nseq * tps;
   int lt, s;
   if (COLMAJOR) { s = pmod(tid, nseq); lt = pdiv(tid, nseq); }
   else { lt = pmod(tid, tps); s = pdiv(tid, tps); }
-  const int base = s * ss;
+  const int base = (s + s0) * ss;
   // straight-line schedule: up to three radix-16 passes (n <= 4096), then radix 2/4/8
   int p = 1, rem = log2n;
 #pragma unroll

@@ -179,6 +179,14 @@ __device__ __forceinline__ void mcol_tile(float2* buf, const MColTile& t, int ti
   }
   if (type == MC_FULL_END) return;
   __syncthreads();
+  if (type == MC_MID_BOTH) {  // only the right (MC_HALF_MID) half goes back
+    fft_smem<float, true, true>(buf, ny, t.log2ny, Cn, 1, W, t.tw, tid, Cn);
+    for (int e = tid; e < ny * Cn; e += nth) {
+      const int ky = e >> lc, c = e & (Cn - 1), kx = kx0 + c;
+      if (kx < t.ncols) t.zb[t.off + ky * ldc + kx] = buf[sp(ky * W + Cn + c)];
+    }
+    return;
+  }
   const int nseq = (type == MC_HALF_MID) ? Cn : W;
   fft_smem<float, true, true>(buf, ny, t.log2ny, nseq, 1, W, t.tw, tid);
   const int lns = __ffs(nseq) - 1;
@@ -187,7 +195,6 @@ __device__ __forceinline__ void mcol_tile(float2* buf, const MColTile& t, int ti
     const int half = col >> lc, c = col & (Cn - 1), kx = kx0 + c;
     if (kx >= t.ncols) continue;
     const long long g = t.off + ky * ldc + kx;
-    if (type == MC_MID_BOTH && half == 0) continue;  // only the MC_HALF_MID half goes back
     const float2 v = buf[sp(ky * W + col)];
     if (type == MC_HALF_MID) t.zb[g] = v;
     else if (half == 0) t.za[g] = v;

@@ -788,8 +788,10 @@ static cudaError_t implicit_step(NKRun& r, const NKParamsC& P, const double* abc
     lincomb_kernel<<<r.grid, 256, 0, r.s>>>(yc, a1, yp, a2, cst, nullptr, N2);
   }
   // initial guess: BDF2 -> 2 y_n - y_{n-1}; BE/CN -> explicit Euler y_n + dt F(y_n)
-  // (stepping.py:195-196, 242-243) or, with guess_previous, y_n
-  if (method == MJX_METHOD_BDF2) {
+  // (stepping.py:195-196, 242-243) or, with guess_previous == 1, y_n; guess_previous == 2
+  // keeps the guess the caller left in yout (newton_krylov_solve's x0)
+  if (guess_previous == 2) {
+  } else if (method == MJX_METHOD_BDF2) {
     lincomb_kernel<<<r.grid, 256, 0, r.s>>>(yc, 2.0, yp, -1.0, yout, nullptr, N2);
   } else if (guess_previous) {
     lincomb_kernel<<<r.grid, 256, 0, r.s>>>(yc, 1.0, nullptr, 0.0, yout, nullptr, N2);
@@ -928,6 +930,8 @@ mjx_status mjx_nk_vardiff_step2d(const void* plan2, int n, double dy, double dx,
   cudaError_t e = cudaMemcpyAsync(yc, y_n, sizeof(double) * N2, cudaMemcpyDeviceToDevice, r.s);
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(yp, y_prev ? y_prev : y_n, sizeof(double) * N2, cudaMemcpyDeviceToDevice, r.s);
+  if (e == cudaSuccess && be_guess_previous == 2)  // the caller's guess, in y_out on entry
+    e = cudaMemcpyAsync(yn, y_out, sizeof(double) * N2, cudaMemcpyDeviceToDevice, r.s);
   StepOut so;
   memset(&so, 0, sizeof(so));
   if (e == cudaSuccess) e = implicit_step(r, P, model_abc, method, dt, dt_prev, be_guess_previous, yc, yp, yn, &so);

@@ -200,3 +200,28 @@ def test_vardiff_jvp_vs_oracle_and_difference_quotient(cuda):
     Fp = ONK.vardiff_F(u + eps * v, 1.0 / n, 1.0 / n)
     Fm = ONK.vardiff_F(u - eps * v, 1.0 / n, 1.0 / n)
     assert _rel(jv, (Fp - Fm) / (2 * eps)) < 1e-7
+
+
+@pytest.mark.parametrize("method", ["be", "cn", "bdf2"])
+def test_newton_krylov_solve_routes_factory_residuals(cuda, method):
+    """newton_krylov_solve on a create_implicit_residual / create_bdf2_residual residual of
+    the variable-diffusion model runs the native solver from the given guess: the same root as
+    be_step / cn_step / bdf2_step and the oracle."""
+    import moljax_gb300 as M
+    M_, grid, model, u0, y = _vardiff_setup(32, cuda)
+    dx = grid.dx
+    dt, dt_prev = 60 * dx * dx, 100 * dx * dx
+    nkp = M.NKParams(gmres_restart=30)
+    yp = {"u": y["u"] * 0.9}
+    if method == "bdf2":
+        res = M.create_bdf2_residual(model, y, yp, dt, dt, dt_prev)
+        ref, conv, it, _ = ONK.implicit_step(u0, 0.9 * u0, method, dt, dt_prev, dx, dx, restart=30)
+        guess = {"u": 2 * y["u"] - yp["u"]}
+    else:
+        res = M.create_implicit_residual(model, y, dt, dt, method)
+        ref, conv, it, _ = ONK.implicit_step(u0, u0, method, dt, dt, dx, dx, restart=30, be_guess="previous")
+        guess = {"u": y["u"].clone()}
+    assert hasattr(res, "native")
+    out = M.newton_krylov_solve(res, guess, nk_params=nkp)
+    assert out.stats.converged and conv and abs(out.stats.newton_iters - it) <= 1
+    assert _rel(out.solution["u"][1:-1, 1:-1].cpu().numpy(), ref) < 1e-7
