@@ -406,6 +406,25 @@ mjx_status mjx_nk_vardiff_integrate2d(const void* plan2, int n, double dy, doubl
 mjx_status mjx_vardiff_rhs2d(int n, double dy, double dx, const double* model_abc, const double* y,
                              double* out, void* stream);
 
+/* ---- generic restarted GMRES (the Krylov cycle of newton_krylov_solve) ----------- */
+/* A linear operator as a host callback: enqueues out = Op(v) on `stream` (device FP32
+ * vectors of n elements) and returns 0, or non-zero to abort the solve. */
+typedef int (*mjx_vec_op)(const float* v, float* out, void* user, void* stream);
+/* Workspace of mjx_gmres_solve: the Arnoldi basis (restart + 1 vectors), two work vectors,
+ * the partial sums and the GMRES header; 0 for restart outside [1, 64]. */
+size_t mjx_gmres_ws_bytes(long long n, int restart);
+/* Left-preconditioned restarted GMRES(restart) on A x = b: the Krylov solve of
+ * newton_krylov_solve (moljax/core/newton_krylov.py:111-125, jax.scipy.sparse.linalg.gmres)
+ * for any operator the host can enqueue.  precond may be NULL (identity).  x holds the initial
+ * guess on entry and the solution on return.  Stops when the preconditioned residual estimate
+ * falls to tol times the first cycle's |M^-1 (b - A x0)|, or after max_cycles cycles.
+ * Orthogonalisation (classical Gram-Schmidt, FP64 dots), Givens steps and the update run on
+ * the device; the host synchronises once per cycle.  iterations: Arnoldi steps used;
+ * rel_res: final relative residual estimate; converged: 1 or 0. */
+mjx_status mjx_gmres_solve(long long n, mjx_vec_op matvec, mjx_vec_op precond, void* user, const float* b,
+                           float* x, double tol, int restart, int max_cycles, int* iterations, double* rel_res,
+                           int* converged, void* ws, size_t ws_bytes, void* stream);
+
 /* out = a0 v - beta J_F(u) v in FP64: the hand-written Jacobian-vector product of
  * F(u) = div((a + b u^2) grad u) - c u^3 (homogeneous Dirichlet ghosts), i.e. the JVP of
  * the residual a0 y + cst - beta F(y) at u (newton_krylov.py:61-80, _jvp_matvec, which

@@ -103,6 +103,9 @@ class GsInstanceC(C.Structure):
 
 
 _vp, _sz, _i, _d = C.c_void_p, C.c_size_t, C.c_int, C.c_double
+# a linear-operator callback of mjx_gmres_solve: (v, out, user, stream) -> 0 on success
+VecOp = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p)
+
 # name -> (restype, argtypes); the list is the exported C ABI
 SIGNATURES = {
     "mjx_version": (C.c_char_p, []),
@@ -147,6 +150,9 @@ SIGNATURES = {
     "mjx_reactor_smem_bytes": (_sz, [_i, _i]),
     "mjx_reactor_cn_batch": (_i, [_vp, _i, _i, _i, _vp, _vp]),
     "mjx_reactor_rk4_batch": (_i, [_vp, _i, _i, _i, _vp, _vp]),
+    "mjx_gmres_ws_bytes": (_sz, [C.c_longlong, _i]),
+    "mjx_gmres_solve": (_i, [C.c_longlong, VecOp, VecOp, _vp, _vp, _vp, _d, _i, _i, C.POINTER(C.c_int),
+                             C.POINTER(C.c_double), C.POINTER(C.c_int), _vp, _sz, _vp]),
     "mjx_nk_vardiff_ws_bytes": (_sz, [_i, _i]),
     "mjx_nk_vardiff_integrate2d": (_i, [_vp, _i, _d, _d, C.POINTER(C.c_double), _i, _d, _i, _i,
                                         C.POINTER(NKParamsC), _vp, _vp, C.POINTER(C.c_int), _vp, _sz,

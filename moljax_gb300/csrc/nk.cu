@@ -1092,4 +1092,95 @@ mjx_status mjx_nk_vardiff_adaptive2d(const void* plan2, int n, double dy, double
   return rc;
 }
 
+// ---- generic restarted GMRES over host callbacks ------------------------------------
+// The Arnoldi basis (FP32, m + 1 vectors of n), the work vectors and the GMRES header live
+// in the caller's workspace; the matvec / preconditioner callbacks enqueue their own work on
+// the stream.  Per cycle: r = b - A x, V_0 = M^-1 r, its norm; per Arnoldi step: V_j
+// normalised on the device, w = M^-1 A V_j, the Gram-Schmidt dots, the orthogonalisation and
+// the Givens step on the device (the GMRES kernels of the Newton-Krylov solver above); after
+// the m steps the small triangular solve and x += V y.  The host reads the header once per
+// cycle.  Steps after the device has converged inside a cycle return at entry (the
+// callbacks still run on the unused basis slots).
+struct GLayout {
+  size_t V, t, w, part, gs, total;
+  int nblk;
+};
+static GLayout g_layout(long long n, int m) {
+  GLayout L;
+  L.nblk = 152 * 4;
+  size_t o = 0;
+  L.V = o; o += al((size_t)(m + 1) * (size_t)n * 4);
+  L.t = o; o += al((size_t)n * 4);
+  L.w = o; o += al((size_t)n * 4);
+  L.part = o; o += al((size_t)(m + 2) * L.nblk * 8);
+  L.gs = o; o += al(sizeof(GmresState));
+  L.total = o;
+  return L;
+}
+
+size_t mjx_gmres_ws_bytes(long long n, int restart) {
+  if (n < 1 || restart < 1 || restart > NK_MAXM) return 0;
+  return g_layout(n, restart).total;
+}
+
+mjx_status mjx_gmres_solve(long long n, mjx_vec_op matvec, mjx_vec_op precond, void* user, const float* b,
+                           float* x, double tol, int restart, int max_cycles, int* iterations, double* rel_res,
+                           int* converged, void* ws, size_t ws_bytes, void* stream) {
+  if (n < 1 || matvec == nullptr || b == nullptr || x == nullptr || restart < 1 || restart > NK_MAXM ||
+      max_cycles < 1 || !(tol >= 0))
+    return MJX_BAD_ARG;
+  const GLayout L = g_layout(n, restart);
+  if (ws == nullptr || ws_bytes < L.total) return MJX_WORKSPACE;
+  cudaStream_t s = (cudaStream_t)stream;
+  char* w8 = (char*)ws;
+  float* V = (float*)(w8 + L.V);
+  float* t = (float*)(w8 + L.t);
+  float* w = (float*)(w8 + L.w);
+  double* part = (double*)(w8 + L.part);
+  GmresState* gs = (GmresState*)(w8 + L.gs);
+  const int grid = L.nblk;
+  auto fail = [&](cudaError_t e) -> mjx_status { set_last_error(e, __FILE__, __LINE__); return MJX_CUDA_ERROR; };
+  auto pre = [&](const float* in, float* out) -> int {
+    if (precond != nullptr) return precond(in, out, user, stream);
+    return cudaMemcpyAsync(out, in, sizeof(float) * (size_t)n, cudaMemcpyDeviceToDevice, s) == cudaSuccess ? 0 : 1;
+  };
+  int its = 0, conv = 0;
+  double res = 0.0, b0 = 0.0;
+  for (int cyc = 0; cyc < max_cycles && !conv; ++cyc) {
+    if (matvec(x, t, user, stream) != 0) return MJX_BAD_ARG;  // r = b - A x
+    sub_kernel<<<grid, 256, 0, s>>>(b, t, t, n);
+    if (pre(t, V) != 0) return MJX_BAD_ARG;                     // V_0 = M^-1 r
+    sumsq32_kernel<<<grid, 256, 0, s>>>(V, part, n);
+    gmres_init_kernel<<<1, 256, 0, s>>>(part, grid, gs, cyc == 0, tol, restart);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(e);
+    for (int j = 0; j < restart; ++j) {
+      nk_scale_j_kernel<<<grid, 256, 0, s>>>(V, gs, n);          // V_j /= |V_j|
+      if (matvec(V + (size_t)j * n, t, user, stream) != 0) return MJX_BAD_ARG;
+      if (pre(t, w) != 0) return MJX_BAD_ARG;                    // w = M^-1 A V_j
+      gmres_dots_kernel<<<grid, 256, 0, s>>>(V, w, gs, part, n);
+      gmres_hcol_kernel<<<1, 256, 0, s>>>(part, grid, gs);
+      gmres_orth_kernel<<<grid, 256, 0, s>>>(V, w, gs, part, n);
+      gmres_givens_kernel<<<1, 256, 0, s>>>(part, grid, gs, 0, 0);
+      if ((e = cudaGetLastError()) != cudaSuccess) return fail(e);
+    }
+    gmres_solve_kernel<<<1, 1, 0, s>>>(gs);
+    gmres_update_kernel<<<grid, 256, 0, s>>>(x, V, gs, n);
+    if ((e = cudaGetLastError()) != cudaSuccess) return fail(e);
+    GmresState h;
+    if ((e = cudaMemcpyAsync(&h, gs, sizeof(int) * 4 + sizeof(double) * 4, cudaMemcpyDeviceToHost, s)) !=
+        cudaSuccess)
+      return fail(e);
+    if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return fail(e);
+    its += h.k_used;
+    conv = h.converged;
+    if (cyc == 0) b0 = h.beta0;
+    res = h.res_est;
+  }
+  if (iterations) *iterations = its;
+  if (converged) *converged = conv;
+  if (rel_res) *rel_res = b0 > 0 ? res / b0 : 0.0;
+  return MJX_OK;
+}
+
 }  // extern "C"

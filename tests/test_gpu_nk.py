@@ -225,3 +225,42 @@ def test_newton_krylov_solve_routes_factory_residuals(cuda, method):
     out = M.newton_krylov_solve(res, guess, nk_params=nkp)
     assert out.stats.converged and conv and abs(out.stats.newton_iters - it) <= 1
     assert _rel(out.solution["u"][1:-1, 1:-1].cpu().numpy(), ref) < 1e-7
+
+
+def test_generic_gmres_entry(cuda):
+    """mjx_gmres_solve with host callbacks that enqueue library kernels: A = (I - h D Lap)^-1
+    (a periodic Helmholtz solve), left preconditioner (I + h/2 D Lap)^-1; the solution must
+    be (I - h D Lap) b.  A callback that reports failure aborts the solve."""
+    import ctypes as C
+    from moljax_gb300 import _native as N
+    from moljax_gb300.core.fft_solvers import get_plan
+    n = 64
+    plan = get_plan(n, n, 1.0 / n, 1.0 / n, "fd", torch.float32, cuda)
+    lib = N.lib()
+    wsz = plan.ws_bytes(1)
+    wsp = torch.empty(wsz, dtype=torch.uint8, device=cuda)
+    h, D = 1e-3, 1.0
+    Dc = (C.c_double * 1)(D)
+
+    def op(mult, hh):
+        def f(v, out, user, stream):
+            return lib.mjx_spectral_apply2d(N.ptr(plan.buf), C.byref(plan.cgrid), plan.code, 1, Dc, hh, mult, v, out,
+                                            N.ptr(wsp), wsz, stream)
+        return N.VecOp(f)
+    A, P = op(N.MULT_HELMHOLTZ, h), op(N.MULT_HELMHOLTZ, -0.5 * h)
+    rng = np.random.default_rng(2)
+    b = torch.tensor(rng.standard_normal((n, n)), dtype=torch.float32, device=cuda)
+    x = torch.zeros_like(b)
+    gw = torch.empty(lib.mjx_gmres_ws_bytes(n * n, 30), dtype=torch.uint8, device=cuda)
+    its, conv, rr = C.c_int(), C.c_int(), C.c_double()
+    stream = N.stream_ptr(cuda)
+    N.check("mjx_gmres_solve", lib.mjx_gmres_solve(n * n, A, P, None, N.ptr(b), N.ptr(x), 1e-6, 30, 10,
+                                                  C.byref(its), C.byref(rr), C.byref(conv), N.ptr(gw),
+                                                  gw.numel(), stream))
+    assert conv.value == 1 and 0 < its.value <= 300 and rr.value <= 1e-6
+    hlap = plan.apply(b, D, h, N.MULT_LAP)  # h D Lap b
+    exact = b - hlap
+    assert float(torch.linalg.norm(x - exact) / torch.linalg.norm(exact)) < 1e-4
+    bad = N.VecOp(lambda v, out, user, stream: 1)
+    assert lib.mjx_gmres_solve(n * n, bad, None, None, N.ptr(b), N.ptr(x), 1e-6, 30, 10, C.byref(its),
+                               C.byref(rr), C.byref(conv), N.ptr(gw), gw.numel(), stream) != 0
