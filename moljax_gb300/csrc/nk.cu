@@ -23,6 +23,8 @@
 #include <math.h>
 #include <string.h>
 
+#include <vector>
+
 #include "spectral.cuh"
 
 namespace mjx {
@@ -492,9 +494,140 @@ __global__ void nk_scale_j_kernel(float* V, const GmresState* gs, long long N2) 
 }
 
 
+// --------------------------------------------------------------- device Newton loop
+// The Newton iteration of newton_krylov_solve (newton_krylov.py:171-359) as one CUDA graph:
+// while (iterating) { R(x) and its norm; restarted GMRES (while cycles { cycle set-up; while
+// Arnoldi steps; solve and update }); backtracking line search (while tries { trial point
+// and its residual; sufficient-decrease test }); accept or take the damped step }.  Every
+// decision is made by a one-CTA kernel that sets the conditional flag of its loop; the host
+// launches the graph once per solve and reads the counters once.
+struct NewtonDev {
+  int it, converged, cyc, bt, accepted, lits, max_newton, max_krylov, max_backtrack, restart;
+  double rn, rb, res, newton_tol, krylov_tol, damping, backtrack, min_decrease;
+};
+
+// sum of the block partials (one CTA of 256 threads)
+__device__ __forceinline__ double nd_sum(const double* part, int nblk) {
+  __shared__ double red[8];
+  double acc = 0.0;
+  for (int b = threadIdx.x; b < nblk; b += blockDim.x) acc += part[b];
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  double s = 0.0;
+  for (int q = 0; q < (int)(blockDim.x >> 5); ++q) s += red[q];
+  return s;
+}
+
+// before the loop: |R(x0)|, converged (newton_krylov.py:338-346), the loop flag
+__global__ void nd_init_kernel(const double* part, int nblk, NewtonDev* nd, cudaGraphConditionalHandle hN) {
+  const double s = nd_sum(part, nblk);
+  if (threadIdx.x != 0) return;
+  nd->rn = sqrt(s);
+  nd->res = nd->rn;
+  nd->it = 0;
+  nd->lits = 0;
+  nd->converged = nd->rn < nd->newton_tol;
+  cudaGraphSetConditional(hN, (!nd->converged && nd->max_newton > 0) ? 1u : 0u);
+}
+
+// iteration top: |R(x)|, converged evaluated before the update (249-254); GMRES from dx = 0
+__global__ void nd_head_kernel(const double* part, int nblk, NewtonDev* nd, cudaGraphConditionalHandle hG) {
+  const double s = nd_sum(part, nblk);
+  if (threadIdx.x != 0) return;
+  nd->rn = sqrt(s);
+  nd->converged = nd->rn < nd->newton_tol;
+  nd->cyc = 0;
+  cudaGraphSetConditional(hG, nd->max_krylov > 0 ? 1u : 0u);
+}
+
+// GMRES cycle start (gmres_init_kernel with the first-cycle flag read on the device) and
+// the Arnoldi loop flag
+__global__ void nd_gmres_init_kernel(const double* part, int nblk, GmresState* gs, const NewtonDev* nd,
+                                     cudaGraphConditionalHandle hA) {
+  const double s = nd_sum(part, nblk);
+  if (threadIdx.x != 0) return;
+  const double b0 = sqrt(s);
+  const int m = nd->restart;
+  if (nd->cyc == 0) gs->tol_abs = nd->krylov_tol * b0;
+  gs->beta0 = b0;
+  gs->j = 0;
+  gs->m = m;
+  gs->k_used = 0;
+  for (int i = 0; i <= m; ++i) gs->g[i] = 0.0;
+  gs->g[0] = b0;
+  gs->res_est = b0;
+  gs->hnext_inv = b0 > 0 ? 1.0 / b0 : 0.0;
+  gs->converged = (b0 <= gs->tol_abs || b0 == 0.0) ? 1 : 0;
+  cudaGraphSetConditional(hA, gs->converged ? 0u : 1u);
+}
+
+// GMRES cycle end: Krylov iterations, next cycle while not converged and cycles remain
+__global__ void nd_cycle_end_kernel(const GmresState* gs, NewtonDev* nd, cudaGraphConditionalHandle hG) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  nd->lits += gs->k_used;
+  nd->cyc += 1;
+  cudaGraphSetConditional(hG, (!gs->converged && nd->cyc < nd->max_krylov) ? 1u : 0u);
+}
+
+// line search start (270-276): alpha = damping, reference norm |R(x)|
+__global__ void nd_ls_begin_kernel(NewtonDev* nd, NKConsts* K, cudaGraphConditionalHandle hL) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  K->alpha = nd->damping;
+  nd->rb = nd->rn;
+  nd->bt = 0;
+  nd->accepted = 0;
+  cudaGraphSetConditional(hL, nd->max_backtrack > 0 ? 1u : 0u);
+}
+
+// one try (277-316): sufficient decrease accepts, otherwise alpha *= backtrack
+__global__ void nd_ls_ctl_kernel(const double* part, int nblk, NewtonDev* nd, NKConsts* K,
+                                 cudaGraphConditionalHandle hL) {
+  const double s = nd_sum(part, nblk);
+  if (threadIdx.x != 0) return;
+  const double rnn = sqrt(s);
+  const double alpha = K->alpha;
+  nd->bt += 1;
+  if (rnn < (1.0 - nd->min_decrease * alpha) * nd->rb) {
+    nd->accepted = 1;
+    nd->rb = rnn;
+    cudaGraphSetConditional(hL, 0u);
+  } else {
+    K->alpha = alpha * nd->backtrack;
+    cudaGraphSetConditional(hL, nd->bt < nd->max_backtrack ? 1u : 0u);
+  }
+}
+
+// x <- the accepted trial point, or the full damped step when no try was accepted
+// (318-322); the FP32 copy for the next JVPs
+__global__ void nd_update_kernel(double* x, const double* xt, const float* dx, float* y32, const NewtonDev* nd,
+                                 long long N2) {
+  const bool acc = nd->accepted != 0;
+  const double al = nd->damping;
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < N2;
+       p += (long long)gridDim.x * blockDim.x) {
+    const double v = acc ? xt[p] : x[p] + al * (double)dx[p];
+    x[p] = v;
+    y32[p] = (float)v;
+  }
+}
+
+__global__ void nd_tail_kernel(NewtonDev* nd, cudaGraphConditionalHandle hN) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  nd->res = nd->rb;
+  nd->it += 1;
+  cudaGraphSetConditional(hN, (nd->it < nd->max_newton && !nd->converged) ? 1u : 0u);
+}
+
+__global__ void zero32_kernel(float* v, long long N2) {
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < N2;
+       p += (long long)gridDim.x * blockDim.x)
+    v[p] = 0.0f;
+}
+
 // --------------------------------------------------------------- host driver
 struct NKLayout {
-  size_t y0, y1, y2, y3, y4, cst, R, xt, y32, b32, dx, t, e, V, spec, part, gs, K, pst, total;
+  size_t y0, y1, y2, y3, y4, cst, R, xt, xn, y32, b32, dx, t, e, V, spec, part, gs, K, pst, nd, total;
   int nblk, m;
 };
 static inline size_t al(size_t b) { return (b + 255) & ~size_t(255); }
@@ -513,6 +646,7 @@ static NKLayout nk_layout(int n, int m) {
   L.cst = o; o += al(N2 * 8);
   L.R = o; o += al(N2 * 8);
   L.xt = o; o += al(N2 * 8);
+  L.xn = o; o += al(N2 * 8);
   L.y32 = o; o += al(N2 * 4);
   L.b32 = o; o += al(N2 * 4);
   L.dx = o; o += al(N2 * 4);
@@ -524,6 +658,7 @@ static NKLayout nk_layout(int n, int m) {
   L.gs = o; o += al(sizeof(GmresState));
   L.K = o; o += al(sizeof(NKConsts));
   L.pst = o; o += al(sizeof(DevState));
+  L.nd = o; o += al(256);  // NewtonDev
   L.total = o;
   return L;
 }
@@ -537,6 +672,7 @@ struct NKRun {
   cudaStream_t s;
   int grid;  // elementwise grid
   cudaGraphExec_t arnoldi;
+  cudaGraphExec_t newton;  // the device Newton loop (null: the host loop)
 };
 
 static double* P64(NKRun& r, size_t off) { return (double*)(r.ws + off); }
@@ -636,6 +772,202 @@ static cudaError_t build_arnoldi_graph(NKRun& r) {
   return ce;
 }
 
+struct NKParamsC {
+  int max_newton, max_krylov, restart, max_backtrack;
+  double newton_tol, krylov_tol, damping, backtrack, min_decrease;
+};
+
+// ---- the device Newton loop as one graph (nested conditional while nodes) ----
+// Appends the work that seg() enqueues on the capture stream to graph g after deps and
+// returns the nodes that end it.
+template <typename F>
+static cudaError_t capture_seg(cudaStream_t cs, cudaGraph_t g, std::vector<cudaGraphNode_t>& deps, F seg) {
+  cudaError_t ce = cudaStreamBeginCaptureToGraph(cs, g, deps.empty() ? nullptr : deps.data(), nullptr, deps.size(),
+                                                 cudaStreamCaptureModeThreadLocal);
+  if (ce != cudaSuccess) return ce;
+  const cudaError_t le = seg(cs);
+  cudaStreamCaptureStatus stt;
+  const cudaGraphNode_t* d = nullptr;
+  size_t nd = 0;
+  ce = cudaStreamGetCaptureInfo(cs, &stt, nullptr, nullptr, &d, nullptr, &nd);
+  std::vector<cudaGraphNode_t> out;
+  if (ce == cudaSuccess) out.assign(d, d + nd);
+  cudaGraph_t captured = nullptr;
+  const cudaError_t ee = cudaStreamEndCapture(cs, &captured);
+  if (le != cudaSuccess) return le;
+  if (ce != cudaSuccess) return ce;
+  if (ee != cudaSuccess) return ee;
+  deps = out;
+  return cudaSuccess;
+}
+
+// Builds r.newton: the Newton loop on the iterate buffer xn with the preconditioned
+// restarted GMRES, line search and counters of NewtonDev (parameters written here).
+static cudaError_t build_newton_graph(NKRun& r, const NKParamsC& P) {
+  const long long N2 = (long long)r.n * r.n;
+  NewtonDev h;
+  memset(&h, 0, sizeof(h));
+  h.max_newton = P.max_newton; h.max_krylov = P.max_krylov; h.max_backtrack = P.max_backtrack; h.restart = P.restart;
+  h.newton_tol = P.newton_tol; h.krylov_tol = P.krylov_tol; h.damping = P.damping; h.backtrack = P.backtrack;
+  h.min_decrease = P.min_decrease;
+  NewtonDev* nd = (NewtonDev*)(r.ws + r.L.nd);
+  cudaError_t ce = cudaMemcpyAsync(nd, &h, sizeof(h), cudaMemcpyHostToDevice, r.s);
+  if (ce == cudaSuccess) ce = cudaStreamSynchronize(r.s);  // h is a host stack value
+  if (ce != cudaSuccess) return ce;
+  NKConsts* K = (NKConsts*)(r.ws + r.L.K);
+  GmresState* gs = (GmresState*)(r.ws + r.L.gs);
+  double* x = P64(r, r.L.xn);
+  double* xt = P64(r, r.L.xt);
+  float* y32 = P32(r, r.L.y32);
+  float* dx = P32(r, r.L.dx);
+  float* V = P32(r, r.L.V);
+  float* t = P32(r, r.L.t);
+  float* b32 = P32(r, r.L.b32);
+  double* part = P64(r, r.L.part);
+  double* R = P64(r, r.L.R);
+  double* cst = P64(r, r.L.cst);
+  const int nblk = r.L.nblk, grid = r.grid, n = r.n;
+  const double idx2 = 1.0 / (r.dx * r.dx), idy2 = 1.0 / (r.dy * r.dy);
+  const float fidx2 = (float)idx2, fidy2 = (float)idy2;
+  cudaStream_t cs = nullptr;
+  cudaGraph_t top = nullptr;
+  do {
+    if ((ce = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking)) != cudaSuccess) break;
+    if ((ce = cudaGraphCreate(&top, 0)) != cudaSuccess) break;
+    NKRun rc = r;
+    rc.s = cs;
+    cudaGraphConditionalHandle hN, hG, hA, hL;
+    cudaGraph_t bN, bG, bA, bL;
+    std::vector<cudaGraphNode_t> d;
+    // before the loop: y32 = x, R(x), converged
+    if ((ce = capture_seg(cs, top, d, [&](cudaStream_t q) {
+           lincomb_kernel<<<grid, 256, 0, q>>>(x, 1.0, nullptr, 0.0, x, y32, N2);
+           vd_residual_kernel<<<nblk, 256, 0, q>>>(x, cst, R, b32, part, K, n, idx2, idy2);
+           return cudaGetLastError();
+         })) != cudaSuccess) break;
+    if ((ce = cudaGraphConditionalHandleCreate(&hN, top, 0, 0)) != cudaSuccess) break;
+    if ((ce = capture_seg(cs, top, d, [&](cudaStream_t q) {
+           nd_init_kernel<<<1, 256, 0, q>>>(part, nblk, nd, hN);
+           return cudaGetLastError();
+         })) != cudaSuccess) break;
+    {
+      cudaGraphNodeParams np = {cudaGraphNodeTypeConditional};
+      np.conditional.handle = hN;
+      np.conditional.type = cudaGraphCondTypeWhile;
+      np.conditional.size = 1;
+      cudaGraphNode_t node;
+      if ((ce = cudaGraphAddNode(&node, top, d.data(), nullptr, d.size(), &np)) != cudaSuccess) break;
+      bN = np.conditional.phGraph_out[0];
+    }
+    // Newton body: R(x) and its norm, dx = 0
+    std::vector<cudaGraphNode_t> dn;
+    if ((ce = capture_seg(cs, bN, dn, [&](cudaStream_t q) {
+           vd_residual_kernel<<<nblk, 256, 0, q>>>(x, cst, R, b32, part, K, n, idx2, idy2);
+           zero32_kernel<<<grid, 256, 0, q>>>(dx, N2);
+           return cudaGetLastError();
+         })) != cudaSuccess) break;
+    // the GMRES cycle loop (its flag set by the head kernel)
+    if ((ce = cudaGraphConditionalHandleCreate(&hG, bN, 0, 0)) != cudaSuccess) break;
+    if ((ce = capture_seg(cs, bN, dn, [&](cudaStream_t q) {
+           nd_head_kernel<<<1, 256, 0, q>>>(part, nblk, nd, hG);
+           return cudaGetLastError();
+         })) != cudaSuccess) break;
+    {
+      cudaGraphNodeParams np = {cudaGraphNodeTypeConditional};
+      np.conditional.handle = hG;
+      np.conditional.type = cudaGraphCondTypeWhile;
+      np.conditional.size = 1;
+      cudaGraphNode_t node;
+      if ((ce = cudaGraphAddNode(&node, bN, dn.data(), nullptr, dn.size(), &np)) != cudaSuccess) break;
+      bG = np.conditional.phGraph_out[0];
+      dn.assign(1, node);
+    }
+    // GMRES cycle: r = b - J dx, V_0 = M^-1 r, |V_0|; the Arnoldi loop; solve and update
+    std::vector<cudaGraphNode_t> dg;
+    if ((ce = cudaGraphConditionalHandleCreate(&hA, bG, 0, 0)) != cudaSuccess) break;
+    if ((ce = capture_seg(cs, bG, dg, [&](cudaStream_t q) {
+           vd_jvp_j_kernel<<<grid, 256, 0, q>>>(y32, dx, nullptr, t, K, n, fidx2, fidy2, N2);
+           sub_kernel<<<grid, 256, 0, q>>>(b32, t, t, N2);
+           cudaError_t e = precond(rc, t, V, nullptr);
+           if (e != cudaSuccess) return e;
+           sumsq32_kernel<<<nblk, 256, 0, q>>>(V, part, N2);
+           nd_gmres_init_kernel<<<1, 256, 0, q>>>(part, nblk, gs, nd, hA);
+           return cudaGetLastError();
+         })) != cudaSuccess) break;
+    {
+      cudaGraphNodeParams np = {cudaGraphNodeTypeConditional};
+      np.conditional.handle = hA;
+      np.conditional.type = cudaGraphCondTypeWhile;
+      np.conditional.size = 1;
+      cudaGraphNode_t node;
+      if ((ce = cudaGraphAddNode(&node, bG, dg.data(), nullptr, dg.size(), &np)) != cudaSuccess) break;
+      bA = np.conditional.phGraph_out[0];
+      dg.assign(1, node);
+    }
+    std::vector<cudaGraphNode_t> da;
+    if ((ce = capture_seg(cs, bA, da, [&](cudaStream_t) { return arnoldi_step(rc, hA, 1); })) != cudaSuccess) break;
+    if ((ce = capture_seg(cs, bG, dg, [&](cudaStream_t q) {
+           gmres_solve_kernel<<<1, 1, 0, q>>>(gs);
+           gmres_update_kernel<<<grid, 256, 0, q>>>(dx, V, gs, N2);
+           nd_cycle_end_kernel<<<1, 32, 0, q>>>(gs, nd, hG);
+           return cudaGetLastError();
+         })) != cudaSuccess) break;
+    // line search
+    if ((ce = cudaGraphConditionalHandleCreate(&hL, bN, 0, 0)) != cudaSuccess) break;
+    if ((ce = capture_seg(cs, bN, dn, [&](cudaStream_t q) {
+           nd_ls_begin_kernel<<<1, 32, 0, q>>>(nd, K, hL);
+           return cudaGetLastError();
+         })) != cudaSuccess) break;
+    {
+      cudaGraphNodeParams np = {cudaGraphNodeTypeConditional};
+      np.conditional.handle = hL;
+      np.conditional.type = cudaGraphCondTypeWhile;
+      np.conditional.size = 1;
+      cudaGraphNode_t node;
+      if ((ce = cudaGraphAddNode(&node, bN, dn.data(), nullptr, dn.size(), &np)) != cudaSuccess) break;
+      bL = np.conditional.phGraph_out[0];
+      dn.assign(1, node);
+    }
+    std::vector<cudaGraphNode_t> dl;
+    if ((ce = capture_seg(cs, bL, dl, [&](cudaStream_t q) {
+           trial_kernel<<<grid, 256, 0, q>>>(x, dx, xt, K, nullptr, N2);
+           vd_residual_kernel<<<nblk, 256, 0, q>>>(xt, cst, R, b32, part, K, n, idx2, idy2);
+           nd_ls_ctl_kernel<<<1, 256, 0, q>>>(part, nblk, nd, K, hL);
+           return cudaGetLastError();
+         })) != cudaSuccess) break;
+    // the step and the loop flag
+    if ((ce = capture_seg(cs, bN, dn, [&](cudaStream_t q) {
+           nd_update_kernel<<<grid, 256, 0, q>>>(x, xt, dx, y32, nd, N2);
+           nd_tail_kernel<<<1, 32, 0, q>>>(nd, hN);
+           return cudaGetLastError();
+         })) != cudaSuccess) break;
+    ce = cudaGraphInstantiate(&r.newton, top, 0);
+  } while (0);
+  if (top) cudaGraphDestroy(top);
+  if (cs) cudaStreamDestroy(cs);
+  if (ce != cudaSuccess) {
+    if (r.newton) cudaGraphExecDestroy(r.newton);
+    r.newton = nullptr;
+  }
+  return ce;
+}
+
+// Newton on the device graph: x is copied into the iterate buffer, the graph runs the
+// whole iteration, the counters come back with one synchronisation.
+static cudaError_t newton_dev(NKRun& r, double* x, int* n_newton, int* n_lin, int* conv_out, double* res_out) {
+  const long long N2 = (long long)r.n * r.n;
+  double* xn = P64(r, r.L.xn);
+  cudaError_t e = cudaMemcpyAsync(xn, x, sizeof(double) * N2, cudaMemcpyDeviceToDevice, r.s);
+  if (e == cudaSuccess) e = cudaGraphLaunch(r.newton, r.s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(x, xn, sizeof(double) * N2, cudaMemcpyDeviceToDevice, r.s);
+  NewtonDev h;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&h, r.ws + r.L.nd, sizeof(h), cudaMemcpyDeviceToHost, r.s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(r.s);
+  if (e != cudaSuccess) return e;
+  *n_newton = h.it; *n_lin = h.lits; *conv_out = h.converged; *res_out = h.res;
+  return cudaSuccess;
+}
+
 static cudaError_t norm_of(NKRun& r, double* part_dev, double* host_out) {
   // the residual kernel already left per-block partial sums in part_dev
   double h[152 * 4];
@@ -659,10 +991,6 @@ static cudaError_t residual(NKRun& r, const double* x, double* rnorm, bool rhs) 
   return norm_of(r, P64(r, r.L.part), rnorm);
 }
 
-struct NKParamsC {
-  int max_newton, max_krylov, restart, max_backtrack;
-  double newton_tol, krylov_tol, damping, backtrack, min_decrease;
-};
 
 // Newton on R(x) = 0 from the guess in x (FP64, updated in place)
 static cudaError_t newton(NKRun& r, double* x, const NKParamsC& P, int* n_newton, int* n_lin,
@@ -807,6 +1135,7 @@ static cudaError_t implicit_step(NKRun& r, const NKParamsC& P, const double* abc
   sumsq_kernel<<<r.L.nblk, 256, 0, r.s>>>(yc, P64(r, r.L.part), N2);
   nk_consts_kernel<<<1, 256, 0, r.s>>>(P64(r, r.L.part), r.L.nblk, K, pst, (double)N2);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  if (r.newton != nullptr) return newton_dev(r, yout, &so->newton, &so->lin, &so->converged, &so->res);
   return newton(r, yout, P, &so->newton, &so->lin, &so->converged, &so->res);
 }
 
@@ -831,6 +1160,7 @@ static mjx_status nk_setup(NKRun& r, const void* plan2, int n, double dy, double
   r.s = (cudaStream_t)stream;
   r.grid = 152 * 4;
   r.arnoldi = nullptr;
+  r.newton = nullptr;
   if (ws == nullptr || ws_bytes < r.L.total) return MJX_WORKSPACE;
   MJX_TRY(ensure_kernel_attrs());
   MJX_CUDA_TRY(cudaMemsetAsync(r.ws + r.L.pst, 0, sizeof(DevState), r.s));
@@ -838,6 +1168,8 @@ static mjx_status nk_setup(NKRun& r, const void* plan2, int n, double dy, double
   P->max_backtrack = nkp->max_backtrack; P->newton_tol = nkp->newton_tol; P->krylov_tol = nkp->krylov_tol;
   P->damping = nkp->damping; P->backtrack = nkp->backtrack_factor; P->min_decrease = nkp->min_residual_decrease;
   MJX_CUDA_TRY(build_arnoldi_graph(r));
+  // the device Newton loop; without nested conditional graphs the host loop runs instead
+  if (!host_loop_mode() && build_newton_graph(r, *P) != cudaSuccess) (void)cudaGetLastError();
   return MJX_OK;
 }
 
@@ -888,6 +1220,7 @@ mjx_status mjx_nk_vardiff_integrate2d(const void* plan2, int n, double dy, doubl
     if (e != cudaSuccess) { set_last_error(e, __FILE__, __LINE__); rc = MJX_CUDA_ERROR; }
   }
   if (r.arnoldi) cudaGraphExecDestroy(r.arnoldi);
+  if (r.newton) cudaGraphExecDestroy(r.newton);
   return rc;
 }
 
@@ -941,6 +1274,7 @@ mjx_status mjx_nk_vardiff_step2d(const void* plan2, int n, double dy, double dx,
   if (stats) { stats[0] = so.newton; stats[1] = so.lin; stats[2] = so.converged; }
   if (res_norm) *res_norm = so.res;
   if (r.arnoldi) cudaGraphExecDestroy(r.arnoldi);
+  if (r.newton) cudaGraphExecDestroy(r.newton);
   return rc;
 }
 
@@ -1089,6 +1423,7 @@ mjx_status mjx_nk_vardiff_adaptive2d(const void* plan2, int n, double dy, double
   }
   if (nk_totals) { nk_totals[0] = tot_newton; nk_totals[1] = tot_lin; nk_totals[2] = not_conv; }
   if (r.arnoldi) cudaGraphExecDestroy(r.arnoldi);
+  if (r.newton) cudaGraphExecDestroy(r.newton);
   return rc;
 }
 

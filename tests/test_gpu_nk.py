@@ -229,8 +229,9 @@ def test_newton_krylov_solve_routes_factory_residuals(cuda, method):
 
 def test_generic_gmres_entry(cuda):
     """mjx_gmres_solve with host callbacks that enqueue library kernels: A = (I - h D Lap)^-1
-    (a periodic Helmholtz solve), left preconditioner (I + h/2 D Lap)^-1; the solution must
-    be (I - h D Lap) b.  A callback that reports failure aborts the solve."""
+    (a periodic Helmholtz solve, condition number ~34 here), without a preconditioner and with
+    the mild SPD left preconditioner (I - h' D Lap)^-1, h' = h/100; the solution must be
+    (I - h D Lap) b.  A callback that reports failure aborts the solve."""
     import ctypes as C
     from moljax_gb300 import _native as N
     from moljax_gb300.core.fft_solvers import get_plan
@@ -247,20 +248,57 @@ def test_generic_gmres_entry(cuda):
             return lib.mjx_spectral_apply2d(N.ptr(plan.buf), C.byref(plan.cgrid), plan.code, 1, Dc, hh, mult, v, out,
                                             N.ptr(wsp), wsz, stream)
         return N.VecOp(f)
-    A, P = op(N.MULT_HELMHOLTZ, h), op(N.MULT_HELMHOLTZ, -0.5 * h)
+    A, P = op(N.MULT_HELMHOLTZ, h), op(N.MULT_HELMHOLTZ, 0.01 * h)
     rng = np.random.default_rng(2)
     b = torch.tensor(rng.standard_normal((n, n)), dtype=torch.float32, device=cuda)
-    x = torch.zeros_like(b)
+    exact = b - plan.apply(b, D, h, N.MULT_LAP)  # (I - h D Lap) b
     gw = torch.empty(lib.mjx_gmres_ws_bytes(n * n, 30), dtype=torch.uint8, device=cuda)
-    its, conv, rr = C.c_int(), C.c_int(), C.c_double()
     stream = N.stream_ptr(cuda)
-    N.check("mjx_gmres_solve", lib.mjx_gmres_solve(n * n, A, P, None, N.ptr(b), N.ptr(x), 1e-6, 30, 10,
-                                                  C.byref(its), C.byref(rr), C.byref(conv), N.ptr(gw),
-                                                  gw.numel(), stream))
-    assert conv.value == 1 and 0 < its.value <= 300 and rr.value <= 1e-6
-    hlap = plan.apply(b, D, h, N.MULT_LAP)  # h D Lap b
-    exact = b - hlap
-    assert float(torch.linalg.norm(x - exact) / torch.linalg.norm(exact)) < 1e-4
+    for pre in (N.VecOp(), P):  # VecOp(): a NULL callback, no preconditioner
+        x = torch.zeros_like(b)
+        its, conv, rr = C.c_int(), C.c_int(), C.c_double()
+        N.check("mjx_gmres_solve", lib.mjx_gmres_solve(n * n, A, pre, None, N.ptr(b), N.ptr(x), 1e-5, 30, 20,
+                                                      C.byref(its), C.byref(rr), C.byref(conv), N.ptr(gw),
+                                                      gw.numel(), stream))
+        assert conv.value == 1 and 0 < its.value <= 600 and rr.value <= 1e-5, (its.value, rr.value)
+        assert float(torch.linalg.norm(x - exact) / torch.linalg.norm(exact)) < 1e-3
     bad = N.VecOp(lambda v, out, user, stream: 1)
-    assert lib.mjx_gmres_solve(n * n, bad, None, None, N.ptr(b), N.ptr(x), 1e-6, 30, 10, C.byref(its),
+    assert lib.mjx_gmres_solve(n * n, bad, N.VecOp(), None, N.ptr(b), N.ptr(x), 1e-5, 30, 10, C.byref(its),
                                C.byref(rr), C.byref(conv), N.ptr(gw), gw.numel(), stream) != 0
+
+
+_NK_HOST_CHILD = r"""
+import sys
+sys.path.insert(0, sys.argv[1])
+import numpy as np, torch
+import moljax_gb300 as M
+from oracle import nk as ONK
+n = 64
+u0 = ONK.gaussians_ic(n)
+dx = 1.0 / n
+u, st = M.integrate_implicit_vardiff(torch.tensor(u0, device="cuda"), dx, 100 * dx * dx, 4, method="bdf2",
+                                     nk_params=M.NKParams(gmres_restart=30), be_guess="previous")
+np.savez(sys.argv[2], u=u.cpu().numpy(), st=st.cpu().numpy())
+"""
+
+
+def test_device_newton_loop_matches_host_loop(cuda, tmp_path):
+    """The Newton iteration as one graph of nested conditional loops (default) against the
+    host-driven iteration (MJX_HOST_LOOP=1, read once per process): the same kernels and the
+    same decisions, so the same Newton / GMRES counts and the same states."""
+    import os
+    import subprocess
+    import sys
+    import moljax_gb300 as M
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    path = str(tmp_path / "nk_host.npz")
+    subprocess.run([sys.executable, "-c", _NK_HOST_CHILD, root, path], env=dict(os.environ, MJX_HOST_LOOP="1"),
+                   check=True, timeout=600)
+    child = np.load(path)
+    n = 64
+    u0 = ONK.gaussians_ic(n)
+    dx = 1.0 / n
+    u, st = M.integrate_implicit_vardiff(torch.tensor(u0, device=cuda), dx, 100 * dx * dx, 4, method="bdf2",
+                                         nk_params=M.NKParams(gmres_restart=30), be_guess="previous")
+    np.testing.assert_array_equal(st.cpu().numpy(), child["st"])
+    assert _rel(u.cpu().numpy(), child["u"]) < 1e-12
