@@ -103,12 +103,12 @@ __host__ __device__ __forceinline__ unsigned witem(int inst, int job, int blk) {
 template <int PASS>
 __device__ __forceinline__ void bcol_item(float2* buf, const BInst* I, unsigned it) {
   const int job = (it >> 16) & 15, tile = it & 0xffff;
-  const int f = PASS == BPASS_C2 ? job >> 1 : job;
+  const int f = job;
   const int cur = I->st.cur;
   const double h = I->st.dtc;
   MColTile t;
   t.ny = I->ny; t.log2ny = I->log2ny; t.ncols = I->ncols; t.C = I->colC;
-  t.type = PASS == BPASS_C1 ? MC_SPLIT : (PASS == BPASS_C3 ? MC_HALF_END : ((job & 1) ? MC_HALF_MID : MC_FULL_END));
+  t.type = PASS == BPASS_C1 ? MC_SPLIT : (PASS == BPASS_C3 ? MC_HALF_END : MC_MID_BOTH);
   t.kx0 = tile * I->colC;
   t.ldc = I->ldc; t.off = (long long)f * I->fs;
   t.ys_cur = I->ys[cur]; t.ys_next = I->ys[1 - cur];
@@ -366,8 +366,7 @@ static void inst_items(const BInst& I, int slot, std::vector<unsigned>* w) {
   for (int f = 0; f < 2; ++f)
     for (int t = 0; t < tiles; ++t) {
       w[BPASS_C1].push_back(witem(slot, f, t));
-      w[BPASS_C2].push_back(witem(slot, 2 * f, t));
-      w[BPASS_C2].push_back(witem(slot, 2 * f + 1, t));
+      w[BPASS_C2].push_back(witem(slot, f, t));  // both C2 jobs of the field in one tile
       w[BPASS_C3].push_back(witem(slot, f, t));
     }
   for (int b = 0; b < I.nblk; ++b) {
@@ -381,8 +380,8 @@ static void inst_items(const BInst& I, int slot, std::vector<unsigned>* w) {
 
 static size_t inst_item_count(int ny, int nx) {
   const int C = b_colC(ny), tiles = (nx / 2 + 1 + C - 1) / C, nblk = ny / b_rseq(ny, nx);
-  const size_t c2 = (size_t)tiles * 4, r1 = (size_t)nblk * 2;
-  return c2 > r1 ? c2 : r1;  // the largest pass (C2 or R1)
+  const size_t c = (size_t)tiles * 2, r1 = (size_t)nblk * 2;
+  return c > r1 ? c : r1;  // the largest pass (a column pass: one tile per field and tile; or R1)
 }
 
 struct EngLayout {
