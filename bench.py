@@ -7,7 +7,7 @@ precision is "mixed": float-float (FP32 pair) spectral state, FP32 transforms
 of the reaction increments (rel-L2 vs the FP64 path is reported in the line).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-  python bench.py --kernels-only [--reps R]   # per-kernel CUDA-event times only
+  python bench.py --kernels-only [--reps R] [--graph]   # per-kernel CUDA-event times only
   python bench.py --workload etdrk4 --n 4096 [--etd-steps S] [--kernels-only] [--etd-method etd1|etd2]
   python bench.py --workload serve [--requests R]
   python bench.py --workload fft3d --n 512 [--etd-steps S] [--fp32]
@@ -66,6 +66,7 @@ def parse():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp32"])
     ap.add_argument("--kernels-only", action="store_true")
+    ap.add_argument("--graph", action="store_true", help="--kernels-only: time each kernel inside a CUDA graph")
     ap.add_argument("--workload", default="imex", choices=["imex", "etdrk4", "serve", "fft3d", "explicit", "nk", "stencil",
                                                           "gs256", "tubular"])
     ap.add_argument("--fp32", action="store_true", help="fft3d: FP32 instead of FP64")
@@ -182,8 +183,11 @@ def kernel_bytes_mixed(n):
             "C3 col end+err": f * nc * 72, "R3 row err": f * nc * 16}
 
 
-def time_kernels_mixed(M, model, cache, diff, y0, dev, reps=30):
-    """CUDA-event time of each mixed-precision attempt kernel on the launching stream."""
+def time_kernels_mixed(M, model, cache, diff, y0, dev, reps=30, graph=False):
+    """CUDA-event time of each mixed-precision attempt kernel on the launching stream.  With
+    graph=True each kernel is captured reps times back to back into a CUDA graph and the
+    graph replayed (the kernel's cost inside the attempt loop, without the host's launch
+    rate), and 'attempt' is the six kernels in order, captured 20 times."""
     import torch
     from moljax_gb300 import _native as N
     from moljax_gb300.core import stencil
@@ -205,6 +209,35 @@ def time_kernels_mixed(M, model, cache, diff, y0, dev, reps=30):
     names = list(kernel_bytes_mixed(grid.nx).keys())
     out = {}
     s = torch.cuda.current_stream(dev)
+    if graph:
+        for w in range(1, 7):
+            call(w)
+        torch.cuda.synchronize(dev)
+
+        def graph_time(seq, n):
+            g = torch.cuda.CUDAGraph()
+            cs = torch.cuda.Stream(dev)
+            cs.wait_stream(s)
+            with torch.cuda.stream(cs):
+                with torch.cuda.graph(g, stream=cs):
+                    for _ in range(n):
+                        for w in seq:
+                            N.check("mjx_imex_mixed_attempt_kernel2d", lib.mjx_imex_mixed_attempt_kernel2d(
+                                N.ptr(p32.buf), N.ptr(p64.buf), C.byref(p32.cgrid), C.byref(prob), C.byref(pid),
+                                w, 0.9, N.ptr(interior), N.ptr(ws), ws.numel(), cs.cuda_stream))
+            g.replay()
+            torch.cuda.synchronize(dev)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(s)
+            for _ in range(5):
+                g.replay()
+            e1.record(s)
+            e1.synchronize()
+            return e0.elapsed_time(e1) / 5 / n * 1e-3
+        for w in range(1, 7):
+            out[names[w - 1]] = graph_time([w], reps)
+        out["attempt"] = graph_time([1, 2, 3, 4, 5, 6], 20)
+        return out
     for w in range(1, 7):
         for _ in range(min(3, reps)):
             call(w)
@@ -1007,11 +1040,11 @@ def run_kernels_only(args, local):
     torch.cuda.set_device(dev)
     M, grid, model, cache, diff, y0 = make_problem(torch.float32, dev, args.n)
     if args.precision == "mixed":
-        kt = time_kernels_mixed(M, model, cache, diff, y0, dev, reps=args.reps)
+        kt = time_kernels_mixed(M, model, cache, diff, y0, dev, reps=args.reps, graph=args.graph)
     else:
         kt = time_kernels(M, model, cache, diff, y0, dev, reps=args.reps)
     return {"kernels_us": {k: v * 1e6 for k, v in kt.items()}, "precision": args.precision,
-            "n": args.n, "reps": args.reps}
+            "n": args.n, "reps": args.reps, "in_graph": bool(args.graph and args.precision == "mixed")}
 
 
 # ------------------------------------------------------------------ CPU (oracle) arms
