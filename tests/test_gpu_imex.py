@@ -128,11 +128,12 @@ sys.path.insert(0, sys.argv[1])
 import moljax_gb300 as M
 from oracle import mol
 dev = torch.device("cuda", 0)
+ny, nx = int(sys.argv[3]), int(sys.argv[4])
 out = {}
 for prec, dtype in (("fp64", torch.float64), ("fp32", torch.float32), ("mixed", torch.float32)):
-    grid = M.Grid2D(64, 64, 0.0, 2.5, 0.0, 2.5)
+    grid = M.Grid2D(nx, ny, 0.0, 2.5, 0.0, 2.5)
     model, cache, diff = M.create_gray_scott_periodic_fft(grid, 2e-5, 1e-5, 0.035, 0.065, dtype, dev)
-    y0 = mol.gray_scott_ic(mol.Grid2D(64, 64, 0, 2.5, 0, 2.5), 11)
+    y0 = mol.gray_scott_ic(mol.Grid2D(nx, ny, 0, 2.5, 0, 2.5), 11)
     ym = {k: torch.tensor(v, dtype=dtype, device=dev) for k, v in y0.items()}
     r = M.adaptive_integrate_imex(model, ym, 0.0, 25.0, 1.0, cache, diff,
                                   pid_params=M.PIDParams(atol=1e-7, rtol=1e-5), save_every=3,
@@ -144,24 +145,26 @@ np.savez(sys.argv[2], **out)
 """
 
 
-def test_host_driven_loop_matches_device_loop(cuda, tmp_path):
+@pytest.mark.parametrize("ny,nx", [(64, 64), (32, 1024)])
+def test_host_driven_loop_matches_device_loop(cuda, tmp_path, ny, nx):
     # MJX_HOST_LOOP=1 (read once per process) launches the attempts from the host in
-    # batches instead of the conditional graph: identical kernels, identical results
+    # batches instead of the conditional graph: identical kernels, identical results, bit for
+    # bit.  Rows of 1024 take the warp-row pass.
     import os
     import subprocess
     import sys
     from oracle import mol as omol
     root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-    path = str(tmp_path / "host_loop.npz")
+    path = str(tmp_path / "child.npz")
     env = dict(os.environ, MJX_HOST_LOOP="1")
-    subprocess.run([sys.executable, "-c", _HOST_LOOP_CHILD, root, path], env=env, check=True,
-                   timeout=600)
+    subprocess.run([sys.executable, "-c", _HOST_LOOP_CHILD, root, path, str(ny), str(nx)], env=env,
+                   check=True, timeout=600)
     child = np.load(path)
     import moljax_gb300 as M
     for prec, dtype in (("fp64", torch.float64), ("fp32", torch.float32), ("mixed", torch.float32)):
-        grid = M.Grid2D(64, 64, 0.0, 2.5, 0.0, 2.5)
+        grid = M.Grid2D(nx, ny, 0.0, 2.5, 0.0, 2.5)
         model, cache, diff = M.create_gray_scott_periodic_fft(grid, 2e-5, 1e-5, 0.035, 0.065, dtype, cuda)
-        y0 = omol.gray_scott_ic(omol.Grid2D(64, 64, 0, 2.5, 0, 2.5), 11)
+        y0 = omol.gray_scott_ic(omol.Grid2D(nx, ny, 0, 2.5, 0, 2.5), 11)
         ym = {k: torch.tensor(v, dtype=dtype, device=cuda) for k, v in y0.items()}
         r = M.adaptive_integrate_imex(model, ym, 0.0, 25.0, 1.0, cache, diff,
                                       pid_params=M.PIDParams(atol=1e-7, rtol=1e-5), save_every=3,
