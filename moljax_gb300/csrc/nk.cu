@@ -18,14 +18,19 @@
 // Dirichlet = DST-II diagonalisation), applied with the periodic spectral pass.
 //
 // The Arnoldi steps of a GMRES cycle run as one CUDA graph with a conditional
-// while node; the Givens kernel updates the residual estimate on the device and
-// clears the loop flag, so a cycle costs one host synchronisation.
+// while node, four kernels per step (the fused passes below: operand + forward
+// row transforms, column pass, inverse row transforms + Gram-Schmidt dots,
+// orthogonalisation + Givens step); the last CTA of the last kernel updates the
+// residual estimate on the device and clears the loop flag.  In the default
+// mode the whole Newton iteration is one graph of nested conditional loops.
 #include <math.h>
 #include <string.h>
 
 #include <vector>
 
+#include "mixed.cuh"
 #include "spectral.cuh"
+#include "wfft.cuh"
 
 namespace mjx {
 
@@ -34,6 +39,7 @@ int elem_size(int dtype);
 void set_last_error(cudaError_t e, const char* file, int line);
 
 enum { NK_MAXM = 64 };
+enum { NK_RING = 256 };  // steps of counts kept on the device between host reads
 
 struct NKConsts {
   double a0, beta;      // residual R = a0 y + cst - beta F(y)
@@ -73,31 +79,23 @@ __device__ __forceinline__ void nk_rowcol(long long p, int n, int& i, int& j) {
   }
 }
 
-// R = a0 y + cst - beta F(y); part[block] = sum R^2; b32 = -R (optional)
-__global__ void vd_residual_kernel(const double* __restrict__ y, const double* __restrict__ cst,
-                                   double* __restrict__ R, float* __restrict__ b32,
-                                   double* __restrict__ part, const NKConsts* __restrict__ K,
-                                   int n, double idx2, double idy2) {
-  const double a = K->pa, b = K->pb, c = K->pc, a0 = K->a0, beta = K->beta;
-  double acc = 0.0;
-  const long long N2 = (long long)n * n;
-  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < N2;
-       p += (long long)gridDim.x * blockDim.x) {
-    int i, j;
-    nk_rowcol(p, n, i, j);
-    const double uc = y[p];
-    const double ue = dval(y, i, j + 1, n), uw = dval(y, i, j - 1, n);
-    const double un = dval(y, i + 1, j, n), us = dval(y, i - 1, j, n);
-    const double Dc = a + b * uc * uc;
-    const double De = a + b * ue * ue, Dw = a + b * uw * uw, Dn = a + b * un * un, Ds = a + b * us * us;
-    const double fx = 0.5 * (Dc + De) * (ue - uc) - 0.5 * (Dw + Dc) * (uc - uw);
-    const double fy = 0.5 * (Dc + Dn) * (un - uc) - 0.5 * (Ds + Dc) * (uc - us);
-    const double F = fx * idx2 + fy * idy2 - c * uc * uc * uc;
-    const double r = a0 * uc + cst[p] - beta * F;
-    R[p] = r;
-    if (b32) b32[p] = (float)(-r);
-    acc += r * r;
-  }
+// R = a0 u + cst - beta F(u) at (i, j); u(i, j) returns the ghosted value
+template <class G>
+__device__ __forceinline__ double vd_resid_at(G u, int i, int j, double cst_p, double a, double b, double c,
+                                              double a0, double beta, double idx2, double idy2) {
+  const double uc = u(i, j);
+  const double ue = u(i, j + 1), uw = u(i, j - 1);
+  const double un = u(i + 1, j), us = u(i - 1, j);
+  const double Dc = a + b * uc * uc;
+  const double De = a + b * ue * ue, Dw = a + b * uw * uw, Dn = a + b * un * un, Ds = a + b * us * us;
+  const double fx = 0.5 * (Dc + De) * (ue - uc) - 0.5 * (Dw + Dc) * (uc - uw);
+  const double fy = 0.5 * (Dc + Dn) * (un - uc) - 0.5 * (Ds + Dc) * (uc - us);
+  const double F = fx * idx2 + fy * idy2 - c * uc * uc * uc;
+  return a0 * uc + cst_p - beta * F;
+}
+
+// block sum of acc into part[blockIdx.x] (FP64)
+__device__ __forceinline__ void block_partial(double acc, double* part) {
   __shared__ double red[32];
   for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
   if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
@@ -107,6 +105,27 @@ __global__ void vd_residual_kernel(const double* __restrict__ y, const double* _
     for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += red[w];
     part[blockIdx.x] = s;
   }
+}
+
+// R = a0 y + cst - beta F(y); part[block] = sum R^2; b32 = -R (optional)
+__global__ void vd_residual_kernel(const double* __restrict__ y, const double* __restrict__ cst,
+                                   double* __restrict__ R, float* __restrict__ b32,
+                                   double* __restrict__ part, const NKConsts* __restrict__ K,
+                                   int n, double idx2, double idy2) {
+  const double a = K->pa, b = K->pb, c = K->pc, a0 = K->a0, beta = K->beta;
+  double acc = 0.0;
+  const long long N2 = (long long)n * n;
+  auto u = [&](int ii, int jj) { return dval(y, ii, jj, n); };
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < N2;
+       p += (long long)gridDim.x * blockDim.x) {
+    int i, j;
+    nk_rowcol(p, n, i, j);
+    const double r = vd_resid_at(u, i, j, cst[p], a, b, c, a0, beta, idx2, idy2);
+    R[p] = r;
+    if (b32) b32[p] = (float)(-r);
+    acc += r * r;
+  }
+  block_partial(acc, part);
 }
 
 // out = s F(y) (the model right-hand side, scaled), constants by value
@@ -125,37 +144,6 @@ __global__ void vd_rhs_kernel(const double* __restrict__ y, double* __restrict__
     const double fx = 0.5 * (Dc + De) * (ue - uc) - 0.5 * (Dw + Dc) * (uc - uw);
     const double fy = 0.5 * (Dc + Dn) * (un - uc) - 0.5 * (Ds + Dc) * (uc - us);
     out[p] = s * (fx * idx2 + fy * idy2 - c * uc * uc * uc);
-  }
-}
-
-// odd extension N x N -> 2N x 2N (Dirichlet cell-centred <-> periodic)
-// rows 0..n-1 of the 2n x 2n cell-centred odd extension (each row [r_i, -reverse(r_i)]);
-// rows n..2n-1, the negated mirror, are synthesised by the column pass (ColArgs::oddy)
-__global__ void oddext_kernel(const float* __restrict__ r, float* __restrict__ e, int n,
-                              const GmresState* gs) {
-  if (gs && gs->converged) return;
-  const int m = 2 * n;
-  const long long M2 = (long long)n * m;
-  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < M2;
-       p += (long long)gridDim.x * blockDim.x) {
-    int i, j;
-    nk_rowcol(p, m, i, j);
-    const int jj = j < n ? j : 2 * n - 1 - j;
-    const float sgn = j < n ? 1.f : -1.f;
-    e[p] = sgn * r[(long long)i * n + jj];
-  }
-}
-
-__global__ void restrict_kernel(const float* __restrict__ e, float* __restrict__ w, int n,
-                                const NKConsts* K, const GmresState* gs) {
-  if (gs && gs->converged) return;
-  const float s = (float)K->inv_a0;
-  const long long N2 = (long long)n * n;
-  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < N2;
-       p += (long long)gridDim.x * blockDim.x) {
-    int i, j;
-    nk_rowcol(p, n, i, j);
-    w[p] = s * e[(long long)i * 2 * n + j];
   }
 }
 
@@ -430,10 +418,32 @@ __global__ void nk_consts_kernel(const double* part, int nblk, NKConsts* K, DevS
   pst->done = 0;
 }
 
+// a0 (s v) - beta J_F(u) (s v) at (i, jj) in FP32: the hand-written JVP of the variable
+// diffusion model (a + b u^2 faces averaged, - c u^3), Dirichlet ghosts on u and v
+__device__ __forceinline__ float vd_jvp_at(const float* __restrict__ y32, const float* __restrict__ vin,
+                                           float s, int i, int jj, int n, float a, float b, float c,
+                                           float a0, float beta, float idx2, float idy2) {
+  const long long p = (long long)i * n + jj;
+  const float uc = y32[p], ue = dval(y32, i, jj + 1, n), uw = dval(y32, i, jj - 1, n);
+  const float un = dval(y32, i + 1, jj, n), us = dval(y32, i - 1, jj, n);
+  const float vc = s * vin[p], ve = s * dval(vin, i, jj + 1, n), vw = s * dval(vin, i, jj - 1, n);
+  const float vn = s * dval(vin, i + 1, jj, n), vs = s * dval(vin, i - 1, jj, n);
+  const float Dc = a + b * uc * uc, De = a + b * ue * ue, Dw = a + b * uw * uw;
+  const float Dn = a + b * un * un, Ds = a + b * us * us;
+  const float dc = 2.f * b * uc * vc, de = 2.f * b * ue * ve, dw = 2.f * b * uw * vw;
+  const float dn = 2.f * b * un * vn, ds = 2.f * b * us * vs;
+  const float gx = 0.5f * (Dc + De) * (ve - vc) + 0.5f * (dc + de) * (ue - uc)
+                 - 0.5f * (Dw + Dc) * (vc - vw) - 0.5f * (dw + dc) * (uc - uw);
+  const float gy = 0.5f * (Dc + Dn) * (vn - vc) + 0.5f * (dc + dn) * (un - uc)
+                 - 0.5f * (Ds + Dc) * (vc - vs) - 0.5f * (ds + dc) * (uc - us);
+  return a0 * vc - beta * (gx * idx2 + gy * idy2 - 3.f * c * uc * uc * vc);
+}
+
 // JVP of the current Arnoldi vector V_j (j read on the device)
-// (gs == nullptr: t = J vin for the plain vector vin = V)
+// (gs == nullptr: t = J vin for the plain vector vin = V; with bsub, t = bsub - J vin)
 __global__ void vd_jvp_j_kernel(const float* y32, float* V, const GmresState* gs, float* t,
-                                const NKConsts* K, int n, float idx2, float idy2, long long N2) {
+                                const NKConsts* K, int n, float idx2, float idy2, long long N2,
+                                const float* bsub = nullptr) {
   if (gs && gs->converged) return;
   const int j = gs ? gs->j : 0;
   const float* vin = V + (long long)j * N2;
@@ -444,19 +454,8 @@ __global__ void vd_jvp_j_kernel(const float* y32, float* V, const GmresState* gs
        p += (long long)gridDim.x * blockDim.x) {
     int i, jj;
     nk_rowcol(p, n, i, jj);
-    const float uc = y32[p], ue = dval(y32, i, jj + 1, n), uw = dval(y32, i, jj - 1, n);
-    const float un = dval(y32, i + 1, jj, n), us = dval(y32, i - 1, jj, n);
-    const float vc = s * vin[p], ve = s * dval(vin, i, jj + 1, n), vw = s * dval(vin, i, jj - 1, n);
-    const float vn = s * dval(vin, i + 1, jj, n), vs = s * dval(vin, i - 1, jj, n);
-    const float Dc = a + b * uc * uc, De = a + b * ue * ue, Dw = a + b * uw * uw;
-    const float Dn = a + b * un * un, Ds = a + b * us * us;
-    const float dc = 2.f * b * uc * vc, de = 2.f * b * ue * ve, dw = 2.f * b * uw * vw;
-    const float dn = 2.f * b * un * vn, ds = 2.f * b * us * vs;
-    const float gx = 0.5f * (Dc + De) * (ve - vc) + 0.5f * (dc + de) * (ue - uc)
-                   - 0.5f * (Dw + Dc) * (vc - vw) - 0.5f * (dw + dc) * (uc - uw);
-    const float gy = 0.5f * (Dc + Dn) * (vn - vc) + 0.5f * (dc + dn) * (un - uc)
-                   - 0.5f * (Ds + Dc) * (vc - vs) - 0.5f * (ds + dc) * (uc - us);
-    t[p] = a0 * vc - beta * (gx * idx2 + gy * idy2 - 3.f * c * uc * uc * vc);
+    const float jv = vd_jvp_at(y32, vin, s, i, jj, n, a, b, c, a0, beta, idx2, idy2);
+    t[p] = bsub ? bsub[p] - jv : jv;
   }
 }
 
@@ -531,45 +530,6 @@ __global__ void nd_init_kernel(const double* part, int nblk, NewtonDev* nd, cuda
   cudaGraphSetConditional(hN, (!nd->converged && nd->max_newton > 0) ? 1u : 0u);
 }
 
-// iteration top: |R(x)|, converged evaluated before the update (249-254); GMRES from dx = 0
-__global__ void nd_head_kernel(const double* part, int nblk, NewtonDev* nd, cudaGraphConditionalHandle hG) {
-  const double s = nd_sum(part, nblk);
-  if (threadIdx.x != 0) return;
-  nd->rn = sqrt(s);
-  nd->converged = nd->rn < nd->newton_tol;
-  nd->cyc = 0;
-  cudaGraphSetConditional(hG, nd->max_krylov > 0 ? 1u : 0u);
-}
-
-// GMRES cycle start (gmres_init_kernel with the first-cycle flag read on the device) and
-// the Arnoldi loop flag
-__global__ void nd_gmres_init_kernel(const double* part, int nblk, GmresState* gs, const NewtonDev* nd,
-                                     cudaGraphConditionalHandle hA) {
-  const double s = nd_sum(part, nblk);
-  if (threadIdx.x != 0) return;
-  const double b0 = sqrt(s);
-  const int m = nd->restart;
-  if (nd->cyc == 0) gs->tol_abs = nd->krylov_tol * b0;
-  gs->beta0 = b0;
-  gs->j = 0;
-  gs->m = m;
-  gs->k_used = 0;
-  for (int i = 0; i <= m; ++i) gs->g[i] = 0.0;
-  gs->g[0] = b0;
-  gs->res_est = b0;
-  gs->hnext_inv = b0 > 0 ? 1.0 / b0 : 0.0;
-  gs->converged = (b0 <= gs->tol_abs || b0 == 0.0) ? 1 : 0;
-  cudaGraphSetConditional(hA, gs->converged ? 0u : 1u);
-}
-
-// GMRES cycle end: Krylov iterations, next cycle while not converged and cycles remain
-__global__ void nd_cycle_end_kernel(const GmresState* gs, NewtonDev* nd, cudaGraphConditionalHandle hG) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  nd->lits += gs->k_used;
-  nd->cyc += 1;
-  cudaGraphSetConditional(hG, (!gs->converged && nd->cyc < nd->max_krylov) ? 1u : 0u);
-}
-
 // line search start (270-276): alpha = damping, reference norm |R(x)|
 __global__ void nd_ls_begin_kernel(NewtonDev* nd, NKConsts* K, cudaGraphConditionalHandle hL) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
@@ -580,28 +540,515 @@ __global__ void nd_ls_begin_kernel(NewtonDev* nd, NKConsts* K, cudaGraphConditio
   cudaGraphSetConditional(hL, nd->max_backtrack > 0 ? 1u : 0u);
 }
 
-// one try (277-316): sufficient decrease accepts, otherwise alpha *= backtrack
-__global__ void nd_ls_ctl_kernel(const double* part, int nblk, NewtonDev* nd, NKConsts* K,
-                                 cudaGraphConditionalHandle hL) {
-  const double s = nd_sum(part, nblk);
+
+// --------------------------------------------------------------- fused Arnoldi step
+// One GMRES iteration on M^-1 A in six kernels (the separate sequence above takes eleven):
+//   JVP       t = A V_j / |V_j| (vd_jvp_j_kernel: elementwise, every SM busy);
+//   nka_fwd   the odd extension of t and the forward row transforms of the extension, two
+//             real rows per complex sequence, half spectra out;
+//   col pass  the Helmholtz inverse along the columns (launch_col, oddy);
+//   nka_inv   inverse row transforms and w = M^-1 A V_j on the n x n block (at a cycle
+//             start: V_0 = w and its |.|^2 partials, the last CTA starts the cycle);
+//   nka_dots  V_j normalised in place and the Gram-Schmidt partial dots <V_i, w> (i <= j),
+//             accumulated in float-float on the FP32 pipe; the last CTA sums them in a
+//             fixed order into H[:, j];
+//   nka_orth  V_{j+1} = w - sum_i H_ij V_i and |V_{j+1}|^2 partials; the last CTA applies
+//             the Givens rotations, back-substitutes when the cycle ends and sets the loop
+//             flag.
+// The row passes have one warp (2n = 1024) or 2n/16 threads per row pair of the extension,
+// i.e. few warps in all, so the stencil and the dot products, whose loads need many
+// warps in flight, stay in the elementwise kernels.  "Last CTA" is a ticket: every CTA
+// publishes its partials, fences and draws a ticket from a counter in the workspace; the
+// CTA that draws the final ticket reads all partials and resets the counter.  No CTA ever
+// waits for another.
+enum { NKA_STORE_W = 0, NKA_START = 1 };
+
+struct NkaArgs {
+  int n, log2L, ldc, nseq;
+  long long N2;
+  const float* src;     // operand of the preconditioner (n x n)
+  float* V;             // Krylov basis, m + 1 vectors of N2
+  float* t;             // w = M^-1 A V_j (Arnoldi)
+  cx<float>* spec;      // n rows of ldc half-spectrum points (the distinct rows of the extension)
+  const cx<float>* tw;  // twiddles of length 2n
+  GmresState* gs;
+  const NKConsts* K;
+  double* part;         // per-CTA partials
+  unsigned* ticket;     // zero between kernels
+  // cycle start: from nd (graph Newton loop) when set, else first / tol / m
+  const NewtonDev* nd;
+  int first, m;
+  double tol;
+  cudaGraphConditionalHandle h;
+  int use_handle;
+  int skip_converged;   // Arnoldi passes: return at entry once the cycle has converged
+};
+
+// true in the CTA that finished last (block-uniform); its reads of the other CTAs'
+// partials must bypass L1 (__ldcg)
+__device__ __forceinline__ bool nka_last(unsigned* ticket) {
+  __shared__ int last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+  __syncthreads();
+  return last != 0;
+}
+
+// sum of nb partials read through L2, the same order in every call (all threads of the CTA)
+__device__ __forceinline__ double nka_sum(const double* part, int nb) {
+  __shared__ double red[32];
+  double acc = 0.0;
+  for (int b = threadIdx.x; b < nb; b += blockDim.x) acc += __ldcg(&part[b]);
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  double s = 0.0;
+  for (int q = 0; q < (int)((blockDim.x + 31) >> 5); ++q) s += red[q];
+  return s;
+}
+
+// (hi, lo) += a b: the FMA two-product and Knuth's two-sum on the FP32 pipe (the dot-product
+// accumulation of Ogita, Rump and Oishi); hi + lo carries about twice the FP32 precision
+__device__ __forceinline__ void ff_dot_acc(float& hi, float& lo, float a, float b) {
+  const float p = __fmul_rn(a, b);
+  const float pe = __fmaf_rn(a, b, -p);
+  const float s = __fadd_rn(hi, p);
+  lo = __fadd_rn(lo, __fadd_rn(ff_2sum_err(hi, p, s), pe));
+  hi = s;
+}
+
+// cycle start from |V_0|^2 = s (as gmres_init_kernel; in the graph Newton loop the first-cycle
+// flag, tolerance and restart come from NewtonDev)
+__device__ void gmres_start(GmresState* gs, double s, int first, double tol, int m) {
+  const double b0 = sqrt(s);
+  if (first) gs->tol_abs = tol * b0;
+  gs->beta0 = b0;
+  gs->j = 0;
+  gs->m = m;
+  gs->k_used = 0;
+  for (int i = 0; i <= m; ++i) gs->g[i] = 0.0;
+  gs->g[0] = b0;
+  gs->res_est = b0;
+  gs->hnext_inv = b0 > 0 ? 1.0 / b0 : 0.0;
+  gs->converged = (b0 <= gs->tol_abs || b0 == 0.0) ? 1 : 0;
+}
+
+// back substitution R y = g over the k_used columns (as gmres_solve_kernel)
+__device__ void gmres_backsub(GmresState* gs) {
+  const int k = gs->k_used;
+  for (int i = k - 1; i >= 0; --i) {
+    double s = gs->g[i];
+    for (int q = i + 1; q < k; ++q) s -= gs->H[i * NK_MAXM + q] * gs->y[q];
+    const double d = gs->H[i * NK_MAXM + i];
+    gs->y[i] = d != 0.0 ? s / d : 0.0;
+  }
+}
+
+// Work after the inverse transform: this thread holds w at columns x0 + m xs (m < M,
+// x < n) of rows y and y + n/2.
+template <int MODE, int M>
+__device__ __forceinline__ void nka_finish(const NkaArgs& a, int y, int x0, int xs, const float (&wa)[M],
+                                           const float (&wb)[M]) {
+  const int n = a.n;
+  const long long ra = (long long)y * n, rb = (long long)(y + (n >> 1)) * n;
+  if (MODE == NKA_STORE_W) {
+#pragma unroll
+    for (int m = 0; m < M; ++m) {
+      const int x = x0 + m * xs;
+      if (x < n) { a.t[ra + x] = wa[m]; a.t[rb + x] = wb[m]; }
+    }
+    return;
+  }
+  // cycle start: V_0 = w, |V_0|^2
+  __shared__ double red[8];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = (blockDim.x + 31) >> 5;
+  double acc = 0.0;
+#pragma unroll
+  for (int m = 0; m < M; ++m) {
+    const int x = x0 + m * xs;
+    if (x < n) {
+      a.V[ra + x] = wa[m]; a.V[rb + x] = wb[m];
+      acc += (double)wa[m] * (double)wa[m];
+      acc += (double)wb[m] * (double)wb[m];
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if (lane == 0) red[warp] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int q = 0; q < nw; ++q) s += red[q];
+    a.part[blockIdx.x] = s;
+  }
+  if (nka_last(a.ticket)) {
+    const double s = nka_sum(a.part, gridDim.x);
+    if (threadIdx.x == 0) {
+      GmresState* gs = a.gs;
+      const NewtonDev* nd = a.nd;
+      if (nd) gmres_start(gs, s, nd->cyc == 0, nd->krylov_tol, nd->restart);
+      else gmres_start(gs, s, a.first, a.tol, a.m);
+      if (a.use_handle) cudaGraphSetConditional(a.h, gs->converged ? 0u : 1u);
+      *a.ticket = 0u;
+    }
+  }
+}
+
+// forward row transforms of the odd extension of src (shared-memory Stockham, 2n <= 4096)
+__global__ void __launch_bounds__(256) nka_fwd_kernel(const __grid_constant__ NkaArgs a) {
+  typedef cx<float> C;
+  if (a.skip_converged && a.gs->converged) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* buf = reinterpret_cast<C*>(smem_raw);
+  const int n = a.n, L = 2 * n, hn = n >> 1;
+  const int tps = L >= 16 ? L >> 4 : 1;
+  const int tid = threadIdx.x, s_loc = pdiv(tid, tps), lt = tid - s_loc * tps;
+  const bool active = s_loc < a.nseq;  // whole warps are launched
+  const int y = blockIdx.x * a.nseq + s_loc;
+  const int zb = s_loc * L;
+  const float* ra = a.src + (long long)y * n;
+  const float* rb = a.src + (long long)(y + hn) * n;
+#pragma unroll
+  for (int m = 0; m < 8; ++m) {
+    const int x = lt + m * tps;
+    if (active && x < n) {
+      const float ta = ra[x], tb = rb[x];
+      buf[sp(zb + x)] = mk<C>(ta, tb);
+      buf[sp(zb + L - 1 - x)] = mk<C>(-ta, -tb);
+    }
+  }
+  __syncthreads();
+  fft_smem<float, false, false>(buf, L, a.log2L, a.nseq, L, 1, a.tw, tid);
+  if (!active) return;
+  C* A = a.spec + (long long)y * a.ldc;
+  C* B = a.spec + (long long)(y + hn) * a.ldc;
+#pragma unroll
+  for (int m = 0; m < 9; ++m) {
+    const int kk = lt + m * tps;
+    if (kk > n) continue;
+    const C Zk = buf[sp(zb + kk)], Zm = buf[sp(zb + ((L - kk) & (L - 1)))];
+    A[kk] = mk<C>(0.5f * (Zk.x + Zm.x), 0.5f * (Zk.y - Zm.y));
+    B[kk] = mk<C>(0.5f * (Zk.y + Zm.y), 0.5f * (Zm.x - Zk.x));
+  }
+}
+
+// inverse row transforms and w (any 2n <= 4096)
+template <int MODE>
+__global__ void __launch_bounds__(256) nka_inv_kernel(const __grid_constant__ NkaArgs a) {
+  typedef cx<float> C;
+  if (a.skip_converged && a.gs->converged) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* buf = reinterpret_cast<C*>(smem_raw);
+  const int n = a.n, L = 2 * n, hn = n >> 1;
+  const int tps = L >= 16 ? L >> 4 : 1;
+  const int tid = threadIdx.x, s_loc = pdiv(tid, tps), lt = tid - s_loc * tps;
+  const bool active = s_loc < a.nseq;  // whole warps are launched
+  const int y = blockIdx.x * a.nseq + s_loc;
+  const int zb = s_loc * L;
+  const C* A = a.spec + (long long)y * a.ldc;
+  const C* B = a.spec + (long long)(y + hn) * a.ldc;
+  C Ak[9], Bk[9];
+#pragma unroll
+  for (int m = 0; m < 9; ++m) {
+    const int kk = lt + m * tps;
+    if (active && kk <= n) { Ak[m] = A[kk]; Bk[m] = B[kk]; }
+  }
+#pragma unroll
+  for (int m = 0; m < 9; ++m) {
+    const int kk = lt + m * tps;
+    if (active && kk <= n) {
+      buf[sp(zb + kk)] = mk<C>(Ak[m].x - Bk[m].y, Ak[m].y + Bk[m].x);
+      if (kk > 0 && kk < n) buf[sp(zb + L - kk)] = mk<C>(Ak[m].x + Bk[m].y, Bk[m].x - Ak[m].y);
+    }
+  }
+  __syncthreads();
+  fft_smem<float, true, false>(buf, L, a.log2L, a.nseq, L, 1, a.tw, tid);
+  const float sc = (float)a.K->inv_a0;
+  float wa[8], wb[8];
+#pragma unroll
+  for (int m = 0; m < 8; ++m) {
+    const int x = lt + m * tps;
+    wa[m] = wb[m] = 0.f;
+    if (active && x < n) {
+      const C v = buf[sp(zb + x)];
+      wa[m] = sc * v.x;
+      wb[m] = sc * v.y;
+    }
+  }
+  // idle threads (x0 = n) contribute nothing
+  nka_finish<MODE, 8>(a, active ? y : 0, active ? lt : n, tps, wa, wb);
+}
+
+// The same two passes for 2n = 1024, one warp per sequence (the transform of wfft.cuh)
+__global__ void __launch_bounds__(128) nka_fwd_w32_kernel(const __grid_constant__ NkaArgs a) {
+  typedef float2 C;
+  if (a.skip_converged && a.gs->converged) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int lane = threadIdx.x & 31, s_loc = threadIdx.x >> 5;
+  C* tile = reinterpret_cast<C*>(smem_raw) + s_loc * (32 * 33);
+  const int y = blockIdx.x * a.nseq + s_loc;
+  const float* ra = a.src + (long long)y * 512;
+  const float* rb = a.src + (long long)(y + 256) * 512;
+  C z[32];
+#pragma unroll
+  for (int j = 0; j < 16; ++j) z[j] = mk<C>(ra[lane + 32 * j], rb[lane + 32 * j]);
+  // element 1023 - x = (31 - lane) + 32 (31 - j) carries the negated value
+#pragma unroll
+  for (int j = 16; j < 32; ++j) {
+    const C v = shfl2(z[31 - j], 31 - lane);
+    z[j] = mk<C>(-v.x, -v.y);
+  }
+  wfft1024<false>(z, tile, a.tw, lane);
+  C* A = a.spec + (long long)y * a.ldc;
+  C* B = a.spec + (long long)(y + 256) * a.ldc;
+  const int src = (32 - lane) & 31;
+#pragma unroll
+  for (int k2 = 0; k2 <= 16; ++k2) {
+    C Zm = shfl2(z[k2 <= 15 ? 31 - k2 : 15], src);  // X_{1024-k} (lanes > 0)
+    if (lane == 0) Zm = z[(32 - k2) & 31];
+    const int k = lane + 32 * k2;
+    if (k2 == 16 && lane != 0) continue;
+    const C Zk = z[k2];
+    A[k] = mk<C>(0.5f * (Zk.x + Zm.x), 0.5f * (Zk.y - Zm.y));
+    B[k] = mk<C>(0.5f * (Zk.y + Zm.y), 0.5f * (Zm.x - Zk.x));
+  }
+}
+
+template <int MODE>
+__global__ void __launch_bounds__(128) nka_inv_w32_kernel(const __grid_constant__ NkaArgs a) {
+  typedef float2 C;
+  if (a.skip_converged && a.gs->converged) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int lane = threadIdx.x & 31, s_loc = threadIdx.x >> 5;
+  C* tile = reinterpret_cast<C*>(smem_raw) + s_loc * (32 * 33);
+  const int y = blockIdx.x * a.nseq + s_loc;
+  const C* A = a.spec + (long long)y * a.ldc;
+  const C* B = a.spec + (long long)(y + 256) * a.ldc;
+  const int src = (32 - lane) & 31;
+  C z[32], Ar[17], Br[17];
+#pragma unroll
+  for (int j = 0; j < 16; ++j) { Ar[j] = A[32 * j + lane]; Br[j] = B[32 * j + lane]; }
+  Ar[16] = lane == 0 ? A[512] : mk<C>(0.f, 0.f);
+  Br[16] = lane == 0 ? B[512] : mk<C>(0.f, 0.f);
+#pragma unroll
+  for (int j = 0; j < 16; ++j) z[j] = mk<C>(Ar[j].x - Br[j].y, Ar[j].y + Br[j].x);
+#pragma unroll
+  for (int j = 16; j < 32; ++j) {
+    C av = shfl2(Ar[31 - j], src), bv = shfl2(Br[31 - j], src);
+    if (lane == 0) { av = Ar[32 - j]; bv = Br[32 - j]; }
+    if (lane == 0 && j == 16) z[j] = mk<C>(av.x - bv.y, av.y + bv.x);
+    else z[j] = mk<C>(av.x + bv.y, bv.x - av.y);
+  }
+  wfft1024<true>(z, tile, a.tw, lane);
+  const float sc = (float)a.K->inv_a0;
+  float wa[16], wb[16];
+#pragma unroll
+  for (int j = 0; j < 16; ++j) { wa[j] = sc * z[j].x; wb[j] = sc * z[j].y; }
+  nka_finish<MODE, 16>(a, y, lane, 32, wa, wb);
+}
+
+// V_j /= |V_j| in place and the partial dots <V_i, w>, i = 0..j, in float-float per thread;
+// the last CTA sums them (FP64, fixed order) into H[i][j]
+__global__ void __launch_bounds__(256) nka_dots_kernel(const __grid_constant__ NkaArgs a) {
+  GmresState* gs = a.gs;
+  if (gs->converged) return;
+  const int jv = gs->j;
+  const long long N2 = a.N2;
+  const float sj = (float)gs->hnext_inv;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  __shared__ double red[NK_MAXM][8];
+  const long long p0 = blockIdx.x * (long long)blockDim.x + threadIdx.x, ps = (long long)gridDim.x * blockDim.x;
+  float* vj = a.V + (long long)jv * N2;
+  for (long long p = p0; p < N2; p += ps) vj[p] *= sj;  // as nk_scale_j_kernel
+  for (int i = 0; i <= jv; ++i) {
+    const float* vi = a.V + (long long)i * N2;
+    float hi = 0.f, lo = 0.f;
+    for (long long p = p0; p < N2; p += ps) ff_dot_acc(hi, lo, vi[p], a.t[p]);
+    double acc = (double)hi + (double)lo;
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) red[i][warp] = acc;
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i <= jv; i += blockDim.x) {
+    double s = 0.0;
+    for (int q = 0; q < nw; ++q) s += red[i][q];
+    a.part[(long long)i * gridDim.x + blockIdx.x] = s;
+  }
+  if (!nka_last(a.ticket)) return;
+  // H[i][j]: one warp per i, lanes strided over the CTAs (a fixed order)
+  for (int i = warp; i <= jv; i += nw) {
+    double s = 0.0;
+    for (int b = lane; b < (int)gridDim.x; b += 32) s += __ldcg(&a.part[(long long)i * gridDim.x + b]);
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (lane == 0) gs->H[i * NK_MAXM + jv] = s;
+  }
+  if (threadIdx.x == 0) *a.ticket = 0u;
+}
+
+// V_{j+1} = w - sum_i H_ij V_i (classical Gram-Schmidt), |V_{j+1}|^2; the last CTA runs the
+// Givens step of gmres_givens_kernel and, at the end of a cycle, the back substitution
+__global__ void __launch_bounds__(256) nka_orth_kernel(const __grid_constant__ NkaArgs a) {
+  GmresState* gs = a.gs;
+  if (gs->converged) {
+    if (a.use_handle && blockIdx.x == 0 && threadIdx.x == 0) cudaGraphSetConditional(a.h, 0u);
+    return;
+  }
+  const int jv = gs->j;
+  const long long N2 = a.N2;
+  float hc[NK_MAXM];
+  for (int i = 0; i <= jv; ++i) hc[i] = (float)gs->H[i * NK_MAXM + jv];
+  float* vn = a.V + (long long)(jv + 1) * N2;
+  double acc = 0.0;
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < N2;
+       p += (long long)gridDim.x * blockDim.x) {
+    float x = a.t[p];
+    for (int i = 0; i <= jv; ++i) x -= hc[i] * a.V[(long long)i * N2 + p];
+    vn[p] = x;
+    acc += (double)x * (double)x;
+  }
+  __shared__ double red[8];
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int q = 0; q < (int)(blockDim.x >> 5); ++q) s += red[q];
+    a.part[blockIdx.x] = s;
+  }
+  if (!nka_last(a.ticket)) return;
+  const double s = nka_sum(a.part, gridDim.x);
+  if (threadIdx.x != 0) return;
+  const double hn = sqrt(s);
+  double* H = gs->H;
+  H[(jv + 1) * NK_MAXM + jv] = hn;
+  for (int i = 0; i < jv; ++i) {
+    const double x = H[i * NK_MAXM + jv], y = H[(i + 1) * NK_MAXM + jv];
+    H[i * NK_MAXM + jv] = gs->cs[i] * x + gs->sn[i] * y;
+    H[(i + 1) * NK_MAXM + jv] = -gs->sn[i] * x + gs->cs[i] * y;
+  }
+  const double x = H[jv * NK_MAXM + jv], y = H[(jv + 1) * NK_MAXM + jv];
+  const double den = hypot(x, y);
+  const double c = den > 0 ? x / den : 1.0, sn = den > 0 ? y / den : 0.0;
+  gs->cs[jv] = c;
+  gs->sn[jv] = sn;
+  H[jv * NK_MAXM + jv] = den;
+  H[(jv + 1) * NK_MAXM + jv] = 0.0;
+  gs->g[jv + 1] = -sn * gs->g[jv];
+  gs->g[jv] = c * gs->g[jv];
+  gs->k_used = jv + 1;
+  gs->res_est = fabs(gs->g[jv + 1]);
+  const bool conv = gs->res_est <= gs->tol_abs || hn == 0.0;
+  gs->j = jv + 1;
+  gs->hnext_inv = hn > 0 ? 1.0 / hn : 0.0;
+  const bool more = !conv && gs->j < gs->m;
+  if (conv) gs->converged = 1;
+  if (!more) gmres_backsub(gs);
+  if (a.use_handle) cudaGraphSetConditional(a.h, more ? 1u : 0u);
+  *a.ticket = 0u;
+}
+
+// dx += sum_i y_i V_i; with nd, the cycle-end bookkeeping of the graph Newton loop in one
+// thread: Krylov iterations, the cycle count, the next cycle while not converged and cycles remain
+__global__ void nka_update_kernel(float* dx, const float* V, const GmresState* gs, long long N2, NewtonDev* nd,
+                                  cudaGraphConditionalHandle hG) {
+  const int k = gs->k_used;
+  if (nd != nullptr && blockIdx.x == 0 && threadIdx.x == 0) {
+    nd->lits += k;
+    nd->cyc += 1;
+    cudaGraphSetConditional(hG, (!gs->converged && nd->cyc < nd->max_krylov) ? 1u : 0u);
+  }
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < N2;
+       p += (long long)gridDim.x * blockDim.x) {
+    double x = dx[p];
+    for (int i = 0; i < k; ++i) x += gs->y[i] * (double)V[(long long)i * N2 + p];
+    dx[p] = (float)x;
+  }
+}
+
+// ---- fused kernels of the graph Newton loop: each does a grid-wide pass and, in its last
+// CTA (the ticket of nka_last), the one-thread decision that a separate control kernel made
+
+// Newton iteration head: R(x), -R in FP32, |R|^2 partials, dx = 0; the last CTA sets
+// |R|, converged (evaluated before the update, newton_krylov.py:249-254) and the cycle flag
+__global__ void nd_resid_head_kernel(const double* __restrict__ x, const double* __restrict__ cst,
+                                     double* __restrict__ R, float* __restrict__ b32, float* __restrict__ dx,
+                                     double* part, const NKConsts* __restrict__ K, int n, double idx2,
+                                     double idy2, NewtonDev* nd, unsigned* ticket,
+                                     cudaGraphConditionalHandle hG) {
+  const double a = K->pa, b = K->pb, c = K->pc, a0 = K->a0, beta = K->beta;
+  double acc = 0.0;
+  const long long N2 = (long long)n * n;
+  auto u = [&](int ii, int jj) { return dval(x, ii, jj, n); };
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < N2;
+       p += (long long)gridDim.x * blockDim.x) {
+    int i, j;
+    nk_rowcol(p, n, i, j);
+    const double r = vd_resid_at(u, i, j, cst[p], a, b, c, a0, beta, idx2, idy2);
+    R[p] = r;
+    b32[p] = (float)(-r);
+    dx[p] = 0.0f;
+    acc += r * r;
+  }
+  block_partial(acc, part);
+  if (!nka_last(ticket)) return;
+  const double s = nka_sum(part, gridDim.x);
+  if (threadIdx.x != 0) return;
+  nd->rn = sqrt(s);
+  nd->converged = nd->rn < nd->newton_tol;
+  nd->cyc = 0;
+  cudaGraphSetConditional(hG, nd->max_krylov > 0 ? 1u : 0u);
+  *ticket = 0u;
+}
+
+// One line-search try (newton_krylov.py:277-316): the trial point xt = x + alpha dx (built on
+// the fly at every stencil point), R(xt) and its partials; the last CTA accepts on
+// sufficient decrease or halves alpha, and sets the loop flag
+__global__ void nd_ls_try_kernel(const double* __restrict__ x, const float* __restrict__ dx,
+                                 double* __restrict__ xt, const double* __restrict__ cst, double* __restrict__ R,
+                                 float* __restrict__ b32, double* part, NKConsts* K, int n, double idx2,
+                                 double idy2, NewtonDev* nd, unsigned* ticket, cudaGraphConditionalHandle hL) {
+  const double a = K->pa, b = K->pb, c = K->pc, a0 = K->a0, beta = K->beta, al = K->alpha;
+  double acc = 0.0;
+  const long long N2 = (long long)n * n;
+  auto u = [&](int ii, int jj) {
+    const int i2 = ii < 0 ? 0 : (ii >= n ? n - 1 : ii);
+    const int j2 = jj < 0 ? 0 : (jj >= n ? n - 1 : jj);
+    const long long q = (long long)i2 * n + j2;
+    const double v = x[q] + al * (double)dx[q];
+    return ((ii < 0) != (ii >= n)) || ((jj < 0) != (jj >= n)) ? -v : v;
+  };
+  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < N2;
+       p += (long long)gridDim.x * blockDim.x) {
+    int i, j;
+    nk_rowcol(p, n, i, j);
+    xt[p] = x[p] + al * (double)dx[p];
+    const double r = vd_resid_at(u, i, j, cst[p], a, b, c, a0, beta, idx2, idy2);
+    R[p] = r;
+    b32[p] = (float)(-r);
+    acc += r * r;
+  }
+  block_partial(acc, part);
+  if (!nka_last(ticket)) return;
+  const double s = nka_sum(part, gridDim.x);
   if (threadIdx.x != 0) return;
   const double rnn = sqrt(s);
-  const double alpha = K->alpha;
   nd->bt += 1;
-  if (rnn < (1.0 - nd->min_decrease * alpha) * nd->rb) {
+  if (rnn < (1.0 - nd->min_decrease * al) * nd->rb) {
     nd->accepted = 1;
     nd->rb = rnn;
     cudaGraphSetConditional(hL, 0u);
   } else {
-    K->alpha = alpha * nd->backtrack;
+    K->alpha = al * nd->backtrack;
     cudaGraphSetConditional(hL, nd->bt < nd->max_backtrack ? 1u : 0u);
   }
+  *ticket = 0u;
 }
 
 // x <- the accepted trial point, or the full damped step when no try was accepted
-// (318-322); the FP32 copy for the next JVPs
-__global__ void nd_update_kernel(double* x, const double* xt, const float* dx, float* y32, const NewtonDev* nd,
-                                 long long N2) {
+// (318-322), and the FP32 copy; one thread closes the iteration (residual norm, count,
+// the Newton loop flag)
+__global__ void nd_update_tail_kernel(double* x, const double* xt, const float* dx, float* y32, NewtonDev* nd,
+                                      long long N2, cudaGraphConditionalHandle hN) {
   const bool acc = nd->accepted != 0;
   const double al = nd->damping;
   for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < N2;
@@ -610,24 +1057,30 @@ __global__ void nd_update_kernel(double* x, const double* xt, const float* dx, f
     x[p] = v;
     y32[p] = (float)v;
   }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    nd->res = nd->rb;
+    nd->it += 1;
+    cudaGraphSetConditional(hN, (nd->it < nd->max_newton && !nd->converged) ? 1u : 0u);
+  }
 }
 
-__global__ void nd_tail_kernel(NewtonDev* nd, cudaGraphConditionalHandle hN) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  nd->res = nd->rb;
-  nd->it += 1;
-  cudaGraphSetConditional(hN, (nd->it < nd->max_newton && !nd->converged) ? 1u : 0u);
+// the step constants as a kernel argument (no host staging, no stream synchronisation)
+__global__ void nk_put_consts_kernel(NKConsts* K, NKConsts h) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) *K = h;
 }
 
-__global__ void zero32_kernel(float* v, long long N2) {
-  for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < N2;
-       p += (long long)gridDim.x * blockDim.x)
-    v[p] = 0.0f;
+// Newton / GMRES counts and the converged flag of the solve just run, into a device slot
+__global__ void nd_stats_kernel(const NewtonDev* nd, int* slot) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    slot[0] = nd->it;
+    slot[1] = nd->lits;
+    slot[2] = nd->converged;
+  }
 }
 
 // --------------------------------------------------------------- host driver
 struct NKLayout {
-  size_t y0, y1, y2, y3, y4, cst, R, xt, xn, y32, b32, dx, t, e, V, spec, part, gs, K, pst, nd, total;
+  size_t y0, y1, y2, y3, y4, cst, R, xt, xn, y32, b32, dx, t, V, spec, part, gs, K, pst, nd, tick, ring, total;
   int nblk, m;
 };
 static inline size_t al(size_t b) { return (b + 255) & ~size_t(255); }
@@ -651,14 +1104,16 @@ static NKLayout nk_layout(int n, int m) {
   L.b32 = o; o += al(N2 * 4);
   L.dx = o; o += al(N2 * 4);
   L.t = o; o += al(N2 * 4);
-  L.e = o; o += al(4 * N2 * 4);
   L.V = o; o += al((size_t)(m + 1) * N2 * 4);
   L.spec = o; o += al((size_t)(2 * n) * spec_ldc(2 * n) * 8);
-  L.part = o; o += al((size_t)(m + 2) * L.nblk * 8);
+  // per-CTA partials: elementwise passes (nblk CTAs) and the fused row passes (up to n/2 CTAs)
+  L.part = o; o += al((size_t)(m + 2) * (size_t)(L.nblk > n / 2 ? L.nblk : n / 2) * 8);
   L.gs = o; o += al(sizeof(GmresState));
   L.K = o; o += al(sizeof(NKConsts));
   L.pst = o; o += al(sizeof(DevState));
   L.nd = o; o += al(256);  // NewtonDev
+  L.tick = o; o += al(sizeof(unsigned));  // last-CTA ticket of the fused Arnoldi passes
+  L.ring = o; o += al(3 * NK_RING * sizeof(int));  // per-step counts of the fixed-step driver
   L.total = o;
   return L;
 }
@@ -678,65 +1133,120 @@ struct NKRun {
 static double* P64(NKRun& r, size_t off) { return (double*)(r.ws + off); }
 static float* P32(NKRun& r, size_t off) { return (float*)(r.ws + off); }
 
-// w = M^-1 src (FP32): odd extension, periodic Helmholtz on (2n)^2, restriction
-static cudaError_t precond(NKRun& r, const float* src, float* w, const GmresState* gs) {
+// Arguments of the fused Arnoldi passes for this run (mode fields left zero)
+static NkaArgs nka_args(NKRun& r) {
+  NkaArgs a;
+  memset(&a, 0, sizeof(a));
   const int n = r.n;
-  oddext_kernel<<<r.grid * 4, 256, 0, r.s>>>(src, P32(r, r.L.e), n, gs);
-  cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) return e;
   const PlanView pv = plan_view(r.plan2, 2 * n, 2 * n, 4);
-  cx<float>* spec = (cx<float>*)(r.ws + r.L.spec);
-  RowArgs<float> ro;
-  memset(&ro, 0, sizeof(ro));
-  // the n distinct rows of the extension as n/2 pairs (i, i + n/2)
-  const int hn = n / 2;
-  ro.n = 2 * n; ro.log2n = ilog2_exact(2 * n); ro.ldc = spec_ldc(2 * n); ro.nrows = hn; ro.npairs = 1;
-  ro.nseq = row_nseq(2 * n, hn); ro.rstride = 2 * n; ro.rin_sel = -1; ro.rout_sel = -1;
-  ro.rin[0] = P32(r, r.L.e); ro.rout[0] = P32(r, r.L.e); ro.spec = spec; ro.tw = (const cx<float>*)pv.twx;
-  ro.inv_scale = 1.0f;
-  ro.pr[0].ra = 0; ro.pr[0].rb = (long long)hn * 2 * n; ro.pr[0].sa = 0; ro.pr[0].sb = (long long)hn * ro.ldc;
-  ro.pr[0].flags = ROW_STORE_SPEC;
-  // converged Arnoldi steps skip the pass through the state flag of the spectral kernels
-  ro.st = (const DevState*)(r.ws + r.L.pst);
-  if ((e = launch_row<float, RX_NONE>(ro, r.s)) != cudaSuccess) return e;
-  ColArgs<float> c;
-  memset(&c, 0, sizeof(c));
-  c.ny = 2 * n; c.log2ny = ilog2_exact(2 * n); c.ncols = n + 1; c.ldc = ro.ldc;
-  c.C = col_tile(2 * n, c.ncols, 1, 4); c.spec = spec; c.lamx = (const float*)pv.lamx;
-  c.lamy = (const float*)pv.lamy; c.tw = (const cx<float>*)pv.twy;
-  c.scale = (float)(1.0 / (4.0 * n * n)); c.st = ro.st; c.njobs = 1; c.oddy = 1;
-  c.job[0].nout = 1; c.job[0].mul = MUL_HELMHOLTZ; c.job[0].D = 1.0; c.job[0].hfac[0] = c.job[0].hfac[1] = 1.0;
-  c.job[0].pow[0] = c.job[0].pow[1] = 1;
-  if ((e = launch_col<float>(c, r.s)) != cudaSuccess) return e;
-  ro.pr[0].flags = ROW_LOAD_SPEC | ROW_STORE_REAL;
-  if ((e = launch_row<float, RX_NONE>(ro, r.s)) != cudaSuccess) return e;
-  restrict_kernel<<<r.grid, 256, 0, r.s>>>(P32(r, r.L.e), w, n, (const NKConsts*)(r.ws + r.L.K), gs);
+  a.n = n; a.log2L = ilog2_exact(2 * n); a.ldc = spec_ldc(2 * n);
+  a.N2 = (long long)n * n;
+  a.V = P32(r, r.L.V); a.t = P32(r, r.L.t); a.src = a.t;
+  a.spec = (cx<float>*)(r.ws + r.L.spec); a.tw = (const cx<float>*)pv.twx;
+  a.gs = (GmresState*)(r.ws + r.L.gs); a.K = (const NKConsts*)(r.ws + r.L.K);
+  a.part = P64(r, r.L.part); a.ticket = (unsigned*)(r.ws + r.L.tick);
+  return a;
+}
+
+// CTA geometry of the fused row passes over the n/2 row pairs of the extension: one warp
+// per pair when 2n = 1024, else the shared-memory Stockham with 2n/16 threads per pair;
+// fewer pairs per CTA until the pass covers every SM; whole warps (the reductions shuffle
+// over full warps), the threads past nseq * tps idle
+struct NkaGeom { bool w32; int nseq, ctas, threads; size_t smem; };
+static NkaGeom nka_geom(int n) {
+  NkaGeom g;
+  const int L = 2 * n, hn = n / 2;
+  g.w32 = L == 1024;
+  int ns = g.w32 ? 4 : row_nseq(L, hn);
+  if (ns > hn) ns = hn;
+  while (ns > 1 && hn / ns < 152) ns >>= 1;
+  g.nseq = ns;
+  g.ctas = hn / ns;
+  const int tps = L >= 16 ? L / 16 : 1;
+  g.threads = g.w32 ? 32 * ns : ((ns * tps + 31) / 32) * 32;
+  g.smem = g.w32 ? (size_t)ns * 32 * 33 * sizeof(float2) : (size_t)sp_size(ns * L) * sizeof(float2);
+  return g;
+}
+
+static cudaError_t nka_fwd(NKRun& r, const NkaArgs& a0) {
+  NkaArgs a = a0;
+  const NkaGeom g = nka_geom(r.n);
+  a.nseq = g.nseq;
+  if (g.w32) nka_fwd_w32_kernel<<<g.ctas, g.threads, g.smem, r.s>>>(a);
+  else nka_fwd_kernel<<<g.ctas, g.threads, g.smem, r.s>>>(a);
   return cudaGetLastError();
 }
 
+template <int MODE>
+static cudaError_t nka_inv(NKRun& r, const NkaArgs& a0) {
+  NkaArgs a = a0;
+  const NkaGeom g = nka_geom(r.n);
+  a.nseq = g.nseq;
+  if (g.w32) nka_inv_w32_kernel<MODE><<<g.ctas, g.threads, g.smem, r.s>>>(a);
+  else nka_inv_kernel<MODE><<<g.ctas, g.threads, g.smem, r.s>>>(a);
+  return cudaGetLastError();
+}
+
+// the column pass of the preconditioner: M^-1 = (1/a0) (I - (beta Dbar/a0) Lap_D)^-1 along y
+// on the odd extension (rows 2n - 1 - ky synthesised as the negated mirror), Helmholtz step
+// from the state word written by nk_consts_kernel
+static cudaError_t nka_col(NKRun& r) {
+  const int n = r.n;
+  const PlanView pv = plan_view(r.plan2, 2 * n, 2 * n, 4);
+  ColArgs<float> c;
+  memset(&c, 0, sizeof(c));
+  c.ny = 2 * n; c.log2ny = ilog2_exact(2 * n); c.ncols = n + 1; c.ldc = spec_ldc(2 * n);
+  c.C = col_tile(2 * n, c.ncols, 1, 4); c.spec = (cx<float>*)(r.ws + r.L.spec); c.lamx = (const float*)pv.lamx;
+  c.lamy = (const float*)pv.lamy; c.tw = (const cx<float>*)pv.twy;
+  c.scale = (float)(1.0 / (4.0 * n * n)); c.st = (const DevState*)(r.ws + r.L.pst); c.njobs = 1; c.oddy = 1;
+  c.job[0].nout = 1; c.job[0].mul = MUL_HELMHOLTZ; c.job[0].D = 1.0; c.job[0].hfac[0] = c.job[0].hfac[1] = 1.0;
+  c.job[0].pow[0] = c.job[0].pow[1] = 1;
+  return launch_col<float>(c, r.s);
+}
+
+// w = M^-1 a.src: forward row transforms of the odd extension, the column pass, the inverse
+// row transforms (MODE: w into t, or the cycle start V_0 = w)
+template <int MODE>
+static cudaError_t nka_precond(NKRun& r, const NkaArgs& a) {
+  cudaError_t e = nka_fwd(r, a);
+  if (e == cudaSuccess) e = nka_col(r);
+  if (e == cudaSuccess) e = nka_inv<MODE>(r, a);
+  return e;
+}
+
+// The cycle start: V_0 = M^-1 (b - A dx) (first: M^-1 b), |V_0|, the GMRES header and, with a
+// handle, the Arnoldi loop flag
+static cudaError_t cycle_start(NKRun& r, NkaArgs a, bool first_plain) {
+  const long long N2 = (long long)r.n * r.n;
+  if (!first_plain) {
+    vd_jvp_j_kernel<<<r.grid, 256, 0, r.s>>>(P32(r, r.L.y32), P32(r, r.L.dx), nullptr, P32(r, r.L.t),
+                                             (const NKConsts*)(r.ws + r.L.K), r.n, (float)(1.0 / (r.dx * r.dx)),
+                                             (float)(1.0 / (r.dy * r.dy)), N2, P32(r, r.L.b32));
+    const cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    a.src = P32(r, r.L.t);
+  } else {
+    a.src = P32(r, r.L.b32);
+  }
+  a.skip_converged = 0;
+  return nka_precond<NKA_START>(r, a);
+}
+
+// One Arnoldi step: t = A V_j/|V_j|, w = M^-1 t, V_j normalised and H[:, j], V_{j+1}, the
+// Givens step and the loop flag, in six kernels (the index j lives on the device)
 static cudaError_t arnoldi_step(NKRun& r, cudaGraphConditionalHandle h, int use_handle) {
   const long long N2 = (long long)r.n * r.n;
-  GmresState* gs = (GmresState*)(r.ws + r.L.gs);
-  NKConsts* K = (NKConsts*)(r.ws + r.L.K);
-  double* part = P64(r, r.L.part);
-  // V_j arrives unnormalised: the JVP applies 1/|V_j| on the fly, then V_j is normalised in place
-  // (the index j lives on the device, so the kernels get V and read j themselves)
-  float* V = P32(r, r.L.V);
-  float* t = P32(r, r.L.t);
-  cudaError_t e;
-  vd_jvp_j_kernel<<<r.grid, 256, 0, r.s>>>(P32(r, r.L.y32), V, gs, t, K, r.n,
-                                           (float)(1.0 / (r.dx * r.dx)), (float)(1.0 / (r.dy * r.dy)), N2);
-  if ((e = cudaGetLastError()) != cudaSuccess) return e;
-  nk_scale_j_kernel<<<r.grid, 256, 0, r.s>>>(V, gs, N2);
-  if ((e = cudaGetLastError()) != cudaSuccess) return e;
-  if ((e = precond(r, t, t, gs)) != cudaSuccess) return e;
-  gmres_dots_kernel<<<r.L.nblk, 256, 0, r.s>>>(V, t, gs, part, N2);
-  if ((e = cudaGetLastError()) != cudaSuccess) return e;
-  gmres_hcol_kernel<<<1, 256, 0, r.s>>>(part, r.L.nblk, gs);
-  if ((e = cudaGetLastError()) != cudaSuccess) return e;
-  gmres_orth_kernel<<<r.L.nblk, 256, 0, r.s>>>(V, t, gs, part, N2);
-  if ((e = cudaGetLastError()) != cudaSuccess) return e;
-  gmres_givens_kernel<<<1, 256, 0, r.s>>>(part, r.L.nblk, gs, h, use_handle);
+  NkaArgs a = nka_args(r);
+  a.h = h;
+  a.use_handle = use_handle;
+  a.skip_converged = 1;
+  vd_jvp_j_kernel<<<r.grid, 256, 0, r.s>>>(P32(r, r.L.y32), a.V, a.gs, a.t, a.K, r.n, (float)(1.0 / (r.dx * r.dx)),
+                                           (float)(1.0 / (r.dy * r.dy)), N2);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  if ((e = nka_precond<NKA_STORE_W>(r, a)) != cudaSuccess) return e;
+  nka_dots_kernel<<<r.L.nblk, 256, 0, r.s>>>(a);
+  nka_orth_kernel<<<r.L.nblk, 256, 0, r.s>>>(a);
   return cudaGetLastError();
 }
 
@@ -821,14 +1331,13 @@ static cudaError_t build_newton_graph(NKRun& r, const NKParamsC& P) {
   float* y32 = P32(r, r.L.y32);
   float* dx = P32(r, r.L.dx);
   float* V = P32(r, r.L.V);
-  float* t = P32(r, r.L.t);
   float* b32 = P32(r, r.L.b32);
   double* part = P64(r, r.L.part);
   double* R = P64(r, r.L.R);
   double* cst = P64(r, r.L.cst);
+  unsigned* tick = (unsigned*)(r.ws + r.L.tick);
   const int nblk = r.L.nblk, grid = r.grid, n = r.n;
   const double idx2 = 1.0 / (r.dx * r.dx), idy2 = 1.0 / (r.dy * r.dy);
-  const float fidx2 = (float)idx2, fidy2 = (float)idy2;
   cudaStream_t cs = nullptr;
   cudaGraph_t top = nullptr;
   do {
@@ -859,17 +1368,11 @@ static cudaError_t build_newton_graph(NKRun& r, const NKParamsC& P) {
       if ((ce = cudaGraphAddNode(&node, top, d.data(), nullptr, d.size(), &np)) != cudaSuccess) break;
       bN = np.conditional.phGraph_out[0];
     }
-    // Newton body: R(x) and its norm, dx = 0
+    // Newton body: R(x) and its norm, dx = 0, and the GMRES cycle loop flag
     std::vector<cudaGraphNode_t> dn;
-    if ((ce = capture_seg(cs, bN, dn, [&](cudaStream_t q) {
-           vd_residual_kernel<<<nblk, 256, 0, q>>>(x, cst, R, b32, part, K, n, idx2, idy2);
-           zero32_kernel<<<grid, 256, 0, q>>>(dx, N2);
-           return cudaGetLastError();
-         })) != cudaSuccess) break;
-    // the GMRES cycle loop (its flag set by the head kernel)
     if ((ce = cudaGraphConditionalHandleCreate(&hG, bN, 0, 0)) != cudaSuccess) break;
     if ((ce = capture_seg(cs, bN, dn, [&](cudaStream_t q) {
-           nd_head_kernel<<<1, 256, 0, q>>>(part, nblk, nd, hG);
+           nd_resid_head_kernel<<<nblk, 256, 0, q>>>(x, cst, R, b32, dx, part, K, n, idx2, idy2, nd, tick, hG);
            return cudaGetLastError();
          })) != cudaSuccess) break;
     {
@@ -886,13 +1389,12 @@ static cudaError_t build_newton_graph(NKRun& r, const NKParamsC& P) {
     std::vector<cudaGraphNode_t> dg;
     if ((ce = cudaGraphConditionalHandleCreate(&hA, bG, 0, 0)) != cudaSuccess) break;
     if ((ce = capture_seg(cs, bG, dg, [&](cudaStream_t q) {
-           vd_jvp_j_kernel<<<grid, 256, 0, q>>>(y32, dx, nullptr, t, K, n, fidx2, fidy2, N2);
-           sub_kernel<<<grid, 256, 0, q>>>(b32, t, t, N2);
-           cudaError_t e = precond(rc, t, V, nullptr);
-           if (e != cudaSuccess) return e;
-           sumsq32_kernel<<<nblk, 256, 0, q>>>(V, part, N2);
-           nd_gmres_init_kernel<<<1, 256, 0, q>>>(part, nblk, gs, nd, hA);
-           return cudaGetLastError();
+           // V_0 = M^-1 (b - A dx), |V_0|, the cycle start and the Arnoldi loop flag
+           NkaArgs a = nka_args(rc);
+           a.nd = nd;
+           a.h = hA;
+           a.use_handle = 1;
+           return cycle_start(rc, a, false);
          })) != cudaSuccess) break;
     {
       cudaGraphNodeParams np = {cudaGraphNodeTypeConditional};
@@ -907,9 +1409,8 @@ static cudaError_t build_newton_graph(NKRun& r, const NKParamsC& P) {
     std::vector<cudaGraphNode_t> da;
     if ((ce = capture_seg(cs, bA, da, [&](cudaStream_t) { return arnoldi_step(rc, hA, 1); })) != cudaSuccess) break;
     if ((ce = capture_seg(cs, bG, dg, [&](cudaStream_t q) {
-           gmres_solve_kernel<<<1, 1, 0, q>>>(gs);
-           gmres_update_kernel<<<grid, 256, 0, q>>>(dx, V, gs, N2);
-           nd_cycle_end_kernel<<<1, 32, 0, q>>>(gs, nd, hG);
+           // y was back-substituted by the last Arnoldi step of the cycle
+           nka_update_kernel<<<grid, 256, 0, q>>>(dx, V, gs, N2, nd, hG);
            return cudaGetLastError();
          })) != cudaSuccess) break;
     // line search
@@ -930,15 +1431,12 @@ static cudaError_t build_newton_graph(NKRun& r, const NKParamsC& P) {
     }
     std::vector<cudaGraphNode_t> dl;
     if ((ce = capture_seg(cs, bL, dl, [&](cudaStream_t q) {
-           trial_kernel<<<grid, 256, 0, q>>>(x, dx, xt, K, nullptr, N2);
-           vd_residual_kernel<<<nblk, 256, 0, q>>>(xt, cst, R, b32, part, K, n, idx2, idy2);
-           nd_ls_ctl_kernel<<<1, 256, 0, q>>>(part, nblk, nd, K, hL);
+           nd_ls_try_kernel<<<nblk, 256, 0, q>>>(x, dx, xt, cst, R, b32, part, K, n, idx2, idy2, nd, tick, hL);
            return cudaGetLastError();
          })) != cudaSuccess) break;
     // the step and the loop flag
     if ((ce = capture_seg(cs, bN, dn, [&](cudaStream_t q) {
-           nd_update_kernel<<<grid, 256, 0, q>>>(x, xt, dx, y32, nd, N2);
-           nd_tail_kernel<<<1, 32, 0, q>>>(nd, hN);
+           nd_update_tail_kernel<<<grid, 256, 0, q>>>(x, xt, dx, y32, nd, N2, hN);
            return cudaGetLastError();
          })) != cudaSuccess) break;
     ce = cudaGraphInstantiate(&r.newton, top, 0);
@@ -966,6 +1464,18 @@ static cudaError_t newton_dev(NKRun& r, double* x, int* n_newton, int* n_lin, in
   if (e != cudaSuccess) return e;
   *n_newton = h.it; *n_lin = h.lits; *conv_out = h.converged; *res_out = h.res;
   return cudaSuccess;
+}
+
+// The same without the read-back: the counts go to a device slot (fixed-step driver)
+static cudaError_t newton_dev_async(NKRun& r, double* x, int* slot) {
+  const long long N2 = (long long)r.n * r.n;
+  double* xn = P64(r, r.L.xn);
+  cudaError_t e = cudaMemcpyAsync(xn, x, sizeof(double) * N2, cudaMemcpyDeviceToDevice, r.s);
+  if (e == cudaSuccess) e = cudaGraphLaunch(r.newton, r.s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(x, xn, sizeof(double) * N2, cudaMemcpyDeviceToDevice, r.s);
+  if (e != cudaSuccess) return e;
+  nd_stats_kernel<<<1, 32, 0, r.s>>>((const NewtonDev*)(r.ws + r.L.nd), slot);
+  return cudaGetLastError();
 }
 
 static cudaError_t norm_of(NKRun& r, double* part_dev, double* host_out) {
@@ -1001,10 +1511,7 @@ static cudaError_t newton(NKRun& r, double* x, const NKParamsC& P, int* n_newton
   float* y32 = P32(r, r.L.y32);
   float* dx = P32(r, r.L.dx);
   float* V = P32(r, r.L.V);
-  float* t = P32(r, r.L.t);
-  double* part = P64(r, r.L.part);
   double* xt = P64(r, r.L.xt);
-  const float idx2 = (float)(1.0 / (r.dx * r.dx)), idy2 = (float)(1.0 / (r.dy * r.dy));
   cudaError_t e;
   double rn;
   lincomb_kernel<<<r.grid, 256, 0, r.s>>>(x, 1.0, nullptr, 0.0, x, y32, N2);
@@ -1022,19 +1529,27 @@ static cudaError_t newton(NKRun& r, double* x, const NKParamsC& P, int* n_newton
     // restarted GMRES on M^-1 J dx = -M^-1 R
     if ((e = cudaMemsetAsync(dx, 0, sizeof(float) * N2, r.s)) != cudaSuccess) return e;
     for (int cyc = 0; cyc < P.max_krylov; ++cyc) {
-      const float* src = P32(r, r.L.b32);
-      if (cyc > 0) {  // r = b - J dx
-        vd_jvp_j_kernel<<<r.grid, 256, 0, r.s>>>(y32, dx, nullptr, t, K, r.n, idx2, idy2, N2);
-        sub_kernel<<<r.grid, 256, 0, r.s>>>(P32(r, r.L.b32), t, t, N2);
-        src = t;
+      // V_0 = M^-1 b (first cycle) or M^-1 (b - J dx), |V_0| and the cycle start
+      NkaArgs a = nka_args(r);
+      a.first = cyc == 0;
+      a.tol = P.krylov_tol;
+      a.m = P.restart;
+      if ((e = cycle_start(r, a, cyc == 0)) != cudaSuccess) return e;
+      if (host_loop_mode()) {
+        // MJX_HOST_LOOP=1: the host launches every Arnoldi step and reads the GMRES header
+        // after it (the same kernels and decisions; profilers then see each launch)
+        for (int k = 0; k < P.restart; ++k) {
+          int g4[4];
+          if ((e = cudaMemcpyAsync(g4, gs, sizeof(g4), cudaMemcpyDeviceToHost, r.s)) != cudaSuccess) return e;
+          if ((e = cudaStreamSynchronize(r.s)) != cudaSuccess) return e;
+          if (g4[2] || g4[0] >= g4[1]) break;  // converged, or j == m
+          if ((e = arnoldi_step(r, 0, 0)) != cudaSuccess) return e;
+        }
+      } else if ((e = cudaGraphLaunch(r.arnoldi, r.s)) != cudaSuccess) {
+        return e;
       }
-      if ((e = precond(r, src, V, nullptr)) != cudaSuccess) return e;
-      sumsq32_kernel<<<r.L.nblk, 256, 0, r.s>>>(V, part, N2);
-      gmres_init_kernel<<<1, 256, 0, r.s>>>(part, r.L.nblk, gs, cyc == 0, P.krylov_tol, P.restart);
-      if ((e = cudaGetLastError()) != cudaSuccess) return e;
-      if ((e = cudaGraphLaunch(r.arnoldi, r.s)) != cudaSuccess) return e;
-      gmres_solve_kernel<<<1, 1, 0, r.s>>>(gs);
-      gmres_update_kernel<<<r.grid, 256, 0, r.s>>>(dx, V, gs, N2);
+      // the last Arnoldi step of the cycle back-substituted y
+      nka_update_kernel<<<r.grid, 256, 0, r.s>>>(dx, V, gs, N2, nullptr, 0);
       if ((e = cudaGetLastError()) != cudaSuccess) return e;
       int hdr[4];
       if ((e = cudaMemcpyAsync(hdr, gs, sizeof(hdr), cudaMemcpyDeviceToHost, r.s)) != cudaSuccess) return e;
@@ -1082,9 +1597,11 @@ static cudaError_t newton(NKRun& r, double* x, const NKParamsC& P, int* n_newton
 // yc = y_n, yp = y_{n-1} (BDF2 only); the solution is written to yout.
 struct StepOut { int newton, lin, converged; double res; };
 
+// With dev_slot (device Newton loop only) the step enqueues its work and leaves the counts
+// in dev_slot without a host synchronisation; so is left untouched.
 static cudaError_t implicit_step(NKRun& r, const NKParamsC& P, const double* abc, int method,
                                  double dt, double dt_prev, int guess_previous, const double* yc,
-                                 const double* yp, double* yout, StepOut* so) {
+                                 const double* yp, double* yout, StepOut* so, int* dev_slot = nullptr) {
   const long long N2 = (long long)r.n * r.n;
   NKConsts* K = (NKConsts*)(r.ws + r.L.K);
   DevState* pst = (DevState*)(r.ws + r.L.pst);
@@ -1104,7 +1621,8 @@ static cudaError_t implicit_step(NKRun& r, const NKParamsC& P, const double* abc
     h.a0 = 1.0; h.beta = 0.5 * dt;
   }
   h.alpha = 1.0;
-  cudaError_t e = cudaMemcpyAsync(K, &h, sizeof(h), cudaMemcpyHostToDevice, r.s);
+  nk_put_consts_kernel<<<1, 32, 0, r.s>>>(K, h);
+  cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   if (method == MJX_METHOD_CN) {
     // R(y_n) with cst = 0 is y_n - dt/2 F(y_n); cst = -y_n - dt/2 F(y_n) = R(y_n) - 2 y_n
@@ -1127,14 +1645,15 @@ static cudaError_t implicit_step(NKRun& r, const NKParamsC& P, const double* abc
     // the residual kernel with a0 = 0, beta = -dt, cst = y_n gives y_n + dt F(y_n)
     NKConsts ge = h;
     ge.a0 = 0.0; ge.beta = -dt;
-    if ((e = cudaMemcpyAsync(K, &ge, sizeof(ge), cudaMemcpyHostToDevice, r.s)) != cudaSuccess) return e;
+    nk_put_consts_kernel<<<1, 32, 0, r.s>>>(K, ge);
     vd_residual_kernel<<<r.L.nblk, 256, 0, r.s>>>(yc, yc, yout, nullptr, P64(r, r.L.part), K, r.n, idx2, idy2);
-    if ((e = cudaMemcpyAsync(K, &h, sizeof(h), cudaMemcpyHostToDevice, r.s)) != cudaSuccess) return e;
+    nk_put_consts_kernel<<<1, 32, 0, r.s>>>(K, h);
   }
   // preconditioner constants from y_n
   sumsq_kernel<<<r.L.nblk, 256, 0, r.s>>>(yc, P64(r, r.L.part), N2);
   nk_consts_kernel<<<1, 256, 0, r.s>>>(P64(r, r.L.part), r.L.nblk, K, pst, (double)N2);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  if (r.newton != nullptr && dev_slot != nullptr) return newton_dev_async(r, yout, dev_slot);
   if (r.newton != nullptr) return newton_dev(r, yout, &so->newton, &so->lin, &so->converged, &so->res);
   return newton(r, yout, P, &so->newton, &so->lin, &so->converged, &so->res);
 }
@@ -1164,6 +1683,7 @@ static mjx_status nk_setup(NKRun& r, const void* plan2, int n, double dy, double
   if (ws == nullptr || ws_bytes < r.L.total) return MJX_WORKSPACE;
   MJX_TRY(ensure_kernel_attrs());
   MJX_CUDA_TRY(cudaMemsetAsync(r.ws + r.L.pst, 0, sizeof(DevState), r.s));
+  MJX_CUDA_TRY(cudaMemsetAsync(r.ws + r.L.tick, 0, sizeof(unsigned), r.s));
   P->max_newton = nkp->max_newton_iters; P->max_krylov = nkp->max_krylov_iters; P->restart = nkp->restart;
   P->max_backtrack = nkp->max_backtrack; P->newton_tol = nkp->newton_tol; P->krylov_tol = nkp->krylov_tol;
   P->damping = nkp->damping; P->backtrack = nkp->backtrack_factor; P->min_decrease = nkp->min_residual_decrease;
@@ -1204,13 +1724,24 @@ mjx_status mjx_nk_vardiff_integrate2d(const void* plan2, int n, double dy, doubl
   cudaError_t e = cudaMemcpyAsync(yc, y0, sizeof(double) * N2, cudaMemcpyDeviceToDevice, r.s);
   if (e == cudaSuccess) e = cudaMemcpyAsync(yp, y0, sizeof(double) * N2, cudaMemcpyDeviceToDevice, r.s);
   if (e != cudaSuccess) { set_last_error(e, __FILE__, __LINE__); rc = MJX_CUDA_ERROR; }
-  // integrate_fixed_dt (stepping.py:1028-1139): BDF2 takes a BE first step
+  // integrate_fixed_dt (stepping.py:1028-1139): BDF2 takes a BE first step.  With the
+  // device Newton loop no step reads anything back: the counts collect in a device ring
+  // that the host reads every NK_RING steps.
+  int* ring = (int*)(r.ws + r.L.ring);
   for (int step = 0; step < n_steps && rc == MJX_OK; ++step) {
     const int m = (method == MJX_METHOD_BDF2 && step == 0) ? MJX_METHOD_BE : method;
     StepOut so;
-    e = implicit_step(r, P, model_abc, m, dt, dt, be_guess_previous, yc, yp, yn, &so);
+    int* slot = r.newton != nullptr ? ring + 3 * (step % NK_RING) : nullptr;
+    e = implicit_step(r, P, model_abc, m, dt, dt, be_guess_previous, yc, yp, yn, &so, slot);
+    if (e == cudaSuccess && slot != nullptr && (step % NK_RING == NK_RING - 1 || step == n_steps - 1)) {
+      const int first = step - step % NK_RING, cnt = step - first + 1;
+      if (stats) e = cudaMemcpyAsync(stats + 3 * first, ring, sizeof(int) * 3 * cnt, cudaMemcpyDeviceToHost, r.s);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(r.s);
+    }
     if (e != cudaSuccess) { set_last_error(e, __FILE__, __LINE__); rc = MJX_CUDA_ERROR; break; }
-    if (stats) { stats[3 * step] = so.newton; stats[3 * step + 1] = so.lin; stats[3 * step + 2] = so.converged; }
+    if (stats && slot == nullptr) {
+      stats[3 * step] = so.newton; stats[3 * step + 1] = so.lin; stats[3 * step + 2] = so.converged;
+    }
     // rotate y_{n-1} <- y_n <- y_{n+1}
     double* tmp = yp; yp = yc; yc = yn; yn = tmp;
   }

@@ -11,6 +11,7 @@
 
 #include "spectral.cuh"
 #include "tma.cuh"
+#include "wfft.cuh"
 
 namespace mjx {
 
@@ -18,9 +19,15 @@ static inline size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 
 int spec_ldc(int nx) { return ((nx / 2 + 1) + 3) & ~3; }
 
+// Entries of the x twiddle table: FP32 plans of 1024-point rows append the same 1024 values
+// transposed for the one-warp transform (entry 1024 + 32 k1 + l holds w^(l k1)), so that
+// the 32 lanes of a warp read one contiguous 256-byte run per twiddle instead of 32 rows
+// of the table.
+static int twx_count(int nx, int elem) { return (nx == 1024 && elem == 4) ? 2048 : nx; }
+
 size_t plan_bytes(int ny, int nx, int elem) {
   const size_t c = 2 * (size_t)elem;
-  return align256(nx * c) + align256(ny * c) + align256(spec_ldc(nx) * (size_t)elem) +
+  return align256(twx_count(nx, elem) * c) + align256(ny * c) + align256(spec_ldc(nx) * (size_t)elem) +
          align256(ny * (size_t)elem);
 }
 
@@ -28,7 +35,7 @@ PlanView plan_view(const void* plan, int ny, int nx, int elem) {
   const size_t c = 2 * (size_t)elem;
   const char* p = (const char*)plan;
   PlanView v;
-  v.twx = p; p += align256(nx * c);
+  v.twx = p; p += align256(twx_count(nx, elem) * c);
   v.twy = p; p += align256(ny * c);
   v.lamx = p; p += align256(spec_ldc(nx) * (size_t)elem);
   v.lamy = p;
@@ -399,68 +406,6 @@ __global__ void __launch_bounds__(ColThreads<T>::v, 1) col_kernel(const __grid_c
 }
 
 // ------------------------------------------------------------------ warp row pass (n = 1024)
-// A 1024-point row transform held by one warp: lane l keeps the 32 elements l + 32 j in
-// registers.  Four-step split 1024 = 32 x 32: a 32-point DFT per lane over j, the twiddles
-// w^(l k1) (the row table, w = exp(-2 pi i/1024)), one transpose through a 32 x 33 shared
-// tile of the warp (only __syncwarp, no block barrier), and a second 32-point DFT per lane;
-// element k1 + 32 k2 of the result ends in register k2 of lane k1, which is again the
-// layout "lane = index mod 32", so the inverse transform's output feeds the pointwise work
-// and the forward transform without any reordering.  The two-for-one packing of two real
-// rows pairs index k with 1024 - k, which lives in lane (32 - l) mod 32: one shuffle each.
-
-// cos / sin of 2 pi k / 32, k = 0..15
-__constant__ const float kW32C[16] = {1.0f, 0.98078528040323044913f, 0.92387953251128675613f,
-                                      0.83146961230254523708f, 0.70710678118654752440f, 0.55557023301960222474f,
-                                      0.38268343236508977173f, 0.19509032201612826785f, 0.0f,
-                                      -0.19509032201612826785f, -0.38268343236508977173f, -0.55557023301960222474f,
-                                      -0.70710678118654752440f, -0.83146961230254523708f, -0.92387953251128675613f,
-                                      -0.98078528040323044913f};
-__constant__ const float kW32S[16] = {0.0f, 0.19509032201612826785f, 0.38268343236508977173f,
-                                      0.55557023301960222474f, 0.70710678118654752440f, 0.83146961230254523708f,
-                                      0.92387953251128675613f, 0.98078528040323044913f, 1.0f,
-                                      0.98078528040323044913f, 0.92387953251128675613f, 0.83146961230254523708f,
-                                      0.70710678118654752440f, 0.55557023301960222474f, 0.38268343236508977173f,
-                                      0.19509032201612826785f};
-
-// 32-point DFT in registers, natural order in and out: 16-point DFTs of the even and odd
-// samples and one radix-2 step with w32^k
-template <bool INV>
-__device__ __forceinline__ void dft32(float2 (&a)[32]) {
-  float2 e[16], o[16];
-#pragma unroll
-  for (int m = 0; m < 16; ++m) { e[m] = a[2 * m]; o[m] = a[2 * m + 1]; }
-  dft16<INV>(e);
-  dft16<INV>(o);
-#pragma unroll
-  for (int k = 0; k < 16; ++k) {
-    const float c = kW32C[k], sn = INV ? kW32S[k] : -kW32S[k];
-    const float2 t = mk<float2>(o[k].x * c - o[k].y * sn, o[k].x * sn + o[k].y * c);
-    a[k] = cadd(e[k], t);
-    a[k + 16] = csub(e[k], t);
-  }
-}
-
-template <bool INV>
-__device__ __forceinline__ void wfft1024(float2 (&z)[32], float2* tile, const float2* __restrict__ tw, int lane) {
-  dft32<INV>(z);
-#pragma unroll
-  for (int k1 = 1; k1 < 32; ++k1) {
-    const float2 w = __ldg(&tw[lane * k1]);
-    z[k1] = INV ? cmulc(z[k1], w) : cmul(z[k1], w);
-  }
-#pragma unroll
-  for (int k1 = 0; k1 < 32; ++k1) tile[k1 * 33 + lane] = z[k1];
-  __syncwarp();
-#pragma unroll
-  for (int j2 = 0; j2 < 32; ++j2) z[j2] = tile[lane * 33 + j2];
-  __syncwarp();
-  dft32<INV>(z);
-}
-
-__device__ __forceinline__ float2 shfl2(float2 v, int src) {
-  return mk<float2>(__shfl_sync(0xffffffffu, v.x, src), __shfl_sync(0xffffffffu, v.y, src));
-}
-
 // The row pass of row_kernel (same flags, pair table, pointwise work and error partials) for
 // FP32 rows of 1024 points, one warp per sequence.
 template <int RX>
@@ -1010,6 +955,14 @@ mjx_status mjx_spec2d_plan_init(void* plan, const mjx_grid2d* g, int symbol, int
     return -k * k;
   };
   put_tw(pv.twx, nx);
+  if (twx_count(nx, e) != nx) {  // the transposed copy for the one-warp 1024-point transform
+    float* p = (float*)pv.twx;
+    for (int k1 = 0; k1 < 32; ++k1)
+      for (int l = 0; l < 32; ++l) {
+        p[2 * (1024 + 32 * k1 + l)] = p[2 * (l * k1)];
+        p[2 * (1024 + 32 * k1 + l) + 1] = p[2 * (l * k1) + 1];
+      }
+  }
   put_tw(pv.twy, ny);
   for (int kx = 0; kx < ldc; ++kx) {
     const double v = kx <= nx / 2 ? lam1(kx, nx, g->dx) : 0.0;

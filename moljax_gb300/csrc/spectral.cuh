@@ -146,7 +146,8 @@ template <typename T> struct ColArgs {
   ColJob job[MJX_MAXJOB];
 };
 
-// Plan layout (device bytes): twx[nx] twy[ny] lamx[ldc] lamy[ny], 256-byte aligned parts.
+// Plan layout (device bytes): twx[nx] twy[ny] lamx[ldc] lamy[ny], 256-byte aligned parts;
+// FP32 plans of 1024-point rows hold 2048 x twiddles (the second half transposed, wfft.cuh).
 struct PlanView {
   const void* twx; const void* twy; const void* lamx; const void* lamy;
 };
