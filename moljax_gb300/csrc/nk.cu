@@ -14,8 +14,9 @@
 // preconditioner in FP32.
 //
 // Preconditioner M^-1 = (alpha0 I - beta Dbar Lap_D)^-1, Dbar = a + b mean(u_n^2),
-// exact through the odd extension to a (2N)^2 periodic box (cell-centred
-// Dirichlet = DST-II diagonalisation), applied with the periodic spectral pass.
+// exact in the DST-II basis of the cell-centred Dirichlet grid: a real DST-II /
+// DST-III pair in Makhoul's n-point form (three passes, eigenvalues from the
+// FD symbol of the (2N)^2 periodic plan, which the odd extension shares).
 //
 // The Arnoldi steps of a GMRES cycle run as one CUDA graph with a conditional
 // while node, four kernels per step (the fused passes below: operand + forward
@@ -543,34 +544,30 @@ __global__ void nd_ls_begin_kernel(NewtonDev* nd, NKConsts* K, cudaGraphConditio
 
 // --------------------------------------------------------------- fused Arnoldi step
 // One GMRES iteration on M^-1 A in six kernels (the separate sequence above takes eleven):
-//   JVP       t = A V_j / |V_j| (vd_jvp_j_kernel: elementwise, every SM busy);
-//   nka_fwd   the odd extension of t and the forward row transforms of the extension, two
-//             real rows per complex sequence, half spectra out;
-//   col pass  the Helmholtz inverse along the columns (launch_col, oddy);
-//   nka_inv   inverse row transforms and w = M^-1 A V_j on the n x n block (at a cycle
-//             start: V_0 = w and its |.|^2 partials, the last CTA starts the cycle);
-//   nka_dots  V_j normalised in place and the Gram-Schmidt partial dots <V_i, w> (i <= j),
-//             accumulated in float-float on the FP32 pipe; the last CTA sums them in a
-//             fixed order into H[:, j];
-//   nka_orth  V_{j+1} = w - sum_i H_ij V_i and |V_{j+1}|^2 partials; the last CTA applies
-//             the Givens rotations, back-substitutes when the cycle ends and sets the loop
-//             flag.
-// The row passes have one warp (2n = 1024) or 2n/16 threads per row pair of the extension,
-// i.e. few warps in all, so the stencil and the dot products, whose loads need many
-// warps in flight, stay in the elementwise kernels.  "Last CTA" is a ticket: every CTA
-// publishes its partials, fences and draws a ticket from a counter in the workspace; the
-// CTA that draws the final ticket reads all partials and resets the counter.  No CTA ever
-// waits for another.
+//   JVP        t = A V_j / |V_j| (vd_jvp_j_kernel: elementwise, every SM busy);
+//   DST rows   DST-II along x of t, two rows per complex n-point transform;
+//   DST cols   DST-II along y, the Helmholtz inverse, DST-III along y (in place);
+//   DST rows   DST-III along x and w = M^-1 A V_j (at a cycle start: V_0 = w and its |.|^2
+//              partials, the last CTA starts the cycle);
+//   nka_dots   V_j normalised in place and the Gram-Schmidt partial dots <V_i, w> (i <= j),
+//              accumulated in float-float on the FP32 pipe; the last CTA sums them in a
+//              fixed order into H[:, j];
+//   nka_orth   V_{j+1} = w - sum_i H_ij V_i and |V_{j+1}|^2 partials; the last CTA applies
+//              the Givens rotations, back-substitutes when the cycle ends and sets the loop
+//              flag.
+// The row passes have n/16 threads per row pair, i.e. few warps in all, so the stencil and
+// the dot products, whose loads need many warps in flight, stay in the elementwise
+// kernels.  "Last CTA" is a ticket: every CTA publishes its partials, fences and draws a
+// ticket from a counter in the workspace; the CTA that draws the final ticket reads all
+// partials and resets the counter.  No CTA ever waits for another.
 enum { NKA_STORE_W = 0, NKA_START = 1 };
 
 struct NkaArgs {
-  int n, log2L, ldc, nseq;
+  int n, nseq;
   long long N2;
   const float* src;     // operand of the preconditioner (n x n)
   float* V;             // Krylov basis, m + 1 vectors of N2
   float* t;             // w = M^-1 A V_j (Arnoldi)
-  cx<float>* spec;      // n rows of ldc half-spectrum points (the distinct rows of the extension)
-  const cx<float>* tw;  // twiddles of length 2n
   GmresState* gs;
   const NKConsts* K;
   double* part;         // per-CTA partials
@@ -582,6 +579,15 @@ struct NkaArgs {
   cudaGraphConditionalHandle h;
   int use_handle;
   int skip_converged;   // Arnoldi passes: return at entry once the cycle has converged
+  // the DST passes
+  int log2n, C;         // transform length n; column tile width (even)
+  float* S;             // real DST coefficients, n x n
+  const cx<float>* twn; // twiddles of length n
+  const float2* ph;     // (cos, sin)(pi k / 2n), k < n
+  const float2* tw512;  // n = 512: the twiddles of wfft512
+  const float* lamx;    // the plan's (2n)-point symbol along x (index = frequency 0..n)
+  const float* lamy;    // along y (fftfreq order of 2n)
+  const DevState* st;   // Helmholtz step dtc
 };
 
 // true in the CTA that finished last (block-uniform); its reads of the other CTAs'
@@ -694,157 +700,353 @@ __device__ __forceinline__ void nka_finish(const NkaArgs& a, int y, int x0, int 
   }
 }
 
-// forward row transforms of the odd extension of src (shared-memory Stockham, 2n <= 4096)
-__global__ void __launch_bounds__(256) nka_fwd_kernel(const __grid_constant__ NkaArgs a) {
-  typedef cx<float> C;
+// ---- the preconditioner as a real DST-II / DST-III pair (Makhoul's n-point form)
+// M^-1 = (1/a0) (I - (beta Dbar/a0) Lap_D)^-1 is diagonal in the DST-II basis of the
+// cell-centred Dirichlet grid (the odd-extension form above carries the same coefficients
+// with four times the transform work).  DST-II of a real row x of length n:
+//   DST-II(x)[n-1-k] = DCT-II(y)[k], y_j = (-1)^j x_j,
+//   DCT-II(y)[k] = Re(e^{-i pi k/2n} V_k), V = FFT_n(v), v_{j} = y_{2j}, v_{n-1-j} = y_{2j+1}
+// (Makhoul 1980), two real rows (or columns) per complex FFT; the inverse runs the same
+// steps backwards: V_k = e^{i pi k/2n} (C_k - i C_{n-k}) (C_n = 0), v = IFFT_n(V), y from v.
+// DST index s has frequency s + 1: eigenvalue lam_2n(s + 1) of the plan's (2n)-point FD
+// symbol, the same as the odd extension's.  Three kernels: rows forward (from the
+// operand), columns forward * multiplier * inverse (in place), rows inverse (w, or the
+// cycle start).
+
+// position of element j in Makhoul's reordering
+__device__ __forceinline__ int mk_pos(int j, int n) { return (j & 1) ? n - 1 - (j >> 1) : (j >> 1); }
+
+// DCT-II coefficients of index k of the two sequences packed in Z (Zk = Z[k], Zm = Z[n-k])
+__device__ __forceinline__ void dct_split(float2 Zk, float2 Zm, float2 p, float& ca, float& cb) {
+  const float vax = 0.5f * (Zk.x + Zm.x), vay = 0.5f * (Zk.y - Zm.y);
+  const float vbx = 0.5f * (Zk.y + Zm.y), vby = 0.5f * (Zm.x - Zk.x);
+  ca = p.x * vax + p.y * vay;
+  cb = p.x * vbx + p.y * vby;
+}
+
+// inverse input of index k from the coefficients (C_k, C_{n-k}) of the two sequences
+__device__ __forceinline__ float2 dct_merge(float cak, float cam, float cbk, float cbm, float2 p) {
+  const float vax = p.x * cak + p.y * cam, vay = p.y * cak - p.x * cam;
+  const float vbx = p.x * cbk + p.y * cbm, vby = p.y * cbk - p.x * cbm;
+  return make_float2(vax - vby, vay + vbx);
+}
+
+// forward DST-II along x of the row pairs (y, y + n/2) of a.src into a.S
+__global__ void __launch_bounds__(256) dst_row_fwd_kernel(const __grid_constant__ NkaArgs a) {
+  typedef float2 C;
   if (a.skip_converged && a.gs->converged) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* buf = reinterpret_cast<C*>(smem_raw);
-  const int n = a.n, L = 2 * n, hn = n >> 1;
-  const int tps = L >= 16 ? L >> 4 : 1;
+  const int n = a.n, hn = n >> 1;
+  const int tps = n >= 16 ? n >> 4 : 1;
   const int tid = threadIdx.x, s_loc = pdiv(tid, tps), lt = tid - s_loc * tps;
   const bool active = s_loc < a.nseq;  // whole warps are launched
   const int y = blockIdx.x * a.nseq + s_loc;
-  const int zb = s_loc * L;
+  const int zb = s_loc * n;
   const float* ra = a.src + (long long)y * n;
   const float* rb = a.src + (long long)(y + hn) * n;
 #pragma unroll
-  for (int m = 0; m < 8; ++m) {
+  for (int m = 0; m < 16; ++m) {
     const int x = lt + m * tps;
     if (active && x < n) {
-      const float ta = ra[x], tb = rb[x];
-      buf[sp(zb + x)] = mk<C>(ta, tb);
-      buf[sp(zb + L - 1 - x)] = mk<C>(-ta, -tb);
+      const float sg = (x & 1) ? -1.f : 1.f;
+      buf[sp(zb + mk_pos(x, n))] = make_float2(sg * ra[x], sg * rb[x]);
     }
   }
   __syncthreads();
-  fft_smem<float, false, false>(buf, L, a.log2L, a.nseq, L, 1, a.tw, tid);
+  fft_smem<float, false, false>(buf, n, a.log2n, a.nseq, n, 1, a.twn, tid);
   if (!active) return;
-  C* A = a.spec + (long long)y * a.ldc;
-  C* B = a.spec + (long long)(y + hn) * a.ldc;
+  float* Sa = a.S + (long long)y * n;
+  float* Sb = a.S + (long long)(y + hn) * n;
 #pragma unroll
-  for (int m = 0; m < 9; ++m) {
-    const int kk = lt + m * tps;
-    if (kk > n) continue;
-    const C Zk = buf[sp(zb + kk)], Zm = buf[sp(zb + ((L - kk) & (L - 1)))];
-    A[kk] = mk<C>(0.5f * (Zk.x + Zm.x), 0.5f * (Zk.y - Zm.y));
-    B[kk] = mk<C>(0.5f * (Zk.y + Zm.y), 0.5f * (Zm.x - Zk.x));
+  for (int m = 0; m < 16; ++m) {
+    const int k = lt + m * tps;
+    if (k < n) {
+      float ca, cb;
+      dct_split(buf[sp(zb + k)], buf[sp(zb + ((n - k) & (n - 1)))], a.ph[k], ca, cb);
+      Sa[n - 1 - k] = ca;
+      Sb[n - 1 - k] = cb;
+    }
   }
 }
 
-// inverse row transforms and w (any 2n <= 4096)
-template <int MODE>
-__global__ void __launch_bounds__(256) nka_inv_kernel(const __grid_constant__ NkaArgs a) {
-  typedef cx<float> C;
+// columns kx0 .. kx0 + C - 1 of a.S: DST-II along y, the Helmholtz inverse (with the 1/n^2
+// of the two unnormalised inverse transforms), DST-III along y, in place
+__global__ void __launch_bounds__(256) dst_col_kernel(const __grid_constant__ NkaArgs a) {
+  typedef float2 C;
   if (a.skip_converged && a.gs->converged) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* buf = reinterpret_cast<C*>(smem_raw);
-  const int n = a.n, L = 2 * n, hn = n >> 1;
-  const int tps = L >= 16 ? L >> 4 : 1;
+  const int n = a.n, Cn = a.C, ns = Cn >> 1, lc = __ffs(Cn) - 1, ls = lc - 1;
+  const int kx0 = blockIdx.x * Cn;
+  const int tid = threadIdx.x, nth = blockDim.x;
+  // load (sign and Makhoul position along y), columns 2q and 2q + 1 as sequence q
+  for (int e = tid; e < n * Cn; e += nth) {
+    const int y = e >> lc, c = e & (Cn - 1);
+    const float v = a.S[(long long)y * n + kx0 + c];
+    float* slot = reinterpret_cast<float*>(&buf[sp((c >> 1) + mk_pos(y, n) * ns)]) + (c & 1);
+    *slot = (y & 1) ? -v : v;
+  }
+  __syncthreads();
+  fft_smem<float, false, true>(buf, n, a.log2n, ns, 1, ns, a.twn, tid);
+  // per (sequence, k <= n/2): the coefficients of k and n - k, the multiplier, the inverse
+  // inputs of k and n - k (each item owns its two slots)
+  const float hD = (float)a.st->dtc, inv_n2 = 1.0f / ((float)n * (float)n);
+  for (int it = tid; it < ns * ((n >> 1) + 1); it += nth) {
+    const int q = it & (ns - 1), k = it >> ls;
+    const int km = (n - k) & (n - 1);
+    const C Zk = buf[sp(q + k * ns)], Zm = buf[sp(q + km * ns)];
+    float cak, cbk, cam = 0.f, cbm = 0.f;
+    dct_split(Zk, Zm, a.ph[k], cak, cbk);
+    if (k > 0) dct_split(Zm, Zk, a.ph[n - k], cam, cbm);
+    const float lxa = a.lamx[kx0 + 2 * q + 1], lxb = a.lamx[kx0 + 2 * q + 2];
+    auto mult = [&](float lam) {
+      float den = 1.0f - hD * lam;
+      if (fabsf(den) < 1e-14f) den = 1e-14f;
+      return inv_n2 / den;
+    };
+    // DCT index k <-> frequency n - k along y (lamy in fftfreq order of 2n: index n - k)
+    cak *= mult(lxa + a.lamy[n - k]);
+    cbk *= mult(lxb + a.lamy[n - k]);
+    if (k > 0) {
+      cam *= mult(lxa + a.lamy[k]);
+      cbm *= mult(lxb + a.lamy[k]);
+    }
+    buf[sp(q + k * ns)] = dct_merge(cak, cam, cbk, cbm, a.ph[k]);
+    if (k > 0 && km != k) buf[sp(q + km * ns)] = dct_merge(cam, cak, cbm, cbk, a.ph[n - k]);
+  }
+  __syncthreads();
+  fft_smem<float, true, true>(buf, n, a.log2n, ns, 1, ns, a.twn, tid);
+  for (int e = tid; e < n * Cn; e += nth) {
+    const int y = e >> lc, c = e & (Cn - 1);
+    const float v = reinterpret_cast<const float*>(&buf[sp((c >> 1) + mk_pos(y, n) * ns)])[c & 1];
+    a.S[(long long)y * n + kx0 + c] = (y & 1) ? -v : v;
+  }
+}
+
+// inverse DST-III along x of the row pairs (y, y + n/2) of a.S; w = (1/a0) result
+template <int MODE>
+__global__ void __launch_bounds__(256) dst_row_inv_kernel(const __grid_constant__ NkaArgs a) {
+  typedef float2 C;
+  if (a.skip_converged && a.gs->converged) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  C* buf = reinterpret_cast<C*>(smem_raw);
+  const int n = a.n, hn = n >> 1;
+  const int tps = n >= 16 ? n >> 4 : 1;
   const int tid = threadIdx.x, s_loc = pdiv(tid, tps), lt = tid - s_loc * tps;
   const bool active = s_loc < a.nseq;  // whole warps are launched
   const int y = blockIdx.x * a.nseq + s_loc;
-  const int zb = s_loc * L;
-  const C* A = a.spec + (long long)y * a.ldc;
-  const C* B = a.spec + (long long)(y + hn) * a.ldc;
-  C Ak[9], Bk[9];
+  const int zb = s_loc * n;
+  const float* Ta = a.S + (long long)y * n;
+  const float* Tb = a.S + (long long)(y + hn) * n;
+  // DCT coefficient k of row r is T_r[n - 1 - k]; each k <= n/2 fills slots k and n - k
 #pragma unroll
   for (int m = 0; m < 9; ++m) {
-    const int kk = lt + m * tps;
-    if (active && kk <= n) { Ak[m] = A[kk]; Bk[m] = B[kk]; }
-  }
-#pragma unroll
-  for (int m = 0; m < 9; ++m) {
-    const int kk = lt + m * tps;
-    if (active && kk <= n) {
-      buf[sp(zb + kk)] = mk<C>(Ak[m].x - Bk[m].y, Ak[m].y + Bk[m].x);
-      if (kk > 0 && kk < n) buf[sp(zb + L - kk)] = mk<C>(Ak[m].x + Bk[m].y, Bk[m].x - Ak[m].y);
+    const int k = lt + m * tps;
+    if (active && k <= hn) {
+      const float cak = Ta[n - 1 - k], cbk = Tb[n - 1 - k];
+      const float cam = k > 0 ? Ta[k - 1] : 0.f, cbm = k > 0 ? Tb[k - 1] : 0.f;
+      buf[sp(zb + k)] = dct_merge(cak, cam, cbk, cbm, a.ph[k]);
+      if (k > 0 && k < n - k) buf[sp(zb + n - k)] = dct_merge(cam, cak, cbm, cbk, a.ph[n - k]);
     }
   }
   __syncthreads();
-  fft_smem<float, true, false>(buf, L, a.log2L, a.nseq, L, 1, a.tw, tid);
-  const float sc = (float)a.K->inv_a0;
-  float wa[8], wb[8];
-#pragma unroll
-  for (int m = 0; m < 8; ++m) {
-    const int x = lt + m * tps;
-    wa[m] = wb[m] = 0.f;
-    if (active && x < n) {
-      const C v = buf[sp(zb + x)];
-      wa[m] = sc * v.x;
-      wb[m] = sc * v.y;
-    }
-  }
-  // idle threads (x0 = n) contribute nothing
-  nka_finish<MODE, 8>(a, active ? y : 0, active ? lt : n, tps, wa, wb);
-}
-
-// The same two passes for 2n = 1024, one warp per sequence (the transform of wfft.cuh)
-__global__ void __launch_bounds__(128) nka_fwd_w32_kernel(const __grid_constant__ NkaArgs a) {
-  typedef float2 C;
-  if (a.skip_converged && a.gs->converged) return;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int lane = threadIdx.x & 31, s_loc = threadIdx.x >> 5;
-  C* tile = reinterpret_cast<C*>(smem_raw) + s_loc * (32 * 33);
-  const int y = blockIdx.x * a.nseq + s_loc;
-  const float* ra = a.src + (long long)y * 512;
-  const float* rb = a.src + (long long)(y + 256) * 512;
-  C z[32];
-#pragma unroll
-  for (int j = 0; j < 16; ++j) z[j] = mk<C>(ra[lane + 32 * j], rb[lane + 32 * j]);
-  // element 1023 - x = (31 - lane) + 32 (31 - j) carries the negated value
-#pragma unroll
-  for (int j = 16; j < 32; ++j) {
-    const C v = shfl2(z[31 - j], 31 - lane);
-    z[j] = mk<C>(-v.x, -v.y);
-  }
-  wfft1024<false>(z, tile, a.tw, lane);
-  C* A = a.spec + (long long)y * a.ldc;
-  C* B = a.spec + (long long)(y + 256) * a.ldc;
-  const int src = (32 - lane) & 31;
-#pragma unroll
-  for (int k2 = 0; k2 <= 16; ++k2) {
-    C Zm = shfl2(z[k2 <= 15 ? 31 - k2 : 15], src);  // X_{1024-k} (lanes > 0)
-    if (lane == 0) Zm = z[(32 - k2) & 31];
-    const int k = lane + 32 * k2;
-    if (k2 == 16 && lane != 0) continue;
-    const C Zk = z[k2];
-    A[k] = mk<C>(0.5f * (Zk.x + Zm.x), 0.5f * (Zk.y - Zm.y));
-    B[k] = mk<C>(0.5f * (Zk.y + Zm.y), 0.5f * (Zm.x - Zk.x));
-  }
-}
-
-template <int MODE>
-__global__ void __launch_bounds__(128) nka_inv_w32_kernel(const __grid_constant__ NkaArgs a) {
-  typedef float2 C;
-  if (a.skip_converged && a.gs->converged) return;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int lane = threadIdx.x & 31, s_loc = threadIdx.x >> 5;
-  C* tile = reinterpret_cast<C*>(smem_raw) + s_loc * (32 * 33);
-  const int y = blockIdx.x * a.nseq + s_loc;
-  const C* A = a.spec + (long long)y * a.ldc;
-  const C* B = a.spec + (long long)(y + 256) * a.ldc;
-  const int src = (32 - lane) & 31;
-  C z[32], Ar[17], Br[17];
-#pragma unroll
-  for (int j = 0; j < 16; ++j) { Ar[j] = A[32 * j + lane]; Br[j] = B[32 * j + lane]; }
-  Ar[16] = lane == 0 ? A[512] : mk<C>(0.f, 0.f);
-  Br[16] = lane == 0 ? B[512] : mk<C>(0.f, 0.f);
-#pragma unroll
-  for (int j = 0; j < 16; ++j) z[j] = mk<C>(Ar[j].x - Br[j].y, Ar[j].y + Br[j].x);
-#pragma unroll
-  for (int j = 16; j < 32; ++j) {
-    C av = shfl2(Ar[31 - j], src), bv = shfl2(Br[31 - j], src);
-    if (lane == 0) { av = Ar[32 - j]; bv = Br[32 - j]; }
-    if (lane == 0 && j == 16) z[j] = mk<C>(av.x - bv.y, av.y + bv.x);
-    else z[j] = mk<C>(av.x + bv.y, bv.x - av.y);
-  }
-  wfft1024<true>(z, tile, a.tw, lane);
+  fft_smem<float, true, false>(buf, n, a.log2n, a.nseq, n, 1, a.twn, tid);
   const float sc = (float)a.K->inv_a0;
   float wa[16], wb[16];
 #pragma unroll
-  for (int j = 0; j < 16; ++j) { wa[j] = sc * z[j].x; wb[j] = sc * z[j].y; }
+  for (int m = 0; m < 16; ++m) {
+    const int x = lt + m * tps;
+    wa[m] = wb[m] = 0.f;
+    if (active && x < n) {
+      const C v = buf[sp(zb + mk_pos(x, n))];
+      const float s = (x & 1) ? -sc : sc;
+      wa[m] = s * v.x;
+      wb[m] = s * v.y;
+    }
+  }
+  // idle threads (x0 = n) contribute nothing
+  nka_finish<MODE, 16>(a, active ? y : 0, active ? lt : n, tps, wa, wb);
+}
+
+// ---- one-warp 512-point transform for the n = 512 DST passes
+// Lane l holds elements l + 32 j (j < 16).  512 = 32 x 16: a 16-point DFT per lane over j,
+// the twiddles w512^(l k1) (tw[32 k1 + l]), a transpose through a 16 x 33 shared tile of the
+// warp; lane L = k1 + 16 h then takes the elements l = h + 2 m (m < 16) of column k1, a
+// 16-point DFT over m, and the radix-2 step with its partner lane L ^ 16 (w32^k).  On
+// return lane L holds X[k1 + 16 k + 256 h] in x[k].  INV: conjugate twiddles (unnormalised).
+template <bool INV>
+__device__ __forceinline__ void wfft512(float2 (&x)[16], float2* tile, const float2* __restrict__ tw, int lane) {
+  dft16<INV>(x);
+#pragma unroll
+  for (int k1 = 1; k1 < 16; ++k1) {
+    const float2 w = __ldg(&tw[32 * k1 + lane]);
+    x[k1] = INV ? cmulc(x[k1], w) : cmul(x[k1], w);
+  }
+#pragma unroll
+  for (int k1 = 0; k1 < 16; ++k1) tile[k1 * 33 + lane] = x[k1];
+  __syncwarp();
+  const int k1 = lane & 15, h = lane >> 4;
+#pragma unroll
+  for (int m = 0; m < 16; ++m) x[m] = tile[k1 * 33 + h + 2 * m];
+  __syncwarp();
+  dft16<INV>(x);
+#pragma unroll
+  for (int k = 0; k < 16; ++k) {
+    const float2 o = shfl2(x[k], lane ^ 16);
+    const float2 E = h == 0 ? x[k] : o, O = h == 0 ? o : x[k];
+    const float c = kW32C[k], s = INV ? kW32S[k] : -kW32S[k];
+    const float2 wO = make_float2(O.x * c - O.y * s, O.x * s + O.y * c);
+    x[k] = h == 0 ? make_float2(E.x + wO.x, E.y + wO.y) : make_float2(E.x - wO.x, E.y - wO.y);
+  }
+}
+
+// the transform's output in natural order into a warp's 512-entry shared buffer
+__device__ __forceinline__ void w512_store(const float2 (&x)[16], float2* nat, int lane) {
+  const int base = (lane & 15) + 256 * (lane >> 4);
+#pragma unroll
+  for (int k = 0; k < 16; ++k) nat[base + 16 * k] = x[k];
+  __syncwarp();
+}
+
+// DST-II along x, n = 512, one warp per row pair (y, y + 256)
+__global__ void __launch_bounds__(128) dst_row_fwd_w512_kernel(const __grid_constant__ NkaArgs a) {
+  if (a.skip_converged && a.gs->converged) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int lane = threadIdx.x & 31, s_loc = threadIdx.x >> 5;
+  float2* tile = reinterpret_cast<float2*>(smem_raw) + s_loc * (16 * 33 + 512);
+  float2* nat = tile + 16 * 33;
+  const int y = blockIdx.x * a.nseq + s_loc;
+  const float* ra = a.src + (long long)y * 512;
+  const float* rb = a.src + (long long)(y + 256) * 512;
+  float2 z[16];
+  // Makhoul order: position p < 256 holds element 2p, position p >= 256 element 1023 - 2p,
+  // with the sign (-1)^element (+ for the even, - for the odd elements)
+#pragma unroll
+  for (int j = 0; j < 16; ++j) {
+    const int p = lane + 32 * j;
+    const int src = p < 256 ? 2 * p : 1023 - 2 * p;
+    const float sg = p < 256 ? 1.f : -1.f;
+    z[j] = make_float2(sg * ra[src], sg * rb[src]);
+  }
+  wfft512<false>(z, tile, a.tw512, lane);
+  w512_store(z, nat, lane);
+  float* Sa = a.S + (long long)y * 512;
+  float* Sb = a.S + (long long)(y + 256) * 512;
+#pragma unroll
+  for (int j = 0; j < 16; ++j) {
+    const int k = lane + 32 * j;
+    float ca, cb;
+    dct_split(nat[k], nat[(512 - k) & 511], a.ph[k], ca, cb);
+    Sa[511 - k] = ca;
+    Sb[511 - k] = cb;
+  }
+}
+
+// columns kx0, kx0 + 1 of a.S (n = 512, one warp per column pair): DST-II along y, the
+// multiplier, DST-III along y, in place
+__global__ void __launch_bounds__(128) dst_col_w512_kernel(const __grid_constant__ NkaArgs a) {
+  if (a.skip_converged && a.gs->converged) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int lane = threadIdx.x & 31, s_loc = threadIdx.x >> 5;
+  float2* tile = reinterpret_cast<float2*>(smem_raw) + s_loc * (16 * 33 + 512);
+  float2* nat = tile + 16 * 33;
+  const int kx0 = 2 * (blockIdx.x * (blockDim.x >> 5) + s_loc);
+  float2 z[16];
+#pragma unroll
+  for (int j = 0; j < 16; ++j) {
+    const int p = lane + 32 * j;
+    const int src = p < 256 ? 2 * p : 1023 - 2 * p;
+    const float sg = p < 256 ? 1.f : -1.f;
+    const float2 v = *reinterpret_cast<const float2*>(a.S + (long long)src * 512 + kx0);
+    z[j] = make_float2(sg * v.x, sg * v.y);
+  }
+  wfft512<false>(z, tile, a.tw512, lane);
+  w512_store(z, nat, lane);
+  const float hD = (float)a.st->dtc, inv_n2 = 1.0f / (512.0f * 512.0f);
+  const float lxa = a.lamx[kx0 + 1], lxb = a.lamx[kx0 + 2];
+  auto mult = [&](float lam) {
+    float den = 1.0f - hD * lam;
+    if (fabsf(den) < 1e-14f) den = 1e-14f;
+    return inv_n2 / den;
+  };
+  // inverse input of index k from the scaled coefficients of k and 512 - k
+#pragma unroll
+  for (int j = 0; j < 16; ++j) {
+    const int k = lane + 32 * j, km = (512 - k) & 511;
+    const float2 Zk = nat[k], Zm = nat[km];
+    float cak, cbk, cam = 0.f, cbm = 0.f;
+    dct_split(Zk, Zm, a.ph[k], cak, cbk);
+    cak *= mult(lxa + a.lamy[512 - k]);
+    cbk *= mult(lxb + a.lamy[512 - k]);
+    if (k > 0) {
+      dct_split(Zm, Zk, a.ph[512 - k], cam, cbm);
+      cam *= mult(lxa + a.lamy[k]);
+      cbm *= mult(lxb + a.lamy[k]);
+    }
+    z[j] = dct_merge(cak, cam, cbk, cbm, a.ph[k]);
+  }
+  __syncwarp();
+  wfft512<true>(z, tile, a.tw512, lane);
+  w512_store(z, nat, lane);
+#pragma unroll
+  for (int j = 0; j < 16; ++j) {
+    const int y = lane + 32 * j;
+    const float2 v = nat[mk_pos(y, 512)];
+    const float sg = (y & 1) ? -1.f : 1.f;
+    *reinterpret_cast<float2*>(a.S + (long long)y * 512 + kx0) = make_float2(sg * v.x, sg * v.y);
+  }
+}
+
+// DST-III along x, n = 512, one warp per row pair; w = (1/a0) result
+template <int MODE>
+__global__ void __launch_bounds__(128) dst_row_inv_w512_kernel(const __grid_constant__ NkaArgs a) {
+  if (a.skip_converged && a.gs->converged) return;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int lane = threadIdx.x & 31, s_loc = threadIdx.x >> 5;
+  float2* tile = reinterpret_cast<float2*>(smem_raw) + s_loc * (16 * 33 + 512);
+  float2* nat = tile + 16 * 33;
+  const int y = blockIdx.x * a.nseq + s_loc;
+  const float* Ta = a.S + (long long)y * 512;
+  const float* Tb = a.S + (long long)(y + 256) * 512;
+  float2 z[16];
+#pragma unroll
+  for (int j = 0; j < 16; ++j) {
+    const int k = lane + 32 * j;
+    const float cak = Ta[511 - k], cbk = Tb[511 - k];
+    const float cam = k > 0 ? Ta[k - 1] : 0.f, cbm = k > 0 ? Tb[k - 1] : 0.f;
+    z[j] = dct_merge(cak, cam, cbk, cbm, a.ph[k]);
+  }
+  wfft512<true>(z, tile, a.tw512, lane);
+  w512_store(z, nat, lane);
+  const float sc = (float)a.K->inv_a0;
+  float wa[16], wb[16];
+#pragma unroll
+  for (int j = 0; j < 16; ++j) {
+    const int x = lane + 32 * j;
+    const float2 v = nat[mk_pos(x, 512)];
+    const float s = (x & 1) ? -sc : sc;
+    wa[j] = s * v.x;
+    wb[j] = s * v.y;
+  }
   nka_finish<MODE, 16>(a, y, lane, 32, wa, wb);
+}
+
+// twiddles exp(-2 pi i j/n) of the n-point transforms and the phases (cos, sin)(pi k/2n)
+// (and, for n = 512, w512^(l k1) at 32 k1 + l, l < 32, k1 < 16, for wfft512)
+__global__ void dst_tables_kernel(cx<float>* twn, float2* ph, float2* tw512, int n) {
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+    double s, c;
+    sincospi(2.0 * (double)j / (double)n, &s, &c);
+    twn[j] = mk<cx<float>>((float)c, (float)(-s));
+    sincospi((double)j / (2.0 * (double)n), &s, &c);
+    ph[j] = make_float2((float)c, (float)s);
+    if (n == 512) {
+      const int k1 = j >> 5, l = j & 31;
+      sincospi(2.0 * (double)(l * k1) / 512.0, &s, &c);
+      tw512[j] = make_float2((float)c, (float)(-s));
+    }
+  }
 }
 
 // V_j /= |V_j| in place and the partial dots <V_i, w>, i = 0..j, in float-float per thread;
@@ -1080,7 +1282,7 @@ __global__ void nd_stats_kernel(const NewtonDev* nd, int* slot) {
 
 // --------------------------------------------------------------- host driver
 struct NKLayout {
-  size_t y0, y1, y2, y3, y4, cst, R, xt, xn, y32, b32, dx, t, V, spec, part, gs, K, pst, nd, tick, ring, total;
+  size_t y0, y1, y2, y3, y4, cst, R, xt, xn, y32, b32, dx, t, V, S, dtab, part, gs, K, pst, nd, tick, ring, total;
   int nblk, m;
 };
 static inline size_t al(size_t b) { return (b + 255) & ~size_t(255); }
@@ -1105,7 +1307,8 @@ static NKLayout nk_layout(int n, int m) {
   L.dx = o; o += al(N2 * 4);
   L.t = o; o += al(N2 * 4);
   L.V = o; o += al((size_t)(m + 1) * N2 * 4);
-  L.spec = o; o += al((size_t)(2 * n) * spec_ldc(2 * n) * 8);
+  L.S = o; o += al(N2 * 4);                              // real DST coefficients
+  L.dtab = o; o += al((size_t)(2 * n + 512) * sizeof(float2));  // n-point twiddles, phases, wfft512 twiddles
   // per-CTA partials: elementwise passes (nblk CTAs) and the fused row passes (up to n/2 CTAs)
   L.part = o; o += al((size_t)(m + 2) * (size_t)(L.nblk > n / 2 ? L.nblk : n / 2) * 8);
   L.gs = o; o += al(sizeof(GmresState));
@@ -1139,79 +1342,63 @@ static NkaArgs nka_args(NKRun& r) {
   memset(&a, 0, sizeof(a));
   const int n = r.n;
   const PlanView pv = plan_view(r.plan2, 2 * n, 2 * n, 4);
-  a.n = n; a.log2L = ilog2_exact(2 * n); a.ldc = spec_ldc(2 * n);
+  a.n = n;
   a.N2 = (long long)n * n;
   a.V = P32(r, r.L.V); a.t = P32(r, r.L.t); a.src = a.t;
-  a.spec = (cx<float>*)(r.ws + r.L.spec); a.tw = (const cx<float>*)pv.twx;
   a.gs = (GmresState*)(r.ws + r.L.gs); a.K = (const NKConsts*)(r.ws + r.L.K);
   a.part = P64(r, r.L.part); a.ticket = (unsigned*)(r.ws + r.L.tick);
+  a.log2n = ilog2_exact(n);
+  a.S = P32(r, r.L.S);
+  a.twn = (const cx<float>*)(r.ws + r.L.dtab);
+  a.ph = (const float2*)(r.ws + r.L.dtab) + n;
+  a.tw512 = (const float2*)(r.ws + r.L.dtab) + 2 * n;
+  a.lamx = (const float*)pv.lamx; a.lamy = (const float*)pv.lamy;
+  a.st = (const DevState*)(r.ws + r.L.pst);
   return a;
 }
 
-// CTA geometry of the fused row passes over the n/2 row pairs of the extension: one warp
-// per pair when 2n = 1024, else the shared-memory Stockham with 2n/16 threads per pair;
-// fewer pairs per CTA until the pass covers every SM; whole warps (the reductions shuffle
-// over full warps), the threads past nseq * tps idle
-struct NkaGeom { bool w32; int nseq, ctas, threads; size_t smem; };
-static NkaGeom nka_geom(int n) {
-  NkaGeom g;
-  const int L = 2 * n, hn = n / 2;
-  g.w32 = L == 1024;
-  int ns = g.w32 ? 4 : row_nseq(L, hn);
+// CTA geometry of the DST passes: rows in pairs (y, y + n/2), n/16 threads per pair, fewer
+// pairs per CTA until the pass covers every SM, whole warps (the threads past nseq * tps
+// idle); columns in tiles of C (even) real columns, C/2 complex sequences, at least 152
+// tiles where n allows and within the default 48 KB of shared memory
+struct DstGeom { int nseq, ctas, threads, C, col_threads; size_t smem, col_smem; };
+static DstGeom dst_geom(int n) {
+  DstGeom g;
+  const int hn = n / 2, tps = n >= 16 ? n / 16 : 1;
+  int ns = row_nseq(n, hn);
   if (ns > hn) ns = hn;
   while (ns > 1 && hn / ns < 152) ns >>= 1;
   g.nseq = ns;
   g.ctas = hn / ns;
-  const int tps = L >= 16 ? L / 16 : 1;
-  g.threads = g.w32 ? 32 * ns : ((ns * tps + 31) / 32) * 32;
-  g.smem = g.w32 ? (size_t)ns * 32 * 33 * sizeof(float2) : (size_t)sp_size(ns * L) * sizeof(float2);
+  g.threads = ((ns * tps + 31) / 32) * 32;
+  g.smem = (size_t)sp_size(ns * n) * sizeof(float2);
+  int C = 8 < n ? 8 : n;
+  while (C > 2 && (n / C < 152 || (size_t)sp_size(n * (C / 2)) * sizeof(float2) > 48 * 1024)) C >>= 1;
+  g.C = C;
+  g.col_threads = (((C / 2) * tps + 31) / 32) * 32;
+  g.col_smem = (size_t)sp_size(n * (C / 2)) * sizeof(float2);
   return g;
 }
 
-static cudaError_t nka_fwd(NKRun& r, const NkaArgs& a0) {
-  NkaArgs a = a0;
-  const NkaGeom g = nka_geom(r.n);
-  a.nseq = g.nseq;
-  if (g.w32) nka_fwd_w32_kernel<<<g.ctas, g.threads, g.smem, r.s>>>(a);
-  else nka_fwd_kernel<<<g.ctas, g.threads, g.smem, r.s>>>(a);
-  return cudaGetLastError();
-}
-
+// w = M^-1 a.src: DST-II along x, along y with the multiplier and DST-III along y, DST-III
+// along x (MODE: w into t, or the cycle start V_0 = w)
 template <int MODE>
-static cudaError_t nka_inv(NKRun& r, const NkaArgs& a0) {
-  NkaArgs a = a0;
-  const NkaGeom g = nka_geom(r.n);
+static cudaError_t nka_precond(NKRun& r, NkaArgs a) {
+  const DstGeom g = dst_geom(r.n);
   a.nseq = g.nseq;
-  if (g.w32) nka_inv_w32_kernel<MODE><<<g.ctas, g.threads, g.smem, r.s>>>(a);
-  else nka_inv_kernel<MODE><<<g.ctas, g.threads, g.smem, r.s>>>(a);
+  a.C = g.C;
+  if (r.n == 512) {  // one warp per row or column pair (wfft512)
+    a.nseq = 1;
+    const size_t sm = (16 * 33 + 512) * sizeof(float2);
+    dst_row_fwd_w512_kernel<<<256, 32, sm, r.s>>>(a);
+    dst_col_w512_kernel<<<256, 32, sm, r.s>>>(a);
+    dst_row_inv_w512_kernel<MODE><<<256, 32, sm, r.s>>>(a);
+    return cudaGetLastError();
+  }
+  dst_row_fwd_kernel<<<g.ctas, g.threads, g.smem, r.s>>>(a);
+  dst_col_kernel<<<r.n / g.C, g.col_threads, g.col_smem, r.s>>>(a);
+  dst_row_inv_kernel<MODE><<<g.ctas, g.threads, g.smem, r.s>>>(a);
   return cudaGetLastError();
-}
-
-// the column pass of the preconditioner: M^-1 = (1/a0) (I - (beta Dbar/a0) Lap_D)^-1 along y
-// on the odd extension (rows 2n - 1 - ky synthesised as the negated mirror), Helmholtz step
-// from the state word written by nk_consts_kernel
-static cudaError_t nka_col(NKRun& r) {
-  const int n = r.n;
-  const PlanView pv = plan_view(r.plan2, 2 * n, 2 * n, 4);
-  ColArgs<float> c;
-  memset(&c, 0, sizeof(c));
-  c.ny = 2 * n; c.log2ny = ilog2_exact(2 * n); c.ncols = n + 1; c.ldc = spec_ldc(2 * n);
-  c.C = col_tile(2 * n, c.ncols, 1, 4); c.spec = (cx<float>*)(r.ws + r.L.spec); c.lamx = (const float*)pv.lamx;
-  c.lamy = (const float*)pv.lamy; c.tw = (const cx<float>*)pv.twy;
-  c.scale = (float)(1.0 / (4.0 * n * n)); c.st = (const DevState*)(r.ws + r.L.pst); c.njobs = 1; c.oddy = 1;
-  c.job[0].nout = 1; c.job[0].mul = MUL_HELMHOLTZ; c.job[0].D = 1.0; c.job[0].hfac[0] = c.job[0].hfac[1] = 1.0;
-  c.job[0].pow[0] = c.job[0].pow[1] = 1;
-  return launch_col<float>(c, r.s);
-}
-
-// w = M^-1 a.src: forward row transforms of the odd extension, the column pass, the inverse
-// row transforms (MODE: w into t, or the cycle start V_0 = w)
-template <int MODE>
-static cudaError_t nka_precond(NKRun& r, const NkaArgs& a) {
-  cudaError_t e = nka_fwd(r, a);
-  if (e == cudaSuccess) e = nka_col(r);
-  if (e == cudaSuccess) e = nka_inv<MODE>(r, a);
-  return e;
 }
 
 // The cycle start: V_0 = M^-1 (b - A dx) (first: M^-1 b), |V_0|, the GMRES header and, with a
@@ -1684,6 +1871,10 @@ static mjx_status nk_setup(NKRun& r, const void* plan2, int n, double dy, double
   MJX_TRY(ensure_kernel_attrs());
   MJX_CUDA_TRY(cudaMemsetAsync(r.ws + r.L.pst, 0, sizeof(DevState), r.s));
   MJX_CUDA_TRY(cudaMemsetAsync(r.ws + r.L.tick, 0, sizeof(unsigned), r.s));
+  dst_tables_kernel<<<(n + 255) / 256, 256, 0, r.s>>>((cx<float>*)(r.ws + r.L.dtab),
+                                                      (float2*)(r.ws + r.L.dtab) + n,
+                                                      (float2*)(r.ws + r.L.dtab) + 2 * n, n);
+  MJX_CUDA_TRY(cudaGetLastError());
   P->max_newton = nkp->max_newton_iters; P->max_krylov = nkp->max_krylov_iters; P->restart = nkp->restart;
   P->max_backtrack = nkp->max_backtrack; P->newton_tol = nkp->newton_tol; P->krylov_tol = nkp->krylov_tol;
   P->damping = nkp->damping; P->backtrack = nkp->backtrack_factor; P->min_decrease = nkp->min_residual_decrease;
