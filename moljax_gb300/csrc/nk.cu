@@ -1062,13 +1062,29 @@ __global__ void __launch_bounds__(256) nka_dots_kernel(const __grid_constant__ N
   const long long p0 = blockIdx.x * (long long)blockDim.x + threadIdx.x, ps = (long long)gridDim.x * blockDim.x;
   float* vj = a.V + (long long)jv * N2;
   for (long long p = p0; p < N2; p += ps) vj[p] *= sj;  // as nk_scale_j_kernel
-  for (int i = 0; i <= jv; ++i) {
-    const float* vi = a.V + (long long)i * N2;
-    float hi = 0.f, lo = 0.f;
-    for (long long p = p0; p < N2; p += ps) ff_dot_acc(hi, lo, vi[p], a.t[p]);
-    double acc = (double)hi + (double)lo;
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-    if (lane == 0) red[i][warp] = acc;
+  // four vectors per sweep, so that their loads are in flight together
+  for (int i0 = 0; i0 <= jv; i0 += 4) {
+    float hi[4] = {0.f, 0.f, 0.f, 0.f}, lo[4] = {0.f, 0.f, 0.f, 0.f};
+    for (long long p = p0; p < N2; p += ps) {
+      const float tp = a.t[p];
+      float v[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) v[u] = i0 + u <= jv ? a.V[(long long)(i0 + u) * N2 + p] : 0.f;
+#pragma unroll
+      for (int u = 0; u < 4; ++u) ff_dot_acc(hi[u], lo[u], v[u], tp);
+    }
+    double acc[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) acc[u] = (double)hi[u] + (double)lo[u];
+    for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+      for (int u = 0; u < 4; ++u) acc[u] += __shfl_xor_sync(0xffffffffu, acc[u], o);
+    }
+    if (lane == 0) {
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+        if (i0 + u <= jv) red[i0 + u][warp] = acc[u];
+    }
   }
   __syncthreads();
   for (int i = threadIdx.x; i <= jv; i += blockDim.x) {
@@ -1104,7 +1120,16 @@ __global__ void __launch_bounds__(256) nka_orth_kernel(const __grid_constant__ N
   for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < N2;
        p += (long long)gridDim.x * blockDim.x) {
     float x = a.t[p];
-    for (int i = 0; i <= jv; ++i) x -= hc[i] * a.V[(long long)i * N2 + p];
+    int i = 0;
+    for (; i + 3 <= jv; i += 4) {  // loads of four vectors in flight, the same subtraction order
+      const float v0 = a.V[(long long)i * N2 + p], v1 = a.V[(long long)(i + 1) * N2 + p];
+      const float v2 = a.V[(long long)(i + 2) * N2 + p], v3 = a.V[(long long)(i + 3) * N2 + p];
+      x -= hc[i] * v0;
+      x -= hc[i + 1] * v1;
+      x -= hc[i + 2] * v2;
+      x -= hc[i + 3] * v3;
+    }
+    for (; i <= jv; ++i) x -= hc[i] * a.V[(long long)i * N2 + p];
     vn[p] = x;
     acc += (double)x * (double)x;
   }
