@@ -171,13 +171,14 @@ template <typename T> struct EArgs {
 // FP64 keeps 512 threads (its butterflies need the registers).
 template <typename T> struct EThreads { static constexpr int v = sizeof(T) == 4 ? 1024 : 512; };
 
-template <typename T>
+// The stage type is a template argument, so that each instance holds only its own operands.
+template <typename T, int TYPE>
 __global__ void __launch_bounds__(EThreads<T>::v, 1) etd_col_kernel(const __grid_constant__ EArgs<T> a) {
   typedef cx<T> Cx;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   Cx* buf = reinterpret_cast<Cx*>(smem_raw);
   const int f = blockIdx.y;
-  const int type = a.type;
+  constexpr int type = TYPE;
   const int Cn = a.C, W = Cn;
   const int lc = __ffs(Cn) - 1;  // the tile width is a power of two (halved from 16)
   const int kx0 = blockIdx.x * Cn;
@@ -194,52 +195,90 @@ __global__ void __launch_bounds__(EThreads<T>::v, 1) etd_col_kernel(const __grid
   __syncthreads();
   fft_smem<T, false, true>(buf, ny, a.log2ny, Cn, 1, W, a.tw, tid);
 
-  for (int e = tid; e < ny * Cn; e += nth) {
-    const int ky = e >> lc, c = e & (Cn - 1), kx = kx0 + c;
-    if (kx >= a.ncols) { buf[sp(ky * W + c)] = mk<Cx>((T)0, (T)0); continue; }
-    const long long g = fo + ky * ldc + kx, tg = ky * ldc + kx;
-    const Cx x = buf[sp(ky * W + c)];
-    Cx out;
-    if (type == E0) {  // the initial U^ (later steps get it from E4)
-      a.uh[g] = x;
-      continue;
-    } else if (type == E1) {
-      const T e2 = tab[1 * per + tg], q = tab[2 * per + tg];
-      const Cx u = a.uh[g];
-      a.nu[g] = x;
-      out = mk<Cx>(e2 * u.x + q * x.x, e2 * u.y + q * x.y);
-      a.ah[g] = out;
-    } else if (type == E2S) {
-      const T e2 = tab[1 * per + tg], q = tab[2 * per + tg];
-      const Cx u = a.uh[g];
-      a.ss[g] = x;
-      out = mk<Cx>(e2 * u.x + q * x.x, e2 * u.y + q * x.y);
-    } else if (type == E3) {
-      const T e2 = tab[1 * per + tg], q = tab[2 * per + tg];
-      const Cx ah = a.ah[g], nu = a.nu[g], s = a.ss[g];
-      a.ss[g] = cadd(s, x);
-      out = mk<Cx>(e2 * ah.x + q * ((T)2 * x.x - nu.x), e2 * ah.y + q * ((T)2 * x.y - nu.y));
-    } else if (type >= E5) {
-      // ETD1 (fft_integrators.py:165-166) / ETD2 (234-236)
-      const T E = tab[0 * per + tg], p1 = tab[1 * per + tg];
-      const Cx u = a.uh[g];
-      T ox = E * u.x + p1 * x.x, oy = E * u.y + p1 * x.y;
-      if (type == E7) {
-        const T p2 = tab[2 * per + tg];
-        const Cx np = a.nu[g];
-        ox += p2 * (x.x - np.x);
-        oy += p2 * (x.y - np.y);
+  // The stage combination, two elements per thread at a time: the operands are read and
+  // written in place, so the compiler cannot issue a later element's loads before an
+  // earlier element's stores; loading both elements' operands first doubles the loads in
+  // flight of the one CTA per SM (the 4096-row passes wait on DRAM).
+  const T* tb0 = tab + 0 * per;
+  const T* tb1 = tab + 1 * per;
+  const T* tb2 = tab + 2 * per;
+  const T* tb3 = tab + 3 * per;
+  const T* tb4 = tab + 4 * per;
+  const T* tb5 = tab + 5 * per;
+  const Cx zero = mk<Cx>((T)0, (T)0);
+  for (int e0 = tid; e0 < ny * Cn; e0 += 2 * nth) {
+    Cx x[2], u[2], nu[2], s3[2];
+    T c0[2], c1[2], c2[2], c3[2];
+    long long g[2];
+    int sidx[2];
+    bool ok[2];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int e = e0 + h * nth;
+      const int ky = e >> lc, c = e & (Cn - 1), kx = kx0 + c;
+      ok[h] = e < ny * Cn && kx < a.ncols;
+      sidx[h] = e < ny * Cn ? sp(ky * W + c) : -1;
+      g[h] = fo + (long long)ky * ldc + kx;
+      const long long tg = (long long)ky * ldc + kx;
+      x[h] = u[h] = nu[h] = s3[h] = zero;
+      c0[h] = c1[h] = c2[h] = c3[h] = (T)0;
+      if (!ok[h]) continue;
+      x[h] = buf[sidx[h]];
+      if (type == E1 || type == E2S) {
+        c0[h] = tb1[tg]; c1[h] = tb2[tg];
+        u[h] = a.uh[g[h]];
+      } else if (type == E3) {
+        c0[h] = tb1[tg]; c1[h] = tb2[tg];
+        u[h] = a.ah[g[h]]; nu[h] = a.nu[g[h]]; s3[h] = a.ss[g[h]];
+      } else if (type >= E5) {
+        c0[h] = tb0[tg]; c1[h] = tb1[tg];
+        u[h] = a.uh[g[h]];
+        if (type == E7) { c2[h] = tb2[tg]; nu[h] = a.nu[g[h]]; }
+      } else if (type == E4) {
+        c0[h] = tb0[tg]; c1[h] = tb3[tg]; c2[h] = tb4[tg]; c3[h] = tb5[tg];
+        u[h] = a.uh[g[h]]; nu[h] = a.nu[g[h]]; s3[h] = a.ss[g[h]];
       }
-      if (type != E5) a.nu[g] = x;
-      out = mk<Cx>(ox, oy);
-      a.uh[g] = out;
-    } else {
-      const T E = tab[0 * per + tg], f1 = tab[3 * per + tg], f2 = tab[4 * per + tg], f3 = tab[5 * per + tg];
-      const Cx u = a.uh[g], nu = a.nu[g], s = a.ss[g];
-      out = mk<Cx>(E * u.x + f1 * nu.x + f2 * s.x + f3 * x.x, E * u.y + f1 * nu.y + f2 * s.y + f3 * x.y);
-      a.uh[g] = out;  // next step's U^ (unnormalised, as the forward transform leaves it)
     }
-    buf[sp(ky * W + c)] = cscale(out, a.scale);
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      if (sidx[h] < 0) continue;
+      if (!ok[h]) { buf[sidx[h]] = zero; continue; }
+      const Cx xv = x[h];
+      Cx out;
+      if (type == E0) {  // the initial U^ (later steps get it from E4)
+        a.uh[g[h]] = xv;
+        continue;
+      } else if (type == E1) {
+        a.nu[g[h]] = xv;
+        out = mk<Cx>(c0[h] * u[h].x + c1[h] * xv.x, c0[h] * u[h].y + c1[h] * xv.y);
+        a.ah[g[h]] = out;
+      } else if (type == E2S) {
+        a.ss[g[h]] = xv;
+        out = mk<Cx>(c0[h] * u[h].x + c1[h] * xv.x, c0[h] * u[h].y + c1[h] * xv.y);
+      } else if (type == E3) {
+        // u = a^, nu = N^u, s3 = S
+        a.ss[g[h]] = cadd(s3[h], xv);
+        out = mk<Cx>(c0[h] * u[h].x + c1[h] * ((T)2 * xv.x - nu[h].x),
+                     c0[h] * u[h].y + c1[h] * ((T)2 * xv.y - nu[h].y));
+      } else if (type >= E5) {
+        // ETD1 (fft_integrators.py:165-166) / ETD2 (234-236): c0 = E, c1 = phi1, c2 = phi2
+        T ox = c0[h] * u[h].x + c1[h] * xv.x, oy = c0[h] * u[h].y + c1[h] * xv.y;
+        if (type == E7) {
+          ox += c2[h] * (xv.x - nu[h].x);
+          oy += c2[h] * (xv.y - nu[h].y);
+        }
+        if (type != E5) a.nu[g[h]] = xv;
+        out = mk<Cx>(ox, oy);
+        a.uh[g[h]] = out;
+      } else {
+        // E4: c0 = E, c1 = f1, c2 = f2, c3 = f3; next step's U^ (unnormalised, as the forward
+        // transform leaves it)
+        out = mk<Cx>(c0[h] * u[h].x + c1[h] * nu[h].x + c2[h] * s3[h].x + c3[h] * xv.x,
+                     c0[h] * u[h].y + c1[h] * nu[h].y + c2[h] * s3[h].y + c3[h] * xv.y);
+        a.uh[g[h]] = out;
+      }
+      buf[sidx[h]] = cscale(out, a.scale);
+    }
   }
   if (type == E0) return;
   __syncthreads();
@@ -344,11 +383,31 @@ static EtdPlan<T> build_etd(const void* plan, const mjx_grid2d* g, int nf, doubl
 }
 
 template <typename T>
+static mjx_status etd_col_attrs(int optin) {
+  const void* k[8] = {(const void*)etd_col_kernel<T, E0>, (const void*)etd_col_kernel<T, E1>,
+                      (const void*)etd_col_kernel<T, E2S>, (const void*)etd_col_kernel<T, E3>,
+                      (const void*)etd_col_kernel<T, E4>, (const void*)etd_col_kernel<T, E5>,
+                      (const void*)etd_col_kernel<T, E6>, (const void*)etd_col_kernel<T, E7>};
+  for (int i = 0; i < 8; ++i)
+    MJX_CUDA_TRY(cudaFuncSetAttribute(k[i], cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
+  return MJX_OK;
+}
+
+template <typename T>
 static cudaError_t etd_col(const EArgs<T>& e, cudaStream_t s) {
   const int tps = e.ny >= 16 ? e.ny / 16 : 1;
   dim3 grid((e.ncols + e.C - 1) / e.C, e.njobs);
   const size_t smem = (size_t)sp_size(e.ny * e.C) * 2 * sizeof(T);
-  etd_col_kernel<T><<<grid, e.C * tps, smem, s>>>(e);
+  switch (e.type) {
+    case E0: etd_col_kernel<T, E0><<<grid, e.C * tps, smem, s>>>(e); break;
+    case E1: etd_col_kernel<T, E1><<<grid, e.C * tps, smem, s>>>(e); break;
+    case E2S: etd_col_kernel<T, E2S><<<grid, e.C * tps, smem, s>>>(e); break;
+    case E3: etd_col_kernel<T, E3><<<grid, e.C * tps, smem, s>>>(e); break;
+    case E4: etd_col_kernel<T, E4><<<grid, e.C * tps, smem, s>>>(e); break;
+    case E5: etd_col_kernel<T, E5><<<grid, e.C * tps, smem, s>>>(e); break;
+    case E6: etd_col_kernel<T, E6><<<grid, e.C * tps, smem, s>>>(e); break;
+    default: etd_col_kernel<T, E7><<<grid, e.C * tps, smem, s>>>(e); break;
+  }
   return cudaGetLastError();
 }
 
@@ -413,8 +472,8 @@ static mjx_status etd_run(const void* plan, const mjx_grid2d* g, const mjx_etd_p
     int dev = 0, optin = 0;
     MJX_CUDA_TRY(cudaGetDevice(&dev));
     MJX_CUDA_TRY(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-    MJX_CUDA_TRY(cudaFuncSetAttribute(etd_col_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
-    MJX_CUDA_TRY(cudaFuncSetAttribute(etd_col_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
+    MJX_TRY(etd_col_attrs<float>(optin));
+    MJX_TRY(etd_col_attrs<double>(optin));
     return MJX_OK;
   }));
   const int nf = pb->nfields, rx = pb->reaction;
