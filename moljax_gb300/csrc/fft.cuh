@@ -178,7 +178,7 @@ __device__ __forceinline__ void stockham_pass(cx<T>* buf, int n, int p, int tps,
 // All threads of the block must call it; threads with tid >= nseq*tps only join the
 // barriers.  The caller must __syncthreads() after filling buf; on return buf is complete.
 template <typename T, bool INV, bool COLMAJOR>
-__device__ void fft_smem(cx<T>* buf, int n, int log2n, int nseq, int ss, int es,
+__device__ __forceinline__ void fft_smem_inl(cx<T>* buf, int n, int log2n, int nseq, int ss, int es,
                          const cx<T>* __restrict__ tw, int tid, int s0 = 0) {
   const int tps = n >= 16 ? pdiv(n, 16) : 1;
   const bool active = tid < nseq * tps;
@@ -201,4 +201,12 @@ __device__ void fft_smem(cx<T>* buf, int n, int log2n, int nseq, int ss, int es,
   else if (rem == 1) stockham_pass<T, 2, INV, !COLMAJOR>(buf, n, p, tps, lt, base, es, active, tw);
 }
 
+
+// fft_smem_inl is always inlined, so that a caller passing compile-time lengths gets the
+// index arithmetic and the radix schedule folded; fft_smem leaves the choice to the compiler.
+template <typename T, bool INV, bool COLMAJOR>
+__device__ void fft_smem(cx<T>* buf, int n, int log2n, int nseq, int ss, int es, const cx<T>* __restrict__ tw,
+                         int tid, int s0 = 0) {
+  fft_smem_inl<T, INV, COLMAJOR>(buf, n, log2n, nseq, ss, es, tw, tid, s0);
+}
 }  // namespace mjx

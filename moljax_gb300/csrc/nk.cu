@@ -624,6 +624,18 @@ __device__ __forceinline__ void ff_dot_acc(float& hi, float& lo, float a, float 
   hi = s;
 }
 
+// warp sum of float-float values (hi, lo), a two-sum per step, the same order in every lane:
+// the reduction stays on the FP32 pipe (an FP64 add per step waits on GB300's narrow FP64 units)
+__device__ __forceinline__ void ff_warp_sum(float& hi, float& lo) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const float oh = __shfl_xor_sync(0xffffffffu, hi, o), ol = __shfl_xor_sync(0xffffffffu, lo, o);
+    const float s = __fadd_rn(hi, oh);
+    lo = __fadd_rn(lo, __fadd_rn(ol, ff_2sum_err(hi, oh, s)));
+    hi = s;
+  }
+}
+
 // cycle start from |V_0|^2 = s (as gmres_init_kernel; in the graph Newton loop the first-cycle
 // flag, tolerance and restart come from NewtonDev)
 __device__ void gmres_start(GmresState* gs, double s, int first, double tol, int m) {
@@ -1073,17 +1085,12 @@ __global__ void __launch_bounds__(256) nka_dots_kernel(const __grid_constant__ N
 #pragma unroll
       for (int u = 0; u < 4; ++u) ff_dot_acc(hi[u], lo[u], v[u], tp);
     }
-    double acc[4];
 #pragma unroll
-    for (int u = 0; u < 4; ++u) acc[u] = (double)hi[u] + (double)lo[u];
-    for (int o = 16; o > 0; o >>= 1) {
-#pragma unroll
-      for (int u = 0; u < 4; ++u) acc[u] += __shfl_xor_sync(0xffffffffu, acc[u], o);
-    }
+    for (int u = 0; u < 4; ++u) ff_warp_sum(hi[u], lo[u]);
     if (lane == 0) {
 #pragma unroll
       for (int u = 0; u < 4; ++u)
-        if (i0 + u <= jv) red[i0 + u][warp] = acc[u];
+        if (i0 + u <= jv) red[i0 + u][warp] = (double)hi[u] + (double)lo[u];
     }
   }
   __syncthreads();
@@ -1116,7 +1123,7 @@ __global__ void __launch_bounds__(256) nka_orth_kernel(const __grid_constant__ N
   float hc[NK_MAXM];
   for (int i = 0; i <= jv; ++i) hc[i] = (float)gs->H[i * NK_MAXM + jv];
   float* vn = a.V + (long long)(jv + 1) * N2;
-  double acc = 0.0;
+  float nh = 0.f, nl = 0.f;  // |V_{j+1}|^2 partial in float-float
   for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < N2;
        p += (long long)gridDim.x * blockDim.x) {
     float x = a.t[p];
@@ -1131,11 +1138,11 @@ __global__ void __launch_bounds__(256) nka_orth_kernel(const __grid_constant__ N
     }
     for (; i <= jv; ++i) x -= hc[i] * a.V[(long long)i * N2 + p];
     vn[p] = x;
-    acc += (double)x * (double)x;
+    ff_dot_acc(nh, nl, x, x);
   }
   __shared__ double red[8];
-  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  ff_warp_sum(nh, nl);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = (double)nh + (double)nl;
   __syncthreads();
   if (threadIdx.x == 0) {
     double s = 0.0;

@@ -99,7 +99,10 @@ template <typename T> __device__ __forceinline__ bool finite_(T v) { return isfi
 // ------------------------------------------------------------------ row pass
 template <typename T> struct Occ { static constexpr int row = sizeof(T) == 4 ? 4 : 2, col = sizeof(T) == 4 ? 2 : 1; };
 
-template <typename T, int RX>
+// LOG2N > 0: the row length 2^LOG2N and one sequence per CTA are compile-time constants
+// (FP32 rows of 2048 and 4096 points), so that the transform's index arithmetic and radix
+// schedule fold into the code; LOG2N = 0 reads both from the arguments.
+template <typename T, int RX, int LOG2N = 0>
 __global__ void __launch_bounds__(256, Occ<T>::row) row_kernel(const __grid_constant__ RowArgs<T> a) {
   typedef cx<T> C;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -107,11 +110,12 @@ __global__ void __launch_bounds__(256, Occ<T>::row) row_kernel(const __grid_cons
   const DevState* st = a.st;
   if (st != nullptr && st->done) return;
 
-  const int n = a.n, half = n >> 1;
+  const int n = LOG2N ? (1 << LOG2N) : a.n, half = n >> 1;
+  const int log2n = LOG2N ? LOG2N : a.log2n, nseq = LOG2N ? 1 : a.nseq;
   const int tps = n >= 16 ? n / 16 : 1;
   const int tid = threadIdx.x;
   const int s_loc = tid / tps, lt = tid % tps;
-  const int seq0 = blockIdx.x * a.nseq;
+  const int seq0 = blockIdx.x * nseq;
   const int q = seq0 / a.nrows;  // uniform within the CTA (nrows % nseq == 0)
   const RowPair pr = a.pr[q];
   const int flags = pr.flags;
@@ -142,7 +146,8 @@ __global__ void __launch_bounds__(256, Occ<T>::row) row_kernel(const __grid_cons
       }
     }
     __syncthreads();
-    fft_smem<T, true, false>(buf, n, a.log2n, a.nseq, n, 1, a.tw, tid);
+    if (LOG2N) fft_smem_inl<T, true, false>(buf, n, log2n, nseq, n, 1, a.tw, tid);
+    else fft_smem<T, true, false>(buf, n, log2n, nseq, n, 1, a.tw, tid);
   } else {
     const T* ra = rin + pr.ra + y * a.rstride;
     const T* rb = rin + pr.rb + y * a.rstride;
@@ -226,7 +231,8 @@ __global__ void __launch_bounds__(256, Occ<T>::row) row_kernel(const __grid_cons
   // 3. r2c and split into the two half spectra
   if (flags & ROW_STORE_SPEC) {
     __syncthreads();
-    fft_smem<T, false, false>(buf, n, a.log2n, a.nseq, n, 1, a.tw, tid);
+    if (LOG2N) fft_smem_inl<T, false, false>(buf, n, log2n, nseq, n, 1, a.tw, tid);
+    else fft_smem<T, false, false>(buf, n, log2n, nseq, n, 1, a.tw, tid);
     C* A = a.spec + ((flags & ROW_SPEC_ALT) ? pr.oa : pr.sa) + y * a.ldc;
     C* B = a.spec + ((flags & ROW_SPEC_ALT) ? pr.ob : pr.sb) + y * a.ldc;
 #pragma unroll
@@ -570,6 +576,16 @@ cudaError_t launch_row(const RowArgs<T>& a0, cudaStream_t s) {
     }
   }
   const size_t smem = row_smem(a.n, a.nseq, sizeof(T));
+  if constexpr (sizeof(T) == 4) {
+    if (a.n == 4096 && a.nseq == 1) {
+      row_kernel<T, RX, 12><<<grid, tps, smem, s>>>(a);
+      return cudaGetLastError();
+    }
+    if (a.n == 2048 && a.nseq == 1) {
+      row_kernel<T, RX, 11><<<grid, tps, smem, s>>>(a);
+      return cudaGetLastError();
+    }
+  }
   row_kernel<T, RX><<<grid, a.nseq * tps, smem, s>>>(a);
   return cudaGetLastError();
 }
@@ -639,6 +655,13 @@ mjx_status ensure_kernel_attrs() {
     MJX_TRY(raise_smem(row_kernel<double, RX_NONE>, optin));
     MJX_TRY(raise_smem(row_kernel<double, RX_GRAY_SCOTT>, optin));
     MJX_TRY(raise_smem(row_kernel<double, RX_FISHER>, optin));
+    MJX_TRY(raise_smem(row_kernel<float, RX_NONE, 11>, optin));
+    MJX_TRY(raise_smem(row_kernel<float, RX_GRAY_SCOTT, 11>, optin));
+    MJX_TRY(raise_smem(row_kernel<float, RX_FISHER, 11>, optin));
+    MJX_TRY(raise_smem(row_kernel<float, RX_NONE, 12>, optin));
+    MJX_TRY(raise_smem(row_kernel<float, RX_GRAY_SCOTT, 12>, optin));
+    MJX_TRY(raise_smem(row_kernel<float, RX_FISHER, 12>, optin));
+
     MJX_TRY(raise_smem(col_kernel<float>, optin));
     MJX_TRY(raise_smem(col_kernel<double>, optin));
     return MJX_OK;
