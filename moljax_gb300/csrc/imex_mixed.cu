@@ -58,7 +58,8 @@ struct MColArgs {
   MJob job[8];
 };
 
-template <int NT, int MINB>
+// LOG2NY, CN: compile-time column length and tile width (mcol_tile), launched with NT threads
+template <int NT, int MINB, int LOG2NY = 0, int CN = 0>
 __global__ void __launch_bounds__(NT, MINB) mcol_kernel(const __grid_constant__ MColArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   float2* buf = reinterpret_cast<float2*>(smem_raw);
@@ -75,7 +76,7 @@ __global__ void __launch_bounds__(NT, MINB) mcol_kernel(const __grid_constant__ 
   t.pa = a.pa; t.pb = a.pb; t.za = a.za; t.zb = a.zb;
   t.lamx = a.lamx; t.lamy = a.lamy; t.tw = a.tw;
   t.hA = (float)(0.5 * h * jb.D); t.hB = (float)(0.25 * h * jb.D); t.nrm = a.inv_norm;
-  mcol_tile(buf, t, threadIdx.x, blockDim.x);
+  mcol_tile<LOG2NY, CN, LOG2NY ? NT : 0>(buf, t, threadIdx.x, blockDim.x);
 }
 
 __global__ void f32_to_f64(const float* in, double* out, long long n) {
@@ -229,7 +230,8 @@ static cudaError_t mcol(const MColArgs& c, cudaStream_t s) {
   const size_t smem = (size_t)sp_size(c.ny * 2 * c.C) * sizeof(float2);
   dim3 grid((c.ncols + c.C - 1) / c.C, c.njobs);
   const int nt = 2 * c.C * tps;
-  if (nt <= 256) mcol_kernel<256, 4><<<grid, nt, smem, s>>>(c);
+  if (c.ny == 1024 && c.C == 4 && nt == 512) mcol_kernel<512, 2, 10, 4><<<grid, nt, smem, s>>>(c);
+  else if (nt <= 256) mcol_kernel<256, 4><<<grid, nt, smem, s>>>(c);
   else mcol_kernel<512, 2><<<grid, nt, smem, s>>>(c);
   return cudaGetLastError();
 }
@@ -351,6 +353,7 @@ mjx_status ensure_mix_attrs() {
     MJX_CUDA_TRY(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
     MJX_CUDA_TRY(cudaFuncSetAttribute(mcol_kernel<256, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
     MJX_CUDA_TRY(cudaFuncSetAttribute(mcol_kernel<512, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
+    MJX_CUDA_TRY(cudaFuncSetAttribute(mcol_kernel<512, 2, 10, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
     return MJX_OK;
   });
 }

@@ -90,16 +90,24 @@ struct MColTile {
 // other's load latency (the column passes are latency-bound at 1024^2, where the
 // whole working set sits in L2).  Only ny = 4096 needs 512-thread CTAs.
 // The caller synchronises the block before buf is reused for another tile.
-__device__ __forceinline__ void mcol_tile(float2* buf, const MColTile& t, int tid, int nth) {
+// LOG2NY, CN, NTH > 0 fix the column length, the tile width and the thread count at compile
+// time (the 1024-row passes of the benchmark size), so that the index arithmetic and the
+// transforms' radix schedule fold into the code; 0 reads them at run time.
+__host__ __device__ constexpr int mc_log2(int v) { return v <= 1 ? 0 : 1 + mc_log2(v >> 1); }
+
+template <int LOG2NY = 0, int CN = 0, int NTH = 0>
+__device__ __forceinline__ void mcol_tile(float2* buf, const MColTile& t, int tid, int nth_rt) {
   // the tile holds two outputs side by side (W = 2C) where a job writes two transforms
   // (C1 split, C3 end); the single-output jobs of C2 use a compact tile (W = C), whose
   // column transforms then walk shared memory with half the stride
   const int type = t.type;
-  const int Cn = t.C, W = (type == MC_FULL_END || type == MC_HALF_MID) ? Cn : 2 * Cn;
+  const int nth = NTH ? NTH : nth_rt;
+  const int Cn = CN ? CN : t.C, W = (type == MC_FULL_END || type == MC_HALF_MID) ? Cn : 2 * Cn;
   const int kx0 = t.kx0;
-  const int ny = t.ny;
+  const int ny = LOG2NY ? (1 << LOG2NY) : t.ny;
+  const int log2ny = LOG2NY ? LOG2NY : t.log2ny;
   const int total = ny * Cn;
-  const int lc = __ffs(Cn) - 1;  // the tile width is a power of two
+  const int lc = CN ? mc_log2(CN) : __ffs(Cn) - 1;  // the tile width is a power of two
   const long long ldc = t.ldc;
   const float hA = t.hA, hB = t.hB, nrm = t.nrm;
 
@@ -123,7 +131,8 @@ __device__ __forceinline__ void mcol_tile(float2* buf, const MColTile& t, int ti
       }
     }
     __syncthreads();
-    fft_smem<float, false, true>(buf, ny, t.log2ny, type == MC_MID_BOTH ? W : Cn, 1, W, t.tw, tid);
+    if (LOG2NY) fft_smem_inl<float, false, true>(buf, ny, log2ny, type == MC_MID_BOTH ? W : Cn, 1, W, t.tw, tid);
+    else fft_smem<float, false, true>(buf, ny, log2ny, type == MC_MID_BOTH ? W : Cn, 1, W, t.tw, tid);
   }
 
   // float-float combine, element by element
@@ -180,7 +189,8 @@ __device__ __forceinline__ void mcol_tile(float2* buf, const MColTile& t, int ti
   if (type == MC_FULL_END) return;
   __syncthreads();
   if (type == MC_MID_BOTH) {  // only the right (MC_HALF_MID) half goes back
-    fft_smem<float, true, true>(buf, ny, t.log2ny, Cn, 1, W, t.tw, tid, Cn);
+    if (LOG2NY) fft_smem_inl<float, true, true>(buf, ny, log2ny, Cn, 1, W, t.tw, tid, Cn);
+    else fft_smem<float, true, true>(buf, ny, log2ny, Cn, 1, W, t.tw, tid, Cn);
     for (int e = tid; e < ny * Cn; e += nth) {
       const int ky = e >> lc, c = e & (Cn - 1), kx = kx0 + c;
       if (kx < t.ncols) t.zb[t.off + ky * ldc + kx] = buf[sp(ky * W + Cn + c)];
@@ -188,7 +198,8 @@ __device__ __forceinline__ void mcol_tile(float2* buf, const MColTile& t, int ti
     return;
   }
   const int nseq = (type == MC_HALF_MID) ? Cn : W;
-  fft_smem<float, true, true>(buf, ny, t.log2ny, nseq, 1, W, t.tw, tid);
+  if (LOG2NY) fft_smem_inl<float, true, true>(buf, ny, log2ny, nseq, 1, W, t.tw, tid);
+  else fft_smem<float, true, true>(buf, ny, log2ny, nseq, 1, W, t.tw, tid);
   const int lns = __ffs(nseq) - 1;
   for (int e = tid; e < ny * nseq; e += nth) {
     const int ky = e >> lns, col = e & (nseq - 1);
