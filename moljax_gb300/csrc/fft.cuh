@@ -209,4 +209,26 @@ __device__ void fft_smem(cx<T>* buf, int n, int log2n, int nseq, int ss, int es,
                          int tid, int s0 = 0) {
   fft_smem_inl<T, INV, COLMAJOR>(buf, n, log2n, nseq, ss, es, tw, tid, s0);
 }
+
+// The same transform in radix-4 passes (a final radix-2 pass when log2 n is odd), n/4
+// threads per sequence with one butterfly each: four times the threads of the radix-16
+// schedule and about a third of the arithmetic per thread.  Used for short FP64 transforms,
+// where each warp of the radix-16 schedule would keep only n/16 lanes busy and wait on
+// GB300's narrow FP64 pipe.  Same layout, barriers and output order as fft_smem.
+template <typename T, bool INV, bool COLMAJOR>
+__device__ void fft_smem_r4(cx<T>* buf, int n, int log2n, int nseq, int ss, int es, const cx<T>* __restrict__ tw,
+                            int tid, int s0 = 0) {
+  const int tps = n >= 4 ? pdiv(n, 4) : 1;
+  const bool active = tid < nseq * tps;
+  int lt, s;
+  if (COLMAJOR) { s = pmod(tid, nseq); lt = pdiv(tid, nseq); }
+  else { lt = pmod(tid, tps); s = pdiv(tid, tps); }
+  const int base = (s + s0) * ss;
+  int p = 1;
+  for (int rem = log2n; rem >= 2; rem -= 2) {
+    stockham_pass<T, 4, INV, !COLMAJOR>(buf, n, p, tps, lt, base, es, active, tw);
+    p <<= 2;
+  }
+  if (log2n & 1) stockham_pass<T, 2, INV, !COLMAJOR>(buf, n, p, tps, lt, base, es, active, tw);
+}
 }  // namespace mjx

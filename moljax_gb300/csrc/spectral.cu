@@ -102,7 +102,8 @@ template <typename T> struct Occ { static constexpr int row = sizeof(T) == 4 ? 4
 // LOG2N > 0: the row length 2^LOG2N and one sequence per CTA are compile-time constants
 // (FP32 rows of 2048 and 4096 points), so that the transform's index arithmetic and radix
 // schedule fold into the code; LOG2N = 0 reads both from the arguments.
-template <typename T, int RX, int LOG2N = 0>
+// R4: radix-4 transforms with n/4 threads per sequence (short FP64 rows, fft_smem_r4).
+template <typename T, int RX, int LOG2N = 0, bool R4 = false>
 __global__ void __launch_bounds__(256, Occ<T>::row) row_kernel(const __grid_constant__ RowArgs<T> a) {
   typedef cx<T> C;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -112,7 +113,7 @@ __global__ void __launch_bounds__(256, Occ<T>::row) row_kernel(const __grid_cons
 
   const int n = LOG2N ? (1 << LOG2N) : a.n, half = n >> 1;
   const int log2n = LOG2N ? LOG2N : a.log2n, nseq = LOG2N ? 1 : a.nseq;
-  const int tps = n >= 16 ? n / 16 : 1;
+  const int tps = R4 ? (n >= 4 ? n / 4 : 1) : (n >= 16 ? n / 16 : 1);
   const int tid = threadIdx.x;
   const int s_loc = tid / tps, lt = tid % tps;
   const int seq0 = blockIdx.x * nseq;
@@ -146,7 +147,8 @@ __global__ void __launch_bounds__(256, Occ<T>::row) row_kernel(const __grid_cons
       }
     }
     __syncthreads();
-    if (LOG2N) fft_smem_inl<T, true, false>(buf, n, log2n, nseq, n, 1, a.tw, tid);
+    if (R4) fft_smem_r4<T, true, false>(buf, n, log2n, nseq, n, 1, a.tw, tid);
+    else if (LOG2N) fft_smem_inl<T, true, false>(buf, n, log2n, nseq, n, 1, a.tw, tid);
     else fft_smem<T, true, false>(buf, n, log2n, nseq, n, 1, a.tw, tid);
   } else {
     const T* ra = rin + pr.ra + y * a.rstride;
@@ -231,7 +233,8 @@ __global__ void __launch_bounds__(256, Occ<T>::row) row_kernel(const __grid_cons
   // 3. r2c and split into the two half spectra
   if (flags & ROW_STORE_SPEC) {
     __syncthreads();
-    if (LOG2N) fft_smem_inl<T, false, false>(buf, n, log2n, nseq, n, 1, a.tw, tid);
+    if (R4) fft_smem_r4<T, false, false>(buf, n, log2n, nseq, n, 1, a.tw, tid);
+    else if (LOG2N) fft_smem_inl<T, false, false>(buf, n, log2n, nseq, n, 1, a.tw, tid);
     else fft_smem<T, false, false>(buf, n, log2n, nseq, n, 1, a.tw, tid);
     C* A = a.spec + ((flags & ROW_SPEC_ALT) ? pr.oa : pr.sa) + y * a.ldc;
     C* B = a.spec + ((flags & ROW_SPEC_ALT) ? pr.ob : pr.sb) + y * a.ldc;
@@ -298,7 +301,8 @@ __device__ __forceinline__ T multiplier(int mul, T hD, T lam, int pw) {
 
 template <typename T> struct ColThreads { static constexpr int v = sizeof(T) == 4 ? 1024 : 512; };
 
-template <typename T>
+// R4: radix-4 column transforms with ny/4 threads per column (short FP64 columns).
+template <typename T, bool R4 = false>
 __global__ void __launch_bounds__(ColThreads<T>::v, 1) col_kernel(const __grid_constant__ ColArgs<T> a) {
   typedef cx<T> C;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -334,7 +338,10 @@ __global__ void __launch_bounds__(ColThreads<T>::v, 1) col_kernel(const __grid_c
   }
   __syncthreads();
   const int dirs = jb.dirs ? jb.dirs : 3;
-  if (dirs & 1) fft_smem<T, false, true>(buf, ny, a.log2ny, Cn, 1, W, a.tw, tid);
+  if (dirs & 1) {
+    if (R4) fft_smem_r4<T, false, true>(buf, ny, a.log2ny, Cn, 1, W, a.tw, tid);
+    else fft_smem<T, false, true>(buf, ny, a.log2ny, Cn, 1, W, a.tw, tid);
+  }
   const T jscale = jb.scale != 0.0 ? (T)jb.scale : a.scale;
 
   const double h = a.st != nullptr ? a.st->dtc : a.hfixed;
@@ -401,7 +408,10 @@ __global__ void __launch_bounds__(ColThreads<T>::v, 1) col_kernel(const __grid_c
     if (nout > 1) buf[sp(ky * W + Cn + c)] = cscale(v, jscale * multiplier<T>(jb.mul, hD1, lam, jb.pow[1]));
   }
   __syncthreads();
-  if (dirs & 2) fft_smem<T, true, true>(buf, ny, a.log2ny, W, 1, W, a.tw, tid);
+  if (dirs & 2) {
+    if (R4) fft_smem_r4<T, true, true>(buf, ny, a.log2ny, W, 1, W, a.tw, tid);
+    else fft_smem<T, true, true>(buf, ny, a.log2ny, W, 1, W, a.tw, tid);
+  }
 
   const int lw = __ffs(W) - 1;  // W = Cn or 2 Cn
   for (int e = tid; e < ny * W; e += nth) {
@@ -575,6 +585,19 @@ cudaError_t launch_row(const RowArgs<T>& a0, cudaStream_t s) {
       return cudaGetLastError();
     }
   }
+  if constexpr (sizeof(T) == 8) {
+    // short FP64 rows (no error partials, whose CTA count is fixed): radix-4 transforms,
+    // n/4 threads per sequence, at most 256 threads per CTA, every SM covered where possible
+    if (!partials && a.n >= 4 && a.n <= 256) {
+      RowArgs<T> b = a;
+      const int tps4 = a.n / 4;
+      while (b.nseq > 1 && b.nseq * tps4 > 256) b.nseq >>= 1;
+      while (b.nseq > 1 && b.npairs * b.nrows / b.nseq < 152) b.nseq >>= 1;
+      const int grid4 = b.npairs * b.nrows / b.nseq;
+      row_kernel<T, RX, 0, true><<<grid4, b.nseq * tps4, row_smem(b.n, b.nseq, sizeof(T)), s>>>(b);
+      return cudaGetLastError();
+    }
+  }
   const size_t smem = row_smem(a.n, a.nseq, sizeof(T));
   if constexpr (sizeof(T) == 4) {
     if (a.n == 4096 && a.nseq == 1) {
@@ -599,6 +622,19 @@ cudaError_t launch_col(const ColArgs<T>& a0, cudaStream_t s) {
   // small grids: narrower tiles until the pass covers every SM (as launch_row)
   const long long planes = a.nplanes > 1 ? a.nplanes : 1;
   while (a.C > 1 && (long long)((a.ncols + a.C - 1) / a.C) * a.njobs * planes < 152) a.C >>= 1;
+  if constexpr (sizeof(T) == 8) {
+    // short FP64 columns: radix-4 transforms, ny/4 threads per column, narrower tiles to
+    // stay within the thread cap
+    if (a.ny >= 4 && a.ny <= 256) {
+      ColArgs<T> b = a;
+      const int tps4 = a.ny / 4;
+      while (b.C > 1 && b.C * maxout * tps4 > ColThreads<T>::v) b.C >>= 1;
+      dim3 g4((b.ncols + b.C - 1) / b.C, b.njobs, b.nplanes > 1 ? b.nplanes : 1);
+      const size_t sm4 = (size_t)sp_size(b.ny * b.C * maxout) * sizeof(cx<T>);
+      col_kernel<T, true><<<g4, b.C * maxout * tps4, sm4, s>>>(b);
+      return cudaGetLastError();
+    }
+  }
   dim3 grid((a.ncols + a.C - 1) / a.C, a.njobs, a.nplanes > 1 ? a.nplanes : 1);
   const size_t smem = (size_t)sp_size(a.ny * a.C * maxout) * sizeof(cx<T>);
   col_kernel<T><<<grid, a.C * maxout * tps, smem, s>>>(a);
@@ -664,6 +700,10 @@ mjx_status ensure_kernel_attrs() {
 
     MJX_TRY(raise_smem(col_kernel<float>, optin));
     MJX_TRY(raise_smem(col_kernel<double>, optin));
+    MJX_TRY(raise_smem(col_kernel<double, true>, optin));
+    MJX_TRY(raise_smem(row_kernel<double, RX_NONE, 0, true>, optin));
+    MJX_TRY(raise_smem(row_kernel<double, RX_GRAY_SCOTT, 0, true>, optin));
+    MJX_TRY(raise_smem(row_kernel<double, RX_FISHER, 0, true>, optin));
     return MJX_OK;
   });
 }
