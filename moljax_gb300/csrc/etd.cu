@@ -172,7 +172,8 @@ template <typename T> struct EArgs {
 template <typename T> struct EThreads { static constexpr int v = sizeof(T) == 4 ? 1024 : 512; };
 
 // The stage type is a template argument, so that each instance holds only its own operands.
-template <typename T, int TYPE>
+// R4: radix-4 column transforms with ny/4 threads per column (short FP64 columns).
+template <typename T, int TYPE, bool R4 = false>
 __global__ void __launch_bounds__(EThreads<T>::v, 1) etd_col_kernel(const __grid_constant__ EArgs<T> a) {
   typedef cx<T> Cx;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -193,7 +194,8 @@ __global__ void __launch_bounds__(EThreads<T>::v, 1) etd_col_kernel(const __grid
     buf[sp(ky * W + c)] = kx < a.ncols ? in0[fo + ky * ldc + kx] : mk<Cx>((T)0, (T)0);
   }
   __syncthreads();
-  fft_smem<T, false, true>(buf, ny, a.log2ny, Cn, 1, W, a.tw, tid);
+  if (R4) fft_smem_r4<T, false, true>(buf, ny, a.log2ny, Cn, 1, W, a.tw, tid);
+  else fft_smem<T, false, true>(buf, ny, a.log2ny, Cn, 1, W, a.tw, tid);
 
   // The stage combination, two elements per thread at a time: the operands are read and
   // written in place, so the compiler cannot issue a later element's loads before an
@@ -282,7 +284,8 @@ __global__ void __launch_bounds__(EThreads<T>::v, 1) etd_col_kernel(const __grid
   }
   if (type == E0) return;
   __syncthreads();
-  fft_smem<T, true, true>(buf, ny, a.log2ny, Cn, 1, W, a.tw, tid);
+  if (R4) fft_smem_r4<T, true, true>(buf, ny, a.log2ny, Cn, 1, W, a.tw, tid);
+  else fft_smem<T, true, true>(buf, ny, a.log2ny, Cn, 1, W, a.tw, tid);
   Cx* dst = type >= E4 ? a.zu : a.zx;
   for (int e = tid; e < ny * Cn; e += nth) {
     const int ky = e >> lc, c = e & (Cn - 1), kx = kx0 + c;
@@ -382,31 +385,49 @@ static EtdPlan<T> build_etd(const void* plan, const mjx_grid2d* g, int nf, doubl
   return P;
 }
 
-template <typename T>
+template <typename T, bool R4>
 static mjx_status etd_col_attrs(int optin) {
-  const void* k[8] = {(const void*)etd_col_kernel<T, E0>, (const void*)etd_col_kernel<T, E1>,
-                      (const void*)etd_col_kernel<T, E2S>, (const void*)etd_col_kernel<T, E3>,
-                      (const void*)etd_col_kernel<T, E4>, (const void*)etd_col_kernel<T, E5>,
-                      (const void*)etd_col_kernel<T, E6>, (const void*)etd_col_kernel<T, E7>};
+  const void* k[8] = {(const void*)etd_col_kernel<T, E0, R4>, (const void*)etd_col_kernel<T, E1, R4>,
+                      (const void*)etd_col_kernel<T, E2S, R4>, (const void*)etd_col_kernel<T, E3, R4>,
+                      (const void*)etd_col_kernel<T, E4, R4>, (const void*)etd_col_kernel<T, E5, R4>,
+                      (const void*)etd_col_kernel<T, E6, R4>, (const void*)etd_col_kernel<T, E7, R4>};
   for (int i = 0; i < 8; ++i)
     MJX_CUDA_TRY(cudaFuncSetAttribute(k[i], cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
   return MJX_OK;
 }
 
-template <typename T>
-static cudaError_t etd_col(const EArgs<T>& e, cudaStream_t s) {
+template <typename T, int TYPE>
+static void etd_col_launch(const EArgs<T>& e, cudaStream_t s) {
   const int tps = e.ny >= 16 ? e.ny / 16 : 1;
+  if constexpr (sizeof(T) == 8) {
+    // FP64 columns of at most 256 points: radix-4 transforms (ny/4 threads per column),
+    // narrower tiles within the thread cap
+    if (e.ny >= 4 && e.ny <= 256) {
+      EArgs<T> b = e;
+      const int tps4 = e.ny / 4;
+      while (b.C > 1 && b.C * tps4 > EThreads<T>::v) b.C >>= 1;
+      dim3 g4((b.ncols + b.C - 1) / b.C, b.njobs);
+      const size_t sm4 = (size_t)sp_size(b.ny * b.C) * 2 * sizeof(T);
+      etd_col_kernel<T, TYPE, true><<<g4, b.C * tps4, sm4, s>>>(b);
+      return;
+    }
+  }
   dim3 grid((e.ncols + e.C - 1) / e.C, e.njobs);
   const size_t smem = (size_t)sp_size(e.ny * e.C) * 2 * sizeof(T);
+  etd_col_kernel<T, TYPE><<<grid, e.C * tps, smem, s>>>(e);
+}
+
+template <typename T>
+static cudaError_t etd_col(const EArgs<T>& e, cudaStream_t s) {
   switch (e.type) {
-    case E0: etd_col_kernel<T, E0><<<grid, e.C * tps, smem, s>>>(e); break;
-    case E1: etd_col_kernel<T, E1><<<grid, e.C * tps, smem, s>>>(e); break;
-    case E2S: etd_col_kernel<T, E2S><<<grid, e.C * tps, smem, s>>>(e); break;
-    case E3: etd_col_kernel<T, E3><<<grid, e.C * tps, smem, s>>>(e); break;
-    case E4: etd_col_kernel<T, E4><<<grid, e.C * tps, smem, s>>>(e); break;
-    case E5: etd_col_kernel<T, E5><<<grid, e.C * tps, smem, s>>>(e); break;
-    case E6: etd_col_kernel<T, E6><<<grid, e.C * tps, smem, s>>>(e); break;
-    default: etd_col_kernel<T, E7><<<grid, e.C * tps, smem, s>>>(e); break;
+    case E0: etd_col_launch<T, E0>(e, s); break;
+    case E1: etd_col_launch<T, E1>(e, s); break;
+    case E2S: etd_col_launch<T, E2S>(e, s); break;
+    case E3: etd_col_launch<T, E3>(e, s); break;
+    case E4: etd_col_launch<T, E4>(e, s); break;
+    case E5: etd_col_launch<T, E5>(e, s); break;
+    case E6: etd_col_launch<T, E6>(e, s); break;
+    default: etd_col_launch<T, E7>(e, s); break;
   }
   return cudaGetLastError();
 }
@@ -472,8 +493,9 @@ static mjx_status etd_run(const void* plan, const mjx_grid2d* g, const mjx_etd_p
     int dev = 0, optin = 0;
     MJX_CUDA_TRY(cudaGetDevice(&dev));
     MJX_CUDA_TRY(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
-    MJX_TRY(etd_col_attrs<float>(optin));
-    MJX_TRY(etd_col_attrs<double>(optin));
+    MJX_TRY((etd_col_attrs<float, false>(optin)));
+    MJX_TRY((etd_col_attrs<double, false>(optin)));
+    MJX_TRY((etd_col_attrs<double, true>(optin)));
     return MJX_OK;
   }));
   const int nf = pb->nfields, rx = pb->reaction;

@@ -31,13 +31,14 @@ struct GrkRowArgs {
   double dt, F, k;
 };
 
-template <typename T>
+// R4: radix-4 transforms with n/4 threads per row (short FP64 rows, fft_smem_r4)
+template <typename T, bool R4 = false>
 __global__ void __launch_bounds__(256) grk_row_kernel(const __grid_constant__ GrkRowArgs<T> a) {
   typedef cx<T> C;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* buf = reinterpret_cast<C*>(smem_raw);
   const int n = a.n, half = n >> 1;
-  const int tps = n >= 16 ? n / 16 : 1;
+  const int tps = R4 ? (n >= 4 ? n / 4 : 1) : (n >= 16 ? n / 16 : 1);
   const int tid = threadIdx.x;
   const int s_loc = tid / tps, lt = tid % tps;
   const bool active = s_loc < a.nseq;
@@ -63,7 +64,8 @@ __global__ void __launch_bounds__(256) grk_row_kernel(const __grid_constant__ Gr
     }
   }
   __syncthreads();
-  fft_smem<T, true, false>(buf, n, a.log2n, a.nseq, n, 1, a.tw, tid);
+  if (R4) fft_smem_r4<T, true, false>(buf, n, a.log2n, a.nseq, n, 1, a.tw, tid);
+  else fft_smem<T, true, false>(buf, n, a.log2n, a.nseq, n, 1, a.tw, tid);
   const T dt = (T)a.dt, hh = (T)(0.5 * a.dt), d6 = (T)(a.dt / 6.0);
   const T F = (T)a.F, FK = (T)(a.F + a.k);
   const int stage = a.stage;
@@ -96,7 +98,8 @@ __global__ void __launch_bounds__(256) grk_row_kernel(const __grid_constant__ Gr
     }
   }
   __syncthreads();
-  fft_smem<T, false, false>(buf, n, a.log2n, a.nseq, n, 1, a.tw, tid);
+  if (R4) fft_smem_r4<T, false, false>(buf, n, a.log2n, a.nseq, n, 1, a.tw, tid);
+  else fft_smem<T, false, false>(buf, n, a.log2n, a.nseq, n, 1, a.tw, tid);
   if (active) {
     C* A = a.spec + y * a.ldc;
     C* B = a.spec + a.fs + y * a.ldc;
@@ -174,7 +177,9 @@ static mjx_status grk_run(const void* plan, const mjx_grid2d* g, const double* D
     st[q].Ys = q == 0 ? y_out : S;
     st[q].out = q == 3 ? y_out : S;
   }
-  const int tps = nx >= 16 ? nx / 16 : 1;
+  // FP64 rows of at most 256 points: radix-4 transforms (nx/4 threads per row)
+  const bool r4 = sizeof(T) == 8 && nx >= 4 && nx <= 256 && nseq * (nx / 4) <= 256;
+  const int tps = r4 ? nx / 4 : (nx >= 16 ? nx / 16 : 1);
   const unsigned rblocks = (unsigned)(ny / nseq), rthreads = (unsigned)(nseq * tps);
   const size_t rsmem = (size_t)sp_size(nseq * nx) * sizeof(cx<T>);
   static ContextOnce attr;
@@ -184,13 +189,15 @@ static mjx_status grk_run(const void* plan, const mjx_grid2d* g, const double* D
     MJX_CUDA_TRY(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
     MJX_CUDA_TRY(cudaFuncSetAttribute(grk_row_kernel<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
     MJX_CUDA_TRY(cudaFuncSetAttribute(grk_row_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
+    MJX_CUDA_TRY(cudaFuncSetAttribute(grk_row_kernel<double, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin));
     return MJX_OK;
   }));
   auto one_step = [&](cudaStream_t q) -> cudaError_t {
     for (int i = 0; i < 4; ++i) {
       cudaError_t e = launch_col<T>(c, q);
       if (e != cudaSuccess) return e;
-      grk_row_kernel<T><<<rblocks, rthreads, rsmem, q>>>(st[i]);
+      if (r4) grk_row_kernel<T, true><<<rblocks, rthreads, rsmem, q>>>(st[i]);
+      else grk_row_kernel<T><<<rblocks, rthreads, rsmem, q>>>(st[i]);
       if ((e = cudaGetLastError()) != cudaSuccess) return e;
     }
     return cudaSuccess;
