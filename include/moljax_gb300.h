@@ -389,8 +389,9 @@ size_t mjx_nk_vardiff_ws_bytes(int n, int restart);
  * newton_krylov_solve semantics (171-359): FP64 residual, FP32 hand-written
  * JVP and Krylov vectors, left-preconditioned restarted GMRES with the
  * Hessenberg/Givens least squares in FP64 on the GPU, preconditioner
- * (alpha0 I - beta Dbar Lap_D)^-1 (DST diagonal via the odd extension,
- * plan2 = FP32 FD plan of the (2n)^2 periodic grid with the same spacing).
+ * (alpha0 I - beta Dbar Lap_D)^-1 (exact in the DST-II basis: a real DST-II /
+ * DST-III pair of n-point transforms; plan2 = FP32 FD plan of the (2n)^2
+ * periodic grid with the same spacing, whose symbols give the eigenvalues).
  * BE/CN initial guess: explicit Euler (stepping.py:195-196, 242-243) or, with
  * be_guess_previous != 0, y_n.  stats (optional, 3 ints per step): Newton
  * iterations, GMRES iterations, converged. */

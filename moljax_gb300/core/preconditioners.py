@@ -7,9 +7,10 @@
   (preconditioners.py:121-198), applied with torch on padded fields;
 * README form ``DiffusionPreconditioner(D, dx, dt)`` (README.md:148) -- the
   exact diagonal inverse (alpha0 I - kappa Lap_D)^-1 for homogeneous Dirichlet
-  ghosts by the sine transform (DST-II through the odd extension to a periodic
-  box, native spectral pass).  This is the preconditioner of the native
-  Newton-Krylov path.
+  ghosts by the sine transform (here through the odd extension to a periodic
+  box and the native spectral pass).  The native Newton-Krylov driver applies
+  the same inverse inside its Arnoldi step as a real DST-II / DST-III pair of
+  n-point transforms.
 """
 
 from __future__ import annotations
