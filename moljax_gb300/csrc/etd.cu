@@ -400,9 +400,9 @@ template <typename T, int TYPE>
 static void etd_col_launch(const EArgs<T>& e, cudaStream_t s) {
   const int tps = e.ny >= 16 ? e.ny / 16 : 1;
   if constexpr (sizeof(T) == 8) {
-    // FP64 columns of at most 256 points: radix-4 transforms (ny/4 threads per column),
-    // narrower tiles within the thread cap
-    if (e.ny >= 4 && e.ny <= 256) {
+    // FP64 columns of at most 256 points on a small grid (fewer than four warps per SM at
+    // radix 16): radix-4 transforms (ny/4 threads per column), narrower tiles within the cap
+    if (e.ny >= 4 && e.ny <= 256 && (long long)e.ncols * e.njobs * tps < 152LL * 128) {
       EArgs<T> b = e;
       const int tps4 = e.ny / 4;
       while (b.C > 1 && b.C * tps4 > EThreads<T>::v) b.C >>= 1;

@@ -177,8 +177,10 @@ static mjx_status grk_run(const void* plan, const mjx_grid2d* g, const double* D
     st[q].Ys = q == 0 ? y_out : S;
     st[q].out = q == 3 ? y_out : S;
   }
-  // FP64 rows of at most 256 points: radix-4 transforms (nx/4 threads per row)
-  const bool r4 = sizeof(T) == 8 && nx >= 4 && nx <= 256 && nseq * (nx / 4) <= 256;
+  // FP64 rows of at most 256 points on a small grid (fewer than four warps per SM at radix
+  // 16): radix-4 transforms (nx/4 threads per row)
+  const bool r4 = sizeof(T) == 8 && nx >= 4 && nx <= 256 && nseq * (nx / 4) <= 256 &&
+                  (long long)ny * (nx / 16) < 152LL * 128;
   const int tps = r4 ? nx / 4 : (nx >= 16 ? nx / 16 : 1);
   const unsigned rblocks = (unsigned)(ny / nseq), rthreads = (unsigned)(nseq * tps);
   const size_t rsmem = (size_t)sp_size(nseq * nx) * sizeof(cx<T>);

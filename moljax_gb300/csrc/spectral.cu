@@ -586,9 +586,11 @@ cudaError_t launch_row(const RowArgs<T>& a0, cudaStream_t s) {
     }
   }
   if constexpr (sizeof(T) == 8) {
-    // short FP64 rows (no error partials, whose CTA count is fixed): radix-4 transforms,
-    // n/4 threads per sequence, at most 256 threads per CTA, every SM covered where possible
-    if (!partials && a.n >= 4 && a.n <= 256) {
+    // short FP64 rows on a small grid (no error partials, whose CTA count is fixed): radix-4
+    // transforms, n/4 threads per sequence, at most 256 threads per CTA, every SM covered
+    // where possible.  Only when the radix-16 pass would run fewer than four warps per SM:
+    // with more rows the extra passes of radix 4 cost more than the threads gain.
+    if (!partials && a.n >= 4 && a.n <= 256 && (long long)a.npairs * a.nrows * tps < 152LL * 128) {
       RowArgs<T> b = a;
       const int tps4 = a.n / 4;
       while (b.nseq > 1 && b.nseq * tps4 > 256) b.nseq >>= 1;
@@ -623,9 +625,9 @@ cudaError_t launch_col(const ColArgs<T>& a0, cudaStream_t s) {
   const long long planes = a.nplanes > 1 ? a.nplanes : 1;
   while (a.C > 1 && (long long)((a.ncols + a.C - 1) / a.C) * a.njobs * planes < 152) a.C >>= 1;
   if constexpr (sizeof(T) == 8) {
-    // short FP64 columns: radix-4 transforms, ny/4 threads per column, narrower tiles to
-    // stay within the thread cap
-    if (a.ny >= 4 && a.ny <= 256) {
+    // short FP64 columns on a small grid (fewer than four warps per SM at radix 16): radix-4
+    // transforms, ny/4 threads per column, narrower tiles to stay within the thread cap
+    if (a.ny >= 4 && a.ny <= 256 && (long long)a.ncols * a.njobs * planes * tps < 152LL * 128) {
       ColArgs<T> b = a;
       const int tps4 = a.ny / 4;
       while (b.C > 1 && b.C * maxout * tps4 > ColThreads<T>::v) b.C >>= 1;
