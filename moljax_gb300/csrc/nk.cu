@@ -503,6 +503,7 @@ __global__ void nk_scale_j_kernel(float* V, const GmresState* gs, long long N2) 
 // launches the graph once per solve and reads the counters once.
 struct NewtonDev {
   int it, converged, cyc, bt, accepted, lits, max_newton, max_krylov, max_backtrack, restart;
+  int rvalid;  // R and -R hold R(x) and rn its norm (initial residual, or an accepted trial point)
   double rn, rb, res, newton_tol, krylov_tol, damping, backtrack, min_decrease;
 };
 
@@ -527,6 +528,7 @@ __global__ void nd_init_kernel(const double* part, int nblk, NewtonDev* nd, cuda
   nd->res = nd->rn;
   nd->it = 0;
   nd->lits = 0;
+  nd->rvalid = 1;
   nd->converged = nd->rn < nd->newton_tol;
   cudaGraphSetConditional(hN, (!nd->converged && nd->max_newton > 0) ? 1u : 0u);
 }
@@ -1203,15 +1205,29 @@ __global__ void nka_update_kernel(float* dx, const float* V, const GmresState* g
 // CTA (the ticket of nka_last), the one-thread decision that a separate control kernel made
 
 // Newton iteration head: R(x), -R in FP32, |R|^2 partials, dx = 0; the last CTA sets
-// |R|, converged (evaluated before the update, newton_krylov.py:249-254) and the cycle flag
+// |R|, converged (evaluated before the update, newton_krylov.py:249-254) and the cycle flag.
+// When R(x) is already at hand (nd->rvalid) the pass only clears dx.
 __global__ void nd_resid_head_kernel(const double* __restrict__ x, const double* __restrict__ cst,
                                      double* __restrict__ R, float* __restrict__ b32, float* __restrict__ dx,
                                      double* part, const NKConsts* __restrict__ K, int n, double idx2,
                                      double idy2, NewtonDev* nd, unsigned* ticket,
                                      cudaGraphConditionalHandle hG) {
+  const long long N2 = (long long)n * n;
+  if (nd->rvalid) {
+    // R(x) is already in R and -R (the initial residual, or the trial point the line search
+    // accepted): the same values this pass would compute, so only dx is cleared
+    for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < N2;
+         p += (long long)gridDim.x * blockDim.x)
+      dx[p] = 0.0f;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      nd->converged = nd->rn < nd->newton_tol;
+      nd->cyc = 0;
+      cudaGraphSetConditional(hG, nd->max_krylov > 0 ? 1u : 0u);
+    }
+    return;
+  }
   const double a = K->pa, b = K->pb, c = K->pc, a0 = K->a0, beta = K->beta;
   double acc = 0.0;
-  const long long N2 = (long long)n * n;
   auto u = [&](int ii, int jj) { return dval(x, ii, jj, n); };
   for (long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x; p < N2;
        p += (long long)gridDim.x * blockDim.x) {
@@ -1294,6 +1310,9 @@ __global__ void nd_update_tail_kernel(double* x, const double* xt, const float* 
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     nd->res = nd->rb;
     nd->it += 1;
+    // an accepted trial point left R(x_new) in R and -R (the host loop's have_r)
+    nd->rvalid = acc ? 1 : 0;
+    if (acc) nd->rn = nd->rb;
     cudaGraphSetConditional(hN, (nd->it < nd->max_newton && !nd->converged) ? 1u : 0u);
   }
 }
@@ -1346,6 +1365,7 @@ static NKLayout nk_layout(int n, int m) {
   L.gs = o; o += al(sizeof(GmresState));
   L.K = o; o += al(sizeof(NKConsts));
   L.pst = o; o += al(sizeof(DevState));
+  static_assert(sizeof(NewtonDev) <= 256, "NewtonDev outgrew its workspace slot");
   L.nd = o; o += al(256);  // NewtonDev
   L.tick = o; o += al(sizeof(unsigned));  // last-CTA ticket of the fused Arnoldi passes
   L.ring = o; o += al(3 * NK_RING * sizeof(int));  // per-step counts of the fixed-step driver
