@@ -31,7 +31,6 @@
 
 #include "mixed.cuh"
 #include "spectral.cuh"
-#include "wfft.cuh"
 
 namespace mjx {
 
@@ -586,7 +585,6 @@ struct NkaArgs {
   float* S;             // real DST coefficients, n x n
   const cx<float>* twn; // twiddles of length n
   const float2* ph;     // (cos, sin)(pi k / 2n), k < n
-  const float2* tw512;  // n = 512: the twiddles of wfft512
   const float* lamx;    // the plan's (2n)-point symbol along x (index = frequency 0..n)
   const float* lamy;    // along y (fftfreq order of 2n)
   const DevState* st;   // Helmholtz step dtc
@@ -745,14 +743,28 @@ __device__ __forceinline__ float2 dct_merge(float cak, float cam, float cbk, flo
   return make_float2(vax - vby, vay + vbx);
 }
 
+// Threads per sequence of the shared-memory transforms of the DST passes: n/16 for the
+// radix-16 Stockham (fft_smem), n/4 for the radix-4 one (fft_smem_r4: a quarter of the
+// dependent work per thread, for passes with few sequences)
+template <bool R4>
+__device__ __forceinline__ int dst_tps(int n) { return R4 ? (n >= 4 ? n >> 2 : 1) : (n >= 16 ? n >> 4 : 1); }
+
+template <bool R4, bool INV, bool COLMAJOR>
+__device__ __forceinline__ void dst_fft(float2* buf, const NkaArgs& a, int nseq, int ss, int es, int tid) {
+  if (R4) fft_smem_r4<float, INV, COLMAJOR>(buf, a.n, a.log2n, nseq, ss, es, a.twn, tid);
+  else fft_smem<float, INV, COLMAJOR>(buf, a.n, a.log2n, nseq, ss, es, a.twn, tid);
+}
+
 // forward DST-II along x of the row pairs (y, y + n/2) of a.src into a.S
+template <bool R4>
 __global__ void __launch_bounds__(256) dst_row_fwd_kernel(const __grid_constant__ NkaArgs a) {
   typedef float2 C;
+  constexpr int PTS = R4 ? 4 : 16;  // elements per thread
   if (a.skip_converged && a.gs->converged) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* buf = reinterpret_cast<C*>(smem_raw);
   const int n = a.n, hn = n >> 1;
-  const int tps = n >= 16 ? n >> 4 : 1;
+  const int tps = dst_tps<R4>(n);
   const int tid = threadIdx.x, s_loc = pdiv(tid, tps), lt = tid - s_loc * tps;
   const bool active = s_loc < a.nseq;  // whole warps are launched
   const int y = blockIdx.x * a.nseq + s_loc;
@@ -760,7 +772,7 @@ __global__ void __launch_bounds__(256) dst_row_fwd_kernel(const __grid_constant_
   const float* ra = a.src + (long long)y * n;
   const float* rb = a.src + (long long)(y + hn) * n;
 #pragma unroll
-  for (int m = 0; m < 16; ++m) {
+  for (int m = 0; m < PTS; ++m) {
     const int x = lt + m * tps;
     if (active && x < n) {
       const float sg = (x & 1) ? -1.f : 1.f;
@@ -768,12 +780,12 @@ __global__ void __launch_bounds__(256) dst_row_fwd_kernel(const __grid_constant_
     }
   }
   __syncthreads();
-  fft_smem<float, false, false>(buf, n, a.log2n, a.nseq, n, 1, a.twn, tid);
+  dst_fft<R4, false, false>(buf, a, a.nseq, n, 1, tid);
   if (!active) return;
   float* Sa = a.S + (long long)y * n;
   float* Sb = a.S + (long long)(y + hn) * n;
 #pragma unroll
-  for (int m = 0; m < 16; ++m) {
+  for (int m = 0; m < PTS; ++m) {
     const int k = lt + m * tps;
     if (k < n) {
       float ca, cb;
@@ -786,6 +798,7 @@ __global__ void __launch_bounds__(256) dst_row_fwd_kernel(const __grid_constant_
 
 // columns kx0 .. kx0 + C - 1 of a.S: DST-II along y, the Helmholtz inverse (with the 1/n^2
 // of the two unnormalised inverse transforms), DST-III along y, in place
+template <bool R4>
 __global__ void __launch_bounds__(256) dst_col_kernel(const __grid_constant__ NkaArgs a) {
   typedef float2 C;
   if (a.skip_converged && a.gs->converged) return;
@@ -802,7 +815,7 @@ __global__ void __launch_bounds__(256) dst_col_kernel(const __grid_constant__ Nk
     *slot = (y & 1) ? -v : v;
   }
   __syncthreads();
-  fft_smem<float, false, true>(buf, n, a.log2n, ns, 1, ns, a.twn, tid);
+  dst_fft<R4, false, true>(buf, a, ns, 1, ns, tid);
   // per (sequence, k <= n/2): the coefficients of k and n - k, the multiplier, the inverse
   // inputs of k and n - k (each item owns its two slots)
   const float hD = (float)a.st->dtc, inv_n2 = 1.0f / ((float)n * (float)n);
@@ -830,7 +843,7 @@ __global__ void __launch_bounds__(256) dst_col_kernel(const __grid_constant__ Nk
     if (k > 0 && km != k) buf[sp(q + km * ns)] = dct_merge(cam, cak, cbm, cbk, a.ph[n - k]);
   }
   __syncthreads();
-  fft_smem<float, true, true>(buf, n, a.log2n, ns, 1, ns, a.twn, tid);
+  dst_fft<R4, true, true>(buf, a, ns, 1, ns, tid);
   for (int e = tid; e < n * Cn; e += nth) {
     const int y = e >> lc, c = e & (Cn - 1);
     const float v = reinterpret_cast<const float*>(&buf[sp((c >> 1) + mk_pos(y, n) * ns)])[c & 1];
@@ -839,14 +852,15 @@ __global__ void __launch_bounds__(256) dst_col_kernel(const __grid_constant__ Nk
 }
 
 // inverse DST-III along x of the row pairs (y, y + n/2) of a.S; w = (1/a0) result
-template <int MODE>
+template <int MODE, bool R4>
 __global__ void __launch_bounds__(256) dst_row_inv_kernel(const __grid_constant__ NkaArgs a) {
   typedef float2 C;
+  constexpr int PTS = R4 ? 4 : 16, KPTS = PTS / 2 + 1;  // elements, coefficient pairs per thread
   if (a.skip_converged && a.gs->converged) return;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* buf = reinterpret_cast<C*>(smem_raw);
   const int n = a.n, hn = n >> 1;
-  const int tps = n >= 16 ? n >> 4 : 1;
+  const int tps = dst_tps<R4>(n);
   const int tid = threadIdx.x, s_loc = pdiv(tid, tps), lt = tid - s_loc * tps;
   const bool active = s_loc < a.nseq;  // whole warps are launched
   const int y = blockIdx.x * a.nseq + s_loc;
@@ -855,7 +869,7 @@ __global__ void __launch_bounds__(256) dst_row_inv_kernel(const __grid_constant_
   const float* Tb = a.S + (long long)(y + hn) * n;
   // DCT coefficient k of row r is T_r[n - 1 - k]; each k <= n/2 fills slots k and n - k
 #pragma unroll
-  for (int m = 0; m < 9; ++m) {
+  for (int m = 0; m < KPTS; ++m) {
     const int k = lt + m * tps;
     if (active && k <= hn) {
       const float cak = Ta[n - 1 - k], cbk = Tb[n - 1 - k];
@@ -865,11 +879,11 @@ __global__ void __launch_bounds__(256) dst_row_inv_kernel(const __grid_constant_
     }
   }
   __syncthreads();
-  fft_smem<float, true, false>(buf, n, a.log2n, a.nseq, n, 1, a.twn, tid);
+  dst_fft<R4, true, false>(buf, a, a.nseq, n, 1, tid);
   const float sc = (float)a.K->inv_a0;
-  float wa[16], wb[16];
+  float wa[PTS], wb[PTS];
 #pragma unroll
-  for (int m = 0; m < 16; ++m) {
+  for (int m = 0; m < PTS; ++m) {
     const int x = lt + m * tps;
     wa[m] = wb[m] = 0.f;
     if (active && x < n) {
@@ -880,186 +894,17 @@ __global__ void __launch_bounds__(256) dst_row_inv_kernel(const __grid_constant_
     }
   }
   // idle threads (x0 = n) contribute nothing
-  nka_finish<MODE, 16>(a, active ? y : 0, active ? lt : n, tps, wa, wb);
-}
-
-// ---- one-warp 512-point transform for the n = 512 DST passes
-// Lane l holds elements l + 32 j (j < 16).  512 = 32 x 16: a 16-point DFT per lane over j,
-// the twiddles w512^(l k1) (tw[32 k1 + l]), a transpose through a 16 x 33 shared tile of the
-// warp; lane L = k1 + 16 h then takes the elements l = h + 2 m (m < 16) of column k1, a
-// 16-point DFT over m, and the radix-2 step with its partner lane L ^ 16 (w32^k).  On
-// return lane L holds X[k1 + 16 k + 256 h] in x[k].  INV: conjugate twiddles (unnormalised).
-template <bool INV>
-__device__ __forceinline__ void wfft512(float2 (&x)[16], float2* tile, const float2* __restrict__ tw, int lane) {
-  dft16<INV>(x);
-#pragma unroll
-  for (int k1 = 1; k1 < 16; ++k1) {
-    const float2 w = __ldg(&tw[32 * k1 + lane]);
-    x[k1] = INV ? cmulc(x[k1], w) : cmul(x[k1], w);
-  }
-#pragma unroll
-  for (int k1 = 0; k1 < 16; ++k1) tile[k1 * 33 + lane] = x[k1];
-  __syncwarp();
-  const int k1 = lane & 15, h = lane >> 4;
-#pragma unroll
-  for (int m = 0; m < 16; ++m) x[m] = tile[k1 * 33 + h + 2 * m];
-  __syncwarp();
-  dft16<INV>(x);
-#pragma unroll
-  for (int k = 0; k < 16; ++k) {
-    const float2 o = shfl2(x[k], lane ^ 16);
-    const float2 E = h == 0 ? x[k] : o, O = h == 0 ? o : x[k];
-    const float c = kW32C[k], s = INV ? kW32S[k] : -kW32S[k];
-    const float2 wO = make_float2(O.x * c - O.y * s, O.x * s + O.y * c);
-    x[k] = h == 0 ? make_float2(E.x + wO.x, E.y + wO.y) : make_float2(E.x - wO.x, E.y - wO.y);
-  }
-}
-
-// the transform's output in natural order into a warp's 512-entry shared buffer
-__device__ __forceinline__ void w512_store(const float2 (&x)[16], float2* nat, int lane) {
-  const int base = (lane & 15) + 256 * (lane >> 4);
-#pragma unroll
-  for (int k = 0; k < 16; ++k) nat[base + 16 * k] = x[k];
-  __syncwarp();
-}
-
-// DST-II along x, n = 512, one warp per row pair (y, y + 256)
-__global__ void __launch_bounds__(128) dst_row_fwd_w512_kernel(const __grid_constant__ NkaArgs a) {
-  if (a.skip_converged && a.gs->converged) return;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int lane = threadIdx.x & 31, s_loc = threadIdx.x >> 5;
-  float2* tile = reinterpret_cast<float2*>(smem_raw) + s_loc * (16 * 33 + 512);
-  float2* nat = tile + 16 * 33;
-  const int y = blockIdx.x * a.nseq + s_loc;
-  const float* ra = a.src + (long long)y * 512;
-  const float* rb = a.src + (long long)(y + 256) * 512;
-  float2 z[16];
-  // Makhoul order: position p < 256 holds element 2p, position p >= 256 element 1023 - 2p,
-  // with the sign (-1)^element (+ for the even, - for the odd elements)
-#pragma unroll
-  for (int j = 0; j < 16; ++j) {
-    const int p = lane + 32 * j;
-    const int src = p < 256 ? 2 * p : 1023 - 2 * p;
-    const float sg = p < 256 ? 1.f : -1.f;
-    z[j] = make_float2(sg * ra[src], sg * rb[src]);
-  }
-  wfft512<false>(z, tile, a.tw512, lane);
-  w512_store(z, nat, lane);
-  float* Sa = a.S + (long long)y * 512;
-  float* Sb = a.S + (long long)(y + 256) * 512;
-#pragma unroll
-  for (int j = 0; j < 16; ++j) {
-    const int k = lane + 32 * j;
-    float ca, cb;
-    dct_split(nat[k], nat[(512 - k) & 511], a.ph[k], ca, cb);
-    Sa[511 - k] = ca;
-    Sb[511 - k] = cb;
-  }
-}
-
-// columns kx0, kx0 + 1 of a.S (n = 512, one warp per column pair): DST-II along y, the
-// multiplier, DST-III along y, in place
-__global__ void __launch_bounds__(128) dst_col_w512_kernel(const __grid_constant__ NkaArgs a) {
-  if (a.skip_converged && a.gs->converged) return;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int lane = threadIdx.x & 31, s_loc = threadIdx.x >> 5;
-  float2* tile = reinterpret_cast<float2*>(smem_raw) + s_loc * (16 * 33 + 512);
-  float2* nat = tile + 16 * 33;
-  const int kx0 = 2 * (blockIdx.x * (blockDim.x >> 5) + s_loc);
-  float2 z[16];
-#pragma unroll
-  for (int j = 0; j < 16; ++j) {
-    const int p = lane + 32 * j;
-    const int src = p < 256 ? 2 * p : 1023 - 2 * p;
-    const float sg = p < 256 ? 1.f : -1.f;
-    const float2 v = *reinterpret_cast<const float2*>(a.S + (long long)src * 512 + kx0);
-    z[j] = make_float2(sg * v.x, sg * v.y);
-  }
-  wfft512<false>(z, tile, a.tw512, lane);
-  w512_store(z, nat, lane);
-  const float hD = (float)a.st->dtc, inv_n2 = 1.0f / (512.0f * 512.0f);
-  const float lxa = a.lamx[kx0 + 1], lxb = a.lamx[kx0 + 2];
-  auto mult = [&](float lam) {
-    float den = 1.0f - hD * lam;
-    if (fabsf(den) < 1e-14f) den = 1e-14f;
-    return inv_n2 / den;
-  };
-  // inverse input of index k from the scaled coefficients of k and 512 - k
-#pragma unroll
-  for (int j = 0; j < 16; ++j) {
-    const int k = lane + 32 * j, km = (512 - k) & 511;
-    const float2 Zk = nat[k], Zm = nat[km];
-    float cak, cbk, cam = 0.f, cbm = 0.f;
-    dct_split(Zk, Zm, a.ph[k], cak, cbk);
-    cak *= mult(lxa + a.lamy[512 - k]);
-    cbk *= mult(lxb + a.lamy[512 - k]);
-    if (k > 0) {
-      dct_split(Zm, Zk, a.ph[512 - k], cam, cbm);
-      cam *= mult(lxa + a.lamy[k]);
-      cbm *= mult(lxb + a.lamy[k]);
-    }
-    z[j] = dct_merge(cak, cam, cbk, cbm, a.ph[k]);
-  }
-  __syncwarp();
-  wfft512<true>(z, tile, a.tw512, lane);
-  w512_store(z, nat, lane);
-#pragma unroll
-  for (int j = 0; j < 16; ++j) {
-    const int y = lane + 32 * j;
-    const float2 v = nat[mk_pos(y, 512)];
-    const float sg = (y & 1) ? -1.f : 1.f;
-    *reinterpret_cast<float2*>(a.S + (long long)y * 512 + kx0) = make_float2(sg * v.x, sg * v.y);
-  }
-}
-
-// DST-III along x, n = 512, one warp per row pair; w = (1/a0) result
-template <int MODE>
-__global__ void __launch_bounds__(128) dst_row_inv_w512_kernel(const __grid_constant__ NkaArgs a) {
-  if (a.skip_converged && a.gs->converged) return;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int lane = threadIdx.x & 31, s_loc = threadIdx.x >> 5;
-  float2* tile = reinterpret_cast<float2*>(smem_raw) + s_loc * (16 * 33 + 512);
-  float2* nat = tile + 16 * 33;
-  const int y = blockIdx.x * a.nseq + s_loc;
-  const float* Ta = a.S + (long long)y * 512;
-  const float* Tb = a.S + (long long)(y + 256) * 512;
-  float2 z[16];
-#pragma unroll
-  for (int j = 0; j < 16; ++j) {
-    const int k = lane + 32 * j;
-    const float cak = Ta[511 - k], cbk = Tb[511 - k];
-    const float cam = k > 0 ? Ta[k - 1] : 0.f, cbm = k > 0 ? Tb[k - 1] : 0.f;
-    z[j] = dct_merge(cak, cam, cbk, cbm, a.ph[k]);
-  }
-  wfft512<true>(z, tile, a.tw512, lane);
-  w512_store(z, nat, lane);
-  const float sc = (float)a.K->inv_a0;
-  float wa[16], wb[16];
-#pragma unroll
-  for (int j = 0; j < 16; ++j) {
-    const int x = lane + 32 * j;
-    const float2 v = nat[mk_pos(x, 512)];
-    const float s = (x & 1) ? -sc : sc;
-    wa[j] = s * v.x;
-    wb[j] = s * v.y;
-  }
-  nka_finish<MODE, 16>(a, y, lane, 32, wa, wb);
+  nka_finish<MODE, PTS>(a, active ? y : 0, active ? lt : n, tps, wa, wb);
 }
 
 // twiddles exp(-2 pi i j/n) of the n-point transforms and the phases (cos, sin)(pi k/2n)
-// (and, for n = 512, w512^(l k1) at 32 k1 + l, l < 32, k1 < 16, for wfft512)
-__global__ void dst_tables_kernel(cx<float>* twn, float2* ph, float2* tw512, int n) {
+__global__ void dst_tables_kernel(cx<float>* twn, float2* ph, int n) {
   for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
     double s, c;
     sincospi(2.0 * (double)j / (double)n, &s, &c);
     twn[j] = mk<cx<float>>((float)c, (float)(-s));
     sincospi((double)j / (2.0 * (double)n), &s, &c);
     ph[j] = make_float2((float)c, (float)s);
-    if (n == 512) {
-      const int k1 = j >> 5, l = j & 31;
-      sincospi(2.0 * (double)(l * k1) / 512.0, &s, &c);
-      tw512[j] = make_float2((float)c, (float)(-s));
-    }
   }
 }
 
@@ -1359,7 +1204,7 @@ static NKLayout nk_layout(int n, int m) {
   L.t = o; o += al(N2 * 4);
   L.V = o; o += al((size_t)(m + 1) * N2 * 4);
   L.S = o; o += al(N2 * 4);                              // real DST coefficients
-  L.dtab = o; o += al((size_t)(2 * n + 512) * sizeof(float2));  // n-point twiddles, phases, wfft512 twiddles
+  L.dtab = o; o += al((size_t)(2 * n) * sizeof(float2));  // n-point twiddles, phases
   // per-CTA partials: elementwise passes (nblk CTAs) and the fused row passes (up to n/2 CTAs)
   L.part = o; o += al((size_t)(m + 2) * (size_t)(L.nblk > n / 2 ? L.nblk : n / 2) * 8);
   L.gs = o; o += al(sizeof(GmresState));
@@ -1403,53 +1248,59 @@ static NkaArgs nka_args(NKRun& r) {
   a.S = P32(r, r.L.S);
   a.twn = (const cx<float>*)(r.ws + r.L.dtab);
   a.ph = (const float2*)(r.ws + r.L.dtab) + n;
-  a.tw512 = (const float2*)(r.ws + r.L.dtab) + 2 * n;
   a.lamx = (const float*)pv.lamx; a.lamy = (const float*)pv.lamy;
   a.st = (const DevState*)(r.ws + r.L.pst);
   return a;
 }
 
-// CTA geometry of the DST passes: rows in pairs (y, y + n/2), n/16 threads per pair, fewer
-// pairs per CTA until the pass covers every SM, whole warps (the threads past nseq * tps
-// idle); columns in tiles of C (even) real columns, C/2 complex sequences, at least 152
-// tiles where n allows and within the default 48 KB of shared memory
+// CTA geometry of the DST passes: rows in pairs (y, y + n/2), tps threads per pair (n/16 for
+// radix 16, n/4 for radix 4), fewer pairs per CTA until the pass covers every SM, at most 256
+// threads, whole warps (the threads past nseq * tps idle); columns in tiles of C (even) real
+// columns, C/2 complex sequences, at least 152 tiles where n allows and within the default
+// 48 KB of shared memory
 struct DstGeom { int nseq, ctas, threads, C, col_threads; size_t smem, col_smem; };
-static DstGeom dst_geom(int n) {
+static DstGeom dst_geom(int n, bool r4) {
   DstGeom g;
-  const int hn = n / 2, tps = n >= 16 ? n / 16 : 1;
+  const int hn = n / 2, tps = r4 ? (n >= 4 ? n / 4 : 1) : (n >= 16 ? n / 16 : 1);
   int ns = row_nseq(n, hn);
   if (ns > hn) ns = hn;
-  while (ns > 1 && hn / ns < 152) ns >>= 1;
+  while (ns > 1 && (hn / ns < 152 || ns * tps > 256)) ns >>= 1;
   g.nseq = ns;
   g.ctas = hn / ns;
   g.threads = ((ns * tps + 31) / 32) * 32;
   g.smem = (size_t)sp_size(ns * n) * sizeof(float2);
   int C = 8 < n ? 8 : n;
-  while (C > 2 && (n / C < 152 || (size_t)sp_size(n * (C / 2)) * sizeof(float2) > 48 * 1024)) C >>= 1;
+  while (C > 2 && (n / C < 152 || (size_t)sp_size(n * (C / 2)) * sizeof(float2) > 48 * 1024 ||
+                   (C / 2) * tps > 256))
+    C >>= 1;
   g.C = C;
   g.col_threads = (((C / 2) * tps + 31) / 32) * 32;
   g.col_smem = (size_t)sp_size(n * (C / 2)) * sizeof(float2);
   return g;
 }
 
+// Radix 4 for the DST passes up to n = 512: at most n/2 row pairs and n/2 column pairs per
+// pass, too few sequences for the radix-16 schedule's n/16 threads each to fill the SMs, so the
+// pass lasts one sequence's dependent work, a quarter as long with n/4 threads per sequence
+static bool dst_r4(int n) { return n <= 512; }
+
 // w = M^-1 a.src: DST-II along x, along y with the multiplier and DST-III along y, DST-III
 // along x (MODE: w into t, or the cycle start V_0 = w)
 template <int MODE>
 static cudaError_t nka_precond(NKRun& r, NkaArgs a) {
-  const DstGeom g = dst_geom(r.n);
+  const bool r4 = dst_r4(r.n);
+  const DstGeom g = dst_geom(r.n, r4);
   a.nseq = g.nseq;
   a.C = g.C;
-  if (r.n == 512) {  // one warp per row or column pair (wfft512)
-    a.nseq = 1;
-    const size_t sm = (16 * 33 + 512) * sizeof(float2);
-    dst_row_fwd_w512_kernel<<<256, 32, sm, r.s>>>(a);
-    dst_col_w512_kernel<<<256, 32, sm, r.s>>>(a);
-    dst_row_inv_w512_kernel<MODE><<<256, 32, sm, r.s>>>(a);
-    return cudaGetLastError();
+  if (r4) {
+    dst_row_fwd_kernel<true><<<g.ctas, g.threads, g.smem, r.s>>>(a);
+    dst_col_kernel<true><<<r.n / g.C, g.col_threads, g.col_smem, r.s>>>(a);
+    dst_row_inv_kernel<MODE, true><<<g.ctas, g.threads, g.smem, r.s>>>(a);
+  } else {
+    dst_row_fwd_kernel<false><<<g.ctas, g.threads, g.smem, r.s>>>(a);
+    dst_col_kernel<false><<<r.n / g.C, g.col_threads, g.col_smem, r.s>>>(a);
+    dst_row_inv_kernel<MODE, false><<<g.ctas, g.threads, g.smem, r.s>>>(a);
   }
-  dst_row_fwd_kernel<<<g.ctas, g.threads, g.smem, r.s>>>(a);
-  dst_col_kernel<<<r.n / g.C, g.col_threads, g.col_smem, r.s>>>(a);
-  dst_row_inv_kernel<MODE><<<g.ctas, g.threads, g.smem, r.s>>>(a);
   return cudaGetLastError();
 }
 
@@ -1924,8 +1775,7 @@ static mjx_status nk_setup(NKRun& r, const void* plan2, int n, double dy, double
   MJX_CUDA_TRY(cudaMemsetAsync(r.ws + r.L.pst, 0, sizeof(DevState), r.s));
   MJX_CUDA_TRY(cudaMemsetAsync(r.ws + r.L.tick, 0, sizeof(unsigned), r.s));
   dst_tables_kernel<<<(n + 255) / 256, 256, 0, r.s>>>((cx<float>*)(r.ws + r.L.dtab),
-                                                      (float2*)(r.ws + r.L.dtab) + n,
-                                                      (float2*)(r.ws + r.L.dtab) + 2 * n, n);
+                                                      (float2*)(r.ws + r.L.dtab) + n, n);
   MJX_CUDA_TRY(cudaGetLastError());
   P->max_newton = nkp->max_newton_iters; P->max_krylov = nkp->max_krylov_iters; P->restart = nkp->restart;
   P->max_backtrack = nkp->max_backtrack; P->newton_tol = nkp->newton_tol; P->krylov_tol = nkp->krylov_tol;
