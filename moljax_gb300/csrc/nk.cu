@@ -19,8 +19,8 @@
 // FD symbol of the (2N)^2 periodic plan, which the odd extension shares).
 //
 // The Arnoldi steps of a GMRES cycle run as one CUDA graph with a conditional
-// while node, four kernels per step (the fused passes below: operand + forward
-// row transforms, column pass, inverse row transforms + Gram-Schmidt dots,
+// while node, six kernels per step (the JVP; DST-II along x; DST-II along y, the
+// multiplier and DST-III along y; DST-III along x; the Gram-Schmidt dots; the
 // orthogonalisation + Givens step); the last CTA of the last kernel updates the
 // residual estimate on the device and clears the loop flag.  In the default
 // mode the whole Newton iteration is one graph of nested conditional loops.
