@@ -52,13 +52,16 @@ struct GcnRowArgs {
   GcnState* gs;
 };
 
-template <typename T>
+// R4: radix-4 transforms, n/4 threads per row (short FP64 rows on a small grid, where the
+// radix-16 pass leaves most SMs idle and each row's FP64 work is the pass's length)
+template <typename T, bool R4 = false>
 __global__ void __launch_bounds__(256) gcn_row_kernel(const __grid_constant__ GcnRowArgs<T> a) {
   typedef cx<T> C;
+  constexpr int PTS = R4 ? 4 : 16, KPTS = PTS / 2 + 1;  // elements, half-spectrum bins per thread
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* buf = reinterpret_cast<C*>(smem_raw);
   const int n = a.n, half = n >> 1;
-  const int tps = n >= 16 ? n / 16 : 1;
+  const int tps = R4 ? (n >= 4 ? n / 4 : 1) : (n >= 16 ? n / 16 : 1);
   const int tid = threadIdx.x;
   const int s_loc = tid / tps, lt = tid % tps;
   const bool active = s_loc < a.nseq;
@@ -69,14 +72,14 @@ __global__ void __launch_bounds__(256) gcn_row_kernel(const __grid_constant__ Gc
   if (active) {
     const C* A = a.spec + y * a.ldc;
     const C* B = a.spec + a.fs + y * a.ldc;
-    C Ak[9], Bk[9];
+    C Ak[KPTS], Bk[KPTS];
 #pragma unroll
-    for (int m = 0; m < 9; ++m) {
+    for (int m = 0; m < KPTS; ++m) {
       const int kk = lt + m * tps;
       if (kk <= half) { Ak[m] = A[kk]; Bk[m] = B[kk]; }
     }
 #pragma unroll
-    for (int m = 0; m < 9; ++m) {
+    for (int m = 0; m < KPTS; ++m) {
       const int kk = lt + m * tps;
       if (kk <= half) {
         Z(kk) = mk<C>(Ak[m].x - Bk[m].y, Ak[m].y + Bk[m].x);
@@ -85,13 +88,14 @@ __global__ void __launch_bounds__(256) gcn_row_kernel(const __grid_constant__ Gc
     }
   }
   __syncthreads();
-  fft_smem<T, true, false>(buf, n, a.log2n, a.nseq, n, 1, a.tw, tid);
+  if (R4) fft_smem_r4<T, true, false>(buf, n, a.log2n, a.nseq, n, 1, a.tw, tid);
+  else fft_smem<T, true, false>(buf, n, a.log2n, a.nseq, n, 1, a.tw, tid);
   const T h = (T)a.h, F = (T)a.F, FK = (T)(a.F + a.k);
   T mu = (T)0, mv = (T)0;
   if (active) {
     const long long ro = y * n;
 #pragma unroll
-    for (int m = 0; m < 16; ++m) {
+    for (int m = 0; m < PTS; ++m) {
       const int x = lt + m * tps;
       if (x >= n) continue;
       const C z = Z(x);
@@ -129,12 +133,13 @@ __global__ void __launch_bounds__(256) gcn_row_kernel(const __grid_constant__ Gc
     }
   }
   __syncthreads();
-  fft_smem<T, false, false>(buf, n, a.log2n, a.nseq, n, 1, a.tw, tid);
+  if (R4) fft_smem_r4<T, false, false>(buf, n, a.log2n, a.nseq, n, 1, a.tw, tid);
+  else fft_smem<T, false, false>(buf, n, a.log2n, a.nseq, n, 1, a.tw, tid);
   if (active) {
     C* A = a.spec + y * a.ldc;
     C* B = a.spec + a.fs + y * a.ldc;
 #pragma unroll
-    for (int m = 0; m < 9; ++m) {
+    for (int m = 0; m < KPTS; ++m) {
       const int kk = lt + m * tps;
       if (kk > half) continue;
       const C Zk = Z(kk), Zm = Z((n - kk) & (n - 1));
@@ -213,7 +218,7 @@ static inline size_t al256g(size_t b) { return (b + 255) & ~size_t(255); }
 static GcnLayout gcn_layout(int ny, int nx, int elem) {
   GcnLayout L;
   const size_t fr = (size_t)ny * nx * elem, fsb = (size_t)ny * spec_ldc(nx) * 2 * elem;
-  L.nparts = row_ctas(nx, ny, 1);
+  L.nparts = ny;  // at most one row per CTA
   size_t o = 0;
   L.spec = o; o += al256g(2 * fsb);
   L.C = o; o += al256g(2 * fr);
@@ -274,6 +279,16 @@ static mjx_status gcn_run(const void* plan, const mjx_grid2d* g, const double* D
   ra.fs = fs; ra.fr = fr; ra.tw = (const cx<T>*)pv.twx; ra.spec = spec; ra.Y = y_out;
   ra.Cb = (T*)(ws + L.C); ra.W = (T*)(ws + L.W); ra.h = 0.5 * dt; ra.F = F; ra.k = k;
   ra.part = (double*)(ws + L.part); ra.gs = gs;
+  // FP64 rows of at most 256 points on a small grid (the rule of the spectral row passes):
+  // radix 4, at most 256 threads per CTA, fewer rows per CTA until every SM has one
+  const bool r4 = sizeof(T) == 8 && nx >= 4 && nx <= 256 && (long long)ny * (nx / 16) < 152LL * 128;
+  int rthreads = 256;
+  if (r4) {
+    const int tps4 = nx / 4;
+    while (ra.nseq > 1 && ra.nseq * tps4 > 256) ra.nseq >>= 1;
+    while (ra.nseq > 1 && ny / ra.nseq < 152) ra.nseq >>= 1;
+    rthreads = ((ra.nseq * tps4 + 31) / 32) * 32;
+  }
   const unsigned rblocks = (unsigned)(ny / ra.nseq);
   const size_t rsmem = (size_t)sp_size(ra.nseq * nx) * sizeof(cx<T>);
   static ContextOnce attr;
@@ -288,6 +303,9 @@ static mjx_status gcn_run(const void* plan, const mjx_grid2d* g, const double* D
                                       optin - (int)fa.sharedSizeBytes));
     MJX_CUDA_TRY(cudaFuncGetAttributes(&fa, gcn_row_kernel<double>));
     MJX_CUDA_TRY(cudaFuncSetAttribute(gcn_row_kernel<double>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      optin - (int)fa.sharedSizeBytes));
+    MJX_CUDA_TRY(cudaFuncGetAttributes(&fa, gcn_row_kernel<double, true>));
+    MJX_CUDA_TRY(cudaFuncSetAttribute(gcn_row_kernel<double, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       optin - (int)fa.sharedSizeBytes));
     return MJX_OK;
   }));
@@ -310,7 +328,8 @@ static mjx_status gcn_run(const void* plan, const mjx_grid2d* g, const double* D
     if ((ce = cudaGraphAddNode(&node, graph, nullptr, nullptr, 0, &np)) != cudaSuccess) break;
     cudaGraph_t body = np.conditional.phGraph_out[0];
     if ((ce = cudaStreamBeginCaptureToGraph(cs, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal)) != cudaSuccess) break;
-    gcn_row_kernel<T><<<rblocks, 256, rsmem, cs>>>(ra);
+    if (r4) gcn_row_kernel<T, true><<<rblocks, rthreads, rsmem, cs>>>(ra);
+    else gcn_row_kernel<T><<<rblocks, 256, rsmem, cs>>>(ra);
     cudaError_t le = cudaGetLastError();
     if (le == cudaSuccess) le = launch_col<T>(cc, cs);
     if (le == cudaSuccess) {
